@@ -1,0 +1,209 @@
+/*
+ * gbrelion.h -- C ABI of libgbrelion, a GB300-native (sm_103a) expectation
+ * step for RELION's relion_refine.
+ *
+ * The reference plugs its accelerated E-step into MlOptimiser through
+ * opaque handles (src/ml_optimiser.h:108-109, gpuOptimisers/accDataBundles)
+ * and one dispatch function (src/ml_optimiser.cpp:78-97).  Each entry point
+ * below replaces one call of that surface; the comment on each names it.
+ * All entry points return 0 on success or a negative gbr_status; the text of
+ * the last error of the calling thread is available from gbr_last_error().
+ * No entry point takes or returns a PyTorch or C++ type.
+ *
+ * Layout conventions (FFTW half-transform, as in the reference):
+ *   a 2D Fourier image of size s is stored row-major as [s][s/2+1]; row i
+ *   holds frequency y = i for i <= s/2 and y = i - s otherwise.
+ *   Complex values are interleaved (re, im).
+ *   A padded 3D reference / backprojector volume is [zdim][ydim][xdim] with
+ *   logical origin (x=0, y=yinit, z=zinit), as Projector::data
+ *   (src/projector.cpp:59-90).
+ */
+#ifndef GBRELION_H
+#define GBRELION_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    GBR_OK = 0,
+    GBR_ERR_INVALID = -1,      /* bad argument / size                       */
+    GBR_ERR_CUDA = -2,         /* CUDA runtime error                        */
+    GBR_ERR_OOM = -3,          /* device memory budget exceeded             */
+    GBR_ERR_NUMERICAL = -4,    /* zero sum of weights / no significant pose */
+    GBR_ERR_STATE = -5,        /* call out of order (e.g. no reference yet) */
+    GBR_ERR_UNSUPPORTED = -6   /* option outside the implemented path       */
+} gbr_status;
+
+/* Precision of the coarse-pass cross-term contraction. */
+typedef enum {
+    GBR_PREC_FP32 = 0,         /* plain path: FP32 SIMT, matches the CPU oracle */
+    GBR_PREC_BF16 = 1          /* precision form: tcgen05 BF16, FP32 accumulate */
+} gbr_precision;
+
+/* Model, sampling and option state of one iteration (the MlOptimiser /
+ * MlModel / HealpixSampling members the E-step reads). */
+typedef struct {
+    int64_t ori_size;            /* mymodel.ori_size                          */
+    int64_t nr_classes;          /* mymodel.nr_classes                        */
+    int64_t current_size;        /* image_current_size (fine pass, wsums)     */
+    int64_t coarse_size;         /* image_coarse_size (coarse pass)           */
+    int64_t padding_factor;      /* projector / backprojector padding (2)     */
+    int64_t healpix_order;       /* --healpix_order                          */
+    int64_t adaptive_oversampling;   /* --oversampling (1)                   */
+    int64_t maximum_significants;    /* --maxsig (<= 0: off)                 */
+    int64_t sigma2_len;          /* XSIZE(mymodel.sigma2_noise[group])       */
+    int64_t do_scale_correction; /* --scale                                  */
+    int64_t do_norm_correction;  /* --norm                                   */
+    int64_t do_map;              /* !--no_map                                */
+    int64_t precision;           /* gbr_precision                            */
+    int64_t reserved_;
+    double pixel_size;           /* Angstrom per pixel                       */
+    double psi_step;             /* degrees; <= 0: 360/(6*2^order)           */
+    double offset_range;         /* Angstrom                                 */
+    double offset_step;          /* Angstrom                                 */
+    double adaptive_fraction;    /* --adaptive_fraction (0.999)              */
+    double sigma2_fudge;         /* --sigma2_fudge (1)                       */
+    double sigma2_offset;        /* mymodel.sigma2_offset, Angstrom^2        */
+    double avg_norm_correction;  /* mymodel.avg_norm_correction              */
+} gbr_model_desc;
+
+/* One batch of particles (one image each, one optics group).  Pointers are
+ * host memory unless `device_resident` is set, in which case they are device
+ * pointers on the bundle's GPU.  Sizes: cur = current_size, X = cur/2+1. */
+typedef struct {
+    int64_t n;                   /* number of particles                      */
+    int64_t device_resident;     /* 0: host pointers (copied in), 1: device   */
+    const float *fimg;           /* [n][cur][X][2] masked image FT            */
+    const float *fimg_nomask;    /* [n][cur][X][2] unmasked image FT          */
+    const float *fctf;           /* [n][cur][X]    CTF image                   */
+    const double *power_img;     /* [n][ori/2+1]   power spectrum             */
+    const double *old_offset;    /* [n][2] pixels                             */
+    const double *prior;         /* [n][2] pixels                             */
+    const double *highres_Xi2;   /* [n]                                       */
+    const double *norm_correction; /* [n] metadata NORM                       */
+    const double *scale;         /* [n] scale_correction of the group         */
+} gbr_particle_batch;
+
+/* Per-particle metadata written back by the E-step (the exp_metadata columns
+ * set in storeWeightedSums, src/ml_optimiser.cpp:8810-8870, :9040-9060). */
+typedef struct {
+    double rot, tilt, psi;       /* degrees, best (PMAX) pose                */
+    double xoff, yoff;           /* pixels                                   */
+    double cls;                  /* 1-based class                            */
+    double pmax;                 /* max normalised weight                    */
+    double dLL;                  /* log-likelihood contribution              */
+    double norm;                 /* norm correction                          */
+    double nr_sign;              /* significant coarse samples               */
+    double coarse_min_diff2, coarse_sum_weight, coarse_significant_weight;
+    double fine_min_diff2, fine_sum_weight, fine_significant_weight;
+    int64_t best_ihidden_over;   /* fine-pass hidden index of the PMAX pose  */
+    int64_t n_fine;              /* fine poses evaluated                     */
+} gbr_particle_result;
+
+/* Scalar and per-shell weighted sums (MlWsumModel), accumulated over all
+ * batches since the last gbr_bundle_reset_wsum(). */
+typedef struct {
+    double *sigma2_noise;        /* [ori/2+1]                                */
+    double *pdf_class;           /* [K]                                      */
+    double *pdf_direction;       /* [K][ndir]                                */
+    double sigma2_offset, sumw_group, LL, ave_Pmax, avg_norm_correction;
+    double wsum_signal_product, wsum_reference_power;
+    double reserved_;
+} gbr_wsum;
+
+typedef struct gbr_bundle gbr_bundle;
+typedef struct gbr_worker gbr_worker;
+
+/* Text of the last error on this thread ("" if none).  Returns its length. */
+size_t gbr_last_error(char *buf, size_t len);
+
+/* Library / kernel build identification (e.g. "sm_103a"). */
+const char *gbr_version(void);
+
+/* new MlDeviceBundle(MlOptimiser*) + setDevice(id) + setupFixedSizedObjects()
+ * (src/ml_optimiser.cpp:3579-3582, src/acc/cuda/cuda_ml_optimiser.cu:85-152).
+ * Also initialises the zeroed backprojector volumes
+ * (AccBackprojector::setMdlDim/initMdl) from current_size. */
+int gbr_bundle_create(const gbr_model_desc *desc, int device, gbr_bundle **out);
+
+/* AccProjector::setMdlDim(xdim,ydim,zdim,yinit,zinit,r_max,pad) + initMdl
+ * (src/acc/acc_projector_impl.h:5-105): upload the padded Fourier reference
+ * of one class, [zdim][ydim][xdim] complex, single precision. */
+int gbr_projector_upload(gbr_bundle *b, int64_t iclass, const float *data, int64_t xdim,
+                         int64_t ydim, int64_t zdim, int64_t yinit, int64_t zinit,
+                         int64_t r_max, int64_t padding_factor);
+
+/* Model arrays read by the E-step: mymodel.sigma2_noise[group] (sigma2_len),
+ * pdf_class [K], pdf_direction [K][ndir], data_vs_prior_class [K][ori/2+1]
+ * (may be NULL unless do_scale_correction). */
+int gbr_model_set_arrays(gbr_bundle *b, const double *sigma2_noise, const double *pdf_class,
+                         const double *pdf_direction, const double *data_vs_prior);
+
+/* setupTunableSizedObjects(allocationSize) (cuda_ml_optimiser.cu:154-226):
+ * cap the device memory the bundle and its workers may use. */
+int gbr_bundle_reserve(gbr_bundle *b, size_t bytes);
+
+/* new MlOptimiserCuda(MlOptimiser*, bundle, name) (src/ml_optimiser.cpp:3587). */
+int gbr_worker_create(gbr_bundle *b, gbr_worker **out);
+
+/* Keep device copies of the last batch's intermediate arrays for
+ * gbr_worker_debug_fetch (the RELION_TESTING dumps of
+ * src/ml_optimiser.cpp:4600-4700 serve the same purpose). */
+int gbr_worker_set_debug(gbr_worker *w, int on);
+
+/* MlOptimiserCuda::doThreadExpectationSomeParticles(thread_id)
+ * (cuda_ml_optimiser.cu:250-299 -> accDoExpectationOneParticle,
+ * src/acc/acc_ml_optimiser_impl.h:3673), for a batch of particles:
+ * coarse search, significance, fine search, weights, weighted sums and
+ * backprojection into the bundle's volumes.  `res` has batch->n entries. */
+int gbr_expect_batch(gbr_worker *w, const gbr_particle_batch *batch, gbr_particle_result *res);
+
+/* Number of coarse directions / psi angles / translations of the sampling,
+ * and the fine oversampling factors (HealpixSampling::NrDirections etc.). */
+int gbr_sampling_sizes(const gbr_bundle *b, int64_t *ndir, int64_t *npsi, int64_t *ntrans,
+                       int64_t *nover_rot, int64_t *nover_trans);
+
+/* Debug read-back of the last batch, for parity tests: `what` selects
+ *   0: coarse diff2 of particle i (absolute, double [R*T]; +inf = skipped)
+ *   1: coarse weights of particle i (double [R*T])
+ *   2: fine entries of particle i: int64 hidden indices [m] (what=2) and
+ *   3: fine diff2 [m] (double), 4: fine weights [m] (double).
+ * Returns the number of elements written, or a negative status. */
+int64_t gbr_worker_debug_fetch(gbr_worker *w, int what, int64_t i, void *host, int64_t capacity);
+
+/* AccBackprojector::getMdlData (src/acc/acc_backprojector_impl.h:109-138):
+ * download the accumulated data (complex, interleaved) and weight volumes of
+ * one class in double precision; dims via gbr_backprojector_dims. */
+int gbr_backprojector_dims(const gbr_bundle *b, int64_t *xdim, int64_t *ydim, int64_t *zdim,
+                           int64_t *yinit, int64_t *zinit, int64_t *r_max);
+int gbr_backprojector_download(gbr_bundle *b, int64_t iclass, double *data, double *weight);
+
+/* Weighted sums accumulated since the last reset (added into `out`). */
+int gbr_wsum_download(gbr_bundle *b, gbr_wsum *out);
+/* Zero the volumes and weighted sums (start of a new iteration). */
+int gbr_bundle_reset_wsum(gbr_bundle *b);
+
+/* Device-side timing of the last batch: kernel time of each stage (ms),
+ * measured with CUDA events on the worker's stream. */
+int gbr_worker_stage_times(const gbr_worker *w, double *ms, int64_t n, int64_t *n_written);
+
+/* Number of CUDA kernels this worker has launched (all batches so far). */
+int gbr_worker_launch_count(const gbr_worker *w, int64_t *count);
+
+/* Measured FP32 FMA throughput of the device (TFLOP/s, register-resident
+ * FMA chains on every SM): the roofline peak of the FP32 SIMT kernels.
+ * No counterpart in the reference (a measurement utility). */
+int gbr_measure_fp32_peak(int device, double *tflops);
+
+/* delete MlOptimiserCuda / MlDeviceBundle (src/ml_optimiser.cpp:3840-3868). */
+int gbr_worker_destroy(gbr_worker *w);
+int gbr_bundle_destroy(gbr_bundle *b);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBRELION_H */

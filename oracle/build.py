@@ -1,0 +1,31 @@
+"""Build the oracle (TEST INFRASTRUCTURE ONLY).
+
+Compiles oracle/relion_oracle.cpp into oracle/_build/liboracle.so and, when
+the reference tree is present, the reference's own HEALPix sources into
+oracle/_ref/libref_healpix.so (oracle/build_ref.sh).
+"""
+import os
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "liboracle.so")
+REF_LIB = os.path.join(HERE, "_ref", "libref_healpix.so")
+
+
+def build(force=False):
+    os.makedirs(os.path.join(HERE, "_build"), exist_ok=True)
+    src = os.path.join(HERE, "relion_oracle.cpp")
+    hdr = os.path.join(HERE, "relion_oracle.h")
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(
+            os.path.getmtime(src), os.path.getmtime(hdr)):
+        subprocess.run(["g++", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-std=c++17",
+                        src, "-o", LIB + ".tmp"], check=True)
+        os.replace(LIB + ".tmp", LIB)
+    ref = os.environ.get("RELION_REFERENCE", "/root/reference")
+    if os.path.isdir(os.path.join(ref, "src", "Healpix_2.15a")) and (force or not os.path.exists(REF_LIB)):
+        subprocess.run(["sh", os.path.join(HERE, "build_ref.sh")], check=True)
+    return LIB
+
+
+if __name__ == "__main__":
+    build(force=True)

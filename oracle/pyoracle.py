@@ -1,0 +1,214 @@
+"""ctypes binding of the oracle (TEST INFRASTRUCTURE ONLY).
+
+Loads oracle/_build/liboracle.so (the CPU double-precision restatement of
+the reference's E-step) and, if built, oracle/_ref/libref_healpix.so (the
+reference's own HEALPix code).  Only tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline legs import this module.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+I64, F64, P = C.c_int64, C.c_double, C.c_void_p
+
+
+class OracleModel(C.Structure):
+    _fields_ = [(n, I64) for n in (
+        "ori_size", "nr_classes", "current_size", "coarse_size", "padding_factor",
+        "proj_r_max", "proj_xdim", "proj_ydim", "proj_zdim", "proj_yinit", "proj_zinit",
+        "bp_r_max", "bp_xdim", "bp_ydim", "bp_zdim", "bp_yinit", "bp_zinit",
+        "healpix_order", "adaptive_oversampling", "maximum_significants", "sigma2_len",
+        "do_scale_correction", "do_norm_correction", "do_map", "pad_int_")] + \
+        [(n, F64) for n in ("pixel_size", "psi_step", "offset_range", "offset_step",
+                            "adaptive_fraction", "sigma2_fudge", "sigma2_offset",
+                            "avg_norm_correction")] + \
+        [(n, P) for n in ("ppref", "sigma2_noise", "pdf_class", "pdf_direction", "data_vs_prior")]
+
+
+class OracleParticle(C.Structure):
+    _fields_ = [(n, P) for n in ("fimg", "fimg_nomask", "fctf", "power_img")] + \
+        [("old_offset", F64 * 2), ("prior", F64 * 2)] + \
+        [(n, F64) for n in ("highres_Xi2", "norm_correction", "scale", "pad_")]
+
+
+class OracleResult(C.Structure):
+    _fields_ = [(n, F64) for n in (
+        "rot", "tilt", "psi", "xoff", "yoff", "cls", "pmax", "dLL", "norm", "nr_sign",
+        "coarse_min_diff2", "coarse_sum_weight", "coarse_significant_weight",
+        "fine_min_diff2", "fine_sum_weight", "fine_significant_weight")] + \
+        [("best_ihidden_over", I64), ("pad_", I64)]
+
+
+class OracleDebug(C.Structure):
+    _fields_ = [(n, P) for n in ("coarse_diff2", "coarse_weight", "coarse_significant",
+                                 "fine_diff2", "fine_weight")]
+
+
+class OracleWsum(C.Structure):
+    _fields_ = [(n, P) for n in ("sigma2_noise", "pdf_class", "pdf_direction", "bp_data",
+                                 "bp_weight")] + \
+        [(n, F64) for n in ("sigma2_offset", "sumw_group", "LL", "ave_Pmax",
+                            "avg_norm_correction", "wsum_signal_product",
+                            "wsum_reference_power", "pad_")]
+
+
+_O = None
+_R = None
+
+
+def load():
+    global _O
+    if _O is None:
+        path = os.path.join(HERE, "_build", "liboracle.so")
+        if not os.path.exists(path):
+            raise RuntimeError("oracle not built: %s (run oracle/build.py)" % path)
+        lib = C.CDLL(path)
+        lib.oracle_expectation.restype = C.c_int
+        lib.oracle_ctf.restype = F64
+        lib.oracle_ctf.argtypes = [F64] * 11
+        lib.oracle_hpx_xyf2nest.restype = I64
+        lib.oracle_hpx_xyf2nest.argtypes = [I64] * 4
+        lib.oracle_oversampled_orientations.restype = C.c_int
+        lib.oracle_translations.restype = C.c_int
+        lib.oracle_oversampled_translations.restype = C.c_int
+        _O = lib
+    return _O
+
+
+def load_ref():
+    """The reference's own Healpix_Base (None if oracle/_ref was not built)."""
+    global _R
+    if _R is None:
+        path = os.path.join(HERE, "_ref", "libref_healpix.so")
+        if not os.path.exists(path):
+            return None
+        lib = C.CDLL(path)
+        lib.ref_hpx_xyf2nest.restype = C.c_int
+        _R = lib
+    return _R
+
+
+def sampling_sizes(order, psi_step, offset_range, offset_step):
+    o = load()
+    v = [I64() for _ in range(3)]
+    o.oracle_sampling_sizes(I64(order), F64(psi_step), F64(offset_range), F64(offset_step),
+                            *[C.byref(x) for x in v])
+    return [x.value for x in v]
+
+
+def ctf(defU, defV, defAng, kV, Cs, Q0, Bfac, scale, phase_shift, X, Y):
+    return load().oracle_ctf(defU, defV, defAng, kV, Cs, Q0, Bfac, scale, phase_shift, X, Y)
+
+
+def directions(order):
+    n = 12 * 4 ** order
+    rot, tilt, ipix = np.zeros(n), np.zeros(n), np.zeros(n, np.int64)
+    load().oracle_directions(I64(order), rot.ctypes.data_as(P), tilt.ctypes.data_as(P),
+                             ipix.ctypes.data_as(P))
+    return rot, tilt, ipix
+
+
+def bp_geometry(current_size, ori_size, pad=2):
+    r_max = min(current_size // 2, ori_size // 2)
+    pad_size = 2 * (int(pad * r_max + 0.5) + 1) + 1
+    return dict(r_max=r_max, xdim=pad_size // 2 + 1, ydim=pad_size, zdim=pad_size,
+                yinit=-(pad_size // 2), zinit=-(pad_size // 2))
+
+
+def run(model, refs, batch, debug=False):
+    """Oracle E-step for a batch.
+
+    model: dict (same keys as relion_gb300's model dict); refs: list of
+    reference dicts from relion_gb300.datagen.padded_reference (one per
+    class); batch: host particle batch dict.  Returns (results, debug,
+    wsum dict, bp_data [K][z][y][x] complex, bp_weight).
+    """
+    o = load()
+    K = int(model["nr_classes"])
+    keep = []
+
+    def arr(a, dt=np.float64):
+        a = np.ascontiguousarray(a, dtype=dt)
+        keep.append(a)
+        return a.ctypes.data
+
+    r0 = refs[0]
+    ppref = np.stack([np.asarray(r["data"], np.complex128) for r in refs])
+    bg = bp_geometry(int(model["current_size"]), int(model["ori_size"]), int(model["padding_factor"]))
+    m = OracleModel()
+    for k in ("ori_size", "nr_classes", "current_size", "coarse_size", "padding_factor",
+              "healpix_order", "adaptive_oversampling", "maximum_significants", "sigma2_len",
+              "do_scale_correction", "do_norm_correction", "do_map"):
+        setattr(m, k, int(model[k]))
+    m.proj_r_max, m.proj_xdim, m.proj_ydim, m.proj_zdim = r0["r_max"], r0["xdim"], r0["ydim"], r0["zdim"]
+    m.proj_yinit, m.proj_zinit = r0["yinit"], r0["zinit"]
+    m.bp_r_max, m.bp_xdim, m.bp_ydim, m.bp_zdim = bg["r_max"], bg["xdim"], bg["ydim"], bg["zdim"]
+    m.bp_yinit, m.bp_zinit = bg["yinit"], bg["zinit"]
+    for k in ("pixel_size", "psi_step", "offset_range", "offset_step", "adaptive_fraction",
+              "sigma2_fudge", "sigma2_offset", "avg_norm_correction"):
+        setattr(m, k, float(model[k]))
+    m.ppref = arr(ppref, np.complex128)
+    m.sigma2_noise = arr(model["sigma2_noise"])
+    m.pdf_class = arr(model["pdf_class"])
+    m.pdf_direction = arr(model["pdf_direction"])
+    m.data_vs_prior = arr(model["data_vs_prior"]) if model.get("data_vs_prior") is not None else None
+
+    n = int(batch["n"])
+    parts = (OracleParticle * n)()
+    fimg = np.ascontiguousarray(batch["fimg"], np.complex64).astype(np.complex128)
+    fnm = np.ascontiguousarray(batch["fimg_nomask"], np.complex64).astype(np.complex128)
+    fctf = np.ascontiguousarray(batch["fctf"], np.float32).astype(np.float64)
+    keep += [fimg, fnm, fctf]
+    power = np.ascontiguousarray(batch["power_img"], np.float64)
+    keep.append(power)
+    for i in range(n):
+        p = parts[i]
+        p.fimg = fimg[i].ctypes.data
+        p.fimg_nomask = fnm[i].ctypes.data
+        p.fctf = fctf[i].ctypes.data
+        p.power_img = power[i].ctypes.data
+        p.old_offset[0], p.old_offset[1] = batch["old_offset"][i]
+        p.prior[0], p.prior[1] = batch["prior"][i]
+        p.highres_Xi2 = float(batch["highres_Xi2"][i])
+        p.norm_correction = float(batch["norm_correction"][i])
+        p.scale = float(batch["scale"][i])
+    res = (OracleResult * n)()
+    ndir, npsi, ntr = sampling_sizes(int(model["healpix_order"]), float(model["psi_step"]),
+                                     float(model["offset_range"]), float(model["offset_step"]))
+    RT = K * ndir * npsi * ntr
+    nfine = RT * 32
+    dbg = None
+    dbg_arrays = []
+    if debug:
+        dbg = (OracleDebug * n)()
+        for i in range(n):
+            a = dict(coarse_diff2=np.zeros(RT), coarse_weight=np.zeros(RT),
+                     coarse_significant=np.zeros(RT, np.uint8), fine_diff2=np.zeros(nfine),
+                     fine_weight=np.zeros(nfine))
+            for k, v in a.items():
+                setattr(dbg[i], k, v.ctypes.data)
+            dbg_arrays.append(a)
+    half = int(model["ori_size"]) // 2 + 1
+    vox = bg["xdim"] * bg["ydim"] * bg["zdim"]
+    ws = dict(sigma2_noise=np.zeros(half), pdf_class=np.zeros(K), pdf_direction=np.zeros(K * ndir),
+              bp_data=np.zeros((K, bg["zdim"], bg["ydim"], bg["xdim"]), np.complex128),
+              bp_weight=np.zeros((K, bg["zdim"], bg["ydim"], bg["xdim"])))
+    w = OracleWsum()
+    for k in ("sigma2_noise", "pdf_class", "pdf_direction", "bp_data", "bp_weight"):
+        setattr(w, k, ws[k].ctypes.data)
+    st = o.oracle_expectation(C.byref(m), I64(n), parts, res, dbg, C.byref(w))
+    if st != 0:
+        raise RuntimeError("oracle_expectation failed with status %d" % st)
+    out = np.zeros(n, dtype=[(f, np.float64) for f, _ in OracleResult._fields_ if f != "pad_"])
+    for i in range(n):
+        for f in out.dtype.names:
+            out[f][i] = getattr(res[i], f)
+    wsum = {k: getattr(w, k) for k in ("sigma2_offset", "sumw_group", "LL", "ave_Pmax",
+                                       "avg_norm_correction", "wsum_signal_product",
+                                       "wsum_reference_power")}
+    wsum.update(sigma2_noise=ws["sigma2_noise"], pdf_class=ws["pdf_class"],
+                pdf_direction=ws["pdf_direction"].reshape(K, ndir))
+    del keep, vox
+    return out, dbg_arrays, wsum, ws["bp_data"], ws["bp_weight"]

@@ -1,0 +1,141 @@
+/*
+ * relion_oracle.h -- TEST INFRASTRUCTURE ONLY.
+ *
+ * C ABI of the CPU double-precision restatement of relion_refine's CPU
+ * expectation step (relion_refine without --gpu, RFLOAT = double).  Only
+ * tests/, __graft_entry__.smoke() and bench.py's cpu_baseline / reference
+ * arm may load the library built from relion_oracle.cpp; the product path
+ * (libgbrelion) never links or calls it.
+ *
+ * Parity pins:
+ *   - CTF value: reference tests/ctf.cpp:8-9 (getCTF(10,10) = 0.59154).
+ *   - HEALPix NEST enumeration: compared index-for-index and bit-for-bit
+ *     against the reference's own src/Healpix_2.15a/healpix_base.cc, compiled
+ *     from its source files into oracle/_ref (see oracle/build_ref.sh).
+ *   - Everything downstream of the enumeration (projection, diff2, weights,
+ *     significance, weighted sums, backprojection) is a restatement of
+ *     src/ml_optimiser.cpp, src/projector.cpp and src/backprojector.cpp
+ *     that the reference's tests do not pin (no golden vectors exist).
+ */
+#ifndef RELION_ORACLE_H
+#define RELION_ORACLE_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Model and sampling state read by the E-step (MlOptimiser / MlModel /
+ * HealpixSampling members).  All lengths in pixels unless stated. */
+typedef struct {
+    int64_t ori_size;            /* mymodel.ori_size                               */
+    int64_t nr_classes;          /* mymodel.nr_classes                             */
+    int64_t current_size;        /* image_current_size[optics_group]              */
+    int64_t coarse_size;         /* image_coarse_size[optics_group]               */
+    int64_t padding_factor;      /* PPref/BPref padding factor (2)                 */
+    /* padded Fourier reference (Projector::data), one per class               */
+    int64_t proj_r_max, proj_xdim, proj_ydim, proj_zdim, proj_yinit, proj_zinit;
+    /* backprojector volumes (BackProjector::data / weight), one per class      */
+    int64_t bp_r_max, bp_xdim, bp_ydim, bp_zdim, bp_yinit, bp_zinit;
+    /* sampling (HealpixSampling)                                               */
+    int64_t healpix_order;
+    int64_t adaptive_oversampling;
+    int64_t maximum_significants;  /* --maxsig (<=0: off)                         */
+    int64_t sigma2_len;            /* XSIZE(mymodel.sigma2_noise[optics_group])   */
+    int64_t do_scale_correction;
+    int64_t do_norm_correction;
+    int64_t do_map;
+    int64_t pad_int_;
+    double pixel_size;           /* mymodel.pixel_size == particle pixel size     */
+    double psi_step;             /* degrees (<=0: 360/(6*2^order))                */
+    double offset_range;         /* Angstrom (command line px * pixel size)       */
+    double offset_step;          /* Angstrom                                      */
+    double adaptive_fraction;
+    double sigma2_fudge;
+    double sigma2_offset;        /* Angstrom^2                                     */
+    double avg_norm_correction;
+    const double *ppref;         /* [K][z][y][x][2]                                */
+    const double *sigma2_noise;  /* [sigma2_len]                                    */
+    const double *pdf_class;     /* [K]                                            */
+    const double *pdf_direction; /* [K][ndir]                                      */
+    const double *data_vs_prior; /* [K][ori/2+1] (scale correction only)           */
+} oracle_model;
+
+typedef struct {
+    const double *fimg;          /* [cur][cur/2+1][2] masked image FT              */
+    const double *fimg_nomask;   /* [cur][cur/2+1][2]                              */
+    const double *fctf;          /* [cur][cur/2+1]                                 */
+    const double *power_img;     /* [ori/2+1]                                       */
+    double old_offset[2];        /* pixels                                         */
+    double prior[2];             /* pixels                                         */
+    double highres_Xi2;
+    double norm_correction;      /* metadata NORM                                   */
+    double scale;                /* scale_correction[group]                         */
+    double pad_;
+} oracle_particle;
+
+/* per-particle results (metadata columns written by storeWeightedSums) */
+typedef struct {
+    double rot, tilt, psi, xoff, yoff;
+    double cls;                  /* 1-based class                                   */
+    double pmax, dLL, norm;
+    double nr_sign;
+    double coarse_min_diff2, coarse_sum_weight, coarse_significant_weight;
+    double fine_min_diff2, fine_sum_weight, fine_significant_weight;
+    int64_t best_ihidden_over;   /* fine-pass index of the PMAX pose               */
+    int64_t pad_;
+} oracle_result;
+
+/* optional per-particle debug arrays (NULL to skip) */
+typedef struct {
+    double *coarse_diff2;        /* [R*T] before conversion, -999 = not computed   */
+    double *coarse_weight;       /* [R*T] after conversion                          */
+    uint8_t *coarse_significant; /* [R*T]                                          */
+    double *fine_diff2;          /* [R*T*nOR*nOT]                                   */
+    double *fine_weight;         /* [R*T*nOR*nOT]                                   */
+} oracle_debug;
+
+/* weighted sums (MlWsumModel members), accumulated (+=) by the oracle */
+typedef struct {
+    double *sigma2_noise;        /* [ori/2+1]                                       */
+    double *pdf_class;           /* [K]                                             */
+    double *pdf_direction;       /* [K][ndir]                                       */
+    double *bp_data;             /* [K][bz][by][bx][2]                              */
+    double *bp_weight;           /* [K][bz][by][bx]                                 */
+    double sigma2_offset, sumw_group, LL, ave_Pmax, avg_norm_correction;
+    double wsum_signal_product, wsum_reference_power;
+    double pad_;
+} oracle_wsum;
+
+int oracle_expectation(const oracle_model *m, int64_t n, const oracle_particle *parts,
+                       oracle_result *res, oracle_debug *dbg, oracle_wsum *wsum);
+
+/* --- building blocks exposed for unit checks --------------------------- */
+double oracle_ctf(double defU, double defV, double defAng, double kV, double Cs,
+                  double Q0, double Bfac, double scale, double phase_shift,
+                  double X, double Y);
+/* number of coarse directions/psi/translations */
+int oracle_sampling_sizes(int64_t order, double psi_step, double offset_range,
+                          double offset_step, int64_t *ndir, int64_t *npsi, int64_t *ntrans);
+/* coarse direction table: rot/tilt (degrees) and NEST pixel per direction */
+int oracle_directions(int64_t order, double *rot, double *tilt, int64_t *ipix);
+/* oversampled orientations of (idir, ipsi): nOR entries */
+int oracle_oversampled_orientations(int64_t order, double psi_step, int64_t idir, int64_t ipsi,
+                                    int64_t ov, double *rot, double *tilt, double *psi);
+/* translations (Angstrom) of the coarse grid */
+int oracle_translations(double offset_range, double offset_step, double *tx, double *ty);
+/* oversampled translations of itrans, in pixels */
+int oracle_oversampled_translations(double offset_range, double offset_step, int64_t itrans,
+                                    int64_t ov, double pixel_size, double *tx, double *ty);
+/* HEALPix raw functions */
+void oracle_hpx_pix2ang_z_phi(int64_t order, int64_t pix, double *z, double *phi);
+void oracle_hpx_nest2xyf(int64_t order, int64_t pix, int64_t *ix, int64_t *iy, int64_t *face);
+int64_t oracle_hpx_xyf2nest(int64_t order, int64_t ix, int64_t iy, int64_t face);
+/* Euler (rot,tilt,psi) -> 3x3 row-major */
+void oracle_euler(double rot, double tilt, double psi, double *A);
+/* Fourier slice of one class at the given size, A row-major 3x3; out [size][size/2+1][2] */
+void oracle_project(const oracle_model *m, int64_t iclass, const double *A, int64_t size, double *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

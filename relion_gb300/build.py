@@ -1,0 +1,65 @@
+"""Build libgbrelion (the sm_103a CUDA E-step) in-tree with nvcc.
+
+The four translation units are compiled in parallel and linked into
+relion_gb300/_build/libgbrelion.so.  Host code is compiled with
+-ffp-contract=off so that the pose enumeration is bit-identical to the
+reference's double-precision arithmetic.
+"""
+import os
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "libgbrelion.so")
+SOURCES = ["k_project.cu", "k_gemm.cu", "k_estep.cu", "estep.cu"]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def _nvcc():
+    for cand in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", "nvcc"):
+        if cand and (os.path.isabs(cand) and os.path.exists(cand) or not os.path.isabs(cand)):
+            return cand
+    return "nvcc"
+
+
+def _run(cmd):
+    proc = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if proc.returncode != 0:
+        raise RuntimeError("command failed: %s\n%s" % (" ".join(cmd), proc.stdout))
+    return proc.stdout
+
+
+def build(verbose=False, force=False):
+    """Compile libgbrelion.so if any source is newer than it; return its path."""
+    os.makedirs(BUILD, exist_ok=True)
+    deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
+    deps.append(os.path.join(HERE, "..", "include", "gbrelion.h"))
+    if (not force and os.path.exists(LIB)
+            and os.path.getmtime(LIB) >= max(os.path.getmtime(d) for d in deps)):
+        return LIB
+    nvcc = _nvcc()
+    flags = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
+                    "-Xcompiler", "-ffp-contract=off", "-Xptxas", "-v"]
+
+    def one(src):
+        obj = os.path.join(BUILD, src.replace(".cu", ".o"))
+        out = _run([nvcc] + flags + ["-c", os.path.join(CSRC, src), "-o", obj])
+        with open(obj + ".ptxas.txt", "w") as fh:
+            fh.write(out)
+        return obj
+
+    with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
+        objs = list(ex.map(one, SOURCES))
+    tmp = LIB + ".tmp"
+    _run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"])
+    os.replace(tmp, LIB)
+    if verbose:
+        print("built", LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    build(verbose=True, force="--force" in sys.argv)

@@ -1,0 +1,981 @@
+// estep.cu -- host side of libgbrelion: the C ABI of include/gbrelion.h,
+// the per-iteration device tables (MlDeviceBundle) and the batched E-step
+// driver (MlOptimiserCuda::doThreadExpectationSomeParticles).
+//
+// One batch runs as: particle preparation -> coarse norm GEMM -> coarse
+// cross GEMM (diff2) -> weights + threshold search -> significance masks and
+// fine jobs -> fine projections (cached per iteration) -> fine diff2 ->
+// weights + threshold search -> weighted sums -> backprojection.  The host
+// synchronises once per batch, after the coarse significance, to size the
+// fine pass, and once at the end to read the per-particle results.
+#include "../../include/gbrelion.h"
+#include "gbr_internal.h"
+#include "sampling.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+using namespace gbr;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int status, const std::string &msg) {
+    g_last_error = msg;
+    return status;
+}
+
+#define GBR_CUDA(expr)                                                                     \
+    do {                                                                                   \
+        cudaError_t e_ = (expr);                                                           \
+        if (e_ != cudaSuccess) {                                                           \
+            int st_ = (e_ == cudaErrorMemoryAllocation) ? GBR_ERR_OOM : GBR_ERR_CUDA;      \
+            return fail(st_, std::string(#expr) + ": " + cudaGetErrorString(e_));          \
+        }                                                                                  \
+    } while (0)
+
+template <class T>
+struct DevBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    DevBuf(DevBuf &&o) noexcept : p(o.p), n(o.n) {
+        o.p = nullptr;
+        o.n = 0;
+    }
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    // grow to at least m elements (contents discarded)
+    cudaError_t reserve(size_t m) {
+        if (m <= n && p) return cudaSuccess;
+        release();
+        size_t bytes = std::max<size_t>(m, 1) * sizeof(T);
+        cudaError_t e = cudaMalloc(&p, bytes);
+        if (e == cudaSuccess) n = std::max<size_t>(m, 1);
+        return e;
+    }
+    cudaError_t upload(const T *h, size_t m) {
+        cudaError_t e = reserve(m);
+        if (e != cudaSuccess) return e;
+        return cudaMemcpy(p, h, m * sizeof(T), cudaMemcpyHostToDevice);
+    }
+    cudaError_t zero(cudaStream_t st = 0) { return cudaMemsetAsync(p, 0, n * sizeof(T), st); }
+};
+
+inline int pad16(int v) { return (v + 15) / 16 * 16; }
+
+// Resolution-shell index (Mresol) of pixel (x, y) of an image of size s.
+inline int shell_of(int x, int y, int s) {
+    const int ires = iround(std::sqrt((double)(x * x + y * y)));
+    if (ires < s / 2 + 1 && !(x == 0 && y < 0)) return ires;
+    return -1;
+}
+
+inline float ord2f_host(unsigned int u) {
+    unsigned int b = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u;
+    float f;
+    std::memcpy(&f, &b, 4);
+    return f;
+}
+
+enum Stage { ST_PREP = 0, ST_NORM, ST_CROSS, ST_WCOARSE, ST_SIG, ST_PROJF, ST_FINE, ST_WFINE,
+             ST_WSUM, ST_BP, ST_N };
+
+}  // namespace
+
+struct gbr_bundle {
+    gbr_model_desc d{};
+    int device = 0;
+    PoseGrid grid;
+    long K = 0, ND = 0, NP = 0, T = 0, R = 0, nOR = 0, nOT = 0, RF = 0, TF = 0;
+    int nshell = 0;  // ori/2+1
+    int cur = 0, crs = 0, full_npix = 0;
+    // pixel lists
+    std::vector<PixelRef> pc_h, pf_h;
+    int nc = 0, nf = 0, ldk_c = 0, lda_c = 0;
+    double logsigma2 = 0.;
+    size_t budget = 0;
+    // model arrays (host copies)
+    std::vector<double> sigma2, pdf_class, pdf_dir, dvp;
+    bool have_arrays = false;
+    // projector
+    VolGeom pg{}, bg{};
+    std::vector<DevBuf<float2>> vol;
+    std::vector<char> have_vol;
+    DevBuf<const float2 *> vols_d;
+    // backprojector (FP64)
+    std::vector<DevBuf<double2>> bp_data;
+    std::vector<DevBuf<double>> bp_weight;
+    DevBuf<double2 *> bpd_ptrs;
+    DevBuf<double *> bpw_ptrs;
+    size_t bp_vox = 0;
+    // iteration tables
+    bool tables_ready = false;
+    DevBuf<PixelRef> pc, pf;
+    DevBuf<float> minv_c, minv_f, minv_store;
+    DevBuf<float> eul_c, eul_f;
+    DevBuf<int> cls_c, cls_f, cls_of_r;
+    DevBuf<float> pdf_orient;
+    DevBuf<double> tx, ty, otx, oty;
+    std::vector<double> otx_h, oty_h;
+    DevBuf<float2> phase_c, phase_f;
+    DevBuf<float> proj_c, proj2_c;
+    DevBuf<float2> proj_f;
+    std::vector<unsigned char> proj_f_done;
+    DevBuf<float2> bpimg;
+    DevBuf<float> bpw;
+    DevBuf<unsigned char> active;
+    DevBuf<unsigned char> dvp_mask;
+    // weighted sums
+    DevBuf<double> w_pdf_cls, w_pdf_dir;
+    std::vector<double> w_sigma2;
+    double w_sigma2_offset = 0, w_sumw_group = 0, w_LL = 0, w_ave_Pmax = 0, w_avg_norm = 0, w_XA = 0,
+           w_AA = 0;
+};
+
+struct gbr_worker {
+    gbr_bundle *b = nullptr;
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev[ST_N + 1] = {};
+    double stage_ms[ST_N] = {};
+    int debug = 0;
+    int cap = 0;  // particles the batch buffers hold
+    long long launches = 0;  // kernels launched by this worker
+    // inputs
+    DevBuf<float2> X, Xn;
+    DevBuf<float> C;
+    DevBuf<double> pdat, power;
+    // prepared
+    DevBuf<float> a_c, a_f, Cf;
+    DevBuf<float2> b_c, b_f, Xf, Xnf;
+    DevBuf<ParticleState> ps;
+    DevBuf<float> pdf_off, nrm, vals;
+    DevBuf<long long> seg_c, seg_f;
+    DevBuf<HistBin> hist;
+    DevBuf<unsigned int> mask;
+    DevBuf<int> cnt;
+    DevBuf<long long> flags, entries, jpos, epos, scan_tmp;
+    DevBuf<FineJob> jobs;
+    DevBuf<unsigned char> need_r;
+    DevBuf<int> proj_ids, act_list, act_count;
+    DevBuf<float> fd;
+    DevBuf<int> ejob;
+    DevBuf<unsigned int> ecode;
+    DevBuf<double> shell, pacc;
+    // debug copies of the last batch
+    int dbg_n = 0;
+    std::vector<float> dbg_coarse;   // relative diff2
+    std::vector<float> dbg_wcoarse;
+    std::vector<double> dbg_cc, dbg_cf;
+    std::vector<float> dbg_fine, dbg_wfine;
+    std::vector<int> dbg_ejob;
+    std::vector<unsigned int> dbg_ecode;
+    std::vector<FineJob> dbg_jobs;
+    std::vector<long long> dbg_segf;
+};
+
+namespace {
+
+int build_tables(gbr_bundle *b) {
+    if (b->tables_ready) return GBR_OK;
+    if (!b->have_arrays) return fail(GBR_ERR_STATE, "model arrays not set (gbr_model_set_arrays)");
+    for (long k = 0; k < b->K; ++k)
+        if (!b->have_vol[k]) return fail(GBR_ERR_STATE, "reference of class " + std::to_string(k) + " not uploaded");
+    const gbr_model_desc &d = b->d;
+    const double pix = d.pixel_size;
+    // ---- pixel lists and noise weights (src/ml_optimiser.cpp:6880-6892) ----
+    auto minv_of = [&](int shell) -> double {
+        if (shell > 0 && shell < d.sigma2_len) return 1. / (d.sigma2_fudge * b->sigma2[shell]);
+        return 0.;
+    };
+    b->pc_h.clear();
+    std::vector<float> mc;
+    for (int i = 0; i < b->crs; ++i) {
+        const int X = b->crs / 2 + 1;
+        const int y = (i < X) ? i : i - b->crs;
+        for (int x = 0; x < X; ++x) {
+            const int sh = shell_of(x, y, b->crs);
+            const double m = minv_of(sh);
+            if (m > 0.) {
+                const int yi = y < 0 ? y + b->cur : y;  // row in the fine image
+                b->pc_h.push_back(PixelRef{x, y, yi * (b->cur / 2 + 1) + x, sh});
+                mc.push_back((float)(0.5 * m));
+            }
+        }
+    }
+    b->pf_h.clear();
+    std::vector<float> mf, ms;
+    for (int i = 0; i < b->cur; ++i) {
+        const int X = b->cur / 2 + 1;
+        const int y = (i < X) ? i : i - b->cur;
+        for (int x = 0; x < X; ++x) {
+            const int sh = shell_of(x, y, b->cur);
+            if (sh < 0) continue;
+            b->pf_h.push_back(PixelRef{x, y, i * X + x, sh});
+            const double m = minv_of(sh);
+            mf.push_back((float)(0.5 * m));
+            double mst = m;
+            if (x == 0 && y == 0) mst = 1. / (d.sigma2_fudge * b->sigma2[0]);  // :8301
+            ms.push_back(d.do_map ? (float)mst : 1.f);
+        }
+    }
+    b->nc = (int)b->pc_h.size();
+    b->nf = (int)b->pf_h.size();
+    b->ldk_c = pad16(std::max(b->nc, 1));
+    b->lda_c = pad16(2 * std::max(b->nc, 1));
+    // log(2 pi sigma2) over the fine pixels (storeWeightedSums :9032-9038)
+    b->logsigma2 = 0.;
+    for (const PixelRef &p : b->pf_h)
+        if (p.shell > 0 && p.shell < d.sigma2_len) b->logsigma2 += std::log(2. * kPi * b->sigma2[p.shell]);
+    GBR_CUDA(b->pc.upload(b->pc_h.data(), b->pc_h.size()));
+    GBR_CUDA(b->pf.upload(b->pf_h.data(), b->pf_h.size()));
+    GBR_CUDA(b->minv_c.upload(mc.data(), mc.size()));
+    GBR_CUDA(b->minv_f.upload(mf.data(), mf.size()));
+    GBR_CUDA(b->minv_store.upload(ms.data(), ms.size()));
+
+    // ---- orientation tables ----
+    const long R = b->R, RF = b->RF;
+    std::vector<float> ec((size_t)R * 9), ef((size_t)RF * 9), po(R);
+    std::vector<int> cc(R), cf(RF), cr(R);
+    double mean = 0.;
+    for (long ic = 0; ic < b->K; ++ic)
+        for (long id = 0; id < b->ND; ++id)
+            for (long is = 0; is < b->NP; ++is) mean += b->pdf_dir[ic * b->ND + id];
+    mean /= (double)R;
+    std::vector<double> fr(b->nOR), ft(b->nOR), fp(b->nOR);
+    double A[9];
+    for (long ic = 0; ic < b->K; ++ic)
+        for (long id = 0; id < b->ND; ++id)
+            for (long is = 0; is < b->NP; ++is) {
+                const long r = (ic * b->ND + id) * b->NP + is;
+                euler_to_matrix(b->grid.dir_rot[id], b->grid.dir_tilt[id], b->grid.psi[is], A);
+                for (int a = 0; a < 3; ++a)
+                    for (int c = 0; c < 3; ++c) ec[(size_t)r * 9 + a * 3 + c] = (float)(A[c * 3 + a] * d.padding_factor);
+                double pdf = b->pdf_dir[ic * b->ND + id];
+                if (mean != 0.) pdf /= mean;
+                po[r] = (b->pdf_class[ic] > 0. && b->pdf_dir[ic * b->ND + id] > 0.) ? (float)pdf : 0.f;
+                cc[r] = (int)ic;
+                cr[r] = (int)ic;
+                b->grid.fine_orientations(id, is, fr.data(), ft.data(), fp.data());
+                for (long io = 0; io < b->nOR; ++io) {
+                    const long rf = r * b->nOR + io;
+                    euler_to_matrix(fr[io], ft[io], fp[io], A);
+                    for (int a = 0; a < 3; ++a)
+                        for (int c = 0; c < 3; ++c)
+                            ef[(size_t)rf * 9 + a * 3 + c] = (float)(A[c * 3 + a] * d.padding_factor);
+                    cf[rf] = (int)ic;
+                }
+            }
+    GBR_CUDA(b->eul_c.upload(ec.data(), ec.size()));
+    GBR_CUDA(b->eul_f.upload(ef.data(), ef.size()));
+    GBR_CUDA(b->cls_c.upload(cc.data(), cc.size()));
+    GBR_CUDA(b->cls_f.upload(cf.data(), cf.size()));
+    GBR_CUDA(b->cls_of_r.upload(cr.data(), cr.size()));
+    GBR_CUDA(b->pdf_orient.upload(po.data(), po.size()));
+
+    // ---- translations and phase tables ----
+    std::vector<double> tx(b->grid.trans_x), ty(b->grid.trans_y);
+    std::vector<double> ctx(b->T), cty(b->T);
+    for (long t = 0; t < b->T; ++t) {
+        ctx[t] = tx[t] / pix;
+        cty[t] = ty[t] / pix;
+    }
+    b->otx_h.assign(b->TF, 0.);
+    b->oty_h.assign(b->TF, 0.);
+    for (long t = 0; t < b->T; ++t) b->grid.fine_translations(t, pix, &b->otx_h[t * b->nOT], &b->oty_h[t * b->nOT]);
+    GBR_CUDA(b->tx.upload(tx.data(), tx.size()));
+    GBR_CUDA(b->ty.upload(ty.data(), ty.size()));
+    GBR_CUDA(b->otx.upload(b->otx_h.data(), b->otx_h.size()));
+    GBR_CUDA(b->oty.upload(b->oty_h.data(), b->oty_h.size()));
+    DevBuf<double> ctx_d, cty_d;
+    GBR_CUDA(ctx_d.upload(ctx.data(), ctx.size()));
+    GBR_CUDA(cty_d.upload(cty.data(), cty.size()));
+    GBR_CUDA(b->phase_c.reserve((size_t)b->T * b->ldk_c));
+    GBR_CUDA(b->phase_c.zero());
+    GBR_CUDA(launch_phase_table(b->phase_c.p, ctx_d.p, cty_d.p, (int)b->T, b->pc.p, b->nc, b->ldk_c,
+                                (double)d.ori_size, 0));
+    GBR_CUDA(b->phase_f.reserve((size_t)b->TF * b->nf));
+    GBR_CUDA(launch_phase_table(b->phase_f.p, b->otx.p, b->oty.p, (int)b->TF, b->pf.p, b->nf, b->nf,
+                                (double)d.ori_size, 0));
+
+    // ---- coarse projections (shared by every batch of the iteration) ----
+    std::vector<const float2 *> vp(b->K);
+    for (long k = 0; k < b->K; ++k) vp[k] = b->vol[k].p;
+    GBR_CUDA(b->vols_d.upload(vp.data(), vp.size()));
+    GBR_CUDA(b->proj_c.reserve((size_t)R * b->lda_c));
+    GBR_CUDA(b->proj2_c.reserve((size_t)R * b->ldk_c));
+    GBR_CUDA(b->proj_c.zero());
+    GBR_CUDA(b->proj2_c.zero());
+    GBR_CUDA(launch_project_rows(b->vols_d.p, b->pg, b->eul_c.p, b->cls_c.p, nullptr, (int)R, b->pc.p, b->nc,
+                                 b->proj_c.p, b->lda_c, b->proj2_c.p, b->ldk_c, nullptr, 0));
+    // ---- fine projection cache, slice accumulators ----
+    GBR_CUDA(b->proj_f.reserve((size_t)RF * b->nf));
+    b->proj_f_done.assign(RF, 0);
+    GBR_CUDA(b->bpimg.reserve((size_t)RF * b->nf));
+    GBR_CUDA(b->bpw.reserve((size_t)RF * b->nf));
+    GBR_CUDA(b->active.reserve(RF));
+    GBR_CUDA(b->bpimg.zero());
+    GBR_CUDA(b->bpw.zero());
+    GBR_CUDA(b->active.zero());
+    // scale-correction shell mask data_vs_prior > 3
+    std::vector<unsigned char> dm((size_t)b->K * b->nshell, 0);
+    if (d.do_scale_correction && !b->dvp.empty())
+        for (size_t i = 0; i < dm.size(); ++i) dm[i] = b->dvp[i] > 3. ? 1 : 0;
+    GBR_CUDA(b->dvp_mask.upload(dm.data(), dm.size()));
+    GBR_CUDA(cudaDeviceSynchronize());
+    b->tables_ready = true;
+    return GBR_OK;
+}
+
+int ensure_capacity(gbr_worker *w, int n) {
+    gbr_bundle *b = w->b;
+    if (n <= w->cap) return GBR_OK;
+    const size_t full = (size_t)b->full_npix;
+    GBR_CUDA(w->X.reserve(n * full));
+    GBR_CUDA(w->Xn.reserve(n * full));
+    GBR_CUDA(w->C.reserve(n * full));
+    GBR_CUDA(w->pdat.reserve((size_t)n * 8));
+    GBR_CUDA(w->power.reserve((size_t)n * b->nshell));
+    GBR_CUDA(w->a_c.reserve((size_t)n * b->ldk_c));
+    GBR_CUDA(w->b_c.reserve((size_t)n * b->ldk_c));
+    GBR_CUDA(w->a_f.reserve((size_t)n * b->nf));
+    GBR_CUDA(w->b_f.reserve((size_t)n * b->nf));
+    GBR_CUDA(w->Xf.reserve((size_t)n * b->nf));
+    GBR_CUDA(w->Xnf.reserve((size_t)n * b->nf));
+    GBR_CUDA(w->Cf.reserve((size_t)n * b->nf));
+    GBR_CUDA(w->ps.reserve(n));
+    GBR_CUDA(w->pdf_off.reserve((size_t)n * b->T));
+    GBR_CUDA(w->nrm.reserve((size_t)n * b->R));
+    GBR_CUDA(w->vals.reserve((size_t)n * b->R * b->T));
+    GBR_CUDA(w->seg_c.reserve(n + 1));
+    GBR_CUDA(w->seg_f.reserve(n + 1));
+    GBR_CUDA(w->hist.reserve((size_t)n * kHistBins));
+    const int W = (int)((b->T + 31) / 32);
+    GBR_CUDA(w->mask.reserve((size_t)n * b->R * W));
+    GBR_CUDA(w->cnt.reserve((size_t)n * b->R));
+    GBR_CUDA(w->flags.reserve((size_t)n * b->R + 1));
+    GBR_CUDA(w->entries.reserve((size_t)n * b->R + 1));
+    GBR_CUDA(w->jpos.reserve((size_t)n * b->R + 1));
+    GBR_CUDA(w->epos.reserve((size_t)n * b->R + 1));
+    GBR_CUDA(w->scan_tmp.reserve(((size_t)n * b->R + 1023) / 1024 + 2));
+    GBR_CUDA(w->jobs.reserve((size_t)n * b->R));
+    GBR_CUDA(w->need_r.reserve(b->R));
+    GBR_CUDA(w->shell.reserve((size_t)n * b->nshell));
+    GBR_CUDA(w->pacc.reserve((size_t)n * 8));
+    GBR_CUDA(w->hist.zero());
+    std::vector<long long> seg(n + 1);
+    for (int p = 0; p <= n; ++p) seg[p] = (long long)p * b->R * b->T;
+    GBR_CUDA(w->seg_c.upload(seg.data(), seg.size()));
+    w->cap = n;
+    return GBR_OK;
+}
+
+int threshold_search(gbr_worker *w, int n, float *vals, const long long *seg, long long max_len, int coarse) {
+    gbr_bundle *b = w->b;
+    w->launches += 5;
+    GBR_CUDA(launch_select(n, 0, b->d.adaptive_fraction, coarse, w->ps.p, w->hist.p, w->st));
+    GBR_CUDA(launch_hist_refine(vals, seg, n, max_len, 1, w->ps.p, w->hist.p, w->st));
+    GBR_CUDA(launch_select(n, 1, b->d.adaptive_fraction, coarse, w->ps.p, w->hist.p, w->st));
+    GBR_CUDA(launch_hist_refine(vals, seg, n, max_len, 2, w->ps.p, w->hist.p, w->st));
+    GBR_CUDA(launch_select(n, 2, b->d.adaptive_fraction, coarse, w->ps.p, w->hist.p, w->st));
+    return GBR_OK;
+}
+
+// One sub-batch of n <= cap particles whose inputs are already in w->X etc.
+int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h, gbr_particle_result *res) {
+    gbr_bundle *b = w->b;
+    const gbr_model_desc &d = b->d;
+    cudaStream_t st = w->st;
+    const int R = (int)b->R, T = (int)b->T, nOR = (int)b->nOR, nOT = (int)b->nOT;
+    const int W = (T + 31) / 32;
+    const long long RT = (long long)R * T;
+    GBR_CUDA(cudaEventRecord(w->ev[0], st));
+    // ---- prep ----
+    GBR_CUDA(launch_prep(w->X.p, w->C.p, w->pdat.p, n, b->full_npix, b->pc.p, b->nc, b->minv_c.p, b->ldk_c,
+                         b->pf.p, b->nf, b->minv_f.p, w->a_c.p, w->b_c.p, w->a_f.p, w->b_f.p, w->Xf.p,
+                         w->Xnf.p, w->Cf.p, w->Xn.p, (int)d.do_scale_correction, w->ps.p, st));
+    GBR_CUDA(launch_pdf_offset(w->pdat.p, n, b->tx.p, b->ty.p, T, d.sigma2_offset, d.pixel_size, w->pdf_off.p, st));
+    GBR_CUDA(cudaMemsetAsync(w->shell.p, 0, sizeof(double) * n * b->nshell, st));
+    GBR_CUDA(cudaMemsetAsync(w->pacc.p, 0, sizeof(double) * n * 8, st));
+    GBR_CUDA(cudaEventRecord(w->ev[1], st));
+    // ---- coarse norm and cross GEMMs ----
+    GBR_CUDA(launch_gemm_norm(b->proj2_c.p, b->ldk_c, R, b->ldk_c, w->a_c.p, b->ldk_c, n, w->nrm.p, st));
+    GBR_CUDA(cudaEventRecord(w->ev[2], st));
+    CrossEpilogue ep{w->vals.p, w->nrm.p, b->pdf_orient.p, w->ps.p, T, RT};
+    GBR_CUDA(launch_gemm_cross(b->proj_c.p, b->lda_c, R, 2 * b->nc, w->b_c.p, b->ldk_c, b->phase_c.p, b->ldk_c,
+                               n, T, ep, st));
+    GBR_CUDA(cudaEventRecord(w->ev[3], st));
+    if (w->debug) {
+        w->dbg_coarse.resize((size_t)n * RT);
+        GBR_CUDA(cudaMemcpyAsync(w->dbg_coarse.data(), w->vals.p, sizeof(float) * n * RT, cudaMemcpyDeviceToHost, st));
+    }
+    // ---- coarse weights and significance ----
+    GBR_CUDA(launch_weights(w->vals.p, w->seg_c.p, n, RT, 1, T, nullptr, nullptr, nullptr, nOR, nOT,
+                            b->pdf_orient.p, w->pdf_off.p, w->ps.p, w->hist.p, st));
+    {
+        int s = threshold_search(w, n, w->vals.p, w->seg_c.p, RT, 1);
+        if (s) return s;
+    }
+    GBR_CUDA(cudaEventRecord(w->ev[4], st));
+    if (w->debug) {
+        w->dbg_wcoarse.resize((size_t)n * RT);
+        GBR_CUDA(cudaMemcpyAsync(w->dbg_wcoarse.data(), w->vals.p, sizeof(float) * n * RT, cudaMemcpyDeviceToHost, st));
+    }
+    GBR_CUDA(launch_sig_masks(w->vals.p, n, R, T, W, w->ps.p, w->mask.p, w->cnt.p, st));
+    const long long nR = (long long)n * R;
+    GBR_CUDA(launch_flag_counts(w->cnt.p, nR, w->flags.p, w->entries.p, nOR * nOT, st));
+    GBR_CUDA(launch_scan_i64(w->flags.p, w->jpos.p, nR, w->scan_tmp.p, st));
+    GBR_CUDA(launch_scan_i64(w->entries.p, w->epos.p, nR, w->scan_tmp.p, st));
+    GBR_CUDA(cudaMemsetAsync(w->need_r.p, 0, R, st));
+    GBR_CUDA(launch_build_jobs(w->cnt.p, n, R, w->jpos.p, w->epos.p, w->jobs.p, w->seg_f.p, w->need_r.p, st));
+    long long njobs = 0, nfine = 0;
+    GBR_CUDA(cudaMemcpyAsync(&njobs, w->jpos.p + nR, sizeof(long long), cudaMemcpyDeviceToHost, st));
+    GBR_CUDA(cudaMemcpyAsync(&nfine, w->epos.p + nR, sizeof(long long), cudaMemcpyDeviceToHost, st));
+    std::vector<unsigned char> need(R);
+    GBR_CUDA(cudaMemcpyAsync(need.data(), w->need_r.p, R, cudaMemcpyDeviceToHost, st));
+    std::vector<long long> segf(n + 1);
+    GBR_CUDA(cudaMemcpyAsync(segf.data(), w->seg_f.p, sizeof(long long) * (n + 1), cudaMemcpyDeviceToHost, st));
+    GBR_CUDA(cudaStreamSynchronize(st));
+    if (njobs <= 0 || nfine <= 0) return fail(GBR_ERR_NUMERICAL, "no significant coarse samples");
+    const long long fine_cap = std::min<long long>(0x7fffffffLL, b->budget ? (long long)b->budget / 24 : (2LL << 30));
+    if (nfine > fine_cap)
+        return fail(GBR_ERR_OOM, "fine pass needs " + std::to_string(nfine) + " poses in this batch (cap " +
+                                     std::to_string(fine_cap) + "); use smaller batches");
+    long long max_seg = 0;
+    for (int p = 0; p < n; ++p) max_seg = std::max(max_seg, segf[p + 1] - segf[p]);
+    GBR_CUDA(w->fd.reserve(nfine));
+    GBR_CUDA(w->ejob.reserve(nfine));
+    GBR_CUDA(w->ecode.reserve(nfine));
+    // ---- fine projections not yet in the cache ----
+    std::vector<int> ids;
+    for (int r = 0; r < R; ++r)
+        if (need[r] && !b->proj_f_done[r]) {
+            for (int io = 0; io < nOR; ++io) ids.push_back(r * nOR + io);
+            b->proj_f_done[r] = 1;
+        }
+    if (!ids.empty()) {
+        GBR_CUDA(w->proj_ids.reserve(ids.size()));
+        GBR_CUDA(cudaMemcpyAsync(w->proj_ids.p, ids.data(), sizeof(int) * ids.size(), cudaMemcpyHostToDevice, st));
+        GBR_CUDA(launch_project_rows(b->vols_d.p, b->pg, b->eul_f.p, b->cls_f.p, w->proj_ids.p, (int)ids.size(),
+                                     b->pf.p, b->nf, nullptr, 0, nullptr, 0, b->proj_f.p, st));
+    }
+    GBR_CUDA(cudaEventRecord(w->ev[5], st));
+    // ---- fine diff2 ----
+    GBR_CUDA(launch_fine_diff2(w->jobs.p, njobs, w->mask.p, R, T, W, nOR, nOT, b->proj_f.p, w->b_f.p, w->a_f.p,
+                               b->nf, b->phase_f.p, w->fd.p, w->ejob.p, w->ecode.p, w->ps.p, st));
+    GBR_CUDA(cudaEventRecord(w->ev[6], st));
+    if (w->debug) {
+        w->dbg_fine.resize(nfine);
+        w->dbg_ejob.resize(nfine);
+        w->dbg_ecode.resize(nfine);
+        w->dbg_jobs.resize(njobs);
+        GBR_CUDA(cudaMemcpyAsync(w->dbg_fine.data(), w->fd.p, sizeof(float) * nfine, cudaMemcpyDeviceToHost, st));
+        GBR_CUDA(cudaMemcpyAsync(w->dbg_ejob.data(), w->ejob.p, sizeof(int) * nfine, cudaMemcpyDeviceToHost, st));
+        GBR_CUDA(cudaMemcpyAsync(w->dbg_ecode.data(), w->ecode.p, sizeof(unsigned) * nfine, cudaMemcpyDeviceToHost, st));
+        GBR_CUDA(cudaMemcpyAsync(w->dbg_jobs.data(), w->jobs.p, sizeof(FineJob) * njobs, cudaMemcpyDeviceToHost, st));
+        w->dbg_segf = segf;
+    }
+    // ---- fine weights and significance ----
+    GBR_CUDA(launch_weights(w->fd.p, w->seg_f.p, n, max_seg, 0, T, w->ejob.p, w->ecode.p, w->jobs.p, nOR, nOT,
+                            b->pdf_orient.p, w->pdf_off.p, w->ps.p, w->hist.p, st));
+    {
+        int s = threshold_search(w, n, w->fd.p, w->seg_f.p, max_seg, 0);
+        if (s) return s;
+    }
+    GBR_CUDA(cudaEventRecord(w->ev[7], st));
+    if (w->debug) {
+        w->dbg_wfine.resize(nfine);
+        GBR_CUDA(cudaMemcpyAsync(w->dbg_wfine.data(), w->fd.p, sizeof(float) * nfine, cudaMemcpyDeviceToHost, st));
+    }
+    // ---- weighted sums ----
+    WsumArgs wa{};
+    wa.jobs = w->jobs.p;
+    wa.njobs = njobs;
+    wa.mask = w->mask.p;
+    wa.R = R; wa.T = T; wa.W = W; wa.nOR = nOR; wa.nOT = nOT; wa.nf = b->nf; wa.nshell = b->nshell;
+    wa.ndir = (int)b->ND; wa.npsi = (int)b->NP; wa.K = (int)b->K;
+    wa.w = w->fd.p;
+    wa.ps = w->ps.p;
+    wa.projf = b->proj_f.p;
+    wa.Xf = w->Xf.p; wa.Xnf = w->Xnf.p; wa.Cf = w->Cf.p;
+    wa.minv_store = b->minv_store.p;
+    wa.pf = b->pf.p;
+    wa.phase_f = b->phase_f.p;
+    wa.otx = b->otx.p; wa.oty = b->oty.p;
+    wa.pdat = w->pdat.p;
+    wa.pixel = d.pixel_size;
+    wa.do_scale = (int)d.do_scale_correction;
+    wa.dvp_mask = b->dvp_mask.p;
+    wa.bpimg = b->bpimg.p; wa.bpw = b->bpw.p; wa.active = b->active.p;
+    wa.shell = w->shell.p; wa.pacc = w->pacc.p;
+    wa.pdf_dir = b->w_pdf_dir.p; wa.pdf_cls = b->w_pdf_cls.p;
+    GBR_CUDA(launch_wsum(wa, st));
+    GBR_CUDA(cudaEventRecord(w->ev[8], st));
+    // ---- backprojection of the touched slices ----
+    GBR_CUDA(w->act_list.reserve(b->RF));
+    GBR_CUDA(w->act_count.reserve(1));
+    GBR_CUDA(cudaMemsetAsync(w->act_count.p, 0, sizeof(int), st));
+    GBR_CUDA(launch_compact_flags(b->active.p, (int)b->RF, w->act_list.p, w->act_count.p, st));
+    int nact = 0;
+    GBR_CUDA(cudaMemcpyAsync(&nact, w->act_count.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    GBR_CUDA(cudaStreamSynchronize(st));
+    GBR_CUDA(launch_backproject(w->act_list.p, nact, b->eul_f.p, nOR, b->cls_of_r.p, b->bpimg.p, b->bpw.p, b->pf.p,
+                                b->nf, b->cur / 2 + 1, b->bg, b->bpd_ptrs.p, b->bpw_ptrs.p, b->active.p, st));
+    GBR_CUDA(cudaEventRecord(w->ev[9], st));
+    w->launches += 18 + (long long)((ids.size() + 65534) / 65535) + (nact > 0 ? 1 : 0);
+    // ---- results ----
+    std::vector<ParticleState> psh(n);
+    std::vector<double> shell((size_t)n * b->nshell), pacc((size_t)n * 8);
+    GBR_CUDA(cudaMemcpyAsync(psh.data(), w->ps.p, sizeof(ParticleState) * n, cudaMemcpyDeviceToHost, st));
+    GBR_CUDA(cudaMemcpyAsync(shell.data(), w->shell.p, sizeof(double) * shell.size(), cudaMemcpyDeviceToHost, st));
+    GBR_CUDA(cudaMemcpyAsync(pacc.data(), w->pacc.p, sizeof(double) * pacc.size(), cudaMemcpyDeviceToHost, st));
+    GBR_CUDA(cudaEventRecord(w->ev[10], st));
+    GBR_CUDA(cudaStreamSynchronize(st));
+    for (int s = 0; s < ST_N; ++s) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, w->ev[s], w->ev[s + 1]);
+        w->stage_ms[s] += ms;
+    }
+    if (w->debug) {
+        w->dbg_n = n;
+        w->dbg_cc.resize(n);
+        w->dbg_cf.resize(n);
+        for (int p = 0; p < n; ++p) {
+            w->dbg_cc[p] = psh[p].c_coarse;
+            w->dbg_cf[p] = psh[p].c_fine;
+        }
+    }
+    // ---- per-particle finalisation (storeWeightedSums :8990-9150) ----
+    std::vector<double> fr(nOR), ft(nOR), fp(nOR);
+    for (int p = 0; p < n; ++p) {
+        const ParticleState &s = psh[p];
+        gbr_particle_result &o = res[p];
+        std::memset(&o, 0, sizeof(o));
+        if (!(s.sum_fine > 0.) || !std::isfinite(s.sum_fine))
+            return fail(GBR_ERR_NUMERICAL, "zero sum of weights for particle " + std::to_string(p));
+        const double *pd = pdat_h + (size_t)p * 8;
+        o.coarse_min_diff2 = s.c_coarse + (double)ord2f_host(s.min_coarse);
+        o.coarse_sum_weight = s.sum_coarse;
+        o.coarse_significant_weight = s.thr_coarse;
+        o.fine_min_diff2 = s.c_fine + (double)ord2f_host(s.min_fine);
+        o.fine_sum_weight = s.sum_fine;
+        o.fine_significant_weight = s.thr_fine;
+        o.nr_sign = s.nr_sign;
+        o.n_fine = segf[p + 1] - segf[p];
+        const unsigned long long key = s.argmax_key;
+        const unsigned long long idx = 0xFFFFFFFFull - (key & 0xFFFFFFFFull);
+        unsigned int wb = (unsigned int)(key >> 32);
+        float wmax;
+        std::memcpy(&wmax, &wb, 4);
+        const long iot = (long)(idx % nOT), t = (long)((idx / nOT) % T);
+        const long ior = (long)((idx / ((unsigned long long)nOT * T)) % nOR);
+        const long r = (long)(idx / ((unsigned long long)nOT * T * nOR));
+        const long ic = r / (b->ND * b->NP), id = (r / b->NP) % b->ND, is = r % b->NP;
+        b->grid.fine_orientations(id, is, fr.data(), ft.data(), fp.data());
+        o.rot = fr[ior];
+        o.tilt = ft[ior];
+        o.psi = fp[ior];
+        o.xoff = pd[0] + b->otx_h[t * nOT + iot];
+        o.yoff = pd[1] + b->oty_h[t * nOT + iot];
+        o.cls = (double)ic + 1;
+        o.pmax = (double)wmax / s.sum_fine;
+        o.best_ihidden_over = ((r * T + t) * nOR + ior) * nOT + iot;
+        o.dLL = std::log(s.sum_fine) - o.fine_min_diff2 - b->logsigma2;
+        // sigma2 noise shells + power beyond the current size
+        double wnorm = 0.;
+        const double *sp = &shell[(size_t)p * b->nshell];
+        for (int i = 0; i < b->nshell; ++i) {
+            b->w_sigma2[i] += sp[i];
+            wnorm += sp[i];
+        }
+        for (int i = b->cur / 2 + 1; i < b->nshell; ++i) {
+            b->w_sigma2[i] += power_h[(size_t)p * b->nshell + i];
+            wnorm += power_h[(size_t)p * b->nshell + i];
+        }
+        o.norm = pd[5];
+        if (d.do_norm_correction) {
+            o.norm = pd[5] / d.avg_norm_correction * std::sqrt(wnorm * 2.);
+            b->w_avg_norm += o.norm;
+        }
+        if (d.do_scale_correction) {
+            b->w_XA += pacc[(size_t)p * 8 + 2] / pd[6];
+            b->w_AA += pacc[(size_t)p * 8 + 3] / (pd[6] * pd[6]);
+        }
+        b->w_sumw_group += pacc[(size_t)p * 8 + 0];
+        b->w_sigma2_offset += pacc[(size_t)p * 8 + 1];
+        b->w_LL += o.dLL;
+        b->w_ave_Pmax += o.pmax;
+    }
+    return GBR_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+size_t gbr_last_error(char *buf, size_t len) {
+    if (buf && len) {
+        std::strncpy(buf, g_last_error.c_str(), len - 1);
+        buf[len - 1] = 0;
+    }
+    return g_last_error.size();
+}
+
+const char *gbr_version(void) { return "libgbrelion 0.1 (sm_103a)"; }
+
+int gbr_bundle_create(const gbr_model_desc *desc, int device, gbr_bundle **out) {
+    if (!desc || !out) return fail(GBR_ERR_INVALID, "null argument");
+    const gbr_model_desc &d = *desc;
+    if (d.ori_size <= 0 || d.nr_classes <= 0 || d.current_size <= 0 || d.coarse_size <= 0 ||
+        d.coarse_size > d.current_size || d.current_size > d.ori_size || d.current_size % 2 ||
+        d.coarse_size % 2 || d.padding_factor <= 0 || d.pixel_size <= 0 || d.offset_step <= 0 ||
+        d.offset_range < 0 || d.sigma2_len <= 0 || d.healpix_order < 0 || d.healpix_order > 8)
+        return fail(GBR_ERR_INVALID, "invalid model description");
+    if (d.adaptive_oversampling != 1)
+        return fail(GBR_ERR_UNSUPPORTED, "only --oversampling 1 is implemented");
+    if (d.maximum_significants > 0)
+        return fail(GBR_ERR_UNSUPPORTED, "--maxsig is not implemented");
+    if (d.precision != GBR_PREC_FP32)
+        return fail(GBR_ERR_UNSUPPORTED, "only the FP32 path is implemented");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev)
+        return fail(GBR_ERR_CUDA, "no CUDA device " + std::to_string(device));
+    GBR_CUDA(cudaSetDevice(device));
+    std::unique_ptr<gbr_bundle> b(new gbr_bundle());
+    b->d = d;
+    b->device = device;
+    b->grid.build((int)d.healpix_order, d.psi_step, d.offset_range, d.offset_step, (int)d.adaptive_oversampling);
+    b->K = d.nr_classes;
+    b->ND = b->grid.ndir();
+    b->NP = b->grid.npsi();
+    b->T = b->grid.ntrans();
+    b->R = b->K * b->ND * b->NP;
+    b->nOR = b->grid.nover_rot();
+    b->nOT = b->grid.nover_trans();
+    b->RF = b->R * b->nOR;
+    b->TF = b->T * b->nOT;
+    if (b->R > 0x7fffffffL / 8) return fail(GBR_ERR_INVALID, "sampling too large");
+    b->nshell = (int)(d.ori_size / 2 + 1);
+    b->cur = (int)d.current_size;
+    b->crs = (int)d.coarse_size;
+    b->full_npix = b->cur * (b->cur / 2 + 1);
+    b->vol.resize(b->K);
+    b->have_vol.assign(b->K, 0);
+    // backprojector volumes (BackProjector::initZeros(current_size))
+    const int r_max = (int)std::min<int64_t>(d.current_size / 2, d.ori_size / 2);
+    const int pad_size = 2 * (iround((double)d.padding_factor * r_max) + 1) + 1;
+    b->bg = VolGeom{pad_size / 2 + 1, pad_size, pad_size, -(pad_size / 2), -(pad_size / 2), r_max,
+                    (int)d.padding_factor};
+    b->bp_vox = (size_t)b->bg.xdim * b->bg.ydim * b->bg.zdim;
+    b->bp_data.resize(b->K);
+    b->bp_weight.resize(b->K);
+    std::vector<double2 *> dp(b->K);
+    std::vector<double *> wp(b->K);
+    for (long k = 0; k < b->K; ++k) {
+        GBR_CUDA(b->bp_data[k].reserve(b->bp_vox));
+        GBR_CUDA(b->bp_weight[k].reserve(b->bp_vox));
+        GBR_CUDA(b->bp_data[k].zero());
+        GBR_CUDA(b->bp_weight[k].zero());
+        dp[k] = b->bp_data[k].p;
+        wp[k] = b->bp_weight[k].p;
+    }
+    GBR_CUDA(b->bpd_ptrs.upload(dp.data(), dp.size()));
+    GBR_CUDA(b->bpw_ptrs.upload(wp.data(), wp.size()));
+    GBR_CUDA(b->w_pdf_cls.reserve(b->K));
+    GBR_CUDA(b->w_pdf_dir.reserve((size_t)b->K * b->ND));
+    GBR_CUDA(b->w_pdf_cls.zero());
+    GBR_CUDA(b->w_pdf_dir.zero());
+    b->w_sigma2.assign(b->nshell, 0.);
+    GBR_CUDA(cudaDeviceSynchronize());
+    *out = b.release();
+    return GBR_OK;
+}
+
+int gbr_projector_upload(gbr_bundle *b, int64_t iclass, const float *data, int64_t xdim, int64_t ydim,
+                         int64_t zdim, int64_t yinit, int64_t zinit, int64_t r_max, int64_t padding_factor) {
+    if (!b || !data || iclass < 0 || iclass >= b->K) return fail(GBR_ERR_INVALID, "bad class or data");
+    if (xdim <= 1 || ydim <= 1 || zdim <= 1 || padding_factor != b->d.padding_factor)
+        return fail(GBR_ERR_INVALID, "bad projector dimensions");
+    if (-yinit + 1 > ydim || -zinit + 1 > zdim || r_max * padding_factor + 1 >= xdim)
+        return fail(GBR_ERR_INVALID, "projector origin / r_max outside the volume");
+    VolGeom g{(int)xdim, (int)ydim, (int)zdim, (int)yinit, (int)zinit, (int)r_max, (int)padding_factor};
+    bool any = false;
+    for (long k = 0; k < b->K; ++k) any |= (k != iclass && b->have_vol[k] != 0);
+    if (any && std::memcmp(&g, &b->pg, sizeof(g)) != 0)
+        return fail(GBR_ERR_INVALID, "all classes must share one projector geometry");
+    GBR_CUDA(cudaSetDevice(b->device));
+    b->pg = g;
+    GBR_CUDA(b->vol[iclass].upload(reinterpret_cast<const float2 *>(data), (size_t)xdim * ydim * zdim));
+    b->have_vol[iclass] = 1;
+    b->tables_ready = false;
+    return GBR_OK;
+}
+
+int gbr_model_set_arrays(gbr_bundle *b, const double *sigma2_noise, const double *pdf_class,
+                         const double *pdf_direction, const double *data_vs_prior) {
+    if (!b || !sigma2_noise || !pdf_class || !pdf_direction) return fail(GBR_ERR_INVALID, "null array");
+    if (b->d.do_scale_correction && !data_vs_prior)
+        return fail(GBR_ERR_INVALID, "data_vs_prior needed with scale correction");
+    b->sigma2.assign(sigma2_noise, sigma2_noise + b->d.sigma2_len);
+    b->pdf_class.assign(pdf_class, pdf_class + b->K);
+    b->pdf_dir.assign(pdf_direction, pdf_direction + b->K * b->ND);
+    if (data_vs_prior) b->dvp.assign(data_vs_prior, data_vs_prior + b->K * b->nshell);
+    b->have_arrays = true;
+    b->tables_ready = false;
+    return GBR_OK;
+}
+
+int gbr_bundle_reserve(gbr_bundle *b, size_t bytes) {
+    if (!b) return fail(GBR_ERR_INVALID, "null bundle");
+    b->budget = bytes;
+    return GBR_OK;
+}
+
+int gbr_worker_create(gbr_bundle *b, gbr_worker **out) {
+    if (!b || !out) return fail(GBR_ERR_INVALID, "null argument");
+    GBR_CUDA(cudaSetDevice(b->device));
+    std::unique_ptr<gbr_worker> w(new gbr_worker());
+    w->b = b;
+    GBR_CUDA(cudaStreamCreateWithFlags(&w->st, cudaStreamNonBlocking));
+    for (int i = 0; i <= ST_N; ++i) GBR_CUDA(cudaEventCreate(&w->ev[i]));
+    const char *dbg = std::getenv("GBR_DEBUG_FETCH");
+    w->debug = dbg && dbg[0] == '1';
+    *out = w.release();
+    return GBR_OK;
+}
+
+int gbr_worker_set_debug(gbr_worker *w, int on) {
+    if (!w) return fail(GBR_ERR_INVALID, "null worker");
+    w->debug = on ? 1 : 0;
+    return GBR_OK;
+}
+
+int gbr_expect_batch(gbr_worker *w, const gbr_particle_batch *batch, gbr_particle_result *res) {
+    if (!w || !batch || !res || batch->n < 0) return fail(GBR_ERR_INVALID, "null argument");
+    if (batch->n == 0) return GBR_OK;
+    if (!batch->fimg || !batch->fimg_nomask || !batch->fctf || !batch->power_img || !batch->old_offset ||
+        !batch->prior || !batch->highres_Xi2 || !batch->norm_correction || !batch->scale)
+        return fail(GBR_ERR_INVALID, "null particle array");
+    gbr_bundle *b = w->b;
+    GBR_CUDA(cudaSetDevice(b->device));
+    int s = build_tables(b);
+    if (s) return s;
+    const long long per_part = (long long)b->R * b->T * 4;
+    const long long mem_cap = b->budget ? (long long)b->budget / 4 : (4LL << 30);
+    int cap = (int)std::max<long long>(1, std::min<long long>(1024, mem_cap / std::max<long long>(per_part, 1)));
+    const int n_all = (int)batch->n;
+    if (w->debug) cap = n_all;  // debug read-back covers the whole call
+    s = ensure_capacity(w, std::min(cap, n_all));
+    if (s) return s;
+    const size_t full = (size_t)b->full_npix;
+    const cudaMemcpyKind kind = batch->device_resident ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    std::vector<double> pdat, power;
+    for (int p0 = 0; p0 < n_all; p0 += w->cap) {
+        const int n = std::min(w->cap, n_all - p0);
+        GBR_CUDA(cudaMemcpyAsync(w->X.p, batch->fimg + 2 * full * p0, sizeof(float2) * full * n, kind, w->st));
+        GBR_CUDA(cudaMemcpyAsync(w->Xn.p, batch->fimg_nomask + 2 * full * p0, sizeof(float2) * full * n, kind, w->st));
+        GBR_CUDA(cudaMemcpyAsync(w->C.p, batch->fctf + full * p0, sizeof(float) * full * n, kind, w->st));
+        pdat.assign((size_t)n * 8, 0.);
+        power.assign((size_t)n * b->nshell, 0.);
+        if (batch->device_resident) {
+            std::vector<double> tmp((size_t)n * 2);
+            GBR_CUDA(cudaMemcpy(tmp.data(), batch->old_offset + 2 * p0, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost));
+            for (int p = 0; p < n; ++p) { pdat[p * 8 + 0] = tmp[2 * p]; pdat[p * 8 + 1] = tmp[2 * p + 1]; }
+            GBR_CUDA(cudaMemcpy(tmp.data(), batch->prior + 2 * p0, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost));
+            for (int p = 0; p < n; ++p) { pdat[p * 8 + 2] = tmp[2 * p]; pdat[p * 8 + 3] = tmp[2 * p + 1]; }
+            GBR_CUDA(cudaMemcpy(tmp.data(), batch->highres_Xi2 + p0, sizeof(double) * n, cudaMemcpyDeviceToHost));
+            for (int p = 0; p < n; ++p) pdat[p * 8 + 4] = tmp[p];
+            GBR_CUDA(cudaMemcpy(tmp.data(), batch->norm_correction + p0, sizeof(double) * n, cudaMemcpyDeviceToHost));
+            for (int p = 0; p < n; ++p) pdat[p * 8 + 5] = tmp[p];
+            GBR_CUDA(cudaMemcpy(tmp.data(), batch->scale + p0, sizeof(double) * n, cudaMemcpyDeviceToHost));
+            for (int p = 0; p < n; ++p) pdat[p * 8 + 6] = tmp[p];
+            GBR_CUDA(cudaMemcpy(power.data(), batch->power_img + (size_t)b->nshell * p0,
+                                sizeof(double) * b->nshell * n, cudaMemcpyDeviceToHost));
+        } else {
+            for (int p = 0; p < n; ++p) {
+                const int q = p0 + p;
+                pdat[p * 8 + 0] = batch->old_offset[2 * q];
+                pdat[p * 8 + 1] = batch->old_offset[2 * q + 1];
+                pdat[p * 8 + 2] = batch->prior[2 * q];
+                pdat[p * 8 + 3] = batch->prior[2 * q + 1];
+                pdat[p * 8 + 4] = batch->highres_Xi2[q];
+                pdat[p * 8 + 5] = batch->norm_correction[q];
+                pdat[p * 8 + 6] = batch->scale[q];
+            }
+            std::memcpy(power.data(), batch->power_img + (size_t)b->nshell * p0, sizeof(double) * b->nshell * n);
+        }
+        GBR_CUDA(cudaMemcpyAsync(w->pdat.p, pdat.data(), sizeof(double) * pdat.size(), cudaMemcpyHostToDevice, w->st));
+        s = run_batch(w, n, power.data(), pdat.data(), res + p0);
+        if (s) return s;
+    }
+    return GBR_OK;
+}
+
+int gbr_sampling_sizes(const gbr_bundle *b, int64_t *ndir, int64_t *npsi, int64_t *ntrans, int64_t *nover_rot,
+                       int64_t *nover_trans) {
+    if (!b) return fail(GBR_ERR_INVALID, "null bundle");
+    if (ndir) *ndir = b->ND;
+    if (npsi) *npsi = b->NP;
+    if (ntrans) *ntrans = b->T;
+    if (nover_rot) *nover_rot = b->nOR;
+    if (nover_trans) *nover_trans = b->nOT;
+    return GBR_OK;
+}
+
+int64_t gbr_worker_debug_fetch(gbr_worker *w, int what, int64_t i, void *host, int64_t capacity) {
+    if (!w || !host) return fail(GBR_ERR_INVALID, "null argument");
+    if (!w->debug) return fail(GBR_ERR_STATE, "debug read-back needs GBR_DEBUG_FETCH=1 at worker creation");
+    if (i < 0 || i >= w->dbg_n) return fail(GBR_ERR_INVALID, "particle index out of range");
+    gbr_bundle *b = w->b;
+    const long long RT = (long long)b->R * b->T;
+    if (what == 0 || what == 1) {
+        if (capacity < RT) return fail(GBR_ERR_INVALID, "capacity too small");
+        double *o = static_cast<double *>(host);
+        const float *src = (what == 0 ? w->dbg_coarse.data() : w->dbg_wcoarse.data()) + (size_t)i * RT;
+        for (long long e = 0; e < RT; ++e)
+            o[e] = (what == 0) ? (std::isfinite(src[e]) ? w->dbg_cc[i] + (double)src[e] : INFINITY) : (double)src[e];
+        return RT;
+    }
+    const long long b0 = w->dbg_segf[i], b1 = w->dbg_segf[i + 1];
+    if (capacity < b1 - b0) return fail(GBR_ERR_INVALID, "capacity too small");
+    const int nOR = (int)b->nOR, nOT = (int)b->nOT, T = (int)b->T;
+    for (long long e = b0; e < b1; ++e) {
+        const long long k = e - b0;
+        if (what == 2) {
+            const FineJob &j = w->dbg_jobs[w->dbg_ejob[e]];
+            const unsigned code = w->dbg_ecode[e];
+            const long long t = code / (nOR * nOT), ior = (code / nOT) % nOR, iot = code % nOT;
+            static_cast<int64_t *>(host)[k] = (((long long)j.r * T + t) * nOR + ior) * nOT + iot;
+        } else if (what == 3) {
+            static_cast<double *>(host)[k] = w->dbg_cf[i] + (double)w->dbg_fine[e];
+        } else if (what == 4) {
+            static_cast<double *>(host)[k] = (double)w->dbg_wfine[e];
+        } else {
+            return fail(GBR_ERR_INVALID, "unknown debug selector");
+        }
+    }
+    return b1 - b0;
+}
+
+int gbr_backprojector_dims(const gbr_bundle *b, int64_t *xdim, int64_t *ydim, int64_t *zdim, int64_t *yinit,
+                           int64_t *zinit, int64_t *r_max) {
+    if (!b) return fail(GBR_ERR_INVALID, "null bundle");
+    if (xdim) *xdim = b->bg.xdim;
+    if (ydim) *ydim = b->bg.ydim;
+    if (zdim) *zdim = b->bg.zdim;
+    if (yinit) *yinit = b->bg.yinit;
+    if (zinit) *zinit = b->bg.zinit;
+    if (r_max) *r_max = b->bg.r_max;
+    return GBR_OK;
+}
+
+int gbr_backprojector_download(gbr_bundle *b, int64_t iclass, double *data, double *weight) {
+    if (!b || iclass < 0 || iclass >= b->K) return fail(GBR_ERR_INVALID, "bad class");
+    GBR_CUDA(cudaSetDevice(b->device));
+    GBR_CUDA(cudaDeviceSynchronize());
+    if (data) GBR_CUDA(cudaMemcpy(data, b->bp_data[iclass].p, sizeof(double2) * b->bp_vox, cudaMemcpyDeviceToHost));
+    if (weight) GBR_CUDA(cudaMemcpy(weight, b->bp_weight[iclass].p, sizeof(double) * b->bp_vox, cudaMemcpyDeviceToHost));
+    return GBR_OK;
+}
+
+int gbr_wsum_download(gbr_bundle *b, gbr_wsum *out) {
+    if (!b || !out) return fail(GBR_ERR_INVALID, "null argument");
+    GBR_CUDA(cudaSetDevice(b->device));
+    GBR_CUDA(cudaDeviceSynchronize());
+    if (out->sigma2_noise)
+        for (int i = 0; i < b->nshell; ++i) out->sigma2_noise[i] += b->w_sigma2[i];
+    if (out->pdf_class) {
+        std::vector<double> v(b->K);
+        GBR_CUDA(cudaMemcpy(v.data(), b->w_pdf_cls.p, sizeof(double) * b->K, cudaMemcpyDeviceToHost));
+        for (long k = 0; k < b->K; ++k) out->pdf_class[k] += v[k];
+    }
+    if (out->pdf_direction) {
+        std::vector<double> v((size_t)b->K * b->ND);
+        GBR_CUDA(cudaMemcpy(v.data(), b->w_pdf_dir.p, sizeof(double) * v.size(), cudaMemcpyDeviceToHost));
+        for (size_t k = 0; k < v.size(); ++k) out->pdf_direction[k] += v[k];
+    }
+    out->sigma2_offset += b->w_sigma2_offset;
+    out->sumw_group += b->w_sumw_group;
+    out->LL += b->w_LL;
+    out->ave_Pmax += b->w_ave_Pmax;
+    out->avg_norm_correction += b->w_avg_norm;
+    out->wsum_signal_product += b->w_XA;
+    out->wsum_reference_power += b->w_AA;
+    return GBR_OK;
+}
+
+int gbr_bundle_reset_wsum(gbr_bundle *b) {
+    if (!b) return fail(GBR_ERR_INVALID, "null bundle");
+    GBR_CUDA(cudaSetDevice(b->device));
+    for (long k = 0; k < b->K; ++k) {
+        GBR_CUDA(b->bp_data[k].zero());
+        GBR_CUDA(b->bp_weight[k].zero());
+    }
+    GBR_CUDA(b->w_pdf_cls.zero());
+    GBR_CUDA(b->w_pdf_dir.zero());
+    std::fill(b->w_sigma2.begin(), b->w_sigma2.end(), 0.);
+    b->w_sigma2_offset = b->w_sumw_group = b->w_LL = b->w_ave_Pmax = b->w_avg_norm = b->w_XA = b->w_AA = 0.;
+    GBR_CUDA(cudaDeviceSynchronize());
+    return GBR_OK;
+}
+
+int gbr_worker_stage_times(const gbr_worker *w, double *ms, int64_t n, int64_t *n_written) {
+    if (!w || !ms) return fail(GBR_ERR_INVALID, "null argument");
+    const int64_t m = std::min<int64_t>(n, ST_N);
+    for (int64_t i = 0; i < m; ++i) ms[i] = w->stage_ms[i];
+    if (n_written) *n_written = m;
+    return GBR_OK;
+}
+
+int gbr_worker_launch_count(const gbr_worker *w, int64_t *count) {
+    if (!w || !count) return fail(GBR_ERR_INVALID, "null argument");
+    *count = w->launches;
+    return GBR_OK;
+}
+
+int gbr_measure_fp32_peak(int device, double *tflops) {
+    if (!tflops) return fail(GBR_ERR_INVALID, "null argument");
+    GBR_CUDA(cudaSetDevice(device));
+    float ms = 0.f;
+    double flops = 0.;
+    GBR_CUDA(gbr::launch_fp32_probe(&ms, &flops));
+    *tflops = flops / (ms * 1e-3) / 1e12;
+    return GBR_OK;
+}
+
+int gbr_worker_destroy(gbr_worker *w) {
+    if (!w) return GBR_OK;
+    cudaSetDevice(w->b->device);
+    if (w->st) cudaStreamSynchronize(w->st);
+    for (int i = 0; i <= ST_N; ++i)
+        if (w->ev[i]) cudaEventDestroy(w->ev[i]);
+    if (w->st) cudaStreamDestroy(w->st);
+    delete w;
+    return GBR_OK;
+}
+
+int gbr_bundle_destroy(gbr_bundle *b) {
+    if (!b) return GBR_OK;
+    cudaSetDevice(b->device);
+    cudaDeviceSynchronize();
+    delete b;
+    return GBR_OK;
+}
+
+}  // extern "C"

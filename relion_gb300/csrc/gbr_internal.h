@@ -1,0 +1,166 @@
+// gbr_internal.h -- internal types and kernel launch declarations of
+// libgbrelion.  Kernels live in k_*.cu; the host driver in estep.cu.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <string>
+
+namespace gbr {
+
+// Error channel: every launch wrapper returns cudaError_t; the driver turns
+// it into a gbr_status plus text (gbr_last_error).
+struct Error {
+    int status;
+    std::string text;
+};
+
+// One active Fourier pixel of a 2D image of size s (FFTW half layout):
+// logical frequency (x, y), its index in the full [s][s/2+1] image, and its
+// resolution shell (Mresol, src/ml_optimiser.cpp:5784-5795).
+struct PixelRef {
+    int x, y;
+    int full;   // index into [s][s/2+1]
+    int shell;  // ROUND(sqrt(x^2+y^2)); -1 if excluded
+};
+
+// Padded Fourier volume geometry (Projector::data, src/projector.cpp:59-90).
+struct VolGeom {
+    int xdim, ydim, zdim, yinit, zinit, r_max, pad;
+};
+
+// Per-particle state on the device (one per particle of the batch).
+struct ParticleState {
+    double c_coarse;     // highres_Xi2/2 + sum_k minv_c |X|^2 (coarse pixels)
+    double c_fine;       // same for the fine pixels
+    double sum_coarse;   // sum of coarse weights
+    double sum_fine;     // sum of fine weights
+    double sel_above;    // threshold search: weight sum above the current bucket
+    double target;       // adaptive_fraction * sum of the pass being searched
+    unsigned long long argmax_key;  // (weight bits << 32) | ~loop-order index
+    unsigned int min_coarse;        // ordered-int encoding of min relative diff2
+    unsigned int min_fine;
+    unsigned int sel_prefix;        // threshold search: selected bit prefix
+    unsigned int sel_count_above;   // elements strictly above the bucket
+    float thr_coarse;               // significant weight of the coarse pass
+    float thr_fine;                 // significant weight of the fine pass
+    unsigned int nr_sign;           // significant count (coarse pass)
+    unsigned int pad_;
+};
+
+// Fine-pass job: one (particle, significant coarse orientation).
+struct FineJob {
+    int p;          // particle in batch
+    int r;          // coarse orientation (iclass*ndir + idir)*npsi + ipsi
+    int n_t;        // significant coarse translations of this orientation
+    int pad_;
+    long long off;  // first fine entry of this job
+};
+
+// Histogram bin used by the threshold search.
+struct HistBin {
+    double sum;
+    unsigned int count;
+    unsigned int pad_;
+};
+
+constexpr int kHistBins = 4096;
+
+// ---- launch wrappers (all asynchronous on `st`) -------------------------
+// k_project.cu
+cudaError_t launch_phase_table(float2 *out, const double *tx, const double *ty, int ntrans,
+                               const PixelRef *pix, int npix, int ld, double ori_size, cudaStream_t st);
+// Project n orientations (matrices Ainv*pad, row-major float[9]) of class
+// volumes; orientation o uses class cls[o].  Output either interleaved
+// (re,im) rows of `ld` floats (+ |P|^2 rows of `ld2` floats) or float2 rows.
+cudaError_t launch_project_rows(const float2 *const *vols, const VolGeom &g, const float *eul,
+                                const int *cls, const int *orient_ids, int n_orient,
+                                const PixelRef *pix, int npix, float *out_ri, int ld, float *out_p2,
+                                int ld2, float2 *out_c, cudaStream_t st);
+
+// FP32 FMA throughput probe (ms of one timed launch and its flop count).
+cudaError_t launch_fp32_probe(float *ms, double *flops);
+
+// k_gemm.cu: C[m][n] = sum_k A[m][k] * Bop[n][k], FP32 SIMT.
+struct CrossEpilogue {
+    float *diff2;            // [p][M*T] relative diff2 (+inf if skipped)
+    const float *norm;       // [p][M] coarse norm term
+    const float *pdf_orient; // [M] (0 = skip)
+    ParticleState *ps;       // min tracking (min_coarse)
+    int T;
+    long long MT;            // M*T
+};
+cudaError_t launch_gemm_cross(const float *A, int lda, int M, int K2, const float2 *bimg,
+                              int ldb, const float2 *phase, int ldp, int nparticles, int T,
+                              const CrossEpilogue &ep, cudaStream_t st);
+cudaError_t launch_gemm_norm(const float *A, int lda, int M, int K, const float *a, int lda_b,
+                             int nparticles, float *out /*[p][M]*/, cudaStream_t st);
+
+// k_estep.cu
+cudaError_t launch_prep(const float2 *X, const float *C, const double *pdat, int n, int full_npix,
+                        const PixelRef *pc, int nc, const float *minv_c, int ldk_c,
+                        const PixelRef *pf, int nf, const float *minv_f, float *a_c, float2 *b_c,
+                        float *a_f, float2 *b_f, float2 *Xf, float2 *Xnf, float *Cf,
+                        const float2 *Xn, int do_scale, ParticleState *ps, cudaStream_t st);
+cudaError_t launch_pdf_offset(const double *pdat, int n, const double *tx, const double *ty, int T,
+                              double sigma2_offset, double pixel, float *pdf_off, cudaStream_t st);
+// Weights of per-particle segments [seg[p], seg[p+1]) of `vals` (in place).
+// Coarse: element e of particle p has r = e / T, t = e % T.
+// Fine: element e has job = ejob[e] and code = ecode[e].
+cudaError_t launch_weights(float *vals, const long long *seg, int n, long long max_len, int coarse,
+                           int T, const int *ejob, const unsigned int *ecode, const FineJob *jobs,
+                           int nOR, int nOT, const float *pdf_orient, const float *pdf_off,
+                           ParticleState *ps, HistBin *hist, cudaStream_t st);
+// Threshold search levels 0..2 (12, 12, 7 bits).
+cudaError_t launch_hist_refine(const float *vals, const long long *seg, int n, long long max_len,
+                               int level, ParticleState *ps, HistBin *hist, cudaStream_t st);
+cudaError_t launch_select(int n, int level, double adaptive_fraction, int coarse, ParticleState *ps,
+                          HistBin *hist, cudaStream_t st);
+cudaError_t launch_sig_masks(const float *w, int n, int R, int T, int W, const ParticleState *ps,
+                             unsigned int *mask, int *cnt, cudaStream_t st);
+cudaError_t launch_scan_i64(const long long *in, long long *out, long long n, long long *tmp,
+                            cudaStream_t st);
+cudaError_t launch_flag_counts(const int *cnt, long long n, long long *flags, long long *entries,
+                               int per, cudaStream_t st);
+cudaError_t launch_build_jobs(const int *cnt, int n, int R, const long long *jpos,
+                              const long long *epos, FineJob *jobs, long long *seg,
+                              unsigned char *need_r, cudaStream_t st);
+cudaError_t launch_fine_diff2(const FineJob *jobs, long long njobs, const unsigned int *mask,
+                              int R, int T, int W, int nOR, int nOT, const float2 *projf,
+                              const float2 *b_f, const float *a_f, int nf, const float2 *phase_f,
+                              float *d, int *ejob, unsigned int *ecode, ParticleState *ps,
+                              cudaStream_t st);
+struct WsumArgs {
+    const FineJob *jobs;
+    long long njobs;
+    const unsigned int *mask;
+    int R, T, W, nOR, nOT, nf, nshell, ndir, npsi, K;
+    const float *w;            // fine weights
+    const ParticleState *ps;
+    const float2 *projf;       // [R*nOR][nf]
+    const float2 *Xf, *Xnf;    // [p][nf]
+    const float *Cf;           // [p][nf] (scaled CTF)
+    const float *minv_store;   // [nf]
+    const PixelRef *pf;
+    const float2 *phase_f;     // [T*nOT][nf]
+    const double *otx, *oty;   // [T*nOT] fine translations in pixels
+    const double *pdat;        // [p][8]
+    double pixel;
+    int do_scale;
+    const unsigned char *dvp_mask;  // [K][nshell] data_vs_prior > 3 (scale corr.)
+    float2 *bpimg;             // [R*nOR][nf]
+    float *bpw;                // [R*nOR][nf]
+    unsigned char *active;     // [R*nOR]
+    double *shell;             // [p][nshell]
+    double *pacc;              // [p][8]: sumw, sigma2_offset, XA, AA
+    double *pdf_dir;           // [K*ndir]
+    double *pdf_cls;           // [K]
+};
+cudaError_t launch_wsum(const WsumArgs &a, cudaStream_t st);
+cudaError_t launch_compact_flags(const unsigned char *flags, int n, int *list, int *count,
+                                 cudaStream_t st);
+cudaError_t launch_backproject(const int *list, int nlist, const float *eul_f, int nOR,
+                               const int *cls_of_r, float2 *bpimg, float *bpw, const PixelRef *pf,
+                               int nf, int sh, const VolGeom &g, double2 *const *data,
+                               double *const *weight, unsigned char *active, cudaStream_t st);
+
+}  // namespace gbr

@@ -1,0 +1,956 @@
+// k_estep.cu -- per-batch kernels of the E-step other than the coarse GEMMs:
+// particle preparation, diff2 -> weight conversion, the significance
+// threshold search, the fine (oversampled) pass, the weighted sums of
+// storeWeightedSums and the Fourier backprojection.
+//
+// Reference semantics (CPU path, src/ml_optimiser.cpp):
+//   weights      convertAllSquaredDifferencesToWeights  :7704-8239
+//   significance sorted cumulative pruning              :8120-8200
+//   fine pass    getAllSquaredDifferences (ipass 1)      :7098-7700
+//   wsums / BP   storeWeightedSums                      :8241-9157
+//   insertion    BackProjector::backproject2Dto3D        src/backprojector.cpp:55-296
+#include "gbr_internal.h"
+
+#include <cfloat>
+
+namespace gbr {
+namespace {
+
+__device__ __forceinline__ unsigned int f2ord(float f) {
+    unsigned int u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ord2f(unsigned int u) {
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+template <class T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block-wide double sum; result valid in thread 0.  `sh` holds >= 32 doubles.
+__device__ double block_sum(double v, double *sh) {
+    v = warp_sum(v);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[wid] = v;
+    __syncthreads();
+    double r = 0.;
+    if (wid == 0) {
+        r = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : 0.;
+        r = warp_sum(r);
+    }
+    return r;
+}
+
+// ---------------------------------------------------------------------------
+// Particle preparation: one block per particle.
+//   coarse pixel j:  a_c = m C^2,  b_c = m C X          (m = invsigma2/2)
+//   fine pixel j:    a_f, b_f likewise, plus compacted X, Xn, C
+//   c = Xi2/2 + sum m |X|^2 in FP64 for each pass.
+// pdat[p] = {old_x, old_y, prior_x, prior_y, highres_Xi2, norm, scale, 0}.
+// ---------------------------------------------------------------------------
+__global__ void k_prep(const float2 *__restrict__ X, const float *__restrict__ C,
+                       const float2 *__restrict__ Xn, const double *__restrict__ pdat,
+                       int full_npix, const PixelRef *__restrict__ pc, int nc,
+                       const float *__restrict__ minv_c, int ldk_c, const PixelRef *__restrict__ pf,
+                       int nf, const float *__restrict__ minv_f, float *__restrict__ a_c,
+                       float2 *__restrict__ b_c, float *__restrict__ a_f, float2 *__restrict__ b_f,
+                       float2 *__restrict__ Xf, float2 *__restrict__ Xnf, float *__restrict__ Cf,
+                       int do_scale, ParticleState *__restrict__ ps) {
+    __shared__ double sh[32];
+    const int p = blockIdx.x;
+    const double *pd = pdat + (size_t)p * 8;
+    const float scale = do_scale ? (float)pd[6] : 1.f;
+    const float2 *x = X + (size_t)p * full_npix;
+    const float2 *xn = Xn + (size_t)p * full_npix;
+    const float *c = C + (size_t)p * full_npix;
+    double acc = 0.;
+    for (int j = threadIdx.x; j < ldk_c; j += blockDim.x) {
+        float a = 0.f;
+        float2 b = make_float2(0.f, 0.f);
+        if (j < nc) {
+            const int k = pc[j].full;
+            const float cs = c[k] * scale, m = minv_c[j];
+            const float2 v = x[k];
+            a = m * cs * cs;
+            b = make_float2(m * cs * v.x, m * cs * v.y);
+            acc += (double)m * ((double)v.x * v.x + (double)v.y * v.y);
+        }
+        a_c[(size_t)p * ldk_c + j] = a;
+        b_c[(size_t)p * ldk_c + j] = b;
+    }
+    double tot = block_sum(acc, sh);
+    if (threadIdx.x == 0) {
+        ParticleState s{};
+        s.c_coarse = pd[4] / 2. + tot;
+        s.min_coarse = 0xFFFFFFFFu;
+        s.min_fine = 0xFFFFFFFFu;
+        ps[p] = s;
+    }
+    acc = 0.;
+    for (int j = threadIdx.x; j < nf; j += blockDim.x) {
+        const int k = pf[j].full;
+        const float cr = c[k];
+        const float cs = cr * scale, m = minv_f[j];
+        const float2 v = x[k];
+        a_f[(size_t)p * nf + j] = m * cs * cs;
+        b_f[(size_t)p * nf + j] = make_float2(m * cs * v.x, m * cs * v.y);
+        Xf[(size_t)p * nf + j] = v;
+        Xnf[(size_t)p * nf + j] = xn[k];
+        Cf[(size_t)p * nf + j] = cr;
+        acc += (double)m * ((double)v.x * v.x + (double)v.y * v.y);
+    }
+    tot = block_sum(acc, sh);
+    if (threadIdx.x == 0) ps[p].c_fine = pd[4] / 2. + tot;
+}
+
+// pdf_offset per (particle, coarse translation), normalised by its mean over
+// the translations (src/ml_optimiser.cpp:7779-7863, :7913-7958).  The
+// translations tx, ty are in Angstrom and the old offset and prior in
+// pixels, combined exactly as the reference does.
+__global__ void k_pdf_offset(const double *__restrict__ pdat, const double *__restrict__ tx,
+                             const double *__restrict__ ty, int T, double s2, double pixel,
+                             float *__restrict__ out) {
+    __shared__ double sh[32];
+    extern __shared__ double vals[];
+    const int p = blockIdx.x;
+    const double *pd = pdat + (size_t)p * 8;
+    const double norm = 2. * 3.14159265358979323846 * sqrt(s2) * sqrt(s2);
+    double acc = 0.;
+    for (int t = threadIdx.x; t < T; t += blockDim.x) {
+        const double ox = pd[0] + tx[t], oy = pd[1] + ty[t];
+        double td = 0.;
+        td += (ox - pd[2]) * (ox - pd[2]) / (-2. * s2);
+        td += (oy - pd[3]) * (oy - pd[3]) / (-2. * s2);
+        td *= pixel * pixel;
+        const double v = (s2 < 0.0001) ? ((td > 0.) ? 0. : 1.) : exp(td) / norm;
+        vals[t] = v;
+        acc += v;
+    }
+    double tot = block_sum(acc, sh);
+    __shared__ double mean;
+    if (threadIdx.x == 0) mean = tot / (double)T;
+    __syncthreads();
+    for (int t = threadIdx.x; t < T; t += blockDim.x)
+        out[(size_t)p * T + t] = (float)(mean > 0. ? vals[t] / mean : vals[t]);
+}
+
+// ---------------------------------------------------------------------------
+// diff2 -> weight, in place, over per-particle segments.  A block handles
+// kChunk elements of one particle; also accumulates the FP64 weight sum, the
+// level-0 histogram of the threshold search and (fine pass) the arg-max.
+// ---------------------------------------------------------------------------
+constexpr int kChunk = 8192;
+constexpr int kWThreads = 512;
+
+__global__ void __launch_bounds__(kWThreads)
+k_weights(float *__restrict__ vals, const long long *__restrict__ seg, int coarse, int T,
+          const int *__restrict__ ejob, const unsigned int *__restrict__ ecode,
+          const FineJob *__restrict__ jobs, int nOR, int nOT, const float *__restrict__ pdf_orient,
+          const float *__restrict__ pdf_off, ParticleState *__restrict__ ps,
+          HistBin *__restrict__ hist) {
+    extern __shared__ double dsm[];
+    double *hsum = dsm;                                            // [kHistBins]
+    unsigned int *hcnt = reinterpret_cast<unsigned int *>(hsum + kHistBins);  // [kHistBins]
+    __shared__ double sh[32];
+    __shared__ unsigned long long smax;
+    const int p = blockIdx.y;
+    const long long b0 = seg[p], b1 = seg[p + 1];
+    const long long beg = b0 + (long long)blockIdx.x * kChunk;
+    if (beg >= b1) return;
+    const long long end = min(beg + (long long)kChunk, b1);
+    for (int i = threadIdx.x; i < kHistBins; i += blockDim.x) {
+        hsum[i] = 0.;
+        hcnt[i] = 0u;
+    }
+    if (threadIdx.x == 0) smax = 0ull;
+    __syncthreads();
+    const float mn = ord2f(coarse ? ps[p].min_coarse : ps[p].min_fine);
+    double acc = 0.;
+    unsigned long long kmax = 0ull;
+    for (long long e = beg + threadIdx.x; e < end; e += blockDim.x) {
+        const float d = vals[e];
+        float w = 0.f;
+        if (d < FLT_MAX) {  // finite: computed
+            const float x = d - mn;
+            if (!(x > 700.f)) {
+                int r, t;
+                unsigned int code = 0;
+                if (coarse) {
+                    const long long loc = e - b0;
+                    r = (int)(loc / T);
+                    t = (int)(loc - (long long)r * T);
+                } else {
+                    r = jobs[ejob[e]].r;
+                    code = ecode[e];
+                    t = (int)(code / (unsigned)(nOR * nOT));
+                }
+                w = pdf_orient[r] * pdf_off[(size_t)p * T + t] * expf(-x);
+                if (!coarse && w > 0.f) {
+                    // loop order of storeWeightedSums: (r, iover_rot, itrans, iover_trans)
+                    const unsigned int ior = (code / nOT) % nOR, iot = code % nOT;
+                    const unsigned long long idx =
+                        (((unsigned long long)r * nOR + ior) * T + t) * nOT + iot;
+                    const unsigned long long key =
+                        ((unsigned long long)__float_as_uint(w) << 32) | (0xFFFFFFFFull - idx);
+                    kmax = key > kmax ? key : kmax;
+                }
+            }
+        }
+        vals[e] = w;
+        if (w > 0.f) {
+            acc += (double)w;
+            const unsigned int bin = __float_as_uint(w) >> 19;
+            atomicAdd(&hsum[bin], (double)w);
+            atomicAdd(&hcnt[bin], 1u);
+        }
+    }
+    const double tot = block_sum(acc, sh);
+    if (!coarse) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long other = __shfl_xor_sync(0xffffffffu, kmax, o);
+            kmax = other > kmax ? other : kmax;
+        }
+        if ((threadIdx.x & 31) == 0 && kmax) atomicMax(&smax, kmax);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        atomicAdd(coarse ? &ps[p].sum_coarse : &ps[p].sum_fine, tot);
+        if (!coarse && smax) atomicMax(&ps[p].argmax_key, smax);
+    }
+    HistBin *hp = hist + (size_t)p * kHistBins;
+    for (int i = threadIdx.x; i < kHistBins; i += blockDim.x)
+        if (hcnt[i]) {
+            atomicAdd(&hp[i].sum, hsum[i]);
+            atomicAdd(&hp[i].count, hcnt[i]);
+        }
+}
+
+// Histogram of the next 12 (level 1) or 7 (level 2) bits of the weights that
+// share the prefix selected so far.
+__global__ void __launch_bounds__(kWThreads)
+k_hist_refine(const float *__restrict__ vals, const long long *__restrict__ seg, int level,
+              const ParticleState *__restrict__ ps, HistBin *__restrict__ hist) {
+    extern __shared__ double dsm[];
+    double *hsum = dsm;
+    unsigned int *hcnt = reinterpret_cast<unsigned int *>(hsum + kHistBins);
+    const int p = blockIdx.y;
+    const long long b0 = seg[p], b1 = seg[p + 1];
+    const long long beg = b0 + (long long)blockIdx.x * kChunk;
+    if (beg >= b1) return;
+    const long long end = min(beg + (long long)kChunk, b1);
+    const int nb = level == 1 ? kHistBins : 128;
+    const int shift = level == 1 ? 19 : 7;   // bits above the new field
+    const int fshift = level == 1 ? 7 : 0;   // position of the new field
+    const unsigned int fmask = level == 1 ? 0xFFFu : 0x7Fu;
+    const unsigned int prefix = ps[p].sel_prefix;
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+        hsum[i] = 0.;
+        hcnt[i] = 0u;
+    }
+    __syncthreads();
+    for (long long e = beg + threadIdx.x; e < end; e += blockDim.x) {
+        const float w = vals[e];
+        if (w > 0.f) {
+            const unsigned int u = __float_as_uint(w);
+            if ((u >> shift) == prefix) {
+                const unsigned int bin = (u >> fshift) & fmask;
+                atomicAdd(&hsum[bin], (double)w);
+                atomicAdd(&hcnt[bin], 1u);
+            }
+        }
+    }
+    __syncthreads();
+    HistBin *hp = hist + (size_t)p * kHistBins;
+    for (int i = threadIdx.x; i < nb; i += blockDim.x)
+        if (hcnt[i]) {
+            atomicAdd(&hp[i].sum, hsum[i]);
+            atomicAdd(&hp[i].count, hcnt[i]);
+        }
+}
+
+// One block per particle: walk the histogram from the largest weights down
+// and find the bucket in which the cumulative weight first exceeds the
+// target (the break of the loop at src/ml_optimiser.cpp:8158-8179).  After
+// level 2 the bucket is a single float value: the significant weight.
+// The histogram is cleared for the next level.
+__global__ void k_select(int level, double fraction, int coarse, ParticleState *__restrict__ ps,
+                         HistBin *__restrict__ hist) {
+    const int p = blockIdx.x;
+    const int nb = level == 2 ? 128 : kHistBins;
+    const int per = (nb + blockDim.x - 1) / blockDim.x;   // bins per thread
+    __shared__ double ssum[256];
+    __shared__ unsigned int scnt[256];
+    __shared__ int found_bin;
+    __shared__ double found_above;
+    __shared__ unsigned int found_cnt_above;
+    HistBin *hp = hist + (size_t)p * kHistBins;
+    ParticleState &s = ps[p];
+    if (level == 0) {
+        if (threadIdx.x == 0) {
+            s.target = fraction * (coarse ? s.sum_coarse : s.sum_fine);
+            s.sel_above = 0.;
+            s.sel_count_above = 0u;
+            s.sel_prefix = 0u;
+        }
+        __syncthreads();
+    }
+    const double target = s.target, above0 = s.sel_above;
+    // thread i covers bins hi_i .. hi_i-per+1 (descending)
+    const int hi = nb - 1 - (int)threadIdx.x * per;
+    double my = 0.;
+    unsigned int myc = 0;
+    for (int q = 0; q < per; ++q) {
+        const int b = hi - q;
+        if (b >= 0) {
+            my += hp[b].sum;
+            myc += hp[b].count;
+        }
+    }
+    ssum[threadIdx.x] = my;
+    scnt[threadIdx.x] = myc;
+    if (threadIdx.x == 0) found_bin = -1;
+    __syncthreads();
+    // inclusive scan (Hillis-Steele) over threads in descending-bin order
+    for (int o = 1; o < (int)blockDim.x; o <<= 1) {
+        double v = threadIdx.x >= (unsigned)o ? ssum[threadIdx.x - o] : 0.;
+        unsigned int c = threadIdx.x >= (unsigned)o ? scnt[threadIdx.x - o] : 0u;
+        __syncthreads();
+        ssum[threadIdx.x] += v;
+        scnt[threadIdx.x] += c;
+        __syncthreads();
+    }
+    const double incl = ssum[threadIdx.x];
+    const double excl = incl - my;
+    const unsigned int excl_c = scnt[threadIdx.x] - myc;
+    if (above0 + excl <= target && above0 + incl > target) {
+        double cum = above0 + excl;
+        unsigned int cc = excl_c;
+        for (int q = 0; q < per; ++q) {
+            const int b = hi - q;
+            if (b < 0) break;
+            const double bs = hp[b].sum;
+            if (cum + bs > target) {
+                found_bin = b;
+                found_above = cum;
+                found_cnt_above = cc;
+                break;
+            }
+            cum += bs;
+            cc += hp[b].count;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && found_bin < 0) {
+        // target not exceeded (fraction >= 1): the smallest positive weight
+        double cum = above0;
+        unsigned int cc = s.sel_count_above;
+        int last = -1;
+        for (int b = nb - 1; b >= 0; --b)
+            if (hp[b].count) {
+                if (last >= 0) {
+                    cum += hp[last].sum;
+                    cc += hp[last].count;
+                }
+                last = b;
+            }
+        found_bin = last < 0 ? 0 : last;
+        found_above = cum;
+        found_cnt_above = cc - s.sel_count_above;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int b = found_bin;
+        const unsigned int prefix = (level == 0) ? (unsigned)b
+                                  : (level == 1) ? ((s.sel_prefix << 12) | (unsigned)b)
+                                                 : ((s.sel_prefix << 7) | (unsigned)b);
+        s.sel_prefix = prefix;
+        s.sel_count_above += found_cnt_above;
+        s.sel_above = found_above;
+        if (level == 2) {
+            const float v = __uint_as_float(prefix);
+            // ties: the loop stops inside the run of equal values
+            const double need = (s.target - s.sel_above) / (double)v;
+            unsigned int k = (need >= 0.) ? (unsigned int)floor(need) + 1u : 1u;
+            const unsigned int nb_cnt = hp[b].count;
+            if (k > nb_cnt) k = nb_cnt;
+            if (k < 1u) k = 1u;
+            if (coarse) {
+                s.thr_coarse = v;
+                s.nr_sign = s.sel_count_above + k;
+            } else {
+                s.thr_fine = v;
+            }
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < kHistBins; i += blockDim.x) {
+        hp[i].sum = 0.;
+        hp[i].count = 0u;
+    }
+}
+
+// Significance bitmask per (particle, coarse orientation): bit t set where
+// the coarse weight >= the significant weight (Mcoarse_significant,
+// src/ml_optimiser.cpp:8210-8218).  One warp per (p, r).
+__global__ void k_sig_masks(const float *__restrict__ w, int n, int R, int T, int W,
+                            const ParticleState *__restrict__ ps, unsigned int *__restrict__ mask,
+                            int *__restrict__ cnt) {
+    const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (gw >= (long long)n * R) return;
+    const int p = (int)(gw / R);
+    const float thr = ps[p].thr_coarse;
+    const float *row = w + (size_t)gw * T;
+    int c = 0;
+    for (int word = 0; word < W; ++word) {
+        const int t = word * 32 + lane;
+        const float v = t < T ? row[t] : 0.f;
+        const unsigned int bits = __ballot_sync(0xffffffffu, v > 0.f && v >= thr);
+        if (lane == 0) mask[(size_t)gw * W + word] = bits;
+        c += __popc(bits);
+    }
+    if (lane == 0) cnt[gw] = c;
+}
+
+// Exclusive scan of int64 (out has n+1 entries, out[n] = total).
+constexpr int kScanBlock = 1024;
+__global__ void k_scan_blocks(const long long *__restrict__ in, long long *__restrict__ out,
+                              long long n, long long *__restrict__ sums) {
+    __shared__ long long sh[kScanBlock];
+    const long long i = (long long)blockIdx.x * kScanBlock + threadIdx.x;
+    const long long v = i < n ? in[i] : 0;
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = 1; o < kScanBlock; o <<= 1) {
+        long long a = threadIdx.x >= (unsigned)o ? sh[threadIdx.x - o] : 0;
+        __syncthreads();
+        sh[threadIdx.x] += a;
+        __syncthreads();
+    }
+    if (i < n) out[i] = sh[threadIdx.x] - v;
+    if (threadIdx.x == kScanBlock - 1) sums[blockIdx.x] = sh[threadIdx.x];
+}
+__global__ void k_scan_sums(long long *__restrict__ sums, int nb) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        long long run = 0;
+        for (int b = 0; b < nb; ++b) {
+            const long long v = sums[b];
+            sums[b] = run;
+            run += v;
+        }
+        sums[nb] = run;
+    }
+}
+__global__ void k_scan_add(long long *__restrict__ out, long long n, const long long *__restrict__ sums,
+                           int nb) {
+    const long long i = (long long)blockIdx.x * kScanBlock + threadIdx.x;
+    if (i < n) out[i] += sums[blockIdx.x];
+    if (i == 0) out[n] = sums[nb];
+}
+
+__global__ void k_flag_counts(const int *__restrict__ cnt, long long n, long long *__restrict__ flags,
+                              long long *__restrict__ entries, int per) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int c = cnt[i];
+    flags[i] = c > 0 ? 1 : 0;
+    entries[i] = (long long)c * per;
+}
+
+__global__ void k_build_jobs(const int *__restrict__ cnt, int n, int R, const long long *__restrict__ jpos,
+                             const long long *__restrict__ epos, FineJob *__restrict__ jobs,
+                             long long *__restrict__ seg, unsigned char *__restrict__ need_r) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long tot = (long long)n * R;
+    if (i < tot) {
+        const int c = cnt[i];
+        const int p = (int)(i / R), r = (int)(i - (long long)p * R);
+        if (c > 0) {
+            FineJob j;
+            j.p = p;
+            j.r = r;
+            j.n_t = c;
+            j.pad_ = 0;
+            j.off = epos[i];
+            jobs[jpos[i]] = j;
+            need_r[r] = 1;
+        }
+        if (r == 0) seg[p] = epos[i];
+    }
+    if (i == 0) seg[n] = epos[tot];
+}
+
+// ---------------------------------------------------------------------------
+// Fine pass: one block per job (particle p, coarse orientation r).
+// For every oversampled orientation ior and every significant coarse
+// translation t with its oversampled shifts iot:
+//   diff2 - c_fine = N_ior - 2 sum_k Re(Q_ior,k conj(E_(t,iot),k)),
+//   Q = P_(r,ior) conj(m C X),  N_ior = sum_k m C^2 |P|^2.
+// Q is staged in shared memory per pixel chunk; one warp per (t, iot) row.
+// Entries are written in hidden-index order (t, ior, iot) within the job.
+// ---------------------------------------------------------------------------
+constexpr int kFineChunk = 512;
+constexpr int kFineThreads = 256;
+
+__global__ void __launch_bounds__(kFineThreads)
+k_fine_diff2(const FineJob *__restrict__ jobs, const unsigned int *__restrict__ mask, int R, int T,
+             int W, int nOR, int nOT, const float2 *__restrict__ projf, const float2 *__restrict__ b_f,
+             const float *__restrict__ a_f, int nf, const float2 *__restrict__ phase_f,
+             float *__restrict__ d, int *__restrict__ ejob, unsigned int *__restrict__ ecode,
+             ParticleState *__restrict__ ps) {
+    extern __shared__ float4 fsm[];
+    float2 *Q = reinterpret_cast<float2 *>(fsm);                   // [nOR][kFineChunk]
+    float *acc = reinterpret_cast<float *>(Q + nOR * kFineChunk);  // [rows][nOR]
+    int *tlist = reinterpret_cast<int *>(acc + T * nOT * nOR);     // [T]
+    float *norm = reinterpret_cast<float *>(tlist + T);            // [nOR]
+    __shared__ unsigned int smin;
+    const long long jid = blockIdx.x;
+    const FineJob job = jobs[jid];
+    const int p = job.p, r = job.r, n_t = job.n_t;
+    const int rows = n_t * nOT;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    const unsigned int *mk = mask + ((size_t)p * R + r) * W;
+    if (threadIdx.x == 0) {
+        int m = 0;
+        for (int w = 0; w < W; ++w) {
+            unsigned int bits = mk[w];
+            while (bits) {
+                const int b = __ffs(bits) - 1;
+                bits &= bits - 1;
+                tlist[m++] = w * 32 + b;
+            }
+        }
+        smin = 0xFFFFFFFFu;
+    }
+    for (int i = threadIdx.x; i < rows * nOR; i += blockDim.x) acc[i] = 0.f;
+    for (int i = threadIdx.x; i < nOR; i += blockDim.x) norm[i] = 0.f;
+    __syncthreads();
+    const float2 *bp = b_f + (size_t)p * nf;
+    const float *ap = a_f + (size_t)p * nf;
+    for (int c0 = 0; c0 < nf; c0 += kFineChunk) {
+        const int cl = min(kFineChunk, nf - c0);
+        // stage Q, accumulate norms (one warp per ior at a time)
+        for (int ior = warp; ior < nOR; ior += nwarp) {
+            const float2 *P = projf + ((size_t)r * nOR + ior) * nf + c0;
+            float nacc = 0.f;
+            for (int k = lane; k < cl; k += 32) {
+                const float2 pv = P[k], bv = bp[c0 + k];
+                Q[ior * kFineChunk + k] = make_float2(pv.x * bv.x + pv.y * bv.y, pv.y * bv.x - pv.x * bv.y);
+                nacc = fmaf(ap[c0 + k], pv.x * pv.x + pv.y * pv.y, nacc);
+            }
+            nacc = warp_sum(nacc);
+            if (lane == 0) norm[ior] += nacc;
+        }
+        __syncthreads();
+        for (int row = warp; row < rows; row += nwarp) {
+            const int tr = row / nOT, iot = row - tr * nOT;
+            const int tf = tlist[tr] * nOT + iot;
+            const float2 *E = phase_f + (size_t)tf * nf + c0;
+            float s[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) s[i] = 0.f;
+            for (int k = lane; k < cl; k += 32) {
+                const float2 e = E[k];
+#pragma unroll
+                for (int i = 0; i < 8; ++i)
+                    if (i < nOR) {
+                        const float2 q = Q[i * kFineChunk + k];
+                        s[i] = fmaf(q.x, e.x, fmaf(q.y, e.y, s[i]));
+                    }
+            }
+#pragma unroll
+            for (int i = 0; i < 8; ++i) s[i] = warp_sum(s[i]);
+            if (lane < nOR && lane < 8) {
+                float v = s[0];
+#pragma unroll
+                for (int i = 1; i < 8; ++i)
+                    if (lane == i) v = s[i];
+                acc[row * nOR + lane] += v;
+            }
+        }
+        __syncthreads();
+    }
+    // write entries: entry = off + (tr*nOR + ior)*nOT + iot
+    float lmin = FLT_MAX;
+    for (int i = threadIdx.x; i < rows * nOR; i += blockDim.x) {
+        const int row = i / nOR, ior = i - row * nOR;
+        const int tr = row / nOT, iot = row - tr * nOT;
+        const float v = norm[ior] - 2.f * acc[i];
+        const long long e = job.off + ((long long)tr * nOR + ior) * nOT + iot;
+        d[e] = v;
+        ejob[e] = (int)jid;
+        ecode[e] = ((unsigned)tlist[tr] * nOR + ior) * nOT + iot;
+        lmin = fminf(lmin, v);
+    }
+    if (lmin < FLT_MAX) atomicMin(&smin, f2ord(lmin));
+    __syncthreads();
+    if (threadIdx.x == 0 && smin != 0xFFFFFFFFu) atomicMin(&ps[p].min_fine, smin);
+}
+
+// ---------------------------------------------------------------------------
+// storeWeightedSums for one job (particle p, coarse orientation r): for each
+// oversampled orientation, the significant fine weights (w >= thr_fine,
+// normalised by the sum) give W = sum w~ and the weighted phase sum
+// Phi_k = sum w~ E_(t,iot),k, from which
+//   sigma2 shell sums:  W C^2 |P|^2 - 2 C Re(P conj(X Phi)) + W |X|^2
+//   backprojection:     img += C Minv Xn Phi,  weight += W C^2 Minv
+// (the per-translation sums of :8562-8780 rewritten with Phi).
+// One warp per oversampled orientation.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_wsum(WsumArgs a) {
+    extern __shared__ double wsm[];
+    double *shell = wsm;                                            // [nshell]
+    float *wt = reinterpret_cast<float *>(shell + a.nshell);        // [nOR][rows]
+    int *tlist = reinterpret_cast<int *>(wt + a.nOR * a.T * a.nOT); // [T]
+    __shared__ double red[8];  // sumw, sigma2_offset, XA, AA
+    const FineJob job = a.jobs[blockIdx.x];
+    const int p = job.p, r = job.r, n_t = job.n_t;
+    const int rows = n_t * a.nOT;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    const ParticleState ps = a.ps[p];
+    const float thr = ps.thr_fine;
+    const double inv_sum = 1. / ps.sum_fine;
+    const double *pd = a.pdat + (size_t)p * 8;
+    const int ic = r / (a.ndir * a.npsi), idir = (r / a.npsi) % a.ndir;
+    const float scale = a.do_scale ? fmaxf((float)pd[6], 0.001f) : 1.f;
+    if (threadIdx.x == 0) {
+        const unsigned int *mk = a.mask + ((size_t)p * a.R + r) * a.W;
+        int m = 0;
+        for (int w = 0; w < a.W; ++w) {
+            unsigned int bits = mk[w];
+            while (bits) {
+                const int b = __ffs(bits) - 1;
+                bits &= bits - 1;
+                tlist[m++] = w * 32 + b;
+            }
+        }
+    }
+    if (threadIdx.x < 8) red[threadIdx.x] = 0.;
+    for (int i = threadIdx.x; i < a.nshell; i += blockDim.x) shell[i] = 0.;
+    __syncthreads();
+    // normalised significant weights per (ior, row); FP64 scalar sums
+    double l_sumw = 0., l_off = 0.;
+    for (int i = threadIdx.x; i < rows * a.nOR; i += blockDim.x) {
+        const int ior = i / rows, row = i - ior * rows;
+        const int tr = row / a.nOT, iot = row - tr * a.nOT;
+        const long long e = job.off + ((long long)tr * a.nOR + ior) * a.nOT + iot;
+        const float w = a.w[e];
+        float wn = 0.f;
+        if (w > 0.f && w >= thr) {
+            const double wd = (double)w * inv_sum;
+            wn = (float)wd;
+            l_sumw += wd;
+            const int tf = tlist[tr] * a.nOT + iot;
+            const double dx = pd[2] - pd[0] - a.otx[tf];
+            const double dy = pd[3] - pd[1] - a.oty[tf];
+            l_off += wd * a.pixel * a.pixel * dx * dx;
+            l_off += wd * a.pixel * a.pixel * dy * dy;
+        }
+        wt[ior * rows + row] = wn;
+    }
+    l_sumw = warp_sum(l_sumw);
+    l_off = warp_sum(l_off);
+    if (lane == 0) {
+        atomicAdd(&red[0], l_sumw);
+        atomicAdd(&red[1], l_off);
+    }
+    __syncthreads();
+    const float2 *Xp = a.Xf + (size_t)p * a.nf;
+    const float2 *Xnp = a.Xnf + (size_t)p * a.nf;
+    const float *Cp = a.Cf + (size_t)p * a.nf;
+    double l_xa = 0., l_aa = 0.;
+    for (int ior = warp; ior < a.nOR; ior += nwarp) {
+        const float *wr = wt + ior * rows;
+        float Wsum = 0.f;
+        for (int row = 0; row < rows; ++row) Wsum += wr[row];
+        if (!(Wsum > 0.f)) continue;
+        const size_t rf = (size_t)r * a.nOR + ior;
+        const float2 *P = a.projf + rf * a.nf;
+        for (int k = lane; k < a.nf; k += 32) {
+            float2 phi = make_float2(0.f, 0.f);
+            for (int row = 0; row < rows; ++row) {
+                const float wv = wr[row];
+                if (wv != 0.f) {
+                    const int tr = row / a.nOT, iot = row - tr * a.nOT;
+                    const float2 e = a.phase_f[((size_t)tlist[tr] * a.nOT + iot) * a.nf + k];
+                    phi.x = fmaf(wv, e.x, phi.x);
+                    phi.y = fmaf(wv, e.y, phi.y);
+                }
+            }
+            const float2 x = Xp[k], xn = Xnp[k], pv = P[k];
+            const float cs = Cp[k] * scale;
+            const float2 zx = make_float2(x.x * phi.x - x.y * phi.y, x.x * phi.y + x.y * phi.x);
+            const float2 zn = make_float2(xn.x * phi.x - xn.y * phi.y, xn.x * phi.y + xn.y * phi.x);
+            const int sh = a.pf[k].shell;
+            const float p2 = pv.x * pv.x + pv.y * pv.y;
+            const float cross = pv.x * zx.x + pv.y * zx.y;
+            if (sh >= 0) {
+                const double s2 = (double)Wsum * cs * cs * p2 - 2.0 * cs * cross +
+                                  (double)Wsum * (x.x * x.x + x.y * x.y);
+                atomicAdd(&shell[sh], s2);
+                if (a.do_scale && a.dvp_mask[(size_t)ic * a.nshell + sh]) {
+                    l_xa += (double)cs * cross;
+                    l_aa += (double)Wsum * cs * cs * p2;
+                }
+            }
+            const float minv = a.minv_store[k];
+            const float f = cs * minv;
+            const float wgt = Wsum * cs * cs * minv;
+            if (wgt != 0.f || f != 0.f) {
+                atomicAdd(&a.bpimg[rf * a.nf + k].x, f * zn.x);
+                atomicAdd(&a.bpimg[rf * a.nf + k].y, f * zn.y);
+                atomicAdd(&a.bpw[rf * a.nf + k], wgt);
+            }
+        }
+        if (lane == 0) a.active[rf] = 1;
+    }
+    if (a.do_scale) {
+        l_xa = warp_sum(l_xa);
+        l_aa = warp_sum(l_aa);
+        if (lane == 0) {
+            atomicAdd(&red[2], l_xa);
+            atomicAdd(&red[3], l_aa);
+        }
+    }
+    __syncthreads();
+    double *sp = a.shell + (size_t)p * a.nshell;
+    for (int i = threadIdx.x; i < a.nshell; i += blockDim.x)
+        if (shell[i] != 0.) atomicAdd(&sp[i], shell[i]);
+    if (threadIdx.x == 0) {
+        double *pa = a.pacc + (size_t)p * 8;
+        atomicAdd(&pa[0], red[0]);
+        atomicAdd(&pa[1], red[1]);
+        if (a.do_scale) {
+            atomicAdd(&pa[2], red[2]);
+            atomicAdd(&pa[3], red[3]);
+        }
+        atomicAdd(&a.pdf_dir[(size_t)ic * a.ndir + idir], red[0]);
+        atomicAdd(&a.pdf_cls[ic], red[0]);
+    }
+}
+
+__global__ void k_compact_flags(const unsigned char *__restrict__ flags, int n, int *__restrict__ list,
+                                int *__restrict__ count) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && flags[i]) {
+        const int pos = atomicAdd(count, 1);
+        list[pos] = i;
+    }
+}
+
+// Trilinear insertion of the accumulated 2D slices of the active fine
+// orientations into the FP64 data and weight volumes
+// (backproject2Dto3D, src/backprojector.cpp:55-296).  Each block handles
+// one slice; the slice accumulators are cleared for the next batch.
+__global__ void k_backproject(const int *__restrict__ list, const float *__restrict__ eul_f, int nOR,
+                              const int *__restrict__ cls_of_r, float2 *__restrict__ bpimg,
+                              float *__restrict__ bpw, const PixelRef *__restrict__ pf, int nf,
+                              const VolGeom g, double2 *const *__restrict__ data,
+                              double *const *__restrict__ weight, unsigned char *__restrict__ active) {
+    const int rf = list[blockIdx.x];
+    __shared__ float Ai[9];
+    if (threadIdx.x < 9) Ai[threadIdx.x] = eul_f[(size_t)rf * 9 + threadIdx.x];
+    __syncthreads();
+    const int ic = cls_of_r[rf / nOR];
+    double2 *dv = data[ic];
+    double *wv = weight[ic];
+    const int rr = (int)lrintf((float)g.r_max * g.pad);   // ROUND(r_max * pad)
+    const int max_r2 = rr * rr;
+    const size_t sy = (size_t)g.xdim, sz = (size_t)g.xdim * g.ydim;
+    for (int k = threadIdx.x; k < nf; k += blockDim.x) {
+        const size_t idx = (size_t)rf * nf + k;
+        const float w = bpw[idx];
+        const float2 val0 = bpimg[idx];
+        bpw[idx] = 0.f;
+        bpimg[idx] = make_float2(0.f, 0.f);
+        if (!(w > 0.f)) continue;
+        const PixelRef pr = pf[k];
+        if (g.pad * g.pad * (pr.x * pr.x + pr.y * pr.y) > max_r2) continue;
+        float xp = fmaf(Ai[0], (float)pr.x, Ai[1] * (float)pr.y);
+        float yp = fmaf(Ai[3], (float)pr.x, Ai[4] * (float)pr.y);
+        float zp = fmaf(Ai[6], (float)pr.x, Ai[7] * (float)pr.y);
+        float2 val = val0;
+        if (xp < 0.f) {
+            xp = -xp;
+            yp = -yp;
+            zp = -zp;
+            val.y = -val.y;
+        }
+        const float fx0 = floorf(xp), fy0 = floorf(yp), fz0 = floorf(zp);
+        const float fx = xp - fx0, fy = yp - fy0, fz = zp - fz0;
+        const int x0 = (int)fx0, y0 = (int)fy0 - g.yinit, z0 = (int)fz0 - g.zinit;
+        if (x0 < 0 || x0 + 1 >= g.xdim || y0 < 0 || y0 + 1 >= g.ydim || z0 < 0 || z0 + 1 >= g.zdim)
+            continue;
+        const float mfx = 1.f - fx, mfy = 1.f - fy, mfz = 1.f - fz;
+        const float dd[8] = {mfz * mfy * mfx, mfz * mfy * fx, mfz * fy * mfx, mfz * fy * fx,
+                             fz * mfy * mfx,  fz * mfy * fx,  fz * fy * mfx,  fz * fy * fx};
+        const size_t base = (size_t)z0 * sz + (size_t)y0 * sy + x0;
+        const size_t off[8] = {0, 1, sy, sy + 1, sz, sz + 1, sz + sy, sz + sy + 1};
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            const double dc = (double)dd[c];
+            atomicAdd(&dv[base + off[c]].x, dc * val.x);
+            atomicAdd(&dv[base + off[c]].y, dc * val.y);
+            atomicAdd(&wv[base + off[c]], dc * w);
+        }
+    }
+    if (threadIdx.x == 0) active[rf] = 0;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// launch wrappers
+// ---------------------------------------------------------------------------
+cudaError_t launch_prep(const float2 *X, const float *C, const double *pdat, int n, int full_npix,
+                        const PixelRef *pc, int nc, const float *minv_c, int ldk_c,
+                        const PixelRef *pf, int nf, const float *minv_f, float *a_c, float2 *b_c,
+                        float *a_f, float2 *b_f, float2 *Xf, float2 *Xnf, float *Cf,
+                        const float2 *Xn, int do_scale, ParticleState *ps, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    k_prep<<<n, 256, 0, st>>>(X, C, Xn, pdat, full_npix, pc, nc, minv_c, ldk_c, pf, nf, minv_f, a_c,
+                              b_c, a_f, b_f, Xf, Xnf, Cf, do_scale, ps);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pdf_offset(const double *pdat, int n, const double *tx, const double *ty, int T,
+                              double sigma2_offset, double pixel, float *pdf_off, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    k_pdf_offset<<<n, 256, sizeof(double) * T, st>>>(pdat, tx, ty, T, sigma2_offset, pixel, pdf_off);
+    return cudaGetLastError();
+}
+
+static size_t hist_smem() { return kHistBins * (sizeof(double) + sizeof(unsigned int)); }
+
+cudaError_t launch_weights(float *vals, const long long *seg, int n, long long max_len, int coarse,
+                           int T, const int *ejob, const unsigned int *ecode, const FineJob *jobs,
+                           int nOR, int nOT, const float *pdf_orient, const float *pdf_off,
+                           ParticleState *ps, HistBin *hist, cudaStream_t st) {
+    if (n <= 0 || max_len <= 0) return cudaSuccess;
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_weights, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hist_smem());
+        cudaFuncSetAttribute(k_hist_refine, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hist_smem());
+        attr = true;
+    }
+    const long long nb = (max_len + kChunk - 1) / kChunk;
+    if (nb > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+    dim3 grid((unsigned)nb, n);
+    k_weights<<<grid, kWThreads, hist_smem(), st>>>(vals, seg, coarse, T, ejob, ecode, jobs, nOR, nOT,
+                                                    pdf_orient, pdf_off, ps, hist);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_hist_refine(const float *vals, const long long *seg, int n, long long max_len,
+                               int level, ParticleState *ps, HistBin *hist, cudaStream_t st) {
+    if (n <= 0 || max_len <= 0) return cudaSuccess;
+    const long long nb = (max_len + kChunk - 1) / kChunk;
+    dim3 grid((unsigned)nb, n);
+    k_hist_refine<<<grid, kWThreads, hist_smem(), st>>>(vals, seg, level, ps, hist);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_select(int n, int level, double adaptive_fraction, int coarse, ParticleState *ps,
+                          HistBin *hist, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    k_select<<<n, 256, 0, st>>>(level, adaptive_fraction, coarse, ps, hist);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sig_masks(const float *w, int n, int R, int T, int W, const ParticleState *ps,
+                             unsigned int *mask, int *cnt, cudaStream_t st) {
+    const long long warps = (long long)n * R;
+    if (warps <= 0) return cudaSuccess;
+    const long long blocks = (warps * 32 + 255) / 256;
+    k_sig_masks<<<(unsigned)blocks, 256, 0, st>>>(w, n, R, T, W, ps, mask, cnt);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scan_i64(const long long *in, long long *out, long long n, long long *tmp,
+                            cudaStream_t st) {
+    const long long nb = (n + kScanBlock - 1) / kScanBlock;
+    if (nb <= 0) {
+        k_scan_sums<<<1, 1, 0, st>>>(tmp, 0);
+        return cudaMemcpyAsync(out, tmp, sizeof(long long), cudaMemcpyDeviceToDevice, st);
+    }
+    k_scan_blocks<<<(unsigned)nb, kScanBlock, 0, st>>>(in, out, n, tmp);
+    k_scan_sums<<<1, 1, 0, st>>>(tmp, (int)nb);
+    k_scan_add<<<(unsigned)nb, kScanBlock, 0, st>>>(out, n, tmp, (int)nb);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_flag_counts(const int *cnt, long long n, long long *flags, long long *entries,
+                               int per, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    k_flag_counts<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(cnt, n, flags, entries, per);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_build_jobs(const int *cnt, int n, int R, const long long *jpos,
+                              const long long *epos, FineJob *jobs, long long *seg,
+                              unsigned char *need_r, cudaStream_t st) {
+    const long long tot = (long long)n * R;
+    k_build_jobs<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(cnt, n, R, jpos, epos, jobs, seg, need_r);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fine_diff2(const FineJob *jobs, long long njobs, const unsigned int *mask, int R,
+                              int T, int W, int nOR, int nOT, const float2 *projf, const float2 *b_f,
+                              const float *a_f, int nf, const float2 *phase_f, float *d, int *ejob,
+                              unsigned int *ecode, ParticleState *ps, cudaStream_t st) {
+    if (njobs <= 0) return cudaSuccess;
+    if (nOR > 8) return cudaErrorInvalidValue;
+    const size_t smem = sizeof(float2) * nOR * kFineChunk + sizeof(float) * T * nOT * nOR +
+                        sizeof(int) * T + sizeof(float) * nOR + 16;
+    static size_t attr = 0;
+    if (smem > attr) {
+        cudaError_t e = cudaFuncSetAttribute(k_fine_diff2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        attr = smem;
+    }
+    for (long long j0 = 0; j0 < njobs; j0 += 0x7fffffffLL) {
+        const long long nj = njobs - j0 < 0x7fffffffLL ? njobs - j0 : 0x7fffffffLL;
+        k_fine_diff2<<<(unsigned)nj, kFineThreads, smem, st>>>(jobs + j0, mask, R, T, W, nOR, nOT, projf,
+                                                               b_f, a_f, nf, phase_f, d, ejob, ecode, ps);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_wsum(const WsumArgs &a, cudaStream_t st) {
+    if (a.njobs <= 0) return cudaSuccess;
+    const size_t smem = sizeof(double) * a.nshell + sizeof(float) * a.nOR * a.T * a.nOT + sizeof(int) * a.T + 16;
+    static size_t attr = 0;
+    if (smem > attr) {
+        cudaError_t e = cudaFuncSetAttribute(k_wsum, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        attr = smem;
+    }
+    k_wsum<<<(unsigned)a.njobs, 256, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_compact_flags(const unsigned char *flags, int n, int *list, int *count,
+                                 cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    k_compact_flags<<<(n + 255) / 256, 256, 0, st>>>(flags, n, list, count);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_backproject(const int *list, int nlist, const float *eul_f, int nOR,
+                               const int *cls_of_r, float2 *bpimg, float *bpw, const PixelRef *pf,
+                               int nf, int sh, const VolGeom &g, double2 *const *data,
+                               double *const *weight, unsigned char *active, cudaStream_t st) {
+    (void)sh;
+    if (nlist <= 0) return cudaSuccess;
+    k_backproject<<<nlist, 256, 0, st>>>(list, eul_f, nOR, cls_of_r, bpimg, bpw, pf, nf, g, data,
+                                         weight, active);
+    return cudaGetLastError();
+}
+
+}  // namespace gbr

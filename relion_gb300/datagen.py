@@ -1,0 +1,269 @@
+"""Seeded synthetic E-step inputs with the shapes and statistics of the
+benchmark configurations (there is no public dataset for this path).
+
+A ground-truth volume is a sum of isotropic 3D Gaussians.  Its Fourier
+transform is analytic, so both the padded Fourier reference (the
+Projector::data array, low-passed to the initial resolution) and each
+particle's Fourier image (central slice at a random SO(3) pose, phase-shifted,
+multiplied by a CTF, plus complex white noise at the requested SNR) are
+evaluated exactly, without FFTs or interpolation.  The E-step sizes
+(current / coarse image sizes, pose grid) follow the reference's rules in
+MlOptimiser::updateImageSizeAndResolutionPointers (src/ml_optimiser.cpp:
+5684-5777).  Everything is generated in float64 with torch, on CPU or GPU.
+"""
+import math
+
+import numpy as np
+import torch
+
+CONFIGS = {
+    # box 64 px, 2.0 A, 2,000 particles, HEALPix order 2, psi 7.5, +/-4 px step 2
+    "cfg0_box64": dict(box=64, pixel=2.0, n_particles=2000, n_blobs=300, blob_sigma=1.5,
+                       blob_radius=20.0, max_shift=3.0, defocus=(10000.0, 25000.0), snr=0.05,
+                       ini_high=30.0, healpix_order=2, psi_step=7.5, offset_range_px=4.0,
+                       offset_step_px=2.0, diameter=100.0, classes=1),
+    # box 256 px, 1.0 A, 20,000 particles, HEALPix order 3, +/-6 px step 1
+    "cfg1_box256": dict(box=256, pixel=1.0, n_particles=20000, n_blobs=5000, blob_sigma=1.5,
+                        blob_radius=90.0, max_shift=3.0, defocus=(8000.0, 25000.0), snr=0.03,
+                        ini_high=20.0, healpix_order=3, psi_step=-1.0, offset_range_px=6.0,
+                        offset_step_px=1.0, diameter=200.0, classes=1),
+}
+
+KV, CS, Q0 = 300.0, 2.7, 0.1
+
+
+def iround(x):
+    return int(x + 0.5) if x > 0 else int(x - 0.5)
+
+
+def iceil(x):
+    return int(x) if x == int(x) else (int(x + 1) if x > 0 else int(x))
+
+
+def estep_sizes(box, pixel, ini_high, healpix_order, diameter, incr_size=10):
+    """current_size and coarse_size of the first iteration."""
+    maxres = iround(pixel * box / ini_high) + incr_size
+    current = min(2 * maxres, box)
+    ang = 360.0 / (6 * iround(2.0 ** healpix_order))
+    coarse_res = (ang / 360.0) * math.pi * diameter / 1.2
+    coarse = 2 * iceil(pixel * box / coarse_res)
+    coarse = min(coarse, current)
+    return current, coarse
+
+
+def ctf_value(defU, defV, defAng, X, Y, kV=KV, Cs=CS, Q0=Q0, Bfac=0.0, scale=1.0, phase_shift=0.0):
+    """CTF at spatial frequency (X, Y) in 1/Angstrom (CTF::getCTF, src/ctf.h:184-256)."""
+    local_Cs = Cs * 1e7
+    local_kV = kV * 1e3
+    lam = 12.2643247 / math.sqrt(local_kV * (1.0 + local_kV * 0.978466e-6))
+    K1 = math.pi / 2 * 2 * lam
+    K2 = math.pi / 2 * local_Cs * lam ** 3
+    K3 = math.atan(Q0 / math.sqrt(1 - Q0 * Q0))
+    K4 = -Bfac / 4.0
+    K5 = math.radians(phase_shift)
+    a = math.radians(defAng)
+    s, c = math.sin(a), math.cos(a)
+    Axx = c * c * (-defU) + s * s * (-defV)
+    Axy = c * s * (-defU) - s * c * (-defV)
+    Ayy = s * s * (-defU) + c * c * (-defV)
+    u2 = X * X + Y * Y
+    gamma = K1 * (Axx * X * X + 2.0 * Axy * X * Y + Ayy * Y * Y) + K2 * u2 * u2 - K5 - K3
+    ret = -torch.sin(gamma) * torch.exp(K4 * u2) * scale if torch.is_tensor(gamma) else \
+        -math.sin(gamma) * math.exp(K4 * u2) * scale
+    if torch.is_tensor(ret):
+        small = ret.abs() < 1e-8
+        ret = torch.where(small, torch.where(ret < 0, -1e-8, 1e-8) * torch.ones_like(ret), ret)
+    elif abs(ret) < 1e-8:
+        ret = math.copysign(1e-8, ret)
+    return ret
+
+
+def random_rotations(n, gen):
+    """n uniform SO(3) rotation matrices (uniform unit quaternions)."""
+    q = torch.randn(n, 4, generator=gen, dtype=torch.float64)
+    q = q / q.norm(dim=1, keepdim=True)
+    w, x, y, z = q.unbind(1)
+    R = torch.stack([
+        1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w),
+        2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w),
+        2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)], dim=1)
+    return R.view(n, 3, 3)
+
+
+class GaussianVolume:
+    """Sum of isotropic Gaussians; analytic Fourier transform (cycles/pixel)."""
+
+    def __init__(self, n_blobs, sigma, radius, gen, device="cpu"):
+        c = []
+        while sum(len(x) for x in c) < n_blobs:
+            p = (torch.rand(4 * n_blobs, 3, generator=gen, dtype=torch.float64) * 2 - 1) * radius
+            c.append(p[p.norm(dim=1) <= radius])
+        self.centers = torch.cat(c)[:n_blobs].to(device)
+        self.amps = (0.5 + torch.rand(n_blobs, generator=gen, dtype=torch.float64)).to(device)
+        self.sigma = sigma
+        self.device = device
+
+    def ft(self, k, chunk=1 << 15):
+        """F(k) for k [..., 3] in cycles/pixel -> complex128 [...]."""
+        shp = k.shape[:-1]
+        k = k.reshape(-1, 3).to(self.device)
+        out = torch.empty(k.shape[0], dtype=torch.complex128, device=self.device)
+        env_c = -2.0 * math.pi ** 2 * self.sigma ** 2
+        for i in range(0, k.shape[0], chunk):
+            kk = k[i:i + chunk]
+            ph = -2.0 * math.pi * (kk @ self.centers.T)           # [m, B]
+            s = torch.polar(self.amps.expand_as(ph).contiguous(), ph).sum(1)
+            out[i:i + chunk] = s * torch.exp(env_c * (kk * kk).sum(1))
+        return out.reshape(shp)
+
+    def ft_grid_separable(self, xs, ys, zs):
+        """F on the tensor grid zs x ys x xs (1D frequency vectors, cycles/px)."""
+        env_c = -2.0 * math.pi ** 2 * self.sigma ** 2
+
+        def axis(v, c):  # [B, n]
+            return torch.polar(torch.exp(env_c * v * v)[None, :].expand(len(c), -1).contiguous(),
+                               -2.0 * math.pi * c[:, None] * v[None, :])
+        gx = axis(xs.to(self.device), self.centers[:, 0])
+        gy = axis(ys.to(self.device), self.centers[:, 1])
+        gz = axis(zs.to(self.device), self.centers[:, 2])
+        a = self.amps.to(torch.complex128)[:, None]
+        m = (gy[:, :, None] * gx[:, None, :]).reshape(len(a), -1)  # [B, y*x]
+        v = (gz * a).T @ m                                          # [z, y*x]
+        return v.reshape(len(zs), len(ys), len(xs))
+
+
+def padded_reference(vol, box, pixel, r_max, pad, lowpass_A):
+    """Projector::data layout (src/projector.cpp:59-90): complex64 [z][y][x],
+    logical origin x=0, y=yinit, z=zinit; zero beyond ROUND(pad*r_max)."""
+    pad_size = 2 * (iround(pad * r_max) + 1) + 1
+    xdim = pad_size // 2 + 1
+    yinit = -(pad_size // 2)
+    xs = torch.arange(xdim, dtype=torch.float64)
+    ys = torch.arange(pad_size, dtype=torch.float64) + yinit
+    zs = ys.clone()
+    f = 1.0 / (pad * box)
+    data = vol.ft_grid_separable(xs * f, ys * f, zs * f).cpu()
+    r2 = xs[None, None, :] ** 2 + ys[None, :, None] ** 2 + zs[:, None, None] ** 2
+    max_r2 = iround(r_max * pad) ** 2
+    kA = torch.sqrt(r2) * f / pixel     # 1/Angstrom
+    fc = 1.0 / lowpass_A
+    w = torch.clamp((1.1 * fc - kA) / (0.2 * fc), 0.0, 1.0)
+    lp = 0.5 - 0.5 * torch.cos(math.pi * w)
+    data = data * lp * (r2 <= max_r2)
+    return dict(data=data.to(torch.complex64).numpy(), yinit=yinit, zinit=yinit, r_max=r_max,
+                pad=pad, xdim=xdim, ydim=pad_size, zdim=pad_size)
+
+
+def fourier_grid(size):
+    """Logical (x, y) of the [size][size/2+1] FFTW half layout."""
+    X = size // 2 + 1
+    i = torch.arange(size, dtype=torch.float64)
+    y = torch.where(i < X, i, i - size)
+    x = torch.arange(X, dtype=torch.float64)
+    return x[None, :].expand(size, X), y[:, None].expand(size, X)
+
+
+class Dataset:
+    """Seeded synthetic E-step problem for one configuration."""
+
+    def __init__(self, cfg, seed=0, n_particles=None, device="cpu", healpix_order=None,
+                 psi_step=None, offset_range_px=None, offset_step_px=None):
+        c = dict(CONFIGS[cfg]) if isinstance(cfg, str) else dict(cfg)
+        if healpix_order is not None:
+            c["healpix_order"] = healpix_order
+        if psi_step is not None:
+            c["psi_step"] = psi_step
+        if offset_range_px is not None:
+            c["offset_range_px"] = offset_range_px
+        if offset_step_px is not None:
+            c["offset_step_px"] = offset_step_px
+        self.cfg = c
+        self.seed = seed
+        self.device = device
+        self.gen = torch.Generator().manual_seed(seed)
+        self.n = int(n_particles if n_particles is not None else c["n_particles"])
+        box, pix = c["box"], c["pixel"]
+        self.current, self.coarse = estep_sizes(box, pix, c["ini_high"], c["healpix_order"], c["diameter"])
+        self.vol = GaussianVolume(c["n_blobs"], c["blob_sigma"], c["blob_radius"], self.gen, device)
+        self.r_max = min(self.current // 2, box // 2)
+        self.ref = padded_reference(self.vol, box, pix, self.r_max, 2, c["ini_high"])
+        self.sigma2 = None
+
+    def model(self, precision=0):
+        c = self.cfg
+        box, pix = c["box"], c["pixel"]
+        ndir = 12 * 4 ** c["healpix_order"]
+        K = c["classes"]
+        if self.sigma2 is None:
+            self._noise_level()
+        return dict(
+            ori_size=box, nr_classes=K, current_size=self.current, coarse_size=self.coarse,
+            padding_factor=2, healpix_order=c["healpix_order"], adaptive_oversampling=1,
+            maximum_significants=-1, sigma2_len=box // 2 + 1, do_scale_correction=0,
+            do_norm_correction=0, do_map=1, precision=precision, pixel_size=pix,
+            psi_step=c["psi_step"], offset_range=c["offset_range_px"] * pix,
+            offset_step=c["offset_step_px"] * pix, adaptive_fraction=0.999, sigma2_fudge=1.0,
+            sigma2_offset=100.0, avg_norm_correction=1.0,
+            sigma2_noise=np.full(box // 2 + 1, self.sigma2), pdf_class=np.full(K, 1.0 / K),
+            pdf_direction=np.full(K * ndir, 1.0 / (K * ndir)))
+
+    def _noise_level(self):
+        """sigma^2 per complex Fourier coefficient for the configured SNR,
+        from the mean signal power over full-size images of a few poses."""
+        box = self.cfg["box"]
+        g = torch.Generator().manual_seed(self.seed + 7)
+        R = random_rotations(4, g)
+        x, y = fourier_grid(box)
+        k2 = torch.stack([x, y, torch.zeros_like(x)], -1) / box
+        p = 0.0
+        for i in range(4):
+            k3 = k2 @ R[i]          # A^T (x, y, 0): row vector times A
+            f = self.vol.ft(k3)
+            p += float((f.abs() ** 2).mean()) / 4
+        self.signal_power = p
+        self.sigma2 = p / self.cfg["snr"]
+
+    def particles(self, start=0, count=None):
+        """Particle batch [start, start+count) as host numpy arrays (E-step
+        inputs at the current size) plus the true poses."""
+        c = self.cfg
+        if self.sigma2 is None:
+            self._noise_level()
+        count = self.n - start if count is None else count
+        box, pix, cur = c["box"], c["pixel"], self.current
+        g = torch.Generator().manual_seed(self.seed * 1000003 + start)
+        R = random_rotations(count, g)
+        shifts = (torch.rand(count, 2, generator=g, dtype=torch.float64) * 2 - 1) * c["max_shift"]
+        dlo, dhi = c["defocus"]
+        dU = dlo + (dhi - dlo) * torch.rand(count, generator=g, dtype=torch.float64)
+        dV = dlo + (dhi - dlo) * torch.rand(count, generator=g, dtype=torch.float64)
+        dA = 180.0 * torch.rand(count, generator=g, dtype=torch.float64)
+        x, y = fourier_grid(cur)
+        k2 = torch.stack([x, y, torch.zeros_like(x)], -1) / box
+        X = cur // 2 + 1
+        fimg = np.zeros((count, cur, X), np.complex64)
+        fctf = np.zeros((count, cur, X), np.float32)
+        s = math.sqrt(self.sigma2 / 2)
+        for i in range(count):
+            f = self.vol.ft(k2 @ R[i]).cpu()
+            ctf = ctf_value(float(dU[i]), float(dV[i]), float(dA[i]), x / (box * pix), y / (box * pix))
+            ph = torch.exp(-2j * math.pi * (x * shifts[i, 0] + y * shifts[i, 1]) / box)
+            noise = torch.complex(torch.randn(cur, X, generator=g, dtype=torch.float64),
+                                  torch.randn(cur, X, generator=g, dtype=torch.float64)) * s
+            fimg[i] = (f * ctf * ph + noise).numpy()
+            fctf[i] = ctf.numpy()
+        half = box // 2 + 1
+        # power beyond the current size: expected noise power per shell
+        shell_cnt = np.zeros(half)
+        xx, yy = fourier_grid(box)
+        r = torch.round(torch.sqrt(xx ** 2 + yy ** 2)).long().numpy().ravel()
+        ok = (r < half) & ~((xx.numpy().ravel() == 0) & (yy.numpy().ravel() < 0))
+        np.add.at(shell_cnt, r[ok], 1)
+        power = np.tile(shell_cnt * self.sigma2, (count, 1))
+        beyond = shell_cnt[cur // 2 + 1:].sum()
+        return dict(
+            n=count, fimg=fimg, fimg_nomask=fimg.copy(), fctf=fctf, power_img=power,
+            old_offset=np.zeros((count, 2)), prior=np.zeros((count, 2)),
+            highres_Xi2=np.full(count, beyond * 0.5), norm_correction=np.ones(count),
+            scale=np.ones(count), true_rot=R.numpy(), true_shift=shifts.numpy(),
+            defocus=np.stack([dU.numpy(), dV.numpy(), dA.numpy()], 1))

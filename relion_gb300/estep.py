@@ -1,0 +1,193 @@
+"""Python mirror of the reference's accelerated E-step surface.
+
+The reference drives its GPU E-step through MlDeviceBundle (per device:
+projectors, backprojectors, coarse projection plans) and MlOptimiserCuda
+(per host thread: doThreadExpectationSomeParticles), see
+src/acc/cuda/cuda_ml_optimiser.h:18-146 and src/ml_optimiser.cpp:3575-3868.
+These classes keep those names and call libgbrelion's C ABI; the parity
+tests and bench.py use them.  Every computation happens in the CUDA
+library: there is no Python or CPU fallback.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import check, ptr
+
+
+class MlDeviceBundle:
+    """Device state of one iteration: model, pose grid, projector/backprojector.
+
+    `model` is a dict with the gbr_model_desc fields plus the arrays
+    sigma2_noise, pdf_class, pdf_direction (and data_vs_prior for --scale).
+    """
+
+    def __init__(self, model, device=0):
+        self.lib = _lib.load()
+        d = _lib.ModelDesc()
+        for name, _ in _lib.ModelDesc._fields_:
+            if name in model:
+                setattr(d, name, model[name])
+        self.desc = d
+        h = C.c_void_p()
+        check(self.lib.gbr_bundle_create(C.byref(d), int(device), C.byref(h)))
+        self.h = h
+        sz = [C.c_int64() for _ in range(5)]
+        check(self.lib.gbr_sampling_sizes(h, *[C.byref(s) for s in sz]))
+        self.ndir, self.npsi, self.ntrans, self.nover_rot, self.nover_trans = [s.value for s in sz]
+        self.nr_classes = int(model["nr_classes"])
+        self.ori_size = int(model["ori_size"])
+        self._keep = []
+        s2 = _lib.as_f64(model["sigma2_noise"])
+        pc = _lib.as_f64(model["pdf_class"])
+        pdir = _lib.as_f64(model["pdf_direction"])
+        dvp = model.get("data_vs_prior")
+        dvp = _lib.as_f64(dvp) if dvp is not None else None
+        check(self.lib.gbr_model_set_arrays(h, ptr(s2), ptr(pc), ptr(pdir), ptr(dvp)))
+
+    # AccProjector::setMdlDim + initMdl
+    def setup_projector(self, iclass, data, yinit, zinit, r_max, padding_factor):
+        data = np.ascontiguousarray(data, dtype=np.complex64)
+        zdim, ydim, xdim = data.shape
+        check(self.lib.gbr_projector_upload(self.h, int(iclass), data.ctypes.data, xdim, ydim, zdim,
+                                            int(yinit), int(zinit), int(r_max), int(padding_factor)))
+
+    def reserve(self, nbytes):
+        check(self.lib.gbr_bundle_reserve(self.h, int(nbytes)))
+
+    def backprojector_dims(self):
+        v = [C.c_int64() for _ in range(6)]
+        check(self.lib.gbr_backprojector_dims(self.h, *[C.byref(x) for x in v]))
+        return [x.value for x in v]
+
+    # AccBackprojector::getMdlData
+    def get_mdl_data(self, iclass):
+        xd, yd, zd, _, _, _ = self.backprojector_dims()
+        data = np.zeros((zd, yd, xd), dtype=np.complex128)
+        weight = np.zeros((zd, yd, xd), dtype=np.float64)
+        check(self.lib.gbr_backprojector_download(self.h, int(iclass), data.ctypes.data, weight.ctypes.data))
+        return data, weight
+
+    def get_wsum(self):
+        s2 = np.zeros(self.ori_size // 2 + 1)
+        pc = np.zeros(self.nr_classes)
+        pdir = np.zeros(self.nr_classes * self.ndir)
+        w = _lib.Wsum()
+        w.sigma2_noise, w.pdf_class, w.pdf_direction = ptr(s2), ptr(pc), ptr(pdir)
+        check(self.lib.gbr_wsum_download(self.h, C.byref(w)))
+        out = {k: getattr(w, k) for k, _ in _lib.Wsum._fields_[3:] if k != "reserved_"}
+        out.update(sigma2_noise=s2, pdf_class=pc, pdf_direction=pdir.reshape(self.nr_classes, self.ndir))
+        return out
+
+    def reset_wsum(self):
+        check(self.lib.gbr_bundle_reset_wsum(self.h))
+
+    def close(self):
+        if self.h:
+            self.lib.gbr_bundle_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+RESULT_FIELDS = [n for n, _ in _lib.ParticleResult._fields_]
+
+
+class MlOptimiserCuda:
+    """One E-step worker (stream + batch buffers) on a bundle."""
+
+    def __init__(self, bundle, debug=False):
+        self.bundle = bundle
+        self.lib = bundle.lib
+        h = C.c_void_p()
+        check(self.lib.gbr_worker_create(bundle.h, C.byref(h)))
+        self.h = h
+        if debug:
+            check(self.lib.gbr_worker_set_debug(h, 1))
+
+    def do_expectation_some_particles(self, batch):
+        """Run the E-step on a batch (dict of host arrays, or device pointers).
+
+        Host batch keys: fimg, fimg_nomask (complex [n][cur][cur/2+1]), fctf
+        (float [n][cur][cur/2+1]), power_img [n][ori/2+1], old_offset [n][2],
+        prior [n][2], highres_Xi2 [n], norm_correction [n], scale [n].
+        Returns a structured numpy array of gbr_particle_result rows.
+        """
+        n = int(batch["n"]) if "n" in batch else len(batch["fimg"])
+        b = _lib.ParticleBatch()
+        b.n = n
+        keep = []
+        if batch.get("device_resident"):
+            b.device_resident = 1
+            for k in ("fimg", "fimg_nomask", "fctf", "power_img", "old_offset", "prior",
+                      "highres_Xi2", "norm_correction", "scale"):
+                setattr(b, k, int(batch[k]))
+        else:
+            def f32c(a):
+                a = np.ascontiguousarray(a, dtype=np.complex64)
+                keep.append(a)
+                return a.ctypes.data
+
+            def arr(a, dt):
+                a = np.ascontiguousarray(a, dtype=dt)
+                keep.append(a)
+                return a.ctypes.data
+            b.fimg = f32c(batch["fimg"])
+            b.fimg_nomask = f32c(batch["fimg_nomask"])
+            b.fctf = arr(batch["fctf"], np.float32)
+            for k in ("power_img", "old_offset", "prior", "highres_Xi2", "norm_correction", "scale"):
+                setattr(b, k, arr(batch[k], np.float64))
+        res = (_lib.ParticleResult * n)()
+        check(self.lib.gbr_expect_batch(self.h, C.byref(b), res))
+        out = np.zeros(n, dtype=[(f, np.float64) for f in RESULT_FIELDS])
+        for i in range(n):
+            for f in RESULT_FIELDS:
+                out[f][i] = getattr(res[i], f)
+        return out
+
+    def debug_fetch(self, what, i):
+        cap = self.bundle.nr_classes * self.bundle.ndir * self.bundle.npsi * self.bundle.ntrans * \
+            self.bundle.nover_rot * self.bundle.nover_trans
+        buf = np.zeros(cap, dtype=np.int64 if what == 2 else np.float64)
+        m = self.lib.gbr_worker_debug_fetch(self.h, int(what), int(i), buf.ctypes.data, cap)
+        check(m)
+        return buf[:m].copy()
+
+    def stage_times(self):
+        ms = np.zeros(16)
+        n = C.c_int64()
+        check(self.lib.gbr_worker_stage_times(self.h, ms.ctypes.data, 16, C.byref(n)))
+        return ms[:n.value]
+
+    def launch_count(self):
+        n = C.c_int64()
+        check(self.lib.gbr_worker_launch_count(self.h, C.byref(n)))
+        return n.value
+
+    def close(self):
+        if self.h:
+            self.lib.gbr_worker_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+STAGES = ["prep", "norm_gemm", "cross_gemm", "weights_coarse", "jobs_proj_fine", "diff2_fine",
+          "weights_fine", "wsum", "backproject", "readback"]
+
+
+def measure_fp32_peak(device=0):
+    """Measured FP32 FMA throughput of the device in TFLOP/s."""
+    lib = _lib.load()
+    v = C.c_double()
+    check(lib.gbr_measure_fp32_peak(int(device), C.byref(v)))
+    return v.value
