@@ -1,0 +1,320 @@
+"""E-step throughput benchmark (particles/s) on the box-256 configuration.
+
+Workload: relion_refine's expectation step (coarse search, significance,
+fine search, weighted sums, backprojection) on synthetic particles of the
+"plain GPU vs reference CPU at production size" configuration: box 256 px,
+1.0 A/px, 5,000-Gaussian volume in a 90 px radius, defocus 0.8-2.5 um,
+SNR 0.03, initial reference low-passed to 20 A (first iteration: current
+size 46 px), HEALPix order 3 (768 directions x 48 psi), offsets +/-6 px
+step 1 (113 translations), oversampling 1, one class, C1.
+
+A step is one E-step call on a batch of --batch particles.  `value` uses
+inputs already resident in HBM; `e2e` calls the same C-ABI entry point with
+pinned host buffers (host->device copies inside the timed region).  The L2
+cache is flushed (a 512 MB write) before every timed step.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--batch B] [--impl reference]
+
+With torchrun (N > 1) each rank runs an independent replica on its own GPU
+("replicas only": particles are independent; no collective on the data
+path); rank 0 prints the aggregate.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "E-step particles/s @box256, 1 GB300: learned+batched vs plain GPU at equal FSC"
+CONFIG = "cfg1_box256"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--batch", type=int, default=256)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def run_ours(args, world, rank, local):
+    import torch
+    from relion_gb300 import datagen
+    from relion_gb300.estep import MlDeviceBundle, MlOptimiserCuda, STAGES, measure_fp32_peak
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    B = args.batch
+    ds = datagen.Dataset(CONFIG, seed=args.seed + rank, n_particles=B, device=str(dev))
+    model = ds.model()
+    batch = ds.particles(0, B)
+    bundle = MlDeviceBundle(model, device=local)
+    r = ds.ref
+    bundle.setup_projector(0, r["data"], r["yinit"], r["zinit"], r["r_max"], r["pad"])
+    bundle.reserve(64 << 30)
+    worker = MlOptimiserCuda(bundle)
+
+    # device-resident copy of the batch (for `value`) and pinned host copy (for `e2e`)
+    keys = ("fimg", "fimg_nomask", "fctf", "power_img", "old_offset", "prior", "highres_Xi2",
+            "norm_correction", "scale")
+    dtypes = dict(fimg=torch.complex64, fimg_nomask=torch.complex64, fctf=torch.float32)
+    dev_t, pin = {}, {}
+    for k in keys:
+        t = torch.from_numpy(np.ascontiguousarray(batch[k])).to(dtypes.get(k, torch.float64))
+        pin[k] = t.pin_memory()
+        dev_t[k] = t.to(dev)
+    dev_batch = {"n": B, "device_resident": 1}
+    dev_batch.update({k: v.data_ptr() for k, v in dev_t.items()})
+    host_batch = {"n": B}
+    host_batch.update({k: v.numpy() for k, v in pin.items()})
+    h2d = sum(pin[k].numel() * pin[k].element_size() for k in keys)
+
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        worker.do_expectation_some_particles(dev_batch)
+    torch.cuda.synchronize()
+
+    # ---- value: device-resident inputs, per-step device time (CUDA events
+    # on the library's stream, summed over the stages of each call) ----
+    stage0 = worker.stage_times().copy()
+    launches0 = worker.launch_count()
+    barrier()
+    torch.cuda.synchronize()
+    step_ms = []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            before = worker.stage_times().sum()
+            res = worker.do_expectation_some_particles(dev_batch)
+            step_ms.append(worker.stage_times().sum() - before)
+        torch.cuda.synchronize()
+    barrier()
+    stage = (worker.stage_times() - stage0) / args.steps
+    launches = (worker.launch_count() - launches0) // args.steps
+    total_ms = float(sum(step_ms))
+
+    # ---- e2e: host (pinned) buffers through the same C-ABI call ----
+    e2e_ms = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record()
+        worker.do_expectation_some_particles(host_batch)
+        ev1.record()
+        ev1.synchronize()
+        e2e_ms.append(ev0.elapsed_time(ev1))
+    e2e_total = float(sum(e2e_ms))
+
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([total_ms, e2e_total], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms, e2e_total = float(t[0]), float(t[1])
+
+    # ---- roofline of the dominant kernel: the coarse cross-term GEMM ----
+    R = bundle.nr_classes * bundle.ndir * bundle.npsi
+    T = bundle.ntrans
+    nc = active_coarse_pixels(model)
+    flops = 2.0 * R * (B * T) * (2 * nc)
+    cross_ms = float(stage[STAGES.index("cross_gemm")])
+    peak = measure_fp32_peak(local)
+    achieved = flops / (cross_ms * 1e-3) / 1e12
+    d2h = B * (96 + (model["ori_size"] // 2 + 1) * 8 + 64) + (R + 2) * 8
+    out = {
+        "metric": METRIC,
+        "value": world * B * args.steps / (total_ms * 1e-3),
+        "unit": "particles/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "fp32",
+        "data": "synthetic (seeded Gaussian-blob volume, analytic Fourier slices, CTF, white noise)",
+        "config": {"workload": "box256 E-step, iteration-1 sizes (current 46 px), HEALPix order 3 x 48 psi, "
+                               "113 translations, oversampling 1, 1 class",
+                   "batch_particles": B, "precision": "plain FP32 path",
+                   "l2": "flushed (512 MB write) before every timed step",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "e2e": {"value": world * B * args.steps / (e2e_total * 1e-3), "unit": "particles/s",
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "fp32", "kernel": "coarse cross-term GEMM (k_gemm<RowsK,CrossY,Diff2Epi>)",
+                     "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                     "peak_source": "measured live (gbr_measure_fp32_peak: FMA chains on all SMs)",
+                     "traffic": None},
+        "stage_ms": {k: round(float(v), 4) for k, v in zip(STAGES, stage)},
+        "mean_nr_sign": float(np.mean(res["nr_sign"])),
+        "mean_fine_poses": float(np.mean(res["n_fine"])),
+    }
+    if rank == 0:
+        out["clocks"] = clk.summary()
+    return out, ds, batch, model
+
+
+def active_coarse_pixels(model):
+    """Coarse pixels with a non-zero noise weight (the K of the cross term / 2)."""
+    s = model["coarse_size"]
+    X = s // 2 + 1
+    n = 0
+    for i in range(s):
+        y = i if i < X else i - s
+        for x in range(X):
+            r = int(np.sqrt(x * x + y * y) + 0.5)
+            if r < s // 2 + 1 and not (x == 0 and y < 0) and 0 < r < model["sigma2_len"]:
+                n += 1
+    return n
+
+
+def cpu_particles_per_s(ds, batch, model, n_particles, threads):
+    """Oracle (CPU restatement of the reference's CPU E-step) on n particles."""
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    from oracle import build as obuild
+    obuild.build()
+    from oracle import pyoracle
+    sub = {k: (v[:n_particles] if isinstance(v, np.ndarray) else v) for k, v in batch.items()}
+    sub["n"] = n_particles
+    t0 = time.perf_counter()
+    pyoracle.run(model, [ds.ref], sub)
+    return n_particles / (time.perf_counter() - t0)
+
+
+def run_reference(args, world, rank):
+    """Reference arm: the reference's CPU path for this E-step, as restated
+    by the oracle (the reference's relion_refine needs FFTW, MPI and TIFF
+    and is not built here), on all host cores, same config and metric."""
+    if rank != 0:
+        return None
+    from relion_gb300 import datagen
+    cores = os.cpu_count() or 1
+    per_step = 2
+    ds = datagen.Dataset(CONFIG, seed=args.seed, n_particles=per_step)
+    model = ds.model()
+    batch = ds.particles(0, per_step)
+    for _ in range(args.warmup if args.warmup < 1 else 1):
+        cpu_particles_per_s(ds, batch, model, 1, cores)
+    t_total, n_total = 0.0, 0
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        cpu_particles_per_s(ds, batch, model, per_step, cores)
+        t_total += time.perf_counter() - t0
+        n_total += per_step
+    v = n_total / t_total
+    return {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "particles/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": {"workload": "box256 E-step (same as the GPU arm)",
+                                        "batch_particles": per_step},
+        "cpu_baseline": {"value": v, "unit": "particles/s", "cores": cores, "kind": "port",
+                         "sample": "%d particles per step, all host threads (OpenMP)" % per_step},
+        "e2e": {"value": v, "unit": "particles/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_setup()
+    if world > 1:
+        import torch.distributed as dist
+        backend = "gloo" if args.impl == "reference" else "nccl"
+        dist.init_process_group(backend=backend)
+    if args.impl == "reference":
+        out = run_reference(args, world, rank)
+        if out is not None:
+            print(json.dumps(out))
+        return
+    out, ds, batch, model = run_ours(args, world, rank, local)
+    if rank == 0:
+        if not args.no_cpu_baseline:
+            # bounded sample: one particle on one host thread (~10-30 s)
+            v = cpu_particles_per_s(ds, batch, model, 1, 1)
+            out["cpu_baseline"] = {"value": v, "unit": "particles/s", "cores": 1, "kind": "port",
+                                   "sample": "1 particle of the same batch, oracle on 1 host thread"}
+        print(json.dumps(out))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

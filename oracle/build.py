@@ -18,7 +18,7 @@ def build(force=False):
     hdr = os.path.join(HERE, "relion_oracle.h")
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(
             os.path.getmtime(src), os.path.getmtime(hdr)):
-        subprocess.run(["g++", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-std=c++17",
+        subprocess.run(["g++", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-std=c++17", "-fopenmp",
                         src, "-o", LIB + ".tmp"], check=True)
         os.replace(LIB + ".tmp", LIB)
     ref = os.environ.get("RELION_REFERENCE", "/root/reference")

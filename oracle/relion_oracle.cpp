@@ -620,49 +620,55 @@ int oracle_expectation(const oracle_model *mp, int64_t n, const oracle_particle 
             const long nW = R * NT * nor * not_;
             Mw.assign(nW, -999.);
             min_diff2 = 99e99;  // LARGE_NUMBER, src/macros.h:78
-            std::vector<Cplx> Fref(npix), Frefctf(npix);
-            std::vector<double> ro, ti, ps;
-            double A[9];
-            for (long ic = 0; ic < K; ++ic) {
-                if (!(m.pdf_class[ic] > 0.)) continue;
-                for (long id = 0; id < ND; ++id)
-                    for (long is = 0; is < NP; ++is) {
-                        long iorient = id * NP + is;
-                        long ioc = ic * ND * NP + iorient;
-                        double pdf_orient = m.pdf_direction[ic * ND + id];
-                        bool proceed = true;
-                        if (ipass > 0) {
-                            proceed = false;
-                            for (long it = 0; it < NT; ++it)
-                                if (coarse_sig[ioc * NT + it]) { proceed = true; break; }
+            // orientations are independent: threads split (class, direction,
+            // psi); each writes its own hidden indices and a private minimum
+            const long n_orient = K * ND * NP;
+#pragma omp parallel
+            {
+                std::vector<Cplx> Fref(npix), Frefctf(npix);
+                std::vector<double> ro, ti, ps;
+                double A[9];
+                double my_min = 99e99;
+#pragma omp for schedule(dynamic, 4)
+                for (long ioc = 0; ioc < n_orient; ++ioc) {
+                    const long ic = ioc / (ND * NP), id = (ioc / NP) % ND, is = ioc % NP;
+                    if (!(m.pdf_class[ic] > 0.)) continue;
+                    double pdf_orient = m.pdf_direction[ic * ND + id];
+                    bool proceed = true;
+                    if (ipass > 0) {
+                        proceed = false;
+                        for (long it = 0; it < NT; ++it)
+                            if (coarse_sig[ioc * NT + it]) { proceed = true; break; }
+                    }
+                    if (!(proceed && pdf_orient > 0.)) continue;
+                    S.orientations(id, is, cov, ro, ti, ps);
+                    for (long ior = 0; ior < nor; ++ior) {
+                        euler_matrix(ro[ior], ti[ior], ps[ior], A);
+                        project(m, ic, A, size, reinterpret_cast<Cplx *>(Fref.data()));
+                        for (long k = 0; k < npix; ++k) {
+                            Frefctf[k].re = Fref[k].re * Fctf[k] * myscale_d2;
+                            Frefctf[k].im = Fref[k].im * Fctf[k] * myscale_d2;
                         }
-                        if (!(proceed && pdf_orient > 0.)) continue;
-                        S.orientations(id, is, cov, ro, ti, ps);
-                        for (long ior = 0; ior < nor; ++ior) {
-                            euler_matrix(ro[ior], ti[ior], ps[ior], A);
-                            project(m, ic, A, size, reinterpret_cast<Cplx *>(Fref.data()));
-                            for (long k = 0; k < npix; ++k) {
-                                Frefctf[k].re = Fref[k].re * Fctf[k] * myscale_d2;
-                                Frefctf[k].im = Fref[k].im * Fctf[k] * myscale_d2;
-                            }
-                            for (long it = 0; it < NT; ++it) {
-                                long ihidden = ioc * NT + it;
-                                if (ipass > 0 && !coarse_sig[ihidden]) continue;
-                                for (long io = 0; io < not_; ++io) {
-                                    long iho = ipass == 0 ? ihidden : ihidden * nor * not_ + ior * not_ + io;
-                                    const Cplx *Fs = shifted[it * not_ + io].data();
-                                    double diff2 = P.highres_Xi2 / 2.;
-                                    for (long k = 0; k < npix; ++k) {
-                                        double dr = Frefctf[k].re - Fs[k].re;
-                                        double di = Frefctf[k].im - Fs[k].im;
-                                        diff2 += (dr * dr + di * di) * 0.5 * inv[k];
-                                    }
-                                    Mw[iho] = diff2;  // single image: first write
-                                    if (diff2 < min_diff2) min_diff2 = diff2;
+                        for (long it = 0; it < NT; ++it) {
+                            long ihidden = ioc * NT + it;
+                            if (ipass > 0 && !coarse_sig[ihidden]) continue;
+                            for (long io = 0; io < not_; ++io) {
+                                long iho = ipass == 0 ? ihidden : ihidden * nor * not_ + ior * not_ + io;
+                                const Cplx *Fs = shifted[it * not_ + io].data();
+                                double diff2 = P.highres_Xi2 / 2.;
+                                for (long k = 0; k < npix; ++k) {
+                                    double dr = Frefctf[k].re - Fs[k].re;
+                                    double di = Frefctf[k].im - Fs[k].im;
+                                    diff2 += (dr * dr + di * di) * 0.5 * inv[k];
                                 }
+                                Mw[iho] = diff2;  // single image: first write
+                                if (diff2 < my_min) my_min = diff2;
                             }
                         }
                     }
+                }
+#pragma omp critical
+                if (my_min < min_diff2) min_diff2 = my_min;
             }
             if (dbg) {
                 double *dst = ipass == 0 ? dbg[ip].coarse_diff2 : dbg[ip].fine_diff2;

@@ -133,8 +133,8 @@ struct gbr_bundle {
     std::vector<double> otx_h, oty_h;
     DevBuf<float2> phase_c, phase_f;
     DevBuf<float> proj_c, proj2_c;
-    DevBuf<float2> proj_f;
-    std::vector<unsigned char> proj_f_done;
+    DevBuf<float> proj_f, proj2_f;  // all oversampled orientations: [RF][lda_f], [RF][ldk_f]
+    int ldk_f = 0, lda_f = 0;
     DevBuf<float2> bpimg;
     DevBuf<float> bpw;
     DevBuf<unsigned char> active;
@@ -175,6 +175,11 @@ struct gbr_worker {
     DevBuf<int> ejob;
     DevBuf<unsigned int> ecode;
     DevBuf<double> shell, pacc;
+    // dense fine pass
+    int fine_mode = 0;  // 0: by significant density, 1: always dense, 2: always sparse
+    int last_dense = 0;
+    DevBuf<float> Wt, Wp, Zt, CM, S2P, fnrm;
+    DevBuf<float2> G;
     // debug copies of the last batch
     int dbg_n = 0;
     std::vector<float> dbg_coarse;   // relative diff2
@@ -321,9 +326,16 @@ int build_tables(gbr_bundle *b) {
     GBR_CUDA(b->proj2_c.zero());
     GBR_CUDA(launch_project_rows(b->vols_d.p, b->pg, b->eul_c.p, b->cls_c.p, nullptr, (int)R, b->pc.p, b->nc,
                                  b->proj_c.p, b->lda_c, b->proj2_c.p, b->ldk_c, nullptr, 0));
-    // ---- fine projection cache, slice accumulators ----
-    GBR_CUDA(b->proj_f.reserve((size_t)RF * b->nf));
-    b->proj_f_done.assign(RF, 0);
+    // ---- fine projections of every oversampled orientation ----
+    b->ldk_f = pad16(std::max(b->nf, 1));
+    b->lda_f = 2 * b->ldk_f;
+    GBR_CUDA(b->proj_f.reserve((size_t)RF * b->lda_f));
+    GBR_CUDA(b->proj2_f.reserve((size_t)RF * b->ldk_f));
+    GBR_CUDA(b->proj_f.zero());
+    GBR_CUDA(b->proj2_f.zero());
+    GBR_CUDA(launch_project_rows(b->vols_d.p, b->pg, b->eul_f.p, b->cls_f.p, nullptr, (int)RF, b->pf.p, b->nf,
+                                 b->proj_f.p, b->lda_f, b->proj2_f.p, b->ldk_f, nullptr, 0));
+    // ---- slice accumulators ----
     GBR_CUDA(b->bpimg.reserve((size_t)RF * b->nf));
     GBR_CUDA(b->bpw.reserve((size_t)RF * b->nf));
     GBR_CUDA(b->active.reserve(RF));
@@ -351,8 +363,8 @@ int ensure_capacity(gbr_worker *w, int n) {
     GBR_CUDA(w->power.reserve((size_t)n * b->nshell));
     GBR_CUDA(w->a_c.reserve((size_t)n * b->ldk_c));
     GBR_CUDA(w->b_c.reserve((size_t)n * b->ldk_c));
-    GBR_CUDA(w->a_f.reserve((size_t)n * b->nf));
-    GBR_CUDA(w->b_f.reserve((size_t)n * b->nf));
+    GBR_CUDA(w->a_f.reserve((size_t)n * b->ldk_f));
+    GBR_CUDA(w->b_f.reserve((size_t)n * b->ldk_f));
     GBR_CUDA(w->Xf.reserve((size_t)n * b->nf));
     GBR_CUDA(w->Xnf.reserve((size_t)n * b->nf));
     GBR_CUDA(w->Cf.reserve((size_t)n * b->nf));
@@ -394,6 +406,133 @@ int threshold_search(gbr_worker *w, int n, float *vals, const long long *seg, lo
     return GBR_OK;
 }
 
+// Fine pass over sparse jobs (few significant coarse poses): one block per
+// (particle, significant coarse orientation), weighted sums by atomics.
+int fine_sparse(gbr_worker *w, int n, long long njobs, long long nfine, const std::vector<long long> &segf,
+                long long &max_seg) {
+    gbr_bundle *b = w->b;
+    cudaStream_t st = w->st;
+    const int R = (int)b->R, T = (int)b->T, nOR = (int)b->nOR, nOT = (int)b->nOT, W = (T + 31) / 32;
+    max_seg = 0;
+    for (int p = 0; p < n; ++p) max_seg = std::max(max_seg, segf[p + 1] - segf[p]);
+    GBR_CUDA(w->fd.reserve(nfine));
+    GBR_CUDA(w->ejob.reserve(nfine));
+    GBR_CUDA(w->ecode.reserve(nfine));
+    GBR_CUDA(cudaEventRecord(w->ev[5], st));
+    const float2 *projf = reinterpret_cast<const float2 *>(b->proj_f.p);
+    GBR_CUDA(launch_fine_diff2(w->jobs.p, njobs, w->mask.p, R, T, W, nOR, nOT, projf, b->ldk_f, w->b_f.p, w->a_f.p,
+                               b->nf, b->phase_f.p, w->fd.p, w->ejob.p, w->ecode.p, w->ps.p, st));
+    GBR_CUDA(cudaEventRecord(w->ev[6], st));
+    if (w->debug) {
+        w->dbg_fine.resize(nfine);
+        w->dbg_ejob.resize(nfine);
+        w->dbg_ecode.resize(nfine);
+        w->dbg_jobs.resize(njobs);
+        GBR_CUDA(cudaMemcpyAsync(w->dbg_fine.data(), w->fd.p, sizeof(float) * nfine, cudaMemcpyDeviceToHost, st));
+        GBR_CUDA(cudaMemcpyAsync(w->dbg_ejob.data(), w->ejob.p, sizeof(int) * nfine, cudaMemcpyDeviceToHost, st));
+        GBR_CUDA(cudaMemcpyAsync(w->dbg_ecode.data(), w->ecode.p, sizeof(unsigned) * nfine, cudaMemcpyDeviceToHost, st));
+        GBR_CUDA(cudaMemcpyAsync(w->dbg_jobs.data(), w->jobs.p, sizeof(FineJob) * njobs, cudaMemcpyDeviceToHost, st));
+        w->dbg_segf = segf;
+    }
+    GBR_CUDA(launch_weights(w->fd.p, w->seg_f.p, n, max_seg, 0, T, w->ejob.p, w->ecode.p, w->jobs.p, nOR, nOT,
+                            b->pdf_orient.p, w->pdf_off.p, w->ps.p, w->hist.p, st));
+    int s = threshold_search(w, n, w->fd.p, w->seg_f.p, max_seg, 0);
+    if (s) return s;
+    GBR_CUDA(cudaEventRecord(w->ev[7], st));
+    if (w->debug) {
+        w->dbg_wfine.resize(nfine);
+        GBR_CUDA(cudaMemcpyAsync(w->dbg_wfine.data(), w->fd.p, sizeof(float) * nfine, cudaMemcpyDeviceToHost, st));
+    }
+    WsumArgs wa{};
+    wa.jobs = w->jobs.p;
+    wa.njobs = njobs;
+    wa.mask = w->mask.p;
+    wa.R = R; wa.T = T; wa.W = W; wa.nOR = nOR; wa.nOT = nOT; wa.nf = b->nf; wa.ldpf = b->ldk_f;
+    wa.nshell = b->nshell; wa.ndir = (int)b->ND; wa.npsi = (int)b->NP; wa.K = (int)b->K;
+    wa.w = w->fd.p;
+    wa.ps = w->ps.p;
+    wa.projf = projf;
+    wa.Xf = w->Xf.p; wa.Xnf = w->Xnf.p; wa.Cf = w->Cf.p;
+    wa.minv_store = b->minv_store.p;
+    wa.pf = b->pf.p;
+    wa.phase_f = b->phase_f.p;
+    wa.otx = b->otx.p; wa.oty = b->oty.p;
+    wa.pdat = w->pdat.p;
+    wa.pixel = b->d.pixel_size;
+    wa.do_scale = (int)b->d.do_scale_correction;
+    wa.dvp_mask = b->dvp_mask.p;
+    wa.bpimg = b->bpimg.p; wa.bpw = b->bpw.p; wa.active = b->active.p;
+    wa.shell = w->shell.p; wa.pacc = w->pacc.p;
+    wa.pdf_dir = b->w_pdf_dir.p; wa.pdf_cls = b->w_pdf_cls.p;
+    GBR_CUDA(launch_wsum(wa, st));
+    w->launches += 3;
+    return GBR_OK;
+}
+
+// Fine pass over every oversampled pose (most coarse poses significant):
+// fine diff2 and the weighted sums as dense contractions.
+int fine_dense(gbr_worker *w, int n, long long &seg_len) {
+    gbr_bundle *b = w->b;
+    cudaStream_t st = w->st;
+    const int R = (int)b->R, T = (int)b->T, nOR = (int)b->nOR, nOT = (int)b->nOT, W = (T + 31) / 32;
+    const int RF = (int)b->RF, TF = (int)b->TF, nf = b->nf;
+    const long long per = (long long)RF * TF;
+    seg_len = per;
+    GBR_CUDA(w->fd.reserve((size_t)n * per));
+    GBR_CUDA(w->fnrm.reserve((size_t)n * RF));
+    std::vector<long long> seg(n + 1);
+    for (int p = 0; p <= n; ++p) seg[p] = (long long)p * per;
+    GBR_CUDA(cudaMemcpyAsync(w->seg_f.p, seg.data(), sizeof(long long) * (n + 1), cudaMemcpyHostToDevice, st));
+    GBR_CUDA(cudaEventRecord(w->ev[5], st));
+    // fine norm term N_f[p][rf] and masked dense diff2 [p][rf][tf]
+    GBR_CUDA(launch_gemm_rows(b->proj2_f.p, b->ldk_f, RF, w->a_f.p, b->ldk_f, n, b->ldk_f, w->fnrm.p, RF, 1, st));
+    GBR_CUDA(launch_gemm_diff2(b->proj_f.p, b->lda_f, RF, 2 * nf, w->b_f.p, b->ldk_f, b->phase_f.p, nf, n, TF,
+                               w->fd.p, w->fnrm.p, b->pdf_orient.p, w->mask.p, nOR, nOT, W, w->ps.p, 1, st));
+    GBR_CUDA(cudaEventRecord(w->ev[6], st));
+    if (w->debug) {
+        w->dbg_fine.resize((size_t)n * per);
+        GBR_CUDA(cudaMemcpyAsync(w->dbg_fine.data(), w->fd.p, sizeof(float) * n * per, cudaMemcpyDeviceToHost, st));
+        w->dbg_segf = seg;
+    }
+    GBR_CUDA(launch_weights(w->fd.p, w->seg_f.p, n, per, 2, T, nullptr, nullptr, nullptr, nOR, nOT,
+                            b->pdf_orient.p, w->pdf_off.p, w->ps.p, w->hist.p, st));
+    int s = threshold_search(w, n, w->fd.p, w->seg_f.p, per, 0);
+    if (s) return s;
+    GBR_CUDA(cudaEventRecord(w->ev[7], st));
+    if (w->debug) {
+        w->dbg_wfine.resize((size_t)n * per);
+        GBR_CUDA(cudaMemcpyAsync(w->dbg_wfine.data(), w->fd.p, sizeof(float) * n * per, cudaMemcpyDeviceToHost, st));
+    }
+    // normalised weights, row sums, scalar sums
+    const int ldwt = pad16(n);
+    const long long ldz = pad16(n * TF);
+    GBR_CUDA(w->Wt.reserve((size_t)RF * ldwt));
+    const int ldwp = pad16(RF);
+    GBR_CUDA(w->Wp.reserve((size_t)n * ldwp));
+    GBR_CUDA(cudaMemsetAsync(w->Wp.p, 0, sizeof(float) * n * ldwp, st));
+    GBR_CUDA(w->Zt.reserve((size_t)2 * nf * ldz));
+    GBR_CUDA(w->CM.reserve((size_t)nf * ldwt));
+    GBR_CUDA(w->G.reserve((size_t)n * nf));
+    GBR_CUDA(w->S2P.reserve((size_t)n * nf));
+    GBR_CUDA(cudaMemsetAsync(w->Wt.p, 0, sizeof(float) * RF * ldwt, st));
+    GBR_CUDA(cudaMemsetAsync(w->G.p, 0, sizeof(float2) * n * nf, st));
+    GBR_CUDA(launch_fine_normalize(w->fd.p, n, R, nOR, nOT, T, w->ps.p, w->pdat.p, b->otx.p, b->oty.p,
+                                   b->d.pixel_size, (int)b->ND, (int)b->NP, w->Wt.p, ldwt, w->Wp.p, ldwp, b->active.p,
+                                   w->pacc.p, b->w_pdf_dir.p, b->w_pdf_cls.p, st));
+    // BP slices and weights (batch-summed), sigma2 contractions (per particle)
+    GBR_CUDA(launch_make_zt(w->Cf.p, w->Xnf.p, b->minv_store.p, b->phase_f.p, w->pdat.p,
+                            (int)b->d.do_scale_correction, n, TF, nf, w->Zt.p, ldz, w->CM.p, ldwt, st));
+    GBR_CUDA(launch_gemm_bpimg(w->fd.p, RF, TF, n, w->Zt.p, ldz, 2 * nf, reinterpret_cast<float *>(b->bpimg.p),
+                               2 * nf, st));
+    GBR_CUDA(launch_gemm_rows(w->Wt.p, ldwt, RF, w->CM.p, ldwt, nf, ldwt, b->bpw.p, nf, 0, st));
+    GBR_CUDA(launch_gemm_sigma_cross(w->fd.p, RF, TF, n, b->proj_f.p, b->lda_f, nf, b->phase_f.p, w->G.p, st));
+    GBR_CUDA(launch_gemm_sigma_norm(w->Wp.p, ldwp, n, RF, b->proj2_f.p, b->ldk_f, nf, w->S2P.p, st));
+    GBR_CUDA(launch_shell_dense(n, w->S2P.p, w->G.p, w->Xf.p, w->Cf.p, b->pf.p, nf, b->nshell, w->pdat.p,
+                                (int)b->d.do_scale_correction, b->dvp_mask.p, (int)b->K, w->pacc.p, w->shell.p, st));
+    w->launches += 11;
+    return GBR_OK;
+}
+
 // One sub-batch of n <= cap particles whose inputs are already in w->X etc.
 int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h, gbr_particle_result *res) {
     gbr_bundle *b = w->b;
@@ -405,18 +544,17 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
     GBR_CUDA(cudaEventRecord(w->ev[0], st));
     // ---- prep ----
     GBR_CUDA(launch_prep(w->X.p, w->C.p, w->pdat.p, n, b->full_npix, b->pc.p, b->nc, b->minv_c.p, b->ldk_c,
-                         b->pf.p, b->nf, b->minv_f.p, w->a_c.p, w->b_c.p, w->a_f.p, w->b_f.p, w->Xf.p,
+                         b->pf.p, b->nf, b->ldk_f, b->minv_f.p, w->a_c.p, w->b_c.p, w->a_f.p, w->b_f.p, w->Xf.p,
                          w->Xnf.p, w->Cf.p, w->Xn.p, (int)d.do_scale_correction, w->ps.p, st));
     GBR_CUDA(launch_pdf_offset(w->pdat.p, n, b->tx.p, b->ty.p, T, d.sigma2_offset, d.pixel_size, w->pdf_off.p, st));
     GBR_CUDA(cudaMemsetAsync(w->shell.p, 0, sizeof(double) * n * b->nshell, st));
     GBR_CUDA(cudaMemsetAsync(w->pacc.p, 0, sizeof(double) * n * 8, st));
     GBR_CUDA(cudaEventRecord(w->ev[1], st));
     // ---- coarse norm and cross GEMMs ----
-    GBR_CUDA(launch_gemm_norm(b->proj2_c.p, b->ldk_c, R, b->ldk_c, w->a_c.p, b->ldk_c, n, w->nrm.p, st));
+    GBR_CUDA(launch_gemm_rows(b->proj2_c.p, b->ldk_c, R, w->a_c.p, b->ldk_c, n, b->ldk_c, w->nrm.p, R, 1, st));
     GBR_CUDA(cudaEventRecord(w->ev[2], st));
-    CrossEpilogue ep{w->vals.p, w->nrm.p, b->pdf_orient.p, w->ps.p, T, RT};
-    GBR_CUDA(launch_gemm_cross(b->proj_c.p, b->lda_c, R, 2 * b->nc, w->b_c.p, b->ldk_c, b->phase_c.p, b->ldk_c,
-                               n, T, ep, st));
+    GBR_CUDA(launch_gemm_diff2(b->proj_c.p, b->lda_c, R, 2 * b->nc, w->b_c.p, b->ldk_c, b->phase_c.p, b->ldk_c, n, T,
+                               w->vals.p, w->nrm.p, b->pdf_orient.p, nullptr, 1, 1, W, w->ps.p, 0, st));
     GBR_CUDA(cudaEventRecord(w->ev[3], st));
     if (w->debug) {
         w->dbg_coarse.resize((size_t)n * RT);
@@ -444,85 +582,29 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
     long long njobs = 0, nfine = 0;
     GBR_CUDA(cudaMemcpyAsync(&njobs, w->jpos.p + nR, sizeof(long long), cudaMemcpyDeviceToHost, st));
     GBR_CUDA(cudaMemcpyAsync(&nfine, w->epos.p + nR, sizeof(long long), cudaMemcpyDeviceToHost, st));
-    std::vector<unsigned char> need(R);
-    GBR_CUDA(cudaMemcpyAsync(need.data(), w->need_r.p, R, cudaMemcpyDeviceToHost, st));
     std::vector<long long> segf(n + 1);
     GBR_CUDA(cudaMemcpyAsync(segf.data(), w->seg_f.p, sizeof(long long) * (n + 1), cudaMemcpyDeviceToHost, st));
     GBR_CUDA(cudaStreamSynchronize(st));
+    w->launches += 15;
     if (njobs <= 0 || nfine <= 0) return fail(GBR_ERR_NUMERICAL, "no significant coarse samples");
-    const long long fine_cap = std::min<long long>(0x7fffffffLL, b->budget ? (long long)b->budget / 24 : (2LL << 30));
-    if (nfine > fine_cap)
-        return fail(GBR_ERR_OOM, "fine pass needs " + std::to_string(nfine) + " poses in this batch (cap " +
-                                     std::to_string(fine_cap) + "); use smaller batches");
+    // ---- fine pass: dense contractions when most poses are significant ----
+    const double density = (double)nfine / ((double)n * b->RF * b->TF);
+    const long long budget = b->budget ? (long long)b->budget : (48LL << 30);
+    const bool dense_fits = (long long)n * b->RF * b->TF * 4 <= budget / 2;
+    const bool dense = dense_fits && (w->fine_mode == 1 || (w->fine_mode == 0 && density > 0.1));
+    w->last_dense = dense ? 1 : 0;
     long long max_seg = 0;
-    for (int p = 0; p < n; ++p) max_seg = std::max(max_seg, segf[p + 1] - segf[p]);
-    GBR_CUDA(w->fd.reserve(nfine));
-    GBR_CUDA(w->ejob.reserve(nfine));
-    GBR_CUDA(w->ecode.reserve(nfine));
-    // ---- fine projections not yet in the cache ----
-    std::vector<int> ids;
-    for (int r = 0; r < R; ++r)
-        if (need[r] && !b->proj_f_done[r]) {
-            for (int io = 0; io < nOR; ++io) ids.push_back(r * nOR + io);
-            b->proj_f_done[r] = 1;
-        }
-    if (!ids.empty()) {
-        GBR_CUDA(w->proj_ids.reserve(ids.size()));
-        GBR_CUDA(cudaMemcpyAsync(w->proj_ids.p, ids.data(), sizeof(int) * ids.size(), cudaMemcpyHostToDevice, st));
-        GBR_CUDA(launch_project_rows(b->vols_d.p, b->pg, b->eul_f.p, b->cls_f.p, w->proj_ids.p, (int)ids.size(),
-                                     b->pf.p, b->nf, nullptr, 0, nullptr, 0, b->proj_f.p, st));
+    int s;
+    if (dense) {
+        s = fine_dense(w, n, max_seg);
+    } else {
+        const long long fine_cap = std::min<long long>(0x7fffffffLL, b->budget ? (long long)b->budget / 24 : (2LL << 30));
+        if (nfine > fine_cap)
+            return fail(GBR_ERR_OOM, "fine pass needs " + std::to_string(nfine) + " poses in this batch (cap " +
+                                         std::to_string(fine_cap) + "); use smaller batches");
+        s = fine_sparse(w, n, njobs, nfine, segf, max_seg);
     }
-    GBR_CUDA(cudaEventRecord(w->ev[5], st));
-    // ---- fine diff2 ----
-    GBR_CUDA(launch_fine_diff2(w->jobs.p, njobs, w->mask.p, R, T, W, nOR, nOT, b->proj_f.p, w->b_f.p, w->a_f.p,
-                               b->nf, b->phase_f.p, w->fd.p, w->ejob.p, w->ecode.p, w->ps.p, st));
-    GBR_CUDA(cudaEventRecord(w->ev[6], st));
-    if (w->debug) {
-        w->dbg_fine.resize(nfine);
-        w->dbg_ejob.resize(nfine);
-        w->dbg_ecode.resize(nfine);
-        w->dbg_jobs.resize(njobs);
-        GBR_CUDA(cudaMemcpyAsync(w->dbg_fine.data(), w->fd.p, sizeof(float) * nfine, cudaMemcpyDeviceToHost, st));
-        GBR_CUDA(cudaMemcpyAsync(w->dbg_ejob.data(), w->ejob.p, sizeof(int) * nfine, cudaMemcpyDeviceToHost, st));
-        GBR_CUDA(cudaMemcpyAsync(w->dbg_ecode.data(), w->ecode.p, sizeof(unsigned) * nfine, cudaMemcpyDeviceToHost, st));
-        GBR_CUDA(cudaMemcpyAsync(w->dbg_jobs.data(), w->jobs.p, sizeof(FineJob) * njobs, cudaMemcpyDeviceToHost, st));
-        w->dbg_segf = segf;
-    }
-    // ---- fine weights and significance ----
-    GBR_CUDA(launch_weights(w->fd.p, w->seg_f.p, n, max_seg, 0, T, w->ejob.p, w->ecode.p, w->jobs.p, nOR, nOT,
-                            b->pdf_orient.p, w->pdf_off.p, w->ps.p, w->hist.p, st));
-    {
-        int s = threshold_search(w, n, w->fd.p, w->seg_f.p, max_seg, 0);
-        if (s) return s;
-    }
-    GBR_CUDA(cudaEventRecord(w->ev[7], st));
-    if (w->debug) {
-        w->dbg_wfine.resize(nfine);
-        GBR_CUDA(cudaMemcpyAsync(w->dbg_wfine.data(), w->fd.p, sizeof(float) * nfine, cudaMemcpyDeviceToHost, st));
-    }
-    // ---- weighted sums ----
-    WsumArgs wa{};
-    wa.jobs = w->jobs.p;
-    wa.njobs = njobs;
-    wa.mask = w->mask.p;
-    wa.R = R; wa.T = T; wa.W = W; wa.nOR = nOR; wa.nOT = nOT; wa.nf = b->nf; wa.nshell = b->nshell;
-    wa.ndir = (int)b->ND; wa.npsi = (int)b->NP; wa.K = (int)b->K;
-    wa.w = w->fd.p;
-    wa.ps = w->ps.p;
-    wa.projf = b->proj_f.p;
-    wa.Xf = w->Xf.p; wa.Xnf = w->Xnf.p; wa.Cf = w->Cf.p;
-    wa.minv_store = b->minv_store.p;
-    wa.pf = b->pf.p;
-    wa.phase_f = b->phase_f.p;
-    wa.otx = b->otx.p; wa.oty = b->oty.p;
-    wa.pdat = w->pdat.p;
-    wa.pixel = d.pixel_size;
-    wa.do_scale = (int)d.do_scale_correction;
-    wa.dvp_mask = b->dvp_mask.p;
-    wa.bpimg = b->bpimg.p; wa.bpw = b->bpw.p; wa.active = b->active.p;
-    wa.shell = w->shell.p; wa.pacc = w->pacc.p;
-    wa.pdf_dir = b->w_pdf_dir.p; wa.pdf_cls = b->w_pdf_cls.p;
-    GBR_CUDA(launch_wsum(wa, st));
+    if (s) return s;
     GBR_CUDA(cudaEventRecord(w->ev[8], st));
     // ---- backprojection of the touched slices ----
     GBR_CUDA(w->act_list.reserve(b->RF));
@@ -535,7 +617,7 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
     GBR_CUDA(launch_backproject(w->act_list.p, nact, b->eul_f.p, nOR, b->cls_of_r.p, b->bpimg.p, b->bpw.p, b->pf.p,
                                 b->nf, b->cur / 2 + 1, b->bg, b->bpd_ptrs.p, b->bpw_ptrs.p, b->active.p, st));
     GBR_CUDA(cudaEventRecord(w->ev[9], st));
-    w->launches += 18 + (long long)((ids.size() + 65534) / 65535) + (nact > 0 ? 1 : 0);
+    w->launches += 1 + (nact > 0 ? 1 : 0);
     // ---- results ----
     std::vector<ParticleState> psh(n);
     std::vector<double> shell((size_t)n * b->nshell), pacc((size_t)n * 8);
@@ -544,10 +626,10 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
     GBR_CUDA(cudaMemcpyAsync(pacc.data(), w->pacc.p, sizeof(double) * pacc.size(), cudaMemcpyDeviceToHost, st));
     GBR_CUDA(cudaEventRecord(w->ev[10], st));
     GBR_CUDA(cudaStreamSynchronize(st));
-    for (int s = 0; s < ST_N; ++s) {
+    for (int st_i = 0; st_i < ST_N; ++st_i) {
         float ms = 0.f;
-        cudaEventElapsedTime(&ms, w->ev[s], w->ev[s + 1]);
-        w->stage_ms[s] += ms;
+        cudaEventElapsedTime(&ms, w->ev[st_i], w->ev[st_i + 1]);
+        w->stage_ms[st_i] += ms;
     }
     if (w->debug) {
         w->dbg_n = n;
@@ -561,21 +643,21 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
     // ---- per-particle finalisation (storeWeightedSums :8990-9150) ----
     std::vector<double> fr(nOR), ft(nOR), fp(nOR);
     for (int p = 0; p < n; ++p) {
-        const ParticleState &s = psh[p];
+        const ParticleState &ps = psh[p];
         gbr_particle_result &o = res[p];
         std::memset(&o, 0, sizeof(o));
-        if (!(s.sum_fine > 0.) || !std::isfinite(s.sum_fine))
+        if (!(ps.sum_fine > 0.) || !std::isfinite(ps.sum_fine))
             return fail(GBR_ERR_NUMERICAL, "zero sum of weights for particle " + std::to_string(p));
         const double *pd = pdat_h + (size_t)p * 8;
-        o.coarse_min_diff2 = s.c_coarse + (double)ord2f_host(s.min_coarse);
-        o.coarse_sum_weight = s.sum_coarse;
-        o.coarse_significant_weight = s.thr_coarse;
-        o.fine_min_diff2 = s.c_fine + (double)ord2f_host(s.min_fine);
-        o.fine_sum_weight = s.sum_fine;
-        o.fine_significant_weight = s.thr_fine;
-        o.nr_sign = s.nr_sign;
+        o.coarse_min_diff2 = ps.c_coarse + (double)ord2f_host(ps.min_coarse);
+        o.coarse_sum_weight = ps.sum_coarse;
+        o.coarse_significant_weight = ps.thr_coarse;
+        o.fine_min_diff2 = ps.c_fine + (double)ord2f_host(ps.min_fine);
+        o.fine_sum_weight = ps.sum_fine;
+        o.fine_significant_weight = ps.thr_fine;
+        o.nr_sign = ps.nr_sign;
         o.n_fine = segf[p + 1] - segf[p];
-        const unsigned long long key = s.argmax_key;
+        const unsigned long long key = ps.argmax_key;
         const unsigned long long idx = 0xFFFFFFFFull - (key & 0xFFFFFFFFull);
         unsigned int wb = (unsigned int)(key >> 32);
         float wmax;
@@ -591,10 +673,9 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
         o.xoff = pd[0] + b->otx_h[t * nOT + iot];
         o.yoff = pd[1] + b->oty_h[t * nOT + iot];
         o.cls = (double)ic + 1;
-        o.pmax = (double)wmax / s.sum_fine;
+        o.pmax = (double)wmax / ps.sum_fine;
         o.best_ihidden_over = ((r * T + t) * nOR + ior) * nOT + iot;
-        o.dLL = std::log(s.sum_fine) - o.fine_min_diff2 - b->logsigma2;
-        // sigma2 noise shells + power beyond the current size
+        o.dLL = std::log(ps.sum_fine) - o.fine_min_diff2 - b->logsigma2;
         double wnorm = 0.;
         const double *sp = &shell[(size_t)p * b->nshell];
         for (int i = 0; i < b->nshell; ++i) {
@@ -756,6 +837,9 @@ int gbr_worker_create(gbr_bundle *b, gbr_worker **out) {
     for (int i = 0; i <= ST_N; ++i) GBR_CUDA(cudaEventCreate(&w->ev[i]));
     const char *dbg = std::getenv("GBR_DEBUG_FETCH");
     w->debug = dbg && dbg[0] == '1';
+    const char *fm = std::getenv("GBR_FINE_MODE");
+    if (fm && std::strcmp(fm, "dense") == 0) w->fine_mode = 1;
+    if (fm && std::strcmp(fm, "sparse") == 0) w->fine_mode = 2;
     *out = w.release();
     return GBR_OK;
 }
@@ -776,9 +860,11 @@ int gbr_expect_batch(gbr_worker *w, const gbr_particle_batch *batch, gbr_particl
     GBR_CUDA(cudaSetDevice(b->device));
     int s = build_tables(b);
     if (s) return s;
-    const long long per_part = (long long)b->R * b->T * 4;
-    const long long mem_cap = b->budget ? (long long)b->budget / 4 : (4LL << 30);
-    int cap = (int)std::max<long long>(1, std::min<long long>(1024, mem_cap / std::max<long long>(per_part, 1)));
+    // device bytes per particle of the coarse pass (the dense fine pass is
+    // only chosen when its array also fits, see run_batch)
+    const long long per_part = (long long)b->R * b->T * 4 + (1LL << 20);
+    const long long mem_cap = (b->budget ? (long long)b->budget : (48LL << 30)) / 2;
+    int cap = (int)std::max<long long>(1, std::min<long long>(1024, mem_cap / per_part));
     const int n_all = (int)batch->n;
     if (w->debug) cap = n_all;  // debug read-back covers the whole call
     s = ensure_capacity(w, std::min(cap, n_all));
@@ -855,6 +941,22 @@ int64_t gbr_worker_debug_fetch(gbr_worker *w, int what, int64_t i, void *host, i
     const long long b0 = w->dbg_segf[i], b1 = w->dbg_segf[i + 1];
     if (capacity < b1 - b0) return fail(GBR_ERR_INVALID, "capacity too small");
     const int nOR = (int)b->nOR, nOT = (int)b->nOT, T = (int)b->T;
+    if (w->last_dense) {
+        // dense layout [rf][tf]: report the computed (finite diff2) entries
+        const long long TF = (long long)T * nOT;
+        long long m = 0;
+        for (long long e = b0; e < b1; ++e) {
+            if (!std::isfinite(w->dbg_fine[e])) continue;
+            const long long loc = e - b0, rf = loc / TF, tf = loc % TF;
+            const long long r = rf / nOR, ior = rf % nOR, t = tf / nOT, iot = tf % nOT;
+            if (what == 2) static_cast<int64_t *>(host)[m] = ((r * T + t) * nOR + ior) * nOT + iot;
+            else if (what == 3) static_cast<double *>(host)[m] = w->dbg_cf[i] + (double)w->dbg_fine[e];
+            else if (what == 4) static_cast<double *>(host)[m] = (double)w->dbg_wfine[e];
+            else return fail(GBR_ERR_INVALID, "unknown debug selector");
+            ++m;
+        }
+        return m;
+    }
     for (long long e = b0; e < b1; ++e) {
         const long long k = e - b0;
         if (what == 2) {

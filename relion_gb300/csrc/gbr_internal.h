@@ -81,24 +81,37 @@ cudaError_t launch_project_rows(const float2 *const *vols, const VolGeom &g, con
 cudaError_t launch_fp32_probe(float *ms, double *flops);
 
 // k_gemm.cu: C[m][n] = sum_k A[m][k] * Bop[n][k], FP32 SIMT.
-struct CrossEpilogue {
-    float *diff2;            // [p][M*T] relative diff2 (+inf if skipped)
-    const float *norm;       // [p][M] coarse norm term
-    const float *pdf_orient; // [M] (0 = skip)
-    ParticleState *ps;       // min tracking (min_coarse)
-    int T;
-    long long MT;            // M*T
-};
-cudaError_t launch_gemm_cross(const float *A, int lda, int M, int K2, const float2 *bimg,
-                              int ldb, const float2 *phase, int ldp, int nparticles, int T,
-                              const CrossEpilogue &ep, cudaStream_t st);
-cudaError_t launch_gemm_norm(const float *A, int lda, int M, int K, const float *a, int lda_b,
-                             int nparticles, float *out /*[p][M]*/, cudaStream_t st);
+// Cross term + diff2 epilogue; output [p][M][T] relative to c_p, +inf where
+// skipped; fine pass: mask = coarse significance [p][M/mdiv][W].
+cudaError_t launch_gemm_diff2(const float *A, int lda, int M, int K2, const float2 *bimg, int ldb,
+                              const float2 *phase, int ldp, int nparticles, int T, float *out,
+                              const float *norm, const float *pdf_orient, const unsigned int *mask,
+                              int mdiv, int tdiv, int W, ParticleState *ps, int fine, cudaStream_t st);
+// C = A B^T (both K-contiguous rows, K padded to 16); C[m][n] or C[n][m].
+cudaError_t launch_gemm_rows(const float *A, long long lda, int M, const float *B, long long ldb, int N,
+                             int K, float *C, long long ldc, int trans_out, cudaStream_t st);
+cudaError_t launch_gemm_bpimg(const float *W, int RF, int TF, int nparticles, const float *Zt, long long ldz,
+                              int N2, float *img, long long ldi, cudaStream_t st);
+cudaError_t launch_gemm_sigma_cross(const float *W, int RF, int TF, int nparticles, const float *P,
+                                    long long ldp, int nf, const float2 *E, float2 *G, cudaStream_t st);
+cudaError_t launch_gemm_sigma_norm(const float *Wrow, long long ldw, int nparticles, int RF, const float *P2,
+                                   long long ldp2, int nf, float *S, cudaStream_t st);
+cudaError_t launch_fine_normalize(float *w, int n, int R, int nOR, int nOT, int T, const ParticleState *ps,
+                                  const double *pdat, const double *otx, const double *oty, double pixel,
+                                  int ndir, int npsi, float *Wt, int ldwt, float *Wp, int ldwp, unsigned char *active,
+                                  double *pacc, double *pdf_dir, double *pdf_cls, cudaStream_t st);
+cudaError_t launch_make_zt(const float *Cf, const float2 *Xnf, const float *minv_s, const float2 *E,
+                           const double *pdat, int do_scale, int n, int TF, int nf, float *Zt, long long ldz,
+                           float *CM, int ldcm, cudaStream_t st);
+cudaError_t launch_shell_dense(int n, const float *S2P, const float2 *G, const float2 *Xf, const float *Cf,
+                               const PixelRef *pf, int nf, int nshell, const double *pdat, int do_scale,
+                               const unsigned char *dvp_mask, int K, double *pacc, double *shell,
+                               cudaStream_t st);
 
 // k_estep.cu
 cudaError_t launch_prep(const float2 *X, const float *C, const double *pdat, int n, int full_npix,
                         const PixelRef *pc, int nc, const float *minv_c, int ldk_c,
-                        const PixelRef *pf, int nf, const float *minv_f, float *a_c, float2 *b_c,
+                        const PixelRef *pf, int nf, int ldk_f, const float *minv_f, float *a_c, float2 *b_c,
                         float *a_f, float2 *b_f, float2 *Xf, float2 *Xnf, float *Cf,
                         const float2 *Xn, int do_scale, ParticleState *ps, cudaStream_t st);
 cudaError_t launch_pdf_offset(const double *pdat, int n, const double *tx, const double *ty, int T,
@@ -125,7 +138,7 @@ cudaError_t launch_build_jobs(const int *cnt, int n, int R, const long long *jpo
                               const long long *epos, FineJob *jobs, long long *seg,
                               unsigned char *need_r, cudaStream_t st);
 cudaError_t launch_fine_diff2(const FineJob *jobs, long long njobs, const unsigned int *mask,
-                              int R, int T, int W, int nOR, int nOT, const float2 *projf,
+                              int R, int T, int W, int nOR, int nOT, const float2 *projf, int ldpf,
                               const float2 *b_f, const float *a_f, int nf, const float2 *phase_f,
                               float *d, int *ejob, unsigned int *ecode, ParticleState *ps,
                               cudaStream_t st);
@@ -133,7 +146,7 @@ struct WsumArgs {
     const FineJob *jobs;
     long long njobs;
     const unsigned int *mask;
-    int R, T, W, nOR, nOT, nf, nshell, ndir, npsi, K;
+    int R, T, W, nOR, nOT, nf, ldpf, nshell, ndir, npsi, K;
     const float *w;            // fine weights
     const ParticleState *ps;
     const float2 *projf;       // [R*nOR][nf]

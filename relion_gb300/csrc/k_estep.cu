@@ -57,7 +57,7 @@ __global__ void k_prep(const float2 *__restrict__ X, const float *__restrict__ C
                        const float2 *__restrict__ Xn, const double *__restrict__ pdat,
                        int full_npix, const PixelRef *__restrict__ pc, int nc,
                        const float *__restrict__ minv_c, int ldk_c, const PixelRef *__restrict__ pf,
-                       int nf, const float *__restrict__ minv_f, float *__restrict__ a_c,
+                       int nf, int ldk_f, const float *__restrict__ minv_f, float *__restrict__ a_c,
                        float2 *__restrict__ b_c, float *__restrict__ a_f, float2 *__restrict__ b_f,
                        float2 *__restrict__ Xf, float2 *__restrict__ Xnf, float *__restrict__ Cf,
                        int do_scale, ParticleState *__restrict__ ps) {
@@ -92,13 +92,18 @@ __global__ void k_prep(const float2 *__restrict__ X, const float *__restrict__ C
         ps[p] = s;
     }
     acc = 0.;
-    for (int j = threadIdx.x; j < nf; j += blockDim.x) {
+    for (int j = threadIdx.x; j < ldk_f; j += blockDim.x) {
+        if (j >= nf) {
+            a_f[(size_t)p * ldk_f + j] = 0.f;
+            b_f[(size_t)p * ldk_f + j] = make_float2(0.f, 0.f);
+            continue;
+        }
         const int k = pf[j].full;
         const float cr = c[k];
         const float cs = cr * scale, m = minv_f[j];
         const float2 v = x[k];
-        a_f[(size_t)p * nf + j] = m * cs * cs;
-        b_f[(size_t)p * nf + j] = make_float2(m * cs * v.x, m * cs * v.y);
+        a_f[(size_t)p * ldk_f + j] = m * cs * cs;
+        b_f[(size_t)p * ldk_f + j] = make_float2(m * cs * v.x, m * cs * v.y);
         Xf[(size_t)p * nf + j] = v;
         Xnf[(size_t)p * nf + j] = xn[k];
         Cf[(size_t)p * nf + j] = cr;
@@ -169,7 +174,7 @@ k_weights(float *__restrict__ vals, const long long *__restrict__ seg, int coars
     }
     if (threadIdx.x == 0) smax = 0ull;
     __syncthreads();
-    const float mn = ord2f(coarse ? ps[p].min_coarse : ps[p].min_fine);
+    const float mn = ord2f(coarse == 1 ? ps[p].min_coarse : ps[p].min_fine);
     double acc = 0.;
     unsigned long long kmax = 0ull;
     for (long long e = beg + threadIdx.x; e < end; e += blockDim.x) {
@@ -180,21 +185,28 @@ k_weights(float *__restrict__ vals, const long long *__restrict__ seg, int coars
             if (!(x > 700.f)) {
                 int r, t;
                 unsigned int code = 0;
-                if (coarse) {
-                    const long long loc = e - b0;
+                const long long loc = e - b0;
+                unsigned long long idx = 0;
+                if (coarse == 1) {
                     r = (int)(loc / T);
                     t = (int)(loc - (long long)r * T);
+                } else if (coarse == 2) {
+                    // dense fine layout [rf][tf], rf = r*nOR + ior, tf = t*nOT + iot:
+                    // the loop order of storeWeightedSums is the storage order
+                    const long long TF = (long long)T * nOT;
+                    r = (int)(loc / (TF * nOR));
+                    t = (int)((loc % TF) / nOT);
+                    idx = (unsigned long long)loc;
                 } else {
                     r = jobs[ejob[e]].r;
                     code = ecode[e];
                     t = (int)(code / (unsigned)(nOR * nOT));
+                    const unsigned int ior = (code / nOT) % nOR, iot = code % nOT;
+                    idx = (((unsigned long long)r * nOR + ior) * T + t) * nOT + iot;
                 }
                 w = pdf_orient[r] * pdf_off[(size_t)p * T + t] * expf(-x);
-                if (!coarse && w > 0.f) {
+                if (coarse != 1 && w > 0.f) {
                     // loop order of storeWeightedSums: (r, iover_rot, itrans, iover_trans)
-                    const unsigned int ior = (code / nOT) % nOR, iot = code % nOT;
-                    const unsigned long long idx =
-                        (((unsigned long long)r * nOR + ior) * T + t) * nOT + iot;
                     const unsigned long long key =
                         ((unsigned long long)__float_as_uint(w) << 32) | (0xFFFFFFFFull - idx);
                     kmax = key > kmax ? key : kmax;
@@ -210,7 +222,7 @@ k_weights(float *__restrict__ vals, const long long *__restrict__ seg, int coars
         }
     }
     const double tot = block_sum(acc, sh);
-    if (!coarse) {
+    if (coarse != 1) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             const unsigned long long other = __shfl_xor_sync(0xffffffffu, kmax, o);
@@ -220,8 +232,8 @@ k_weights(float *__restrict__ vals, const long long *__restrict__ seg, int coars
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        atomicAdd(coarse ? &ps[p].sum_coarse : &ps[p].sum_fine, tot);
-        if (!coarse && smax) atomicMax(&ps[p].argmax_key, smax);
+        atomicAdd(coarse == 1 ? &ps[p].sum_coarse : &ps[p].sum_fine, tot);
+        if (coarse != 1 && smax) atomicMax(&ps[p].argmax_key, smax);
     }
     HistBin *hp = hist + (size_t)p * kHistBins;
     for (int i = threadIdx.x; i < kHistBins; i += blockDim.x)
@@ -500,7 +512,7 @@ constexpr int kFineThreads = 256;
 
 __global__ void __launch_bounds__(kFineThreads)
 k_fine_diff2(const FineJob *__restrict__ jobs, const unsigned int *__restrict__ mask, int R, int T,
-             int W, int nOR, int nOT, const float2 *__restrict__ projf, const float2 *__restrict__ b_f,
+             int W, int nOR, int nOT, const float2 *__restrict__ projf, int ldpf, const float2 *__restrict__ b_f,
              const float *__restrict__ a_f, int nf, const float2 *__restrict__ phase_f,
              float *__restrict__ d, int *__restrict__ ejob, unsigned int *__restrict__ ecode,
              ParticleState *__restrict__ ps) {
@@ -531,13 +543,13 @@ k_fine_diff2(const FineJob *__restrict__ jobs, const unsigned int *__restrict__ 
     for (int i = threadIdx.x; i < rows * nOR; i += blockDim.x) acc[i] = 0.f;
     for (int i = threadIdx.x; i < nOR; i += blockDim.x) norm[i] = 0.f;
     __syncthreads();
-    const float2 *bp = b_f + (size_t)p * nf;
-    const float *ap = a_f + (size_t)p * nf;
+    const float2 *bp = b_f + (size_t)p * ldpf;
+    const float *ap = a_f + (size_t)p * ldpf;
     for (int c0 = 0; c0 < nf; c0 += kFineChunk) {
         const int cl = min(kFineChunk, nf - c0);
         // stage Q, accumulate norms (one warp per ior at a time)
         for (int ior = warp; ior < nOR; ior += nwarp) {
-            const float2 *P = projf + ((size_t)r * nOR + ior) * nf + c0;
+            const float2 *P = projf + ((size_t)r * nOR + ior) * ldpf + c0;
             float nacc = 0.f;
             for (int k = lane; k < cl; k += 32) {
                 const float2 pv = P[k], bv = bp[c0 + k];
@@ -671,9 +683,15 @@ __global__ void __launch_bounds__(256) k_wsum(WsumArgs a) {
         for (int row = 0; row < rows; ++row) Wsum += wr[row];
         if (!(Wsum > 0.f)) continue;
         const size_t rf = (size_t)r * a.nOR + ior;
-        const float2 *P = a.projf + rf * a.nf;
+        const float2 *P = a.projf + rf * a.ldpf;
         for (int k = lane; k < a.nf; k += 32) {
+            const float2 x = Xp[k], xn = Xnp[k], pv = P[k];
+            const float cs = Cp[k] * scale;
+            const float2 cp = make_float2(cs * pv.x, cs * pv.y);
+            // Phi = sum_t W E_t for the slice; the noise estimate as the
+            // reference forms it, sum_t W |C P - X E_t|^2 (difference first)
             float2 phi = make_float2(0.f, 0.f);
+            float s2acc = 0.f;
             for (int row = 0; row < rows; ++row) {
                 const float wv = wr[row];
                 if (wv != 0.f) {
@@ -681,19 +699,18 @@ __global__ void __launch_bounds__(256) k_wsum(WsumArgs a) {
                     const float2 e = a.phase_f[((size_t)tlist[tr] * a.nOT + iot) * a.nf + k];
                     phi.x = fmaf(wv, e.x, phi.x);
                     phi.y = fmaf(wv, e.y, phi.y);
+                    const float dr = cp.x - (x.x * e.x - x.y * e.y);
+                    const float di = cp.y - (x.x * e.y + x.y * e.x);
+                    s2acc = fmaf(wv, dr * dr + di * di, s2acc);
                 }
             }
-            const float2 x = Xp[k], xn = Xnp[k], pv = P[k];
-            const float cs = Cp[k] * scale;
             const float2 zx = make_float2(x.x * phi.x - x.y * phi.y, x.x * phi.y + x.y * phi.x);
             const float2 zn = make_float2(xn.x * phi.x - xn.y * phi.y, xn.x * phi.y + xn.y * phi.x);
             const int sh = a.pf[k].shell;
             const float p2 = pv.x * pv.x + pv.y * pv.y;
             const float cross = pv.x * zx.x + pv.y * zx.y;
             if (sh >= 0) {
-                const double s2 = (double)Wsum * cs * cs * p2 - 2.0 * cs * cross +
-                                  (double)Wsum * (x.x * x.x + x.y * x.y);
-                atomicAdd(&shell[sh], s2);
+                atomicAdd(&shell[sh], (double)s2acc);
                 if (a.do_scale && a.dvp_mask[(size_t)ic * a.nshell + sh]) {
                     l_xa += (double)cs * cross;
                     l_aa += (double)Wsum * cs * cs * p2;
@@ -803,6 +820,169 @@ __global__ void k_backproject(const int *__restrict__ list, const float *__restr
     if (threadIdx.x == 0) active[rf] = 0;
 }
 
+// ---------------------------------------------------------------------------
+// Dense fine pass (most coarse poses significant): the fine diff2 / weight
+// array is [p][rf][tf] over all oversampled orientations rf = r*nOR + ior
+// and translations tf = t*nOT + iot.
+// ---------------------------------------------------------------------------
+
+// Normalise the fine weights in place: W = w / sum where w >= the fine
+// significant weight, else 0 (storeWeightedSums :8562-8566); row sums per
+// oversampled orientation (into Wt [rf][ldwt] and Wp [p][RF]), FP64 scalar
+// sums (sum of W, sigma2_offset) and the pdf_direction / pdf_class sums.
+// One block per (coarse orientation r, particle p).
+__global__ void k_fine_normalize(float *__restrict__ w, int R, int nOR, int nOT, int T,
+                                 const ParticleState *__restrict__ ps, const double *__restrict__ pdat,
+                                 const double *__restrict__ otx, const double *__restrict__ oty,
+                                 double pixel, int ndir, int npsi, float *__restrict__ Wt, int ldwt,
+                                 float *__restrict__ Wp, int ldwp, unsigned char *__restrict__ active,
+                                 double *__restrict__ pacc, double *__restrict__ pdf_dir,
+                                 double *__restrict__ pdf_cls) {
+    __shared__ double rs[8];
+    __shared__ double red[2];
+    const int r = blockIdx.x, p = blockIdx.y;
+    const int TF = T * nOT, RF = R * nOR;
+    const float thr = ps[p].thr_fine;
+    const double inv = 1. / ps[p].sum_fine;
+    const double *pd = pdat + (size_t)p * 8;
+    float *base = w + ((size_t)p * RF + (size_t)r * nOR) * TF;
+    if (threadIdx.x < 8) rs[threadIdx.x] = 0.;
+    if (threadIdx.x < 2) red[threadIdx.x] = 0.;
+    __syncthreads();
+    double loff = 0.;
+    double lrow[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) lrow[i] = 0.;
+    for (int e = threadIdx.x; e < nOR * TF; e += blockDim.x) {
+        const int ior = e / TF, tf = e - ior * TF;
+        const float v = base[e];
+        float wn = 0.f;
+        if (v > 0.f && v >= thr) {
+            const double wd = (double)v * inv;
+            wn = (float)wd;
+            const double dx = pd[2] - pd[0] - otx[tf];
+            const double dy = pd[3] - pd[1] - oty[tf];
+            loff += wd * pixel * pixel * dx * dx;
+            loff += wd * pixel * pixel * dy * dy;
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+                if (i == ior) lrow[i] += wd;
+        }
+        base[e] = wn;
+    }
+    loff = warp_sum(loff);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) lrow[i] = warp_sum(lrow[i]);
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&red[1], loff);
+        for (int i = 0; i < nOR && i < 8; ++i)
+            if (lrow[i] != 0.) atomicAdd(&rs[i], lrow[i]);
+    }
+    __syncthreads();
+    if (threadIdx.x < nOR) {
+        const int rf = r * nOR + threadIdx.x;
+        const float v = (float)rs[threadIdx.x];
+        Wt[(size_t)rf * ldwt + p] = v;
+        Wp[(size_t)p * ldwp + rf] = v;
+        if (v > 0.f) active[rf] = 1;
+    }
+    if (threadIdx.x == 0) {
+        double tot = 0.;
+        for (int i = 0; i < nOR && i < 8; ++i) tot += rs[i];
+        if (tot != 0.) {
+            const int ic = r / (ndir * npsi), idir = (r / npsi) % ndir;
+            atomicAdd(&pacc[(size_t)p * 8 + 0], tot);
+            atomicAdd(&pdf_dir[(size_t)ic * ndir + idir], tot);
+            atomicAdd(&pdf_cls[ic], tot);
+        }
+        if (red[1] != 0.) atomicAdd(&pacc[(size_t)p * 8 + 1], red[1]);
+    }
+}
+
+// B operand of the BP-slice contraction, stored transposed for K-contiguous
+// rows: Zt[2k+c][(p,tf)] = Re/Im(C_pk s Minv_k Xn_pk E_tf,k); and
+// CM[k][p] = (C_pk s)^2 Minv_k for the BP-weight contraction.
+__global__ void k_make_zt(const float *__restrict__ Cf, const float2 *__restrict__ Xnf,
+                          const float *__restrict__ minv_s, const float2 *__restrict__ E,
+                          const double *__restrict__ pdat, int do_scale, int n, int TF, int nf,
+                          float *__restrict__ Zt, long long ldz, float *__restrict__ CM, int ldcm) {
+    const int k = blockIdx.y;
+    const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const float ms = minv_s[k];
+    if (j < ldz) {
+        float zr = 0.f, zi = 0.f;
+        if (j < (long long)n * TF) {
+            const int p = (int)(j / TF), tf = (int)(j - (long long)p * TF);
+            const float s = do_scale ? fmaxf((float)pdat[(size_t)p * 8 + 6], 0.001f) : 1.f;
+            const float f = Cf[(size_t)p * nf + k] * s * ms;
+            const float2 x = Xnf[(size_t)p * nf + k], e = __ldg(E + (size_t)tf * nf + k);
+            zr = f * (x.x * e.x - x.y * e.y);
+            zi = f * (x.x * e.y + x.y * e.x);
+        }
+        Zt[(size_t)(2 * k) * ldz + j] = zr;
+        Zt[(size_t)(2 * k + 1) * ldz + j] = zi;
+    }
+    if (blockIdx.x == 0)
+        for (int p = threadIdx.x; p < ldcm; p += blockDim.x) {
+            float v = 0.f;
+            if (p < n) {
+                const float s = do_scale ? fmaxf((float)pdat[(size_t)p * 8 + 6], 0.001f) : 1.f;
+                const float c = Cf[(size_t)p * nf + k] * s;
+                v = c * c * ms;
+            }
+            CM[(size_t)k * ldcm + p] = v;
+        }
+}
+
+// sigma2 shell sums of the dense path, one block per particle:
+//   sum_poses W |C P - X E|^2 = C^2 S - 2 C Re(conj(X) G) + (sum W) |X|^2
+// per pixel, binned by resolution shell (plus the scale-correction sums).
+__global__ void k_shell_dense(const float *__restrict__ S2P, const float2 *__restrict__ G,
+                              const float2 *__restrict__ Xf, const float *__restrict__ Cf,
+                              const PixelRef *__restrict__ pf, int nf, int nshell,
+                              const double *__restrict__ pdat, int do_scale,
+                              const unsigned char *__restrict__ dvp_mask, int K, int ic_single,
+                              double *__restrict__ pacc, double *__restrict__ shell) {
+    extern __shared__ double ssh[];
+    __shared__ double red[2];
+    const int p = blockIdx.x;
+    for (int i = threadIdx.x; i < nshell; i += blockDim.x) ssh[i] = 0.;
+    if (threadIdx.x < 2) red[threadIdx.x] = 0.;
+    __syncthreads();
+    const double wtot = pacc[(size_t)p * 8 + 0];
+    const float s = do_scale ? fmaxf((float)pdat[(size_t)p * 8 + 6], 0.001f) : 1.f;
+    double lxa = 0., laa = 0.;
+    for (int k = threadIdx.x; k < nf; k += blockDim.x) {
+        const int sh = pf[k].shell;
+        if (sh < 0) continue;
+        const float c = Cf[(size_t)p * nf + k] * s;
+        const float2 x = Xf[(size_t)p * nf + k], g = G[(size_t)p * nf + k];
+        const double sp = S2P[(size_t)p * nf + k];
+        const double cross = (double)x.x * g.x + (double)x.y * g.y;
+        const double v = (double)c * c * sp - 2.0 * c * cross + wtot * ((double)x.x * x.x + (double)x.y * x.y);
+        atomicAdd(&ssh[sh], v);
+        if (do_scale && K == 1 && dvp_mask[(size_t)ic_single * nshell + sh]) {
+            lxa += (double)c * cross;
+            laa += (double)c * c * sp;
+        }
+    }
+    if (do_scale) {
+        lxa = warp_sum(lxa);
+        laa = warp_sum(laa);
+        if ((threadIdx.x & 31) == 0) {
+            atomicAdd(&red[0], lxa);
+            atomicAdd(&red[1], laa);
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nshell; i += blockDim.x)
+        if (ssh[i] != 0.) shell[(size_t)p * nshell + i] += ssh[i];
+    if (threadIdx.x == 0 && do_scale) {
+        pacc[(size_t)p * 8 + 2] += red[0];
+        pacc[(size_t)p * 8 + 3] += red[1];
+    }
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -810,11 +990,11 @@ __global__ void k_backproject(const int *__restrict__ list, const float *__restr
 // ---------------------------------------------------------------------------
 cudaError_t launch_prep(const float2 *X, const float *C, const double *pdat, int n, int full_npix,
                         const PixelRef *pc, int nc, const float *minv_c, int ldk_c,
-                        const PixelRef *pf, int nf, const float *minv_f, float *a_c, float2 *b_c,
+                        const PixelRef *pf, int nf, int ldk_f, const float *minv_f, float *a_c, float2 *b_c,
                         float *a_f, float2 *b_f, float2 *Xf, float2 *Xnf, float *Cf,
                         const float2 *Xn, int do_scale, ParticleState *ps, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    k_prep<<<n, 256, 0, st>>>(X, C, Xn, pdat, full_npix, pc, nc, minv_c, ldk_c, pf, nf, minv_f, a_c,
+    k_prep<<<n, 256, 0, st>>>(X, C, Xn, pdat, full_npix, pc, nc, minv_c, ldk_c, pf, nf, ldk_f, minv_f, a_c,
                               b_c, a_f, b_f, Xf, Xnf, Cf, do_scale, ps);
     return cudaGetLastError();
 }
@@ -901,7 +1081,7 @@ cudaError_t launch_build_jobs(const int *cnt, int n, int R, const long long *jpo
 }
 
 cudaError_t launch_fine_diff2(const FineJob *jobs, long long njobs, const unsigned int *mask, int R,
-                              int T, int W, int nOR, int nOT, const float2 *projf, const float2 *b_f,
+                              int T, int W, int nOR, int nOT, const float2 *projf, int ldpf, const float2 *b_f,
                               const float *a_f, int nf, const float2 *phase_f, float *d, int *ejob,
                               unsigned int *ecode, ParticleState *ps, cudaStream_t st) {
     if (njobs <= 0) return cudaSuccess;
@@ -916,7 +1096,7 @@ cudaError_t launch_fine_diff2(const FineJob *jobs, long long njobs, const unsign
     }
     for (long long j0 = 0; j0 < njobs; j0 += 0x7fffffffLL) {
         const long long nj = njobs - j0 < 0x7fffffffLL ? njobs - j0 : 0x7fffffffLL;
-        k_fine_diff2<<<(unsigned)nj, kFineThreads, smem, st>>>(jobs + j0, mask, R, T, W, nOR, nOT, projf,
+        k_fine_diff2<<<(unsigned)nj, kFineThreads, smem, st>>>(jobs + j0, mask, R, T, W, nOR, nOT, projf, ldpf,
                                                                b_f, a_f, nf, phase_f, d, ejob, ecode, ps);
     }
     return cudaGetLastError();
@@ -950,6 +1130,37 @@ cudaError_t launch_backproject(const int *list, int nlist, const float *eul_f, i
     if (nlist <= 0) return cudaSuccess;
     k_backproject<<<nlist, 256, 0, st>>>(list, eul_f, nOR, cls_of_r, bpimg, bpw, pf, nf, g, data,
                                          weight, active);
+    return cudaGetLastError();
+}
+
+
+cudaError_t launch_fine_normalize(float *w, int n, int R, int nOR, int nOT, int T, const ParticleState *ps,
+                                  const double *pdat, const double *otx, const double *oty, double pixel,
+                                  int ndir, int npsi, float *Wt, int ldwt, float *Wp, int ldwp, unsigned char *active,
+                                  double *pacc, double *pdf_dir, double *pdf_cls, cudaStream_t st) {
+    if (n <= 0 || nOR > 8) return nOR > 8 ? cudaErrorInvalidValue : cudaSuccess;
+    dim3 grid(R, n);
+    k_fine_normalize<<<grid, 256, 0, st>>>(w, R, nOR, nOT, T, ps, pdat, otx, oty, pixel, ndir, npsi, Wt, ldwt,
+                                           Wp, ldwp, active, pacc, pdf_dir, pdf_cls);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_make_zt(const float *Cf, const float2 *Xnf, const float *minv_s, const float2 *E,
+                           const double *pdat, int do_scale, int n, int TF, int nf, float *Zt, long long ldz,
+                           float *CM, int ldcm, cudaStream_t st) {
+    if (n <= 0 || nf <= 0) return cudaSuccess;
+    dim3 grid((unsigned)((ldz + 255) / 256), nf);
+    k_make_zt<<<grid, 256, 0, st>>>(Cf, Xnf, minv_s, E, pdat, do_scale, n, TF, nf, Zt, ldz, CM, ldcm);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_shell_dense(int n, const float *S2P, const float2 *G, const float2 *Xf, const float *Cf,
+                               const PixelRef *pf, int nf, int nshell, const double *pdat, int do_scale,
+                               const unsigned char *dvp_mask, int K, double *pacc, double *shell,
+                               cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    k_shell_dense<<<n, 256, sizeof(double) * nshell, st>>>(S2P, G, Xf, Cf, pf, nf, nshell, pdat, do_scale,
+                                                           dvp_mask, K, 0, pacc, shell);
     return cudaGetLastError();
 }
 

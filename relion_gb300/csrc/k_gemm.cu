@@ -1,19 +1,26 @@
-// k_gemm.cu -- coarse-pass contractions of the plain (FP32) path.
+// k_gemm.cu -- the E-step's contractions as FP32 SIMT GEMMs (plain path).
 //
-// The coarse squared difference of src/ml_optimiser.cpp:7436-7442,
+// Squared difference (src/ml_optimiser.cpp:7436-7442),
 //   diff2(r,p,t) = Xi2/2 + sum_k m_k |C_pk P_rk - X_pk E_tk|^2,
 // m_k = invsigma2_k / 2, E_tk = exp(-2 pi i k.t / N), is evaluated as
-//   diff2 = c_p + N(r,p) - 2 Re sum_k P_rk conj(m_k C_pk X_pk E_tk)
-// with c_p = Xi2/2 + sum_k m_k |X_pk|^2 (per particle, FP64),
-//      N(r,p) = sum_k (m_k C_pk^2) |P_rk|^2                (norm GEMM) and
-// the cross term a real GEMM of K = 2 * active pixels (cross GEMM), whose
-// B operand Y(p,t) = m C X E is formed on the fly while staging tiles, so
-// it never exists in HBM.  The epilogue stores diff2 - c_p (relative to the
-// per-particle constant, which cancels in every weight) in the reference's
-// hidden-index order [p][r*T + t] and tracks the per-particle minimum.
+//   diff2 = c_p + N(r,p) - 2 Re sum_k P_rk conj(m_k C_pk X_pk E_tk),
+// c_p = Xi2/2 + sum_k m_k |X_pk|^2 (FP64, per particle), the norm term
+// N(r,p) = sum_k (m_k C_pk^2) |P_rk|^2 and the cross term a real GEMM over
+// K = 2 x pixels whose B operand Y(p,t) = m C X E is formed while staging
+// tiles.  The same holds for the coarse pass (coarse pixels, coarse
+// orientations and translations) and the fine pass (oversampled ones).
 //
-// Tiles: 128x128 outputs per CTA, BK = 16, 256 threads with an 8x8
-// register block each, double-buffered shared memory.
+// The weighted sums of storeWeightedSums (:8562-8780) become contractions
+// over the normalised fine weights W(p, rf, tf):
+//   BP slice      img(rf,k) = sum_{p,tf} W (C Minv Xn)_pk E_tf,k
+//   BP weight     wgt(rf,k) = sum_p (sum_tf W) (C^2 Minv)_pk
+//   sigma2 cross  G(p,k)    = sum_tf conj(E_tf,k) sum_rf W P_rf,k
+//   sigma2 norm   S(p,k)    = sum_rf (sum_tf W) |P_rf,k|^2
+//
+// One templated kernel: 128x128 outputs per CTA, BK = 16, 256 threads with
+// an 8x8 register block, double-buffered shared memory.  Operand loaders
+// stage either "K-major" rows (8 consecutive k of one row per thread) or
+// "M-major" columns (8 consecutive rows of one k per thread).
 #include "gbr_internal.h"
 
 namespace gbr {
@@ -26,13 +33,69 @@ __device__ __forceinline__ unsigned int f2ord(float f) {
     return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
 }
 
-// B operand of the cross GEMM: Y[n][2j+c] = Re/Im(b[p][j] * E[t][j]).
-struct CrossB {
-    const float2 *b;   // [p][ldb]
-    const float2 *E;   // [t][ldp]
+// ---- operand loaders -------------------------------------------------------
+// K-major mapping: thread -> row (tid & 127), k half (tid >> 7): 8 k values.
+// M-major mapping: thread -> k (tid >> 4), row group (tid & 15): 8 rows.
+struct KMajor {
+    __device__ __forceinline__ static void store(float (*S)[BM], int tid, const float v[8]) {
+        const int r = tid & 127, kh = tid >> 7;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) S[kh * 8 + i][r] = v[i];
+    }
+};
+struct MMajor {
+    __device__ __forceinline__ static void store(float (*S)[BM], int tid, const float v[8]) {
+        const int k = tid >> 4, rg = tid & 15;
+        *reinterpret_cast<float4 *>(&S[k][rg * 8]) = make_float4(v[0], v[1], v[2], v[3]);
+        *reinterpret_cast<float4 *>(&S[k][rg * 8 + 4]) = make_float4(v[4], v[5], v[6], v[7]);
+    }
+};
+
+// Plain K-contiguous rows, zero-padded to a multiple of 16 columns.
+struct RowsK : KMajor {
+    const float *a;
+    long long ld, zstride;
+    int rows;
+    __device__ __forceinline__ void load(int z, int m0, int k0, int tid, float v[8]) const {
+        const int r = m0 + (tid & 127), k = k0 + (tid >> 7) * 8;
+        if (r < rows) {
+            const float4 *s = reinterpret_cast<const float4 *>(a + z * zstride + r * ld + k);
+            const float4 u0 = __ldg(s), u1 = __ldg(s + 1);
+            v[0] = u0.x; v[1] = u0.y; v[2] = u0.z; v[3] = u0.w;
+            v[4] = u1.x; v[5] = u1.y; v[6] = u1.z; v[7] = u1.w;
+        } else {
+#pragma unroll
+            for (int i = 0; i < 8; ++i) v[i] = 0.f;
+        }
+    }
+};
+
+// Rows of an operand stored k-major ([k][row], rows contiguous, ld % 4 == 0).
+struct ColsM : MMajor {
+    const float *a;
+    long long ld, zstride;
+    int rows, kmax;
+    __device__ __forceinline__ void load(int z, int m0, int k0, int tid, float v[8]) const {
+        const int k = k0 + (tid >> 4), r = m0 + (tid & 15) * 8;
+        if (k < kmax && r + 8 <= rows) {
+            const float4 *s = reinterpret_cast<const float4 *>(a + z * zstride + (long long)k * ld + r);
+            const float4 u0 = __ldg(s), u1 = __ldg(s + 1);
+            v[0] = u0.x; v[1] = u0.y; v[2] = u0.z; v[3] = u0.w;
+            v[4] = u1.x; v[5] = u1.y; v[6] = u1.z; v[7] = u1.w;
+        } else {
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+                v[i] = (k < kmax && r + i < rows) ? __ldg(a + z * zstride + (long long)k * ld + r + i) : 0.f;
+        }
+    }
+};
+
+// Cross-term B operand: Y[n][2j+c] = Re/Im(b[p][j] E[t][j]), n = p*T + t.
+struct CrossY : KMajor {
+    const float2 *b, *E;
     int ldb, ldp, T, N, npix;
-    // Stage 8 consecutive k (4 pixels from pixel j) of column n.
-    __device__ __forceinline__ void load(int n, int j, float v[8]) const {
+    __device__ __forceinline__ void load(int, int n0, int k0, int tid, float v[8]) const {
+        const int n = n0 + (tid & 127), j = (k0 >> 1) + (tid >> 7) * 4;
         if (n >= N) {
 #pragma unroll
             for (int i = 0; i < 8; ++i) v[i] = 0.f;
@@ -54,76 +117,161 @@ struct CrossB {
     }
 };
 
-// B operand of the norm GEMM: plain rows a[n][k] (k contiguous, zero padded).
-struct PlainB {
-    const float *a;
-    int lda, N;
-    __device__ __forceinline__ void load(int n, int k8, float v[8]) const {
-        if (n >= N) {
+// Normalised fine weights as A[rf][(p, tf)] of the BP-slice contraction;
+// stored [p][rf][tf].
+struct WeightsByRow : KMajor {
+    const float *w;
+    int RF, TF, KB;  // KB = n * TF
+    __device__ __forceinline__ void load(int, int m0, int k0, int tid, float v[8]) const {
+        const int r = m0 + (tid & 127);
+        int k = k0 + (tid >> 7) * 8;
 #pragma unroll
-            for (int i = 0; i < 8; ++i) v[i] = 0.f;
-            return;
+        for (int i = 0; i < 8; ++i, ++k) {
+            float x = 0.f;
+            if (r < RF && k < KB) {
+                const int p = k / TF, tf = k - p * TF;
+                x = __ldg(w + ((size_t)p * RF + r) * TF + tf);
+            }
+            v[i] = x;
         }
-        const float4 *src = reinterpret_cast<const float4 *>(a + (size_t)n * lda + k8);
-        float4 u0 = __ldg(src), u1 = __ldg(src + 1);
-        v[0] = u0.x; v[1] = u0.y; v[2] = u0.z; v[3] = u0.w;
-        v[4] = u1.x; v[5] = u1.y; v[6] = u1.z; v[7] = u1.w;
     }
 };
 
-template <bool kCross, class BL>
-__global__ void __launch_bounds__(NT, 2)
-k_gemm(const float *__restrict__ A, int lda, int M, int K, BL bl, int N, CrossEpilogue ep,
-       float *__restrict__ out_norm) {
+// Normalised fine weights of particle z as A[tf][rf] (rows tf contiguous).
+struct WeightsByTrans : MMajor {
+    const float *w;
+    int RF, TF;
+    __device__ __forceinline__ void load(int z, int m0, int k0, int tid, float v[8]) const {
+        const int k = k0 + (tid >> 4), r = m0 + (tid & 15) * 8;
+        const float *base = w + ((size_t)z * RF + k) * TF;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) v[i] = (k < RF && r + i < TF) ? __ldg(base + r + i) : 0.f;
+    }
+};
+
+// ---- epilogues ---------------------------------------------------------------
+// Thread (tm, tn) holds rows tm*4+i (i<4) and 64+tm*4+i-4, columns likewise.
+__device__ __forceinline__ int row_of(int tm, int i) { return i < 4 ? tm * 4 + i : 64 + tm * 4 + (i - 4); }
+
+struct StoreEpi {  // C[m][n] (row stride ldc) or, transposed, C[n][m]
+    float *c;
+    long long ldc;
+    int M, N, trans;
+    __device__ void run(int, int m0, int n0, int tm, int tn, float (&acc)[8][8], unsigned int *) const {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const int m = m0 + row_of(tm, i);
+            if (m >= M) continue;
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const int n = n0 + row_of(tn, j);
+                if (n >= N) continue;
+                if (trans) c[(long long)n * ldc + m] = acc[i][j];
+                else c[(long long)m * ldc + n] = acc[i][j];
+            }
+        }
+    }
+};
+
+// diff2 - c_p = N - 2 * cross, masked by significance, with per-particle min.
+// Output layout [p][M][T] (row m, translation t); coarse: mask == nullptr.
+struct Diff2Epi {
+    float *out;
+    const float *norm;        // [p][M]
+    const float *pdf_orient;  // [M / mdiv] (0 = skip)
+    const unsigned int *mask; // [p][M/mdiv][W]: coarse significance (fine pass)
+    ParticleState *ps;
+    int M, T, N, mdiv, tdiv, W, fine;
+    __device__ void run(int, int m0, int n0, int tm, int tn, float (&acc)[8][8], unsigned int *smin) const {
+        const int p_first = n0 / T;
+        for (int i = threadIdx.x; i < BN + 2; i += NT) smin[i] = 0xFFFFFFFFu;
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const int m = m0 + row_of(tm, i);
+            if (m >= M) continue;
+            const int r = m / mdiv;
+            const bool skip = !(pdf_orient[r] > 0.f);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const int n = n0 + row_of(tn, j);
+                if (n >= N) continue;
+                const int p = n / T, t = n - p * T;
+                bool ok = !skip;
+                if (ok && mask) {
+                    const int tc = t / tdiv;
+                    ok = (mask[((size_t)p * (M / mdiv) + r) * W + (tc >> 5)] >> (tc & 31)) & 1u;
+                }
+                float d = __int_as_float(0x7f800000);  // +inf: not computed
+                if (ok) {
+                    d = norm[(size_t)p * M + m] - 2.f * acc[i][j];
+                    atomicMin(&smin[p - p_first], f2ord(d));
+                }
+                out[((size_t)p * M + m) * T + t] = d;
+            }
+        }
+        __syncthreads();
+        const int n_last = min(n0 + BN, N) - 1;
+        const int np = n_last / T - p_first + 1;
+        for (int i = threadIdx.x; i < np; i += NT)
+            if (smin[i] != 0xFFFFFFFFu)
+                atomicMin(fine ? &ps[p_first + i].min_fine : &ps[p_first + i].min_coarse, smin[i]);
+    }
+};
+
+// H(tf, 2k+c) tile of particle z -> G[z][k] += sum_tf H(tf,k) conj(E_tf,k).
+struct ConjPhaseReduceEpi {
+    float2 *G;          // [p][nf]
+    const float2 *E;    // [TF][nf]
+    int TF, nf;
+    __device__ void run(int z, int m0, int n0, int tm, int tn, float (&acc)[8][8], unsigned int *) const {
+#pragma unroll
+        for (int jj = 0; jj < 8; jj += 2) {
+            const int n = n0 + row_of(tn, jj);  // even column: Re; n+1: Im
+            const int k = n >> 1;
+            if (k >= nf) continue;
+            float gr = 0.f, gi = 0.f;
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                const int tf = m0 + row_of(tm, i);
+                if (tf >= TF) continue;
+                const float2 e = __ldg(E + (size_t)tf * nf + k);
+                const float hr = acc[i][jj], hi = acc[i][jj + 1];
+                gr = fmaf(hr, e.x, fmaf(hi, e.y, gr));   // Re(h conj(e))
+                gi = fmaf(hi, e.x, fmaf(-hr, e.y, gi));  // Im(h conj(e))
+            }
+            atomicAdd(&G[(size_t)z * nf + k].x, gr);
+            atomicAdd(&G[(size_t)z * nf + k].y, gi);
+        }
+    }
+};
+
+template <class AL, class BL, class EP>
+__global__ void __launch_bounds__(NT, 2) k_gemm(AL al, BL bl, EP ep, int K) {
     __shared__ __align__(16) float As[2][BK][BM];
     __shared__ __align__(16) float Bs[2][BK][BN];
     __shared__ unsigned int smin[BN + 2];
-
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, z = blockIdx.z;
     const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
-    const int lrow = tid & (BM - 1), lhalf = tid >> 7;  // loader: row/col, k half
-    const int tm = tid >> 4, tn = tid & 15;               // compute: 4x4 groups
-
-    if (kCross) {
-        for (int i = tid; i < BN + 2; i += NT) smin[i] = 0xFFFFFFFFu;
-    }
-
+    const int tm = tid >> 4, tn = tid & 15;
     float ra[8], rb[8];
-    auto gload = [&](int k0) {
-        const int m = m0 + lrow;
-        if (m < M) {
-            const float4 *src = reinterpret_cast<const float4 *>(A + (size_t)m * lda + k0 + lhalf * 8);
-            float4 u0 = __ldg(src), u1 = __ldg(src + 1);
-            ra[0] = u0.x; ra[1] = u0.y; ra[2] = u0.z; ra[3] = u0.w;
-            ra[4] = u1.x; ra[5] = u1.y; ra[6] = u1.z; ra[7] = u1.w;
-        } else {
-#pragma unroll
-            for (int i = 0; i < 8; ++i) ra[i] = 0.f;
-        }
-        if (kCross) bl.load(n0 + lrow, (k0 >> 1) + lhalf * 4, rb);
-        else bl.load(n0 + lrow, k0 + lhalf * 8, rb);
-    };
-    auto sstore = [&](int buf) {
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-            As[buf][lhalf * 8 + i][lrow] = ra[i];
-            Bs[buf][lhalf * 8 + i][lrow] = rb[i];
-        }
-    };
-
     float acc[8][8];
 #pragma unroll
     for (int i = 0; i < 8; ++i)
 #pragma unroll
         for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
-
     const int nk = (K + BK - 1) / BK;
-    gload(0);
-    sstore(0);
+    al.load(z, m0, 0, tid, ra);
+    bl.load(z, n0, 0, tid, rb);
+    AL::store(As[0], tid, ra);
+    BL::store(Bs[0], tid, rb);
     __syncthreads();
     for (int kt = 0; kt < nk; ++kt) {
         const int cur = kt & 1;
-        if (kt + 1 < nk) gload((kt + 1) * BK);
+        if (kt + 1 < nk) {
+            al.load(z, m0, (kt + 1) * BK, tid, ra);
+            bl.load(z, n0, (kt + 1) * BK, tid, rb);
+        }
 #pragma unroll
         for (int k = 0; k < BK; ++k) {
             float a[8], b[8];
@@ -141,52 +289,21 @@ k_gemm(const float *__restrict__ A, int lda, int M, int K, BL bl, int N, CrossEp
                 for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
         }
         if (kt + 1 < nk) {
-            sstore(cur ^ 1);
+            AL::store(As[cur ^ 1], tid, ra);
+            BL::store(Bs[cur ^ 1], tid, rb);
             __syncthreads();
         }
     }
+    ep.run(z, m0, n0, tm, tn, acc, smin);
+}
 
-    // ---- epilogue ----
-    if (kCross) {
-        const int T = ep.T;
-        const int p_first = n0 / T;
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-            const int m = m0 + (i < 4 ? tm * 4 + i : 64 + tm * 4 + (i - 4));
-            if (m >= M) continue;
-            const bool skip = !(ep.pdf_orient[m] > 0.f);
-#pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                const int n = n0 + (j < 4 ? tn * 4 + j : 64 + tn * 4 + (j - 4));
-                if (n >= N) continue;
-                const int p = n / T, t = n - p * T;
-                float d;
-                if (skip) {
-                    d = __int_as_float(0x7f800000);  // +inf: not computed
-                } else {
-                    d = ep.norm[(size_t)p * M + m] - 2.f * acc[i][j];
-                    atomicMin(&smin[p - p_first], f2ord(d));
-                }
-                ep.diff2[(size_t)p * ep.MT + (size_t)m * T + t] = d;
-            }
-        }
-        __syncthreads();
-        const int n_last = min(n0 + BN, N) - 1;
-        const int np = n_last / T - p_first + 1;
-        for (int i = tid; i < np; i += NT)
-            if (smin[i] != 0xFFFFFFFFu) atomicMin(&ep.ps[p_first + i].min_coarse, smin[i]);
-    } else {
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-            const int m = m0 + (i < 4 ? tm * 4 + i : 64 + tm * 4 + (i - 4));
-            if (m >= M) continue;
-#pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                const int n = n0 + (j < 4 ? tn * 4 + j : 64 + tn * 4 + (j - 4));
-                if (n < N) out_norm[(size_t)n * M + m] = acc[i][j];
-            }
-        }
-    }
+template <class AL, class BL, class EP>
+cudaError_t gemm(const AL &al, const BL &bl, const EP &ep, int M, int N, int K, int batch, cudaStream_t st) {
+    if (M <= 0 || N <= 0 || K <= 0 || batch <= 0) return cudaSuccess;
+    dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM, batch);
+    if (grid.y > 65535 || grid.z > 65535) return cudaErrorInvalidConfiguration;
+    k_gemm<AL, BL, EP><<<grid, NT, 0, st>>>(al, bl, ep, K);
+    return cudaGetLastError();
 }
 
 // Independent FMA chains per thread (8 accumulators) for a peak estimate.
@@ -201,7 +318,7 @@ __global__ void k_fp32_probe(float *out, int iters, float a, float b) {
     float s = 0.f;
 #pragma unroll
     for (int i = 0; i < 8; ++i) s += x[i];
-    if (s == 12345.678f) out[0] = s;  // keep the chains live
+    if (s == 12345.678f) out[0] = s;  // keeps the chains live
 }
 
 }  // namespace
@@ -230,24 +347,66 @@ cudaError_t launch_fp32_probe(float *ms, double *flops) {
     return e != cudaSuccess ? e : cudaGetLastError();
 }
 
-cudaError_t launch_gemm_cross(const float *A, int lda, int M, int K2, const float2 *bimg, int ldb,
-                              const float2 *phase, int ldp, int nparticles, int T,
-                              const CrossEpilogue &ep, cudaStream_t st) {
+// Cross term + diff2 epilogue.  A = projections [M][lda] (interleaved re/im),
+// B = b (x) E on the fly; output [p][M][T].  Fine pass: M = R*nOR rows,
+// T = T*nOT, mask = coarse significance, mdiv = nOR, tdiv = nOT.
+cudaError_t launch_gemm_diff2(const float *A, int lda, int M, int K2, const float2 *bimg, int ldb,
+                              const float2 *phase, int ldp, int nparticles, int T, float *out,
+                              const float *norm, const float *pdf_orient, const unsigned int *mask,
+                              int mdiv, int tdiv, int W, ParticleState *ps, int fine, cudaStream_t st) {
     const int N = nparticles * T;
-    CrossB bl{bimg, phase, ldb, ldp, T, N, K2 / 2};
-    dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM);
-    if (grid.y > 65535) return cudaErrorInvalidConfiguration;
-    k_gemm<true, CrossB><<<grid, NT, 0, st>>>(A, lda, M, K2, bl, N, ep, nullptr);
-    return cudaGetLastError();
+    RowsK al{};
+    al.a = A; al.ld = lda; al.zstride = 0; al.rows = M;
+    CrossY bl{};
+    bl.b = bimg; bl.E = phase; bl.ldb = ldb; bl.ldp = ldp; bl.T = T; bl.N = N; bl.npix = K2 / 2;
+    Diff2Epi ep{out, norm, pdf_orient, mask, ps, M, T, N, mdiv, tdiv, W, fine};
+    return gemm(al, bl, ep, M, N, K2, 1, st);
 }
 
-cudaError_t launch_gemm_norm(const float *A, int lda, int M, int K, const float *a, int lda_b,
-                             int nparticles, float *out, cudaStream_t st) {
-    PlainB bl{a, lda_b, nparticles};
-    CrossEpilogue ep{};
-    dim3 grid((nparticles + BN - 1) / BN, (M + BM - 1) / BM);
-    k_gemm<false, PlainB><<<grid, NT, 0, st>>>(A, lda, M, K, bl, nparticles, ep, out);
-    return cudaGetLastError();
+// C = A B^T with K-contiguous rows; output C[m][n] or (trans_out) C[n][m].
+cudaError_t launch_gemm_rows(const float *A, long long lda, int M, const float *B, long long ldb, int N,
+                             int K, float *C, long long ldc, int trans_out, cudaStream_t st) {
+    RowsK al{};
+    al.a = A; al.ld = lda; al.zstride = 0; al.rows = M;
+    RowsK bl{};
+    bl.a = B; bl.ld = ldb; bl.zstride = 0; bl.rows = N;
+    StoreEpi ep{C, ldc, M, N, trans_out};
+    return gemm(al, bl, ep, M, N, K, 1, st);
+}
+
+// BP slices: img[rf][n] = sum_{(p,tf)} W[p][rf][tf] * Zt[n][(p,tf)].
+cudaError_t launch_gemm_bpimg(const float *W, int RF, int TF, int nparticles, const float *Zt, long long ldz,
+                              int N2, float *img, long long ldi, cudaStream_t st) {
+    const int KB = nparticles * TF;
+    WeightsByRow al{};
+    al.w = W; al.RF = RF; al.TF = TF; al.KB = KB;
+    RowsK bl{};
+    bl.a = Zt; bl.ld = ldz; bl.zstride = 0; bl.rows = N2;
+    StoreEpi ep{img, ldi, RF, N2, 0};
+    return gemm(al, bl, ep, RF, N2, KB, 1, st);
+}
+
+// sigma2 cross: per particle z, H[tf][n] = sum_rf W[z][rf][tf] P[rf][n],
+// reduced on the fly into G[z][k] = sum_tf H[tf][k] conj(E[tf][k]).
+cudaError_t launch_gemm_sigma_cross(const float *W, int RF, int TF, int nparticles, const float *P, long long ldp,
+                                    int nf, const float2 *E, float2 *G, cudaStream_t st) {
+    WeightsByTrans al{};
+    al.w = W; al.RF = RF; al.TF = TF;
+    ColsM bl{};
+    bl.a = P; bl.ld = ldp; bl.zstride = 0; bl.rows = 2 * nf; bl.kmax = RF;
+    ConjPhaseReduceEpi ep{G, E, TF, nf};
+    return gemm(al, bl, ep, TF, 2 * nf, RF, nparticles, st);
+}
+
+// S[p][k] = sum_rf Wrow[p][rf] P2[rf][k] (P2 stored [rf][ldp2]).
+cudaError_t launch_gemm_sigma_norm(const float *Wrow, long long ldw, int nparticles, int RF, const float *P2,
+                                   long long ldp2, int nf, float *S, cudaStream_t st) {
+    RowsK al{};
+    al.a = Wrow; al.ld = ldw; al.zstride = 0; al.rows = nparticles;
+    ColsM bl{};
+    bl.a = P2; bl.ld = ldp2; bl.zstride = 0; bl.rows = nf; bl.kmax = RF;
+    StoreEpi ep{S, nf, nparticles, nf, 0};
+    return gemm(al, bl, ep, nparticles, nf, RF, 1, st);
 }
 
 }  // namespace gbr

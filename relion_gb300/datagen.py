@@ -208,20 +208,29 @@ class Dataset:
             pdf_direction=np.full(K * ndir, 1.0 / (K * ndir)))
 
     def _noise_level(self):
-        """sigma^2 per complex Fourier coefficient for the configured SNR,
-        from the mean signal power over full-size images of a few poses."""
-        box = self.cfg["box"]
+        """sigma^2 per complex Fourier coefficient for the configured SNR:
+        SNR = variance of the noise-free, CTF-modulated particle image over
+        the full box (DC excluded) / noise variance, estimated on a few poses
+        and defoci drawn from the configuration's distributions."""
+        c = self.cfg
+        box, pix = c["box"], c["pixel"]
         g = torch.Generator().manual_seed(self.seed + 7)
-        R = random_rotations(4, g)
+        nsamp = 4
+        R = random_rotations(nsamp, g)
+        dlo, dhi = c["defocus"]
         x, y = fourier_grid(box)
         k2 = torch.stack([x, y, torch.zeros_like(x)], -1) / box
+        notdc = ~((x == 0) & (y == 0))
         p = 0.0
-        for i in range(4):
-            k3 = k2 @ R[i]          # A^T (x, y, 0): row vector times A
-            f = self.vol.ft(k3)
-            p += float((f.abs() ** 2).mean()) / 4
+        for i in range(nsamp):
+            dU = dlo + (dhi - dlo) * float(torch.rand(1, generator=g, dtype=torch.float64))
+            dV = dlo + (dhi - dlo) * float(torch.rand(1, generator=g, dtype=torch.float64))
+            dA = 180.0 * float(torch.rand(1, generator=g, dtype=torch.float64))
+            f = self.vol.ft(k2 @ R[i]).cpu()
+            ctf = ctf_value(dU, dV, dA, x / (box * pix), y / (box * pix))
+            p += float(((f * ctf).abs() ** 2)[notdc].mean()) / nsamp
         self.signal_power = p
-        self.sigma2 = p / self.cfg["snr"]
+        self.sigma2 = p / c["snr"]
 
     def particles(self, start=0, count=None):
         """Particle batch [start, start+count) as host numpy arrays (E-step

@@ -181,7 +181,7 @@ class MlOptimiserCuda:
             pass
 
 
-STAGES = ["prep", "norm_gemm", "cross_gemm", "weights_coarse", "jobs_proj_fine", "diff2_fine",
+STAGES = ["prep", "norm_gemm", "cross_gemm", "weights_coarse", "sig_jobs", "diff2_fine",
           "weights_fine", "wsum", "backproject", "readback"]
 
 

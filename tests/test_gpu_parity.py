@@ -41,7 +41,13 @@ def _check(st, tol):
     assert st["dLL_abs"] <= 1e-2
 
 
-def test_parity_order1(cmp):
+@pytest.fixture(params=["dense", "sparse"])
+def fine_mode(request, monkeypatch):
+    monkeypatch.setenv("GBR_FINE_MODE", request.param)
+    return request.param
+
+
+def test_parity_order1(cmp, fine_mode):
     m, refs, b = _case("cfg0_box64", 11, 6, healpix_order=1, psi_step=30.0)
     st = cmp.compare(m, refs, b)
     assert st["sig_mismatch"] == 0 and st["fine_set_mismatch"] == 0
