@@ -246,11 +246,17 @@ struct ConjPhaseReduceEpi {
     }
 };
 
-template <class AL, class BL, class EP>
-__global__ void __launch_bounds__(NT, 2) k_gemm(AL al, BL bl, EP ep, int K) {
+// kMerge: every kMergeTiles K tiles the FP32 register partials are added
+// into an FP64 tile in shared memory (long contractions whose result is
+// later combined with cancellation: sigma2 cross / norm, BP slices).
+constexpr int kMergeTiles = 8;
+
+template <class AL, class BL, class EP, bool kMerge>
+__global__ void __launch_bounds__(NT, kMerge ? 1 : 2) k_gemm(AL al, BL bl, EP ep, int K) {
     __shared__ __align__(16) float As[2][BK][BM];
     __shared__ __align__(16) float Bs[2][BK][BN];
     __shared__ unsigned int smin[BN + 2];
+    extern __shared__ double Cd[];  // [BM * BN] when kMerge
     const int tid = threadIdx.x, z = blockIdx.z;
     const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
     const int tm = tid >> 4, tn = tid & 15;
@@ -260,6 +266,21 @@ __global__ void __launch_bounds__(NT, 2) k_gemm(AL al, BL bl, EP ep, int K) {
     for (int i = 0; i < 8; ++i)
 #pragma unroll
         for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
+    auto merge = [&]() {
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                Cd[row_of(tm, i) * BN + row_of(tn, j)] += (double)acc[i][j];
+                acc[i][j] = 0.f;
+            }
+    };
+    if (kMerge) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+#pragma unroll
+            for (int j = 0; j < 8; ++j) Cd[row_of(tm, i) * BN + row_of(tn, j)] = 0.;
+    }
     const int nk = (K + BK - 1) / BK;
     al.load(z, m0, 0, tid, ra);
     bl.load(z, n0, 0, tid, rb);
@@ -288,21 +309,39 @@ __global__ void __launch_bounds__(NT, 2) k_gemm(AL al, BL bl, EP ep, int K) {
 #pragma unroll
                 for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
         }
+        if (kMerge && ((kt + 1) % kMergeTiles == 0 || kt + 1 == nk)) merge();
         if (kt + 1 < nk) {
             AL::store(As[cur ^ 1], tid, ra);
             BL::store(Bs[cur ^ 1], tid, rb);
             __syncthreads();
         }
     }
+    if (kMerge) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+#pragma unroll
+            for (int j = 0; j < 8; ++j) acc[i][j] = (float)Cd[row_of(tm, i) * BN + row_of(tn, j)];
+    }
     ep.run(z, m0, n0, tm, tn, acc, smin);
 }
 
-template <class AL, class BL, class EP>
+template <bool kMerge = false, class AL, class BL, class EP>
 cudaError_t gemm(const AL &al, const BL &bl, const EP &ep, int M, int N, int K, int batch, cudaStream_t st) {
     if (M <= 0 || N <= 0 || K <= 0 || batch <= 0) return cudaSuccess;
     dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM, batch);
     if (grid.y > 65535 || grid.z > 65535) return cudaErrorInvalidConfiguration;
-    k_gemm<AL, BL, EP><<<grid, NT, 0, st>>>(al, bl, ep, K);
+    size_t smem = 0;
+    if (kMerge) {
+        smem = sizeof(double) * BM * BN;
+        static bool attr = false;  // one flag per instantiation
+        if (!attr) {
+            cudaError_t e = cudaFuncSetAttribute(k_gemm<AL, BL, EP, kMerge>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return e;
+            attr = true;
+        }
+    }
+    k_gemm<AL, BL, EP, kMerge><<<grid, NT, smem, st>>>(al, bl, ep, K);
     return cudaGetLastError();
 }
 
@@ -383,7 +422,7 @@ cudaError_t launch_gemm_bpimg(const float *W, int RF, int TF, int nparticles, co
     RowsK bl{};
     bl.a = Zt; bl.ld = ldz; bl.zstride = 0; bl.rows = N2;
     StoreEpi ep{img, ldi, RF, N2, 0};
-    return gemm(al, bl, ep, RF, N2, KB, 1, st);
+    return gemm<true>(al, bl, ep, RF, N2, KB, 1, st);
 }
 
 // sigma2 cross: per particle z, H[tf][n] = sum_rf W[z][rf][tf] P[rf][n],
@@ -395,7 +434,7 @@ cudaError_t launch_gemm_sigma_cross(const float *W, int RF, int TF, int nparticl
     ColsM bl{};
     bl.a = P; bl.ld = ldp; bl.zstride = 0; bl.rows = 2 * nf; bl.kmax = RF;
     ConjPhaseReduceEpi ep{G, E, TF, nf};
-    return gemm(al, bl, ep, TF, 2 * nf, RF, nparticles, st);
+    return gemm<true>(al, bl, ep, TF, 2 * nf, RF, nparticles, st);
 }
 
 // S[p][k] = sum_rf Wrow[p][rf] P2[rf][k] (P2 stored [rf][ldp2]).
@@ -406,7 +445,7 @@ cudaError_t launch_gemm_sigma_norm(const float *Wrow, long long ldw, int npartic
     ColsM bl{};
     bl.a = P2; bl.ld = ldp2; bl.zstride = 0; bl.rows = nf; bl.kmax = RF;
     StoreEpi ep{S, nf, nparticles, nf, 0};
-    return gemm(al, bl, ep, nparticles, nf, RF, 1, st);
+    return gemm<true>(al, bl, ep, nparticles, nf, RF, 1, st);
 }
 
 }  // namespace gbr
