@@ -35,6 +35,12 @@ sys.path.insert(0, ROOT)
 METRIC = "E-step particles/s @box256, 1 GB300: learned+batched vs plain GPU at equal FSC"
 CONFIG = "cfg1_box256"
 
+# DRAM bytes of one coarse cross-term GEMM launch from the ncu capture of a
+# 16-particle batch (profiles/coarse_cross_gemm_box256_b16.md): the
+# projection-table read is independent of the batch, the diff2 write grows
+# with it.
+NCU_CROSS_B16 = {"read": 262.75e6, "write": 222.41e6, "batch": 16}
+
 
 def parse():
     ap = argparse.ArgumentParser()
@@ -221,7 +227,8 @@ def run_ours(args, world, rank, local):
         "roofline": {"bound": "fp32", "kernel": "coarse cross-term GEMM (k_gemm<RowsK,CrossY,Diff2Epi>)",
                      "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                      "peak_source": "measured live (gbr_measure_fp32_peak: FMA chains on all SMs)",
-                     "traffic": None},
+                     "traffic": NCU_CROSS_B16["read"] + NCU_CROSS_B16["write"] * B / NCU_CROSS_B16["batch"],
+                     "traffic_note": "ncu dram read+write of a 16-particle launch, write scaled to the batch"},
         "stage_ms": {k: round(float(v), 4) for k, v in zip(STAGES, stage)},
         "mean_nr_sign": float(np.mean(res["nr_sign"])),
         "mean_fine_poses": float(np.mean(res["n_fine"])),
