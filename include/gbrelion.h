@@ -199,6 +199,26 @@ int gbr_worker_launch_count(const gbr_worker *w, int64_t *count);
  * No counterpart in the reference (a measurement utility). */
 int gbr_measure_fp32_peak(int device, double *tflops);
 
+/* Significance threshold of n rows of non-negative weights ([n][len],
+ * device memory), with no memory allocation of any kind.  No counterpart in
+ * the reference: it serves callers that cannot allocate device memory where
+ * they need this step (code inside a no-allocation region, a host
+ * application that only hands over device pointers, or a fixed up-front
+ * memory budget).  For each row it returns the weight at which the
+ * descending cumulative sum first exceeds adaptive_fraction x the row's sum
+ * and the number of weights taken until then (the significance rule of
+ * src/ml_optimiser.cpp:8120-8200 without --maxsig), in device arrays
+ * threshold[n] and nr_significant[n]; work is queued on `stream` (a
+ * cudaStream_t, NULL for the default stream) and runs asynchronously.
+ * Limit: n <= 64 rows per call (larger n: GBR_ERR_INVALID).  Its working
+ * memory is one fixed array of about 4.3 MB per GPU, held until the process
+ * exits and shared by all calls: calls that overlap on the GPU race and must
+ * be ordered by the caller.  The first call on a device looks up that
+ * array's address; make it before any stream capture. */
+int gbr_significance_threshold_noalloc(const float *weights, int64_t n, int64_t len,
+                                       double adaptive_fraction, float *threshold,
+                                       uint32_t *nr_significant, void *stream);
+
 /* delete MlOptimiserCuda / MlDeviceBundle (src/ml_optimiser.cpp:3840-3868). */
 int gbr_worker_destroy(gbr_worker *w);
 int gbr_bundle_destroy(gbr_bundle *b);

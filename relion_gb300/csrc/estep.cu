@@ -96,6 +96,8 @@ enum Stage { ST_PREP = 0, ST_NORM, ST_CROSS, ST_WCOARSE, ST_SIG, ST_PROJF, ST_FI
 
 }  // namespace
 
+void gbr::set_error_text(const std::string &msg) { g_last_error = msg; }
+
 struct gbr_bundle {
     gbr_model_desc d{};
     int device = 0;

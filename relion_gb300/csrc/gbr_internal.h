@@ -14,6 +14,9 @@ struct Error {
     std::string text;
 };
 
+// Set the text returned by gbr_last_error() on this thread.
+void set_error_text(const std::string &msg);
+
 // One active Fourier pixel of a 2D image of size s (FFTW half layout):
 // logical frequency (x, y), its index in the full [s][s/2+1] image, and its
 // resolution shell (Mresol, src/ml_optimiser.cpp:5784-5795).
