@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--precision", default="bf16", choices=["fp32", "bf16"],
+                    help="coarse cross term: plain FP32 SIMT or tcgen05 BF16 (precision form)")
     return ap.parse_args()
 
 
@@ -121,7 +123,7 @@ def run_ours(args, world, rank, local):
     dev = torch.device("cuda", local)
     B = args.batch
     ds = datagen.Dataset(CONFIG, seed=args.seed + rank, n_particles=B, device=str(dev))
-    model = ds.model()
+    model = ds.model(precision=1 if args.precision == "bf16" else 0)
     batch = ds.particles(0, B)
     bundle = MlDeviceBundle(model, device=local)
     r = ds.ref
@@ -200,8 +202,17 @@ def run_ours(args, world, rank, local):
     nc = active_coarse_pixels(model)
     flops = 2.0 * R * (B * T) * (2 * nc)
     cross_ms = float(stage[STAGES.index("cross_gemm")])
-    peak = measure_fp32_peak(local)
     achieved = flops / (cross_ms * 1e-3) / 1e12
+    if args.precision == "bf16":
+        peak, bound = measured_peaks().get("bf16_tflops"), "tensor"
+        peak_src = "MEASURED_PEAKS.json bf16_tflops (burst, cuBLAS bf16)"
+        kname = "coarse cross-term GEMM, tcgen05 BF16 (k_tc_diff2)"
+        if not peak:
+            peak, peak_src = 1900.0, "fallback 1.9 PFLOP/s bf16 burst"
+    else:
+        peak, bound = measure_fp32_peak(local), "fp32"
+        peak_src = "measured live (gbr_measure_fp32_peak: FMA chains on all SMs)"
+        kname = "coarse cross-term GEMM, FP32 SIMT (k_gemm<RowsK,CrossY,Diff2Epi>)"
     d2h = B * (96 + (model["ori_size"] // 2 + 1) * 8 + 64) + (R + 2) * 8
     out = {
         "metric": METRIC,
@@ -214,20 +225,24 @@ def run_ours(args, world, rank, local):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "fp32",
+        "dtype": "bf16 (coarse cross term) / fp32 (fine pass) / f64 (sums, volumes)"
+                 if args.precision == "bf16" else "fp32 / f64 (sums, volumes)",
         "data": "synthetic (seeded Gaussian-blob volume, analytic Fourier slices, CTF, white noise)",
         "config": {"workload": "box256 E-step, iteration-1 sizes (current 46 px), HEALPix order 3 x 48 psi, "
                                "113 translations, oversampling 1, 1 class",
-                   "batch_particles": B, "precision": "plain FP32 path",
+                   "batch_particles": B,
+                   "precision": "precision form: tcgen05 BF16 coarse pass, FP32 fine pass"
+                                if args.precision == "bf16" else "plain FP32 path",
                    "l2": "flushed (512 MB write) before every timed step",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "e2e": {"value": world * B * args.steps / (e2e_total * 1e-3), "unit": "particles/s",
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches),
-        "roofline": {"bound": "fp32", "kernel": "coarse cross-term GEMM (k_gemm<RowsK,CrossY,Diff2Epi>)",
+        "roofline": {"bound": bound, "kernel": kname,
                      "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                     "peak_source": "measured live (gbr_measure_fp32_peak: FMA chains on all SMs)",
-                     "traffic": NCU_CROSS_B16["read"] + NCU_CROSS_B16["write"] * B / NCU_CROSS_B16["batch"],
+                     "peak_source": peak_src,
+                     "traffic": (NCU_CROSS_B16["read"] + NCU_CROSS_B16["write"] * B / NCU_CROSS_B16["batch"])
+                     if args.precision == "fp32" else None,
                      "traffic_note": "ncu dram read+write of a 16-particle launch, write scaled to the batch"},
         "stage_ms": {k: round(float(v), 4) for k, v in zip(STAGES, stage)},
         "mean_nr_sign": float(np.mean(res["nr_sign"])),
@@ -236,6 +251,14 @@ def run_ours(args, world, rank, local):
     if rank == 0:
         out["clocks"] = clk.summary()
     return out, ds, batch, model
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return json.load(fh)
+    except (OSError, ValueError):
+        return {}
 
 
 def active_coarse_pixels(model):

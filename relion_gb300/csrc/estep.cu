@@ -131,10 +131,12 @@ struct gbr_bundle {
     DevBuf<float> eul_c, eul_f;
     DevBuf<int> cls_c, cls_f, cls_of_r;
     DevBuf<float> pdf_orient;
+    float pdf_orient_min = 0.f;  // smallest non-zero normalised pdf_orient
     DevBuf<double> tx, ty, otx, oty;
     std::vector<double> otx_h, oty_h;
     DevBuf<float2> phase_c, phase_f;
     DevBuf<float> proj_c, proj2_c;
+    DevBuf<unsigned char> proj_c_tc;  // precision form: BF16 A tiles (tcgen05 smem image)
     DevBuf<float> proj_f, proj2_f;  // all oversampled orientations: [RF][lda_f], [RF][ldk_f]
     int ldk_f = 0, lda_f = 0;
     DevBuf<float2> bpimg;
@@ -177,6 +179,12 @@ struct gbr_worker {
     DevBuf<int> ejob;
     DevBuf<unsigned int> ecode;
     DevBuf<double> shell, pacc;
+    DevBuf<unsigned char> ytc;  // precision form: BF16 B tiles of the batch
+    // coarse significance candidates
+    int cand_cap = 0;
+    DevBuf<unsigned int> cand_idx, cand_cnt;
+    DevBuf<float> cand_w, dense_dbg;
+    DevBuf<long long> cand_seg;  // [2n]: begins, ends
     // dense fine pass
     int fine_mode = 0;  // 0: by significant density, 1: always dense, 2: always sparse
     int last_dense = 0;
@@ -292,6 +300,9 @@ int build_tables(gbr_bundle *b) {
     GBR_CUDA(b->cls_f.upload(cf.data(), cf.size()));
     GBR_CUDA(b->cls_of_r.upload(cr.data(), cr.size()));
     GBR_CUDA(b->pdf_orient.upload(po.data(), po.size()));
+    b->pdf_orient_min = 0.f;
+    for (float v : po)
+        if (v > 0.f && (b->pdf_orient_min == 0.f || v < b->pdf_orient_min)) b->pdf_orient_min = v;
 
     // ---- translations and phase tables ----
     std::vector<double> tx(b->grid.trans_x), ty(b->grid.trans_y);
@@ -328,6 +339,12 @@ int build_tables(gbr_bundle *b) {
     GBR_CUDA(b->proj2_c.zero());
     GBR_CUDA(launch_project_rows(b->vols_d.p, b->pg, b->eul_c.p, b->cls_c.p, nullptr, (int)R, b->pc.p, b->nc,
                                  b->proj_c.p, b->lda_c, b->proj2_c.p, b->ldk_c, nullptr, 0));
+    if (d.precision == GBR_PREC_BF16) {
+        GBR_CUDA(b->proj_c_tc.reserve(tc_a_bytes((int)R, 2 * b->nc)));
+        GBR_CUDA(launch_tc_pack_a(b->proj_c.p, b->lda_c, (int)R, 2 * b->nc, b->proj_c_tc.p, 0));
+        int flag = 0;
+        GBR_CUDA(tc_error_flag(&flag, 1));
+    }
     // ---- fine projections of every oversampled orientation ----
     b->ldk_f = pad16(std::max(b->nf, 1));
     b->lda_f = 2 * b->ldk_f;
@@ -397,14 +414,18 @@ int ensure_capacity(gbr_worker *w, int n) {
     return GBR_OK;
 }
 
-int threshold_search(gbr_worker *w, int n, float *vals, const long long *seg, long long max_len, int coarse) {
+int threshold_search(gbr_worker *w, int n, float *vals, const long long *seg, long long max_len, int coarse,
+                     const long long *seg_end = nullptr, long long n_total = 0) {
     gbr_bundle *b = w->b;
-    w->launches += 5;
-    GBR_CUDA(launch_select(n, 0, b->d.adaptive_fraction, coarse, w->ps.p, w->hist.p, w->st));
-    GBR_CUDA(launch_hist_refine(vals, seg, n, max_len, 1, w->ps.p, w->hist.p, w->st));
-    GBR_CUDA(launch_select(n, 1, b->d.adaptive_fraction, coarse, w->ps.p, w->hist.p, w->st));
-    GBR_CUDA(launch_hist_refine(vals, seg, n, max_len, 2, w->ps.p, w->hist.p, w->st));
-    GBR_CUDA(launch_select(n, 2, b->d.adaptive_fraction, coarse, w->ps.p, w->hist.p, w->st));
+    w->launches += 6;
+    const double f = b->d.adaptive_fraction;
+    const int pass = coarse ? 1 : 2;
+    GBR_CUDA(launch_hist_refine(vals, seg, n, max_len, 0, w->ps.p, w->hist.p, w->st, pass, f, seg_end, n_total));
+    GBR_CUDA(launch_select(n, 0, f, coarse, w->ps.p, w->hist.p, w->st));
+    GBR_CUDA(launch_hist_refine(vals, seg, n, max_len, 1, w->ps.p, w->hist.p, w->st, pass, f, seg_end, n_total));
+    GBR_CUDA(launch_select(n, 1, f, coarse, w->ps.p, w->hist.p, w->st));
+    GBR_CUDA(launch_hist_refine(vals, seg, n, max_len, 2, w->ps.p, w->hist.p, w->st, pass, f, seg_end, n_total));
+    GBR_CUDA(launch_select(n, 2, f, coarse, w->ps.p, w->hist.p, w->st));
     return GBR_OK;
 }
 
@@ -555,26 +576,81 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
     // ---- coarse norm and cross GEMMs ----
     GBR_CUDA(launch_gemm_rows(b->proj2_c.p, b->ldk_c, R, w->a_c.p, b->ldk_c, n, b->ldk_c, w->nrm.p, R, 1, st));
     GBR_CUDA(cudaEventRecord(w->ev[2], st));
-    GBR_CUDA(launch_gemm_diff2(b->proj_c.p, b->lda_c, R, 2 * b->nc, w->b_c.p, b->ldk_c, b->phase_c.p, b->ldk_c, n, T,
-                               w->vals.p, w->nrm.p, b->pdf_orient.p, nullptr, 1, 1, W, w->ps.p, 0, st));
+    if (d.precision == GBR_PREC_BF16) {
+        GBR_CUDA(w->ytc.reserve(tc_y_bytes(n * T, 2 * b->nc)));
+        GBR_CUDA(launch_tc_diff2(b->proj_c_tc.p, w->ytc.p, R, 2 * b->nc, w->b_c.p, b->ldk_c, b->phase_c.p, b->ldk_c, n,
+                                 T, w->vals.p, w->nrm.p, b->pdf_orient.p, w->ps.p, st));
+        w->launches += 1;
+    } else {
+        GBR_CUDA(launch_gemm_diff2(b->proj_c.p, b->lda_c, R, 2 * b->nc, w->b_c.p, b->ldk_c, b->phase_c.p, b->ldk_c,
+                                   n, T, w->vals.p, w->nrm.p, b->pdf_orient.p, nullptr, 1, 1, W, w->ps.p, 0, st));
+    }
     GBR_CUDA(cudaEventRecord(w->ev[3], st));
     if (w->debug) {
         w->dbg_coarse.resize((size_t)n * RT);
         GBR_CUDA(cudaMemcpyAsync(w->dbg_coarse.data(), w->vals.p, sizeof(float) * n * RT, cudaMemcpyDeviceToHost, st));
     }
     // ---- coarse weights and significance ----
-    GBR_CUDA(launch_weights(w->vals.p, w->seg_c.p, n, RT, 1, T, nullptr, nullptr, nullptr, nOR, nOT,
-                            b->pdf_orient.p, w->pdf_off.p, w->ps.p, w->hist.p, st));
-    {
+    // one read of the diff2 array: weights, FP64 sums and the candidate lists;
+    // the threshold search and the significance masks then run on the lists
+    const int cap = (int)std::min<long long>(RT, 1 << 16);
+    if (w->cand_cap < cap || w->cand_idx.n < (size_t)n * cap) {
+        GBR_CUDA(w->cand_idx.reserve((size_t)n * cap));
+        GBR_CUDA(w->cand_w.reserve((size_t)n * cap));
+        w->cand_cap = cap;
+    }
+    GBR_CUDA(w->cand_cnt.reserve(n));
+    GBR_CUDA(w->cand_seg.reserve(2 * (size_t)n));
+    GBR_CUDA(cudaMemsetAsync(w->cand_cnt.p, 0, sizeof(unsigned int) * n, st));
+    float *dense_w = nullptr;
+    if (w->debug) {
+        GBR_CUDA(w->dense_dbg.reserve((size_t)n * RT));
+        dense_w = w->dense_dbg.p;
+    }
+    GBR_CUDA(launch_weights_cand(w->vals.p, n, R, T, b->pdf_orient.p, b->pdf_orient_min, w->pdf_off.p,
+                                 d.adaptive_fraction, w->ps.p, w->cand_idx.p, w->cand_w.p, w->cand_cnt.p, cap,
+                                 dense_w, st));
+    std::vector<unsigned int> ccnt(n);
+    GBR_CUDA(cudaMemcpyAsync(ccnt.data(), w->cand_cnt.p, sizeof(unsigned int) * n, cudaMemcpyDeviceToHost, st));
+    GBR_CUDA(cudaStreamSynchronize(st));
+    if (d.precision == GBR_PREC_BF16) {
+        int flag = 0;
+        GBR_CUDA(tc_error_flag(&flag, 1));
+        if (flag) return fail(GBR_ERR_CUDA, "tensor-core pipeline timed out waiting for its MMAs");
+    }
+    unsigned int cmax = 0;
+    for (unsigned int c : ccnt) cmax = std::max(cmax, c);
+    const bool use_cand = cmax <= (unsigned int)cap;
+    w->launches += 1;
+    if (use_cand) {
+        std::vector<long long> cs(2 * n);
+        for (int p = 0; p < n; ++p) {
+            cs[p] = (long long)p * cap;
+            cs[n + p] = (long long)p * cap + ccnt[p];
+        }
+        GBR_CUDA(cudaMemcpyAsync(w->cand_seg.p, cs.data(), sizeof(long long) * 2 * n, cudaMemcpyHostToDevice, st));
+        int s = threshold_search(w, n, w->cand_w.p, w->cand_seg.p, std::max<long long>(cmax, 1), 1,
+                                 w->cand_seg.p + n, RT);
+        if (s) return s;
+        GBR_CUDA(cudaMemsetAsync(w->mask.p, 0, sizeof(unsigned int) * (size_t)n * R * W, st));
+        GBR_CUDA(cudaMemsetAsync(w->cnt.p, 0, sizeof(int) * (size_t)n * R, st));
+        GBR_CUDA(launch_cand_masks(w->cand_idx.p, w->cand_w.p, w->cand_cnt.p, cap, n, R, T, W, w->ps.p, w->mask.p,
+                                   w->cnt.p, st));
+        w->launches += 1;
+    } else {
+        // a list overflowed (flat posterior): search the full weight array
+        GBR_CUDA(launch_weights(w->vals.p, w->seg_c.p, n, RT, 1, T, nullptr, nullptr, nullptr, nOR, nOT,
+                                b->pdf_orient.p, w->pdf_off.p, w->ps.p, w->hist.p, st, 0));
         int s = threshold_search(w, n, w->vals.p, w->seg_c.p, RT, 1);
         if (s) return s;
+        GBR_CUDA(launch_sig_masks(w->vals.p, n, R, T, W, w->ps.p, w->mask.p, w->cnt.p, st));
+        w->launches += 2;
     }
     GBR_CUDA(cudaEventRecord(w->ev[4], st));
     if (w->debug) {
         w->dbg_wcoarse.resize((size_t)n * RT);
-        GBR_CUDA(cudaMemcpyAsync(w->dbg_wcoarse.data(), w->vals.p, sizeof(float) * n * RT, cudaMemcpyDeviceToHost, st));
+        GBR_CUDA(cudaMemcpyAsync(w->dbg_wcoarse.data(), dense_w, sizeof(float) * n * RT, cudaMemcpyDeviceToHost, st));
     }
-    GBR_CUDA(launch_sig_masks(w->vals.p, n, R, T, W, w->ps.p, w->mask.p, w->cnt.p, st));
     const long long nR = (long long)n * R;
     GBR_CUDA(launch_flag_counts(w->cnt.p, nR, w->flags.p, w->entries.p, nOR * nOT, st));
     GBR_CUDA(launch_scan_i64(w->flags.p, w->jpos.p, nR, w->scan_tmp.p, st));
@@ -587,7 +663,7 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
     std::vector<long long> segf(n + 1);
     GBR_CUDA(cudaMemcpyAsync(segf.data(), w->seg_f.p, sizeof(long long) * (n + 1), cudaMemcpyDeviceToHost, st));
     GBR_CUDA(cudaStreamSynchronize(st));
-    w->launches += 15;
+    w->launches += 10;
     if (njobs <= 0 || nfine <= 0) return fail(GBR_ERR_NUMERICAL, "no significant coarse samples");
     // ---- fine pass: dense contractions when most poses are significant ----
     const double density = (double)nfine / ((double)n * b->RF * b->TF);
@@ -734,8 +810,8 @@ int gbr_bundle_create(const gbr_model_desc *desc, int device, gbr_bundle **out) 
         return fail(GBR_ERR_UNSUPPORTED, "only --oversampling 1 is implemented");
     if (d.maximum_significants > 0)
         return fail(GBR_ERR_UNSUPPORTED, "--maxsig is not implemented");
-    if (d.precision != GBR_PREC_FP32)
-        return fail(GBR_ERR_UNSUPPORTED, "only the FP32 path is implemented");
+    if (d.precision != GBR_PREC_FP32 && d.precision != GBR_PREC_BF16)
+        return fail(GBR_ERR_INVALID, "unknown precision");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev)
         return fail(GBR_ERR_CUDA, "no CUDA device " + std::to_string(device));

@@ -47,7 +47,7 @@ struct ParticleState {
     float thr_coarse;               // significant weight of the coarse pass
     float thr_fine;                 // significant weight of the fine pass
     unsigned int nr_sign;           // significant count (coarse pass)
-    unsigned int pad_;
+    float eps;                      // weights below eps cannot reach the threshold
 };
 
 // Fine-pass job: one (particle, significant coarse orientation).
@@ -82,6 +82,17 @@ cudaError_t launch_project_rows(const float2 *const *vols, const VolGeom &g, con
 
 // FP32 FMA throughput probe (ms of one timed launch and its flop count).
 cudaError_t launch_fp32_probe(float *ms, double *flops);
+
+// k_tc.cu: tcgen05 BF16 coarse cross term (precision form).  Operand tiles
+// are packed into [tiles][ktiles][bytes] images (sizes from tc_*_bytes).
+size_t tc_a_bytes(int M, int K2);
+size_t tc_y_bytes(int N, int K2);
+cudaError_t launch_tc_pack_a(const float *src, int lds, int M, int K2, void *dst, cudaStream_t st);
+cudaError_t launch_tc_diff2(const void *Ablk, void *Yblk, int M, int K2, const float2 *b, int ldb, const float2 *E,
+                            int lde, int nparticles, int T, float *out, const float *norm, const float *pdf_orient,
+                            ParticleState *ps, cudaStream_t st);
+// Read (and optionally clear) the tensor-core pipeline error flag.
+cudaError_t tc_error_flag(int *flag, int reset);
 
 // k_gemm.cu: C[m][n] = sum_k A[m][k] * Bop[n][k], FP32 SIMT.
 // Cross term + diff2 epilogue; output [p][M][T] relative to c_p, +inf where
@@ -125,10 +136,21 @@ cudaError_t launch_pdf_offset(const double *pdat, int n, const double *tx, const
 cudaError_t launch_weights(float *vals, const long long *seg, int n, long long max_len, int coarse,
                            int T, const int *ejob, const unsigned int *ecode, const FineJob *jobs,
                            int nOR, int nOT, const float *pdf_orient, const float *pdf_off,
-                           ParticleState *ps, HistBin *hist, cudaStream_t st);
-// Threshold search levels 0..2 (12, 12, 7 bits).
+                           ParticleState *ps, HistBin *hist, cudaStream_t st, int add_sum = 1);
+// Threshold search levels 0..2 (12, 12, 7 bits).  pass: 1 coarse, 2 fine
+// (weights below (1 - fraction) * sum / segment length are skipped: they
+// cannot reach the threshold), 0: no skipping.
 cudaError_t launch_hist_refine(const float *vals, const long long *seg, int n, long long max_len,
-                               int level, ParticleState *ps, HistBin *hist, cudaStream_t st);
+                               int level, ParticleState *ps, HistBin *hist, cudaStream_t st,
+                               int pass = 0, double fraction = 1.0, const long long *seg_end = nullptr,
+                               long long n_total = 0);
+// Coarse weights + FP64 sums + candidate lists (see k_weights_cand).
+cudaError_t launch_weights_cand(const float *vals, int n, int R, int T, const float *pdf_orient, float pdf_orient_min,
+                                const float *pdf_off, double fraction, ParticleState *ps, unsigned int *cand_idx,
+                                float *cand_w, unsigned int *cand_cnt, int cap, float *dense_out, cudaStream_t st);
+cudaError_t launch_cand_masks(const unsigned int *cand_idx, const float *cand_w, const unsigned int *cand_cnt,
+                              int cap, int n, int R, int T, int W, const ParticleState *ps, unsigned int *mask,
+                              int *cnt, cudaStream_t st);
 cudaError_t launch_select(int n, int level, double adaptive_fraction, int coarse, ParticleState *ps,
                           HistBin *hist, cudaStream_t st);
 cudaError_t launch_sig_masks(const float *w, int n, int R, int T, int W, const ParticleState *ps,

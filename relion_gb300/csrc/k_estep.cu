@@ -156,11 +156,7 @@ __global__ void __launch_bounds__(kWThreads)
 k_weights(float *__restrict__ vals, const long long *__restrict__ seg, int coarse, int T,
           const int *__restrict__ ejob, const unsigned int *__restrict__ ecode,
           const FineJob *__restrict__ jobs, int nOR, int nOT, const float *__restrict__ pdf_orient,
-          const float *__restrict__ pdf_off, ParticleState *__restrict__ ps,
-          HistBin *__restrict__ hist) {
-    extern __shared__ double dsm[];
-    double *hsum = dsm;                                            // [kHistBins]
-    unsigned int *hcnt = reinterpret_cast<unsigned int *>(hsum + kHistBins);  // [kHistBins]
+          const float *__restrict__ pdf_off, ParticleState *__restrict__ ps, int add_sum) {
     __shared__ double sh[32];
     __shared__ unsigned long long smax;
     const int p = blockIdx.y;
@@ -168,12 +164,7 @@ k_weights(float *__restrict__ vals, const long long *__restrict__ seg, int coars
     const long long beg = b0 + (long long)blockIdx.x * kChunk;
     if (beg >= b1) return;
     const long long end = min(beg + (long long)kChunk, b1);
-    for (int i = threadIdx.x; i < kHistBins; i += blockDim.x) {
-        hsum[i] = 0.;
-        hcnt[i] = 0u;
-    }
     if (threadIdx.x == 0) smax = 0ull;
-    __syncthreads();
     const float mn = ord2f(coarse == 1 ? ps[p].min_coarse : ps[p].min_fine);
     double acc = 0.;
     unsigned long long kmax = 0ull;
@@ -188,8 +179,9 @@ k_weights(float *__restrict__ vals, const long long *__restrict__ seg, int coars
                 const long long loc = e - b0;
                 unsigned long long idx = 0;
                 if (coarse == 1) {
-                    r = (int)(loc / T);
-                    t = (int)(loc - (long long)r * T);
+                    const unsigned int l32 = (unsigned int)loc;  // < R*T < 2^32
+                    r = (int)(l32 / (unsigned)T);
+                    t = (int)(l32 - (unsigned)r * (unsigned)T);
                 } else if (coarse == 2) {
                     // dense fine layout [rf][tf], rf = r*nOR + ior, tf = t*nOT + iot:
                     // the loop order of storeWeightedSums is the storage order
@@ -214,13 +206,9 @@ k_weights(float *__restrict__ vals, const long long *__restrict__ seg, int coars
             }
         }
         vals[e] = w;
-        if (w > 0.f) {
-            acc += (double)w;
-            const unsigned int bin = __float_as_uint(w) >> 19;
-            atomicAdd(&hsum[bin], (double)w);
-            atomicAdd(&hcnt[bin], 1u);
-        }
+        acc += (double)w;
     }
+    __syncthreads();
     const double tot = block_sum(acc, sh);
     if (coarse != 1) {
 #pragma unroll
@@ -232,35 +220,139 @@ k_weights(float *__restrict__ vals, const long long *__restrict__ seg, int coars
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        atomicAdd(coarse == 1 ? &ps[p].sum_coarse : &ps[p].sum_fine, tot);
+        if (add_sum) atomicAdd(coarse == 1 ? &ps[p].sum_coarse : &ps[p].sum_fine, tot);
         if (coarse != 1 && smax) atomicMax(&ps[p].argmax_key, smax);
     }
-    HistBin *hp = hist + (size_t)p * kHistBins;
-    for (int i = threadIdx.x; i < kHistBins; i += blockDim.x)
-        if (hcnt[i]) {
-            atomicAdd(&hp[i].sum, hsum[i]);
-            atomicAdd(&hp[i].count, hcnt[i]);
-        }
 }
 
-// Histogram of the next 12 (level 1) or 7 (level 2) bits of the weights that
-// share the prefix selected so far.
+// Coarse pass, first step: diff2 -> weight for every pose, FP64 sum, and a
+// compact list of the candidates for significance: poses whose weight is at
+// least eps_lo = (1 - fraction) * wmin / (R*T), where wmin (the smallest
+// pdf_orient * pdf_offset) is a lower bound on the largest weight and hence
+// eps_lo <= (1 - fraction) * sum / (R*T), the level below which no weight can
+// reach the threshold.  Lists hold at most `cap` entries per particle
+// (overflow -> flag; the driver then runs the full-array search).  The dense
+// weight array is written only when `write_dense` is set.
+__global__ void __launch_bounds__(kWThreads)
+k_weights_cand(const float *__restrict__ vals, int R, int T, const float *__restrict__ pdf_orient,
+               float pdf_orient_min, const float *__restrict__ pdf_off, double fraction,
+               ParticleState *__restrict__ ps, unsigned int *__restrict__ cand_idx,
+               float *__restrict__ cand_w, unsigned int *__restrict__ cand_cnt, int cap,
+               float *__restrict__ dense_out) {
+    __shared__ double sh[32];
+    __shared__ float s_eps;
+    const int p = blockIdx.y;
+    const long long RT = (long long)R * T;
+    const long long beg = (long long)blockIdx.x * kChunk;
+    if (beg >= RT) return;
+    const long long end = min(beg + (long long)kChunk, RT);
+    if (threadIdx.x < 32) {
+        float m = FLT_MAX;
+        for (int t = threadIdx.x; t < T; t += 32) m = fminf(m, pdf_off[(size_t)p * T + t]);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = fminf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (threadIdx.x == 0) s_eps = (float)((1.0 - fraction) * (double)pdf_orient_min * (double)m / (double)RT);
+    }
+    __syncthreads();
+    const float eps_lo = s_eps;
+    const float mn = ord2f(ps[p].min_coarse);
+    const float *row = vals + (size_t)p * RT;
+    unsigned int *ci = cand_idx + (size_t)p * cap;
+    float *cw = cand_w + (size_t)p * cap;
+    const int lane = threadIdx.x & 31;
+    const float invT = 1.f / (float)T;
+    const float *po = pdf_off + (size_t)p * T;
+    // candidates are summed in FP64; the rest (below eps_lo, together less
+    // than (1 - fraction) of the total) in FP32, so the sum is FP64-accurate
+    // to ~1e-10 relative without an FP64 add per pose
+    double acc_c = 0.;
+    float acc_f = 0.f;
+    for (long long e0 = beg; e0 < end; e0 += blockDim.x) {
+        const long long e = e0 + threadIdx.x;
+        float w = 0.f;
+        if (e < end) {
+            const float d = row[e];
+            if (d < FLT_MAX) {
+                const float x = d - mn;
+                if (!(x > 700.f)) {
+                    // e / T by a float reciprocal, corrected to the exact quotient
+                    const int ei = (int)e;
+                    int r = __float2int_rz((float)ei * invT);
+                    int t = ei - r * T;
+                    if (t < 0) { --r; t += T; }
+                    if (t >= T) { ++r; t -= T; }
+                    w = pdf_orient[r] * po[t] * expf(-x);
+                }
+            }
+            if (dense_out) dense_out[(size_t)p * RT + e] = w;
+        }
+        const bool is_c = w > 0.f && w >= eps_lo;
+        if (is_c) acc_c += (double)w;
+        else acc_f += w;
+        const unsigned int ball = __ballot_sync(0xffffffffu, is_c);
+        if (ball) {
+            unsigned int base = 0;
+            if (lane == 0) base = atomicAdd(&cand_cnt[p], (unsigned)__popc(ball));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (is_c) {
+                const unsigned int pos = base + __popc(ball & ((1u << lane) - 1u));
+                if (pos < (unsigned)cap) {
+                    ci[pos] = (unsigned int)e;
+                    cw[pos] = w;
+                }
+            }
+        }
+    }
+    const double tot = block_sum(acc_c + (double)acc_f, sh);
+    if (threadIdx.x == 0) atomicAdd(&ps[p].sum_coarse, tot);
+}
+
+// Significance masks and per-orientation counts from the candidate lists.
+__global__ void k_cand_masks(const unsigned int *__restrict__ cand_idx, const float *__restrict__ cand_w,
+                             const unsigned int *__restrict__ cand_cnt, int cap, int R, int T, int W,
+                             const ParticleState *__restrict__ ps, unsigned int *__restrict__ mask,
+                             int *__restrict__ cnt) {
+    const int p = blockIdx.y;
+    const unsigned int n = min(cand_cnt[p], (unsigned)cap);
+    const float thr = ps[p].thr_coarse;
+    for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float w = cand_w[(size_t)p * cap + i];
+        if (w > 0.f && w >= thr) {
+            const unsigned int e = cand_idx[(size_t)p * cap + i];
+            const int r = (int)(e / (unsigned)T), t = (int)(e - (unsigned)r * (unsigned)T);
+            atomicOr(&mask[((size_t)p * R + r) * W + (t >> 5)], 1u << (t & 31));
+            atomicAdd(&cnt[(size_t)p * R + r], 1);
+        }
+    }
+}
+
+// Histogram of the threshold search: level 0 = top 12 bits of the weights;
+// level 1 / 2 = the next 12 / 7 bits of the weights sharing the prefix
+// selected so far.  With pass 1 / 2 (coarse / fine), weights below
+// eps = (1 - fraction) * sum / (segment length) are skipped: the elements
+// below eps sum to less than (1 - fraction) * sum, so the threshold is >= eps.
 __global__ void __launch_bounds__(kWThreads)
 k_hist_refine(const float *__restrict__ vals, const long long *__restrict__ seg, int level,
-              const ParticleState *__restrict__ ps, HistBin *__restrict__ hist) {
+              const ParticleState *__restrict__ ps, HistBin *__restrict__ hist, int pass,
+              double fraction, const long long *__restrict__ seg_end, long long n_total) {
     extern __shared__ double dsm[];
     double *hsum = dsm;
     unsigned int *hcnt = reinterpret_cast<unsigned int *>(hsum + kHistBins);
     const int p = blockIdx.y;
-    const long long b0 = seg[p], b1 = seg[p + 1];
+    const long long b0 = seg[p], b1 = seg_end ? seg_end[p] : seg[p + 1];
     const long long beg = b0 + (long long)blockIdx.x * kChunk;
     if (beg >= b1) return;
     const long long end = min(beg + (long long)kChunk, b1);
-    const int nb = level == 1 ? kHistBins : 128;
-    const int shift = level == 1 ? 19 : 7;   // bits above the new field
-    const int fshift = level == 1 ? 7 : 0;   // position of the new field
-    const unsigned int fmask = level == 1 ? 0xFFFu : 0x7Fu;
-    const unsigned int prefix = ps[p].sel_prefix;
+    const int nb = level == 2 ? 128 : kHistBins;
+    const int shift = level == 0 ? 31 : (level == 1 ? 19 : 7);   // bits above the new field
+    const int fshift = level == 0 ? 19 : (level == 1 ? 7 : 0);   // position of the new field
+    const unsigned int fmask = level == 2 ? 0x7Fu : 0xFFFu;
+    const unsigned int prefix = level == 0 ? 0u : ps[p].sel_prefix;
+    float eps = 0.f;
+    if (pass) {
+        const double sum = pass == 1 ? ps[p].sum_coarse : ps[p].sum_fine;
+        eps = (float)((1.0 - fraction) * sum / (double)(n_total > 0 ? n_total : b1 - b0));
+    }
     for (int i = threadIdx.x; i < nb; i += blockDim.x) {
         hsum[i] = 0.;
         hcnt[i] = 0u;
@@ -268,7 +360,7 @@ k_hist_refine(const float *__restrict__ vals, const long long *__restrict__ seg,
     __syncthreads();
     for (long long e = beg + threadIdx.x; e < end; e += blockDim.x) {
         const float w = vals[e];
-        if (w > 0.f) {
+        if (w > 0.f && w >= eps) {
             const unsigned int u = __float_as_uint(w);
             if ((u >> shift) == prefix) {
                 const unsigned int bin = (u >> fshift) & fmask;
@@ -1011,28 +1103,25 @@ static size_t hist_smem() { return kHistBins * (sizeof(double) + sizeof(unsigned
 cudaError_t launch_weights(float *vals, const long long *seg, int n, long long max_len, int coarse,
                            int T, const int *ejob, const unsigned int *ecode, const FineJob *jobs,
                            int nOR, int nOT, const float *pdf_orient, const float *pdf_off,
-                           ParticleState *ps, HistBin *hist, cudaStream_t st) {
+                           ParticleState *ps, HistBin *hist, cudaStream_t st, int add_sum) {
+    (void)hist;
     if (n <= 0 || max_len <= 0) return cudaSuccess;
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(k_weights, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hist_smem());
-        cudaFuncSetAttribute(k_hist_refine, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hist_smem());
-        attr = true;
-    }
     const long long nb = (max_len + kChunk - 1) / kChunk;
     if (nb > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
     dim3 grid((unsigned)nb, n);
-    k_weights<<<grid, kWThreads, hist_smem(), st>>>(vals, seg, coarse, T, ejob, ecode, jobs, nOR, nOT,
-                                                    pdf_orient, pdf_off, ps, hist);
+    k_weights<<<grid, kWThreads, 0, st>>>(vals, seg, coarse, T, ejob, ecode, jobs, nOR, nOT, pdf_orient,
+                                          pdf_off, ps, add_sum);
     return cudaGetLastError();
 }
 
 cudaError_t launch_hist_refine(const float *vals, const long long *seg, int n, long long max_len,
-                               int level, ParticleState *ps, HistBin *hist, cudaStream_t st) {
+                               int level, ParticleState *ps, HistBin *hist, cudaStream_t st, int pass,
+                               double fraction, const long long *seg_end, long long n_total) {
     if (n <= 0 || max_len <= 0) return cudaSuccess;
     const long long nb = (max_len + kChunk - 1) / kChunk;
     dim3 grid((unsigned)nb, n);
-    k_hist_refine<<<grid, kWThreads, hist_smem(), st>>>(vals, seg, level, ps, hist);
+    k_hist_refine<<<grid, kWThreads, hist_smem(), st>>>(vals, seg, level, ps, hist, pass, fraction, seg_end,
+                                                        n_total);
     return cudaGetLastError();
 }
 
@@ -1161,6 +1250,27 @@ cudaError_t launch_shell_dense(int n, const float *S2P, const float2 *G, const f
     if (n <= 0) return cudaSuccess;
     k_shell_dense<<<n, 256, sizeof(double) * nshell, st>>>(S2P, G, Xf, Cf, pf, nf, nshell, pdat, do_scale,
                                                            dvp_mask, K, 0, pacc, shell);
+    return cudaGetLastError();
+}
+
+
+cudaError_t launch_weights_cand(const float *vals, int n, int R, int T, const float *pdf_orient, float pdf_orient_min,
+                                const float *pdf_off, double fraction, ParticleState *ps, unsigned int *cand_idx,
+                                float *cand_w, unsigned int *cand_cnt, int cap, float *dense_out, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    const long long RT = (long long)R * T;
+    dim3 grid((unsigned)((RT + kChunk - 1) / kChunk), n);
+    k_weights_cand<<<grid, kWThreads, 0, st>>>(vals, R, T, pdf_orient, pdf_orient_min, pdf_off, fraction, ps,
+                                               cand_idx, cand_w, cand_cnt, cap, dense_out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cand_masks(const unsigned int *cand_idx, const float *cand_w, const unsigned int *cand_cnt,
+                              int cap, int n, int R, int T, int W, const ParticleState *ps, unsigned int *mask,
+                              int *cnt, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    dim3 grid(64, n);
+    k_cand_masks<<<grid, 256, 0, st>>>(cand_idx, cand_w, cand_cnt, cap, R, T, W, ps, mask, cnt);
     return cudaGetLastError();
 }
 

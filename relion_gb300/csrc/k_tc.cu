@@ -1,0 +1,391 @@
+// k_tc.cu -- coarse cross term on the 5th-generation tensor cores (tcgen05),
+// the "precision form" of the coarse pass: BF16 operands, FP32 accumulation
+// in tensor memory (TMEM).
+//
+//   C[r][(p,t)] = sum_k A[r][k] Y[(p,t)][k],  A = projections (BF16 table),
+//   Y = m C X E formed on the fly from FP32 b = m C X and the phase table E,
+// then diff2 - c_p = N(r,p) - 2 C, stored like the FP32 path (k_gemm.cu) with
+// the per-particle minimum.  The coarse pass only decides which poses are
+// significant; every significant pose is re-evaluated in FP32 by the fine pass.
+//
+// Operand tiles are pre-packed in HBM in the exact shared-memory image of a
+// canonical no-swizzle K-major layout (8 x 16-byte core matrices; K-adjacent
+// core matrices 128 B apart, 8-row groups 1024 B apart): the projection
+// table once per iteration (k_pack_a), Y once per batch (k_pack_y).
+// CTA: 256 threads, tile 128 (orientations) x 256 (particle, translation),
+// K tiles of 64 BF16 in a 3-stage shared-memory ring; one thread streams each
+// stage's 48 KB with two cp.async.bulk copies, one thread issues tcgen05.mma
+// (M=128, N=256, K=16, accumulator in 256 TMEM columns), four warps run the
+// epilogue from TMEM.  Every mbarrier wait is bounded: on timeout the CTA
+// records an error, waits (bounded) for its own MMAs, frees its tensor
+// memory and returns.
+#include "gbr_internal.h"
+
+#include <cuda_bf16.h>
+#include <cfloat>
+#include <cstdint>
+
+namespace gbr {
+namespace {
+
+constexpr int TM = 128, TN = 256, TK = 64, STAGES = 3, THREADS = 256;
+constexpr int A_BYTES = TM * TK * 2;          // 16 KB
+constexpr int B_BYTES = TN * TK * 2;          // 32 KB
+constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
+constexpr int TMEM_COLS = 256;
+constexpr unsigned int kWaitLimit = 1u << 22;
+
+__device__ int g_tc_error;  // first failure code of the last launches (0 = ok)
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// Shared-memory matrix descriptor (tcgen05): start >> 4, LBO >> 4, SBO >> 4,
+// descriptor version 1, no swizzle.
+__device__ __forceinline__ uint64_t make_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+
+// Instruction descriptor, kind::f16: D = F32, A = B = BF16, both K-major.
+__host__ __device__ constexpr uint32_t make_idesc() {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TN >> 3) << 17) | ((uint32_t)(TM >> 4) << 24);
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    for (unsigned int it = 0; it < kWaitLimit; ++it) {
+        uint32_t ok;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(ok)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ unsigned int f2ord(float f) {
+    unsigned int u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+    __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<uint32_t *>(&h);
+}
+
+// Byte offset of the 16-byte chunk (row, kg) in a no-swizzle K-major tile
+// with TK/8 = 8 core matrices along K.
+__device__ __forceinline__ uint32_t chunk_off(int row, int kg) {
+    return (uint32_t)((((row >> 3) * (TK / 8) + kg) << 7) + ((row & 7) << 4));
+}
+
+// Chunk c of a tile -> (row, kg): each warp writes 512 contiguous bytes
+// (8 rows x 4 K-groups), so the shared-memory stores are conflict-free.
+__device__ __forceinline__ void chunk_rc(int c, int &row, int &kg) {
+    const int lane = c & 31, wi = c >> 5;
+    kg = (lane >> 3) + 4 * (wi & 1);
+    row = (wi >> 1) * 8 + (lane & 7);
+}
+
+__device__ __forceinline__ bool arrive_expect_tx(uint32_t bar, uint32_t bytes) {
+    uint64_t state;
+    asm volatile("mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 %0, [%1], %2;"
+                 : "=l"(state)
+                 : "r"(bar), "r"(bytes)
+                 : "memory");
+    return state != 0ull || true;
+}
+
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
+
+struct TcArgs {
+    const uint8_t *Ablk;     // [mtiles][ktiles][A_BYTES] BF16 tiles in shared-memory image
+    const uint8_t *Yblk;     // [ntiles][ktiles][B_BYTES]
+    int M, ktiles, T, N;
+    float *out;              // [p][M][T]
+    const float *norm;       // [p][M]
+    const float *pdf_orient; // [M]
+    ParticleState *ps;
+};
+
+// Warp-specialised CTA: warp 0 lane 0 streams the pre-packed operand tiles
+// with cp.async.bulk into the stage ring (full barriers count the bytes),
+// warp 1 lane 0 issues the MMAs and commits each stage to its empty barrier,
+// warps 4-7 read the accumulator from TMEM (lanes 32*(w-4)..) and store.
+__global__ void __launch_bounds__(THREADS, 1) k_tc_diff2(const TcArgs a) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ __align__(8) uint64_t full[STAGES];
+    __shared__ __align__(8) uint64_t empty[STAGES];
+    __shared__ __align__(8) uint64_t done;
+    __shared__ uint32_t tmem_slot;
+    __shared__ int sfail;
+    __shared__ unsigned int smin[TN + 2];  // one per particle of the tile (T >= 1)
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int nt = blockIdx.x, mt = blockIdx.y;
+    const int n0 = nt * TN, m0 = mt * TM;
+    const int nk = a.ktiles;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                     "r"(TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        for (int s = 0; s < STAGES; ++s) {
+            mbar_init(smem_u32(&full[s]), 1);
+            mbar_init(smem_u32(&empty[s]), 1);
+        }
+        mbar_init(smem_u32(&done), 1);
+        sfail = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    for (int i = tid; i < TN + 2; i += THREADS) smin[i] = 0xFFFFFFFFu;
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_slot;
+    const uint32_t sbase = smem_u32(smem);
+
+    if (warp == 0 && lane == 0) {
+        // producer
+        const uint8_t *ab = a.Ablk + (size_t)mt * nk * A_BYTES;
+        const uint8_t *yb = a.Yblk + (size_t)nt * nk * B_BYTES;
+        for (int kt = 0; kt < nk; ++kt) {
+            const int s = kt % STAGES;
+            if (kt >= STAGES && !mbar_wait(smem_u32(&empty[s]), (uint32_t)(((kt / STAGES) - 1) & 1))) {
+                sfail = 1;
+                break;
+            }
+            const uint32_t st = sbase + s * STAGE_BYTES;
+            arrive_expect_tx(smem_u32(&full[s]), (uint32_t)STAGE_BYTES);
+            bulk_g2s(st, ab + (size_t)kt * A_BYTES, A_BYTES, smem_u32(&full[s]));
+            bulk_g2s(st + A_BYTES, yb + (size_t)kt * B_BYTES, B_BYTES, smem_u32(&full[s]));
+        }
+    } else if (warp == 1 && lane == 0) {
+        // MMA issuer
+        const uint32_t idesc = make_idesc();
+        for (int kt = 0; kt < nk; ++kt) {
+            const int s = kt % STAGES;
+            if (!mbar_wait(smem_u32(&full[s]), (uint32_t)((kt / STAGES) & 1))) {
+                sfail = 1;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t a0 = sbase + s * STAGE_BYTES, b0 = a0 + A_BYTES;
+#pragma unroll
+            for (int kk = 0; kk < TK / 16; ++kk) {
+                const uint64_t ad = make_desc(a0 + kk * 256, 128, 1024);
+                const uint64_t bd = make_desc(b0 + kk * 256, 128, 1024);
+                mma_bf16(tmem, ad, bd, idesc, (kt | kk) != 0 ? 1u : 0u);
+            }
+            mma_commit(smem_u32(&empty[s]));
+        }
+        // completion of every MMA issued above (also after a failure)
+        mma_commit(smem_u32(&done));
+    } else if (warp >= 4) {
+        // epilogue: TMEM lanes 32*q.. are rows m0 + 32 q + lane
+        const bool ok = mbar_wait(smem_u32(&done), 0u);
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        if (!ok) {
+            sfail = 1;
+        } else {
+            const int q = warp & 3;
+            const int m = m0 + q * 32 + lane;
+            const int p_first = n0 / a.T;
+            const bool mvalid = m < a.M;
+            const bool skip = !mvalid || !(a.pdf_orient[m] > 0.f);
+            for (int c = 0; c < TN / 32; ++c) {
+                float v[32];
+                tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(c * 32), v);
+                const int nb = n0 + c * 32;
+                if (!mvalid || nb >= a.N) continue;
+                int p = nb / a.T, t = nb - p * a.T;
+                unsigned int lmin = 0xFFFFFFFFu;
+                int pmin = p;
+#pragma unroll
+                for (int jj = 0; jj < 32; ++jj) {
+                    const int n = nb + jj;
+                    if (n < a.N) {
+                        float d = __int_as_float(0x7f800000);
+                        if (!skip) {
+                            d = a.norm[(size_t)p * a.M + m] - 2.f * v[jj];
+                            const unsigned int o = f2ord(d);
+                            if (p != pmin) {
+                                if (lmin != 0xFFFFFFFFu) atomicMin(&smin[pmin - p_first], lmin);
+                                lmin = 0xFFFFFFFFu;
+                                pmin = p;
+                            }
+                            lmin = o < lmin ? o : lmin;
+                        }
+                        a.out[((size_t)p * a.M + m) * a.T + t] = d;
+                    }
+                    if (++t == a.T) {
+                        t = 0;
+                        ++p;
+                    }
+                }
+                if (lmin != 0xFFFFFFFFu) atomicMin(&smin[pmin - p_first], lmin);
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (!sfail) {
+        const int n_last = min(n0 + TN, a.N) - 1;
+        const int np = n_last / a.T - n0 / a.T + 1;
+        for (int i = tid; i < np; i += THREADS)
+            if (smin[i] != 0xFFFFFFFFu) atomicMin(&a.ps[n0 / a.T + i].min_coarse, smin[i]);
+    } else if (tid == 0) {
+        atomicCAS(&g_tc_error, 0, 1);
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+    }
+}
+
+// A operand tiles: BF16 rows of the FP32 projection table, blocked per
+// (M tile, K tile) in the no-swizzle K-major shared-memory image.
+__global__ void k_pack_a(const float *__restrict__ src, int lds, int M, int K2, int ktiles, uint8_t *__restrict__ dst,
+                         long long nchunks) {
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nchunks) return;
+    const long long blk = c >> 10;  // 1024 chunks per A block
+    const int within = (int)(c & 1023), row = within >> 3, kg = within & 7;
+    const int mt = (int)(blk / ktiles), kt = (int)(blk - (long long)mt * ktiles);
+    const int m = mt * TM + row, k0 = kt * TK + kg * 8;
+    float f[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) f[i] = (m < M && k0 + i < K2) ? src[(size_t)m * lds + k0 + i] : 0.f;
+    *reinterpret_cast<uint4 *>(dst + blk * A_BYTES + chunk_off(row, kg)) =
+        make_uint4(pack_bf16(f[0], f[1]), pack_bf16(f[2], f[3]), pack_bf16(f[4], f[5]), pack_bf16(f[6], f[7]));
+}
+
+// B operand tiles: Y[(p,t)][2j+c] = Re/Im(b[p][j] E[t][j]) in BF16, blocked
+// per (N tile, K tile) in the same image.
+__global__ void k_pack_y(const float2 *__restrict__ b, int ldb, const float2 *__restrict__ E, int lde, int npix,
+                         int T, int N, int ktiles, uint8_t *__restrict__ dst, long long nchunks) {
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nchunks) return;
+    const long long blk = c >> 11;  // 2048 chunks per B block
+    const int within = (int)(c & 2047), row = within >> 3, kg = within & 7;
+    const int nt = (int)(blk / ktiles), kt = (int)(blk - (long long)nt * ktiles);
+    const int n = nt * TN + row;
+    float y[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) y[i] = 0.f;
+    if (n < N) {
+        const int p = n / T, t = n - p * T;
+        const int j = kt * (TK / 2) + kg * 4;
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            if (j + q < npix) {
+                const float2 x = __ldg(b + (size_t)p * ldb + j + q), e = __ldg(E + (size_t)t * lde + j + q);
+                y[2 * q] = x.x * e.x - x.y * e.y;
+                y[2 * q + 1] = x.x * e.y + x.y * e.x;
+            }
+    }
+    *reinterpret_cast<uint4 *>(dst + blk * B_BYTES + chunk_off(row, kg)) =
+        make_uint4(pack_bf16(y[0], y[1]), pack_bf16(y[2], y[3]), pack_bf16(y[4], y[5]), pack_bf16(y[6], y[7]));
+}
+
+}  // namespace
+
+size_t tc_a_bytes(int M, int K2) {
+    return (size_t)((M + TM - 1) / TM) * ((K2 + TK - 1) / TK) * A_BYTES;
+}
+size_t tc_y_bytes(int N, int K2) {
+    return (size_t)((N + TN - 1) / TN) * ((K2 + TK - 1) / TK) * B_BYTES;
+}
+
+cudaError_t launch_tc_pack_a(const float *src, int lds, int M, int K2, void *dst, cudaStream_t st) {
+    const int ktiles = (K2 + TK - 1) / TK, mtiles = (M + TM - 1) / TM;
+    const long long nchunks = (long long)mtiles * ktiles * (A_BYTES / 16);
+    if (nchunks <= 0) return cudaSuccess;
+    k_pack_a<<<(unsigned)((nchunks + 255) / 256), 256, 0, st>>>(src, lds, M, K2, ktiles, static_cast<uint8_t *>(dst),
+                                                              nchunks);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tc_diff2(const void *Ablk, void *Yblk, int M, int K2, const float2 *b, int ldb, const float2 *E,
+                            int lde, int nparticles, int T, float *out, const float *norm, const float *pdf_orient,
+                            ParticleState *ps, cudaStream_t st) {
+    const int N = nparticles * T;
+    if (N <= 0 || M <= 0) return cudaSuccess;
+    const int ktiles = (K2 + TK - 1) / TK, ntiles = (N + TN - 1) / TN, mtiles = (M + TM - 1) / TM;
+    const long long ychunks = (long long)ntiles * ktiles * (B_BYTES / 16);
+    k_pack_y<<<(unsigned)((ychunks + 255) / 256), 256, 0, st>>>(b, ldb, E, lde, K2 / 2, T, N, ktiles,
+                                                             static_cast<uint8_t *>(Yblk), ychunks);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    const size_t smem = (size_t)STAGES * STAGE_BYTES;
+    static bool attr = false;
+    if (!attr) {
+        e = cudaFuncSetAttribute(k_tc_diff2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    if (mtiles > 65535) return cudaErrorInvalidConfiguration;
+    dim3 grid(ntiles, mtiles);
+    TcArgs a{static_cast<const uint8_t *>(Ablk), static_cast<const uint8_t *>(Yblk), M, ktiles, T, N, out, norm,
+             pdf_orient, ps};
+    k_tc_diff2<<<grid, THREADS, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t tc_error_flag(int *flag, int reset) {
+    cudaError_t e = cudaMemcpyFromSymbol(flag, g_tc_error, sizeof(int));
+    if (e == cudaSuccess && reset) {
+        const int z = 0;
+        e = cudaMemcpyToSymbol(g_tc_error, &z, sizeof(int));
+    }
+    return e;
+}
+
+}  // namespace gbr
