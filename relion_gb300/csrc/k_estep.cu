@@ -287,10 +287,10 @@ k_weights_cand(const float *__restrict__ vals, int R, int T, const float *__rest
             if (dense_out) dense_out[(size_t)p * RT + e] = w;
         }
         const bool is_c = w > 0.f && w >= eps_lo;
-        if (is_c) acc_c += (double)w;
-        else acc_f += w;
         const unsigned int ball = __ballot_sync(0xffffffffu, is_c);
-        if (ball) {
+        if (!is_c) acc_f += w;
+        if (ball) {  // warp-uniform: the FP64 add runs only where candidates are
+            if (is_c) acc_c += (double)w;
             unsigned int base = 0;
             if (lane == 0) base = atomicAdd(&cand_cnt[p], (unsigned)__popc(ball));
             base = __shfl_sync(0xffffffffu, base, 0);

@@ -13,7 +13,7 @@
 // core matrices 128 B apart, 8-row groups 1024 B apart): the projection
 // table once per iteration (k_pack_a), Y once per batch (k_pack_y).
 // CTA: 256 threads, tile 128 (orientations) x 256 (particle, translation),
-// K tiles of 64 BF16 in a 3-stage shared-memory ring; one thread streams each
+// K tiles of 64 BF16 in a 4-stage shared-memory ring; one thread streams each
 // stage's 48 KB with two cp.async.bulk copies, one thread issues tcgen05.mma
 // (M=128, N=256, K=16, accumulator in 256 TMEM columns), four warps run the
 // epilogue from TMEM.  Every mbarrier wait is bounded: on timeout the CTA
@@ -28,7 +28,7 @@
 namespace gbr {
 namespace {
 
-constexpr int TM = 128, TN = 256, TK = 64, STAGES = 3, THREADS = 256;
+constexpr int TM = 128, TN = 256, TK = 64, STAGES = 4, THREADS = 256;
 constexpr int A_BYTES = TM * TK * 2;          // 16 KB
 constexpr int B_BYTES = TN * TK * 2;          // 32 KB
 constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
@@ -240,37 +240,49 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_diff2(const TcArgs a) {
             const int p_first = n0 / a.T;
             const bool mvalid = m < a.M;
             const bool skip = !mvalid || !(a.pdf_orient[m] > 0.f);
+            // per-warp 32 x 33 transpose buffer in the (now idle) stage ring
+            float *tb = reinterpret_cast<float *>(smem) + (warp - 4) * 32 * 33;
             for (int c = 0; c < TN / 32; ++c) {
                 float v[32];
                 tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(c * 32), v);
                 const int nb = n0 + c * 32;
-                if (!mvalid || nb >= a.N) continue;
+                if (nb >= a.N) break;  // warp-uniform
                 int p = nb / a.T, t = nb - p * a.T;
                 unsigned int lmin = 0xFFFFFFFFu;
                 int pmin = p;
 #pragma unroll
                 for (int jj = 0; jj < 32; ++jj) {
-                    const int n = nb + jj;
-                    if (n < a.N) {
-                        float d = __int_as_float(0x7f800000);
-                        if (!skip) {
-                            d = a.norm[(size_t)p * a.M + m] - 2.f * v[jj];
-                            const unsigned int o = f2ord(d);
-                            if (p != pmin) {
-                                if (lmin != 0xFFFFFFFFu) atomicMin(&smin[pmin - p_first], lmin);
-                                lmin = 0xFFFFFFFFu;
-                                pmin = p;
-                            }
-                            lmin = o < lmin ? o : lmin;
+                    float d = __int_as_float(0x7f800000);
+                    if (!skip && nb + jj < a.N) {
+                        d = a.norm[(size_t)p * a.M + m] - 2.f * v[jj];
+                        const unsigned int o = f2ord(d);
+                        if (p != pmin) {
+                            if (lmin != 0xFFFFFFFFu) atomicMin(&smin[pmin - p_first], lmin);
+                            lmin = 0xFFFFFFFFu;
+                            pmin = p;
                         }
-                        a.out[((size_t)p * a.M + m) * a.T + t] = d;
+                        lmin = o < lmin ? o : lmin;
                     }
+                    tb[lane * 33 + jj] = d;
                     if (++t == a.T) {
                         t = 0;
                         ++p;
                     }
                 }
                 if (lmin != 0xFFFFFFFFu) atomicMin(&smin[pmin - p_first], lmin);
+                __syncwarp();
+                // lane = column: each store writes 32 consecutive translations
+                const int n = nb + lane;
+                const int pn = n / a.T, tn = n - pn * a.T;
+                if (n < a.N) {
+                    float *dst = a.out + (size_t)pn * a.M * a.T + tn;
+#pragma unroll 8
+                    for (int r = 0; r < 32; ++r) {
+                        const int mr = m0 + q * 32 + r;
+                        if (mr < a.M) dst[(size_t)mr * a.T] = tb[r * 33 + lane];
+                    }
+                }
+                __syncwarp();
             }
         }
     }
