@@ -12,27 +12,33 @@
 // canonical no-swizzle K-major layout (8 x 16-byte core matrices; K-adjacent
 // core matrices 128 B apart, 8-row groups 1024 B apart): the projection
 // table once per iteration (k_pack_a), Y once per batch (k_pack_y).
-// CTA: 256 threads, tile 128 (orientations) x 256 (particle, translation),
-// K tiles of 64 BF16 in a 4-stage shared-memory ring; one thread streams each
-// stage's 48 KB with two cp.async.bulk copies, one thread issues tcgen05.mma
-// (M=128, N=256, K=16, accumulator in 256 TMEM columns), four warps run the
-// epilogue from TMEM.  Every mbarrier wait is bounded: on timeout the CTA
-// records an error, waits (bounded) for its own MMAs, frees its tensor
-// memory and returns.
+// Persistent kernel, one 384-thread CTA per SM looping over output tiles of
+// 128 (orientations) x 256 (particle, translation); K tiles of 64 BF16 in a
+// 4-stage shared-memory ring.  One thread streams each stage's 48 KB with two
+// cp.async.bulk copies, one thread issues tcgen05.mma (M=128, N=256, K=16)
+// into one of two TMEM accumulators (2 x 256 columns) while eight warps drain
+// the other, so the epilogue of tile i overlaps the MMAs of tile i+1.  Every
+// mbarrier wait is bounded: on timeout the CTA records an error, waits
+// (bounded) for its own MMAs, frees its tensor memory and returns.
 #include "gbr_internal.h"
 
 #include <cuda_bf16.h>
 #include <cfloat>
+#include <algorithm>
 #include <cstdint>
 
 namespace gbr {
 namespace {
 
-constexpr int TM = 128, TN = 256, TK = 64, STAGES = 4, THREADS = 256;
+constexpr int TM = 128, TN = 256, TK = 64, STAGES = 4;
+constexpr int EPI_WARPS = 8, THREADS = 128 + 32 * EPI_WARPS;
 constexpr int A_BYTES = TM * TK * 2;          // 16 KB
 constexpr int B_BYTES = TN * TK * 2;          // 32 KB
 constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
-constexpr int TMEM_COLS = 256;
+constexpr int TRANSPOSE_BYTES = EPI_WARPS * 32 * 33 * 4;
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + TRANSPOSE_BYTES;
+constexpr int TMEM_COLS = 2 * TN;             // two accumulators
+constexpr int kGroupM = 32;
 constexpr unsigned int kWaitLimit = 1u << 22;
 
 __device__ int g_tc_error;  // first failure code of the last launches (0 = ok)
@@ -146,29 +152,52 @@ __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t
 struct TcArgs {
     const uint8_t *Ablk;     // [mtiles][ktiles][A_BYTES] BF16 tiles in shared-memory image
     const uint8_t *Yblk;     // [ntiles][ktiles][B_BYTES]
-    int M, ktiles, T, N;
+    int M, ktiles, T, N, nparticles;
+    int mtiles, ntiles;
     float *out;              // [p][M][T]
     const float *norm;       // [p][M]
     const float *pdf_orient; // [M]
     ParticleState *ps;
 };
 
-// Warp-specialised CTA: warp 0 lane 0 streams the pre-packed operand tiles
-// with cp.async.bulk into the stage ring (full barriers count the bytes),
-// warp 1 lane 0 issues the MMAs and commits each stage to its empty barrier,
-// warps 4-7 read the accumulator from TMEM (lanes 32*(w-4)..) and store.
+// Tile order of the persistent loop: groups of kGroupM orientation tiles,
+// orientation tile fastest inside a group, so that the CTAs running at the
+// same time share a few A tiles and sweep the Y tiles once per group.
+__device__ __forceinline__ void tile_mn(int tidx, int mtiles, int ntiles, int &mt, int &nt) {
+    const int per_group = kGroupM * ntiles;
+    const int g = tidx / per_group, r = tidx - g * per_group;
+    const int gm = min(kGroupM, mtiles - g * kGroupM);
+    mt = g * kGroupM + r % gm;
+    nt = r / gm;
+}
+
+__device__ __forceinline__ void warp_min_flush(float lmin, unsigned int *dst) {
+    const unsigned int u = lmin < __int_as_float(0x7f800000) ? f2ord(lmin) : 0xFFFFFFFFu;
+    const unsigned int wmin = __reduce_min_sync(0xffffffffu, u);
+    if ((threadIdx.x & 31) == 0 && wmin != 0xFFFFFFFFu) atomicMin(dst, wmin);
+}
+
+// Persistent warp-specialised CTA, one per SM, tiles tidx = blockIdx.x +
+// i * gridDim.x in tile_mn order.  Warp 0 lane 0 streams the pre-packed
+// operand tiles with cp.async.bulk into the stage ring (full barriers count
+// the bytes); warp 1 lane 0 issues the MMAs into one of two TMEM
+// accumulators (256 columns each) and commits each stage to its empty
+// barrier and each finished tile to its accumulator's tfull barrier; warps
+// 4..11 drain the other accumulator meanwhile (warp w reads TMEM lanes
+// 32 (w & 3).. and columns 128 ((w - 4) >> 2)..) and release it on tempty.
 __global__ void __launch_bounds__(THREADS, 1) k_tc_diff2(const TcArgs a) {
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ __align__(8) uint64_t full[STAGES];
     __shared__ __align__(8) uint64_t empty[STAGES];
+    __shared__ __align__(8) uint64_t tfull[2];
+    __shared__ __align__(8) uint64_t tempty[2];
     __shared__ __align__(8) uint64_t done;
     __shared__ uint32_t tmem_slot;
     __shared__ int sfail;
-    __shared__ unsigned int smin[TN + 2];  // one per particle of the tile (T >= 1)
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int nt = blockIdx.x, mt = blockIdx.y;
-    const int n0 = nt * TN, m0 = mt * TM;
     const int nk = a.ktiles;
+    const int ntotal = a.mtiles * a.ntiles;
+    volatile int *vfail = &sfail;
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
@@ -181,11 +210,14 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_diff2(const TcArgs a) {
             mbar_init(smem_u32(&full[s]), 1);
             mbar_init(smem_u32(&empty[s]), 1);
         }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(smem_u32(&tfull[b]), 1);
+            mbar_init(smem_u32(&tempty[b]), EPI_WARPS);
+        }
         mbar_init(smem_u32(&done), 1);
         sfail = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    for (int i = tid; i < TN + 2; i += THREADS) smin[i] = 0xFFFFFFFFu;
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -193,109 +225,160 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_diff2(const TcArgs a) {
     const uint32_t sbase = smem_u32(smem);
 
     if (warp == 0 && lane == 0) {
-        // producer
-        const uint8_t *ab = a.Ablk + (size_t)mt * nk * A_BYTES;
-        const uint8_t *yb = a.Yblk + (size_t)nt * nk * B_BYTES;
-        for (int kt = 0; kt < nk; ++kt) {
-            const int s = kt % STAGES;
-            if (kt >= STAGES && !mbar_wait(smem_u32(&empty[s]), (uint32_t)(((kt / STAGES) - 1) & 1))) {
-                sfail = 1;
-                break;
+        // producer: one running stage counter over all tiles of this CTA
+        uint32_t g = 0;
+        for (int tidx = blockIdx.x; tidx < ntotal && !*vfail; tidx += gridDim.x) {
+            int mt, nt;
+            tile_mn(tidx, a.mtiles, a.ntiles, mt, nt);
+            const uint8_t *ab = a.Ablk + (size_t)mt * nk * A_BYTES;
+            const uint8_t *yb = a.Yblk + (size_t)nt * nk * B_BYTES;
+            for (int kt = 0; kt < nk; ++kt, ++g) {
+                const uint32_t s = g % STAGES;
+                if (g >= STAGES && !mbar_wait(smem_u32(&empty[s]), ((g / STAGES) - 1) & 1u)) {
+                    *vfail = 1;
+                    break;
+                }
+                const uint32_t st = sbase + s * STAGE_BYTES;
+                arrive_expect_tx(smem_u32(&full[s]), (uint32_t)STAGE_BYTES);
+                bulk_g2s(st, ab + (size_t)kt * A_BYTES, A_BYTES, smem_u32(&full[s]));
+                bulk_g2s(st + A_BYTES, yb + (size_t)kt * B_BYTES, B_BYTES, smem_u32(&full[s]));
             }
-            const uint32_t st = sbase + s * STAGE_BYTES;
-            arrive_expect_tx(smem_u32(&full[s]), (uint32_t)STAGE_BYTES);
-            bulk_g2s(st, ab + (size_t)kt * A_BYTES, A_BYTES, smem_u32(&full[s]));
-            bulk_g2s(st + A_BYTES, yb + (size_t)kt * B_BYTES, B_BYTES, smem_u32(&full[s]));
         }
     } else if (warp == 1 && lane == 0) {
         // MMA issuer
         const uint32_t idesc = make_idesc();
-        for (int kt = 0; kt < nk; ++kt) {
-            const int s = kt % STAGES;
-            if (!mbar_wait(smem_u32(&full[s]), (uint32_t)((kt / STAGES) & 1))) {
-                sfail = 1;
+        uint32_t g = 0, i = 0;
+        for (int tidx = blockIdx.x; tidx < ntotal && !*vfail; tidx += gridDim.x, ++i) {
+            const uint32_t b = i & 1u;
+            if (i >= 2 && !mbar_wait(smem_u32(&tempty[b]), ((i >> 1) - 1) & 1u)) {
+                *vfail = 1;
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t a0 = sbase + s * STAGE_BYTES, b0 = a0 + A_BYTES;
+            const uint32_t acc = tmem + b * (uint32_t)TN;
+            bool ok = true;
+            for (int kt = 0; kt < nk; ++kt, ++g) {
+                const uint32_t s = g % STAGES;
+                if (!mbar_wait(smem_u32(&full[s]), (g / STAGES) & 1u)) {
+                    ok = false;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t a0 = sbase + s * STAGE_BYTES, b0 = a0 + A_BYTES;
 #pragma unroll
-            for (int kk = 0; kk < TK / 16; ++kk) {
-                const uint64_t ad = make_desc(a0 + kk * 256, 128, 1024);
-                const uint64_t bd = make_desc(b0 + kk * 256, 128, 1024);
-                mma_bf16(tmem, ad, bd, idesc, (kt | kk) != 0 ? 1u : 0u);
+                for (int kk = 0; kk < TK / 16; ++kk) {
+                    const uint64_t ad = make_desc(a0 + kk * 256, 128, 1024);
+                    const uint64_t bd = make_desc(b0 + kk * 256, 128, 1024);
+                    mma_bf16(acc, ad, bd, idesc, (kt | kk) != 0 ? 1u : 0u);
+                }
+                mma_commit(smem_u32(&empty[s]));
             }
-            mma_commit(smem_u32(&empty[s]));
+            if (!ok) {
+                *vfail = 1;
+                break;
+            }
+            mma_commit(smem_u32(&tfull[b]));
         }
         // completion of every MMA issued above (also after a failure)
         mma_commit(smem_u32(&done));
     } else if (warp >= 4) {
-        // epilogue: TMEM lanes 32*q.. are rows m0 + 32 q + lane
-        const bool ok = mbar_wait(smem_u32(&done), 0u);
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        if (!ok) {
-            sfail = 1;
-        } else {
-            const int q = warp & 3;
+        const int ew = warp - 4, q = warp & 3, h = ew >> 2;
+        float *tb = reinterpret_cast<float *>(smem + STAGES * STAGE_BYTES) + ew * 32 * 33;
+        uint32_t i = 0;
+        for (int tidx = blockIdx.x; tidx < ntotal && !*vfail; tidx += gridDim.x, ++i) {
+            int mt, nt;
+            tile_mn(tidx, a.mtiles, a.ntiles, mt, nt);
+            const uint32_t b = i & 1u;
+            if (!mbar_wait(smem_u32(&tfull[b]), (i >> 1) & 1u)) {
+                *vfail = 1;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const int m0 = mt * TM, n0 = nt * TN;
             const int m = m0 + q * 32 + lane;
-            const int p_first = n0 / a.T;
-            const bool mvalid = m < a.M;
-            const bool skip = !mvalid || !(a.pdf_orient[m] > 0.f);
-            // per-warp 32 x 33 transpose buffer in the (now idle) stage ring
-            float *tb = reinterpret_cast<float *>(smem) + (warp - 4) * 32 * 33;
-            for (int c = 0; c < TN / 32; ++c) {
+            const bool skip = !(m < a.M) || !(a.pdf_orient[m] > 0.f);
+            for (int c = 0; c < 4; ++c) {
+                const int col = h * 128 + c * 32;
                 float v[32];
-                tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(c * 32), v);
-                const int nb = n0 + c * 32;
+                tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + b * (uint32_t)TN + (uint32_t)col, v);
+                const int nb = n0 + col;
                 if (nb >= a.N) break;  // warp-uniform
-                int p = nb / a.T, t = nb - p * a.T;
-                unsigned int lmin = 0xFFFFFFFFu;
-                int pmin = p;
+                const int nvalid = min(32, a.N - nb);
+                const int p_lo = nb / a.T;
+                if (a.T >= 32) {
+                    // at most two particles in these 32 columns: p_lo for jj < bnd
+                    const int bnd = (p_lo + 1) * a.T - nb;
+                    const float n_lo = skip ? 0.f : a.norm[(size_t)p_lo * a.M + m];
+                    const float n_hi = (skip || bnd >= nvalid) ? 0.f : a.norm[(size_t)(p_lo + 1) * a.M + m];
+                    float min_lo = __int_as_float(0x7f800000), min_hi = min_lo;
 #pragma unroll
-                for (int jj = 0; jj < 32; ++jj) {
-                    float d = __int_as_float(0x7f800000);
-                    if (!skip && nb + jj < a.N) {
-                        d = a.norm[(size_t)p * a.M + m] - 2.f * v[jj];
-                        const unsigned int o = f2ord(d);
-                        if (p != pmin) {
-                            if (lmin != 0xFFFFFFFFu) atomicMin(&smin[pmin - p_first], lmin);
-                            lmin = 0xFFFFFFFFu;
-                            pmin = p;
+                    for (int jj = 0; jj < 32; ++jj) {
+                        float d = __int_as_float(0x7f800000);
+                        if (!skip && jj < nvalid) {
+                            d = (jj < bnd ? n_lo : n_hi) - 2.f * v[jj];
+                            if (jj < bnd)
+                                min_lo = fminf(min_lo, d);
+                            else
+                                min_hi = fminf(min_hi, d);
                         }
-                        lmin = o < lmin ? o : lmin;
+                        tb[lane * 33 + jj] = d;
                     }
-                    tb[lane * 33 + jj] = d;
-                    if (++t == a.T) {
-                        t = 0;
-                        ++p;
+                    warp_min_flush(min_lo, &a.ps[p_lo].min_coarse);
+                    if (bnd < nvalid) warp_min_flush(min_hi, &a.ps[p_lo + 1].min_coarse);
+                } else {
+                    // short translation lists: one particle index per column
+                    int p = p_lo, t = nb - p_lo * a.T;
+                    float lmin = __int_as_float(0x7f800000);
+#pragma unroll
+                    for (int jj = 0; jj < 32; ++jj) {
+                        float d = __int_as_float(0x7f800000);
+                        if (jj < nvalid) {
+                            if (!skip) {
+                                d = a.norm[(size_t)p * a.M + m] - 2.f * v[jj];
+                                lmin = fminf(lmin, d);
+                            }
+                            if (++t == a.T || jj + 1 == nvalid) {
+                                warp_min_flush(lmin, &a.ps[p].min_coarse);
+                                lmin = __int_as_float(0x7f800000);
+                                t = 0;
+                                ++p;
+                            }
+                        }
+                        tb[lane * 33 + jj] = d;
                     }
                 }
-                if (lmin != 0xFFFFFFFFu) atomicMin(&smin[pmin - p_first], lmin);
                 __syncwarp();
                 // lane = column: each store writes 32 consecutive translations
                 const int n = nb + lane;
-                const int pn = n / a.T, tn = n - pn * a.T;
-                if (n < a.N) {
+                if (lane < nvalid) {
+                    const int pn = n / a.T, tn = n - pn * a.T;
                     float *dst = a.out + (size_t)pn * a.M * a.T + tn;
+                    const int rows = min(32, a.M - (m0 + q * 32));
 #pragma unroll 8
-                    for (int r = 0; r < 32; ++r) {
-                        const int mr = m0 + q * 32 + r;
-                        if (mr < a.M) dst[(size_t)mr * a.T] = tb[r * 33 + lane];
-                    }
+                    for (int r = 0; r < 32; ++r)
+                        if (r < rows) dst[(size_t)(m0 + q * 32 + r) * a.T] = tb[r * 33 + lane];
                 }
                 __syncwarp();
             }
+            // accumulator drained: hand it back to the MMA issuer
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0)
+                asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tempty[b]))
+                             : "memory");
         }
+    }
+    __syncwarp();
+    if (warp == 0) {
+        // every MMA of this CTA has completed before its tensor memory is freed
+        bool ok = true;
+        if (lane == 0) ok = mbar_wait(smem_u32(&done), 0u);
+        ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+        if (!ok && lane == 0) *vfail = 1;
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
-    if (!sfail) {
-        const int n_last = min(n0 + TN, a.N) - 1;
-        const int np = n_last / a.T - n0 / a.T + 1;
-        for (int i = tid; i < np; i += THREADS)
-            if (smin[i] != 0xFFFFFFFFu) atomicMin(&a.ps[n0 / a.T + i].min_coarse, smin[i]);
-    } else if (tid == 0) {
-        atomicCAS(&g_tc_error, 0, 1);
-    }
+    if (tid == 0 && *vfail) atomicCAS(&g_tc_error, 0, 1);
     if (warp == 0) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
@@ -376,17 +459,24 @@ cudaError_t launch_tc_diff2(const void *Ablk, void *Yblk, int M, int K2, const f
                                                              static_cast<uint8_t *>(Yblk), ychunks);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    const size_t smem = (size_t)STAGES * STAGE_BYTES;
-    static bool attr = false;
-    if (!attr) {
-        e = cudaFuncSetAttribute(k_tc_diff2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        attr = true;
+    const size_t smem = (size_t)SMEM_BYTES;
+    static int nsm = 0;
+    if (!nsm) {
+        int dev = 0;
+        e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_tc_diff2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) {
+            nsm = 0;
+            return e;
+        }
     }
-    if (mtiles > 65535) return cudaErrorInvalidConfiguration;
-    dim3 grid(ntiles, mtiles);
-    TcArgs a{static_cast<const uint8_t *>(Ablk), static_cast<const uint8_t *>(Yblk), M, ktiles, T, N, out, norm,
-             pdf_orient, ps};
+    const long long ntotal = (long long)mtiles * ntiles;
+    if (ntotal > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+    const int grid = (int)std::min<long long>(ntotal, nsm);
+    TcArgs a{static_cast<const uint8_t *>(Ablk), static_cast<const uint8_t *>(Yblk), M, ktiles, T, N, nparticles,
+             mtiles, ntiles, out, norm, pdf_orient, ps};
     k_tc_diff2<<<grid, THREADS, smem, st>>>(a);
     return cudaGetLastError();
 }
