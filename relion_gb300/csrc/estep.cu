@@ -132,6 +132,7 @@ struct gbr_bundle {
     DevBuf<int> cls_c, cls_f, cls_of_r;
     DevBuf<float> pdf_orient;
     float pdf_orient_min = 0.f;  // smallest non-zero normalised pdf_orient
+    float pdf_orient_max = 0.f;
     DevBuf<double> tx, ty, otx, oty;
     std::vector<double> otx_h, oty_h;
     DevBuf<float2> phase_c, phase_f;
@@ -171,7 +172,7 @@ struct gbr_worker {
     DevBuf<HistBin> hist;
     DevBuf<unsigned int> mask;
     DevBuf<int> cnt;
-    DevBuf<long long> flags, entries, jpos, epos, scan_tmp;
+    DevBuf<long long> scan_tmp;
     DevBuf<FineJob> jobs;
     DevBuf<unsigned char> need_r;
     DevBuf<int> proj_ids, act_list, act_count;
@@ -184,9 +185,11 @@ struct gbr_worker {
     int cand_cap = 0;
     DevBuf<unsigned int> cand_idx, cand_cnt;
     DevBuf<float> cand_w, dense_dbg;
+    DevBuf<unsigned int> rowmin;           // [p][R] row minima of the tensor-core coarse pass
     DevBuf<long long> cand_seg;  // [2n]: begins, ends
     // dense fine pass
     int fine_mode = 0;  // 0: by significant density, 1: always dense, 2: always sparse
+    int coarse_rows = 0;  // 0: skip far coarse rows by their minimum (tensor-core pass), 1: read all rows
     int last_dense = 0;
     DevBuf<float> Wt, Wp, Zt, CM, S2P, fnrm;
     DevBuf<float2> G;
@@ -301,8 +304,11 @@ int build_tables(gbr_bundle *b) {
     GBR_CUDA(b->cls_of_r.upload(cr.data(), cr.size()));
     GBR_CUDA(b->pdf_orient.upload(po.data(), po.size()));
     b->pdf_orient_min = 0.f;
-    for (float v : po)
+    b->pdf_orient_max = 0.f;
+    for (float v : po) {
         if (v > 0.f && (b->pdf_orient_min == 0.f || v < b->pdf_orient_min)) b->pdf_orient_min = v;
+        b->pdf_orient_max = std::max(b->pdf_orient_max, v);
+    }
 
     // ---- translations and phase tables ----
     std::vector<double> tx(b->grid.trans_x), ty(b->grid.trans_y);
@@ -397,11 +403,7 @@ int ensure_capacity(gbr_worker *w, int n) {
     const int W = (int)((b->T + 31) / 32);
     GBR_CUDA(w->mask.reserve((size_t)n * b->R * W));
     GBR_CUDA(w->cnt.reserve((size_t)n * b->R));
-    GBR_CUDA(w->flags.reserve((size_t)n * b->R + 1));
-    GBR_CUDA(w->entries.reserve((size_t)n * b->R + 1));
-    GBR_CUDA(w->jpos.reserve((size_t)n * b->R + 1));
-    GBR_CUDA(w->epos.reserve((size_t)n * b->R + 1));
-    GBR_CUDA(w->scan_tmp.reserve(((size_t)n * b->R + 1023) / 1024 + 2));
+    GBR_CUDA(w->scan_tmp.reserve(2 * (((size_t)n * b->R + 1023) / 1024) + 2));
     GBR_CUDA(w->jobs.reserve((size_t)n * b->R));
     GBR_CUDA(w->need_r.reserve(b->R));
     GBR_CUDA(w->shell.reserve((size_t)n * b->nshell));
@@ -569,17 +571,29 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
     GBR_CUDA(launch_prep(w->X.p, w->C.p, w->pdat.p, n, b->full_npix, b->pc.p, b->nc, b->minv_c.p, b->ldk_c,
                          b->pf.p, b->nf, b->ldk_f, b->minv_f.p, w->a_c.p, w->b_c.p, w->a_f.p, w->b_f.p, w->Xf.p,
                          w->Xnf.p, w->Cf.p, w->Xn.p, (int)d.do_scale_correction, w->ps.p, st));
-    GBR_CUDA(launch_pdf_offset(w->pdat.p, n, b->tx.p, b->ty.p, T, d.sigma2_offset, d.pixel_size, w->pdf_off.p, st));
+    // orientation part of the coarse skip distance: ln(R T) + ln(max/min pdf_orient) + ln(1e10)
+    const double log_rt_orient = b->pdf_orient_min > 0.f
+                                     ? std::log((double)RT) + std::log((double)b->pdf_orient_max / b->pdf_orient_min) +
+                                           std::log(1e10)
+                                     : INFINITY;
+    GBR_CUDA(launch_pdf_offset(w->pdat.p, n, b->tx.p, b->ty.p, T, d.sigma2_offset, d.pixel_size, w->pdf_off.p,
+                               log_rt_orient, w->ps.p, st));
     GBR_CUDA(cudaMemsetAsync(w->shell.p, 0, sizeof(double) * n * b->nshell, st));
     GBR_CUDA(cudaMemsetAsync(w->pacc.p, 0, sizeof(double) * n * 8, st));
     GBR_CUDA(cudaEventRecord(w->ev[1], st));
     // ---- coarse norm and cross GEMMs ----
     GBR_CUDA(launch_gemm_rows(b->proj2_c.p, b->ldk_c, R, w->a_c.p, b->ldk_c, n, b->ldk_c, w->nrm.p, R, 1, st));
     GBR_CUDA(cudaEventRecord(w->ev[2], st));
+    const bool use_rowmin = d.precision == GBR_PREC_BF16 && T >= 32 && w->coarse_rows == 0;
+    if (use_rowmin) {
+        GBR_CUDA(w->rowmin.reserve((size_t)n * R));
+        GBR_CUDA(cudaMemsetAsync(w->rowmin.p, 0xFF, sizeof(unsigned int) * (size_t)n * R, st));
+    }
     if (d.precision == GBR_PREC_BF16) {
         GBR_CUDA(w->ytc.reserve(tc_y_bytes(n * T, 2 * b->nc)));
         GBR_CUDA(launch_tc_diff2(b->proj_c_tc.p, w->ytc.p, R, 2 * b->nc, w->b_c.p, b->ldk_c, b->phase_c.p, b->ldk_c, n,
-                                 T, w->vals.p, w->nrm.p, b->pdf_orient.p, w->ps.p, st));
+                                 T, w->vals.p, w->nrm.p, b->pdf_orient.p, w->ps.p,
+                                 use_rowmin ? w->rowmin.p : nullptr, st));
         w->launches += 1;
     } else {
         GBR_CUDA(launch_gemm_diff2(b->proj_c.p, b->lda_c, R, 2 * b->nc, w->b_c.p, b->ldk_c, b->phase_c.p, b->ldk_c,
@@ -609,7 +623,7 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
     }
     GBR_CUDA(launch_weights_cand(w->vals.p, n, R, T, b->pdf_orient.p, b->pdf_orient_min, w->pdf_off.p,
                                  d.adaptive_fraction, w->ps.p, w->cand_idx.p, w->cand_w.p, w->cand_cnt.p, cap,
-                                 dense_w, st));
+                                 dense_w, use_rowmin ? w->rowmin.p : nullptr, st));
     std::vector<unsigned int> ccnt(n);
     GBR_CUDA(cudaMemcpyAsync(ccnt.data(), w->cand_cnt.p, sizeof(unsigned int) * n, cudaMemcpyDeviceToHost, st));
     GBR_CUDA(cudaStreamSynchronize(st));
@@ -652,18 +666,16 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
         GBR_CUDA(cudaMemcpyAsync(w->dbg_wcoarse.data(), dense_w, sizeof(float) * n * RT, cudaMemcpyDeviceToHost, st));
     }
     const long long nR = (long long)n * R;
-    GBR_CUDA(launch_flag_counts(w->cnt.p, nR, w->flags.p, w->entries.p, nOR * nOT, st));
-    GBR_CUDA(launch_scan_i64(w->flags.p, w->jpos.p, nR, w->scan_tmp.p, st));
-    GBR_CUDA(launch_scan_i64(w->entries.p, w->epos.p, nR, w->scan_tmp.p, st));
     GBR_CUDA(cudaMemsetAsync(w->need_r.p, 0, R, st));
-    GBR_CUDA(launch_build_jobs(w->cnt.p, n, R, w->jpos.p, w->epos.p, w->jobs.p, w->seg_f.p, w->need_r.p, st));
-    long long njobs = 0, nfine = 0;
-    GBR_CUDA(cudaMemcpyAsync(&njobs, w->jpos.p + nR, sizeof(long long), cudaMemcpyDeviceToHost, st));
-    GBR_CUDA(cudaMemcpyAsync(&nfine, w->epos.p + nR, sizeof(long long), cudaMemcpyDeviceToHost, st));
+    GBR_CUDA(launch_fine_jobs(w->cnt.p, n, R, nOR * nOT, w->scan_tmp.p, w->jobs.p, w->seg_f.p, w->need_r.p, st));
+    const long long nbj = (nR + 1023) / 1024;
+    long long totals[2] = {0, 0};
+    GBR_CUDA(cudaMemcpyAsync(totals, w->scan_tmp.p + 2 * nbj, sizeof(totals), cudaMemcpyDeviceToHost, st));
     std::vector<long long> segf(n + 1);
     GBR_CUDA(cudaMemcpyAsync(segf.data(), w->seg_f.p, sizeof(long long) * (n + 1), cudaMemcpyDeviceToHost, st));
     GBR_CUDA(cudaStreamSynchronize(st));
-    w->launches += 10;
+    const long long njobs = totals[0], nfine = totals[1];
+    w->launches += 3;
     if (njobs <= 0 || nfine <= 0) return fail(GBR_ERR_NUMERICAL, "no significant coarse samples");
     // ---- fine pass: dense contractions when most poses are significant ----
     const double density = (double)nfine / ((double)n * b->RF * b->TF);
@@ -918,6 +930,8 @@ int gbr_worker_create(gbr_bundle *b, gbr_worker **out) {
     const char *fm = std::getenv("GBR_FINE_MODE");
     if (fm && std::strcmp(fm, "dense") == 0) w->fine_mode = 1;
     if (fm && std::strcmp(fm, "sparse") == 0) w->fine_mode = 2;
+    const char *nm = std::getenv("GBR_COARSE_WEIGHTS");
+    if (nm && std::strcmp(nm, "full") == 0) w->coarse_rows = 1;
     *out = w.release();
     return GBR_OK;
 }

@@ -48,6 +48,8 @@ struct ParticleState {
     float thr_fine;                 // significant weight of the fine pass
     unsigned int nr_sign;           // significant count (coarse pass)
     float eps;                      // weights below eps cannot reach the threshold
+    float xs;                       // coarse diff2 - min beyond which the weights of all
+                                    // poses together stay below 1e-10 of the weight sum
 };
 
 // Fine-pass job: one (particle, significant coarse orientation).
@@ -88,9 +90,12 @@ cudaError_t launch_fp32_probe(float *ms, double *flops);
 size_t tc_a_bytes(int M, int K2);
 size_t tc_y_bytes(int N, int K2);
 cudaError_t launch_tc_pack_a(const float *src, int lds, int M, int K2, void *dst, cudaStream_t st);
+// Coarse cross term on tcgen05 (BF16, FP32 accumulation) with the diff2
+// epilogue; with T >= 32 and rowmin non-null it also records the ordered
+// minimum of every (particle, orientation) row (rowmin set to ~0 by the caller).
 cudaError_t launch_tc_diff2(const void *Ablk, void *Yblk, int M, int K2, const float2 *b, int ldb, const float2 *E,
                             int lde, int nparticles, int T, float *out, const float *norm, const float *pdf_orient,
-                            ParticleState *ps, cudaStream_t st);
+                            ParticleState *ps, unsigned int *rowmin, cudaStream_t st);
 // Read (and optionally clear) the tensor-core pipeline error flag.
 cudaError_t tc_error_flag(int *flag, int reset);
 
@@ -129,7 +134,8 @@ cudaError_t launch_prep(const float2 *X, const float *C, const double *pdat, int
                         float *a_f, float2 *b_f, float2 *Xf, float2 *Xnf, float *Cf,
                         const float2 *Xn, int do_scale, ParticleState *ps, cudaStream_t st);
 cudaError_t launch_pdf_offset(const double *pdat, int n, const double *tx, const double *ty, int T,
-                              double sigma2_offset, double pixel, float *pdf_off, cudaStream_t st);
+                              double sigma2_offset, double pixel, float *pdf_off, double log_rt_orient,
+                              ParticleState *ps, cudaStream_t st);
 // Weights of per-particle segments [seg[p], seg[p+1]) of `vals` (in place).
 // Coarse: element e of particle p has r = e / T, t = e % T.
 // Fine: element e has job = ejob[e] and code = ecode[e].
@@ -145,9 +151,13 @@ cudaError_t launch_hist_refine(const float *vals, const long long *seg, int n, l
                                int pass = 0, double fraction = 1.0, const long long *seg_end = nullptr,
                                long long n_total = 0);
 // Coarse weights + FP64 sums + candidate lists (see k_weights_cand).
+// Coarse weights, FP64 sums and candidate lists in one read of the diff2
+// array; rows whose minimum (rowmin, may be null) lies more than ps[p].xs
+// above the particle minimum are skipped without reading them.
 cudaError_t launch_weights_cand(const float *vals, int n, int R, int T, const float *pdf_orient, float pdf_orient_min,
                                 const float *pdf_off, double fraction, ParticleState *ps, unsigned int *cand_idx,
-                                float *cand_w, unsigned int *cand_cnt, int cap, float *dense_out, cudaStream_t st);
+                                float *cand_w, unsigned int *cand_cnt, int cap, float *dense_out,
+                                const unsigned int *rowmin, cudaStream_t st);
 cudaError_t launch_cand_masks(const unsigned int *cand_idx, const float *cand_w, const unsigned int *cand_cnt,
                               int cap, int n, int R, int T, int W, const ParticleState *ps, unsigned int *mask,
                               int *cnt, cudaStream_t st);
@@ -155,13 +165,11 @@ cudaError_t launch_select(int n, int level, double adaptive_fraction, int coarse
                           HistBin *hist, cudaStream_t st);
 cudaError_t launch_sig_masks(const float *w, int n, int R, int T, int W, const ParticleState *ps,
                              unsigned int *mask, int *cnt, cudaStream_t st);
-cudaError_t launch_scan_i64(const long long *in, long long *out, long long n, long long *tmp,
-                            cudaStream_t st);
-cudaError_t launch_flag_counts(const int *cnt, long long n, long long *flags, long long *entries,
-                               int per, cudaStream_t st);
-cudaError_t launch_build_jobs(const int *cnt, int n, int R, const long long *jpos,
-                              const long long *epos, FineJob *jobs, long long *seg,
-                              unsigned char *need_r, cudaStream_t st);
+// Fine-pass job list: jobs[] in (p, r) order for cnt > 0, seg[p] = first fine
+// entry of particle p, seg[n] = total; sums holds 2 * ceil(n R / 1024) + 2
+// values and ends with (number of jobs, number of fine entries).
+cudaError_t launch_fine_jobs(const int *cnt, int n, int R, int per, long long *sums, FineJob *jobs, long long *seg,
+                             unsigned char *need_r, cudaStream_t st);
 cudaError_t launch_fine_diff2(const FineJob *jobs, long long njobs, const unsigned int *mask,
                               int R, int T, int W, int nOR, int nOT, const float2 *projf, int ldpf,
                               const float2 *b_f, const float *a_f, int nf, const float2 *phase_f,

@@ -11,6 +11,8 @@
 //   insertion    BackProjector::backproject2Dto3D        src/backprojector.cpp:55-296
 #include "gbr_internal.h"
 
+#include <algorithm>
+
 #include <cfloat>
 
 namespace gbr {
@@ -119,7 +121,7 @@ __global__ void k_prep(const float2 *__restrict__ X, const float *__restrict__ C
 // pixels, combined exactly as the reference does.
 __global__ void k_pdf_offset(const double *__restrict__ pdat, const double *__restrict__ tx,
                              const double *__restrict__ ty, int T, double s2, double pixel,
-                             float *__restrict__ out) {
+                             float *__restrict__ out, double log_rt_orient, ParticleState *__restrict__ ps) {
     __shared__ double sh[32];
     extern __shared__ double vals[];
     const int p = blockIdx.x;
@@ -140,8 +142,37 @@ __global__ void k_pdf_offset(const double *__restrict__ pdat, const double *__re
     __shared__ double mean;
     if (threadIdx.x == 0) mean = tot / (double)T;
     __syncthreads();
-    for (int t = threadIdx.x; t < T; t += blockDim.x)
-        out[(size_t)p * T + t] = (float)(mean > 0. ? vals[t] / mean : vals[t]);
+    float vmax = 0.f, vmin = FLT_MAX;
+    for (int t = threadIdx.x; t < T; t += blockDim.x) {
+        const float v = (float)(mean > 0. ? vals[t] / mean : vals[t]);
+        out[(size_t)p * T + t] = v;
+        vmax = fmaxf(vmax, v);
+        vmin = fminf(vmin, v);
+    }
+    // Coarse skip distance: R T poses of weight at most pmax exp(-xs) stay
+    // below 1e-10 pmin <= 1e-10 (largest weight) when
+    // xs = ln(R T) + ln(pmax / pmin) + ln(1e10); log_rt_orient carries the
+    // orientation part, +1 is margin for the FP32 exponential.
+    __shared__ float smx[32], smn[32];
+    for (int o = 16; o > 0; o >>= 1) {
+        vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+        vmin = fminf(vmin, __shfl_xor_sync(0xffffffffu, vmin, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        smx[threadIdx.x >> 5] = vmax;
+        smn[threadIdx.x >> 5] = vmin;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int i = 1; i < (int)(blockDim.x >> 5); ++i) {
+            vmax = fmaxf(vmax, smx[i]);
+            vmin = fminf(vmin, smn[i]);
+        }
+        float xs = __int_as_float(0x7f800000);
+        if (vmin > 0.f && vmax < FLT_MAX && isfinite(log_rt_orient))
+            xs = (float)(log_rt_orient + log((double)vmax / (double)vmin) + 1.0);
+        ps[p].xs = xs;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -151,6 +182,9 @@ __global__ void k_pdf_offset(const double *__restrict__ pdat, const double *__re
 // ---------------------------------------------------------------------------
 constexpr int kChunk = 8192;
 constexpr int kWThreads = 512;
+// k_weights_cand: orientation rows per block and loads in flight per lane
+constexpr int kWRowsPerBlock = 2048;
+constexpr int kWUnroll = 4;
 
 __global__ void __launch_bounds__(kWThreads)
 k_weights(float *__restrict__ vals, const long long *__restrict__ seg, int coarse, int T,
@@ -166,6 +200,7 @@ k_weights(float *__restrict__ vals, const long long *__restrict__ seg, int coars
     const long long end = min(beg + (long long)kChunk, b1);
     if (threadIdx.x == 0) smax = 0ull;
     const float mn = ord2f(coarse == 1 ? ps[p].min_coarse : ps[p].min_fine);
+    const float xcut = coarse == 1 ? fminf(ps[p].xs, 700.f) : 700.f;
     double acc = 0.;
     unsigned long long kmax = 0ull;
     for (long long e = beg + threadIdx.x; e < end; e += blockDim.x) {
@@ -173,7 +208,7 @@ k_weights(float *__restrict__ vals, const long long *__restrict__ seg, int coars
         float w = 0.f;
         if (d < FLT_MAX) {  // finite: computed
             const float x = d - mn;
-            if (!(x > 700.f)) {
+            if (!(x > xcut)) {
                 int r, t;
                 unsigned int code = 0;
                 const long long loc = e - b0;
@@ -238,17 +273,20 @@ k_weights_cand(const float *__restrict__ vals, int R, int T, const float *__rest
                float pdf_orient_min, const float *__restrict__ pdf_off, double fraction,
                ParticleState *__restrict__ ps, unsigned int *__restrict__ cand_idx,
                float *__restrict__ cand_w, unsigned int *__restrict__ cand_cnt, int cap,
-               float *__restrict__ dense_out) {
+               float *__restrict__ dense_out, const unsigned int *__restrict__ rowmin) {
+    extern __shared__ float s_po[];  // pdf_offset row of the particle [T]
     __shared__ double sh[32];
     __shared__ float s_eps;
     const int p = blockIdx.y;
+    const int r0 = blockIdx.x * kWRowsPerBlock;
+    if (r0 >= R) return;
+    const int r1 = min(r0 + kWRowsPerBlock, R);
     const long long RT = (long long)R * T;
-    const long long beg = (long long)blockIdx.x * kChunk;
-    if (beg >= RT) return;
-    const long long end = min(beg + (long long)kChunk, RT);
+    for (int t = threadIdx.x; t < T; t += blockDim.x) s_po[t] = pdf_off[(size_t)p * T + t];
+    __syncthreads();
     if (threadIdx.x < 32) {
         float m = FLT_MAX;
-        for (int t = threadIdx.x; t < T; t += 32) m = fminf(m, pdf_off[(size_t)p * T + t]);
+        for (int t = threadIdx.x; t < T; t += 32) m = fminf(m, s_po[t]);
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) m = fminf(m, __shfl_xor_sync(0xffffffffu, m, o));
         if (threadIdx.x == 0) s_eps = (float)((1.0 - fraction) * (double)pdf_orient_min * (double)m / (double)RT);
@@ -256,49 +294,86 @@ k_weights_cand(const float *__restrict__ vals, int R, int T, const float *__rest
     __syncthreads();
     const float eps_lo = s_eps;
     const float mn = ord2f(ps[p].min_coarse);
-    const float *row = vals + (size_t)p * RT;
+    const float xs = fminf(ps[p].xs, 700.f);
+    const float *rows = vals + (size_t)p * RT;
     unsigned int *ci = cand_idx + (size_t)p * cap;
     float *cw = cand_w + (size_t)p * cap;
-    const int lane = threadIdx.x & 31;
-    const float invT = 1.f / (float)T;
-    const float *po = pdf_off + (size_t)p * T;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     // candidates are summed in FP64; the rest (below eps_lo, together less
     // than (1 - fraction) of the total) in FP32, so the sum is FP64-accurate
     // to ~1e-10 relative without an FP64 add per pose
     double acc_c = 0.;
     float acc_f = 0.f;
-    for (long long e0 = beg; e0 < end; e0 += blockDim.x) {
-        const long long e = e0 + threadIdx.x;
-        float w = 0.f;
-        if (e < end) {
-            const float d = row[e];
-            if (d < FLT_MAX) {
-                const float x = d - mn;
-                if (!(x > 700.f)) {
-                    // e / T by a float reciprocal, corrected to the exact quotient
-                    const int ei = (int)e;
-                    int r = __float2int_rz((float)ei * invT);
-                    int t = ei - r * T;
-                    if (t < 0) { --r; t += T; }
-                    if (t >= T) { ++r; t -= T; }
-                    w = pdf_orient[r] * po[t] * expf(-x);
-                }
-            }
-            if (dense_out) dense_out[(size_t)p * RT + e] = w;
+    // Rows in batches of 32 per warp: each lane tests one row minimum, rows
+    // beyond the skip distance are not read at all (the same float test as
+    // for each pose: d >= rowmin gives d - mn >= rowmin - mn), and the warp
+    // then walks the remaining rows in order, one warp per row so that
+    // pdf_orient[r] is warp-uniform and the translation index is the lane.
+    for (int rb = r0 + 32 * warp; rb < r1; rb += 32 * nwarps) {
+        const int rr = rb + lane;
+        bool keep = rr < r1;
+        if (keep && rowmin) {
+            const unsigned int ru = rowmin[(size_t)p * R + rr];
+            keep = !(ru == 0xFFFFFFFFu || ord2f(ru) - mn > xs);
+            if (!keep && dense_out)
+                for (int t = 0; t < T; ++t) dense_out[(size_t)p * RT + (size_t)rr * T + t] = 0.f;
         }
-        const bool is_c = w > 0.f && w >= eps_lo;
-        const unsigned int ball = __ballot_sync(0xffffffffu, is_c);
-        if (!is_c) acc_f += w;
-        if (ball) {  // warp-uniform: the FP64 add runs only where candidates are
-            if (is_c) acc_c += (double)w;
-            unsigned int base = 0;
-            if (lane == 0) base = atomicAdd(&cand_cnt[p], (unsigned)__popc(ball));
-            base = __shfl_sync(0xffffffffu, base, 0);
-            if (is_c) {
-                const unsigned int pos = base + __popc(ball & ((1u << lane) - 1u));
-                if (pos < (unsigned)cap) {
-                    ci[pos] = (unsigned int)e;
-                    cw[pos] = w;
+        unsigned int rows_left = __ballot_sync(0xffffffffu, keep);
+        while (rows_left) {
+            const int r = rb + __ffs(rows_left) - 1;
+            rows_left &= rows_left - 1u;
+            const float pr = pdf_orient[r];
+            const float *row = rows + (size_t)r * T;
+            for (int t0 = 0; t0 < T; t0 += 32 * kWUnroll) {
+                // kWUnroll independent streaming loads per lane, then one warp
+                // vote: poses with diff2 - min > xs are skipped (all of them
+                // together weigh less than 1e-10 of the sum)
+                float dv[kWUnroll];
+                bool near = false;
+    #pragma unroll
+                for (int k = 0; k < kWUnroll; ++k) {
+                    const int t = t0 + 32 * k + lane;
+                    dv[k] = t < T ? __ldcs(row + t) : __int_as_float(0x7f800000);
+                    near |= !(dv[k] - mn > xs);
+                }
+                if (!__any_sync(0xffffffffu, near)) {
+                    if (dense_out) {
+    #pragma unroll
+                        for (int k = 0; k < kWUnroll; ++k) {
+                            const int t = t0 + 32 * k + lane;
+                            if (t < T) dense_out[(size_t)p * RT + (size_t)r * T + t] = 0.f;
+                        }
+                    }
+                    continue;
+                }
+    #pragma unroll
+                for (int k = 0; k < kWUnroll; ++k) {
+                    const int t = t0 + 32 * k + lane;
+                    float w = 0.f;
+                    if (t < T) {
+                        const float d = dv[k];
+                        if (d < FLT_MAX) {
+                            const float x = d - mn;
+                            if (!(x > xs)) w = pr * s_po[t] * expf(-x);
+                        }
+                        if (dense_out) dense_out[(size_t)p * RT + (size_t)r * T + t] = w;
+                    }
+                    const bool is_c = w > 0.f && w >= eps_lo;
+                    const unsigned int ball = __ballot_sync(0xffffffffu, is_c);
+                    if (!is_c) acc_f += w;
+                    if (ball) {  // warp-uniform: the FP64 add runs only where candidates are
+                        if (is_c) acc_c += (double)w;
+                        unsigned int base = 0;
+                        if (lane == 0) base = atomicAdd(&cand_cnt[p], (unsigned)__popc(ball));
+                        base = __shfl_sync(0xffffffffu, base, 0);
+                        if (is_c) {
+                            const unsigned int pos = base + __popc(ball & ((1u << lane) - 1u));
+                            if (pos < (unsigned)cap) {
+                                ci[pos] = (unsigned int)((long long)r * T + t);
+                                cw[pos] = w;
+                            }
+                        }
+                    }
                 }
             }
         }
@@ -524,56 +599,107 @@ __global__ void k_sig_masks(const float *__restrict__ w, int n, int R, int T, in
 
 // Exclusive scan of int64 (out has n+1 entries, out[n] = total).
 constexpr int kScanBlock = 1024;
-__global__ void k_scan_blocks(const long long *__restrict__ in, long long *__restrict__ out,
-                              long long n, long long *__restrict__ sums) {
-    __shared__ long long sh[kScanBlock];
-    const long long i = (long long)blockIdx.x * kScanBlock + threadIdx.x;
-    const long long v = i < n ? in[i] : 0;
-    sh[threadIdx.x] = v;
-    __syncthreads();
-    for (int o = 1; o < kScanBlock; o <<= 1) {
-        long long a = threadIdx.x >= (unsigned)o ? sh[threadIdx.x - o] : 0;
-        __syncthreads();
-        sh[threadIdx.x] += a;
-        __syncthreads();
-    }
-    if (i < n) out[i] = sh[threadIdx.x] - v;
-    if (threadIdx.x == kScanBlock - 1) sums[blockIdx.x] = sh[threadIdx.x];
-}
-__global__ void k_scan_sums(long long *__restrict__ sums, int nb) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) {
-        long long run = 0;
-        for (int b = 0; b < nb; ++b) {
-            const long long v = sums[b];
-            sums[b] = run;
-            run += v;
+// Fine-pass job list in three launches (reduce, scan of the block sums,
+// re-scan and emit), for the pairs (flag = cnt > 0, entries = cnt * per) of
+// every (particle, coarse orientation) in (p, r) order.
+__device__ __forceinline__ void block_excl_scan2(long long &a, long long &b, long long *wa, long long *wb,
+                                                 long long &ta, long long &tb) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    long long ia = a, ib = b;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const long long xa = __shfl_up_sync(0xffffffffu, ia, o), xb = __shfl_up_sync(0xffffffffu, ib, o);
+        if (lane >= o) {
+            ia += xa;
+            ib += xb;
         }
-        sums[nb] = run;
+    }
+    __syncthreads();
+    if (lane == 31) {
+        wa[warp] = ia;
+        wb[warp] = ib;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        const long long va = lane < nw ? wa[lane] : 0, vb = lane < nw ? wb[lane] : 0;
+        long long sa = va, sb = vb;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const long long xa = __shfl_up_sync(0xffffffffu, sa, o), xb = __shfl_up_sync(0xffffffffu, sb, o);
+            if (lane >= o) {
+                sa += xa;
+                sb += xb;
+            }
+        }
+        const long long tot_a = __shfl_sync(0xffffffffu, sa, 31), tot_b = __shfl_sync(0xffffffffu, sb, 31);
+        if (lane < nw) {
+            wa[lane] = sa - va;
+            wb[lane] = sb - vb;
+        }
+        if (lane == 0) {
+            wa[32] = tot_a;
+            wb[32] = tot_b;
+        }
+    }
+    __syncthreads();
+    a = ia - a + wa[warp];
+    b = ib - b + wb[warp];
+    ta = wa[32];
+    tb = wb[32];
+}
+
+__global__ void __launch_bounds__(kScanBlock) k_jobs_reduce(const int *__restrict__ cnt, long long n, int per,
+                                                           long long *__restrict__ sums) {
+    __shared__ long long wa[33], wb[33];
+    const long long i = (long long)blockIdx.x * kScanBlock + threadIdx.x;
+    const int c = i < n ? cnt[i] : 0;
+    long long f = c > 0 ? 1 : 0, e = (long long)c * per, tf, te;
+    block_excl_scan2(f, e, wa, wb, tf, te);
+    if (threadIdx.x == 0) {
+        sums[2 * blockIdx.x] = tf;
+        sums[2 * blockIdx.x + 1] = te;
     }
 }
-__global__ void k_scan_add(long long *__restrict__ out, long long n, const long long *__restrict__ sums,
-                           int nb) {
-    const long long i = (long long)blockIdx.x * kScanBlock + threadIdx.x;
-    if (i < n) out[i] += sums[blockIdx.x];
-    if (i == 0) out[n] = sums[nb];
+
+// Exclusive scan of nb (flag, entries) block sums in place by one block;
+// the totals land in sums[2 nb], sums[2 nb + 1].
+__global__ void __launch_bounds__(kScanBlock) k_jobs_scan_sums(long long *__restrict__ sums, int nb) {
+    __shared__ long long wa[33], wb[33];
+    const int per_t = (nb + kScanBlock - 1) / kScanBlock;
+    const int b0 = threadIdx.x * per_t, b1 = min(b0 + per_t, nb);
+    long long f = 0, e = 0;
+    for (int b = b0; b < b1; ++b) {
+        f += sums[2 * b];
+        e += sums[2 * b + 1];
+    }
+    long long tf, te;
+    block_excl_scan2(f, e, wa, wb, tf, te);
+    for (int b = b0; b < b1; ++b) {
+        const long long vf = sums[2 * b], ve = sums[2 * b + 1];
+        sums[2 * b] = f;
+        sums[2 * b + 1] = e;
+        f += vf;
+        e += ve;
+    }
+    if (threadIdx.x == 0) {
+        sums[2 * nb] = tf;
+        sums[2 * nb + 1] = te;
+    }
 }
 
-__global__ void k_flag_counts(const int *__restrict__ cnt, long long n, long long *__restrict__ flags,
-                              long long *__restrict__ entries, int per) {
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int c = cnt[i];
-    flags[i] = c > 0 ? 1 : 0;
-    entries[i] = (long long)c * per;
-}
-
-__global__ void k_build_jobs(const int *__restrict__ cnt, int n, int R, const long long *__restrict__ jpos,
-                             const long long *__restrict__ epos, FineJob *__restrict__ jobs,
-                             long long *__restrict__ seg, unsigned char *__restrict__ need_r) {
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(kScanBlock) k_jobs_emit(const int *__restrict__ cnt, int n, int R, int per,
+                                                         const long long *__restrict__ sums, int nb,
+                                                         FineJob *__restrict__ jobs, long long *__restrict__ seg,
+                                                         unsigned char *__restrict__ need_r) {
+    __shared__ long long wa[33], wb[33];
     const long long tot = (long long)n * R;
+    const long long i = (long long)blockIdx.x * kScanBlock + threadIdx.x;
+    const int c = i < tot ? cnt[i] : 0;
+    long long f = c > 0 ? 1 : 0, e = (long long)c * per, tf, te;
+    block_excl_scan2(f, e, wa, wb, tf, te);
+    f += sums[2 * blockIdx.x];
+    e += sums[2 * blockIdx.x + 1];
     if (i < tot) {
-        const int c = cnt[i];
         const int p = (int)(i / R), r = (int)(i - (long long)p * R);
         if (c > 0) {
             FineJob j;
@@ -581,13 +707,13 @@ __global__ void k_build_jobs(const int *__restrict__ cnt, int n, int R, const lo
             j.r = r;
             j.n_t = c;
             j.pad_ = 0;
-            j.off = epos[i];
-            jobs[jpos[i]] = j;
+            j.off = e;
+            jobs[f] = j;
             need_r[r] = 1;
         }
-        if (r == 0) seg[p] = epos[i];
+        if (r == 0) seg[p] = e;
     }
-    if (i == 0) seg[n] = epos[tot];
+    if (i == 0) seg[n] = sums[2 * nb + 1];
 }
 
 // ---------------------------------------------------------------------------
@@ -1092,9 +1218,11 @@ cudaError_t launch_prep(const float2 *X, const float *C, const double *pdat, int
 }
 
 cudaError_t launch_pdf_offset(const double *pdat, int n, const double *tx, const double *ty, int T,
-                              double sigma2_offset, double pixel, float *pdf_off, cudaStream_t st) {
+                              double sigma2_offset, double pixel, float *pdf_off, double log_rt_orient,
+                              ParticleState *ps, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    k_pdf_offset<<<n, 256, sizeof(double) * T, st>>>(pdat, tx, ty, T, sigma2_offset, pixel, pdf_off);
+    k_pdf_offset<<<n, 256, sizeof(double) * T, st>>>(pdat, tx, ty, T, sigma2_offset, pixel, pdf_off,
+                                                     log_rt_orient, ps);
     return cudaGetLastError();
 }
 
@@ -1141,31 +1269,15 @@ cudaError_t launch_sig_masks(const float *w, int n, int R, int T, int W, const P
     return cudaGetLastError();
 }
 
-cudaError_t launch_scan_i64(const long long *in, long long *out, long long n, long long *tmp,
-                            cudaStream_t st) {
-    const long long nb = (n + kScanBlock - 1) / kScanBlock;
-    if (nb <= 0) {
-        k_scan_sums<<<1, 1, 0, st>>>(tmp, 0);
-        return cudaMemcpyAsync(out, tmp, sizeof(long long), cudaMemcpyDeviceToDevice, st);
-    }
-    k_scan_blocks<<<(unsigned)nb, kScanBlock, 0, st>>>(in, out, n, tmp);
-    k_scan_sums<<<1, 1, 0, st>>>(tmp, (int)nb);
-    k_scan_add<<<(unsigned)nb, kScanBlock, 0, st>>>(out, n, tmp, (int)nb);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_flag_counts(const int *cnt, long long n, long long *flags, long long *entries,
-                               int per, cudaStream_t st) {
-    if (n <= 0) return cudaSuccess;
-    k_flag_counts<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(cnt, n, flags, entries, per);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_build_jobs(const int *cnt, int n, int R, const long long *jpos,
-                              const long long *epos, FineJob *jobs, long long *seg,
-                              unsigned char *need_r, cudaStream_t st) {
+cudaError_t launch_fine_jobs(const int *cnt, int n, int R, int per, long long *sums, FineJob *jobs, long long *seg,
+                             unsigned char *need_r, cudaStream_t st) {
     const long long tot = (long long)n * R;
-    k_build_jobs<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(cnt, n, R, jpos, epos, jobs, seg, need_r);
+    if (tot <= 0) return cudaSuccess;
+    const long long nb = (tot + kScanBlock - 1) / kScanBlock;
+    if (nb > 0x7fffffffLL) return cudaErrorInvalidValue;
+    k_jobs_reduce<<<(unsigned)nb, kScanBlock, 0, st>>>(cnt, tot, per, sums);
+    k_jobs_scan_sums<<<1, kScanBlock, 0, st>>>(sums, (int)nb);
+    k_jobs_emit<<<(unsigned)nb, kScanBlock, 0, st>>>(cnt, n, R, per, sums, (int)nb, jobs, seg, need_r);
     return cudaGetLastError();
 }
 
@@ -1256,12 +1368,14 @@ cudaError_t launch_shell_dense(int n, const float *S2P, const float2 *G, const f
 
 cudaError_t launch_weights_cand(const float *vals, int n, int R, int T, const float *pdf_orient, float pdf_orient_min,
                                 const float *pdf_off, double fraction, ParticleState *ps, unsigned int *cand_idx,
-                                float *cand_w, unsigned int *cand_cnt, int cap, float *dense_out, cudaStream_t st) {
+                                float *cand_w, unsigned int *cand_cnt, int cap, float *dense_out,
+                                const unsigned int *rowmin, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    const long long RT = (long long)R * T;
-    dim3 grid((unsigned)((RT + kChunk - 1) / kChunk), n);
-    k_weights_cand<<<grid, kWThreads, 0, st>>>(vals, R, T, pdf_orient, pdf_orient_min, pdf_off, fraction, ps,
-                                               cand_idx, cand_w, cand_cnt, cap, dense_out);
+    if ((size_t)T * sizeof(float) > 48 * 1024) return cudaErrorInvalidValue;
+    dim3 grid((unsigned)((R + kWRowsPerBlock - 1) / kWRowsPerBlock), n);
+    k_weights_cand<<<grid, kWThreads, sizeof(float) * T, st>>>(vals, R, T, pdf_orient, pdf_orient_min, pdf_off,
+                                                               fraction, ps, cand_idx, cand_w, cand_cnt, cap,
+                                                               dense_out, rowmin);
     return cudaGetLastError();
 }
 

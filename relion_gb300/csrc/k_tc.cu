@@ -158,6 +158,7 @@ struct TcArgs {
     const float *norm;       // [p][M]
     const float *pdf_orient; // [M]
     ParticleState *ps;
+    unsigned int *rowmin;    // [p][M] ordered minimum of each orientation row, or null
 };
 
 // Tile order of the persistent loop: groups of kGroupM orientation tiles,
@@ -171,10 +172,18 @@ __device__ __forceinline__ void tile_mn(int tidx, int mtiles, int ntiles, int &m
     nt = r / gm;
 }
 
-__device__ __forceinline__ void warp_min_flush(float lmin, unsigned int *dst) {
+// Warp minimum of lmin into *dst; returns it (ordered encoding, ~0 = none).
+__device__ __forceinline__ unsigned int warp_min_flush(float lmin, unsigned int *dst) {
     const unsigned int u = lmin < __int_as_float(0x7f800000) ? f2ord(lmin) : 0xFFFFFFFFu;
     const unsigned int wmin = __reduce_min_sync(0xffffffffu, u);
     if ((threadIdx.x & 31) == 0 && wmin != 0xFFFFFFFFu) atomicMin(dst, wmin);
+    return wmin;
+}
+
+// Ordered minimum of lane row m for particle p into rowmin (one atomic per
+// lane and particle segment of the tile half).
+__device__ __forceinline__ void rowmin_flush(const TcArgs &a, int p, int m, float v) {
+    if (p >= 0 && v < FLT_MAX) atomicMin(&a.rowmin[(size_t)p * a.M + m], f2ord(v));
 }
 
 // Persistent warp-specialised CTA, one per SM, tiles tidx = blockIdx.x +
@@ -297,6 +306,10 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_diff2(const TcArgs a) {
             const int m0 = mt * TM, n0 = nt * TN;
             const int m = m0 + q * 32 + lane;
             const bool skip = !(m < a.M) || !(a.pdf_orient[m] > 0.f);
+            // running row minimum of the particle segment this lane is in
+            const bool track_rows = a.rowmin != nullptr && a.T >= 32 && !skip;
+            int acc_p = -1;
+            float acc_m = __int_as_float(0x7f800000);
             for (int c = 0; c < 4; ++c) {
                 const int col = h * 128 + c * 32;
                 float v[32];
@@ -321,10 +334,26 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_diff2(const TcArgs a) {
                             else
                                 min_hi = fminf(min_hi, d);
                         }
+                        v[jj] = d;
                         tb[lane * 33 + jj] = d;
                     }
+                    const bool two = bnd < nvalid;
                     warp_min_flush(min_lo, &a.ps[p_lo].min_coarse);
-                    if (bnd < nvalid) warp_min_flush(min_hi, &a.ps[p_lo + 1].min_coarse);
+                    if (two) warp_min_flush(min_hi, &a.ps[p_lo + 1].min_coarse);
+                    if (track_rows) {
+                        if (p_lo != acc_p) {
+                            rowmin_flush(a, acc_p, m, acc_m);
+                            acc_p = p_lo;
+                            acc_m = min_lo;
+                        } else {
+                            acc_m = fminf(acc_m, min_lo);
+                        }
+                        if (two) {
+                            rowmin_flush(a, acc_p, m, acc_m);
+                            acc_p = p_lo + 1;
+                            acc_m = min_hi;
+                        }
+                    }
                 } else {
                     // short translation lists: one particle index per column
                     int p = p_lo, t = nb - p_lo * a.T;
@@ -360,6 +389,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_diff2(const TcArgs a) {
                 }
                 __syncwarp();
             }
+            if (track_rows) rowmin_flush(a, acc_p, m, acc_m);
             // accumulator drained: hand it back to the MMA issuer
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             __syncwarp();
@@ -450,7 +480,7 @@ cudaError_t launch_tc_pack_a(const float *src, int lds, int M, int K2, void *dst
 
 cudaError_t launch_tc_diff2(const void *Ablk, void *Yblk, int M, int K2, const float2 *b, int ldb, const float2 *E,
                             int lde, int nparticles, int T, float *out, const float *norm, const float *pdf_orient,
-                            ParticleState *ps, cudaStream_t st) {
+                            ParticleState *ps, unsigned int *rowmin, cudaStream_t st) {
     const int N = nparticles * T;
     if (N <= 0 || M <= 0) return cudaSuccess;
     const int ktiles = (K2 + TK - 1) / TK, ntiles = (N + TN - 1) / TN, mtiles = (M + TM - 1) / TM;
@@ -476,7 +506,7 @@ cudaError_t launch_tc_diff2(const void *Ablk, void *Yblk, int M, int K2, const f
     if (ntotal > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
     const int grid = (int)std::min<long long>(ntotal, nsm);
     TcArgs a{static_cast<const uint8_t *>(Ablk), static_cast<const uint8_t *>(Yblk), M, ktiles, T, N, nparticles,
-             mtiles, ntiles, out, norm, pdf_orient, ps};
+             mtiles, ntiles, out, norm, pdf_orient, ps, T >= 32 ? rowmin : nullptr};
     k_tc_diff2<<<grid, THREADS, smem, st>>>(a);
     return cudaGetLastError();
 }
