@@ -828,24 +828,29 @@ k_fine_diff2(const FineJob *__restrict__ jobs, const unsigned int *__restrict__ 
 // oversampled orientation, the significant fine weights (w >= thr_fine,
 // normalised by the sum) give W = sum w~ and the weighted phase sum
 // Phi_k = sum w~ E_(t,iot),k, from which
-//   sigma2 shell sums:  W C^2 |P|^2 - 2 C Re(P conj(X Phi)) + W |X|^2
+//   sigma2 shell sums:  sum w~ |C P - X E|^2 (difference first, as the
+//                       reference forms it per translation)
 //   backprojection:     img += C Minv Xn Phi,  weight += W C^2 Minv
 // (the per-translation sums of :8562-8780 rewritten with Phi).
-// One warp per oversampled orientation.
+// Blocks cover (job, chunk of kWsumPix fine pixels), one thread per pixel
+// for all oversampled orientations, so each phase value is loaded once.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_wsum(WsumArgs a) {
+constexpr int kWsumPix = 128;
+constexpr int kMaxOR = 8;
+
+__global__ void __launch_bounds__(kWsumPix) k_wsum(WsumArgs a) {
     extern __shared__ double wsm[];
     double *shell = wsm;                                            // [nshell]
-    float *wt = reinterpret_cast<float *>(shell + a.nshell);        // [nOR][rows]
-    int *tlist = reinterpret_cast<int *>(wt + a.nOR * a.T * a.nOT); // [T]
-    __shared__ double red[8];  // sumw, sigma2_offset, XA, AA
+    float *wt = reinterpret_cast<float *>(shell + a.nshell);        // [rows][kMaxOR]
+    int *tlist = reinterpret_cast<int *>(wt + a.T * a.nOT * kMaxOR); // [T]
+    __shared__ double red[4];  // sumw, sigma2_offset, XA, AA
     const FineJob job = a.jobs[blockIdx.x];
     const int p = job.p, r = job.r, n_t = job.n_t;
-    const int rows = n_t * a.nOT;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-    const ParticleState ps = a.ps[p];
-    const float thr = ps.thr_fine;
-    const double inv_sum = 1. / ps.sum_fine;
+    const int nOR = a.nOR, nOT = a.nOT;
+    const int rows = n_t * nOT;
+    const bool first = blockIdx.y == 0;  // the per-job scalars are added once
+    const float thr = a.ps[p].thr_fine;
+    const double inv_sum = 1. / a.ps[p].sum_fine;
     const double *pd = a.pdat + (size_t)p * 8;
     const int ic = r / (a.ndir * a.npsi), idir = (r / a.npsi) % a.ndir;
     const float scale = a.do_scale ? fmaxf((float)pd[6], 0.001f) : 1.f;
@@ -861,94 +866,104 @@ __global__ void __launch_bounds__(256) k_wsum(WsumArgs a) {
             }
         }
     }
-    if (threadIdx.x < 8) red[threadIdx.x] = 0.;
+    if (threadIdx.x < 4) red[threadIdx.x] = 0.;
     for (int i = threadIdx.x; i < a.nshell; i += blockDim.x) shell[i] = 0.;
     __syncthreads();
-    // normalised significant weights per (ior, row); FP64 scalar sums
+    // normalised significant weights per (row, ior); FP64 scalar sums
     double l_sumw = 0., l_off = 0.;
-    for (int i = threadIdx.x; i < rows * a.nOR; i += blockDim.x) {
-        const int ior = i / rows, row = i - ior * rows;
-        const int tr = row / a.nOT, iot = row - tr * a.nOT;
-        const long long e = job.off + ((long long)tr * a.nOR + ior) * a.nOT + iot;
-        const float w = a.w[e];
+    for (int i = threadIdx.x; i < rows * kMaxOR; i += blockDim.x) {
+        const int row = i / kMaxOR, ior = i - row * kMaxOR;
         float wn = 0.f;
-        if (w > 0.f && w >= thr) {
-            const double wd = (double)w * inv_sum;
-            wn = (float)wd;
-            l_sumw += wd;
-            const int tf = tlist[tr] * a.nOT + iot;
-            const double dx = pd[2] - pd[0] - a.otx[tf];
-            const double dy = pd[3] - pd[1] - a.oty[tf];
-            l_off += wd * a.pixel * a.pixel * dx * dx;
-            l_off += wd * a.pixel * a.pixel * dy * dy;
+        if (ior < nOR) {
+            const int tr = row / nOT, iot = row - tr * nOT;
+            const long long e = job.off + ((long long)tr * nOR + ior) * nOT + iot;
+            const float w = a.w[e];
+            if (w > 0.f && w >= thr) {
+                const double wd = (double)w * inv_sum;
+                wn = (float)wd;
+                l_sumw += wd;
+                const int tf = tlist[tr] * nOT + iot;
+                const double dx = pd[2] - pd[0] - a.otx[tf];
+                const double dy = pd[3] - pd[1] - a.oty[tf];
+                l_off += wd * a.pixel * a.pixel * dx * dx;
+                l_off += wd * a.pixel * a.pixel * dy * dy;
+            }
         }
-        wt[ior * rows + row] = wn;
+        wt[i] = wn;
     }
-    l_sumw = warp_sum(l_sumw);
-    l_off = warp_sum(l_off);
-    if (lane == 0) {
-        atomicAdd(&red[0], l_sumw);
-        atomicAdd(&red[1], l_off);
+    if (first) {
+        l_sumw = warp_sum(l_sumw);
+        l_off = warp_sum(l_off);
+        if ((threadIdx.x & 31) == 0) {
+            atomicAdd(&red[0], l_sumw);
+            atomicAdd(&red[1], l_off);
+        }
     }
     __syncthreads();
-    const float2 *Xp = a.Xf + (size_t)p * a.nf;
-    const float2 *Xnp = a.Xnf + (size_t)p * a.nf;
-    const float *Cp = a.Cf + (size_t)p * a.nf;
+    const int k = blockIdx.y * kWsumPix + threadIdx.x;
     double l_xa = 0., l_aa = 0.;
-    for (int ior = warp; ior < a.nOR; ior += nwarp) {
-        const float *wr = wt + ior * rows;
-        float Wsum = 0.f;
-        for (int row = 0; row < rows; ++row) Wsum += wr[row];
-        if (!(Wsum > 0.f)) continue;
-        const size_t rf = (size_t)r * a.nOR + ior;
-        const float2 *P = a.projf + rf * a.ldpf;
-        for (int k = lane; k < a.nf; k += 32) {
-            const float2 x = Xp[k], xn = Xnp[k], pv = P[k];
-            const float cs = Cp[k] * scale;
-            const float2 cp = make_float2(cs * pv.x, cs * pv.y);
-            // Phi = sum_t W E_t for the slice; the noise estimate as the
-            // reference forms it, sum_t W |C P - X E_t|^2 (difference first)
-            float2 phi = make_float2(0.f, 0.f);
-            float s2acc = 0.f;
-            for (int row = 0; row < rows; ++row) {
-                const float wv = wr[row];
-                if (wv != 0.f) {
-                    const int tr = row / a.nOT, iot = row - tr * a.nOT;
-                    const float2 e = a.phase_f[((size_t)tlist[tr] * a.nOT + iot) * a.nf + k];
-                    phi.x = fmaf(wv, e.x, phi.x);
-                    phi.y = fmaf(wv, e.y, phi.y);
-                    const float dr = cp.x - (x.x * e.x - x.y * e.y);
-                    const float di = cp.y - (x.x * e.y + x.y * e.x);
-                    s2acc = fmaf(wv, dr * dr + di * di, s2acc);
+    if (k < a.nf) {
+        const float2 x = a.Xf[(size_t)p * a.nf + k], xn = a.Xnf[(size_t)p * a.nf + k];
+        const float cs = a.Cf[(size_t)p * a.nf + k] * scale;
+        const size_t rf0 = (size_t)r * nOR;
+        float2 pv[kMaxOR], phi[kMaxOR];
+        float s2[kMaxOR], W[kMaxOR];
+#pragma unroll
+        for (int ior = 0; ior < kMaxOR; ++ior) {
+            pv[ior] = make_float2(0.f, 0.f);
+            if (ior < nOR) pv[ior] = a.projf[(rf0 + ior) * a.ldpf + k];
+            phi[ior] = make_float2(0.f, 0.f);
+            s2[ior] = 0.f;
+            W[ior] = 0.f;
+        }
+        for (int tr = 0; tr < n_t; ++tr) {
+            const float2 *ph = a.phase_f + (size_t)tlist[tr] * nOT * a.nf + k;
+            for (int iot = 0; iot < nOT; ++iot) {
+                const float2 e = ph[(size_t)iot * a.nf];
+                const float xr = x.x * e.x - x.y * e.y, xi = x.x * e.y + x.y * e.x;
+                const float *wr = wt + (tr * nOT + iot) * kMaxOR;
+#pragma unroll
+                for (int ior = 0; ior < kMaxOR; ++ior) {
+                    const float wv = wr[ior];
+                    const float dr = fmaf(cs, pv[ior].x, -xr), di = fmaf(cs, pv[ior].y, -xi);
+                    s2[ior] = fmaf(wv, dr * dr + di * di, s2[ior]);
+                    phi[ior].x = fmaf(wv, e.x, phi[ior].x);
+                    phi[ior].y = fmaf(wv, e.y, phi[ior].y);
+                    W[ior] += wv;
                 }
             }
-            const float2 zx = make_float2(x.x * phi.x - x.y * phi.y, x.x * phi.y + x.y * phi.x);
-            const float2 zn = make_float2(xn.x * phi.x - xn.y * phi.y, xn.x * phi.y + xn.y * phi.x);
-            const int sh = a.pf[k].shell;
-            const float p2 = pv.x * pv.x + pv.y * pv.y;
-            const float cross = pv.x * zx.x + pv.y * zx.y;
-            if (sh >= 0) {
-                atomicAdd(&shell[sh], (double)s2acc);
-                if (a.do_scale && a.dvp_mask[(size_t)ic * a.nshell + sh]) {
-                    l_xa += (double)cs * cross;
-                    l_aa += (double)Wsum * cs * cs * p2;
-                }
+        }
+        const int sh = a.pf[k].shell;
+        const bool scale_shell = sh >= 0 && a.do_scale && a.dvp_mask[(size_t)ic * a.nshell + sh];
+        const float minv = a.minv_store[k];
+        const float f = cs * minv;
+        double s2tot = 0.;
+#pragma unroll
+        for (int ior = 0; ior < kMaxOR; ++ior) {
+            if (!(W[ior] > 0.f)) continue;
+            const size_t rf = rf0 + ior;
+            const float2 zx = make_float2(x.x * phi[ior].x - x.y * phi[ior].y, x.x * phi[ior].y + x.y * phi[ior].x);
+            const float2 zn =
+                make_float2(xn.x * phi[ior].x - xn.y * phi[ior].y, xn.x * phi[ior].y + xn.y * phi[ior].x);
+            s2tot += (double)s2[ior];
+            if (scale_shell) {
+                l_xa += (double)cs * (pv[ior].x * zx.x + pv[ior].y * zx.y);
+                l_aa += (double)W[ior] * cs * cs * (pv[ior].x * pv[ior].x + pv[ior].y * pv[ior].y);
             }
-            const float minv = a.minv_store[k];
-            const float f = cs * minv;
-            const float wgt = Wsum * cs * cs * minv;
+            const float wgt = W[ior] * cs * cs * minv;
             if (wgt != 0.f || f != 0.f) {
                 atomicAdd(&a.bpimg[rf * a.nf + k].x, f * zn.x);
                 atomicAdd(&a.bpimg[rf * a.nf + k].y, f * zn.y);
                 atomicAdd(&a.bpw[rf * a.nf + k], wgt);
             }
+            if (first && threadIdx.x == 0) a.active[rf] = 1;
         }
-        if (lane == 0) a.active[rf] = 1;
+        if (sh >= 0 && s2tot != 0.) atomicAdd(&shell[sh], s2tot);
     }
     if (a.do_scale) {
         l_xa = warp_sum(l_xa);
         l_aa = warp_sum(l_aa);
-        if (lane == 0) {
+        if ((threadIdx.x & 31) == 0) {
             atomicAdd(&red[2], l_xa);
             atomicAdd(&red[3], l_aa);
         }
@@ -959,14 +974,16 @@ __global__ void __launch_bounds__(256) k_wsum(WsumArgs a) {
         if (shell[i] != 0.) atomicAdd(&sp[i], shell[i]);
     if (threadIdx.x == 0) {
         double *pa = a.pacc + (size_t)p * 8;
-        atomicAdd(&pa[0], red[0]);
-        atomicAdd(&pa[1], red[1]);
+        if (first) {
+            atomicAdd(&pa[0], red[0]);
+            atomicAdd(&pa[1], red[1]);
+            atomicAdd(&a.pdf_dir[(size_t)ic * a.ndir + idir], red[0]);
+            atomicAdd(&a.pdf_cls[ic], red[0]);
+        }
         if (a.do_scale) {
             atomicAdd(&pa[2], red[2]);
             atomicAdd(&pa[3], red[3]);
         }
-        atomicAdd(&a.pdf_dir[(size_t)ic * a.ndir + idir], red[0]);
-        atomicAdd(&a.pdf_cls[ic], red[0]);
     }
 }
 
@@ -1305,14 +1322,18 @@ cudaError_t launch_fine_diff2(const FineJob *jobs, long long njobs, const unsign
 
 cudaError_t launch_wsum(const WsumArgs &a, cudaStream_t st) {
     if (a.njobs <= 0) return cudaSuccess;
-    const size_t smem = sizeof(double) * a.nshell + sizeof(float) * a.nOR * a.T * a.nOT + sizeof(int) * a.T + 16;
+    if (a.nOR > kMaxOR) return cudaErrorInvalidValue;
+    if (a.njobs > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+    const size_t smem =
+        sizeof(double) * a.nshell + sizeof(float) * (size_t)kMaxOR * a.T * a.nOT + sizeof(int) * a.T + 16;
     static size_t attr = 0;
     if (smem > attr) {
         cudaError_t e = cudaFuncSetAttribute(k_wsum, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         attr = smem;
     }
-    k_wsum<<<(unsigned)a.njobs, 256, smem, st>>>(a);
+    dim3 grid((unsigned)a.njobs, (unsigned)((a.nf + kWsumPix - 1) / kWsumPix));
+    k_wsum<<<grid, kWsumPix, smem, st>>>(a);
     return cudaGetLastError();
 }
 
