@@ -187,8 +187,11 @@ int gbr_wsum_download(gbr_bundle *b, gbr_wsum *out);
 /* Zero the volumes and weighted sums (start of a new iteration). */
 int gbr_bundle_reset_wsum(gbr_bundle *b);
 
-/* Device-side timing of the last batch: kernel time of each stage (ms),
- * measured with CUDA events on the worker's stream. */
+/* Accumulated timing of the worker's batches (ms): the ten E-step stages
+ * (CUDA events on the worker's stream: prep, norm, cross term, coarse
+ * weights, significance + job list, fine diff2, fine weights, weighted sums,
+ * backprojection, read-back), then the input copies of each batch (device
+ * time before the first stage) and the host finalisation of the results. */
 int gbr_worker_stage_times(const gbr_worker *w, double *ms, int64_t n, int64_t *n_written);
 
 /* Number of CUDA kernels this worker has launched (all batches so far). */

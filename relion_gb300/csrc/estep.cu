@@ -13,6 +13,7 @@
 #include "sampling.h"
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -73,6 +74,33 @@ struct DevBuf {
         return cudaMemcpy(p, h, m * sizeof(T), cudaMemcpyHostToDevice);
     }
     cudaError_t zero(cudaStream_t st = 0) { return cudaMemsetAsync(p, 0, n * sizeof(T), st); }
+};
+
+// Page-locked host buffer: device-to-host copies into it stay asynchronous.
+template <class T>
+struct PinnedBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    PinnedBuf() = default;
+    PinnedBuf(const PinnedBuf &) = delete;
+    PinnedBuf &operator=(const PinnedBuf &) = delete;
+    ~PinnedBuf() { release(); }
+    void release() {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        n = 0;
+    }
+    cudaError_t reserve(size_t m) {
+        if (m <= n && p) return cudaSuccess;
+        release();
+        void *q = nullptr;
+        cudaError_t e = cudaMallocHost(&q, std::max<size_t>(m, 1) * sizeof(T));
+        if (e == cudaSuccess) {
+            p = static_cast<T *>(q);
+            n = std::max<size_t>(m, 1);
+        }
+        return e;
+    }
 };
 
 inline int pad16(int v) { return (v + 15) / 16 * 16; }
@@ -155,7 +183,8 @@ struct gbr_worker {
     gbr_bundle *b = nullptr;
     cudaStream_t st = nullptr;
     cudaEvent_t ev[ST_N + 1] = {};
-    double stage_ms[ST_N] = {};
+    double stage_ms[ST_N + 2] = {};  // device stages, then input copies and host finalisation
+    cudaEvent_t ev_in = nullptr;     // start of the batch's input copies
     int debug = 0;
     int cap = 0;  // particles the batch buffers hold
     long long launches = 0;  // kernels launched by this worker
@@ -187,6 +216,12 @@ struct gbr_worker {
     DevBuf<float> cand_w, dense_dbg;
     DevBuf<unsigned int> rowmin;           // [p][R] row minima of the tensor-core coarse pass
     DevBuf<long long> cand_seg;  // [2n]: begins, ends
+    // page-locked read-back of the batch (counts, job totals, results) and
+    // the host copies of device-resident metadata
+    PinnedBuf<unsigned int> h_ccnt;
+    PinnedBuf<long long> h_totals, h_segf;
+    PinnedBuf<ParticleState> h_ps;
+    PinnedBuf<double> h_shell, h_pacc, h_pdat, h_power;
     // dense fine pass
     int fine_mode = 0;  // 0: by significant density, 1: always dense, 2: always sparse
     int coarse_rows = 0;  // 0: skip far coarse rows by their minimum (tensor-core pass), 1: read all rows
@@ -624,58 +659,56 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
     GBR_CUDA(launch_weights_cand(w->vals.p, n, R, T, b->pdf_orient.p, b->pdf_orient_min, w->pdf_off.p,
                                  d.adaptive_fraction, w->ps.p, w->cand_idx.p, w->cand_w.p, w->cand_cnt.p, cap,
                                  dense_w, use_rowmin ? w->rowmin.p : nullptr, st));
-    std::vector<unsigned int> ccnt(n);
-    GBR_CUDA(cudaMemcpyAsync(ccnt.data(), w->cand_cnt.p, sizeof(unsigned int) * n, cudaMemcpyDeviceToHost, st));
-    GBR_CUDA(cudaStreamSynchronize(st));
-    if (d.precision == GBR_PREC_BF16) {
-        int flag = 0;
-        GBR_CUDA(tc_error_flag(&flag, 1));
-        if (flag) return fail(GBR_ERR_CUDA, "tensor-core pipeline timed out waiting for its MMAs");
-    }
-    unsigned int cmax = 0;
-    for (unsigned int c : ccnt) cmax = std::max(cmax, c);
-    const bool use_cand = cmax <= (unsigned int)cap;
     w->launches += 1;
-    if (use_cand) {
-        std::vector<long long> cs(2 * n);
-        for (int p = 0; p < n; ++p) {
-            cs[p] = (long long)p * cap;
-            cs[n + p] = (long long)p * cap + ccnt[p];
-        }
-        GBR_CUDA(cudaMemcpyAsync(w->cand_seg.p, cs.data(), sizeof(long long) * 2 * n, cudaMemcpyHostToDevice, st));
-        int s = threshold_search(w, n, w->cand_w.p, w->cand_seg.p, std::max<long long>(cmax, 1), 1,
-                                 w->cand_seg.p + n, RT);
-        if (s) return s;
-        GBR_CUDA(cudaMemsetAsync(w->mask.p, 0, sizeof(unsigned int) * (size_t)n * R * W, st));
-        GBR_CUDA(cudaMemsetAsync(w->cnt.p, 0, sizeof(int) * (size_t)n * R, st));
-        GBR_CUDA(launch_cand_masks(w->cand_idx.p, w->cand_w.p, w->cand_cnt.p, cap, n, R, T, W, w->ps.p, w->mask.p,
-                                   w->cnt.p, st));
-        w->launches += 1;
-    } else {
-        // a list overflowed (flat posterior): search the full weight array
-        GBR_CUDA(launch_weights(w->vals.p, w->seg_c.p, n, RT, 1, T, nullptr, nullptr, nullptr, nOR, nOT,
-                                b->pdf_orient.p, w->pdf_off.p, w->ps.p, w->hist.p, st, 0));
-        int s = threshold_search(w, n, w->vals.p, w->seg_c.p, RT, 1);
-        if (s) return s;
-        GBR_CUDA(launch_sig_masks(w->vals.p, n, R, T, W, w->ps.p, w->mask.p, w->cnt.p, st));
-        w->launches += 2;
-    }
-    GBR_CUDA(cudaEventRecord(w->ev[4], st));
+    GBR_CUDA(w->h_ccnt.reserve(n));
+    GBR_CUDA(w->h_totals.reserve(2));
+    GBR_CUDA(w->h_segf.reserve(n + 1));
+    // Speculative: the candidate lists are taken as complete and the host
+    // checks their counts at the job-list read-back; if one overflowed
+    // (flat posterior), the threshold search reruns on the full weight array.
+    GBR_CUDA(launch_cand_seg(w->cand_cnt.p, n, cap, w->cand_seg.p, st));
+    int s = threshold_search(w, n, w->cand_w.p, w->cand_seg.p, cap, 1, w->cand_seg.p + n, RT);
+    if (s) return s;
+    GBR_CUDA(cudaMemsetAsync(w->mask.p, 0, sizeof(unsigned int) * (size_t)n * R * W, st));
+    GBR_CUDA(cudaMemsetAsync(w->cnt.p, 0, sizeof(int) * (size_t)n * R, st));
+    GBR_CUDA(launch_cand_masks(w->cand_idx.p, w->cand_w.p, w->cand_cnt.p, cap, n, R, T, W, w->ps.p, w->mask.p,
+                               w->cnt.p, st));
+    GBR_CUDA(cudaMemcpyAsync(w->h_ccnt.p, w->cand_cnt.p, sizeof(unsigned int) * n, cudaMemcpyDeviceToHost, st));
+    w->launches += 2;
     if (w->debug) {
         w->dbg_wcoarse.resize((size_t)n * RT);
         GBR_CUDA(cudaMemcpyAsync(w->dbg_wcoarse.data(), dense_w, sizeof(float) * n * RT, cudaMemcpyDeviceToHost, st));
     }
     const long long nR = (long long)n * R;
-    GBR_CUDA(cudaMemsetAsync(w->need_r.p, 0, R, st));
-    GBR_CUDA(launch_fine_jobs(w->cnt.p, n, R, nOR * nOT, w->scan_tmp.p, w->jobs.p, w->seg_f.p, w->need_r.p, st));
     const long long nbj = (nR + 1023) / 1024;
-    long long totals[2] = {0, 0};
-    GBR_CUDA(cudaMemcpyAsync(totals, w->scan_tmp.p + 2 * nbj, sizeof(totals), cudaMemcpyDeviceToHost, st));
-    std::vector<long long> segf(n + 1);
-    GBR_CUDA(cudaMemcpyAsync(segf.data(), w->seg_f.p, sizeof(long long) * (n + 1), cudaMemcpyDeviceToHost, st));
-    GBR_CUDA(cudaStreamSynchronize(st));
-    const long long njobs = totals[0], nfine = totals[1];
-    w->launches += 3;
+    for (int attempt = 0;; ++attempt) {
+        GBR_CUDA(cudaEventRecord(w->ev[4], st));
+        GBR_CUDA(cudaMemsetAsync(w->need_r.p, 0, R, st));
+        GBR_CUDA(launch_fine_jobs(w->cnt.p, n, R, nOR * nOT, w->scan_tmp.p, w->jobs.p, w->seg_f.p, w->need_r.p, st));
+        GBR_CUDA(cudaMemcpyAsync(w->h_totals.p, w->scan_tmp.p + 2 * nbj, sizeof(long long) * 2, cudaMemcpyDeviceToHost,
+                                 st));
+        GBR_CUDA(cudaMemcpyAsync(w->h_segf.p, w->seg_f.p, sizeof(long long) * (n + 1), cudaMemcpyDeviceToHost, st));
+        GBR_CUDA(cudaStreamSynchronize(st));
+        w->launches += 3;
+        if (attempt > 0) break;
+        if (d.precision == GBR_PREC_BF16) {
+            int flag = 0;
+            GBR_CUDA(tc_error_flag(&flag, 1));
+            if (flag) return fail(GBR_ERR_CUDA, "tensor-core pipeline timed out waiting for its MMAs");
+        }
+        unsigned int cmax = 0;
+        for (int p = 0; p < n; ++p) cmax = std::max(cmax, w->h_ccnt.p[p]);
+        if (cmax <= (unsigned int)cap) break;
+        // a list overflowed: significance from the full weight array
+        GBR_CUDA(launch_weights(w->vals.p, w->seg_c.p, n, RT, 1, T, nullptr, nullptr, nullptr, nOR, nOT,
+                                b->pdf_orient.p, w->pdf_off.p, w->ps.p, w->hist.p, st, 0));
+        s = threshold_search(w, n, w->vals.p, w->seg_c.p, RT, 1);
+        if (s) return s;
+        GBR_CUDA(launch_sig_masks(w->vals.p, n, R, T, W, w->ps.p, w->mask.p, w->cnt.p, st));
+        w->launches += 2;
+    }
+    const long long njobs = w->h_totals.p[0], nfine = w->h_totals.p[1];
+    const std::vector<long long> segf(w->h_segf.p, w->h_segf.p + n + 1);
     if (njobs <= 0 || nfine <= 0) return fail(GBR_ERR_NUMERICAL, "no significant coarse samples");
     // ---- fine pass: dense contractions when most poses are significant ----
     const double density = (double)nfine / ((double)n * b->RF * b->TF);
@@ -684,7 +717,6 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
     const bool dense = dense_fits && (w->fine_mode == 1 || (w->fine_mode == 0 && density > 0.1));
     w->last_dense = dense ? 1 : 0;
     long long max_seg = 0;
-    int s;
     if (dense) {
         s = fine_dense(w, n, max_seg);
     } else {
@@ -701,19 +733,20 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
     GBR_CUDA(w->act_count.reserve(1));
     GBR_CUDA(cudaMemsetAsync(w->act_count.p, 0, sizeof(int), st));
     GBR_CUDA(launch_compact_flags(b->active.p, (int)b->RF, w->act_list.p, w->act_count.p, st));
-    int nact = 0;
-    GBR_CUDA(cudaMemcpyAsync(&nact, w->act_count.p, sizeof(int), cudaMemcpyDeviceToHost, st));
-    GBR_CUDA(cudaStreamSynchronize(st));
-    GBR_CUDA(launch_backproject(w->act_list.p, nact, b->eul_f.p, nOR, b->cls_of_r.p, b->bpimg.p, b->bpw.p, b->pf.p,
-                                b->nf, b->cur / 2 + 1, b->bg, b->bpd_ptrs.p, b->bpw_ptrs.p, b->active.p, st));
+    GBR_CUDA(launch_backproject(w->act_list.p, w->act_count.p, (int)b->RF, b->eul_f.p, nOR, b->cls_of_r.p,
+                                b->bpimg.p, b->bpw.p, b->pf.p, b->nf, b->bg, b->bpd_ptrs.p, b->bpw_ptrs.p,
+                                b->active.p, st));
     GBR_CUDA(cudaEventRecord(w->ev[9], st));
-    w->launches += 1 + (nact > 0 ? 1 : 0);
+    w->launches += 2;
     // ---- results ----
-    std::vector<ParticleState> psh(n);
-    std::vector<double> shell((size_t)n * b->nshell), pacc((size_t)n * 8);
-    GBR_CUDA(cudaMemcpyAsync(psh.data(), w->ps.p, sizeof(ParticleState) * n, cudaMemcpyDeviceToHost, st));
-    GBR_CUDA(cudaMemcpyAsync(shell.data(), w->shell.p, sizeof(double) * shell.size(), cudaMemcpyDeviceToHost, st));
-    GBR_CUDA(cudaMemcpyAsync(pacc.data(), w->pacc.p, sizeof(double) * pacc.size(), cudaMemcpyDeviceToHost, st));
+    GBR_CUDA(w->h_ps.reserve(n));
+    GBR_CUDA(w->h_shell.reserve((size_t)n * b->nshell));
+    GBR_CUDA(w->h_pacc.reserve((size_t)n * 8));
+    const ParticleState *psh = w->h_ps.p;
+    const double *shell = w->h_shell.p, *pacc = w->h_pacc.p;
+    GBR_CUDA(cudaMemcpyAsync(w->h_ps.p, w->ps.p, sizeof(ParticleState) * n, cudaMemcpyDeviceToHost, st));
+    GBR_CUDA(cudaMemcpyAsync(w->h_shell.p, w->shell.p, sizeof(double) * n * b->nshell, cudaMemcpyDeviceToHost, st));
+    GBR_CUDA(cudaMemcpyAsync(w->h_pacc.p, w->pacc.p, sizeof(double) * n * 8, cudaMemcpyDeviceToHost, st));
     GBR_CUDA(cudaEventRecord(w->ev[10], st));
     GBR_CUDA(cudaStreamSynchronize(st));
     for (int st_i = 0; st_i < ST_N; ++st_i) {
@@ -721,6 +754,12 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
         cudaEventElapsedTime(&ms, w->ev[st_i], w->ev[st_i + 1]);
         w->stage_ms[st_i] += ms;
     }
+    {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, w->ev_in, w->ev[0]);
+        w->stage_ms[ST_N] += ms;
+    }
+    const auto t_final = std::chrono::steady_clock::now();
     if (w->debug) {
         w->dbg_n = n;
         w->dbg_cc.resize(n);
@@ -790,6 +829,8 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
         b->w_LL += o.dLL;
         b->w_ave_Pmax += o.pmax;
     }
+    w->stage_ms[ST_N + 1] +=
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_final).count();
     return GBR_OK;
 }
 
@@ -925,6 +966,7 @@ int gbr_worker_create(gbr_bundle *b, gbr_worker **out) {
     w->b = b;
     GBR_CUDA(cudaStreamCreateWithFlags(&w->st, cudaStreamNonBlocking));
     for (int i = 0; i <= ST_N; ++i) GBR_CUDA(cudaEventCreate(&w->ev[i]));
+    GBR_CUDA(cudaEventCreate(&w->ev_in));
     const char *dbg = std::getenv("GBR_DEBUG_FETCH");
     w->debug = dbg && dbg[0] == '1';
     const char *fm = std::getenv("GBR_FINE_MODE");
@@ -963,28 +1005,23 @@ int gbr_expect_batch(gbr_worker *w, const gbr_particle_batch *batch, gbr_particl
     if (s) return s;
     const size_t full = (size_t)b->full_npix;
     const cudaMemcpyKind kind = batch->device_resident ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
-    std::vector<double> pdat, power;
     for (int p0 = 0; p0 < n_all; p0 += w->cap) {
         const int n = std::min(w->cap, n_all - p0);
+        GBR_CUDA(cudaEventRecord(w->ev_in, w->st));
         GBR_CUDA(cudaMemcpyAsync(w->X.p, batch->fimg + 2 * full * p0, sizeof(float2) * full * n, kind, w->st));
         GBR_CUDA(cudaMemcpyAsync(w->Xn.p, batch->fimg_nomask + 2 * full * p0, sizeof(float2) * full * n, kind, w->st));
         GBR_CUDA(cudaMemcpyAsync(w->C.p, batch->fctf + full * p0, sizeof(float) * full * n, kind, w->st));
-        pdat.assign((size_t)n * 8, 0.);
-        power.assign((size_t)n * b->nshell, 0.);
+        GBR_CUDA(w->h_pdat.reserve((size_t)n * 8));
+        GBR_CUDA(w->h_power.reserve((size_t)n * b->nshell));
+        double *pdat = w->h_pdat.p, *power = w->h_power.p;
         if (batch->device_resident) {
-            std::vector<double> tmp((size_t)n * 2);
-            GBR_CUDA(cudaMemcpy(tmp.data(), batch->old_offset + 2 * p0, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost));
-            for (int p = 0; p < n; ++p) { pdat[p * 8 + 0] = tmp[2 * p]; pdat[p * 8 + 1] = tmp[2 * p + 1]; }
-            GBR_CUDA(cudaMemcpy(tmp.data(), batch->prior + 2 * p0, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost));
-            for (int p = 0; p < n; ++p) { pdat[p * 8 + 2] = tmp[2 * p]; pdat[p * 8 + 3] = tmp[2 * p + 1]; }
-            GBR_CUDA(cudaMemcpy(tmp.data(), batch->highres_Xi2 + p0, sizeof(double) * n, cudaMemcpyDeviceToHost));
-            for (int p = 0; p < n; ++p) pdat[p * 8 + 4] = tmp[p];
-            GBR_CUDA(cudaMemcpy(tmp.data(), batch->norm_correction + p0, sizeof(double) * n, cudaMemcpyDeviceToHost));
-            for (int p = 0; p < n; ++p) pdat[p * 8 + 5] = tmp[p];
-            GBR_CUDA(cudaMemcpy(tmp.data(), batch->scale + p0, sizeof(double) * n, cudaMemcpyDeviceToHost));
-            for (int p = 0; p < n; ++p) pdat[p * 8 + 6] = tmp[p];
-            GBR_CUDA(cudaMemcpy(power.data(), batch->power_img + (size_t)b->nshell * p0,
-                                sizeof(double) * b->nshell * n, cudaMemcpyDeviceToHost));
+            // metadata rows gathered on the device; the host copies (for the
+            // per-particle finalisation) arrive before the batch's last sync
+            GBR_CUDA(launch_gather_pdat(batch->old_offset + 2 * p0, batch->prior + 2 * p0, batch->highres_Xi2 + p0,
+                                        batch->norm_correction + p0, batch->scale + p0, n, w->pdat.p, w->st));
+            GBR_CUDA(cudaMemcpyAsync(pdat, w->pdat.p, sizeof(double) * n * 8, cudaMemcpyDeviceToHost, w->st));
+            GBR_CUDA(cudaMemcpyAsync(power, batch->power_img + (size_t)b->nshell * p0, sizeof(double) * b->nshell * n,
+                                     cudaMemcpyDeviceToHost, w->st));
         } else {
             for (int p = 0; p < n; ++p) {
                 const int q = p0 + p;
@@ -995,11 +1032,12 @@ int gbr_expect_batch(gbr_worker *w, const gbr_particle_batch *batch, gbr_particl
                 pdat[p * 8 + 4] = batch->highres_Xi2[q];
                 pdat[p * 8 + 5] = batch->norm_correction[q];
                 pdat[p * 8 + 6] = batch->scale[q];
+                pdat[p * 8 + 7] = 0.;
             }
-            std::memcpy(power.data(), batch->power_img + (size_t)b->nshell * p0, sizeof(double) * b->nshell * n);
+            std::memcpy(power, batch->power_img + (size_t)b->nshell * p0, sizeof(double) * b->nshell * n);
+            GBR_CUDA(cudaMemcpyAsync(w->pdat.p, pdat, sizeof(double) * n * 8, cudaMemcpyHostToDevice, w->st));
         }
-        GBR_CUDA(cudaMemcpyAsync(w->pdat.p, pdat.data(), sizeof(double) * pdat.size(), cudaMemcpyHostToDevice, w->st));
-        s = run_batch(w, n, power.data(), pdat.data(), res + p0);
+        s = run_batch(w, n, power, pdat, res + p0);
         if (s) return s;
     }
     return GBR_OK;
@@ -1131,7 +1169,7 @@ int gbr_bundle_reset_wsum(gbr_bundle *b) {
 
 int gbr_worker_stage_times(const gbr_worker *w, double *ms, int64_t n, int64_t *n_written) {
     if (!w || !ms) return fail(GBR_ERR_INVALID, "null argument");
-    const int64_t m = std::min<int64_t>(n, ST_N);
+    const int64_t m = std::min<int64_t>(n, ST_N + 2);
     for (int64_t i = 0; i < m; ++i) ms[i] = w->stage_ms[i];
     if (n_written) *n_written = m;
     return GBR_OK;
@@ -1159,6 +1197,7 @@ int gbr_worker_destroy(gbr_worker *w) {
     if (w->st) cudaStreamSynchronize(w->st);
     for (int i = 0; i <= ST_N; ++i)
         if (w->ev[i]) cudaEventDestroy(w->ev[i]);
+    if (w->ev_in) cudaEventDestroy(w->ev_in);
     if (w->st) cudaStreamDestroy(w->st);
     delete w;
     return GBR_OK;

@@ -204,9 +204,12 @@ struct WsumArgs {
 cudaError_t launch_wsum(const WsumArgs &a, cudaStream_t st);
 cudaError_t launch_compact_flags(const unsigned char *flags, int n, int *list, int *count,
                                  cudaStream_t st);
-cudaError_t launch_backproject(const int *list, int nlist, const float *eul_f, int nOR,
-                               const int *cls_of_r, float2 *bpimg, float *bpw, const PixelRef *pf,
-                               int nf, int sh, const VolGeom &g, double2 *const *data,
-                               double *const *weight, unsigned char *active, cudaStream_t st);
+cudaError_t launch_backproject(const int *list, const int *count, int max_list, const float *eul_f, int nOR,
+                               const int *cls_of_r, float2 *bpimg, float *bpw, const PixelRef *pf, int nf,
+                               const VolGeom &g, double2 *const *data, double *const *weight,
+                               unsigned char *active, cudaStream_t st);
+cudaError_t launch_gather_pdat(const double *old_offset, const double *prior, const double *xi2,
+                               const double *norm, const double *scale, int n, double *pdat, cudaStream_t st);
+cudaError_t launch_cand_seg(const unsigned int *cnt, int n, int cap, long long *seg, cudaStream_t st);
 
 }  // namespace gbr

@@ -1004,9 +1004,13 @@ __global__ void k_backproject(const int *__restrict__ list, const float *__restr
                               const int *__restrict__ cls_of_r, float2 *__restrict__ bpimg,
                               float *__restrict__ bpw, const PixelRef *__restrict__ pf, int nf,
                               const VolGeom g, double2 *const *__restrict__ data,
-                              double *const *__restrict__ weight, unsigned char *__restrict__ active) {
-    const int rf = list[blockIdx.x];
+                              double *const *__restrict__ weight, unsigned char *__restrict__ active,
+                              const int *__restrict__ count) {
+    const int nlist = *count;
+    for (int li = blockIdx.x; li < nlist; li += gridDim.x) {
+    const int rf = list[li];
     __shared__ float Ai[9];
+    __syncthreads();  // the previous slice's readers of Ai are done
     if (threadIdx.x < 9) Ai[threadIdx.x] = eul_f[(size_t)rf * 9 + threadIdx.x];
     __syncthreads();
     const int ic = cls_of_r[rf / nOR];
@@ -1053,6 +1057,7 @@ __global__ void k_backproject(const int *__restrict__ list, const float *__restr
         }
     }
     if (threadIdx.x == 0) active[rf] = 0;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1344,17 +1349,60 @@ cudaError_t launch_compact_flags(const unsigned char *flags, int n, int *list, i
     return cudaGetLastError();
 }
 
-cudaError_t launch_backproject(const int *list, int nlist, const float *eul_f, int nOR,
-                               const int *cls_of_r, float2 *bpimg, float *bpw, const PixelRef *pf,
-                               int nf, int sh, const VolGeom &g, double2 *const *data,
-                               double *const *weight, unsigned char *active, cudaStream_t st) {
-    (void)sh;
-    if (nlist <= 0) return cudaSuccess;
-    k_backproject<<<nlist, 256, 0, st>>>(list, eul_f, nOR, cls_of_r, bpimg, bpw, pf, nf, g, data,
-                                         weight, active);
+cudaError_t launch_backproject(const int *list, const int *count, int max_list, const float *eul_f, int nOR,
+                               const int *cls_of_r, float2 *bpimg, float *bpw, const PixelRef *pf, int nf,
+                               const VolGeom &g, double2 *const *data, double *const *weight,
+                               unsigned char *active, cudaStream_t st) {
+    if (max_list <= 0) return cudaSuccess;
+    // slices are read from the device-side list; the grid covers the device
+    // a few times over and loops over the slices present
+    int dev = 0, nsm = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const int grid = std::min(max_list, 8 * nsm);
+    k_backproject<<<grid, 256, 0, st>>>(list, eul_f, nOR, cls_of_r, bpimg, bpw, pf, nf, g, data, weight,
+                                        active, count);
     return cudaGetLastError();
 }
 
+// Per-particle metadata rows pdat[p] = {old_x, old_y, prior_x, prior_y,
+// highres_Xi2, norm, scale, 0} from device-resident batch arrays.
+__global__ void k_gather_pdat(const double *__restrict__ old_offset, const double *__restrict__ prior,
+                              const double *__restrict__ xi2, const double *__restrict__ norm,
+                              const double *__restrict__ scale, int n, double *__restrict__ pdat) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    double *o = pdat + (size_t)p * 8;
+    o[0] = old_offset[2 * p];
+    o[1] = old_offset[2 * p + 1];
+    o[2] = prior[2 * p];
+    o[3] = prior[2 * p + 1];
+    o[4] = xi2[p];
+    o[5] = norm[p];
+    o[6] = scale[p];
+    o[7] = 0.;
+}
+
+cudaError_t launch_gather_pdat(const double *old_offset, const double *prior, const double *xi2,
+                               const double *norm, const double *scale, int n, double *pdat, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    k_gather_pdat<<<(n + 127) / 128, 128, 0, st>>>(old_offset, prior, xi2, norm, scale, n, pdat);
+    return cudaGetLastError();
+}
+
+// Candidate-list segments: [p cap, p cap + min(count, cap)) per particle.
+__global__ void k_cand_seg(const unsigned int *__restrict__ cnt, int n, int cap, long long *__restrict__ seg) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    seg[p] = (long long)p * cap;
+    seg[n + p] = (long long)p * cap + (long long)min(cnt[p], (unsigned int)cap);
+}
+
+cudaError_t launch_cand_seg(const unsigned int *cnt, int n, int cap, long long *seg, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    k_cand_seg<<<(n + 127) / 128, 128, 0, st>>>(cnt, n, cap, seg);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_fine_normalize(float *w, int n, int R, int nOR, int nOT, int T, const ParticleState *ps,
                                   const double *pdat, const double *otx, const double *oty, double pixel,

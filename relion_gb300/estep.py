@@ -96,6 +96,10 @@ class MlDeviceBundle:
 
 
 RESULT_FIELDS = [n for n, _ in _lib.ParticleResult._fields_]
+# numpy image of gbr_particle_result: the library writes the rows in place
+RESULT_DTYPE = np.dtype([(n, np.int64 if t is _lib.I64 else np.float64)
+                         for n, t in _lib.ParticleResult._fields_])
+assert RESULT_DTYPE.itemsize == C.sizeof(_lib.ParticleResult)
 
 
 class MlOptimiserCuda:
@@ -142,12 +146,8 @@ class MlOptimiserCuda:
             b.fctf = arr(batch["fctf"], np.float32)
             for k in ("power_img", "old_offset", "prior", "highres_Xi2", "norm_correction", "scale"):
                 setattr(b, k, arr(batch[k], np.float64))
-        res = (_lib.ParticleResult * n)()
-        check(self.lib.gbr_expect_batch(self.h, C.byref(b), res))
-        out = np.zeros(n, dtype=[(f, np.float64) for f in RESULT_FIELDS])
-        for i in range(n):
-            for f in RESULT_FIELDS:
-                out[f][i] = getattr(res[i], f)
+        out = np.zeros(n, dtype=RESULT_DTYPE)
+        check(self.lib.gbr_expect_batch(self.h, C.byref(b), out.ctypes.data))
         return out
 
     def debug_fetch(self, what, i):
@@ -182,7 +182,7 @@ class MlOptimiserCuda:
 
 
 STAGES = ["prep", "norm_gemm", "cross_gemm", "weights_coarse", "sig_jobs", "diff2_fine",
-          "weights_fine", "wsum", "backproject", "readback"]
+          "weights_fine", "wsum", "backproject", "readback", "inputs", "host_final"]
 
 
 def measure_fp32_peak(device=0):
