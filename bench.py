@@ -196,10 +196,8 @@ def run_ours(args, world, rank, local):
     e2e_total = float(sum(e2e_ms))
 
     if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([total_ms, e2e_total], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms, e2e_total = float(t[0]), float(t[1])
+        from relion_gb300.replicas import max_over_ranks
+        total_ms, e2e_total = max_over_ranks([total_ms, e2e_total], device=dev)
 
     # ---- roofline of the dominant kernel: the coarse cross-term GEMM ----
     R = bundle.nr_classes * bundle.ndir * bundle.npsi

@@ -27,6 +27,14 @@ CONFIGS = {
                         blob_radius=90.0, max_shift=3.0, defocus=(8000.0, 25000.0), snr=0.03,
                         ini_high=20.0, healpix_order=3, psi_step=-1.0, offset_range_px=6.0,
                         offset_step_px=1.0, diameter=200.0, classes=1),
+    # 3D classification, box 256 px, K=4: each class displaces a random 15 %
+    # of a shared 4,000-Gaussian volume by 3-8 A; poses 70 % from three
+    # von Mises-Fisher preferred views (kappa 5), 30 % uniform; search as box 256
+    "cfg4_box256_K4": dict(box=256, pixel=1.0, n_particles=50000, n_blobs=4000, blob_sigma=1.5,
+                           blob_radius=90.0, max_shift=3.0, defocus=(8000.0, 25000.0), snr=0.03,
+                           ini_high=20.0, healpix_order=3, psi_step=-1.0, offset_range_px=6.0,
+                           offset_step_px=1.0, diameter=200.0, classes=4,
+                           class_displace=(0.15, 3.0, 8.0), views=(3, 5.0, 0.7)),
 }
 
 KV, CS, Q0 = 300.0, 2.7, 0.1
@@ -90,6 +98,48 @@ def random_rotations(n, gen):
     return R.view(n, 3, 3)
 
 
+def euler_matrices(rot, tilt, psi):
+    """ZYZ Euler angles (degrees, [n]) -> [n, 3, 3] matrices whose third row
+    is the projection direction (Euler_angles2matrix, src/euler.cpp)."""
+    a, b, g = (torch.as_tensor(v, dtype=torch.float64) * math.pi / 180.0 for v in (rot, tilt, psi))
+    ca, sa, cb, sb, cg, sg = a.cos(), a.sin(), b.cos(), b.sin(), g.cos(), g.sin()
+    cc, cs, sc, ss = cb * ca, cb * sa, sb * ca, sb * sa
+    R = torch.stack([cg * cc - sg * sa, cg * cs + sg * ca, -cg * sb,
+                     -sg * cc - cg * sa, -sg * cs + cg * ca, sg * sb,
+                     sc, ss, cb], dim=-1)
+    return R.view(-1, 3, 3)
+
+
+def preferred_view_rotations(n, gen, views, kappa, fraction):
+    """n rotations: with probability `fraction` the projection direction is
+    drawn from a von Mises-Fisher distribution (concentration kappa) around
+    one of the unit vectors `views` [m, 3] (chosen uniformly), else the pose
+    is uniform on SO(3); psi is uniform.  vMF on the sphere by the inverse
+    CDF of w = cos(angle to the mean): w = 1 + log(u + (1 - u) e^{-2 kappa}) / kappa."""
+    R = random_rotations(n, gen)
+    pick = torch.rand(n, generator=gen, dtype=torch.float64) < fraction
+    k = int(pick.sum())
+    if k == 0:
+        return R
+    mu = views[torch.randint(len(views), (k,), generator=gen)]
+    u = torch.rand(k, generator=gen, dtype=torch.float64)
+    w = 1.0 + torch.log(u + (1.0 - u) * math.exp(-2.0 * kappa)) / kappa
+    phi = 2.0 * math.pi * torch.rand(k, generator=gen, dtype=torch.float64)
+    # orthonormal frame (v1, v2) perpendicular to each mean direction
+    helper = torch.where(mu[:, :1].abs() < 0.9, torch.tensor([1.0, 0, 0], dtype=torch.float64),
+                         torch.tensor([0, 1.0, 0], dtype=torch.float64))
+    v1 = torch.linalg.cross(mu, helper)
+    v1 = v1 / v1.norm(dim=1, keepdim=True)
+    v2 = torch.linalg.cross(mu, v1)
+    st = torch.sqrt(torch.clamp(1.0 - w * w, min=0.0))[:, None]
+    d = w[:, None] * mu + st * (phi.cos()[:, None] * v1 + phi.sin()[:, None] * v2)
+    rot = torch.rad2deg(torch.atan2(d[:, 1], d[:, 0]))
+    tilt = torch.rad2deg(torch.acos(torch.clamp(d[:, 2], -1.0, 1.0)))
+    psi = 360.0 * torch.rand(k, generator=gen, dtype=torch.float64)
+    R[pick] = euler_matrices(rot, tilt, psi)
+    return R
+
+
 class GaussianVolume:
     """Sum of isotropic Gaussians; analytic Fourier transform (cycles/pixel)."""
 
@@ -102,6 +152,22 @@ class GaussianVolume:
         self.amps = (0.5 + torch.rand(n_blobs, generator=gen, dtype=torch.float64)).to(device)
         self.sigma = sigma
         self.device = device
+
+    def displaced(self, fraction, lo, hi, gen):
+        """Copy with a random `fraction` of the Gaussians moved by a random
+        distance in [lo, hi] pixels along a random direction (class variants)."""
+        v = GaussianVolume.__new__(GaussianVolume)
+        v.sigma, v.device, v.amps = self.sigma, self.device, self.amps
+        n = len(self.centers)
+        m = int(round(fraction * n))
+        idx = torch.randperm(n, generator=gen)[:m]
+        d = torch.randn(m, 3, generator=gen, dtype=torch.float64)
+        d = d / d.norm(dim=1, keepdim=True)
+        dist = lo + (hi - lo) * torch.rand(m, 1, generator=gen, dtype=torch.float64)
+        c = self.centers.clone().cpu()
+        c[idx] += d * dist
+        v.centers = c.to(self.device)
+        return v
 
     def ft(self, k, chunk=1 << 15):
         """F(k) for k [..., 3] in cycles/pixel -> complex128 [...]."""
@@ -167,8 +233,11 @@ class Dataset:
     """Seeded synthetic E-step problem for one configuration."""
 
     def __init__(self, cfg, seed=0, n_particles=None, device="cpu", healpix_order=None,
-                 psi_step=None, offset_range_px=None, offset_step_px=None):
+                 psi_step=None, offset_range_px=None, offset_step_px=None, classes=None):
         c = dict(CONFIGS[cfg]) if isinstance(cfg, str) else dict(cfg)
+        if classes is not None:
+            c["classes"] = classes
+            c.setdefault("class_displace", (0.15, 3.0, 8.0))
         if healpix_order is not None:
             c["healpix_order"] = healpix_order
         if psi_step is not None:
@@ -185,8 +254,19 @@ class Dataset:
         box, pix = c["box"], c["pixel"]
         self.current, self.coarse = estep_sizes(box, pix, c["ini_high"], c["healpix_order"], c["diameter"])
         self.vol = GaussianVolume(c["n_blobs"], c["blob_sigma"], c["blob_radius"], self.gen, device)
+        K = int(c.get("classes", 1))
+        self.vols = [self.vol]
+        if K > 1:
+            frac, lo, hi = c.get("class_displace", (0.15, 3.0, 8.0))
+            self.vols = [self.vol.displaced(frac, lo / pix, hi / pix, self.gen) for _ in range(K)]
+        self.views = None
+        if c.get("views"):
+            m = int(c["views"][0])
+            v = torch.randn(m, 3, generator=self.gen, dtype=torch.float64)
+            self.views = v / v.norm(dim=1, keepdim=True)
         self.r_max = min(self.current // 2, box // 2)
-        self.ref = padded_reference(self.vol, box, pix, self.r_max, 2, c["ini_high"])
+        self.refs = [padded_reference(v, box, pix, self.r_max, 2, c["ini_high"]) for v in self.vols]
+        self.ref = self.refs[0]
         self.sigma2 = None
 
     def model(self, precision=0):
@@ -241,7 +321,13 @@ class Dataset:
         count = self.n - start if count is None else count
         box, pix, cur = c["box"], c["pixel"], self.current
         g = torch.Generator().manual_seed(self.seed * 1000003 + start)
-        R = random_rotations(count, g)
+        if self.views is not None:
+            _, kappa, frac = c["views"]
+            R = preferred_view_rotations(count, g, self.views, float(kappa), float(frac))
+        else:
+            R = random_rotations(count, g)
+        K = len(self.vols)
+        labels = torch.randint(K, (count,), generator=g) if K > 1 else torch.zeros(count, dtype=torch.long)
         shifts = (torch.rand(count, 2, generator=g, dtype=torch.float64) * 2 - 1) * c["max_shift"]
         dlo, dhi = c["defocus"]
         dU = dlo + (dhi - dlo) * torch.rand(count, generator=g, dtype=torch.float64)
@@ -254,7 +340,7 @@ class Dataset:
         fctf = np.zeros((count, cur, X), np.float32)
         s = math.sqrt(self.sigma2 / 2)
         for i in range(count):
-            f = self.vol.ft(k2 @ R[i]).cpu()
+            f = self.vols[int(labels[i])].ft(k2 @ R[i]).cpu()
             ctf = ctf_value(float(dU[i]), float(dV[i]), float(dA[i]), x / (box * pix), y / (box * pix))
             ph = torch.exp(-2j * math.pi * (x * shifts[i, 0] + y * shifts[i, 1]) / box)
             noise = torch.complex(torch.randn(cur, X, generator=g, dtype=torch.float64),
@@ -275,4 +361,5 @@ class Dataset:
             old_offset=np.zeros((count, 2)), prior=np.zeros((count, 2)),
             highres_Xi2=np.full(count, beyond * 0.5), norm_correction=np.ones(count),
             scale=np.ones(count), true_rot=R.numpy(), true_shift=shifts.numpy(),
+            true_class=labels.numpy(),
             defocus=np.stack([dU.numpy(), dV.numpy(), dA.numpy()], 1))

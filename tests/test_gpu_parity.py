@@ -23,7 +23,7 @@ def cmp(oracle_lib):
 def _case(name, seed, n, **kw):
     from relion_gb300 import datagen
     ds = datagen.Dataset(name, seed=seed, n_particles=n, **kw)
-    return ds.model(), [ds.ref], ds.particles(0, n)
+    return ds.model(), ds.refs, ds.particles(0, n)
 
 
 def _check(st, tol):
@@ -60,3 +60,14 @@ def test_parity_box64_config(cmp):
     st = cmp.compare(m, refs, b)
     _check(st, cmp.TOL)
     assert st["nr_sign_diff"] <= 2
+
+
+def test_parity_three_classes(cmp):
+    # classification shape: K=3 class volumes (15 % of the Gaussians displaced
+    # per class), the class index packed in the hidden index, per-class
+    # pdf_direction sums and one backprojected volume per class
+    m, refs, b = _case("cfg0_box64", 23, 6, healpix_order=1, psi_step=30.0, classes=3)
+    assert len(refs) == 3
+    st = cmp.compare(m, refs, b)
+    assert st["sig_mismatch"] == 0 and st["fine_set_mismatch"] == 0
+    _check(st, cmp.TOL)
