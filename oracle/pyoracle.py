@@ -20,11 +20,12 @@ class OracleModel(C.Structure):
         "proj_r_max", "proj_xdim", "proj_ydim", "proj_zdim", "proj_yinit", "proj_zinit",
         "bp_r_max", "bp_xdim", "bp_ydim", "bp_zdim", "bp_yinit", "bp_zinit",
         "healpix_order", "adaptive_oversampling", "maximum_significants", "sigma2_len",
-        "do_scale_correction", "do_norm_correction", "do_map", "pad_int_")] + \
+        "do_scale_correction", "do_norm_correction", "do_map", "ref_dim")] + \
         [(n, F64) for n in ("pixel_size", "psi_step", "offset_range", "offset_step",
                             "adaptive_fraction", "sigma2_fudge", "sigma2_offset",
                             "avg_norm_correction")] + \
-        [(n, P) for n in ("ppref", "sigma2_noise", "pdf_class", "pdf_direction", "data_vs_prior")]
+        [(n, P) for n in ("ppref", "sigma2_noise", "pdf_class", "pdf_direction", "data_vs_prior",
+                          "prior_offset_class")]
 
 
 class OracleParticle(C.Structure):
@@ -51,7 +52,8 @@ class OracleWsum(C.Structure):
                                  "bp_weight")] + \
         [(n, F64) for n in ("sigma2_offset", "sumw_group", "LL", "ave_Pmax",
                             "avg_norm_correction", "wsum_signal_product",
-                            "wsum_reference_power", "pad_")]
+                            "wsum_reference_power", "pad_")] + \
+        [("prior_offset_class", P)]
 
 
 _O = None
@@ -90,11 +92,16 @@ def load_ref():
     return _R
 
 
-def sampling_sizes(order, psi_step, offset_range, offset_step):
+def sampling_sizes(order, psi_step, offset_range, offset_step, ref_dim=3):
+    """(ndir, npsi, ntrans); 2D (ref_dim 2): one direction, psi step 10 by default."""
     o = load()
     v = [I64() for _ in range(3)]
+    if ref_dim == 2 and psi_step <= 0:
+        psi_step = 10.0
     o.oracle_sampling_sizes(I64(order), F64(psi_step), F64(offset_range), F64(offset_step),
                             *[C.byref(x) for x in v])
+    if ref_dim == 2:
+        v[0].value = 1
     return [x.value for x in v]
 
 
@@ -110,9 +117,13 @@ def directions(order):
     return rot, tilt, ipix
 
 
-def bp_geometry(current_size, ori_size, pad=2):
+def bp_geometry(current_size, ori_size, pad=2, ref_dim=3):
+    """BackProjector::initialiseDataAndWeight sizes (3D volume, or one 2D plane)."""
     r_max = min(current_size // 2, ori_size // 2)
     pad_size = 2 * (int(pad * r_max + 0.5) + 1) + 1
+    if ref_dim == 2:
+        return dict(r_max=r_max, xdim=pad_size // 2 + 1, ydim=pad_size, zdim=1,
+                    yinit=-(pad_size // 2), zinit=0)
     return dict(r_max=r_max, xdim=pad_size // 2 + 1, ydim=pad_size, zdim=pad_size,
                 yinit=-(pad_size // 2), zinit=-(pad_size // 2))
 
@@ -136,7 +147,8 @@ def run(model, refs, batch, debug=False):
 
     r0 = refs[0]
     ppref = np.stack([np.asarray(r["data"], np.complex128) for r in refs])
-    bg = bp_geometry(int(model["current_size"]), int(model["ori_size"]), int(model["padding_factor"]))
+    ref_dim = int(model.get("ref_dim", 3) or 3)
+    bg = bp_geometry(int(model["current_size"]), int(model["ori_size"]), int(model["padding_factor"]), ref_dim)
     m = OracleModel()
     for k in ("ori_size", "nr_classes", "current_size", "coarse_size", "padding_factor",
               "healpix_order", "adaptive_oversampling", "maximum_significants", "sigma2_len",
@@ -154,6 +166,9 @@ def run(model, refs, batch, debug=False):
     m.pdf_class = arr(model["pdf_class"])
     m.pdf_direction = arr(model["pdf_direction"])
     m.data_vs_prior = arr(model["data_vs_prior"]) if model.get("data_vs_prior") is not None else None
+    m.ref_dim = ref_dim
+    poc = model.get("prior_offset_class")
+    m.prior_offset_class = arr(np.zeros((K, 2)) if poc is None else poc)
 
     n = int(batch["n"])
     parts = (OracleParticle * n)()
@@ -176,7 +191,7 @@ def run(model, refs, batch, debug=False):
         p.scale = float(batch["scale"][i])
     res = (OracleResult * n)()
     ndir, npsi, ntr = sampling_sizes(int(model["healpix_order"]), float(model["psi_step"]),
-                                     float(model["offset_range"]), float(model["offset_step"]))
+                                     float(model["offset_range"]), float(model["offset_step"]), ref_dim)
     RT = K * ndir * npsi * ntr
     nfine = RT * 32
     dbg = None
@@ -194,9 +209,10 @@ def run(model, refs, batch, debug=False):
     vox = bg["xdim"] * bg["ydim"] * bg["zdim"]
     ws = dict(sigma2_noise=np.zeros(half), pdf_class=np.zeros(K), pdf_direction=np.zeros(K * ndir),
               bp_data=np.zeros((K, bg["zdim"], bg["ydim"], bg["xdim"]), np.complex128),
-              bp_weight=np.zeros((K, bg["zdim"], bg["ydim"], bg["xdim"])))
+              bp_weight=np.zeros((K, bg["zdim"], bg["ydim"], bg["xdim"])),
+              prior_offset_class=np.zeros((K, 2)))
     w = OracleWsum()
-    for k in ("sigma2_noise", "pdf_class", "pdf_direction", "bp_data", "bp_weight"):
+    for k in ("sigma2_noise", "pdf_class", "pdf_direction", "bp_data", "bp_weight", "prior_offset_class"):
         setattr(w, k, ws[k].ctypes.data)
     st = o.oracle_expectation(C.byref(m), I64(n), parts, res, dbg, C.byref(w))
     if st != 0:
@@ -209,6 +225,7 @@ def run(model, refs, batch, debug=False):
                                        "avg_norm_correction", "wsum_signal_product",
                                        "wsum_reference_power")}
     wsum.update(sigma2_noise=ws["sigma2_noise"], pdf_class=ws["pdf_class"],
-                pdf_direction=ws["pdf_direction"].reshape(K, ndir))
+                pdf_direction=ws["pdf_direction"].reshape(K, ndir),
+                prior_offset_class=ws["prior_offset_class"])
     del keep, vox
     return out, dbg_arrays, wsum, ws["bp_data"], ws["bp_weight"]

@@ -122,9 +122,10 @@ void direction_from_pix(const Hpx &h, int ipix, double &rot, double &tilt) {
 }
 
 // ---------------------------------------------------------------------------
-// Sampling grid (HealpixSampling), C1 3D case.
+// Sampling grid (HealpixSampling): C1 3D case, and the 2D (in-plane) case.
 // ---------------------------------------------------------------------------
 struct Sampling {
+    bool is3d;
     int order;
     double psi_step;  // after rounding to 360/nr_psi (src/healpix_sampling.cpp:548-551)
     double offset_step, offset_range;  // Angstrom
@@ -132,19 +133,27 @@ struct Sampling {
     std::vector<int> ipix;
     std::vector<double> psi;
     std::vector<double> tx, ty;  // Angstrom
-    Sampling(int order_, double psi_step_in, double range, double step) {
+    Sampling(int order_, double psi_step_in, double range, double step, bool is3d_ = true) {
+        is3d = is3d_;
         order = order_;
-        // default 3D psi step: src/healpix_sampling.cpp:71-76
+        // default psi step: src/healpix_sampling.cpp:71-76 (3D: HEALPix spacing; 2D: 10 degrees)
         double ps = psi_step_in;
-        if (ps <= 0) ps = 360. / (6 * r_round(std::pow(2., order)));
-        Hpx h(order);
-        // src/healpix_sampling.cpp:493-505 (C1: no symmetry-equivalent removal)
-        for (int p = 0; p < h.npix; ++p) {
-            double r, t;
-            direction_from_pix(h, p, r, t);
-            rot.push_back(r);
-            tilt.push_back(t);
-            ipix.push_back(p);
+        if (ps <= 0) ps = is3d ? 360. / (6 * r_round(std::pow(2., order))) : 10.;
+        if (is3d) {
+            Hpx h(order);
+            // src/healpix_sampling.cpp:493-505 (C1: no symmetry-equivalent removal)
+            for (int p = 0; p < h.npix; ++p) {
+                double r, t;
+                direction_from_pix(h, p, r, t);
+                rot.push_back(r);
+                tilt.push_back(t);
+                ipix.push_back(p);
+            }
+        } else {
+            // src/healpix_sampling.cpp:531-536: one direction, rot = tilt = 0
+            rot.push_back(0.);
+            tilt.push_back(0.);
+            ipix.push_back(-1);
         }
         // src/healpix_sampling.cpp:544-555
         int nr_psi = r_ceil(360. / ps);
@@ -170,7 +179,7 @@ struct Sampling {
     long npsi() const { return (long)psi.size(); }
     long ntrans() const { return (long)tx.size(); }
     // src/healpix_sampling.cpp:1644-1659
-    static int over_rot(int ov) { return r_round(std::pow(2., ov * 3)); }
+    int over_rot(int ov) const { return r_round(std::pow(2., ov * (is3d ? 3 : 1))); }
     static int over_trans(int ov) { return r_round(std::pow(2., ov * 2)); }
 
     // src/healpix_sampling.cpp:1832-1967 (no priors, no perturbation)
@@ -181,6 +190,18 @@ struct Sampling {
             r.push_back(rot[idir]);
             t.push_back(tilt[idir]);
             p.push_back(psi[ipsi]);
+            return;
+        }
+        if (!is3d) {
+            // src/healpix_sampling.cpp:1873-1877, 1951-1966: psi only, wrapped above 180
+            int nr_ipsi_over = r_round(std::pow(2., ov));
+            for (int k = 0; k < nr_ipsi_over; ++k) {
+                double overpsi = psi[ipsi] - 0.5 * psi_step + (0.5 + k) * psi_step / nr_ipsi_over;
+                if (overpsi > 180.) overpsi -= 360.;
+                r.push_back(0.);
+                t.push_back(0.);
+                p.push_back(overpsi);
+            }
             return;
         }
         Hpx base(order), over(order + ov);
@@ -248,6 +269,11 @@ struct Cplx {
     double re, im;
 };
 
+// mymodel.prior_offset_class[iclass] (2D classification), zero when not given
+double class_prior(const oracle_model &m, long iclass, int axis) {
+    return m.prior_offset_class ? m.prior_offset_class[iclass * 2 + axis] : 0.;
+}
+
 // Fourier-slice projection: src/projector.cpp:630-733 (TRILINEAR branch).
 // The inverse of the rotation is taken as its transpose (A.inv() in the
 // reference; the two agree to rounding).  `out` is zero-filled first: points
@@ -273,6 +299,33 @@ void project(const oracle_model &m, long iclass, const double A[9], long size, C
             double xp = Ai[0] * x + Ai[1] * y;
             double yp = Ai[3] * x + Ai[4] * y;
             double zp = Ai[6] * x + Ai[7] * y;
+            if (m.ref_dim == 2) {
+                // Projector::rotate2D (src/projector.cpp:1010-1100): bilinear
+                // interpolation in the padded 2D reference (one z plane); the
+                // radius test (:1055-1057) is made in integers as below
+                if ((long)m.padding_factor * m.padding_factor * (x * x + y2) > r_max_ref_2) continue;
+                const bool neg2 = xp < 0;
+                if (neg2) {
+                    xp = -xp;
+                    yp = -yp;
+                }
+                const int x0 = r_floor(xp);
+                const double fx = xp - x0;
+                int y0 = r_floor(yp);
+                const double fy = yp - y0;
+                y0 -= (int)m.proj_yinit;
+                if (x0 < 0 || x0 + 1 >= xd || y0 < 0 || y0 + 1 >= yd) continue;
+                auto at2 = [&](int yy, int xx) { return vol[(size_t)yy * xd + xx]; };
+                auto lerp2 = [](double a, Cplx l, Cplx h) {  // LIN_INTERP, src/macros.h:373
+                    return Cplx{l.re + (h.re - l.re) * a, l.im + (h.im - l.im) * a};
+                };
+                Cplx dx0 = lerp2(fx, at2(y0, x0), at2(y0, x0 + 1));
+                Cplx dx1 = lerp2(fx, at2(y0 + 1, x0), at2(y0 + 1, x0 + 1));
+                Cplx v = lerp2(fy, dx0, dx1);
+                if (neg2) v.im = -v.im;
+                out[i * X + x] = v;
+                continue;
+            }
             // r_ref_2 > r_max_ref_2 in the reference (:672).  For a rotation
             // |Ainv (x,y,0)|^2 = pad^2 (x^2+y^2) exactly; the test is made in
             // integers so that pixels on the circle itself are decided
@@ -361,6 +414,22 @@ void backproject(const oracle_model &m, long iclass, const double A[9], long siz
             double fy = yp - y0;
             y0 -= (int)m.bp_yinit;
             int y1 = y0 + 1;
+            if (m.ref_dim == 2) {
+                // BackProjector::backrotate2D (src/backprojector.cpp:471-660):
+                // bilinear insertion into the 2D data / weight planes
+                if (x0 < 0 || x0 + 1 >= xd || y0 < 0 || y0 + 1 >= yd) continue;
+                const double mx = 1. - fx, my = 1. - fy;
+                const double d4[4] = {my * mx, my * fx, fy * mx, fy * fx};
+                if (neg) val.im = -val.im;
+                const int ys4[4] = {y0, y0, y1, y1}, xs4[4] = {x0, x1, x0, x1};
+                for (int c = 0; c < 4; ++c) {
+                    size_t idx = (size_t)ys4[c] * xd + xs4[c];
+                    data[idx].re += d4[c] * val.re;
+                    data[idx].im += d4[c] * val.im;
+                    weight[idx] += d4[c] * w;
+                }
+                continue;
+            }
             int z0 = r_floor(zp);
             double fz = zp - z0;
             z0 -= (int)m.bp_zinit;
@@ -571,10 +640,11 @@ void oracle_project(const oracle_model *m, int64_t iclass, const double *A, int6
 int oracle_expectation(const oracle_model *mp, int64_t n, const oracle_particle *parts,
                        oracle_result *res, oracle_debug *dbg, oracle_wsum *wsum) {
     const oracle_model &m = *mp;
-    Sampling S((int)m.healpix_order, m.psi_step, m.offset_range, m.offset_step);
+    const bool is2d = m.ref_dim == 2;
+    Sampling S((int)m.healpix_order, m.psi_step, m.offset_range, m.offset_step, !is2d);
     const long K = m.nr_classes, ND = S.ndir(), NP = S.npsi(), NT = S.ntrans();
     const int ov = (int)m.adaptive_oversampling;
-    const long nOR = Sampling::over_rot(ov), nOT = Sampling::over_trans(ov);
+    const long nOR = S.over_rot(ov), nOT = Sampling::over_trans(ov);
     const long R = K * ND * NP;
     const long cur = m.current_size, crs = m.coarse_size;
     const long Xf = cur / 2 + 1;
@@ -680,8 +750,11 @@ int oracle_expectation(const oracle_model *mp, int64_t n, const oracle_particle 
             double offset_norm = 2. * kPI * std::sqrt(s2x) * std::sqrt(s2y);
             double pdf_orient_mean = 0, pdf_offset_mean = 0;
             unsigned long orient_count = 0, offset_count = 0;
-            std::vector<double> tdiff2s(NT);
+            // 2D: the offset prior is the class's (mymodel.prior_offset_class, :7829-7833)
+            std::vector<double> tdiff2s((size_t)K * NT);
             for (long ic = 0; ic < K; ++ic) {
+                const double prx = is2d ? class_prior(m, ic, 0) : P.prior[0];
+                const double pry = is2d ? class_prior(m, ic, 1) : P.prior[1];
                 for (long id = 0; id < ND; ++id)
                     for (long is = 0; is < NP; ++is) {
                         pdf_orient_mean += m.pdf_direction[ic * ND + id];
@@ -691,10 +764,10 @@ int oracle_expectation(const oracle_model *mp, int64_t n, const oracle_particle 
                     double ox = P.old_offset[0] + S.tx[it];
                     double oy = P.old_offset[1] + S.ty[it];
                     double td = 0.;
-                    td += (ox - P.prior[0]) * (ox - P.prior[0]) / (-2. * s2x);
-                    td += (oy - P.prior[1]) * (oy - P.prior[1]) / (-2. * s2y);
+                    td += (ox - prx) * (ox - prx) / (-2. * s2x);
+                    td += (oy - pry) * (oy - pry) / (-2. * s2y);
                     td *= pix * pix;
-                    tdiff2s[it] = td;
+                    tdiff2s[ic * NT + it] = td;
                     if (s2x < 0.0001) pdf_offset_mean += (td > 0.) ? 0. : 1.;
                     else pdf_offset_mean += std::exp(td) / offset_norm;
                     offset_count++;
@@ -710,7 +783,7 @@ int oracle_expectation(const oracle_model *mp, int64_t n, const oracle_particle 
                         double pdf_orient = m.pdf_direction[ic * ND + id];
                         if (pdf_orient_mean != 0.) pdf_orient /= pdf_orient_mean;
                         for (long it = 0; it < NT; ++it) {
-                            double td = tdiff2s[it];
+                            double td = tdiff2s[ic * NT + it];
                             double pdf_offset;
                             if (s2x < 0.0001) pdf_offset = (td > 0.) ? 0. : 1.;
                             else pdf_offset = std::exp(td) / offset_norm;
@@ -795,7 +868,7 @@ int oracle_expectation(const oracle_model *mp, int64_t n, const oracle_particle 
         }
         std::vector<double> thr_sigma2(nhalf, 0.);
         double norm_corr = 0., XA = 0., AA = 0., sumw_group = 0., sigma2_off = 0.;
-        std::vector<double> thr_pdf_class(K, 0.), thr_pdf_dir(K * ND, 0.);
+        std::vector<double> thr_pdf_class(K, 0.), thr_pdf_dir(K * ND, 0.), thr_prior_off(2 * K, 0.);
         double max_weight = -1.;
         std::vector<Cplx> Fref(npix), Frefctf(npix), Fimg(npix);
         std::vector<double> Mctf(npix), Fweight(npix);
@@ -851,10 +924,17 @@ int oracle_expectation(const oracle_model *mp, int64_t n, const oracle_particle 
                                 }
                                 sumw_group += w;
                                 thr_pdf_class[ic] += w;
-                                double dx = P.prior[0] - P.old_offset[0] - otx[it][io];
-                                double dy = P.prior[1] - P.old_offset[1] - oty[it][io];
+                                // 2D: class offset prior and its weighted sum (:8449-8456, :8668-8672)
+                                const double prx = is2d ? class_prior(m, ic, 0) : P.prior[0];
+                                const double pry = is2d ? class_prior(m, ic, 1) : P.prior[1];
+                                double dx = prx - P.old_offset[0] - otx[it][io];
+                                double dy = pry - P.old_offset[1] - oty[it][io];
                                 sigma2_off += w * pix * pix * dx * dx;
                                 sigma2_off += w * pix * pix * dy * dy;
+                                if (is2d) {
+                                    thr_prior_off[ic * 2 + 0] += w * pix * (P.old_offset[0] + otx[it][io]);
+                                    thr_prior_off[ic * 2 + 1] += w * pix * (P.old_offset[1] + oty[it][io]);
+                                }
                                 thr_pdf_dir[ic * ND + id] += w;
                                 for (long k = 0; k < npix; ++k) {
                                     double wis = w * Mctf[k] * Minv[k];
@@ -913,6 +993,8 @@ int oracle_expectation(const oracle_model *mp, int64_t n, const oracle_particle 
             for (long ic = 0; ic < K; ++ic) wsum->pdf_class[ic] += thr_pdf_class[ic];
             for (long i = 0; i < K * ND; ++i) wsum->pdf_direction[i] += thr_pdf_dir[i];
             wsum->sigma2_offset += sigma2_off;
+            if (is2d && wsum->prior_offset_class)
+                for (long i = 0; i < 2 * K; ++i) wsum->prior_offset_class[i] += thr_prior_off[i];
             if (m.do_norm_correction) wsum->avg_norm_correction += normcorr;
             wsum->LL += dLL;
             wsum->ave_Pmax += res[ip].pmax;

@@ -44,7 +44,7 @@ typedef struct {
     int64_t do_scale_correction;
     int64_t do_norm_correction;
     int64_t do_map;
-    int64_t pad_int_;
+    int64_t ref_dim;             /* mymodel.ref_dim: 3 (or 0) 3D, 2 = 2D classes  */
     double pixel_size;           /* mymodel.pixel_size == particle pixel size     */
     double psi_step;             /* degrees (<=0: 360/(6*2^order))                */
     double offset_range;         /* Angstrom (command line px * pixel size)       */
@@ -58,6 +58,7 @@ typedef struct {
     const double *pdf_class;     /* [K]                                            */
     const double *pdf_direction; /* [K][ndir]                                      */
     const double *data_vs_prior; /* [K][ori/2+1] (scale correction only)           */
+    const double *prior_offset_class; /* [K][2] 2D: mymodel.prior_offset_class (or NULL) */
 } oracle_model;
 
 typedef struct {
@@ -104,6 +105,7 @@ typedef struct {
     double sigma2_offset, sumw_group, LL, ave_Pmax, avg_norm_correction;
     double wsum_signal_product, wsum_reference_power;
     double pad_;
+    double *prior_offset_class;  /* [K][2] 2D: += weight * pixel * (old offset + shift) */
 } oracle_wsum;
 
 int oracle_expectation(const oracle_model *m, int64_t n, const oracle_particle *parts,

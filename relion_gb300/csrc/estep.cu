@@ -618,6 +618,7 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
     GBR_CUDA(cudaEventRecord(w->ev[1], st));
     // ---- coarse norm and cross GEMMs ----
     GBR_CUDA(launch_gemm_rows(b->proj2_c.p, b->ldk_c, R, w->a_c.p, b->ldk_c, n, b->ldk_c, w->nrm.p, R, 1, st));
+    w->launches += 3;  // prep, pdf_offset, norms
     GBR_CUDA(cudaEventRecord(w->ev[2], st));
     const bool use_rowmin = d.precision == GBR_PREC_BF16 && T >= 32 && w->coarse_rows == 0;
     if (use_rowmin) {
@@ -629,10 +630,11 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
         GBR_CUDA(launch_tc_diff2(b->proj_c_tc.p, w->ytc.p, R, 2 * b->nc, w->b_c.p, b->ldk_c, b->phase_c.p, b->ldk_c, n,
                                  T, w->vals.p, w->nrm.p, b->pdf_orient.p, w->ps.p,
                                  use_rowmin ? w->rowmin.p : nullptr, st));
-        w->launches += 1;
+        w->launches += 2;  // operand packing + tensor-core kernel
     } else {
         GBR_CUDA(launch_gemm_diff2(b->proj_c.p, b->lda_c, R, 2 * b->nc, w->b_c.p, b->ldk_c, b->phase_c.p, b->ldk_c,
                                    n, T, w->vals.p, w->nrm.p, b->pdf_orient.p, nullptr, 1, 1, W, w->ps.p, 0, st));
+        w->launches += 1;
     }
     GBR_CUDA(cudaEventRecord(w->ev[3], st));
     if (w->debug) {
@@ -1019,6 +1021,7 @@ int gbr_expect_batch(gbr_worker *w, const gbr_particle_batch *batch, gbr_particl
             // per-particle finalisation) arrive before the batch's last sync
             GBR_CUDA(launch_gather_pdat(batch->old_offset + 2 * p0, batch->prior + 2 * p0, batch->highres_Xi2 + p0,
                                         batch->norm_correction + p0, batch->scale + p0, n, w->pdat.p, w->st));
+            w->launches += 1;
             GBR_CUDA(cudaMemcpyAsync(pdat, w->pdat.p, sizeof(double) * n * 8, cudaMemcpyDeviceToHost, w->st));
             GBR_CUDA(cudaMemcpyAsync(power, batch->power_img + (size_t)b->nshell * p0, sizeof(double) * b->nshell * n,
                                      cudaMemcpyDeviceToHost, w->st));

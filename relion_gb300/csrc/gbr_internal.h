@@ -29,6 +29,7 @@ struct PixelRef {
 // Padded Fourier volume geometry (Projector::data, src/projector.cpp:59-90).
 struct VolGeom {
     int xdim, ydim, zdim, yinit, zinit, r_max, pad;
+    int dim = 3;  // 3: padded 3D volume; 2: one padded 2D plane (2D classification)
 };
 
 // Per-particle state on the device (one per particle of the batch).

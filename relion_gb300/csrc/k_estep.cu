@@ -1030,6 +1030,32 @@ __global__ void k_backproject(const int *__restrict__ list, const float *__restr
         if (g.pad * g.pad * (pr.x * pr.x + pr.y * pr.y) > max_r2) continue;
         float xp = fmaf(Ai[0], (float)pr.x, Ai[1] * (float)pr.y);
         float yp = fmaf(Ai[3], (float)pr.x, Ai[4] * (float)pr.y);
+        if (g.dim == 2) {
+            // BackProjector::backrotate2D (src/backprojector.cpp:471-660):
+            // bilinear insertion into the 2D data / weight planes
+            float2 v2 = val0;
+            if (xp < 0.f) {
+                xp = -xp;
+                yp = -yp;
+                v2.y = -v2.y;
+            }
+            const float fx0 = floorf(xp), fy0 = floorf(yp);
+            const float fx = xp - fx0, fy = yp - fy0;
+            const int x0 = (int)fx0, y0 = (int)fy0 - g.yinit;
+            if (x0 < 0 || x0 + 1 >= g.xdim || y0 < 0 || y0 + 1 >= g.ydim) continue;
+            const float mfx = 1.f - fx, mfy = 1.f - fy;
+            const float d4[4] = {mfy * mfx, mfy * fx, fy * mfx, fy * fx};
+            const size_t base = (size_t)y0 * g.xdim + x0;
+            const size_t off4[4] = {0, 1, (size_t)g.xdim, (size_t)g.xdim + 1};
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const double dc = (double)d4[c];
+                atomicAdd(&dv[base + off4[c]].x, dc * v2.x);
+                atomicAdd(&dv[base + off4[c]].y, dc * v2.y);
+                atomicAdd(&wv[base + off4[c]], dc * w);
+            }
+            continue;
+        }
         float zp = fmaf(Ai[6], (float)pr.x, Ai[7] * (float)pr.y);
         float2 val = val0;
         if (xp < 0.f) {

@@ -1,5 +1,6 @@
-// k_project.cu -- Fourier-slice projection of the padded 3D reference and
-// the translation phase tables.
+// k_project.cu -- Fourier-slice projection of the padded 3D reference (or
+// in-plane rotation of a padded 2D class reference) and the translation
+// phase tables.
 //
 // Projection follows Projector::project (src/projector.cpp:630-733): the
 // 2D frequency (x, y) is rotated by pad * A^-1 into the half volume, mirrored
@@ -28,6 +29,25 @@ __device__ __forceinline__ float2 sample_slice(const float2 *__restrict__ vol, c
     if (g.pad * g.pad * (x * x + y * y) > rref * rref) return make_float2(0.f, 0.f);
     float xp = fmaf(Ai[0], (float)x, Ai[1] * (float)y);
     float yp = fmaf(Ai[3], (float)x, Ai[4] * (float)y);
+    if (g.dim == 2) {
+        // Projector::rotate2D (src/projector.cpp:1010-1100): bilinear in the
+        // padded 2D reference, Friedel mate for negative x
+        const bool neg2 = xp < 0.f;
+        if (neg2) {
+            xp = -xp;
+            yp = -yp;
+        }
+        const float fx0 = floorf(xp), fy0 = floorf(yp);
+        const float fx = xp - fx0, fy = yp - fy0;
+        const int x0 = (int)fx0, y0 = (int)fy0 - g.yinit;
+        if (x0 < 0 || x0 + 1 >= g.xdim || y0 < 0 || y0 + 1 >= g.ydim) return make_float2(0.f, 0.f);
+        const float2 *b = vol + (size_t)y0 * g.xdim + x0;
+        const float2 d00 = __ldg(b), d01 = __ldg(b + 1);
+        const float2 d10 = __ldg(b + g.xdim), d11 = __ldg(b + g.xdim + 1);
+        float2 v = lerp2(fy, lerp2(fx, d00, d01), lerp2(fx, d10, d11));
+        if (neg2) v.y = -v.y;
+        return v;
+    }
     float zp = fmaf(Ai[6], (float)x, Ai[7] * (float)y);
     const bool neg = xp < 0.f;
     if (neg) {

@@ -121,6 +121,7 @@ inline void euler_to_matrix(double rot, double tilt, double psi, double A[9]) {
 }
 
 struct PoseGrid {
+    bool is3d = true;  // false: 2D classification (in-plane psi only)
     int order = 0, oversampling = 0;
     double psi_step = 0, offset_range = 0, offset_step = 0;  // degrees, Angstrom
     std::vector<double> dir_rot, dir_tilt;
@@ -131,22 +132,34 @@ struct PoseGrid {
     long ndir() const { return (long)dir_rot.size(); }
     long npsi() const { return (long)psi.size(); }
     long ntrans() const { return (long)trans_x.size(); }
-    int nover_rot() const { return iround(std::pow(2., oversampling * 3)); }
+    int nover_rot() const { return iround(std::pow(2., oversampling * (is3d ? 3 : 1))); }
     int nover_trans() const { return iround(std::pow(2., oversampling * 2)); }
 
-    void build(int order_, double psi_step_in, double range, double step, int ov) {
+    // HealpixSampling::initialise / setOrientations / setTranslations
+    // (src/healpix_sampling.cpp:55-120, 477-560, 291-440): in 3D every HEALPix
+    // pixel (C1) x psi; in 2D one direction (rot = tilt = 0) x psi, psi step 10
+    // degrees by default.
+    void build(int order_, double psi_step_in, double range, double step, int ov, bool three_d = true) {
+        is3d = three_d;
         order = order_;
         oversampling = ov;
-        const HealpixNest h(order);
         dir_rot.clear(); dir_tilt.clear(); dir_pix.clear(); psi.clear(); trans_x.clear(); trans_y.clear();
-        for (int p = 0; p < h.npix(); ++p) {  // C1: every pixel is kept
-            double r, t;
-            healpix_angles(h, p, r, t);
-            dir_rot.push_back(r);
-            dir_tilt.push_back(t);
-            dir_pix.push_back(p);
+        if (is3d) {
+            const HealpixNest h(order);
+            for (int p = 0; p < h.npix(); ++p) {  // C1: every pixel is kept
+                double r, t;
+                healpix_angles(h, p, r, t);
+                dir_rot.push_back(r);
+                dir_tilt.push_back(t);
+                dir_pix.push_back(p);
+            }
+        } else {
+            dir_rot.push_back(0.);
+            dir_tilt.push_back(0.);
+            dir_pix.push_back(-1);
         }
-        double ps = psi_step_in > 0 ? psi_step_in : 360. / (6 * iround(std::pow(2., order)));
+        double ps = psi_step_in > 0 ? psi_step_in
+                                    : (is3d ? 360. / (6 * iround(std::pow(2., order))) : 10.);
         const int nr_psi = iceil(360. / ps);
         psi_step = 360. / (double)nr_psi;
         for (int i = 0; i < nr_psi; ++i) psi.push_back(i * psi_step);
@@ -166,6 +179,19 @@ struct PoseGrid {
     // Oversampled orientations of coarse (idir, ipsi): nover_rot() entries in
     // the reference's order (child pixel j-major, i-minor, then child psi).
     void fine_orientations(long idir, long ipsi, double *rot, double *tilt, double *ps) const {
+        if (!is3d) {
+            // 2D: only the in-plane angle is oversampled, wrapped to (-180, 180]
+            // (pushbackOversampledPsiAngles, src/healpix_sampling.cpp:1941-1968)
+            const int n = iround(std::pow(2., oversampling));
+            for (int k = 0; k < n; ++k) {
+                double o = psi[ipsi] - 0.5 * psi_step + (0.5 + k) * psi_step / n;
+                if (o > 180.) o -= 360.;
+                rot[k] = 0.;
+                tilt[k] = 0.;
+                ps[k] = o;
+            }
+            return;
+        }
         const HealpixNest base(order), fine(order + oversampling);
         const int fact = fine.nside() / base.nside();
         int x, y, face;
