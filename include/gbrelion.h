@@ -60,7 +60,8 @@ typedef struct {
     int64_t do_norm_correction;  /* --norm                                   */
     int64_t do_map;              /* !--no_map                                */
     int64_t precision;           /* gbr_precision                            */
-    int64_t reserved_;
+    int64_t ref_dim;             /* mymodel.ref_dim: 3 (or 0) 3D refinement /
+                                    classification, 2 = 2D classification    */
     double pixel_size;           /* Angstrom per pixel                       */
     double psi_step;             /* degrees; <= 0: 360/(6*2^order)           */
     double offset_range;         /* Angstrom                                 */
@@ -143,6 +144,12 @@ int gbr_projector_upload(gbr_bundle *b, int64_t iclass, const float *data, int64
 int gbr_model_set_arrays(gbr_bundle *b, const double *sigma2_noise, const double *pdf_class,
                          const double *pdf_direction, const double *data_vs_prior);
 
+/* 2D classification (ref_dim 2): mymodel.prior_offset_class [K][2], the
+ * per-class offset prior that replaces the particle's prior in pdf_offset
+ * and sigma2_offset (src/ml_optimiser.cpp:7829-7833, 8449-8456).  Zero until
+ * set; rejected for 3D models. */
+int gbr_model_set_class_offsets(gbr_bundle *b, const double *prior_offset_class);
+
 /* setupTunableSizedObjects(allocationSize) (cuda_ml_optimiser.cu:154-226):
  * cap the device memory the bundle and its workers may use. */
 int gbr_bundle_reserve(gbr_bundle *b, size_t bytes);
@@ -184,6 +191,10 @@ int gbr_backprojector_download(gbr_bundle *b, int64_t iclass, double *data, doub
 
 /* Weighted sums accumulated since the last reset (added into `out`). */
 int gbr_wsum_download(gbr_bundle *b, gbr_wsum *out);
+/* 2D classification: wsum_model.prior_offset_class [K][2] accumulated since
+ * the last reset, sum of weight * pixel * (old offset + translation)
+ * (src/ml_optimiser.cpp:8668-8672, 9122-9126); added into `out`. */
+int gbr_wsum_download_class_offsets(gbr_bundle *b, double *out);
 /* Zero the volumes and weighted sums (start of a new iteration). */
 int gbr_bundle_reset_wsum(gbr_bundle *b);
 

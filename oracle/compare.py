@@ -31,6 +31,8 @@ def run_gpu(model, refs, batch, device=0):
                         fine_idx=w.debug_fetch(2, i), fine_diff2=w.debug_fetch(3, i),
                         fine_weight=w.debug_fetch(4, i)))
     ws = b.get_wsum()
+    if int(model.get("ref_dim", 3) or 3) == 2:
+        ws["prior_offset_class"] = b.get_class_offsets()
     vols = [b.get_mdl_data(k) for k in range(len(refs))]
     times = w.stage_times()
     w.close()
@@ -85,6 +87,9 @@ def compare(model, refs, batch, device=0):
     st["sumw_group_rel"] = abs(gws["sumw_group"] - ows["sumw_group"]) / ows["sumw_group"]
     st["sigma2_offset_rel"] = abs(gws["sigma2_offset"] - ows["sigma2_offset"]) / max(ows["sigma2_offset"], 1e-30)
     st["LL_abs"] = abs(gws["LL"] - ows["LL"])
+    if "prior_offset_class" in gws:
+        o_p, g_p = ows["prior_offset_class"], gws["prior_offset_class"]
+        st["prior_offset_class_rel"] = float(np.linalg.norm(g_p - o_p) / max(np.linalg.norm(o_p), 1e-30))
     bp_d = bp_w = 0.0
     for k, (gd, gw) in enumerate(gvols):
         bp_d = max(bp_d, float(np.linalg.norm(gd - obpd[k]) / np.linalg.norm(obpd[k])))

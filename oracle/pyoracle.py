@@ -193,7 +193,8 @@ def run(model, refs, batch, debug=False):
     ndir, npsi, ntr = sampling_sizes(int(model["healpix_order"]), float(model["psi_step"]),
                                      float(model["offset_range"]), float(model["offset_step"]), ref_dim)
     RT = K * ndir * npsi * ntr
-    nfine = RT * 32
+    ov = int(model["adaptive_oversampling"])
+    nfine = RT * (2 ** ov if ref_dim == 2 else 8 ** ov) * 4 ** ov
     dbg = None
     dbg_arrays = []
     if debug:

@@ -29,7 +29,7 @@ class ModelDesc(C.Structure):
     _fields_ = [(n, I64) for n in (
         "ori_size", "nr_classes", "current_size", "coarse_size", "padding_factor",
         "healpix_order", "adaptive_oversampling", "maximum_significants", "sigma2_len",
-        "do_scale_correction", "do_norm_correction", "do_map", "precision", "reserved_")] + \
+        "do_scale_correction", "do_norm_correction", "do_map", "precision", "ref_dim")] + \
         [(n, F64) for n in (
             "pixel_size", "psi_step", "offset_range", "offset_step", "adaptive_fraction",
             "sigma2_fudge", "sigma2_offset", "avg_norm_correction")]
@@ -62,6 +62,7 @@ EXPORTS = {
     "gbr_bundle_create": (C.c_int, [C.POINTER(ModelDesc), C.c_int, C.POINTER(P)]),
     "gbr_projector_upload": (C.c_int, [P, I64, P, I64, I64, I64, I64, I64, I64, I64]),
     "gbr_model_set_arrays": (C.c_int, [P, P, P, P, P]),
+    "gbr_model_set_class_offsets": (C.c_int, [P, P]),
     "gbr_bundle_reserve": (C.c_int, [P, C.c_size_t]),
     "gbr_worker_create": (C.c_int, [P, C.POINTER(P)]),
     "gbr_worker_set_debug": (C.c_int, [P, C.c_int]),
@@ -71,6 +72,7 @@ EXPORTS = {
     "gbr_backprojector_dims": (C.c_int, [P] + [C.POINTER(I64)] * 6),
     "gbr_backprojector_download": (C.c_int, [P, I64, P, P]),
     "gbr_wsum_download": (C.c_int, [P, C.POINTER(Wsum)]),
+    "gbr_wsum_download_class_offsets": (C.c_int, [P, P]),
     "gbr_bundle_reset_wsum": (C.c_int, [P]),
     "gbr_worker_stage_times": (C.c_int, [P, P, I64, C.POINTER(I64)]),
     "gbr_worker_launch_count": (C.c_int, [P, C.POINTER(I64)]),

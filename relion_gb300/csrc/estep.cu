@@ -141,6 +141,11 @@ struct gbr_bundle {
     // model arrays (host copies)
     std::vector<double> sigma2, pdf_class, pdf_dir, dvp;
     bool have_arrays = false;
+    // 2D classification (ref_dim 2): per-class offset priors and their sums
+    bool is2d = false;
+    int KP = 1;  // offset-prior rows per particle: K in 2D, 1 in 3D
+    std::vector<double> class_prior_h;
+    DevBuf<double> class_prior, w_prior_off;
     // projector
     VolGeom pg{}, bg{};
     std::vector<DevBuf<float2>> vol;
@@ -429,7 +434,7 @@ int ensure_capacity(gbr_worker *w, int n) {
     GBR_CUDA(w->Xnf.reserve((size_t)n * b->nf));
     GBR_CUDA(w->Cf.reserve((size_t)n * b->nf));
     GBR_CUDA(w->ps.reserve(n));
-    GBR_CUDA(w->pdf_off.reserve((size_t)n * b->T));
+    GBR_CUDA(w->pdf_off.reserve((size_t)n * b->KP * b->T));
     GBR_CUDA(w->nrm.reserve((size_t)n * b->R));
     GBR_CUDA(w->vals.reserve((size_t)n * b->R * b->T));
     GBR_CUDA(w->seg_c.reserve(n + 1));
@@ -495,7 +500,7 @@ int fine_sparse(gbr_worker *w, int n, long long njobs, long long nfine, const st
         w->dbg_segf = segf;
     }
     GBR_CUDA(launch_weights(w->fd.p, w->seg_f.p, n, max_seg, 0, T, w->ejob.p, w->ecode.p, w->jobs.p, nOR, nOT,
-                            b->pdf_orient.p, w->pdf_off.p, w->ps.p, w->hist.p, st));
+                            b->pdf_orient.p, w->pdf_off.p, w->ps.p, w->hist.p, st, 1, b->KP, (int)(b->ND * b->NP)));
     int s = threshold_search(w, n, w->fd.p, w->seg_f.p, max_seg, 0);
     if (s) return s;
     GBR_CUDA(cudaEventRecord(w->ev[7], st));
@@ -524,6 +529,8 @@ int fine_sparse(gbr_worker *w, int n, long long njobs, long long nfine, const st
     wa.bpimg = b->bpimg.p; wa.bpw = b->bpw.p; wa.active = b->active.p;
     wa.shell = w->shell.p; wa.pacc = w->pacc.p;
     wa.pdf_dir = b->w_pdf_dir.p; wa.pdf_cls = b->w_pdf_cls.p;
+    wa.class_prior = b->is2d ? b->class_prior.p : nullptr;
+    wa.w_prior_off = b->is2d ? b->w_prior_off.p : nullptr;
     GBR_CUDA(launch_wsum(wa, st));
     w->launches += 3;
     return GBR_OK;
@@ -555,7 +562,7 @@ int fine_dense(gbr_worker *w, int n, long long &seg_len) {
         w->dbg_segf = seg;
     }
     GBR_CUDA(launch_weights(w->fd.p, w->seg_f.p, n, per, 2, T, nullptr, nullptr, nullptr, nOR, nOT,
-                            b->pdf_orient.p, w->pdf_off.p, w->ps.p, w->hist.p, st));
+                            b->pdf_orient.p, w->pdf_off.p, w->ps.p, w->hist.p, st, 1, b->KP, (int)(b->ND * b->NP)));
     int s = threshold_search(w, n, w->fd.p, w->seg_f.p, per, 0);
     if (s) return s;
     GBR_CUDA(cudaEventRecord(w->ev[7], st));
@@ -578,7 +585,8 @@ int fine_dense(gbr_worker *w, int n, long long &seg_len) {
     GBR_CUDA(cudaMemsetAsync(w->G.p, 0, sizeof(float2) * n * nf, st));
     GBR_CUDA(launch_fine_normalize(w->fd.p, n, R, nOR, nOT, T, w->ps.p, w->pdat.p, b->otx.p, b->oty.p,
                                    b->d.pixel_size, (int)b->ND, (int)b->NP, w->Wt.p, ldwt, w->Wp.p, ldwp, b->active.p,
-                                   w->pacc.p, b->w_pdf_dir.p, b->w_pdf_cls.p, st));
+                                   w->pacc.p, b->w_pdf_dir.p, b->w_pdf_cls.p,
+                                   b->is2d ? b->class_prior.p : nullptr, b->is2d ? b->w_prior_off.p : nullptr, st));
     // BP slices and weights (batch-summed), sigma2 contractions (per particle)
     GBR_CUDA(launch_make_zt(w->Cf.p, w->Xnf.p, b->minv_store.p, b->phase_f.p, w->pdat.p,
                             (int)b->d.do_scale_correction, n, TF, nf, w->Zt.p, ldz, w->CM.p, ldwt, st));
@@ -612,7 +620,7 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
                                            std::log(1e10)
                                      : INFINITY;
     GBR_CUDA(launch_pdf_offset(w->pdat.p, n, b->tx.p, b->ty.p, T, d.sigma2_offset, d.pixel_size, w->pdf_off.p,
-                               log_rt_orient, w->ps.p, st));
+                               log_rt_orient, w->ps.p, b->KP, b->is2d ? b->class_prior.p : nullptr, st));
     GBR_CUDA(cudaMemsetAsync(w->shell.p, 0, sizeof(double) * n * b->nshell, st));
     GBR_CUDA(cudaMemsetAsync(w->pacc.p, 0, sizeof(double) * n * 8, st));
     GBR_CUDA(cudaEventRecord(w->ev[1], st));
@@ -660,7 +668,7 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
     }
     GBR_CUDA(launch_weights_cand(w->vals.p, n, R, T, b->pdf_orient.p, b->pdf_orient_min, w->pdf_off.p,
                                  d.adaptive_fraction, w->ps.p, w->cand_idx.p, w->cand_w.p, w->cand_cnt.p, cap,
-                                 dense_w, use_rowmin ? w->rowmin.p : nullptr, st));
+                                 dense_w, use_rowmin ? w->rowmin.p : nullptr, b->KP, (int)(b->ND * b->NP), st));
     w->launches += 1;
     GBR_CUDA(w->h_ccnt.reserve(n));
     GBR_CUDA(w->h_totals.reserve(2));
@@ -703,7 +711,7 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
         if (cmax <= (unsigned int)cap) break;
         // a list overflowed: significance from the full weight array
         GBR_CUDA(launch_weights(w->vals.p, w->seg_c.p, n, RT, 1, T, nullptr, nullptr, nullptr, nOR, nOT,
-                                b->pdf_orient.p, w->pdf_off.p, w->ps.p, w->hist.p, st, 0));
+                                b->pdf_orient.p, w->pdf_off.p, w->ps.p, w->hist.p, st, 0, b->KP, (int)(b->ND * b->NP)));
         s = threshold_search(w, n, w->vals.p, w->seg_c.p, RT, 1);
         if (s) return s;
         GBR_CUDA(launch_sig_masks(w->vals.p, n, R, T, W, w->ps.p, w->mask.p, w->cnt.p, st));
@@ -867,6 +875,9 @@ int gbr_bundle_create(const gbr_model_desc *desc, int device, gbr_bundle **out) 
         return fail(GBR_ERR_UNSUPPORTED, "--maxsig is not implemented");
     if (d.precision != GBR_PREC_FP32 && d.precision != GBR_PREC_BF16)
         return fail(GBR_ERR_INVALID, "unknown precision");
+    if (d.ref_dim != 0 && d.ref_dim != 2 && d.ref_dim != 3)
+        return fail(GBR_ERR_INVALID, "ref_dim must be 2 or 3");
+    const bool is2d = d.ref_dim == 2;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev)
         return fail(GBR_ERR_CUDA, "no CUDA device " + std::to_string(device));
@@ -874,8 +885,11 @@ int gbr_bundle_create(const gbr_model_desc *desc, int device, gbr_bundle **out) 
     std::unique_ptr<gbr_bundle> b(new gbr_bundle());
     b->d = d;
     b->device = device;
-    b->grid.build((int)d.healpix_order, d.psi_step, d.offset_range, d.offset_step, (int)d.adaptive_oversampling);
+    b->is2d = is2d;
+    b->grid.build((int)d.healpix_order, d.psi_step, d.offset_range, d.offset_step, (int)d.adaptive_oversampling,
+                  !is2d);
     b->K = d.nr_classes;
+    b->KP = is2d ? (int)b->K : 1;
     b->ND = b->grid.ndir();
     b->NP = b->grid.npsi();
     b->T = b->grid.ntrans();
@@ -894,8 +908,10 @@ int gbr_bundle_create(const gbr_model_desc *desc, int device, gbr_bundle **out) 
     // backprojector volumes (BackProjector::initZeros(current_size))
     const int r_max = (int)std::min<int64_t>(d.current_size / 2, d.ori_size / 2);
     const int pad_size = 2 * (iround((double)d.padding_factor * r_max) + 1) + 1;
-    b->bg = VolGeom{pad_size / 2 + 1, pad_size, pad_size, -(pad_size / 2), -(pad_size / 2), r_max,
-                    (int)d.padding_factor};
+    // 2D: one padded plane (BackProjector::initialiseDataAndWeight with ref_dim 2)
+    b->bg = is2d ? VolGeom{pad_size / 2 + 1, pad_size, 1, -(pad_size / 2), 0, r_max, (int)d.padding_factor, 2}
+                 : VolGeom{pad_size / 2 + 1, pad_size, pad_size, -(pad_size / 2), -(pad_size / 2), r_max,
+                           (int)d.padding_factor, 3};
     b->bp_vox = (size_t)b->bg.xdim * b->bg.ydim * b->bg.zdim;
     b->bp_data.resize(b->K);
     b->bp_weight.resize(b->K);
@@ -915,6 +931,12 @@ int gbr_bundle_create(const gbr_model_desc *desc, int device, gbr_bundle **out) 
     GBR_CUDA(b->w_pdf_dir.reserve((size_t)b->K * b->ND));
     GBR_CUDA(b->w_pdf_cls.zero());
     GBR_CUDA(b->w_pdf_dir.zero());
+    if (is2d) {
+        b->class_prior_h.assign(2 * b->K, 0.);
+        GBR_CUDA(b->class_prior.upload(b->class_prior_h.data(), b->class_prior_h.size()));
+        GBR_CUDA(b->w_prior_off.reserve(2 * b->K));
+        GBR_CUDA(b->w_prior_off.zero());
+    }
     b->w_sigma2.assign(b->nshell, 0.);
     GBR_CUDA(cudaDeviceSynchronize());
     *out = b.release();
@@ -924,11 +946,13 @@ int gbr_bundle_create(const gbr_model_desc *desc, int device, gbr_bundle **out) 
 int gbr_projector_upload(gbr_bundle *b, int64_t iclass, const float *data, int64_t xdim, int64_t ydim,
                          int64_t zdim, int64_t yinit, int64_t zinit, int64_t r_max, int64_t padding_factor) {
     if (!b || !data || iclass < 0 || iclass >= b->K) return fail(GBR_ERR_INVALID, "bad class or data");
-    if (xdim <= 1 || ydim <= 1 || zdim <= 1 || padding_factor != b->d.padding_factor)
+    if (xdim <= 1 || ydim <= 1 || padding_factor != b->d.padding_factor ||
+        (b->is2d ? (zdim != 1 || zinit != 0) : zdim <= 1))
         return fail(GBR_ERR_INVALID, "bad projector dimensions");
     if (-yinit + 1 > ydim || -zinit + 1 > zdim || r_max * padding_factor + 1 >= xdim)
         return fail(GBR_ERR_INVALID, "projector origin / r_max outside the volume");
-    VolGeom g{(int)xdim, (int)ydim, (int)zdim, (int)yinit, (int)zinit, (int)r_max, (int)padding_factor};
+    VolGeom g{(int)xdim, (int)ydim, (int)zdim, (int)yinit, (int)zinit, (int)r_max, (int)padding_factor,
+              b->is2d ? 2 : 3};
     bool any = false;
     for (long k = 0; k < b->K; ++k) any |= (k != iclass && b->have_vol[k] != 0);
     if (any && std::memcmp(&g, &b->pg, sizeof(g)) != 0)
@@ -1155,6 +1179,26 @@ int gbr_wsum_download(gbr_bundle *b, gbr_wsum *out) {
     return GBR_OK;
 }
 
+int gbr_wsum_download_class_offsets(gbr_bundle *b, double *out) {
+    if (!b || !out) return fail(GBR_ERR_INVALID, "null argument");
+    if (!b->is2d) return fail(GBR_ERR_STATE, "class offset priors exist only for 2D classification");
+    GBR_CUDA(cudaSetDevice(b->device));
+    GBR_CUDA(cudaDeviceSynchronize());
+    std::vector<double> v(2 * b->K);
+    GBR_CUDA(cudaMemcpy(v.data(), b->w_prior_off.p, sizeof(double) * v.size(), cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < v.size(); ++i) out[i] += v[i];
+    return GBR_OK;
+}
+
+int gbr_model_set_class_offsets(gbr_bundle *b, const double *prior_offset_class) {
+    if (!b || !prior_offset_class) return fail(GBR_ERR_INVALID, "null argument");
+    if (!b->is2d) return fail(GBR_ERR_STATE, "class offset priors exist only for 2D classification");
+    GBR_CUDA(cudaSetDevice(b->device));
+    b->class_prior_h.assign(prior_offset_class, prior_offset_class + 2 * b->K);
+    GBR_CUDA(b->class_prior.upload(b->class_prior_h.data(), b->class_prior_h.size()));
+    return GBR_OK;
+}
+
 int gbr_bundle_reset_wsum(gbr_bundle *b) {
     if (!b) return fail(GBR_ERR_INVALID, "null bundle");
     GBR_CUDA(cudaSetDevice(b->device));
@@ -1164,6 +1208,7 @@ int gbr_bundle_reset_wsum(gbr_bundle *b) {
     }
     GBR_CUDA(b->w_pdf_cls.zero());
     GBR_CUDA(b->w_pdf_dir.zero());
+    if (b->is2d) GBR_CUDA(b->w_prior_off.zero());
     std::fill(b->w_sigma2.begin(), b->w_sigma2.end(), 0.);
     b->w_sigma2_offset = b->w_sumw_group = b->w_LL = b->w_ave_Pmax = b->w_avg_norm = b->w_XA = b->w_AA = 0.;
     GBR_CUDA(cudaDeviceSynchronize());

@@ -119,7 +119,8 @@ cudaError_t launch_gemm_sigma_norm(const float *Wrow, long long ldw, int npartic
 cudaError_t launch_fine_normalize(float *w, int n, int R, int nOR, int nOT, int T, const ParticleState *ps,
                                   const double *pdat, const double *otx, const double *oty, double pixel,
                                   int ndir, int npsi, float *Wt, int ldwt, float *Wp, int ldwp, unsigned char *active,
-                                  double *pacc, double *pdf_dir, double *pdf_cls, cudaStream_t st);
+                                  double *pacc, double *pdf_dir, double *pdf_cls, const double *class_prior,
+                                  double *w_prior_off, cudaStream_t st);
 cudaError_t launch_make_zt(const float *Cf, const float2 *Xnf, const float *minv_s, const float2 *E,
                            const double *pdat, int do_scale, int n, int TF, int nf, float *Zt, long long ldz,
                            float *CM, int ldcm, cudaStream_t st);
@@ -136,14 +137,14 @@ cudaError_t launch_prep(const float2 *X, const float *C, const double *pdat, int
                         const float2 *Xn, int do_scale, ParticleState *ps, cudaStream_t st);
 cudaError_t launch_pdf_offset(const double *pdat, int n, const double *tx, const double *ty, int T,
                               double sigma2_offset, double pixel, float *pdf_off, double log_rt_orient,
-                              ParticleState *ps, cudaStream_t st);
+                              ParticleState *ps, int KP, const double *class_prior, cudaStream_t st);
 // Weights of per-particle segments [seg[p], seg[p+1]) of `vals` (in place).
 // Coarse: element e of particle p has r = e / T, t = e % T.
 // Fine: element e has job = ejob[e] and code = ecode[e].
 cudaError_t launch_weights(float *vals, const long long *seg, int n, long long max_len, int coarse,
                            int T, const int *ejob, const unsigned int *ecode, const FineJob *jobs,
                            int nOR, int nOT, const float *pdf_orient, const float *pdf_off,
-                           ParticleState *ps, HistBin *hist, cudaStream_t st, int add_sum = 1);
+                           ParticleState *ps, HistBin *hist, cudaStream_t st, int add_sum = 1, int KP = 1, int rpc = 1);
 // Threshold search levels 0..2 (12, 12, 7 bits).  pass: 1 coarse, 2 fine
 // (weights below (1 - fraction) * sum / segment length are skipped: they
 // cannot reach the threshold), 0: no skipping.
@@ -158,7 +159,7 @@ cudaError_t launch_hist_refine(const float *vals, const long long *seg, int n, l
 cudaError_t launch_weights_cand(const float *vals, int n, int R, int T, const float *pdf_orient, float pdf_orient_min,
                                 const float *pdf_off, double fraction, ParticleState *ps, unsigned int *cand_idx,
                                 float *cand_w, unsigned int *cand_cnt, int cap, float *dense_out,
-                                const unsigned int *rowmin, cudaStream_t st);
+                                const unsigned int *rowmin, int KP, int rpc, cudaStream_t st);
 cudaError_t launch_cand_masks(const unsigned int *cand_idx, const float *cand_w, const unsigned int *cand_cnt,
                               int cap, int n, int R, int T, int W, const ParticleState *ps, unsigned int *mask,
                               int *cnt, cudaStream_t st);
@@ -201,6 +202,8 @@ struct WsumArgs {
     double *pacc;              // [p][8]: sumw, sigma2_offset, XA, AA
     double *pdf_dir;           // [K*ndir]
     double *pdf_cls;           // [K]
+    const double *class_prior; // [K][2] 2D classification: per-class offset prior, else null
+    double *w_prior_off;       // [K][2] 2D: sum w pixel (old offset + shift), else null
 };
 cudaError_t launch_wsum(const WsumArgs &a, cudaStream_t st);
 cudaError_t launch_compact_flags(const unsigned char *flags, int n, int *list, int *count,

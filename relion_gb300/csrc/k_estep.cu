@@ -121,31 +121,37 @@ __global__ void k_prep(const float2 *__restrict__ X, const float *__restrict__ C
 // pixels, combined exactly as the reference does.
 __global__ void k_pdf_offset(const double *__restrict__ pdat, const double *__restrict__ tx,
                              const double *__restrict__ ty, int T, double s2, double pixel,
-                             float *__restrict__ out, double log_rt_orient, ParticleState *__restrict__ ps) {
+                             float *__restrict__ out, double log_rt_orient, ParticleState *__restrict__ ps,
+                             int KP, const double *__restrict__ class_prior) {
     __shared__ double sh[32];
-    extern __shared__ double vals[];
+    extern __shared__ double vals[];  // [KP][T]
     const int p = blockIdx.x;
     const double *pd = pdat + (size_t)p * 8;
     const double norm = 2. * 3.14159265358979323846 * sqrt(s2) * sqrt(s2);
+    const int KT = KP * T;
     double acc = 0.;
-    for (int t = threadIdx.x; t < T; t += blockDim.x) {
+    for (int i = threadIdx.x; i < KT; i += blockDim.x) {
+        const int kc = i / T, t = i - kc * T;
+        // 2D classification: the offset prior is the class's (:7829-7833)
+        const double prx = class_prior ? class_prior[2 * kc] : pd[2];
+        const double pry = class_prior ? class_prior[2 * kc + 1] : pd[3];
         const double ox = pd[0] + tx[t], oy = pd[1] + ty[t];
         double td = 0.;
-        td += (ox - pd[2]) * (ox - pd[2]) / (-2. * s2);
-        td += (oy - pd[3]) * (oy - pd[3]) / (-2. * s2);
+        td += (ox - prx) * (ox - prx) / (-2. * s2);
+        td += (oy - pry) * (oy - pry) / (-2. * s2);
         td *= pixel * pixel;
         const double v = (s2 < 0.0001) ? ((td > 0.) ? 0. : 1.) : exp(td) / norm;
-        vals[t] = v;
+        vals[i] = v;
         acc += v;
     }
     double tot = block_sum(acc, sh);
     __shared__ double mean;
-    if (threadIdx.x == 0) mean = tot / (double)T;
+    if (threadIdx.x == 0) mean = tot / (double)KT;
     __syncthreads();
     float vmax = 0.f, vmin = FLT_MAX;
-    for (int t = threadIdx.x; t < T; t += blockDim.x) {
-        const float v = (float)(mean > 0. ? vals[t] / mean : vals[t]);
-        out[(size_t)p * T + t] = v;
+    for (int i = threadIdx.x; i < KT; i += blockDim.x) {
+        const float v = (float)(mean > 0. ? vals[i] / mean : vals[i]);
+        out[(size_t)p * KT + i] = v;
         vmax = fmaxf(vmax, v);
         vmin = fminf(vmin, v);
     }
@@ -190,7 +196,7 @@ __global__ void __launch_bounds__(kWThreads)
 k_weights(float *__restrict__ vals, const long long *__restrict__ seg, int coarse, int T,
           const int *__restrict__ ejob, const unsigned int *__restrict__ ecode,
           const FineJob *__restrict__ jobs, int nOR, int nOT, const float *__restrict__ pdf_orient,
-          const float *__restrict__ pdf_off, ParticleState *__restrict__ ps, int add_sum) {
+          const float *__restrict__ pdf_off, ParticleState *__restrict__ ps, int add_sum, int KP, int rpc) {
     __shared__ double sh[32];
     __shared__ unsigned long long smax;
     const int p = blockIdx.y;
@@ -231,7 +237,7 @@ k_weights(float *__restrict__ vals, const long long *__restrict__ seg, int coars
                     const unsigned int ior = (code / nOT) % nOR, iot = code % nOT;
                     idx = (((unsigned long long)r * nOR + ior) * T + t) * nOT + iot;
                 }
-                w = pdf_orient[r] * pdf_off[(size_t)p * T + t] * expf(-x);
+                w = pdf_orient[r] * pdf_off[((size_t)p * KP + (KP > 1 ? r / rpc : 0)) * T + t] * expf(-x);
                 if (coarse != 1 && w > 0.f) {
                     // loop order of storeWeightedSums: (r, iover_rot, itrans, iover_trans)
                     const unsigned long long key =
@@ -273,8 +279,8 @@ k_weights_cand(const float *__restrict__ vals, int R, int T, const float *__rest
                float pdf_orient_min, const float *__restrict__ pdf_off, double fraction,
                ParticleState *__restrict__ ps, unsigned int *__restrict__ cand_idx,
                float *__restrict__ cand_w, unsigned int *__restrict__ cand_cnt, int cap,
-               float *__restrict__ dense_out, const unsigned int *__restrict__ rowmin) {
-    extern __shared__ float s_po[];  // pdf_offset row of the particle [T]
+               float *__restrict__ dense_out, const unsigned int *__restrict__ rowmin, int KP, int rpc) {
+    extern __shared__ float s_po[];  // pdf_offset rows of the particle [KP][T]
     __shared__ double sh[32];
     __shared__ float s_eps;
     const int p = blockIdx.y;
@@ -282,11 +288,11 @@ k_weights_cand(const float *__restrict__ vals, int R, int T, const float *__rest
     if (r0 >= R) return;
     const int r1 = min(r0 + kWRowsPerBlock, R);
     const long long RT = (long long)R * T;
-    for (int t = threadIdx.x; t < T; t += blockDim.x) s_po[t] = pdf_off[(size_t)p * T + t];
+    for (int t = threadIdx.x; t < KP * T; t += blockDim.x) s_po[t] = pdf_off[(size_t)p * KP * T + t];
     __syncthreads();
     if (threadIdx.x < 32) {
         float m = FLT_MAX;
-        for (int t = threadIdx.x; t < T; t += 32) m = fminf(m, s_po[t]);
+        for (int t = threadIdx.x; t < KP * T; t += 32) m = fminf(m, s_po[t]);
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) m = fminf(m, __shfl_xor_sync(0xffffffffu, m, o));
         if (threadIdx.x == 0) s_eps = (float)((1.0 - fraction) * (double)pdf_orient_min * (double)m / (double)RT);
@@ -323,6 +329,7 @@ k_weights_cand(const float *__restrict__ vals, int R, int T, const float *__rest
             const int r = rb + __ffs(rows_left) - 1;
             rows_left &= rows_left - 1u;
             const float pr = pdf_orient[r];
+            const float *po_r = s_po + (KP > 1 ? (r / rpc) * T : 0);
             const float *row = rows + (size_t)r * T;
             for (int t0 = 0; t0 < T; t0 += 32 * kWUnroll) {
                 // kWUnroll independent streaming loads per lane, then one warp
@@ -354,7 +361,7 @@ k_weights_cand(const float *__restrict__ vals, int R, int T, const float *__rest
                         const float d = dv[k];
                         if (d < FLT_MAX) {
                             const float x = d - mn;
-                            if (!(x > xs)) w = pr * s_po[t] * expf(-x);
+                            if (!(x > xs)) w = pr * po_r[t] * expf(-x);
                         }
                         if (dense_out) dense_out[(size_t)p * RT + (size_t)r * T + t] = w;
                     }
@@ -843,7 +850,7 @@ __global__ void __launch_bounds__(kWsumPix) k_wsum(WsumArgs a) {
     double *shell = wsm;                                            // [nshell]
     float *wt = reinterpret_cast<float *>(shell + a.nshell);        // [rows][kMaxOR]
     int *tlist = reinterpret_cast<int *>(wt + a.T * a.nOT * kMaxOR); // [T]
-    __shared__ double red[4];  // sumw, sigma2_offset, XA, AA
+    __shared__ double red[6];  // sumw, sigma2_offset, XA, AA, 2D class offset sums x / y
     const FineJob job = a.jobs[blockIdx.x];
     const int p = job.p, r = job.r, n_t = job.n_t;
     const int nOR = a.nOR, nOT = a.nOT;
@@ -866,11 +873,14 @@ __global__ void __launch_bounds__(kWsumPix) k_wsum(WsumArgs a) {
             }
         }
     }
-    if (threadIdx.x < 4) red[threadIdx.x] = 0.;
+    if (threadIdx.x < 6) red[threadIdx.x] = 0.;
     for (int i = threadIdx.x; i < a.nshell; i += blockDim.x) shell[i] = 0.;
     __syncthreads();
+    // 2D classification: the offset prior is the class's (:8449-8456)
+    const double prx = a.class_prior ? a.class_prior[2 * ic] : pd[2];
+    const double pry = a.class_prior ? a.class_prior[2 * ic + 1] : pd[3];
     // normalised significant weights per (row, ior); FP64 scalar sums
-    double l_sumw = 0., l_off = 0.;
+    double l_sumw = 0., l_off = 0., l_px = 0., l_py = 0.;
     for (int i = threadIdx.x; i < rows * kMaxOR; i += blockDim.x) {
         const int row = i / kMaxOR, ior = i - row * kMaxOR;
         float wn = 0.f;
@@ -883,10 +893,13 @@ __global__ void __launch_bounds__(kWsumPix) k_wsum(WsumArgs a) {
                 wn = (float)wd;
                 l_sumw += wd;
                 const int tf = tlist[tr] * nOT + iot;
-                const double dx = pd[2] - pd[0] - a.otx[tf];
-                const double dy = pd[3] - pd[1] - a.oty[tf];
+                const double dx = prx - pd[0] - a.otx[tf];
+                const double dy = pry - pd[1] - a.oty[tf];
                 l_off += wd * a.pixel * a.pixel * dx * dx;
                 l_off += wd * a.pixel * a.pixel * dy * dy;
+                // class offset prior sums (:8668-8672)
+                l_px += wd * a.pixel * (pd[0] + a.otx[tf]);
+                l_py += wd * a.pixel * (pd[1] + a.oty[tf]);
             }
         }
         wt[i] = wn;
@@ -894,9 +907,13 @@ __global__ void __launch_bounds__(kWsumPix) k_wsum(WsumArgs a) {
     if (first) {
         l_sumw = warp_sum(l_sumw);
         l_off = warp_sum(l_off);
+        l_px = warp_sum(l_px);
+        l_py = warp_sum(l_py);
         if ((threadIdx.x & 31) == 0) {
             atomicAdd(&red[0], l_sumw);
             atomicAdd(&red[1], l_off);
+            atomicAdd(&red[4], l_px);
+            atomicAdd(&red[5], l_py);
         }
     }
     __syncthreads();
@@ -979,6 +996,10 @@ __global__ void __launch_bounds__(kWsumPix) k_wsum(WsumArgs a) {
             atomicAdd(&pa[1], red[1]);
             atomicAdd(&a.pdf_dir[(size_t)ic * a.ndir + idir], red[0]);
             atomicAdd(&a.pdf_cls[ic], red[0]);
+            if (a.w_prior_off) {
+                atomicAdd(&a.w_prior_off[2 * ic], red[4]);
+                atomicAdd(&a.w_prior_off[2 * ic + 1], red[5]);
+            }
         }
         if (a.do_scale) {
             atomicAdd(&pa[2], red[2]);
@@ -1103,9 +1124,10 @@ __global__ void k_fine_normalize(float *__restrict__ w, int R, int nOR, int nOT,
                                  double pixel, int ndir, int npsi, float *__restrict__ Wt, int ldwt,
                                  float *__restrict__ Wp, int ldwp, unsigned char *__restrict__ active,
                                  double *__restrict__ pacc, double *__restrict__ pdf_dir,
-                                 double *__restrict__ pdf_cls) {
+                                 double *__restrict__ pdf_cls, const double *__restrict__ class_prior,
+                                 double *__restrict__ w_prior_off) {
     __shared__ double rs[8];
-    __shared__ double red[2];
+    __shared__ double red[4];
     const int r = blockIdx.x, p = blockIdx.y;
     const int TF = T * nOT, RF = R * nOR;
     const float thr = ps[p].thr_fine;
@@ -1113,9 +1135,13 @@ __global__ void k_fine_normalize(float *__restrict__ w, int R, int nOR, int nOT,
     const double *pd = pdat + (size_t)p * 8;
     float *base = w + ((size_t)p * RF + (size_t)r * nOR) * TF;
     if (threadIdx.x < 8) rs[threadIdx.x] = 0.;
-    if (threadIdx.x < 2) red[threadIdx.x] = 0.;
+    if (threadIdx.x < 4) red[threadIdx.x] = 0.;
     __syncthreads();
-    double loff = 0.;
+    const int icl = r / (ndir * npsi);
+    // 2D classification: the offset prior is the class's (:8449-8456)
+    const double prx = class_prior ? class_prior[2 * icl] : pd[2];
+    const double pry = class_prior ? class_prior[2 * icl + 1] : pd[3];
+    double loff = 0., lpx = 0., lpy = 0.;
     double lrow[8];
 #pragma unroll
     for (int i = 0; i < 8; ++i) lrow[i] = 0.;
@@ -1126,10 +1152,12 @@ __global__ void k_fine_normalize(float *__restrict__ w, int R, int nOR, int nOT,
         if (v > 0.f && v >= thr) {
             const double wd = (double)v * inv;
             wn = (float)wd;
-            const double dx = pd[2] - pd[0] - otx[tf];
-            const double dy = pd[3] - pd[1] - oty[tf];
+            const double dx = prx - pd[0] - otx[tf];
+            const double dy = pry - pd[1] - oty[tf];
             loff += wd * pixel * pixel * dx * dx;
             loff += wd * pixel * pixel * dy * dy;
+            lpx += wd * pixel * (pd[0] + otx[tf]);
+            lpy += wd * pixel * (pd[1] + oty[tf]);
 #pragma unroll
             for (int i = 0; i < 8; ++i)
                 if (i == ior) lrow[i] += wd;
@@ -1137,10 +1165,14 @@ __global__ void k_fine_normalize(float *__restrict__ w, int R, int nOR, int nOT,
         base[e] = wn;
     }
     loff = warp_sum(loff);
+    lpx = warp_sum(lpx);
+    lpy = warp_sum(lpy);
 #pragma unroll
     for (int i = 0; i < 8; ++i) lrow[i] = warp_sum(lrow[i]);
     if ((threadIdx.x & 31) == 0) {
         atomicAdd(&red[1], loff);
+        atomicAdd(&red[2], lpx);
+        atomicAdd(&red[3], lpy);
         for (int i = 0; i < nOR && i < 8; ++i)
             if (lrow[i] != 0.) atomicAdd(&rs[i], lrow[i]);
     }
@@ -1162,6 +1194,10 @@ __global__ void k_fine_normalize(float *__restrict__ w, int R, int nOR, int nOT,
             atomicAdd(&pdf_cls[ic], tot);
         }
         if (red[1] != 0.) atomicAdd(&pacc[(size_t)p * 8 + 1], red[1]);
+        if (w_prior_off && (red[2] != 0. || red[3] != 0.)) {
+            atomicAdd(&w_prior_off[2 * icl], red[2]);
+            atomicAdd(&w_prior_off[2 * icl + 1], red[3]);
+        }
     }
 }
 
@@ -1267,10 +1303,16 @@ cudaError_t launch_prep(const float2 *X, const float *C, const double *pdat, int
 
 cudaError_t launch_pdf_offset(const double *pdat, int n, const double *tx, const double *ty, int T,
                               double sigma2_offset, double pixel, float *pdf_off, double log_rt_orient,
-                              ParticleState *ps, cudaStream_t st) {
+                              ParticleState *ps, int KP, const double *class_prior, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    k_pdf_offset<<<n, 256, sizeof(double) * T, st>>>(pdat, tx, ty, T, sigma2_offset, pixel, pdf_off,
-                                                     log_rt_orient, ps);
+    const size_t smem = sizeof(double) * (size_t)KP * T;
+    if (smem > 200 * 1024) return cudaErrorInvalidValue;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(k_pdf_offset, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    k_pdf_offset<<<n, 256, smem, st>>>(pdat, tx, ty, T, sigma2_offset, pixel, pdf_off, log_rt_orient, ps, KP,
+                                       class_prior);
     return cudaGetLastError();
 }
 
@@ -1279,14 +1321,14 @@ static size_t hist_smem() { return kHistBins * (sizeof(double) + sizeof(unsigned
 cudaError_t launch_weights(float *vals, const long long *seg, int n, long long max_len, int coarse,
                            int T, const int *ejob, const unsigned int *ecode, const FineJob *jobs,
                            int nOR, int nOT, const float *pdf_orient, const float *pdf_off,
-                           ParticleState *ps, HistBin *hist, cudaStream_t st, int add_sum) {
+                           ParticleState *ps, HistBin *hist, cudaStream_t st, int add_sum, int KP, int rpc) {
     (void)hist;
     if (n <= 0 || max_len <= 0) return cudaSuccess;
     const long long nb = (max_len + kChunk - 1) / kChunk;
     if (nb > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
     dim3 grid((unsigned)nb, n);
     k_weights<<<grid, kWThreads, 0, st>>>(vals, seg, coarse, T, ejob, ecode, jobs, nOR, nOT, pdf_orient,
-                                          pdf_off, ps, add_sum);
+                                          pdf_off, ps, add_sum, KP, rpc);
     return cudaGetLastError();
 }
 
@@ -1433,11 +1475,12 @@ cudaError_t launch_cand_seg(const unsigned int *cnt, int n, int cap, long long *
 cudaError_t launch_fine_normalize(float *w, int n, int R, int nOR, int nOT, int T, const ParticleState *ps,
                                   const double *pdat, const double *otx, const double *oty, double pixel,
                                   int ndir, int npsi, float *Wt, int ldwt, float *Wp, int ldwp, unsigned char *active,
-                                  double *pacc, double *pdf_dir, double *pdf_cls, cudaStream_t st) {
+                                  double *pacc, double *pdf_dir, double *pdf_cls, const double *class_prior,
+                                  double *w_prior_off, cudaStream_t st) {
     if (n <= 0 || nOR > 8) return nOR > 8 ? cudaErrorInvalidValue : cudaSuccess;
     dim3 grid(R, n);
     k_fine_normalize<<<grid, 256, 0, st>>>(w, R, nOR, nOT, T, ps, pdat, otx, oty, pixel, ndir, npsi, Wt, ldwt,
-                                           Wp, ldwp, active, pacc, pdf_dir, pdf_cls);
+                                           Wp, ldwp, active, pacc, pdf_dir, pdf_cls, class_prior, w_prior_off);
     return cudaGetLastError();
 }
 
@@ -1464,13 +1507,13 @@ cudaError_t launch_shell_dense(int n, const float *S2P, const float2 *G, const f
 cudaError_t launch_weights_cand(const float *vals, int n, int R, int T, const float *pdf_orient, float pdf_orient_min,
                                 const float *pdf_off, double fraction, ParticleState *ps, unsigned int *cand_idx,
                                 float *cand_w, unsigned int *cand_cnt, int cap, float *dense_out,
-                                const unsigned int *rowmin, cudaStream_t st) {
+                                const unsigned int *rowmin, int KP, int rpc, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    if ((size_t)T * sizeof(float) > 48 * 1024) return cudaErrorInvalidValue;
+    const size_t smem = (size_t)KP * T * sizeof(float);
+    if (smem > 48 * 1024) return cudaErrorInvalidValue;
     dim3 grid((unsigned)((R + kWRowsPerBlock - 1) / kWRowsPerBlock), n);
-    k_weights_cand<<<grid, kWThreads, sizeof(float) * T, st>>>(vals, R, T, pdf_orient, pdf_orient_min, pdf_off,
-                                                               fraction, ps, cand_idx, cand_w, cand_cnt, cap,
-                                                               dense_out, rowmin);
+    k_weights_cand<<<grid, kWThreads, smem, st>>>(vals, R, T, pdf_orient, pdf_orient_min, pdf_off, fraction, ps,
+                                                  cand_idx, cand_w, cand_cnt, cap, dense_out, rowmin, KP, rpc);
     return cudaGetLastError();
 }
 

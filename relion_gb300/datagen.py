@@ -30,6 +30,14 @@ CONFIGS = {
     # 3D classification, box 256 px, K=4: each class displaces a random 15 %
     # of a shared 4,000-Gaussian volume by 3-8 A; poses 70 % from three
     # von Mises-Fisher preferred views (kappa 5), 30 % uniform; search as box 256
+    # 2D classification, box 128 px, 1.5 A, K=100: class images are projections
+    # of 100 independent 500-Gaussian volumes at random poses; particles are
+    # in-plane rotated, shifted (+/-4 px), CTF-modulated class images at SNR
+    # 0.02; psi step 6, offsets +/-5 px step 1
+    "cfg3_box128_2d": dict(box=128, pixel=1.5, n_particles=100000, n_blobs=500, blob_sigma=1.5,
+                           blob_radius=30.0, max_shift=4.0, defocus=(8000.0, 30000.0), snr=0.02,
+                           ini_high=20.0, healpix_order=0, psi_step=6.0, offset_range_px=5.0,
+                           offset_step_px=1.0, diameter=150.0, classes=100, ref_dim=2),
     "cfg4_box256_K4": dict(box=256, pixel=1.0, n_particles=50000, n_blobs=4000, blob_sigma=1.5,
                            blob_radius=90.0, max_shift=3.0, defocus=(8000.0, 25000.0), snr=0.03,
                            ini_high=20.0, healpix_order=3, psi_step=-1.0, offset_range_px=6.0,
@@ -48,11 +56,13 @@ def iceil(x):
     return int(x) if x == int(x) else (int(x + 1) if x > 0 else int(x))
 
 
-def estep_sizes(box, pixel, ini_high, healpix_order, diameter, incr_size=10):
-    """current_size and coarse_size of the first iteration."""
+def estep_sizes(box, pixel, ini_high, healpix_order, diameter, incr_size=10, psi_step_2d=None):
+    """current_size and coarse_size of the first iteration (3D: the HEALPix
+    spacing; 2D classification: the psi step is the angular sampling,
+    HealpixSampling::getAngularSampling, src/healpix_sampling.cpp:1589-1598)."""
     maxres = iround(pixel * box / ini_high) + incr_size
     current = min(2 * maxres, box)
-    ang = 360.0 / (6 * iround(2.0 ** healpix_order))
+    ang = psi_step_2d if psi_step_2d else 360.0 / (6 * iround(2.0 ** healpix_order))
     coarse_res = (ang / 360.0) * math.pi * diameter / 1.2
     coarse = 2 * iceil(pixel * box / coarse_res)
     coarse = min(coarse, current)
@@ -220,6 +230,39 @@ def padded_reference(vol, box, pixel, r_max, pad, lowpass_A):
                 pad=pad, xdim=xdim, ydim=pad_size, zdim=pad_size)
 
 
+def padded_reference_2d(vol, R, box, pixel, r_max, pad, lowpass_A):
+    """Padded 2D Fourier reference of the class image = projection of `vol`
+    at rotation R (Projector::data of a 2D reference: complex64 [1][y][x],
+    x = 0.., y from yinit; zero beyond ROUND(pad*r_max)), low-passed."""
+    pad_size = 2 * (iround(pad * r_max) + 1) + 1
+    xdim = pad_size // 2 + 1
+    yinit = -(pad_size // 2)
+    xs = torch.arange(xdim, dtype=torch.float64)
+    ys = torch.arange(pad_size, dtype=torch.float64) + yinit
+    X, Y = xs[None, :].expand(pad_size, xdim), ys[:, None].expand(pad_size, xdim)
+    f = 1.0 / (pad * box)
+    k2 = torch.stack([X * f, Y * f, torch.zeros_like(X)], -1)
+    data = vol.ft(k2 @ R.to(torch.float64)).cpu()
+    r2 = X ** 2 + Y ** 2
+    max_r2 = iround(r_max * pad) ** 2
+    kA = torch.sqrt(r2) * f / pixel
+    fc = 1.0 / lowpass_A
+    w = torch.clamp((1.1 * fc - kA) / (0.2 * fc), 0.0, 1.0)
+    lp = 0.5 - 0.5 * torch.cos(math.pi * w)
+    data = (data * lp * (r2 <= max_r2))[None]
+    return dict(data=data.to(torch.complex64).numpy(), yinit=yinit, zinit=0, r_max=r_max,
+                pad=pad, xdim=xdim, ydim=pad_size, zdim=1)
+
+
+def inplane_matrices(psi_deg):
+    """[n, 3, 3] in-plane rotations blockdiag(A(psi), 1), A = [[c, s], [-s, c]]
+    (Euler_angles2matrix(0, 0, psi))."""
+    a = torch.as_tensor(psi_deg, dtype=torch.float64) * math.pi / 180.0
+    c, s_ = a.cos(), a.sin()
+    z, o = torch.zeros_like(a), torch.ones_like(a)
+    return torch.stack([c, s_, z, -s_, c, z, z, z, o], -1).view(-1, 3, 3)
+
+
 def fourier_grid(size):
     """Logical (x, y) of the [size][size/2+1] FFTW half layout."""
     X = size // 2 + 1
@@ -252,11 +295,19 @@ class Dataset:
         self.gen = torch.Generator().manual_seed(seed)
         self.n = int(n_particles if n_particles is not None else c["n_particles"])
         box, pix = c["box"], c["pixel"]
-        self.current, self.coarse = estep_sizes(box, pix, c["ini_high"], c["healpix_order"], c["diameter"])
+        self.is2d = int(c.get("ref_dim", 3)) == 2
+        self.current, self.coarse = estep_sizes(box, pix, c["ini_high"], c["healpix_order"], c["diameter"],
+                                                psi_step_2d=c["psi_step"] if self.is2d else None)
         self.vol = GaussianVolume(c["n_blobs"], c["blob_sigma"], c["blob_radius"], self.gen, device)
         K = int(c.get("classes", 1))
         self.vols = [self.vol]
-        if K > 1:
+        self.class_R = None
+        if self.is2d:
+            # independent class volumes, each projected at its own random pose
+            self.vols += [GaussianVolume(c["n_blobs"], c["blob_sigma"], c["blob_radius"], self.gen, device)
+                          for _ in range(K - 1)]
+            self.class_R = random_rotations(K, self.gen)
+        elif K > 1:
             frac, lo, hi = c.get("class_displace", (0.15, 3.0, 8.0))
             self.vols = [self.vol.displaced(frac, lo / pix, hi / pix, self.gen) for _ in range(K)]
         self.views = None
@@ -265,14 +316,18 @@ class Dataset:
             v = torch.randn(m, 3, generator=self.gen, dtype=torch.float64)
             self.views = v / v.norm(dim=1, keepdim=True)
         self.r_max = min(self.current // 2, box // 2)
-        self.refs = [padded_reference(v, box, pix, self.r_max, 2, c["ini_high"]) for v in self.vols]
+        if self.is2d:
+            self.refs = [padded_reference_2d(v, self.class_R[k], box, pix, self.r_max, 2, c["ini_high"])
+                         for k, v in enumerate(self.vols)]
+        else:
+            self.refs = [padded_reference(v, box, pix, self.r_max, 2, c["ini_high"]) for v in self.vols]
         self.ref = self.refs[0]
         self.sigma2 = None
 
     def model(self, precision=0):
         c = self.cfg
         box, pix = c["box"], c["pixel"]
-        ndir = 12 * 4 ** c["healpix_order"]
+        ndir = 1 if self.is2d else 12 * 4 ** c["healpix_order"]
         K = c["classes"]
         if self.sigma2 is None:
             self._noise_level()
@@ -285,7 +340,8 @@ class Dataset:
             offset_step=c["offset_step_px"] * pix, adaptive_fraction=0.999, sigma2_fudge=1.0,
             sigma2_offset=100.0, avg_norm_correction=1.0,
             sigma2_noise=np.full(box // 2 + 1, self.sigma2), pdf_class=np.full(K, 1.0 / K),
-            pdf_direction=np.full(K * ndir, 1.0 / (K * ndir)))
+            pdf_direction=np.full(K * ndir, 1.0 / (K * ndir)), ref_dim=2 if self.is2d else 3,
+            prior_offset_class=np.zeros((K, 2)) if self.is2d else None)
 
     def _noise_level(self):
         """sigma^2 per complex Fourier coefficient for the configured SNR:
@@ -321,13 +377,20 @@ class Dataset:
         count = self.n - start if count is None else count
         box, pix, cur = c["box"], c["pixel"], self.current
         g = torch.Generator().manual_seed(self.seed * 1000003 + start)
-        if self.views is not None:
+        K = len(self.vols)
+        true_psi = None
+        if self.is2d:
+            # in-plane rotated class images: k3 = k2 A(psi) R_class (row vectors)
+            labels = torch.randint(K, (count,), generator=g) if K > 1 else torch.zeros(count, dtype=torch.long)
+            true_psi = 360.0 * torch.rand(count, generator=g, dtype=torch.float64)
+            R = inplane_matrices(true_psi) @ self.class_R[labels]
+        elif self.views is not None:
             _, kappa, frac = c["views"]
             R = preferred_view_rotations(count, g, self.views, float(kappa), float(frac))
         else:
             R = random_rotations(count, g)
-        K = len(self.vols)
-        labels = torch.randint(K, (count,), generator=g) if K > 1 else torch.zeros(count, dtype=torch.long)
+        if not self.is2d:
+            labels = torch.randint(K, (count,), generator=g) if K > 1 else torch.zeros(count, dtype=torch.long)
         shifts = (torch.rand(count, 2, generator=g, dtype=torch.float64) * 2 - 1) * c["max_shift"]
         dlo, dhi = c["defocus"]
         dU = dlo + (dhi - dlo) * torch.rand(count, generator=g, dtype=torch.float64)
@@ -361,5 +424,5 @@ class Dataset:
             old_offset=np.zeros((count, 2)), prior=np.zeros((count, 2)),
             highres_Xi2=np.full(count, beyond * 0.5), norm_correction=np.ones(count),
             scale=np.ones(count), true_rot=R.numpy(), true_shift=shifts.numpy(),
-            true_class=labels.numpy(),
+            true_class=labels.numpy(), true_psi=None if true_psi is None else true_psi.numpy(),
             defocus=np.stack([dU.numpy(), dV.numpy(), dA.numpy()], 1))

@@ -45,6 +45,20 @@ class MlDeviceBundle:
         dvp = model.get("data_vs_prior")
         dvp = _lib.as_f64(dvp) if dvp is not None else None
         check(self.lib.gbr_model_set_arrays(h, ptr(s2), ptr(pc), ptr(pdir), ptr(dvp)))
+        self.ref_dim = int(model.get("ref_dim", 3) or 3)
+        if self.ref_dim == 2 and model.get("prior_offset_class") is not None:
+            self.set_class_offsets(model["prior_offset_class"])
+
+    # 2D classification: mymodel.prior_offset_class [K][2]
+    def set_class_offsets(self, prior_offset_class):
+        a = _lib.as_f64(np.asarray(prior_offset_class).reshape(self.nr_classes, 2))
+        check(self.lib.gbr_model_set_class_offsets(self.h, ptr(a)))
+
+    # wsum_model.prior_offset_class accumulated since the last reset
+    def get_class_offsets(self):
+        out = np.zeros((self.nr_classes, 2))
+        check(self.lib.gbr_wsum_download_class_offsets(self.h, out.ctypes.data))
+        return out
 
     # AccProjector::setMdlDim + initMdl
     def setup_projector(self, iclass, data, yinit, zinit, r_max, padding_factor):

@@ -36,8 +36,9 @@ def _run(monkeypatch, ds, model, batch, mode=None):
 
 
 def _rel(a, b):
-    a, b = np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64)
-    return np.linalg.norm((a - b).ravel()) / max(np.linalg.norm(b.ravel()), 1e-300)
+    # relative L2 (complex volumes included)
+    a, b = np.asarray(a), np.asarray(b)
+    return float(np.linalg.norm((a - b).ravel()) / max(np.linalg.norm(b.ravel()), 1e-300))
 
 
 @pytest.mark.parametrize("seed", [17, 18])

@@ -71,3 +71,27 @@ def test_parity_three_classes(cmp):
     st = cmp.compare(m, refs, b)
     assert st["sig_mismatch"] == 0 and st["fine_set_mismatch"] == 0
     _check(st, cmp.TOL)
+
+
+def _cfg2d(**kw):
+    from relion_gb300 import datagen
+    c = dict(datagen.CONFIGS["cfg3_box128_2d"])
+    # the 2D classification shape at a size the oracle finishes in seconds
+    c.update(box=64, pixel=3.0, classes=3, n_blobs=200, blob_radius=15.0, psi_step=10.0,
+             offset_range_px=3.0, max_shift=2.0, snr=0.05)
+    c.update(kw)
+    return c
+
+
+def test_parity_2d_classification(cmp):
+    # ref_dim 2: psi-only sampling (2 oversampled psi), in-plane rotation and
+    # back-rotation of padded 2D class references, per-class offset priors
+    from relion_gb300 import datagen
+    ds = datagen.Dataset(_cfg2d(), seed=29, n_particles=6)
+    m = ds.model()
+    m["prior_offset_class"] = np.array([[0.5, -0.25], [0.0, 0.0], [-1.0, 0.5]])
+    st = cmp.compare(m, ds.refs, ds.particles(0, 6))
+    assert st["sig_mismatch"] == 0 and st["fine_set_mismatch"] == 0
+    _check(st, cmp.TOL)
+    assert st["prior_offset_class_rel"] <= 1e-5
+    assert st["sigma2_offset_rel"] <= 1e-5

@@ -14,12 +14,13 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def _run(model, ref, batch, precision):
+def _run(model, refs, batch, precision):
     from relion_gb300.estep import MlDeviceBundle, MlOptimiserCuda
     m = dict(model)
     m["precision"] = precision
     b = MlDeviceBundle(m, device=0)
-    b.setup_projector(0, ref["data"], ref["yinit"], ref["zinit"], ref["r_max"], ref["pad"])
+    for k, ref in enumerate(refs):
+        b.setup_projector(k, ref["data"], ref["yinit"], ref["zinit"], ref["r_max"], ref["pad"])
     w = MlOptimiserCuda(b, debug=True)
     res = w.do_expectation_some_particles(batch)
     d = [w.debug_fetch(0, i) for i in range(len(res))]
@@ -37,8 +38,8 @@ def test_tcgen05_coarse_matches_fp32(order, psi):
     from relion_gb300 import datagen
     ds = datagen.Dataset("cfg0_box64", seed=31, n_particles=8, healpix_order=order, psi_step=psi)
     model, batch = ds.model(), ds.particles(0, 8)
-    r32, d32, w32 = _run(model, ds.ref, batch, 0)
-    r16, d16, w16 = _run(model, ds.ref, batch, 1)
+    r32, d32, w32 = _run(model, ds.refs, batch, 0)
+    r16, d16, w16 = _run(model, ds.refs, batch, 1)
     for i in range(8):
         a, b = d32[i], d16[i]
         fin = np.isfinite(a)
@@ -56,3 +57,27 @@ def test_tcgen05_coarse_matches_fp32(order, psi):
     agree = np.mean(r32["best_ihidden_over"] == r16["best_ihidden_over"])
     print("best-pose agreement", agree)
     assert agree >= 0.9
+
+
+def test_tcgen05_coarse_2d_classification():
+    # 2D classification shape, +/-4 px in 1 px steps (49 translations: the
+    # tensor-core pass with its row minima), 3 classes x 36 psi
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from relion_gb300 import datagen
+    c = dict(datagen.CONFIGS["cfg3_box128_2d"])
+    c.update(box=64, pixel=3.0, classes=3, n_blobs=200, blob_radius=15.0, psi_step=10.0,
+             offset_range_px=4.0, max_shift=2.0, snr=0.05)
+    ds = datagen.Dataset(c, seed=41, n_particles=8)
+    model, batch = ds.model(), ds.particles(0, 8)
+    r32, d32, w32 = _run(model, ds.refs, batch, 0)
+    r16, d16, w16 = _run(model, ds.refs, batch, 1)
+    for i in range(8):
+        a, b = d32[i], d16[i]
+        fin = np.isfinite(a)
+        assert np.array_equal(fin, np.isfinite(b))
+        ra, rb = a[fin] - a[fin].min(), b[fin] - b[fin].min()
+        assert np.max(np.abs(ra - rb)) <= 0.02 * np.ptp(ra) + 1e-3
+    assert np.mean(r32["best_ihidden_over"] == r16["best_ihidden_over"]) >= 0.9
+    assert np.mean(r16["cls"] - 1 == batch["true_class"]) >= 0.75
