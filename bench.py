@@ -40,6 +40,9 @@ CONFIG = "cfg1_box256"
 # projection-table read is independent of the batch, the diff2 write grows
 # with it.
 NCU_CROSS_B16 = {"read": 262.75e6, "write": 222.41e6, "batch": 16}
+# dram__bytes_read.sum / dram__bytes_write.sum of one k_tc_diff2 launch at the
+# bench's batch of 256 (one-pass metrics, full-size capture; profiles/k_tc_diff2_box256.md)
+NCU_TC_B256 = {"read": 1.39e9, "write": 4.42e9, "batch": 256}
 
 
 def parse():
@@ -245,8 +248,12 @@ def run_ours(args, world, rank, local):
                      "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                      "peak_source": peak_src,
                      "traffic": (NCU_CROSS_B16["read"] + NCU_CROSS_B16["write"] * B / NCU_CROSS_B16["batch"])
-                     if args.precision == "fp32" else None,
-                     "traffic_note": "ncu dram read+write of a 16-particle launch, write scaled to the batch"},
+                     if args.precision == "fp32" else
+                     ((NCU_TC_B256["read"] + NCU_TC_B256["write"]) if B == NCU_TC_B256["batch"] else None),
+                     "traffic_note": "ncu dram read+write of a 16-particle launch, write scaled to the batch"
+                     if args.precision == "fp32" else
+                     "ncu dram read+write of one full-size launch at batch 256 (one-pass metrics); "
+                     "algorithmic: 0.27 GB operands + 4.27 GB diff2 written"},
         "stage_ms": {k: round(float(v), 4) for k, v in zip(STAGES, stage)},
         "stage_sum_ms_per_step": float(sum(stage_sum_ms)) / args.steps,
         "mean_nr_sign": float(np.mean(res["nr_sign"])),
