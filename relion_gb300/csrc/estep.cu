@@ -220,6 +220,7 @@ struct gbr_worker {
     DevBuf<unsigned int> cand_idx, cand_cnt;
     DevBuf<float> cand_w, dense_dbg;
     DevBuf<unsigned int> rowmin;           // [p][R] row minima of the tensor-core coarse pass
+    DevBuf<unsigned int> segmask;          // [p][R] row segments it stored (sparse writes)
     DevBuf<long long> cand_seg;  // [2n]: begins, ends
     // page-locked read-back of the batch (counts, job totals, results) and
     // the host copies of device-resident metadata
@@ -230,6 +231,7 @@ struct gbr_worker {
     // dense fine pass
     int fine_mode = 0;  // 0: by significant density, 1: always dense, 2: always sparse
     int coarse_rows = 0;  // 0: skip far coarse rows by their minimum (tensor-core pass), 1: read all rows
+    int cand_cap_max = 1 << 16;  // candidate-list entries per particle (GBR_CAND_CAP)
     int last_dense = 0;
     DevBuf<float> Wt, Wp, Zt, CM, S2P, fnrm;
     DevBuf<float2> G;
@@ -629,15 +631,23 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
     w->launches += 3;  // prep, pdf_offset, norms
     GBR_CUDA(cudaEventRecord(w->ev[2], st));
     const bool use_rowmin = d.precision == GBR_PREC_BF16 && T >= 32 && w->coarse_rows == 0;
+    // sparse diff2 writes: only row segments near the running minimum are
+    // stored (the debug read-back needs the whole array)
+    const bool sparse = use_rowmin && !w->debug && T <= 960;
     if (use_rowmin) {
         GBR_CUDA(w->rowmin.reserve((size_t)n * R));
         GBR_CUDA(cudaMemsetAsync(w->rowmin.p, 0xFF, sizeof(unsigned int) * (size_t)n * R, st));
     }
+    if (sparse) {
+        GBR_CUDA(w->segmask.reserve((size_t)n * R));
+        GBR_CUDA(cudaMemsetAsync(w->segmask.p, 0, sizeof(unsigned int) * (size_t)n * R, st));
+    }
+    unsigned int *segmask = sparse ? w->segmask.p : nullptr;
     if (d.precision == GBR_PREC_BF16) {
         GBR_CUDA(w->ytc.reserve(tc_y_bytes(n * T, 2 * b->nc)));
         GBR_CUDA(launch_tc_diff2(b->proj_c_tc.p, w->ytc.p, R, 2 * b->nc, w->b_c.p, b->ldk_c, b->phase_c.p, b->ldk_c, n,
                                  T, w->vals.p, w->nrm.p, b->pdf_orient.p, w->ps.p,
-                                 use_rowmin ? w->rowmin.p : nullptr, st));
+                                 use_rowmin ? w->rowmin.p : nullptr, segmask, st));
         w->launches += 2;  // operand packing + tensor-core kernel
     } else {
         GBR_CUDA(launch_gemm_diff2(b->proj_c.p, b->lda_c, R, 2 * b->nc, w->b_c.p, b->ldk_c, b->phase_c.p, b->ldk_c,
@@ -652,7 +662,7 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
     // ---- coarse weights and significance ----
     // one read of the diff2 array: weights, FP64 sums and the candidate lists;
     // the threshold search and the significance masks then run on the lists
-    const int cap = (int)std::min<long long>(RT, 1 << 16);
+    const int cap = (int)std::min<long long>(RT, w->cand_cap_max);
     if (w->cand_cap < cap || w->cand_idx.n < (size_t)n * cap) {
         GBR_CUDA(w->cand_idx.reserve((size_t)n * cap));
         GBR_CUDA(w->cand_w.reserve((size_t)n * cap));
@@ -668,7 +678,8 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
     }
     GBR_CUDA(launch_weights_cand(w->vals.p, n, R, T, b->pdf_orient.p, b->pdf_orient_min, w->pdf_off.p,
                                  d.adaptive_fraction, w->ps.p, w->cand_idx.p, w->cand_w.p, w->cand_cnt.p, cap,
-                                 dense_w, use_rowmin ? w->rowmin.p : nullptr, b->KP, (int)(b->ND * b->NP), st));
+                                 dense_w, use_rowmin ? w->rowmin.p : nullptr, b->KP, (int)(b->ND * b->NP), segmask,
+                                 st));
     w->launches += 1;
     GBR_CUDA(w->h_ccnt.reserve(n));
     GBR_CUDA(w->h_totals.reserve(2));
@@ -711,7 +722,8 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
         if (cmax <= (unsigned int)cap) break;
         // a list overflowed: significance from the full weight array
         GBR_CUDA(launch_weights(w->vals.p, w->seg_c.p, n, RT, 1, T, nullptr, nullptr, nullptr, nOR, nOT,
-                                b->pdf_orient.p, w->pdf_off.p, w->ps.p, w->hist.p, st, 0, b->KP, (int)(b->ND * b->NP)));
+                                b->pdf_orient.p, w->pdf_off.p, w->ps.p, w->hist.p, st, 0, b->KP, (int)(b->ND * b->NP),
+                                segmask));
         s = threshold_search(w, n, w->vals.p, w->seg_c.p, RT, 1);
         if (s) return s;
         GBR_CUDA(launch_sig_masks(w->vals.p, n, R, T, W, w->ps.p, w->mask.p, w->cnt.p, st));
@@ -1000,6 +1012,8 @@ int gbr_worker_create(gbr_bundle *b, gbr_worker **out) {
     if (fm && std::strcmp(fm, "sparse") == 0) w->fine_mode = 2;
     const char *nm = std::getenv("GBR_COARSE_WEIGHTS");
     if (nm && std::strcmp(nm, "full") == 0) w->coarse_rows = 1;
+    const char *cc = std::getenv("GBR_CAND_CAP");
+    if (cc && std::atoi(cc) > 0) w->cand_cap_max = std::atoi(cc);
     *out = w.release();
     return GBR_OK;
 }

@@ -93,10 +93,13 @@ size_t tc_y_bytes(int N, int K2);
 cudaError_t launch_tc_pack_a(const float *src, int lds, int M, int K2, void *dst, cudaStream_t st);
 // Coarse cross term on tcgen05 (BF16, FP32 accumulation) with the diff2
 // epilogue; with T >= 32 and rowmin non-null it also records the ordered
-// minimum of every (particle, orientation) row (rowmin set to ~0 by the caller).
+// minimum of every (particle, orientation) row (rowmin set to ~0 by the
+// caller); with segmask non-null too (and T <= 960) it stores only the row
+// segments within ps[p].xs of the running minimum and marks them in segmask
+// (zeroed by the caller); the rest of `out` is left unwritten.
 cudaError_t launch_tc_diff2(const void *Ablk, void *Yblk, int M, int K2, const float2 *b, int ldb, const float2 *E,
                             int lde, int nparticles, int T, float *out, const float *norm, const float *pdf_orient,
-                            ParticleState *ps, unsigned int *rowmin, cudaStream_t st);
+                            ParticleState *ps, unsigned int *rowmin, unsigned int *segmask, cudaStream_t st);
 // Read (and optionally clear) the tensor-core pipeline error flag.
 cudaError_t tc_error_flag(int *flag, int reset);
 
@@ -144,7 +147,8 @@ cudaError_t launch_pdf_offset(const double *pdat, int n, const double *tx, const
 cudaError_t launch_weights(float *vals, const long long *seg, int n, long long max_len, int coarse,
                            int T, const int *ejob, const unsigned int *ecode, const FineJob *jobs,
                            int nOR, int nOT, const float *pdf_orient, const float *pdf_off,
-                           ParticleState *ps, HistBin *hist, cudaStream_t st, int add_sum = 1, int KP = 1, int rpc = 1);
+                           ParticleState *ps, HistBin *hist, cudaStream_t st, int add_sum = 1, int KP = 1, int rpc = 1,
+                           const unsigned int *segmask = nullptr);
 // Threshold search levels 0..2 (12, 12, 7 bits).  pass: 1 coarse, 2 fine
 // (weights below (1 - fraction) * sum / segment length are skipped: they
 // cannot reach the threshold), 0: no skipping.
@@ -159,7 +163,8 @@ cudaError_t launch_hist_refine(const float *vals, const long long *seg, int n, l
 cudaError_t launch_weights_cand(const float *vals, int n, int R, int T, const float *pdf_orient, float pdf_orient_min,
                                 const float *pdf_off, double fraction, ParticleState *ps, unsigned int *cand_idx,
                                 float *cand_w, unsigned int *cand_cnt, int cap, float *dense_out,
-                                const unsigned int *rowmin, int KP, int rpc, cudaStream_t st);
+                                const unsigned int *rowmin, int KP, int rpc, const unsigned int *segmask,
+                                cudaStream_t st);
 cudaError_t launch_cand_masks(const unsigned int *cand_idx, const float *cand_w, const unsigned int *cand_cnt,
                               int cap, int n, int R, int T, int W, const ParticleState *ps, unsigned int *mask,
                               int *cnt, cudaStream_t st);

@@ -196,7 +196,8 @@ __global__ void __launch_bounds__(kWThreads)
 k_weights(float *__restrict__ vals, const long long *__restrict__ seg, int coarse, int T,
           const int *__restrict__ ejob, const unsigned int *__restrict__ ecode,
           const FineJob *__restrict__ jobs, int nOR, int nOT, const float *__restrict__ pdf_orient,
-          const float *__restrict__ pdf_off, ParticleState *__restrict__ ps, int add_sum, int KP, int rpc) {
+          const float *__restrict__ pdf_off, ParticleState *__restrict__ ps, int add_sum, int KP, int rpc,
+          const unsigned int *__restrict__ segmask) {
     __shared__ double sh[32];
     __shared__ unsigned long long smax;
     const int p = blockIdx.y;
@@ -209,8 +210,17 @@ k_weights(float *__restrict__ vals, const long long *__restrict__ seg, int coars
     const float xcut = coarse == 1 ? fminf(ps[p].xs, 700.f) : 700.f;
     double acc = 0.;
     unsigned long long kmax = 0ull;
+    const int Rrows = (int)((b1 - b0) / T);
     for (long long e = beg + threadIdx.x; e < end; e += blockDim.x) {
-        const float d = vals[e];
+        float d = vals[e];
+        if (coarse == 1 && segmask) {
+            // sparse coarse writes: a segment the coarse pass did not store
+            // lies beyond the skip distance (weight 0)
+            const unsigned int l32 = (unsigned int)(e - b0), rr = l32 / (unsigned int)T;
+            const unsigned int tt = l32 - rr * (unsigned int)T;
+            const unsigned int seg = segmask[(size_t)p * Rrows + rr];
+            if (!((seg >> (((p * T + (int)tt) >> 5) - ((p * T) >> 5))) & 1u)) d = __int_as_float(0x7f800000);
+        }
         float w = 0.f;
         if (d < FLT_MAX) {  // finite: computed
             const float x = d - mn;
@@ -279,7 +289,8 @@ k_weights_cand(const float *__restrict__ vals, int R, int T, const float *__rest
                float pdf_orient_min, const float *__restrict__ pdf_off, double fraction,
                ParticleState *__restrict__ ps, unsigned int *__restrict__ cand_idx,
                float *__restrict__ cand_w, unsigned int *__restrict__ cand_cnt, int cap,
-               float *__restrict__ dense_out, const unsigned int *__restrict__ rowmin, int KP, int rpc) {
+               float *__restrict__ dense_out, const unsigned int *__restrict__ rowmin, int KP, int rpc,
+               const unsigned int *__restrict__ segmask) {
     extern __shared__ float s_po[];  // pdf_offset rows of the particle [KP][T]
     __shared__ double sh[32];
     __shared__ float s_eps;
@@ -331,6 +342,10 @@ k_weights_cand(const float *__restrict__ vals, int R, int T, const float *__rest
             const float pr = pdf_orient[r];
             const float *po_r = s_po + (KP > 1 ? (r / rpc) * T : 0);
             const float *row = rows + (size_t)r * T;
+            // segments of the row the coarse pass stored (sparse writes); the
+            // others lie beyond the skip distance and are not read
+            const unsigned int seg = segmask ? segmask[(size_t)p * R + r] : 0xFFFFFFFFu;
+            const int c0 = (p * T) >> 5;
             for (int t0 = 0; t0 < T; t0 += 32 * kWUnroll) {
                 // kWUnroll independent streaming loads per lane, then one warp
                 // vote: poses with diff2 - min > xs are skipped (all of them
@@ -340,7 +355,8 @@ k_weights_cand(const float *__restrict__ vals, int R, int T, const float *__rest
     #pragma unroll
                 for (int k = 0; k < kWUnroll; ++k) {
                     const int t = t0 + 32 * k + lane;
-                    dv[k] = t < T ? __ldcs(row + t) : __int_as_float(0x7f800000);
+                    const bool stored = t < T && ((seg >> (((p * T + t) >> 5) - c0)) & 1u);
+                    dv[k] = stored ? __ldcs(row + t) : __int_as_float(0x7f800000);
                     near |= !(dv[k] - mn > xs);
                 }
                 if (!__any_sync(0xffffffffu, near)) {
@@ -1321,14 +1337,15 @@ static size_t hist_smem() { return kHistBins * (sizeof(double) + sizeof(unsigned
 cudaError_t launch_weights(float *vals, const long long *seg, int n, long long max_len, int coarse,
                            int T, const int *ejob, const unsigned int *ecode, const FineJob *jobs,
                            int nOR, int nOT, const float *pdf_orient, const float *pdf_off,
-                           ParticleState *ps, HistBin *hist, cudaStream_t st, int add_sum, int KP, int rpc) {
+                           ParticleState *ps, HistBin *hist, cudaStream_t st, int add_sum, int KP, int rpc,
+                           const unsigned int *segmask) {
     (void)hist;
     if (n <= 0 || max_len <= 0) return cudaSuccess;
     const long long nb = (max_len + kChunk - 1) / kChunk;
     if (nb > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
     dim3 grid((unsigned)nb, n);
     k_weights<<<grid, kWThreads, 0, st>>>(vals, seg, coarse, T, ejob, ecode, jobs, nOR, nOT, pdf_orient,
-                                          pdf_off, ps, add_sum, KP, rpc);
+                                          pdf_off, ps, add_sum, KP, rpc, segmask);
     return cudaGetLastError();
 }
 
@@ -1507,13 +1524,15 @@ cudaError_t launch_shell_dense(int n, const float *S2P, const float2 *G, const f
 cudaError_t launch_weights_cand(const float *vals, int n, int R, int T, const float *pdf_orient, float pdf_orient_min,
                                 const float *pdf_off, double fraction, ParticleState *ps, unsigned int *cand_idx,
                                 float *cand_w, unsigned int *cand_cnt, int cap, float *dense_out,
-                                const unsigned int *rowmin, int KP, int rpc, cudaStream_t st) {
+                                const unsigned int *rowmin, int KP, int rpc, const unsigned int *segmask,
+                                cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
     const size_t smem = (size_t)KP * T * sizeof(float);
     if (smem > 48 * 1024) return cudaErrorInvalidValue;
     dim3 grid((unsigned)((R + kWRowsPerBlock - 1) / kWRowsPerBlock), n);
     k_weights_cand<<<grid, kWThreads, smem, st>>>(vals, R, T, pdf_orient, pdf_orient_min, pdf_off, fraction, ps,
-                                                  cand_idx, cand_w, cand_cnt, cap, dense_out, rowmin, KP, rpc);
+                                                  cand_idx, cand_w, cand_cnt, cap, dense_out, rowmin, KP, rpc,
+                                                  segmask);
     return cudaGetLastError();
 }
 

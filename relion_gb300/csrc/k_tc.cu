@@ -159,6 +159,11 @@ struct TcArgs {
     const float *pdf_orient; // [M]
     ParticleState *ps;
     unsigned int *rowmin;    // [p][M] ordered minimum of each orientation row, or null
+    // sparse diff2 writes (null = write every pose): only row segments (the
+    // part of an orientation row inside one 32-column chunk) whose minimum is
+    // within ps[p].xs of the particle's running minimum are stored, and bit
+    // (chunk - first chunk of the row) of segmask[p][M] records them
+    unsigned int *segmask;
 };
 
 // Tile order of the persistent loop: groups of kGroupM orientation tiles,
@@ -178,6 +183,19 @@ __device__ __forceinline__ unsigned int warp_min_flush(float lmin, unsigned int 
     const unsigned int wmin = __reduce_min_sync(0xffffffffu, u);
     if ((threadIdx.x & 31) == 0 && wmin != 0xFFFFFFFFu) atomicMin(dst, wmin);
     return wmin;
+}
+
+__device__ __forceinline__ float ord2f(unsigned int u) {
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+// Near cut of a particle: its running minimum diff2 (never below the final
+// one) plus its skip distance xs; -inf while it has no finite diff2 yet.
+// A segment whose minimum is above the cut is above final minimum + xs too.
+__device__ __forceinline__ float near_cut(const ParticleState *ps, unsigned int u_chunk) {
+    const unsigned int run = min(u_chunk, __ldcg(&ps->min_coarse));
+    if (run == 0xFFFFFFFFu) return -__int_as_float(0x7f800000);
+    return ord2f(run) + __ldcg(&ps->xs) + 1.f;  // +1: margin over the readers' float test
 }
 
 // Ordered minimum of lane row m for particle p into rowmin (one atomic per
@@ -317,10 +335,14 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_diff2(const TcArgs a) {
                 const int nb = n0 + col;
                 if (nb >= a.N) break;  // warp-uniform
                 const int nvalid = min(32, a.N - nb);
+                // rows whose segments of this chunk are stored (bit r = lane r's row)
+                unsigned int lo_rows = 0xFFFFFFFFu, hi_rows = 0xFFFFFFFFu;
+                int bnd_st = 32;
                 const int p_lo = nb / a.T;
                 if (a.T >= 32) {
                     // at most two particles in these 32 columns: p_lo for jj < bnd
                     const int bnd = (p_lo + 1) * a.T - nb;
+                    bnd_st = bnd;
                     const float n_lo = skip ? 0.f : a.norm[(size_t)p_lo * a.M + m];
                     const float n_hi = (skip || bnd >= nvalid) ? 0.f : a.norm[(size_t)(p_lo + 1) * a.M + m];
                     float min_lo = __int_as_float(0x7f800000), min_hi = min_lo;
@@ -335,11 +357,23 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_diff2(const TcArgs a) {
                                 min_hi = fminf(min_hi, d);
                         }
                         v[jj] = d;
-                        tb[lane * 33 + jj] = d;
                     }
                     const bool two = bnd < nvalid;
-                    warp_min_flush(min_lo, &a.ps[p_lo].min_coarse);
-                    if (two) warp_min_flush(min_hi, &a.ps[p_lo + 1].min_coarse);
+                    const unsigned int u_lo = warp_min_flush(min_lo, &a.ps[p_lo].min_coarse);
+                    const unsigned int u_hi = two ? warp_min_flush(min_hi, &a.ps[p_lo + 1].min_coarse) : 0xFFFFFFFFu;
+                    if (a.segmask) {
+                        const bool near_lo = min_lo <= near_cut(a.ps + p_lo, u_lo);
+                        const bool near_hi = two && min_hi <= near_cut(a.ps + p_lo + 1, u_hi);
+                        lo_rows = __ballot_sync(0xffffffffu, near_lo);
+                        hi_rows = __ballot_sync(0xffffffffu, near_hi);
+                        if (near_lo)
+                            atomicOr(&a.segmask[(size_t)p_lo * a.M + m], 1u << ((nb >> 5) - ((p_lo * a.T) >> 5)));
+                        if (near_hi) atomicOr(&a.segmask[(size_t)(p_lo + 1) * a.M + m], 1u);
+                    }
+                    if (lo_rows | hi_rows) {
+#pragma unroll
+                        for (int jj = 0; jj < 32; ++jj) tb[lane * 33 + jj] = v[jj];
+                    }
                     if (track_rows) {
                         if (p_lo != acc_p) {
                             rowmin_flush(a, acc_p, m, acc_m);
@@ -378,14 +412,16 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_diff2(const TcArgs a) {
                 }
                 __syncwarp();
                 // lane = column: each store writes 32 consecutive translations
+                // of one row; rows whose segment is not kept are not stored
                 const int n = nb + lane;
-                if (lane < nvalid) {
+                if ((lo_rows | hi_rows) && lane < nvalid) {
                     const int pn = n / a.T, tn = n - pn * a.T;
                     float *dst = a.out + (size_t)pn * a.M * a.T + tn;
                     const int rows = min(32, a.M - (m0 + q * 32));
+                    const unsigned int my_rows = lane < bnd_st ? lo_rows : hi_rows;
 #pragma unroll 8
                     for (int r = 0; r < 32; ++r)
-                        if (r < rows) dst[(size_t)(m0 + q * 32 + r) * a.T] = tb[r * 33 + lane];
+                        if (r < rows && ((my_rows >> r) & 1u)) dst[(size_t)(m0 + q * 32 + r) * a.T] = tb[r * 33 + lane];
                 }
                 __syncwarp();
             }
@@ -480,7 +516,7 @@ cudaError_t launch_tc_pack_a(const float *src, int lds, int M, int K2, void *dst
 
 cudaError_t launch_tc_diff2(const void *Ablk, void *Yblk, int M, int K2, const float2 *b, int ldb, const float2 *E,
                             int lde, int nparticles, int T, float *out, const float *norm, const float *pdf_orient,
-                            ParticleState *ps, unsigned int *rowmin, cudaStream_t st) {
+                            ParticleState *ps, unsigned int *rowmin, unsigned int *segmask, cudaStream_t st) {
     const int N = nparticles * T;
     if (N <= 0 || M <= 0) return cudaSuccess;
     const int ktiles = (K2 + TK - 1) / TK, ntiles = (N + TN - 1) / TN, mtiles = (M + TM - 1) / TM;
@@ -506,7 +542,8 @@ cudaError_t launch_tc_diff2(const void *Ablk, void *Yblk, int M, int K2, const f
     if (ntotal > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
     const int grid = (int)std::min<long long>(ntotal, nsm);
     TcArgs a{static_cast<const uint8_t *>(Ablk), static_cast<const uint8_t *>(Yblk), M, ktiles, T, N, nparticles,
-             mtiles, ntiles, out, norm, pdf_orient, ps, T >= 32 ? rowmin : nullptr};
+             mtiles, ntiles, out, norm, pdf_orient, ps, T >= 32 ? rowmin : nullptr,
+             (T >= 32 && T <= 960 && rowmin) ? segmask : nullptr};
     k_tc_diff2<<<grid, THREADS, smem, st>>>(a);
     return cudaGetLastError();
 }

@@ -9,7 +9,11 @@ agree with the pass over all rows (GBR_COARSE_WEIGHTS=full): per-particle
 results to 1e-9 relative with identical significant counts and best poses,
 and the accumulated sums (sigma2 noise, backprojection), whose FP64 atomics
 run in a different order on every run, to 1e-6 relative L2.  The debug copy
-of the dense coarse weights must be identical too.
+of the dense coarse weights must be identical too.  Without the debug
+read-back the coarse pass also stores only the row segments near the running
+minimum (sparse diff2 writes); the same bounds hold then, also when the
+candidate lists overflow and the significance search reruns on the full
+(partly unwritten) array (GBR_CAND_CAP small).
 """
 import numpy as np
 import pytest
@@ -17,17 +21,20 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def _run(monkeypatch, ds, model, batch, mode=None):
+def _run(monkeypatch, ds, model, batch, mode=None, debug=True, cand_cap=None):
     from relion_gb300.estep import MlDeviceBundle, MlOptimiserCuda
     monkeypatch.delenv("GBR_COARSE_WEIGHTS", raising=False)
+    monkeypatch.delenv("GBR_CAND_CAP", raising=False)
     if mode:
         monkeypatch.setenv("GBR_COARSE_WEIGHTS", mode)
+    if cand_cap:
+        monkeypatch.setenv("GBR_CAND_CAP", str(cand_cap))
     b = MlDeviceBundle(model, device=0)
     r = ds.ref
     b.setup_projector(0, r["data"], r["yinit"], r["zinit"], r["r_max"], r["pad"])
-    w = MlOptimiserCuda(b, debug=True)
+    w = MlOptimiserCuda(b, debug=debug)
     res = w.do_expectation_some_particles(batch)
-    cw = [w.debug_fetch(1, i) for i in range(len(res))]
+    cw = [w.debug_fetch(1, i) for i in range(len(res))] if debug else None
     wsum = b.get_wsum()
     data, weight = b.get_mdl_data(0)
     w.close()
@@ -60,6 +67,28 @@ def test_row_skip_matches_full_coarse_pass(monkeypatch, seed):
         np.testing.assert_allclose(rn[k], rf[k], rtol=1e-9, err_msg=k)
     for i in range(len(rf)):
         assert np.array_equal(cn[i], cf[i])
+    for k in wf:
+        assert _rel(wn[k], wf[k]) <= 1e-6, k
+    assert _rel(dn, df) <= 1e-6
+    assert _rel(gn, gf) <= 1e-6
+
+
+@pytest.mark.parametrize("cand_cap", [None, 16])
+def test_sparse_writes_match_full_coarse_pass(monkeypatch, cand_cap):
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from relion_gb300 import datagen
+    ds = datagen.Dataset("cfg0_box64", seed=19, n_particles=12, healpix_order=1, psi_step=30.0,
+                         offset_range_px=4.0, offset_step_px=1.0)
+    model = ds.model(precision=1)
+    batch = ds.particles(0, 12)
+    rf, _, wf, df, gf = _run(monkeypatch, ds, model, batch, mode="full", debug=False)
+    rn, _, wn, dn, gn = _run(monkeypatch, ds, model, batch, debug=False, cand_cap=cand_cap)
+    assert np.array_equal(rf["nr_sign"], rn["nr_sign"])
+    assert np.array_equal(rf["best_ihidden_over"], rn["best_ihidden_over"])
+    for k in ("coarse_sum_weight", "coarse_significant_weight", "pmax", "dLL", "fine_sum_weight"):
+        np.testing.assert_allclose(rn[k], rf[k], rtol=1e-9, err_msg=k)
     for k in wf:
         assert _rel(wn[k], wf[k]) <= 1e-6, k
     assert _rel(dn, df) <= 1e-6
