@@ -189,13 +189,13 @@ __device__ __forceinline__ float ord2f(unsigned int u) {
     return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
 }
 
-// Near cut of a particle: its running minimum diff2 (never below the final
-// one) plus its skip distance xs; -inf while it has no finite diff2 yet.
-// A segment whose minimum is above the cut is above final minimum + xs too.
-__device__ __forceinline__ float near_cut(const ParticleState *ps, unsigned int u_chunk) {
-    const unsigned int run = min(u_chunk, __ldcg(&ps->min_coarse));
+// Near cut of a particle from its running minimum diff2 (ordered encoding,
+// never below the final minimum) and its skip distance xs; -inf while it has
+// no finite diff2 yet.  A segment whose minimum is above the cut is above
+// final minimum + xs too.
+__device__ __forceinline__ float near_cut(unsigned int run, float xs) {
     if (run == 0xFFFFFFFFu) return -__int_as_float(0x7f800000);
-    return ord2f(run) + __ldcg(&ps->xs) + 1.f;  // +1: margin over the readers' float test
+    return ord2f(run) + xs + 1.f;  // +1: margin over the readers' float test
 }
 
 // Ordered minimum of lane row m for particle p into rowmin (one atomic per
@@ -330,8 +330,6 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_diff2(const TcArgs a) {
             float acc_m = __int_as_float(0x7f800000);
             for (int c = 0; c < 4; ++c) {
                 const int col = h * 128 + c * 32;
-                float v[32];
-                tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + b * (uint32_t)TN + (uint32_t)col, v);
                 const int nb = n0 + col;
                 if (nb >= a.N) break;  // warp-uniform
                 const int nvalid = min(32, a.N - nb);
@@ -339,12 +337,28 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_diff2(const TcArgs a) {
                 unsigned int lo_rows = 0xFFFFFFFFu, hi_rows = 0xFFFFFFFFu;
                 int bnd_st = 32;
                 const int p_lo = nb / a.T;
+                // operands of the epilogue that do not depend on the accumulator
+                // are loaded before the TMEM read so their latency overlaps it:
+                // at most two particles in these 32 columns (T >= 32), p_lo for jj < bnd
+                const int bnd = (p_lo + 1) * a.T - nb;
+                float n_lo = 0.f, n_hi = 0.f, xs_lo = 0.f, xs_hi = 0.f;
+                unsigned int run_lo = 0xFFFFFFFFu, run_hi = 0xFFFFFFFFu;
                 if (a.T >= 32) {
-                    // at most two particles in these 32 columns: p_lo for jj < bnd
-                    const int bnd = (p_lo + 1) * a.T - nb;
+                    if (!skip) n_lo = a.norm[(size_t)p_lo * a.M + m];
+                    if (!skip && bnd < nvalid) n_hi = a.norm[(size_t)(p_lo + 1) * a.M + m];
+                    if (a.segmask) {
+                        run_lo = __ldcg(&a.ps[p_lo].min_coarse);
+                        xs_lo = __ldg(&a.ps[p_lo].xs);
+                        if (bnd < nvalid) {
+                            run_hi = __ldcg(&a.ps[p_lo + 1].min_coarse);
+                            xs_hi = __ldg(&a.ps[p_lo + 1].xs);
+                        }
+                    }
+                }
+                float v[32];
+                tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + b * (uint32_t)TN + (uint32_t)col, v);
+                if (a.T >= 32) {
                     bnd_st = bnd;
-                    const float n_lo = skip ? 0.f : a.norm[(size_t)p_lo * a.M + m];
-                    const float n_hi = (skip || bnd >= nvalid) ? 0.f : a.norm[(size_t)(p_lo + 1) * a.M + m];
                     float min_lo = __int_as_float(0x7f800000), min_hi = min_lo;
 #pragma unroll
                     for (int jj = 0; jj < 32; ++jj) {
@@ -362,8 +376,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_diff2(const TcArgs a) {
                     const unsigned int u_lo = warp_min_flush(min_lo, &a.ps[p_lo].min_coarse);
                     const unsigned int u_hi = two ? warp_min_flush(min_hi, &a.ps[p_lo + 1].min_coarse) : 0xFFFFFFFFu;
                     if (a.segmask) {
-                        const bool near_lo = min_lo <= near_cut(a.ps + p_lo, u_lo);
-                        const bool near_hi = two && min_hi <= near_cut(a.ps + p_lo + 1, u_hi);
+                        const bool near_lo = min_lo <= near_cut(min(u_lo, run_lo), xs_lo);
+                        const bool near_hi = two && min_hi <= near_cut(min(u_hi, run_hi), xs_hi);
                         lo_rows = __ballot_sync(0xffffffffu, near_lo);
                         hi_rows = __ballot_sync(0xffffffffu, near_hi);
                         if (near_lo)
