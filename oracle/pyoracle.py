@@ -68,6 +68,8 @@ def load():
             raise RuntimeError("oracle not built: %s (run oracle/build.py)" % path)
         lib = C.CDLL(path)
         lib.oracle_expectation.restype = C.c_int
+        lib.oracle_prepare_images.restype = C.c_int
+        lib.oracle_prepare_images.argtypes = [P, I64, P, P, P, P, P, P, P, P]
         lib.oracle_ctf.restype = F64
         lib.oracle_ctf.argtypes = [F64] * 11
         lib.oracle_hpx_xyf2nest.restype = I64
@@ -230,3 +232,51 @@ def run(model, refs, batch, debug=False):
                 prior_offset_class=ws["prior_offset_class"])
     del keep, vox
     return out, dbg_arrays, wsum, ws["bp_data"], ws["bp_weight"]
+
+
+class OraclePrepParams(C.Structure):
+    _fields_ = [(n, I64) for n in ("ori_size", "current_size", "do_norm_correction", "pad_")] + \
+        [(n, F64) for n in ("pixel_size", "mask_radius_px", "width_mask_edge", "avg_norm_correction",
+                            "kV", "Cs", "Q0")]
+
+
+class OracleImageMeta(C.Structure):
+    _fields_ = [("old_offset", F64 * 2)] + \
+        [(n, F64) for n in ("norm_correction", "defU", "defV", "defAngle", "Bfac", "scale", "phase_shift")]
+
+
+META_FIELDS = ("norm_correction", "defU", "defV", "defAngle", "Bfac", "scale", "phase_shift")
+
+
+def prepare_images(params, images, meta):
+    """Oracle image preparation (getFourierTransformsAndCtfs).
+
+    params: dict with the OraclePrepParams fields; images [n][ori][ori]
+    real; meta: dict of per-particle arrays (old_offset [n][2] and
+    META_FIELDS).  Returns dict(fimg, fimg_nomask, fctf, power_img,
+    highres_Xi2, old_offset)."""
+    o = load()
+    pp = OraclePrepParams()
+    for k, _ in OraclePrepParams._fields_:
+        if k in params:
+            setattr(pp, k, params[k])
+    imgs = np.ascontiguousarray(images, np.float64)
+    n, N = imgs.shape[0], imgs.shape[1]
+    cur = int(params["current_size"])
+    X = cur // 2 + 1
+    ms = (OracleImageMeta * n)()
+    for i in range(n):
+        ms[i].old_offset[0], ms[i].old_offset[1] = meta["old_offset"][i]
+        for k in META_FIELDS:
+            setattr(ms[i], k, float(meta[k][i]))
+    fimg = np.zeros((n, cur, X), np.complex128)
+    fnm = np.zeros((n, cur, X), np.complex128)
+    fctf = np.zeros((n, cur, X))
+    power = np.zeros((n, N // 2 + 1))
+    xi2 = np.zeros(n)
+    off = np.zeros((n, 2))
+    st = o.oracle_prepare_images(C.byref(pp), I64(n), imgs.ctypes.data, ms, fimg.ctypes.data, fnm.ctypes.data,
+                                 fctf.ctypes.data, power.ctypes.data, xi2.ctypes.data, off.ctypes.data)
+    if st != 0:
+        raise RuntimeError("oracle_prepare_images failed with status %d" % st)
+    return dict(fimg=fimg, fimg_nomask=fnm, fctf=fctf, power_img=power, highres_Xi2=xi2, old_offset=off)

@@ -1004,4 +1004,171 @@ int oracle_expectation(const oracle_model *mp, int64_t n, const oracle_particle 
     return 0;
 }
 
+
+// ---------------------------------------------------------------------------
+// Image preparation: MlOptimiser::getFourierTransformsAndCtfs
+// (src/ml_optimiser.cpp:5840-6753) for 2D single-particle images, without
+// helical / multi-body / tomography branches, with --zero_mask (background
+// average outside the mask), no CTF padding, no MTF or aberration
+// corrections.  FFTs in double: an iterative radix-2 transform for
+// power-of-two sizes, a direct DFT otherwise.
+// ---------------------------------------------------------------------------
+static void fft1d(std::vector<Cplx> &a, bool inverse) {
+    const size_t n = a.size();
+    if (n && (n & (n - 1)) == 0) {
+        for (size_t i = 1, j = 0; i < n; ++i) {
+            size_t bit = n >> 1;
+            for (; j & bit; bit >>= 1) j ^= bit;
+            j ^= bit;
+            if (i < j) std::swap(a[i], a[j]);
+        }
+        for (size_t len = 2; len <= n; len <<= 1) {
+            const double ang = 2 * kPI / (double)len * (inverse ? 1 : -1);
+            for (size_t i = 0; i < n; i += len)
+                for (size_t k = 0; k < len / 2; ++k) {
+                    const double c = std::cos(ang * k), sn = std::sin(ang * k);
+                    Cplx u = a[i + k], v = a[i + k + len / 2];
+                    Cplx t{v.re * c - v.im * sn, v.re * sn + v.im * c};
+                    a[i + k] = Cplx{u.re + t.re, u.im + t.im};
+                    a[i + k + len / 2] = Cplx{u.re - t.re, u.im - t.im};
+                }
+        }
+        return;
+    }
+    std::vector<Cplx> out(n, Cplx{0, 0});
+    for (size_t k = 0; k < n; ++k)
+        for (size_t x = 0; x < n; ++x) {
+            const double ang = 2 * kPI * (double)((k * x) % n) / (double)n * (inverse ? 1 : -1);
+            out[k].re += a[x].re * std::cos(ang) - a[x].im * std::sin(ang);
+            out[k].im += a[x].re * std::sin(ang) + a[x].im * std::cos(ang);
+        }
+    a = out;
+}
+
+// FourierTransformer::FourierTransform of an N x N real image: FFTW half
+// layout [N][N/2+1], forward transform divided by N^2 (src/fftw.cpp:335-360).
+static std::vector<Cplx> rfft2_half(const std::vector<double> &img, long N) {
+    const long X = N / 2 + 1;
+    std::vector<Cplx> rows((size_t)N * X);
+    std::vector<Cplx> line(N);
+    for (long y = 0; y < N; ++y) {
+        for (long x = 0; x < N; ++x) line[x] = Cplx{img[(size_t)y * N + x], 0.};
+        fft1d(line, false);
+        for (long x = 0; x < X; ++x) rows[(size_t)y * X + x] = line[x];
+    }
+    for (long x = 0; x < X; ++x) {
+        for (long y = 0; y < N; ++y) line[y] = rows[(size_t)y * X + x];
+        fft1d(line, false);
+        for (long y = 0; y < N; ++y) {
+            rows[(size_t)y * X + x].re = line[y].re / ((double)N * N);
+            rows[(size_t)y * X + x].im = line[y].im / ((double)N * N);
+        }
+    }
+    return rows;
+}
+
+// CenterFFTbySign (src/fftw.h:390-403) on a [s][s/2+1] half transform
+static void center_by_sign(std::vector<Cplx> &F, long s) {
+    const long X = s / 2 + 1;
+    for (long i = 0; i < s; ++i)
+        for (long j = 0; j < X; ++j)
+            if ((i ^ j) & 1) {
+                F[(size_t)i * X + j].re = -F[(size_t)i * X + j].re;
+                F[(size_t)i * X + j].im = -F[(size_t)i * X + j].im;
+            }
+}
+
+int oracle_prepare_images(const oracle_prep_params *pp, int64_t n, const double *images,
+                          const oracle_image_meta *meta, double *fimg, double *fimg_nomask, double *fctf,
+                          double *power, double *highres_Xi2, double *old_offset_rounded) {
+    const long N = pp->ori_size, cur = pp->current_size, X = cur / 2 + 1, half = N / 2 + 1;
+    if (N <= 0 || cur <= 0 || cur > N || (N & 1) || (cur & 1)) return -1;
+    const long h = N / 2;  // Xmipp origin of an even N x N image: logical = index - N/2
+    for (long p = 0; p < n; ++p) {
+        const oracle_image_meta &mt = meta[p];
+        const double *in = images + (size_t)p * N * N;
+        std::vector<double> img((size_t)N * N, 0.);
+        // norm correction (:6200-6212)
+        const double f = pp->do_norm_correction ? pp->avg_norm_correction / mt.norm_correction : 1.;
+        // rounded old offset (:6054), integer selfTranslate without wrap (:6214-6219;
+        // src/transformations.h translate: V2(r) = V1(r - v), outside 0)
+        const int dx = r_round(mt.old_offset[0]), dy = r_round(mt.old_offset[1]);
+        old_offset_rounded[2 * p] = dx;
+        old_offset_rounded[2 * p + 1] = dy;
+        for (long y = 0; y < N; ++y)
+            for (long x = 0; x < N; ++x) {
+                const long sy = y - dy, sx = x - dx;
+                if (sy >= 0 && sy < N && sx >= 0 && sx < N) img[(size_t)y * N + x] = f * in[(size_t)sy * N + sx];
+            }
+        // unmasked Fourier image (:6233-6240)
+        std::vector<Cplx> Fa = rfft2_half(img, N);
+        std::vector<Cplx> Fw = window_ft(Fa.data(), N, cur);
+        center_by_sign(Fw, cur);
+        std::memcpy(fimg_nomask + (size_t)p * cur * X * 2, Fw.data(), sizeof(Cplx) * cur * X);
+        // soft mask with the average background (softMaskOutsideMap, src/mask.cpp:43-96)
+        const double radius = pp->mask_radius_px, radius_p = radius + pp->width_mask_edge;
+        double sum = 0., sum_bg = 0.;
+        for (long y = 0; y < N; ++y)
+            for (long x = 0; x < N; ++x) {
+                const double r = std::sqrt((double)((y - h) * (y - h) + (x - h) * (x - h)));
+                if (r < radius) continue;
+                if (r > radius_p) {
+                    sum += 1.;
+                    sum_bg += img[(size_t)y * N + x];
+                } else {
+                    const double rc = 0.5 + 0.5 * std::cos(kPI * (radius_p - r) / pp->width_mask_edge);
+                    sum += rc;
+                    sum_bg += rc * img[(size_t)y * N + x];
+                }
+            }
+        sum_bg /= sum;
+        for (long y = 0; y < N; ++y)
+            for (long x = 0; x < N; ++x) {
+                const double r = std::sqrt((double)((y - h) * (y - h) + (x - h) * (x - h)));
+                if (r < radius) continue;
+                double &v = img[(size_t)y * N + x];
+                if (r > radius_p) {
+                    v = sum_bg;
+                } else {
+                    const double rc = 0.5 + 0.5 * std::cos(kPI * (radius_p - r) / pp->width_mask_edge);
+                    v = (1 - rc) * v + rc * sum_bg;
+                }
+            }
+        // masked Fourier image, power spectrum and high-resolution power (:6320-6350)
+        Fa = rfft2_half(img, N);
+        double *pw = power + (size_t)p * half;
+        for (long i = 0; i < half; ++i) pw[i] = 0.;
+        double xi2 = 0.;
+        if (cur < N) {
+            for (long i = 0; i < N; ++i) {
+                const long ip = (i < half) ? i : i - N;
+                for (long j = 0; j < half; ++j) {
+                    const int ires = r_round(std::sqrt((double)(ip * ip + j * j)));
+                    if (ires > 0 && ires < half && !(j == 0 && ip < 0)) {
+                        const Cplx c = Fa[(size_t)i * half + j];
+                        const double nf = c.re * c.re + c.im * c.im;
+                        pw[ires] += nf;
+                        if (ires >= cur / 2 + 1) xi2 += nf;
+                    }
+                }
+            }
+        }
+        highres_Xi2[p] = xi2;
+        Fw = window_ft(Fa.data(), N, cur);
+        center_by_sign(Fw, cur);
+        std::memcpy(fimg + (size_t)p * cur * X * 2, Fw.data(), sizeof(Cplx) * cur * X);
+        // CTF image (CTF::getFftwImage, src/ctf.cpp:314-450: no padding,
+        // frequencies of the full box, FFTW half layout of the current size)
+        double *fc = fctf + (size_t)p * cur * X;
+        const double xs = (double)N * pp->pixel_size;
+        for (long i = 0; i < cur; ++i) {
+            const long ip = (i < X) ? i : i - cur;
+            for (long j = 0; j < X; ++j)
+                fc[(size_t)i * X + j] = oracle_ctf(mt.defU, mt.defV, mt.defAngle, pp->kV, pp->Cs, pp->Q0, mt.Bfac,
+                                                   mt.scale, mt.phase_shift, (double)j / xs, (double)ip / xs);
+        }
+    }
+    return 0;
+}
+
 }  // extern "C"

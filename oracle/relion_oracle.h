@@ -111,6 +111,34 @@ typedef struct {
 int oracle_expectation(const oracle_model *m, int64_t n, const oracle_particle *parts,
                        oracle_result *res, oracle_debug *dbg, oracle_wsum *wsum);
 
+/* --- image preparation (MlOptimiser::getFourierTransformsAndCtfs) -------- */
+typedef struct {
+    int64_t ori_size;            /* image_full_size                                 */
+    int64_t current_size;        /* image_current_size                              */
+    int64_t do_norm_correction;
+    int64_t pad_;
+    double pixel_size;
+    double mask_radius_px;       /* particle_diameter / (2 pixel)                   */
+    double width_mask_edge;      /* --width_mask_edge (pixels)                      */
+    double avg_norm_correction;
+    double kV, Cs, Q0;           /* optics group: voltage, spherical aberration, amplitude contrast */
+} oracle_prep_params;
+
+typedef struct {
+    double old_offset[2];        /* pixels, before rounding                         */
+    double norm_correction;
+    double defU, defV, defAngle; /* Angstrom, Angstrom, degrees                     */
+    double Bfac, scale, phase_shift;
+} oracle_image_meta;
+
+/* Real-space particle images [n][ori][ori] (row y, column x) -> the E-step
+ * inputs: masked and unmasked Fourier images [n][cur][cur/2+1][2], CTF
+ * images [n][cur][cur/2+1], power spectra [n][ori/2+1], highres_Xi2 [n] and
+ * the rounded old offsets [n][2]. */
+int oracle_prepare_images(const oracle_prep_params *pp, int64_t n, const double *images,
+                          const oracle_image_meta *meta, double *fimg, double *fimg_nomask, double *fctf,
+                          double *power, double *highres_Xi2, double *old_offset_rounded);
+
 /* --- building blocks exposed for unit checks --------------------------- */
 double oracle_ctf(double defU, double defV, double defAng, double kV, double Cs,
                   double Q0, double Bfac, double scale, double phase_shift,
