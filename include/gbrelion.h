@@ -169,6 +169,54 @@ int gbr_worker_set_debug(gbr_worker *w, int on);
  * backprojection into the bundle's volumes.  `res` has batch->n entries. */
 int gbr_expect_batch(gbr_worker *w, const gbr_particle_batch *batch, gbr_particle_result *res);
 
+/* ---- image preparation (the step before the search) ------------------- */
+
+/* Optics and masking of MlOptimiser::getFourierTransformsAndCtfs. */
+typedef struct {
+    double kV;                   /* optics group voltage (kV)                  */
+    double Cs;                   /* spherical aberration (mm)                  */
+    double Q0;                   /* amplitude contrast                         */
+    double particle_diameter;    /* --particle_diameter (Angstrom): the mask
+                                    radius is diameter / (2 pixel size)        */
+    double width_mask_edge;      /* --width_mask_edge (pixels, default 5)      */
+    double reserved_;
+} gbr_optics_desc;
+
+/* A batch of real-space particle images (2D, ori_size x ori_size). */
+typedef struct {
+    int64_t n;
+    int64_t device_resident;     /* 0: host arrays (copied in), 1: device      */
+    const float *images;         /* [n][ori][ori], row y, column x             */
+    const double *old_offset;    /* [n][2] pixels (rounded by the library, as
+                                    the reference does before shifting)        */
+    const double *prior;         /* [n][2] pixels                              */
+    const double *norm_correction;  /* [n] metadata NORM                       */
+    const double *scale;         /* [n] scale correction of the group          */
+    const double *ctf;           /* [n][6] defocusU, defocusV (Angstrom),
+                                    defocus angle (degrees), B-factor,
+                                    CTF scale, phase shift (degrees)           */
+} gbr_image_batch;
+
+/* Set the optics / mask parameters used by the two calls below. */
+int gbr_bundle_set_optics(gbr_bundle *b, const gbr_optics_desc *optics);
+
+/* MlOptimiser::getFourierTransformsAndCtfs (src/ml_optimiser.cpp:5840-6753;
+ * GPU variant src/acc/acc_ml_optimiser_impl.h:11-1013) for a batch, with
+ * --zero_mask semantics (average background outside the soft mask), no CTF
+ * padding and no MTF / aberration terms: norm correction, integer shift by
+ * the rounded old offset, FFT of the unmasked and masked image, window to
+ * the current size, power spectrum, high-resolution power and CTF image.
+ * Outputs are DEVICE arrays in gbr_particle_batch layout: fimg, fimg_nomask
+ * complex [n][cur][cur/2+1], fctf [n][cur][cur/2+1], power_img [n][ori/2+1],
+ * highres_Xi2 [n], old_offset_rounded [n][2]. */
+int gbr_prepare_images(gbr_worker *w, const gbr_image_batch *in, void *fimg, void *fimg_nomask, float *fctf,
+                       double *power_img, double *highres_Xi2, double *old_offset_rounded);
+
+/* gbr_prepare_images followed by gbr_expect_batch on its outputs: the E-step
+ * of a batch of raw images (the reference's per-particle image preparation
+ * plus accDoExpectationOneParticle). */
+int gbr_expect_images(gbr_worker *w, const gbr_image_batch *in, gbr_particle_result *res);
+
 /* Number of coarse directions / psi angles / translations of the sampling,
  * and the fine oversampling factors (HealpixSampling::NrDirections etc.). */
 int gbr_sampling_sizes(const gbr_bundle *b, int64_t *ndir, int64_t *npsi, int64_t *ntrans,

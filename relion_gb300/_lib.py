@@ -56,6 +56,15 @@ class Wsum(C.Structure):
                             "wsum_reference_power", "reserved_")]
 
 
+class OpticsDesc(C.Structure):
+    _fields_ = [(n, F64) for n in ("kV", "Cs", "Q0", "particle_diameter", "width_mask_edge", "reserved_")]
+
+
+class ImageBatch(C.Structure):
+    _fields_ = [("n", I64), ("device_resident", I64)] + \
+        [(n, P) for n in ("images", "old_offset", "prior", "norm_correction", "scale", "ctf")]
+
+
 EXPORTS = {
     "gbr_last_error": (C.c_size_t, [C.c_char_p, C.c_size_t]),
     "gbr_version": (C.c_char_p, []),
@@ -67,6 +76,9 @@ EXPORTS = {
     "gbr_worker_create": (C.c_int, [P, C.POINTER(P)]),
     "gbr_worker_set_debug": (C.c_int, [P, C.c_int]),
     "gbr_expect_batch": (C.c_int, [P, C.POINTER(ParticleBatch), P]),
+    "gbr_bundle_set_optics": (C.c_int, [P, C.POINTER(OpticsDesc)]),
+    "gbr_prepare_images": (C.c_int, [P, C.POINTER(ImageBatch), P, P, P, P, P, P]),
+    "gbr_expect_images": (C.c_int, [P, C.POINTER(ImageBatch), P]),
     "gbr_sampling_sizes": (C.c_int, [P] + [C.POINTER(I64)] * 5),
     "gbr_worker_debug_fetch": (I64, [P, C.c_int, I64, P, I64]),
     "gbr_backprojector_dims": (C.c_int, [P] + [C.POINTER(I64)] * 6),

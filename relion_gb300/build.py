@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libgbrelion.so")
-SOURCES = ["k_project.cu", "k_gemm.cu", "k_estep.cu", "estep.cu", "k_noalloc.cu", "k_tc.cu"]
+SOURCES = ["k_project.cu", "k_gemm.cu", "k_estep.cu", "estep.cu", "k_noalloc.cu", "k_tc.cu", "k_prepimg.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -54,7 +54,7 @@ def build(verbose=False, force=False):
     with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(one, SOURCES))
     tmp = LIB + ".tmp"
-    _run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"])
+    _run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart", "-lcufft"])
     os.replace(tmp, LIB)
     if verbose:
         print("built", LIB)

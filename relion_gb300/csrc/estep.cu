@@ -141,6 +141,9 @@ struct gbr_bundle {
     // model arrays (host copies)
     std::vector<double> sigma2, pdf_class, pdf_dir, dvp;
     bool have_arrays = false;
+    // image preparation (gbr_bundle_set_optics)
+    gbr_optics_desc optics{};
+    bool have_optics = false;
     // 2D classification (ref_dim 2): per-class offset priors and their sums
     bool is2d = false;
     int KP = 1;  // offset-prior rows per particle: K in 2D, 1 in 3D
@@ -228,6 +231,13 @@ struct gbr_worker {
     PinnedBuf<long long> h_totals, h_segf;
     PinnedBuf<ParticleState> h_ps;
     PinnedBuf<double> h_shell, h_pacc, h_pdat, h_power;
+    // image preparation: inputs, scratch, FFT plan and the prepared batch
+    DevBuf<float> pi_images, pi_A, pi_B, pi_factor, pi_fctf;
+    DevBuf<float2> pi_FA, pi_FB, pi_fimg, pi_fnm;
+    DevBuf<double> pi_bg, pi_ctf, pi_power, pi_xi2, pi_off, pi_prior, pi_norm, pi_scale;
+    DevBuf<int> pi_shift;
+    long long fft_plan = -1;
+    int fft_N = 0, fft_batch = 0;
     // dense fine pass
     int fine_mode = 0;  // 0: by significant density, 1: always dense, 2: always sparse
     int coarse_rows = 0;  // 0: skip far coarse rows by their minimum (tensor-core pass), 1: read all rows
@@ -1084,6 +1094,153 @@ int gbr_expect_batch(gbr_worker *w, const gbr_particle_batch *batch, gbr_particl
     return GBR_OK;
 }
 
+int gbr_bundle_set_optics(gbr_bundle *b, const gbr_optics_desc *optics) {
+    if (!b || !optics) return fail(GBR_ERR_INVALID, "null argument");
+    if (!(optics->kV > 0.) || optics->Q0 < 0. || optics->Q0 >= 1. || !(optics->particle_diameter > 0.) ||
+        !(optics->width_mask_edge > 0.))
+        return fail(GBR_ERR_INVALID, "invalid optics / mask parameters");
+    b->optics = *optics;
+    b->have_optics = true;
+    return GBR_OK;
+}
+
+namespace {
+
+// getFourierTransformsAndCtfs for a whole batch into the given device arrays.
+int prepare_images(gbr_worker *w, const gbr_image_batch *in, float2 *fimg, float2 *fnm, float *fctf, double *power,
+                   double *xi2, double *off_out) {
+    gbr_bundle *b = w->b;
+    if (!b->have_optics) return fail(GBR_ERR_STATE, "optics not set (gbr_bundle_set_optics)");
+    const int n = (int)in->n, N = (int)b->d.ori_size, cur = b->cur;
+    if (n <= 0) return GBR_OK;
+    if (n > 4096) return fail(GBR_ERR_INVALID, "gbr_prepare_images: at most 4096 images per call");
+    if (!in->images || !in->old_offset || !in->norm_correction || !in->ctf)
+        return fail(GBR_ERR_INVALID, "null image batch array");
+    cudaStream_t st = w->st;
+    const size_t npx = (size_t)n * N * N, nf = (size_t)n * N * (N / 2 + 1);
+    GBR_CUDA(w->pi_A.reserve(npx));
+    GBR_CUDA(w->pi_B.reserve(npx));
+    GBR_CUDA(w->pi_FA.reserve(nf));
+    GBR_CUDA(w->pi_FB.reserve(nf));
+    GBR_CUDA(w->pi_bg.reserve(n));
+    GBR_CUDA(w->pi_ctf.reserve((size_t)n * 6));
+    GBR_CUDA(w->pi_shift.reserve((size_t)n * 2));
+    GBR_CUDA(w->pi_factor.reserve(n));
+    // rounded old offsets (selfROUND, src/ml_optimiser.cpp:6054) and norm factors on the host
+    std::vector<double> off((size_t)n * 2), nc(n);
+    const cudaMemcpyKind kind = in->device_resident ? cudaMemcpyDeviceToHost : cudaMemcpyHostToHost;
+    GBR_CUDA(cudaMemcpy(off.data(), in->old_offset, sizeof(double) * 2 * n, kind));
+    GBR_CUDA(cudaMemcpy(nc.data(), in->norm_correction, sizeof(double) * n, kind));
+    std::vector<int> sh((size_t)n * 2);
+    std::vector<float> fac(n);
+    std::vector<double> offr((size_t)n * 2);
+    for (int p = 0; p < n; ++p) {
+        for (int k = 0; k < 2; ++k) {
+            const double v = off[2 * p + k];
+            sh[2 * p + k] = v > 0 ? (int)(v + 0.5) : (int)(v - 0.5);
+            offr[2 * p + k] = sh[2 * p + k];
+        }
+        fac[p] = b->d.do_norm_correction ? (float)(b->d.avg_norm_correction / nc[p]) : 1.f;
+    }
+    GBR_CUDA(cudaMemcpyAsync(w->pi_shift.p, sh.data(), sizeof(int) * sh.size(), cudaMemcpyHostToDevice, st));
+    GBR_CUDA(cudaMemcpyAsync(w->pi_factor.p, fac.data(), sizeof(float) * n, cudaMemcpyHostToDevice, st));
+    GBR_CUDA(cudaMemcpyAsync(off_out, offr.data(), sizeof(double) * offr.size(), cudaMemcpyHostToDevice, st));
+    GBR_CUDA(cudaMemcpyAsync(w->pi_ctf.p, in->ctf, sizeof(double) * 6 * n,
+                             in->device_resident ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st));
+    const float *imgs = in->images;
+    if (!in->device_resident) {
+        GBR_CUDA(w->pi_images.reserve(npx));
+        GBR_CUDA(cudaMemcpyAsync(w->pi_images.p, in->images, sizeof(float) * npx, cudaMemcpyHostToDevice, st));
+        imgs = w->pi_images.p;
+    }
+    if (w->fft_plan < 0 || w->fft_N != N || w->fft_batch != n) {
+        if (w->fft_plan >= 0) destroy_fft_plan(w->fft_plan);
+        w->fft_plan = -1;
+        if (make_fft_plan(N, n, &w->fft_plan)) return fail(GBR_ERR_CUDA, "cuFFT plan creation failed");
+        w->fft_N = N;
+        w->fft_batch = n;
+    }
+    PrepImagesArgs a{};
+    a.n = n;
+    a.N = N;
+    a.cur = cur;
+    a.images = imgs;
+    a.shift = w->pi_shift.p;
+    a.factor = w->pi_factor.p;
+    a.ctf = w->pi_ctf.p;
+    a.pixel = b->d.pixel_size;
+    a.kV = b->optics.kV;
+    a.Cs = b->optics.Cs;
+    a.Q0 = b->optics.Q0;
+    a.mask_radius = b->optics.particle_diameter / (2. * b->d.pixel_size);
+    a.mask_width = b->optics.width_mask_edge;
+    a.A = w->pi_A.p;
+    a.B = w->pi_B.p;
+    a.FA = w->pi_FA.p;
+    a.FB = w->pi_FB.p;
+    a.bg = w->pi_bg.p;
+    a.fft_plan = w->fft_plan;
+    a.fimg = fimg;
+    a.fimg_nomask = fnm;
+    a.fctf = fctf;
+    a.power = power;
+    a.xi2 = xi2;
+    GBR_CUDA(launch_prepare_images(a, st));
+    w->launches += 8;
+    return GBR_OK;
+}
+
+}  // namespace
+
+int gbr_prepare_images(gbr_worker *w, const gbr_image_batch *in, void *fimg, void *fimg_nomask, float *fctf,
+                       double *power_img, double *highres_Xi2, double *old_offset_rounded) {
+    if (!w || !in || !fimg || !fimg_nomask || !fctf || !power_img || !highres_Xi2 || !old_offset_rounded)
+        return fail(GBR_ERR_INVALID, "null argument");
+    GBR_CUDA(cudaSetDevice(w->b->device));
+    int s = prepare_images(w, in, static_cast<float2 *>(fimg), static_cast<float2 *>(fimg_nomask), fctf, power_img,
+                           highres_Xi2, old_offset_rounded);
+    if (s) return s;
+    GBR_CUDA(cudaStreamSynchronize(w->st));
+    return GBR_OK;
+}
+
+int gbr_expect_images(gbr_worker *w, const gbr_image_batch *in, gbr_particle_result *res) {
+    if (!w || !in || !res) return fail(GBR_ERR_INVALID, "null argument");
+    if (in->n == 0) return GBR_OK;
+    if (!in->prior || !in->scale) return fail(GBR_ERR_INVALID, "null image batch array");
+    gbr_bundle *b = w->b;
+    GBR_CUDA(cudaSetDevice(b->device));
+    const size_t n = (size_t)in->n, cur = (size_t)b->cur, X = cur / 2 + 1, half = (size_t)b->nshell;
+    GBR_CUDA(w->pi_fimg.reserve(n * cur * X));
+    GBR_CUDA(w->pi_fnm.reserve(n * cur * X));
+    GBR_CUDA(w->pi_fctf.reserve(n * cur * X));
+    GBR_CUDA(w->pi_power.reserve(n * half));
+    GBR_CUDA(w->pi_xi2.reserve(n));
+    GBR_CUDA(w->pi_off.reserve(2 * n));
+    GBR_CUDA(w->pi_prior.reserve(2 * n));
+    GBR_CUDA(w->pi_norm.reserve(n));
+    GBR_CUDA(w->pi_scale.reserve(n));
+    int s = prepare_images(w, in, w->pi_fimg.p, w->pi_fnm.p, w->pi_fctf.p, w->pi_power.p, w->pi_xi2.p, w->pi_off.p);
+    if (s) return s;
+    const cudaMemcpyKind kind = in->device_resident ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    GBR_CUDA(cudaMemcpyAsync(w->pi_prior.p, in->prior, sizeof(double) * 2 * n, kind, w->st));
+    GBR_CUDA(cudaMemcpyAsync(w->pi_norm.p, in->norm_correction, sizeof(double) * n, kind, w->st));
+    GBR_CUDA(cudaMemcpyAsync(w->pi_scale.p, in->scale, sizeof(double) * n, kind, w->st));
+    gbr_particle_batch pb{};
+    pb.n = in->n;
+    pb.device_resident = 1;
+    pb.fimg = reinterpret_cast<const float *>(w->pi_fimg.p);
+    pb.fimg_nomask = reinterpret_cast<const float *>(w->pi_fnm.p);
+    pb.fctf = w->pi_fctf.p;
+    pb.power_img = w->pi_power.p;
+    pb.old_offset = w->pi_off.p;
+    pb.prior = w->pi_prior.p;
+    pb.highres_Xi2 = w->pi_xi2.p;
+    pb.norm_correction = w->pi_norm.p;
+    pb.scale = w->pi_scale.p;
+    return gbr_expect_batch(w, &pb, res);
+}
+
 int gbr_sampling_sizes(const gbr_bundle *b, int64_t *ndir, int64_t *npsi, int64_t *ntrans, int64_t *nover_rot,
                        int64_t *nover_trans) {
     if (!b) return fail(GBR_ERR_INVALID, "null bundle");
@@ -1260,6 +1417,7 @@ int gbr_worker_destroy(gbr_worker *w) {
     for (int i = 0; i <= ST_N; ++i)
         if (w->ev[i]) cudaEventDestroy(w->ev[i]);
     if (w->ev_in) cudaEventDestroy(w->ev_in);
+    if (w->fft_plan >= 0) destroy_fft_plan(w->fft_plan);
     if (w->st) cudaStreamDestroy(w->st);
     delete w;
     return GBR_OK;

@@ -211,6 +211,27 @@ struct WsumArgs {
     double *w_prior_off;       // [K][2] 2D: sum w pixel (old offset + shift), else null
 };
 cudaError_t launch_wsum(const WsumArgs &a, cudaStream_t st);
+// Image preparation (getFourierTransformsAndCtfs) of n real-space images of
+// N x N pixels into the E-step inputs of the current size `cur`.
+struct PrepImagesArgs {
+    int n, N, cur;
+    const float *images;   // [n][N][N] row y, column x (device)
+    const int *shift;      // [n][2] rounded old offset (dx, dy)
+    const float *factor;   // [n] norm-correction factor (1 without --norm)
+    const double *ctf;     // [n][6] defU, defV, defAngle, Bfac, scale, phase shift
+    double pixel, kV, Cs, Q0, mask_radius, mask_width;
+    float *A, *B;          // [n][N][N] scratch: shifted, masked
+    float2 *FA, *FB;       // [n][N][N/2+1] scratch: their transforms
+    double *bg;            // [n] scratch: mask background
+    long long fft_plan;    // batched N x N R2C plan (make_fft_plan)
+    float2 *fimg, *fimg_nomask;  // [n][cur][cur/2+1]
+    float *fctf;                 // [n][cur][cur/2+1]
+    double *power, *xi2;         // [n][N/2+1], [n]
+};
+cudaError_t launch_prepare_images(const PrepImagesArgs &a, cudaStream_t st);
+int make_fft_plan(int N, int batch, long long *plan_out);
+void destroy_fft_plan(long long plan);
+
 cudaError_t launch_compact_flags(const unsigned char *flags, int n, int *list, int *count,
                                  cudaStream_t st);
 cudaError_t launch_backproject(const int *list, const int *count, int max_list, const float *eul_f, int nOR,

@@ -426,3 +426,49 @@ class Dataset:
             scale=np.ones(count), true_rot=R.numpy(), true_shift=shifts.numpy(),
             true_class=labels.numpy(), true_psi=None if true_psi is None else true_psi.numpy(),
             defocus=np.stack([dU.numpy(), dV.numpy(), dA.numpy()], 1))
+
+    def particle_images(self, start=0, count=None):
+        """Real-space particle images [n][box][box] (float32) of the same
+        particles as particles(start, count): the full-box Fourier image
+        (slice x CTF x shift + noise) transformed back with the image centre
+        at box/2 and the forward-FFT normalisation 1/box^2 undone, with the
+        per-particle CTF parameters and metadata of the image preparation."""
+        c = self.cfg
+        if self.sigma2 is None:
+            self._noise_level()
+        count = self.n - start if count is None else count
+        box, pix = c["box"], c["pixel"]
+        g = torch.Generator().manual_seed(self.seed * 1000003 + start)
+        K = len(self.vols)
+        if self.is2d:
+            labels = torch.randint(K, (count,), generator=g) if K > 1 else torch.zeros(count, dtype=torch.long)
+            psi = 360.0 * torch.rand(count, generator=g, dtype=torch.float64)
+            R = inplane_matrices(psi) @ self.class_R[labels]
+        else:
+            R = random_rotations(count, g)
+            labels = torch.randint(K, (count,), generator=g) if K > 1 else torch.zeros(count, dtype=torch.long)
+        shifts = (torch.rand(count, 2, generator=g, dtype=torch.float64) * 2 - 1) * c["max_shift"]
+        dlo, dhi = c["defocus"]
+        dU = dlo + (dhi - dlo) * torch.rand(count, generator=g, dtype=torch.float64)
+        dV = dlo + (dhi - dlo) * torch.rand(count, generator=g, dtype=torch.float64)
+        dA = 180.0 * torch.rand(count, generator=g, dtype=torch.float64)
+        x, y = fourier_grid(box)
+        k2 = torch.stack([x, y, torch.zeros_like(x)], -1) / box
+        i = torch.arange(box)[:, None]
+        j = torch.arange(box // 2 + 1)[None, :]
+        sign = 1.0 - 2.0 * ((i + j) % 2).to(torch.float64)
+        s = math.sqrt(self.sigma2 / 2)
+        imgs = np.zeros((count, box, box), np.float32)
+        for n in range(count):
+            f = self.vols[int(labels[n])].ft(k2 @ R[n]).cpu()
+            ctf = ctf_value(float(dU[n]), float(dV[n]), float(dA[n]), x / (box * pix), y / (box * pix))
+            ph = torch.exp(-2j * math.pi * (x * shifts[n, 0] + y * shifts[n, 1]) / box)
+            noise = torch.complex(torch.randn(box, box // 2 + 1, generator=g, dtype=torch.float64),
+                                  torch.randn(box, box // 2 + 1, generator=g, dtype=torch.float64)) * s
+            F = (f * ctf * ph + noise) * sign
+            imgs[n] = (torch.fft.irfft2(F, s=(box, box)) * box * box).numpy()
+        ctfp = np.stack([dU.numpy(), dV.numpy(), dA.numpy(), np.zeros(count), np.ones(count), np.zeros(count)], 1)
+        return dict(n=count, images=imgs, old_offset=np.zeros((count, 2)), prior=np.zeros((count, 2)),
+                    norm_correction=np.ones(count), scale=np.ones(count), ctf=ctfp,
+                    true_rot=R.numpy(), true_shift=shifts.numpy(), true_class=labels.numpy())
+

@@ -37,6 +37,7 @@ class MlDeviceBundle:
         check(self.lib.gbr_sampling_sizes(h, *[C.byref(s) for s in sz]))
         self.ndir, self.npsi, self.ntrans, self.nover_rot, self.nover_trans = [s.value for s in sz]
         self.nr_classes = int(model["nr_classes"])
+        self.device = int(device)
         self.ori_size = int(model["ori_size"])
         self._keep = []
         s2 = _lib.as_f64(model["sigma2_noise"])
@@ -48,6 +49,11 @@ class MlDeviceBundle:
         self.ref_dim = int(model.get("ref_dim", 3) or 3)
         if self.ref_dim == 2 and model.get("prior_offset_class") is not None:
             self.set_class_offsets(model["prior_offset_class"])
+
+    # optics group and mask of the image preparation
+    def set_optics(self, kV=300.0, Cs=2.7, Q0=0.1, particle_diameter=200.0, width_mask_edge=5.0):
+        o = _lib.OpticsDesc(kV, Cs, Q0, particle_diameter, width_mask_edge, 0.0)
+        check(self.lib.gbr_bundle_set_optics(self.h, C.byref(o)))
 
     # 2D classification: mymodel.prior_offset_class [K][2]
     def set_class_offsets(self, prior_offset_class):
@@ -162,6 +168,49 @@ class MlOptimiserCuda:
                 setattr(b, k, arr(batch[k], np.float64))
         out = np.zeros(n, dtype=RESULT_DTYPE)
         check(self.lib.gbr_expect_batch(self.h, C.byref(b), out.ctypes.data))
+        return out
+
+    def _image_batch(self, batch, keep):
+        b = _lib.ImageBatch()
+        b.n = len(batch["images"])
+
+        def arr(a, dt):
+            a = np.ascontiguousarray(a, dtype=dt)
+            keep.append(a)
+            return a.ctypes.data
+        b.images = arr(batch["images"], np.float32)
+        for k in ("old_offset", "prior", "norm_correction", "scale", "ctf"):
+            setattr(b, k, arr(batch[k], np.float64))
+        return b
+
+    def prepare_images(self, batch):
+        """getFourierTransformsAndCtfs for a batch of host images (dict:
+        images [n][ori][ori], old_offset, prior [n][2], norm_correction,
+        scale [n], ctf [n][6]); returns the E-step inputs as numpy arrays
+        (computed on the device, copied back)."""
+        import torch
+        keep = []
+        b = self._image_batch(batch, keep)
+        n, cur = b.n, int(self.bundle.desc.current_size)
+        X, half = cur // 2 + 1, self.bundle.ori_size // 2 + 1
+        dev = torch.device("cuda", self.bundle.device)
+        out = dict(fimg=torch.empty((n, cur, X), dtype=torch.complex64, device=dev),
+                   fimg_nomask=torch.empty((n, cur, X), dtype=torch.complex64, device=dev),
+                   fctf=torch.empty((n, cur, X), dtype=torch.float32, device=dev),
+                   power_img=torch.empty((n, half), dtype=torch.float64, device=dev),
+                   highres_Xi2=torch.empty(n, dtype=torch.float64, device=dev),
+                   old_offset=torch.empty((n, 2), dtype=torch.float64, device=dev))
+        check(self.lib.gbr_prepare_images(self.h, C.byref(b), *[out[k].data_ptr() for k in (
+            "fimg", "fimg_nomask", "fctf", "power_img", "highres_Xi2", "old_offset")]))
+        return {k: v.cpu().numpy() for k, v in out.items()}
+
+    def do_expectation_images(self, batch):
+        """Image preparation and E-step of a batch of raw images in one call
+        (gbr_expect_images); returns the result rows."""
+        keep = []
+        b = self._image_batch(batch, keep)
+        out = np.zeros(b.n, dtype=RESULT_DTYPE)
+        check(self.lib.gbr_expect_images(self.h, C.byref(b), out.ctypes.data))
         return out
 
     def debug_fetch(self, what, i):
