@@ -250,7 +250,8 @@ int gbr_bundle_reset_wsum(gbr_bundle *b);
  * (CUDA events on the worker's stream: prep, norm, cross term, coarse
  * weights, significance + job list, fine diff2, fine weights, weighted sums,
  * backprojection, read-back), then the input copies of each batch (device
- * time before the first stage) and the host finalisation of the results. */
+ * time before the first stage), the host finalisation of the results, and
+ * for gbr_expect_images the image upload and the image preparation. */
 int gbr_worker_stage_times(const gbr_worker *w, double *ms, int64_t n, int64_t *n_written);
 
 /* Number of CUDA kernels this worker has launched (all batches so far). */

@@ -191,8 +191,10 @@ struct gbr_worker {
     gbr_bundle *b = nullptr;
     cudaStream_t st = nullptr;
     cudaEvent_t ev[ST_N + 1] = {};
-    double stage_ms[ST_N + 2] = {};  // device stages, then input copies and host finalisation
+    double stage_ms[ST_N + 4] = {};  // device stages, input copies, host finalisation,
+                                     // image upload and image preparation
     cudaEvent_t ev_in = nullptr;     // start of the batch's input copies
+    cudaEvent_t ev_img[3] = {};      // image upload start, preparation start, end
     int debug = 0;
     int cap = 0;  // particles the batch buffers hold
     long long launches = 0;  // kernels launched by this worker
@@ -232,7 +234,8 @@ struct gbr_worker {
     PinnedBuf<ParticleState> h_ps;
     PinnedBuf<double> h_shell, h_pacc, h_pdat, h_power;
     // image preparation: inputs, scratch, FFT plan and the prepared batch
-    DevBuf<float> pi_images, pi_A, pi_B, pi_factor, pi_fctf;
+    DevBuf<float> pi_images, pi_A, pi_B, pi_factor, pi_fctf, pi_W;
+    double pi_W_key[3] = {0., 0., 0.};  // N, radius, width of the cached mask weights
     DevBuf<float2> pi_FA, pi_FB, pi_fimg, pi_fnm;
     DevBuf<double> pi_bg, pi_ctf, pi_power, pi_xi2, pi_off, pi_prior, pi_norm, pi_scale;
     DevBuf<int> pi_shift;
@@ -1015,6 +1018,7 @@ int gbr_worker_create(gbr_bundle *b, gbr_worker **out) {
     GBR_CUDA(cudaStreamCreateWithFlags(&w->st, cudaStreamNonBlocking));
     for (int i = 0; i <= ST_N; ++i) GBR_CUDA(cudaEventCreate(&w->ev[i]));
     GBR_CUDA(cudaEventCreate(&w->ev_in));
+    for (auto &ev : w->ev_img) GBR_CUDA(cudaEventCreate(&ev));
     const char *dbg = std::getenv("GBR_DEBUG_FETCH");
     w->debug = dbg && dbg[0] == '1';
     const char *fm = std::getenv("GBR_FINE_MODE");
@@ -1122,7 +1126,8 @@ int prepare_images(gbr_worker *w, const gbr_image_batch *in, float2 *fimg, float
     GBR_CUDA(w->pi_B.reserve(npx));
     GBR_CUDA(w->pi_FA.reserve(nf));
     GBR_CUDA(w->pi_FB.reserve(nf));
-    GBR_CUDA(w->pi_bg.reserve(n));
+    GBR_CUDA(w->pi_bg.reserve((size_t)2 * n));
+    GBR_CUDA(w->pi_W.reserve((size_t)N * N));
     GBR_CUDA(w->pi_ctf.reserve((size_t)n * 6));
     GBR_CUDA(w->pi_shift.reserve((size_t)n * 2));
     GBR_CUDA(w->pi_factor.reserve(n));
@@ -1148,11 +1153,13 @@ int prepare_images(gbr_worker *w, const gbr_image_batch *in, float2 *fimg, float
     GBR_CUDA(cudaMemcpyAsync(w->pi_ctf.p, in->ctf, sizeof(double) * 6 * n,
                              in->device_resident ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st));
     const float *imgs = in->images;
+    GBR_CUDA(cudaEventRecord(w->ev_img[0], st));
     if (!in->device_resident) {
         GBR_CUDA(w->pi_images.reserve(npx));
         GBR_CUDA(cudaMemcpyAsync(w->pi_images.p, in->images, sizeof(float) * npx, cudaMemcpyHostToDevice, st));
         imgs = w->pi_images.p;
     }
+    GBR_CUDA(cudaEventRecord(w->ev_img[1], st));
     if (w->fft_plan < 0 || w->fft_N != N || w->fft_batch != n) {
         if (w->fft_plan >= 0) destroy_fft_plan(w->fft_plan);
         w->fft_plan = -1;
@@ -1179,6 +1186,11 @@ int prepare_images(gbr_worker *w, const gbr_image_batch *in, float2 *fimg, float
     a.FA = w->pi_FA.p;
     a.FB = w->pi_FB.p;
     a.bg = w->pi_bg.p;
+    a.W = w->pi_W.p;
+    a.mask_fresh = (w->pi_W_key[0] != N || w->pi_W_key[1] != a.mask_radius || w->pi_W_key[2] != a.mask_width) ? 1 : 0;
+    w->pi_W_key[0] = N;
+    w->pi_W_key[1] = a.mask_radius;
+    w->pi_W_key[2] = a.mask_width;
     a.fft_plan = w->fft_plan;
     a.fimg = fimg;
     a.fimg_nomask = fnm;
@@ -1186,7 +1198,8 @@ int prepare_images(gbr_worker *w, const gbr_image_batch *in, float2 *fimg, float
     a.power = power;
     a.xi2 = xi2;
     GBR_CUDA(launch_prepare_images(a, st));
-    w->launches += 8;
+    GBR_CUDA(cudaEventRecord(w->ev_img[2], st));
+    w->launches += 6 + a.mask_fresh;  // own kernels (the cuFFT launches are the library's)
     return GBR_OK;
 }
 
@@ -1222,6 +1235,12 @@ int gbr_expect_images(gbr_worker *w, const gbr_image_batch *in, gbr_particle_res
     GBR_CUDA(w->pi_scale.reserve(n));
     int s = prepare_images(w, in, w->pi_fimg.p, w->pi_fnm.p, w->pi_fctf.p, w->pi_power.p, w->pi_xi2.p, w->pi_off.p);
     if (s) return s;
+    GBR_CUDA(cudaEventSynchronize(w->ev_img[2]));
+    float t0 = 0.f, t1 = 0.f;
+    cudaEventElapsedTime(&t0, w->ev_img[0], w->ev_img[1]);
+    cudaEventElapsedTime(&t1, w->ev_img[1], w->ev_img[2]);
+    w->stage_ms[ST_N + 2] += t0;
+    w->stage_ms[ST_N + 3] += t1;
     const cudaMemcpyKind kind = in->device_resident ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     GBR_CUDA(cudaMemcpyAsync(w->pi_prior.p, in->prior, sizeof(double) * 2 * n, kind, w->st));
     GBR_CUDA(cudaMemcpyAsync(w->pi_norm.p, in->norm_correction, sizeof(double) * n, kind, w->st));
@@ -1388,7 +1407,7 @@ int gbr_bundle_reset_wsum(gbr_bundle *b) {
 
 int gbr_worker_stage_times(const gbr_worker *w, double *ms, int64_t n, int64_t *n_written) {
     if (!w || !ms) return fail(GBR_ERR_INVALID, "null argument");
-    const int64_t m = std::min<int64_t>(n, ST_N + 2);
+    const int64_t m = std::min<int64_t>(n, ST_N + 4);
     for (int64_t i = 0; i < m; ++i) ms[i] = w->stage_ms[i];
     if (n_written) *n_written = m;
     return GBR_OK;
@@ -1417,6 +1436,8 @@ int gbr_worker_destroy(gbr_worker *w) {
     for (int i = 0; i <= ST_N; ++i)
         if (w->ev[i]) cudaEventDestroy(w->ev[i]);
     if (w->ev_in) cudaEventDestroy(w->ev_in);
+    for (auto &ev : w->ev_img)
+        if (ev) cudaEventDestroy(ev);
     if (w->fft_plan >= 0) destroy_fft_plan(w->fft_plan);
     if (w->st) cudaStreamDestroy(w->st);
     delete w;

@@ -222,7 +222,9 @@ struct PrepImagesArgs {
     double pixel, kV, Cs, Q0, mask_radius, mask_width;
     float *A, *B;          // [n][N][N] scratch: shifted, masked
     float2 *FA, *FB;       // [n][N][N/2+1] scratch: their transforms
-    double *bg;            // [n] scratch: mask background
+    double *bg;            // [n][2] scratch: mask background sums (sum w v, sum w)
+    float *W;              // [N][N] background weights of the soft mask
+    int mask_fresh;        // 1: (re)compute W for this geometry
     long long fft_plan;    // batched N x N R2C plan (make_fft_plan)
     float2 *fimg, *fimg_nomask;  // [n][cur][cur/2+1]
     float *fctf;                 // [n][cur][cur/2+1]

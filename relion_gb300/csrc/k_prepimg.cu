@@ -17,22 +17,6 @@ namespace {
 
 constexpr double kPiD = 3.14159265358979323846;
 
-// A[p][y][x] = f_p in[p][y - dy_p][x - dx_p], 0 where the source is outside
-// (translate with DONT_WRAP, src/transformations.h; V2(r) = V1(r - v)).
-__global__ void k_img_shift(const float *__restrict__ in, int N, const int *__restrict__ shift,
-                            const float *__restrict__ factor, float *__restrict__ A) {
-    const int p = blockIdx.y;
-    const int dx = shift[2 * p], dy = shift[2 * p + 1];
-    const float f = factor[p];
-    const float *src = in + (size_t)p * N * N;
-    float *dst = A + (size_t)p * N * N;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N * N; i += gridDim.x * blockDim.x) {
-        const int y = i / N, x = i - y * N;
-        const int sy = y - dy, sx = x - dx;
-        dst[i] = (sy >= 0 && sy < N && sx >= 0 && sx < N) ? f * src[(size_t)sy * N + sx] : 0.f;
-    }
-}
-
 // Raised-cosine weight of the background at radius r (softMaskOutsideMap,
 // src/mask.cpp:43-96): 0 inside `radius`, 1 beyond radius + width.
 __device__ __forceinline__ double bg_weight(double r, double radius, double width) {
@@ -42,47 +26,69 @@ __device__ __forceinline__ double bg_weight(double r, double radius, double widt
     return 0.5 + 0.5 * cos(kPiD * (rp - r) / width);
 }
 
-// Average background value per particle (one block per particle).
-__global__ void k_mask_bg(const float *__restrict__ A, int N, double radius, double width, double *__restrict__ bg) {
-    __shared__ double s_sum[32], s_w[32];
-    const int p = blockIdx.x, h = N / 2;
-    const float *img = A + (size_t)p * N * N;
-    double sw = 0., sv = 0.;
-    for (int i = threadIdx.x; i < N * N; i += blockDim.x) {
+// Raised-cosine background weights of the N x N box, once per geometry.
+__global__ void k_mask_weights(int N, double radius, double width, float *__restrict__ W) {
+    const int h = N / 2;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N * N; i += gridDim.x * blockDim.x) {
         const int y = i / N - h, x = i % N - h;
-        const double w = bg_weight(sqrt((double)(y * y + x * x)), radius, width);
-        sw += w;
-        sv += w * (double)img[i];
+        W[i] = (float)bg_weight(sqrt((double)(y * y + x * x)), radius, width);
     }
+}
+
+// A[p][y][x] = f_p in[p][y - dy_p][x - dx_p], 0 where the source is outside
+// (translate with DONT_WRAP, src/transformations.h; V2(r) = V1(r - v)),
+// together with the weighted background sums of the soft mask (sum w A,
+// sum w): a few pixels per thread in FP32, FP64 across threads and blocks.
+__global__ void k_img_shift_bg(const float *__restrict__ in, int N, const int *__restrict__ shift,
+                               const float *__restrict__ factor, const float *__restrict__ W,
+                               float *__restrict__ A, double *__restrict__ sums) {
+    __shared__ double s_v[32], s_w[32];
+    const int p = blockIdx.y;
+    const int dx = shift[2 * p], dy = shift[2 * p + 1];
+    const float f = factor[p];
+    const float *src = in + (size_t)p * N * N;
+    float *dst = A + (size_t)p * N * N;
+    float fw = 0.f, fv = 0.f;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N * N; i += gridDim.x * blockDim.x) {
+        const int y = i / N, x = i - y * N;
+        const int sy = y - dy, sx = x - dx;
+        const float v = (sy >= 0 && sy < N && sx >= 0 && sx < N) ? f * src[(size_t)sy * N + sx] : 0.f;
+        dst[i] = v;
+        const float w = W[i];
+        fw += w;
+        fv = fmaf(w, v, fv);
+    }
+    double sw = fw, sv = fv;
     for (int o = 16; o > 0; o >>= 1) {
         sw += __shfl_xor_sync(0xffffffffu, sw, o);
         sv += __shfl_xor_sync(0xffffffffu, sv, o);
     }
     if ((threadIdx.x & 31) == 0) {
         s_w[threadIdx.x >> 5] = sw;
-        s_sum[threadIdx.x >> 5] = sv;
+        s_v[threadIdx.x >> 5] = sv;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
         double tw = 0., tv = 0.;
         for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {
             tw += s_w[i];
-            tv += s_sum[i];
+            tv += s_v[i];
         }
-        bg[p] = tw > 0. ? tv / tw : 0.;
+        atomicAdd(&sums[2 * p], tv);
+        atomicAdd(&sums[2 * p + 1], tw);
     }
 }
 
-__global__ void k_mask_apply(const float *__restrict__ A, int N, double radius, double width,
-                             const double *__restrict__ bg, float *__restrict__ B) {
-    const int p = blockIdx.y, h = N / 2;
+__global__ void k_mask_apply(const float *__restrict__ A, int N, const float *__restrict__ W,
+                             const double *__restrict__ sums, float *__restrict__ B) {
+    const int p = blockIdx.y;
     const float *src = A + (size_t)p * N * N;
     float *dst = B + (size_t)p * N * N;
-    const double b = bg[p];
+    const double sw = sums[2 * p + 1];
+    const float b = (float)(sw > 0. ? sums[2 * p] / sw : 0.);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N * N; i += gridDim.x * blockDim.x) {
-        const int y = i / N - h, x = i % N - h;
-        const double w = bg_weight(sqrt((double)(y * y + x * x)), radius, width);
-        dst[i] = (float)((1. - w) * (double)src[i] + w * b);
+        const float w = W[i];
+        dst[i] = (1.f - w) * src[i] + w * b;
     }
 }
 
@@ -101,78 +107,99 @@ __global__ void k_window_center(const float2 *__restrict__ F, int N, int cur, fl
     }
 }
 
-// Power spectrum per shell and power beyond the current size (one block per
-// particle, shells in shared memory).
+// Power spectrum per shell and power beyond the current size: blocks over
+// row chunks of each particle, shells in shared memory, then global atomics
+// (power and xi2 zeroed by the caller).
 __global__ void k_img_spectrum(const float2 *__restrict__ F, int N, int cur, double *__restrict__ power,
                                double *__restrict__ xi2) {
-    extern __shared__ double s_pw[];  // [half]
-    const int p = blockIdx.x, half = N / 2 + 1;
-    for (int i = threadIdx.x; i < half; i += blockDim.x) s_pw[i] = 0.;
+    // FP32 partial sums per block (a chunk of N / gridDim.x rows: at most a
+    // few hundred terms per shell), FP64 across blocks
+    extern __shared__ float s_pw[];  // [half]
+    const int p = blockIdx.y, half = N / 2 + 1;
+    for (int i = threadIdx.x; i < half; i += blockDim.x) s_pw[i] = 0.f;
     __syncthreads();
-    const double inv = 1. / ((double)N * (double)N);
-    if (cur < N) {
-        for (int e = threadIdx.x; e < N * half; e += blockDim.x) {
-            const int i = e / half, j = e - i * half;
-            const int ip = i < half ? i : i - N;
-            const int ires = (int)floor(sqrt((double)(ip * ip + j * j)) + 0.5);
-            if (ires > 0 && ires < half && !(j == 0 && ip < 0)) {
-                const float2 v = F[(size_t)p * N * half + e];
-                const double re = (double)v.x * inv, im = (double)v.y * inv;
-                atomicAdd(&s_pw[ires], re * re + im * im);
+    const float inv = 1.f / ((float)N * (float)N);
+    // each thread takes runs of kRun consecutive x of one row and merges
+    // neighbours that fall in the same shell before its shared atomic
+    constexpr int kRun = 8;
+    const int runs_per_row = (half + kRun - 1) / kRun;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < N * runs_per_row; q += gridDim.x * blockDim.x) {
+        const int i = q / runs_per_row, j0 = (q - i * runs_per_row) * kRun;
+        const int ip = i < half ? i : i - N;
+        const float2 *row = F + ((size_t)p * N + i) * half;
+        int cur_s = -1;
+        float acc = 0.f;
+        for (int j = j0; j < j0 + kRun && j < half; ++j) {
+            const int ires = (int)floorf(sqrtf((float)(ip * ip + j * j)) + 0.5f);
+            if (!(ires > 0 && ires < half && !(j == 0 && ip < 0))) continue;
+            const float2 v = row[j];
+            const float re = v.x * inv, im = v.y * inv;
+            if (ires != cur_s) {
+                if (cur_s >= 0) atomicAdd(&s_pw[cur_s], acc);
+                cur_s = ires;
+                acc = 0.f;
             }
+            acc += re * re + im * im;
         }
+        if (cur_s >= 0) atomicAdd(&s_pw[cur_s], acc);
     }
     __syncthreads();
-    double hx = 0.;
-    for (int i = threadIdx.x; i < half; i += blockDim.x) {
-        power[(size_t)p * half + i] = s_pw[i];
-        if (i >= cur / 2 + 1) hx += s_pw[i];
-    }
-    for (int o = 16; o > 0; o >>= 1) hx += __shfl_xor_sync(0xffffffffu, hx, o);
-    __shared__ double s_h[32];
-    if ((threadIdx.x & 31) == 0) s_h[threadIdx.x >> 5] = hx;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double t = 0.;
-        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += s_h[i];
-        xi2[p] = t;
-    }
+    for (int i = threadIdx.x; i < half; i += blockDim.x)
+        if (s_pw[i] != 0.f) {
+            atomicAdd(&power[(size_t)p * half + i], (double)s_pw[i]);
+            if (i >= cur / 2 + 1) atomicAdd(&xi2[p], (double)s_pw[i]);
+        }
 }
 
-// CTF::getCTF (src/ctf.h:184-256, damping on) at spatial frequency (X, Y) in
-// 1/Angstrom, with the constants of CTF::initialise (src/ctf.cpp:211-261).
-__device__ double ctf_at(const double *c, double kV, double Cs, double Q0, double X, double Y) {
+// CTF::getCTF (src/ctf.h:184-256, damping on) with the constants of
+// CTF::initialise (src/ctf.cpp:211-261), per particle: the astigmatic
+// defocus form, K1 (wavelength), K2 (Cs), K3 (amplitude contrast), K4 (B
+// factor), K5 (phase shift), scale.
+struct CtfConst {
+    double Axx, Axy, Ayy, K1, K2, K3, K4, K5, scale;
+};
+
+__device__ CtfConst ctf_const(const double *c, double kV, double Cs, double Q0) {
     const double defU = c[0], defV = c[1], defA = c[2], Bfac = c[3], scale = c[4], phase = c[5];
     const double local_Cs = Cs * 1e7, local_kV = kV * 1e3;
     const double rad_az = defA * kPiD / 180.;
     const double lambda = 12.2643247 / sqrt(local_kV * (1. + local_kV * 0.978466e-6));
-    const double K1 = kPiD / 2 * 2 * lambda;
-    const double K2 = kPiD / 2 * local_Cs * lambda * lambda * lambda;
-    const double K3 = atan(Q0 / sqrt(1 - Q0 * Q0));
-    const double K4 = -Bfac / 4.;
-    const double K5 = phase * kPiD / 180.;
+    CtfConst k;
+    k.K1 = kPiD / 2 * 2 * lambda;
+    k.K2 = kPiD / 2 * local_Cs * lambda * lambda * lambda;
+    k.K3 = atan(Q0 / sqrt(1 - Q0 * Q0));
+    k.K4 = -Bfac / 4.;
+    k.K5 = phase * kPiD / 180.;
     const double s = sin(rad_az), co = cos(rad_az);
-    const double Axx = co * co * (-defU) + s * s * (-defV);
-    const double Axy = co * s * (-defU) - s * co * (-defV);
-    const double Ayy = s * s * (-defU) + co * co * (-defV);
-    const double u2 = X * X + Y * Y, u4 = u2 * u2;
-    const double gamma = K1 * (Axx * X * X + 2.0 * Axy * X * Y + Ayy * Y * Y) + K2 * u4 - K5 - K3;
-    double r = -sin(gamma) * exp(K4 * u2) * scale;
-    if (fabs(r) < 1e-8) r = (r < 0 ? -1. : 1.) * 1e-8;
-    return r;
+    k.Axx = co * co * (-defU) + s * s * (-defV);
+    k.Axy = co * s * (-defU) - s * co * (-defV);
+    k.Ayy = s * s * (-defU) + co * co * (-defV);
+    k.scale = scale;
+    return k;
 }
 
 // CTF image of the current size on the full-box frequencies
-// (CTF::getFftwImage, src/ctf.cpp:314-450, no padding).
+// (CTF::getFftwImage, src/ctf.cpp:314-450, no padding).  The phase gamma is
+// formed in FP64 and reduced modulo 2 pi there; the sine and the damping
+// exponential of the reduced values are FP32 (|CTF| <= 1, error ~1e-7).
 __global__ void k_ctf_image(const double *__restrict__ ctf, int N, int cur, double pixel, double kV, double Cs,
                             double Q0, float *__restrict__ out) {
+    __shared__ CtfConst sk;
     const int p = blockIdx.y, X = cur / 2 + 1;
+    if (threadIdx.x == 0) sk = ctf_const(ctf + (size_t)p * 6, kV, Cs, Q0);
+    __syncthreads();
+    const CtfConst k = sk;
     const double xs = (double)N * pixel;
-    const double *c = ctf + (size_t)p * 6;
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < cur * X; e += gridDim.x * blockDim.x) {
         const int i = e / X, j = e - i * X;
         const int ip = i < X ? i : i - cur;
-        out[(size_t)p * cur * X + e] = (float)ctf_at(c, kV, Cs, Q0, (double)j / xs, (double)ip / xs);
+        const double x = (double)j / xs, y = (double)ip / xs;
+        const double u2 = x * x + y * y;
+        double g = k.K1 * (k.Axx * x * x + 2.0 * k.Axy * x * y + k.Ayy * y * y) + k.K2 * u2 * u2 - k.K5 - k.K3;
+        g -= 2. * kPiD * rint(g * (0.5 / kPiD));
+        float r = -sinf((float)g) * expf((float)(k.K4 * u2)) * (float)k.scale;
+        if (fabsf(r) < 1e-8f) r = (r < 0.f ? -1.f : 1.f) * 1e-8f;
+        out[(size_t)p * cur * X + e] = r;
     }
 }
 
@@ -183,11 +210,16 @@ cudaError_t launch_prepare_images(const PrepImagesArgs &a, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
     if (N <= 0 || (N & 1) || cur <= 0 || (cur & 1) || cur > N) return cudaErrorInvalidValue;
     const int X = cur / 2 + 1, half = N / 2 + 1;
-    const dim3 gimg((unsigned)((N * N + 255) / 256 < 1024 ? (N * N + 255) / 256 : 1024), (unsigned)n);
-    k_img_shift<<<gimg, 256, 0, st>>>(a.images, N, a.shift, a.factor, a.A);
-    k_mask_bg<<<n, 256, 0, st>>>(a.A, N, a.mask_radius, a.mask_width, a.bg);
-    k_mask_apply<<<gimg, 256, 0, st>>>(a.A, N, a.mask_radius, a.mask_width, a.bg, a.B);
-    cudaError_t e = cudaGetLastError();
+    const unsigned bx = (unsigned)((N * N + 255) / 256 < 64 ? (N * N + 255) / 256 : 64);
+    const dim3 gimg(bx, (unsigned)n);
+    if (a.mask_fresh) k_mask_weights<<<(N * N + 255) / 256, 256, 0, st>>>(N, a.mask_radius, a.mask_width, a.W);
+    cudaError_t e = cudaMemsetAsync(a.bg, 0, sizeof(double) * 2 * n, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(a.power, 0, sizeof(double) * (size_t)n * half, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(a.xi2, 0, sizeof(double) * n, st);
+    if (e != cudaSuccess) return e;
+    k_img_shift_bg<<<gimg, 256, 0, st>>>(a.images, N, a.shift, a.factor, a.W, a.A, a.bg);
+    k_mask_apply<<<gimg, 256, 0, st>>>(a.A, N, a.W, a.bg, a.B);
+    e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     cufftHandle plan = (cufftHandle)a.fft_plan;
     if (cufftSetStream(plan, st) != CUFFT_SUCCESS) return cudaErrorUnknown;
@@ -196,7 +228,8 @@ cudaError_t launch_prepare_images(const PrepImagesArgs &a, cudaStream_t st) {
     const dim3 gw((unsigned)((cur * X + 255) / 256), (unsigned)n);
     k_window_center<<<gw, 256, 0, st>>>(a.FA, N, cur, a.fimg_nomask);
     k_window_center<<<gw, 256, 0, st>>>(a.FB, N, cur, a.fimg);
-    k_img_spectrum<<<n, 256, sizeof(double) * half, st>>>(a.FB, N, cur, a.power, a.xi2);
+    const dim3 gs((unsigned)((N * half + 2047) / 2048 < 64 ? (N * half + 2047) / 2048 : 64), (unsigned)n);
+    if (cur < N) k_img_spectrum<<<gs, 256, sizeof(float) * half, st>>>(a.FB, N, cur, a.power, a.xi2);
     k_ctf_image<<<gw, 256, 0, st>>>(a.ctf, N, cur, a.pixel, a.kV, a.Cs, a.Q0, a.fctf);
     return cudaGetLastError();
 }

@@ -245,7 +245,8 @@ class MlOptimiserCuda:
 
 
 STAGES = ["prep", "norm_gemm", "cross_gemm", "weights_coarse", "sig_jobs", "diff2_fine",
-          "weights_fine", "wsum", "backproject", "readback", "inputs", "host_final"]
+          "weights_fine", "wsum", "backproject", "readback", "inputs", "host_final",
+          "image_upload", "image_prep"]
 
 
 def measure_fp32_peak(device=0):
