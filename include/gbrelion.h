@@ -217,6 +217,40 @@ int gbr_prepare_images(gbr_worker *w, const gbr_image_batch *in, void *fimg, voi
  * plus accDoExpectationOneParticle). */
 int gbr_expect_images(gbr_worker *w, const gbr_image_batch *in, gbr_particle_result *res);
 
+/* ---- data formats (MRC image stacks, STAR metadata) --------------------- */
+
+/* MRC header fields (src/rwMRC.h): sizes, data mode, extended-header bytes,
+ * byte order, pixel size (cell a / mx) and the offset of the first image. */
+typedef struct {
+    int64_t nx, ny, nz, mode, nsymbt, swapped;
+    double pixel_size;
+    int64_t data_offset;
+} gbr_mrc_header;
+
+int gbr_mrc_read_header(const char *path, gbr_mrc_header *out);
+/* Images [first, first + count) of a stack as float32 [count][ny][nx] into
+ * `out` (page-locked memory for a direct device upload), `nthreads` readers
+ * (Image::read through readMRC, src/rwMRC.h:140-240; modes 0, 1, 2, 6, 12,
+ * 101). */
+int gbr_mrc_read_images(const char *path, int64_t first, int64_t count, float *out, int nthreads);
+/* A float32 (mode 2) stack [nz][ny][nx] with the given pixel size. */
+int gbr_mrc_write_stack(const char *path, const float *data, int64_t nx, int64_t ny, int64_t nz,
+                        double pixel_size);
+
+/* STAR files (MetaDataTable::read, src/metadata_table.cpp): data_ blocks with
+ * a loop_ table or label / value pairs. */
+typedef struct gbr_star gbr_star;
+int gbr_star_read(const char *path, gbr_star **out);
+int64_t gbr_star_num_blocks(const gbr_star *s);
+int gbr_star_block_info(const gbr_star *s, int64_t block, char *name, size_t len, int64_t *ncols,
+                        int64_t *nrows, int *is_loop);
+int gbr_star_column_name(const gbr_star *s, int64_t block, int64_t col, char *name, size_t len);
+/* Column `label` ("rlnDefocusU" or "_rlnDefocusU") of a block as doubles [nrows]. */
+int gbr_star_column_double(const gbr_star *s, int64_t block, const char *label, double *out);
+int gbr_star_value_string(const gbr_star *s, int64_t block, const char *label, int64_t row, char *buf,
+                          size_t len);
+void gbr_star_free(gbr_star *s);
+
 /* Number of coarse directions / psi angles / translations of the sampling,
  * and the fine oversampling factors (HealpixSampling::NrDirections etc.). */
 int gbr_sampling_sizes(const gbr_bundle *b, int64_t *ndir, int64_t *npsi, int64_t *ntrans,

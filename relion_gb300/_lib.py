@@ -65,6 +65,11 @@ class ImageBatch(C.Structure):
         [(n, P) for n in ("images", "old_offset", "prior", "norm_correction", "scale", "ctf")]
 
 
+class MrcHeader(C.Structure):
+    _fields_ = [(n, I64) for n in ("nx", "ny", "nz", "mode", "nsymbt", "swapped")] + \
+        [("pixel_size", F64), ("data_offset", I64)]
+
+
 EXPORTS = {
     "gbr_last_error": (C.c_size_t, [C.c_char_p, C.c_size_t]),
     "gbr_version": (C.c_char_p, []),
@@ -79,6 +84,17 @@ EXPORTS = {
     "gbr_bundle_set_optics": (C.c_int, [P, C.POINTER(OpticsDesc)]),
     "gbr_prepare_images": (C.c_int, [P, C.POINTER(ImageBatch), P, P, P, P, P, P]),
     "gbr_expect_images": (C.c_int, [P, C.POINTER(ImageBatch), P]),
+    "gbr_mrc_read_header": (C.c_int, [C.c_char_p, C.POINTER(MrcHeader)]),
+    "gbr_mrc_read_images": (C.c_int, [C.c_char_p, I64, I64, P, C.c_int]),
+    "gbr_mrc_write_stack": (C.c_int, [C.c_char_p, P, I64, I64, I64, F64]),
+    "gbr_star_read": (C.c_int, [C.c_char_p, C.POINTER(P)]),
+    "gbr_star_num_blocks": (I64, [P]),
+    "gbr_star_block_info": (C.c_int, [P, I64, C.c_char_p, C.c_size_t, C.POINTER(I64), C.POINTER(I64),
+                                      C.POINTER(C.c_int)]),
+    "gbr_star_column_name": (C.c_int, [P, I64, I64, C.c_char_p, C.c_size_t]),
+    "gbr_star_column_double": (C.c_int, [P, I64, C.c_char_p, P]),
+    "gbr_star_value_string": (C.c_int, [P, I64, C.c_char_p, I64, C.c_char_p, C.c_size_t]),
+    "gbr_star_free": (None, [P]),
     "gbr_sampling_sizes": (C.c_int, [P] + [C.POINTER(I64)] * 5),
     "gbr_worker_debug_fetch": (I64, [P, C.c_int, I64, P, I64]),
     "gbr_backprojector_dims": (C.c_int, [P] + [C.POINTER(I64)] * 6),

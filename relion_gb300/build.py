@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libgbrelion.so")
-SOURCES = ["k_project.cu", "k_gemm.cu", "k_estep.cu", "estep.cu", "k_noalloc.cu", "k_tc.cu", "k_prepimg.cu"]
+SOURCES = ["k_project.cu", "k_gemm.cu", "k_estep.cu", "estep.cu", "k_noalloc.cu", "k_tc.cu", "k_prepimg.cu", "io.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -26,7 +26,7 @@ def _nvcc():
 
 
 def _run(cmd):
-    proc = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    proc = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, errors="replace")
     if proc.returncode != 0:
         raise RuntimeError("command failed: %s\n%s" % (" ".join(cmd), proc.stdout))
     return proc.stdout
@@ -45,7 +45,7 @@ def build(verbose=False, force=False):
                     "-Xcompiler", "-ffp-contract=off", "-Xptxas", "-v"]
 
     def one(src):
-        obj = os.path.join(BUILD, src.replace(".cu", ".o"))
+        obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
         out = _run([nvcc] + flags + ["-c", os.path.join(CSRC, src), "-o", obj])
         with open(obj + ".ptxas.txt", "w") as fh:
             fh.write(out)

@@ -92,3 +92,39 @@ def test_expect_images_equals_expect_batch():
     # per-particle diff2 constant and dLL, move by ~1e-8 relative)
     for k in ("pmax", "dLL", "coarse_sum_weight", "fine_sum_weight", "xoff", "yoff"):
         np.testing.assert_allclose(r2[k], r1[k], rtol=1e-6, err_msg=k)
+
+
+def test_expect_images_from_star_and_mrc(tmp_path):
+    # the data path of a run: MRC stack + STAR metadata on disk, native reader,
+    # device image preparation and E-step; same results as the in-memory batch
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from relion_gb300 import io
+    from relion_gb300.estep import MlOptimiserCuda
+    ds, m, bi = _setup(seed=9, n=6, norm=False)
+    n = len(bi["images"])
+    pix = m["pixel_size"]
+    io.write_mrc_stack(str(tmp_path / "parts.mrcs"), bi["images"], pix)
+    io.write_star(str(tmp_path / "optics.star"), {"optics": {
+        "rlnOpticsGroup": [1], "rlnVoltage": [300.0], "rlnSphericalAberration": [2.7],
+        "rlnAmplitudeContrast": [0.1], "rlnImagePixelSize": [pix], "rlnImageSize": [m["ori_size"]]}})
+    io.write_star(str(tmp_path / "parts.star"), {"particles": {
+        "rlnImageName": ["%06d@parts.mrcs" % (i + 1) for i in range(n)],
+        "rlnDefocusU": list(bi["ctf"][:, 0]), "rlnDefocusV": list(bi["ctf"][:, 1]),
+        "rlnDefocusAngle": list(bi["ctf"][:, 2]),
+        "rlnOriginXAngst": list(bi["old_offset"][:, 0] * pix), "rlnOriginYAngst": list(bi["old_offset"][:, 1] * pix),
+        "rlnOpticsGroup": [1] * n}})
+    star = tmp_path / "run.star"
+    star.write_text((tmp_path / "optics.star").read_text() + (tmp_path / "parts.star").read_text())
+    lb = io.load_particles(str(star))
+    np.testing.assert_array_equal(lb["images"], bi["images"])
+    b = _bundle(ds, m)
+    w = MlOptimiserCuda(b)
+    r_file = w.do_expectation_images(lb)
+    r_mem = w.do_expectation_images(bi)
+    w.close()
+    b.close()
+    assert np.array_equal(r_file["best_ihidden_over"], r_mem["best_ihidden_over"])
+    assert np.array_equal(r_file["nr_sign"], r_mem["nr_sign"])
+    np.testing.assert_allclose(r_file["pmax"], r_mem["pmax"], rtol=1e-5)
