@@ -1,6 +1,7 @@
 """Build the oracle (TEST INFRASTRUCTURE ONLY).
 
-Compiles oracle/relion_oracle.cpp into oracle/_build/liboracle.so and, when
+Compiles oracle/relion_oracle.cpp and oracle/oracle_mstep.cpp into
+oracle/_build/liboracle.so and, when
 the reference tree is present, the reference's own HEALPix sources into
 oracle/_ref/libref_healpix.so (oracle/build_ref.sh).
 """
@@ -14,12 +15,12 @@ REF_LIB = os.path.join(HERE, "_ref", "libref_healpix.so")
 
 def build(force=False):
     os.makedirs(os.path.join(HERE, "_build"), exist_ok=True)
-    src = os.path.join(HERE, "relion_oracle.cpp")
+    srcs = [os.path.join(HERE, f) for f in ("relion_oracle.cpp", "oracle_mstep.cpp")]
     hdr = os.path.join(HERE, "relion_oracle.h")
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(
-            os.path.getmtime(src), os.path.getmtime(hdr)):
-        subprocess.run(["g++", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-std=c++17", "-fopenmp",
-                        src, "-o", LIB + ".tmp"], check=True)
+            [os.path.getmtime(s) for s in srcs] + [os.path.getmtime(hdr)]):
+        subprocess.run(["g++", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-std=c++17", "-fopenmp"]
+                       + srcs + ["-o", LIB + ".tmp"], check=True)
         os.replace(LIB + ".tmp", LIB)
     ref = os.environ.get("RELION_REFERENCE", "/root/reference")
     if os.path.isdir(os.path.join(ref, "src", "Healpix_2.15a")) and (force or not os.path.exists(REF_LIB)):

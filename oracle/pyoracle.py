@@ -77,6 +77,14 @@ def load():
         lib.oracle_oversampled_orientations.restype = C.c_int
         lib.oracle_translations.restype = C.c_int
         lib.oracle_oversampled_translations.restype = C.c_int
+        for f in ("oracle_bp_symmetrise", "oracle_update_ssnr", "oracle_reconstruct",
+                  "oracle_projector_from_map", "oracle_fsc"):
+            getattr(lib, f).restype = C.c_int
+        lib.oracle_bp_symmetrise.argtypes = [P, P, P]
+        lib.oracle_update_ssnr.argtypes = [P, P, F64, P, P, P, P, P, I64, I64]
+        lib.oracle_reconstruct.argtypes = [P, P, P, P, P, P]
+        lib.oracle_projector_from_map.argtypes = [I64, I64, I64, P, I64, I64, I64, P, P]
+        lib.oracle_fsc.argtypes = [I64, I64, P, P, P]
         _O = lib
     return _O
 
@@ -280,3 +288,88 @@ def prepare_images(params, images, meta):
     if st != 0:
         raise RuntimeError("oracle_prepare_images failed with status %d" % st)
     return dict(fimg=fimg, fimg_nomask=fnm, fctf=fctf, power_img=power, highres_Xi2=xi2, old_offset=off)
+
+
+# --- reconstruction side (oracle_mstep.cpp) -------------------------------
+class OracleBpGeom(C.Structure):
+    _fields_ = [(n, I64) for n in ("ori_size", "ref_dim", "pad", "r_max", "xdim", "ydim", "zdim",
+                                   "yinit", "zinit")]
+
+
+class OracleReconParams(C.Structure):
+    _fields_ = [(n, I64) for n in ("max_iter_preweight", "do_map", "skip_gridding", "minres_map")] + \
+        [(n, F64) for n in ("tau2_fudge", "normalise")]
+
+
+def _bp_geom(ori_size, current_size, pad=2, ref_dim=3):
+    g = bp_geometry(current_size, ori_size, pad, ref_dim)
+    return OracleBpGeom(ori_size=ori_size, ref_dim=ref_dim, pad=pad, **g), g
+
+
+def bp_symmetrise(data, weight, ori_size, current_size, pad=2, ref_dim=3):
+    """BackProjector::enforceHermitianSymmetry on copies; returns (data, weight)."""
+    gg, _ = _bp_geom(ori_size, current_size, pad, ref_dim)
+    d = np.ascontiguousarray(data, np.complex128).copy()
+    w = np.ascontiguousarray(weight, np.float64).copy()
+    load().oracle_bp_symmetrise(C.byref(gg), d.ctypes.data, w.ctypes.data)
+    return d, w
+
+
+def update_ssnr(weight, ori_size, current_size, tau2, tau2_fudge=1.0, fsc=None, update_tau2_with_fsc=False,
+                is_whole=False, pad=2, ref_dim=3):
+    """BackProjector::updateSSNRarrays -> dict(tau2, sigma2, data_vs_prior, fourier_coverage)."""
+    gg, _ = _bp_geom(ori_size, current_size, pad, ref_dim)
+    ns = ori_size // 2 + 1
+    t = np.array(tau2, np.float64).copy()
+    out = [np.zeros(ns) for _ in range(3)]
+    f = np.zeros(ns) if fsc is None else np.ascontiguousarray(fsc, np.float64)
+    w = np.ascontiguousarray(weight, np.float64)
+    st = load().oracle_update_ssnr(C.byref(gg), w.ctypes.data, F64(tau2_fudge), t.ctypes.data,
+                                   *[o.ctypes.data for o in out], f.ctypes.data, I64(int(update_tau2_with_fsc)),
+                                   I64(int(is_whole)))
+    if st != 0:
+        raise RuntimeError("oracle_update_ssnr failed with status %d" % st)
+    return dict(tau2=t, sigma2=out[0], data_vs_prior=out[1], fourier_coverage=out[2])
+
+
+def reconstruct(data, weight, ori_size, current_size, tau2=None, do_map=False, tau2_fudge=1.0, normalise=1.0,
+                minres_map=5, skip_gridding=True, max_iter_preweight=10, pad=2, ref_dim=3):
+    """BackProjector::reconstruct -> real-space map [ori]^ref_dim."""
+    gg, _ = _bp_geom(ori_size, current_size, pad, ref_dim)
+    p = OracleReconParams(max_iter_preweight=max_iter_preweight, do_map=int(do_map),
+                          skip_gridding=int(skip_gridding), minres_map=minres_map, tau2_fudge=tau2_fudge,
+                          normalise=normalise)
+    t = np.zeros(ori_size // 2 + 1) if tau2 is None else np.ascontiguousarray(tau2, np.float64)
+    vol = np.zeros((ori_size,) * ref_dim)
+    d = np.ascontiguousarray(data, np.complex128)
+    w = np.ascontiguousarray(weight, np.float64)
+    st = load().oracle_reconstruct(C.byref(gg), d.ctypes.data, w.ctypes.data, C.byref(p), t.ctypes.data,
+                                   vol.ctypes.data)
+    if st != 0:
+        raise RuntimeError("oracle_reconstruct failed with status %d" % st)
+    return vol
+
+
+def projector_from_map(vol, current_size, do_gridding=True, min_ires=-1, pad=2):
+    """Projector::computeFourierTransformMap -> (padded Fourier reference, power spectrum)."""
+    v = np.ascontiguousarray(vol, np.float64)
+    ori, ref_dim = v.shape[-1], v.ndim
+    r_max = min(current_size // 2, ori // 2) if current_size >= 0 else ori // 2
+    ps = 2 * (int(pad * r_max + 0.5) + 1) + 1
+    shape = (ps, ps, ps // 2 + 1) if ref_dim == 3 else (ps, ps // 2 + 1)
+    proj = np.zeros(shape, np.complex128)
+    power = np.zeros(ori // 2 + 1)
+    st = load().oracle_projector_from_map(I64(ori), I64(ref_dim), I64(pad), v.ctypes.data, I64(current_size),
+                                          I64(int(do_gridding)), I64(min_ires), proj.ctypes.data, power.ctypes.data)
+    if st != 0:
+        raise RuntimeError("oracle_projector_from_map failed with status %d" % st)
+    return proj, power
+
+
+def fsc(m1, m2):
+    """getFSC of two real-space maps -> [ori/2+1]."""
+    a = np.ascontiguousarray(m1, np.float64)
+    b = np.ascontiguousarray(m2, np.float64)
+    out = np.zeros(a.shape[-1] // 2 + 1)
+    load().oracle_fsc(I64(a.shape[-1]), I64(a.ndim), a.ctypes.data, b.ctypes.data, out.ctypes.data)
+    return out

@@ -139,6 +139,38 @@ int oracle_prepare_images(const oracle_prep_params *pp, int64_t n, const double 
                           const oracle_image_meta *meta, double *fimg, double *fimg_nomask, double *fctf,
                           double *power, double *highres_Xi2, double *old_offset_rounded);
 
+/* --- reconstruction side (oracle_mstep.cpp) ----------------------------- */
+typedef struct {
+    int64_t ori_size, ref_dim, pad; /* integer padding factor                          */
+    int64_t r_max;                  /* BackProjector r_max                              */
+    int64_t xdim, ydim, zdim, yinit, zinit; /* data / weight layout (x from 0)          */
+} oracle_bp_geom;
+
+typedef struct {
+    int64_t max_iter_preweight;  /* --gridding_iter                                    */
+    int64_t do_map;
+    int64_t skip_gridding;       /* default of relion_refine: no --dont_skip_gridding  */
+    int64_t minres_map;
+    double tau2_fudge;
+    double normalise;            /* wsum pdf_class of the class                        */
+} oracle_recon_params;
+
+/* data: complex [zdim][ydim][xdim][2], weight [zdim][ydim][xdim]; modified in place */
+int oracle_bp_symmetrise(const oracle_bp_geom *g, double *data, double *weight);
+/* all shell arrays [ori/2+1]; tau2_io read and written */
+int oracle_update_ssnr(const oracle_bp_geom *g, const double *weight, double tau2_fudge, double *tau2_io,
+                       double *sigma2_out, double *dvp_out, double *cov_out, const double *fsc,
+                       int64_t update_tau2_with_fsc, int64_t is_whole_instead_of_half);
+/* real-space map [ori]^ref_dim (z, y, x) */
+int oracle_reconstruct(const oracle_bp_geom *g, const double *data, const double *weight,
+                       const oracle_recon_params *p, const double *tau2, double *vol_out);
+/* map [ori]^ref_dim -> padded Fourier reference (projector layout of current_size) and power [ori/2+1] */
+int oracle_projector_from_map(int64_t ori, int64_t ref_dim, int64_t padding_factor, const double *vol,
+                              int64_t current_size, int64_t do_gridding, int64_t min_ires, double *proj_out,
+                              double *power_out);
+/* Fourier shell correlation of two maps [ori]^ref_dim -> fsc [ori/2+1] */
+int oracle_fsc(int64_t ori, int64_t ref_dim, const double *m1, const double *m2, double *fsc);
+
 /* --- building blocks exposed for unit checks --------------------------- */
 double oracle_ctf(double defU, double defV, double defAng, double kV, double Cs,
                   double Q0, double Bfac, double scale, double phase_shift,
