@@ -271,6 +271,59 @@ int gbr_backprojector_dims(const gbr_bundle *b, int64_t *xdim, int64_t *ydim, in
                            int64_t *yinit, int64_t *zinit, int64_t *r_max);
 int gbr_backprojector_download(gbr_bundle *b, int64_t iclass, double *data, double *weight);
 
+/* Replace one class's volumes (layout of gbr_backprojector_download), e.g.
+ * with the sums over all ranks after MlOptimiserMpi::combineAllWeightedSums
+ * (src/ml_optimiser_mpi.cpp:2028), before the reconstruction below. */
+int gbr_backprojector_upload(gbr_bundle *b, int64_t iclass, const double *data, const double *weight);
+
+/* --- reconstruction side of an iteration (FP64 on the device) ------------ */
+
+/* BackProjector::enforceHermitianSymmetry (src/backprojector.cpp:2148-2165)
+ * on one class's volumes: BackProjector::symmetrise for C1, as called by
+ * MlOptimiser::symmetriseReconstructions (src/ml_optimiser.cpp:4729). */
+int gbr_backprojector_symmetrise(gbr_bundle *b, int64_t iclass);
+
+/* BackProjector::updateSSNRarrays (src/backprojector.cpp:1041-1204) of one
+ * class: tau2_io [ori/2+1] is read and written; sigma2, data_vs_prior and
+ * fourier_coverage [ori/2+1] are written (any may be NULL); fsc [ori/2+1] is
+ * read when update_tau2_with_fsc.  CTF-premultiplied correction not
+ * supported. */
+int gbr_update_ssnr(gbr_bundle *b, int64_t iclass, double tau2_fudge, double *tau2_io, double *sigma2_out,
+                    double *data_vs_prior_out, double *fourier_coverage_out, const double *fsc,
+                    int update_tau2_with_fsc, int is_whole_instead_of_half);
+
+typedef struct {
+    int max_iter_preweight; /* gridding_nr_iter (--gridding_iter, 10)                    */
+    int do_map;             /* add 1 / tau2 to the weights (MAP)                         */
+    int skip_gridding;      /* 1 unless --dont_skip_gridding (relion_refine default 1)   */
+    int minres_map;         /* --minres_map (5)                                          */
+    double tau2_fudge;
+    double normalise;       /* wsum_model.pdf_class[iclass] (used with gridding)         */
+} gbr_recon_params;
+
+/* BackProjector::reconstruct (src/backprojector.cpp:1379-1872) of one
+ * class's device volumes into the real-space map vol_out [ori]^ref_dim
+ * (z, y, x; mymodel.Iref[iclass]); tau2 [ori/2+1] is read when do_map.
+ * Transforms are cuFFT double precision. */
+int gbr_reconstruct(gbr_bundle *b, int64_t iclass, const gbr_recon_params *p, const double *tau2, double *vol_out);
+
+/* Projector::computeFourierTransformMap (src/projector.cpp:116-593, called by
+ * MlModel::setFourierTransformMaps, src/ml_model.cpp:1505-1555) of the map
+ * vol [ori]^ref_dim straight into class iclass's device projector, in place
+ * of gbr_projector_upload: gridding pre-correction, zero padding, forward
+ * transform, r <= r_max(current_size) kept; power_spectrum [ori/2+1]
+ * (tau2_class when updating it) or NULL; min_ires <= 0: no high-pass. */
+int gbr_projector_from_map(gbr_bundle *b, int64_t iclass, const double *vol, int64_t current_size,
+                           int do_gridding, int64_t min_ires, double *power_spectrum);
+
+/* Read back one class's device projector (complex FP32, interleaved) and
+ * its geometry: dims[7] = xdim, ydim, zdim, yinit, zinit, r_max, padding
+ * factor.  data may be NULL to query the geometry only. */
+int gbr_projector_download(gbr_bundle *b, int64_t iclass, float *data, int64_t *dims);
+
+/* getFSC (src/fftw.cpp:481-525) of two maps [ori]^ref_dim -> fsc [ori/2+1]. */
+int gbr_fsc(gbr_bundle *b, const double *map1, const double *map2, double *fsc);
+
 /* Weighted sums accumulated since the last reset (added into `out`). */
 int gbr_wsum_download(gbr_bundle *b, gbr_wsum *out);
 /* 2D classification: wsum_model.prior_offset_class [K][2] accumulated since

@@ -70,6 +70,11 @@ class MrcHeader(C.Structure):
         [("pixel_size", F64), ("data_offset", I64)]
 
 
+class ReconParams(C.Structure):
+    _fields_ = [(n, C.c_int) for n in ("max_iter_preweight", "do_map", "skip_gridding", "minres_map")] + \
+        [(n, F64) for n in ("tau2_fudge", "normalise")]
+
+
 EXPORTS = {
     "gbr_last_error": (C.c_size_t, [C.c_char_p, C.c_size_t]),
     "gbr_version": (C.c_char_p, []),
@@ -99,6 +104,13 @@ EXPORTS = {
     "gbr_worker_debug_fetch": (I64, [P, C.c_int, I64, P, I64]),
     "gbr_backprojector_dims": (C.c_int, [P] + [C.POINTER(I64)] * 6),
     "gbr_backprojector_download": (C.c_int, [P, I64, P, P]),
+    "gbr_backprojector_upload": (C.c_int, [P, I64, P, P]),
+    "gbr_backprojector_symmetrise": (C.c_int, [P, I64]),
+    "gbr_update_ssnr": (C.c_int, [P, I64, F64, P, P, P, P, P, C.c_int, C.c_int]),
+    "gbr_reconstruct": (C.c_int, [P, I64, P, P, P]),
+    "gbr_projector_from_map": (C.c_int, [P, I64, P, I64, C.c_int, I64, P]),
+    "gbr_fsc": (C.c_int, [P, P, P, P]),
+    "gbr_projector_download": (C.c_int, [P, I64, P, P]),
     "gbr_wsum_download": (C.c_int, [P, C.POINTER(Wsum)]),
     "gbr_wsum_download_class_offsets": (C.c_int, [P, P]),
     "gbr_bundle_reset_wsum": (C.c_int, [P]),

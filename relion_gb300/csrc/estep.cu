@@ -185,6 +185,9 @@ struct gbr_bundle {
     std::vector<double> w_sigma2;
     double w_sigma2_offset = 0, w_sumw_group = 0, w_LL = 0, w_ave_Pmax = 0, w_avg_norm = 0, w_XA = 0,
            w_AA = 0;
+    // reconstruction side: scratch and FFT plans, created on first use
+    gbr::ReconWork *recon = nullptr;
+    ~gbr_bundle() { gbr::recon_work_destroy(recon); }
 };
 
 struct gbr_worker {
@@ -1341,6 +1344,96 @@ int gbr_backprojector_download(gbr_bundle *b, int64_t iclass, double *data, doub
     if (data) GBR_CUDA(cudaMemcpy(data, b->bp_data[iclass].p, sizeof(double2) * b->bp_vox, cudaMemcpyDeviceToHost));
     if (weight) GBR_CUDA(cudaMemcpy(weight, b->bp_weight[iclass].p, sizeof(double) * b->bp_vox, cudaMemcpyDeviceToHost));
     return GBR_OK;
+}
+
+int gbr_backprojector_upload(gbr_bundle *b, int64_t iclass, const double *data, const double *weight) {
+    if (!b || !data || !weight || iclass < 0 || iclass >= b->K) return fail(GBR_ERR_INVALID, "bad class or data");
+    GBR_CUDA(cudaSetDevice(b->device));
+    GBR_CUDA(cudaDeviceSynchronize());
+    GBR_CUDA(cudaMemcpy(b->bp_data[iclass].p, data, sizeof(double2) * b->bp_vox, cudaMemcpyHostToDevice));
+    GBR_CUDA(cudaMemcpy(b->bp_weight[iclass].p, weight, sizeof(double) * b->bp_vox, cudaMemcpyHostToDevice));
+    return GBR_OK;
+}
+
+namespace {
+int recon_begin(gbr_bundle *b, int64_t iclass) {
+    if (!b || iclass < 0 || iclass >= b->K) return fail(GBR_ERR_INVALID, "bad class");
+    GBR_CUDA(cudaSetDevice(b->device));
+    GBR_CUDA(cudaDeviceSynchronize());
+    if (!b->recon) b->recon = gbr::recon_work_create();
+    return GBR_OK;
+}
+}  // namespace
+
+int gbr_backprojector_symmetrise(gbr_bundle *b, int64_t iclass) {
+    int st = recon_begin(b, iclass);
+    if (st) return st;
+    return gbr::recon_symmetrise(b->bp_data[iclass].p, b->bp_weight[iclass].p, b->bg);
+}
+
+int gbr_update_ssnr(gbr_bundle *b, int64_t iclass, double tau2_fudge, double *tau2_io, double *sigma2_out,
+                    double *data_vs_prior_out, double *fourier_coverage_out, const double *fsc,
+                    int update_tau2_with_fsc, int is_whole_instead_of_half) {
+    int st = recon_begin(b, iclass);
+    if (st) return st;
+    if (!tau2_io || (update_tau2_with_fsc && !fsc)) return fail(GBR_ERR_INVALID, "null tau2 / fsc");
+    return gbr::recon_update_ssnr(b->recon, b->bp_weight[iclass].p, b->bg, (int)b->d.ori_size, tau2_fudge, tau2_io,
+                                  sigma2_out, data_vs_prior_out, fourier_coverage_out, fsc, update_tau2_with_fsc,
+                                  is_whole_instead_of_half);
+}
+
+int gbr_reconstruct(gbr_bundle *b, int64_t iclass, const gbr_recon_params *p, const double *tau2, double *vol_out) {
+    int st = recon_begin(b, iclass);
+    if (st) return st;
+    if (!p || !vol_out) return fail(GBR_ERR_INVALID, "null argument");
+    const gbr::ReconParams rp{p->max_iter_preweight, p->do_map, p->skip_gridding, p->minres_map, p->tau2_fudge,
+                              p->normalise};
+    return gbr::recon_reconstruct(b->recon, b->bp_data[iclass].p, b->bp_weight[iclass].p, b->bg,
+                                  (int)b->d.ori_size, rp, tau2, vol_out);
+}
+
+int gbr_projector_from_map(gbr_bundle *b, int64_t iclass, const double *vol, int64_t current_size,
+                           int do_gridding, int64_t min_ires, double *power_spectrum) {
+    int st = recon_begin(b, iclass);
+    if (st) return st;
+    if (!vol) return fail(GBR_ERR_INVALID, "null map");
+    const int dim = b->is2d ? 2 : 3;
+    const gbr::VolGeom g = gbr::projector_geometry((int)b->d.ori_size, dim, (int)b->d.padding_factor,
+                                                   (int)current_size);
+    bool any = false;
+    for (long k = 0; k < b->K; ++k) any |= (k != iclass && b->have_vol[k] != 0);
+    if (any && std::memcmp(&g, &b->pg, sizeof(g)) != 0)
+        return fail(GBR_ERR_INVALID, "all classes must share one projector geometry");
+    GBR_CUDA(b->vol[iclass].reserve((size_t)g.xdim * g.ydim * g.zdim));
+    st = gbr::recon_projector_from_map(b->recon, vol, (int)b->d.ori_size, dim, (int)b->d.padding_factor, g,
+                                       do_gridding, (int)min_ires, b->vol[iclass].p, power_spectrum);
+    if (st) return st;
+    b->pg = g;
+    b->have_vol[iclass] = 1;
+    b->tables_ready = false;
+    return GBR_OK;
+}
+
+int gbr_projector_download(gbr_bundle *b, int64_t iclass, float *data, int64_t *dims) {
+    if (!b || !dims || iclass < 0 || iclass >= b->K) return fail(GBR_ERR_INVALID, "bad class");
+    if (!b->have_vol[iclass]) return fail(GBR_ERR_STATE, "no projector for this class");
+    const gbr::VolGeom &g = b->pg;
+    const int64_t v[7] = {g.xdim, g.ydim, g.zdim, g.yinit, g.zinit, g.r_max, g.pad};
+    std::copy(v, v + 7, dims);
+    if (data) {
+        GBR_CUDA(cudaSetDevice(b->device));
+        GBR_CUDA(cudaDeviceSynchronize());
+        GBR_CUDA(cudaMemcpy(data, b->vol[iclass].p, sizeof(float2) * (size_t)g.xdim * g.ydim * g.zdim,
+                            cudaMemcpyDeviceToHost));
+    }
+    return GBR_OK;
+}
+
+int gbr_fsc(gbr_bundle *b, const double *map1, const double *map2, double *fsc) {
+    int st = recon_begin(b, 0);
+    if (st) return st;
+    if (!map1 || !map2 || !fsc) return fail(GBR_ERR_INVALID, "null argument");
+    return gbr::recon_fsc(b->recon, map1, map2, (int)b->d.ori_size, b->is2d ? 2 : 3, fsc);
 }
 
 int gbr_wsum_download(gbr_bundle *b, gbr_wsum *out) {

@@ -245,3 +245,27 @@ cudaError_t launch_gather_pdat(const double *old_offset, const double *prior, co
 cudaError_t launch_cand_seg(const unsigned int *cnt, int n, int cap, long long *seg, cudaStream_t st);
 
 }  // namespace gbr
+
+// Reconstruction side of an iteration (k_recon.cu).  Host entry points run
+// on the legacy default stream and synchronise; they return 0 or a
+// gbr_status with the text set through set_error_text.
+namespace gbr {
+struct ReconWork;  // device scratch and cached double-precision FFT plans
+ReconWork *recon_work_create();
+void recon_work_destroy(ReconWork *w);
+struct ReconParams {
+    int max_iter_preweight, do_map, skip_gridding, minres_map;
+    double tau2_fudge, normalise;
+};
+// Projector::initialiseData(current_size) geometry for a padded reference
+VolGeom projector_geometry(int ori, int dim, int pad, int current_size);
+int recon_symmetrise(double2 *data, double *weight, const VolGeom &g);
+int recon_update_ssnr(ReconWork *w, const double *weight, const VolGeom &g, int ori, double tau2_fudge,
+                      double *tau2_io, double *sigma2_out, double *dvp_out, double *cov_out, const double *fsc,
+                      int upd, int whole);
+int recon_reconstruct(ReconWork *w, const double2 *data, const double *weight, const VolGeom &g, int ori,
+                      const ReconParams &p, const double *tau2_host, double *vol_host);
+int recon_projector_from_map(ReconWork *w, const double *vol_host, int ori, int dim, int pad, const VolGeom &pg,
+                             int do_gridding, int min_ires, float2 *proj, double *power_host);
+int recon_fsc(ReconWork *w, const double *m1, const double *m2, int ori, int dim, double *fsc_host);
+}  // namespace gbr

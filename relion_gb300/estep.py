@@ -89,6 +89,72 @@ class MlDeviceBundle:
         check(self.lib.gbr_backprojector_download(self.h, int(iclass), data.ctypes.data, weight.ctypes.data))
         return data, weight
 
+    def set_mdl_data(self, iclass, data, weight):
+        """Replace one class's volumes (e.g. with the sums over all ranks)."""
+        xd, yd, zd, _, _, _ = self.backprojector_dims()
+        d = np.ascontiguousarray(data, dtype=np.complex128).reshape(zd, yd, xd)
+        w = np.ascontiguousarray(weight, dtype=np.float64).reshape(zd, yd, xd)
+        check(self.lib.gbr_backprojector_upload(self.h, int(iclass), d.ctypes.data, w.ctypes.data))
+
+    # BackProjector::symmetrise (C1: enforceHermitianSymmetry)
+    def symmetrise(self, iclass):
+        check(self.lib.gbr_backprojector_symmetrise(self.h, int(iclass)))
+
+    # BackProjector::updateSSNRarrays
+    def update_ssnr_arrays(self, iclass, tau2_fudge, tau2, fsc=None, update_tau2_with_fsc=False,
+                           is_whole_instead_of_half=False):
+        """Returns dict(tau2, sigma2, data_vs_prior, fourier_coverage), [ori/2+1] each."""
+        ns = self.ori_size // 2 + 1
+        t = np.array(tau2, dtype=np.float64).reshape(ns).copy()
+        out = [np.zeros(ns) for _ in range(3)]
+        f = np.zeros(ns) if fsc is None else np.ascontiguousarray(fsc, dtype=np.float64)
+        check(self.lib.gbr_update_ssnr(self.h, int(iclass), float(tau2_fudge), t.ctypes.data,
+                                       *[o.ctypes.data for o in out], f.ctypes.data, int(update_tau2_with_fsc),
+                                       int(is_whole_instead_of_half)))
+        return dict(tau2=t, sigma2=out[0], data_vs_prior=out[1], fourier_coverage=out[2])
+
+    # BackProjector::reconstruct
+    def reconstruct(self, iclass, max_iter_preweight=10, do_map=False, tau2=None, tau2_fudge=1.0, normalise=1.0,
+                    minres_map=5, skip_gridding=True):
+        """Real-space map [ori]^ref_dim (mymodel.Iref[iclass])."""
+        p = _lib.ReconParams(max_iter_preweight=int(max_iter_preweight), do_map=int(do_map),
+                             skip_gridding=int(skip_gridding), minres_map=int(minres_map),
+                             tau2_fudge=float(tau2_fudge), normalise=float(normalise))
+        vol = np.zeros((self.ori_size,) * self.ref_dim)
+        t = None if tau2 is None else np.ascontiguousarray(tau2, dtype=np.float64)
+        check(self.lib.gbr_reconstruct(self.h, int(iclass), C.byref(p), None if t is None else t.ctypes.data,
+                                       vol.ctypes.data))
+        return vol
+
+    # Projector::computeFourierTransformMap (MlModel::setFourierTransformMaps)
+    def set_fourier_transform_map(self, iclass, vol, current_size, do_gridding=True, min_ires=-1):
+        """Fill class iclass's projector from a real-space map; returns its power spectrum."""
+        v = np.ascontiguousarray(vol, dtype=np.float64)
+        if v.shape != (self.ori_size,) * self.ref_dim:
+            raise ValueError("map must be %s" % ((self.ori_size,) * self.ref_dim,))
+        ps = np.zeros(self.ori_size // 2 + 1)
+        check(self.lib.gbr_projector_from_map(self.h, int(iclass), v.ctypes.data, int(current_size),
+                                              int(do_gridding), int(min_ires), ps.ctypes.data))
+        return ps
+
+    def get_projector(self, iclass):
+        """(padded Fourier reference as complex64 [zdim][ydim][xdim], geometry dict)."""
+        dims = np.zeros(7, np.int64)
+        check(self.lib.gbr_projector_download(self.h, int(iclass), None, dims.ctypes.data))
+        xd, yd, zd = (int(x) for x in dims[:3])
+        data = np.zeros((zd, yd, xd), np.complex64)
+        check(self.lib.gbr_projector_download(self.h, int(iclass), data.ctypes.data, dims.ctypes.data))
+        geom = dict(zip(("xdim", "ydim", "zdim", "yinit", "zinit", "r_max", "pad"), (int(x) for x in dims)))
+        return data, geom
+
+    # getFSC
+    def fsc(self, map1, map2):
+        a = np.ascontiguousarray(map1, dtype=np.float64)
+        b = np.ascontiguousarray(map2, dtype=np.float64)
+        out = np.zeros(self.ori_size // 2 + 1)
+        check(self.lib.gbr_fsc(self.h, a.ctypes.data, b.ctypes.data, out.ctypes.data))
+        return out
+
     def get_wsum(self):
         s2 = np.zeros(self.ori_size // 2 + 1)
         pc = np.zeros(self.nr_classes)
