@@ -226,6 +226,8 @@ def run_ours(args, world, rank, local):
         from relion_gb300.replicas import max_over_ranks
         total_ms, e2e_total, img_total = max_over_ranks([total_ms, e2e_total, img_total], device=dev)
 
+    mstep = mstep_section(args, ds, model, bundle, worker, dev_batch, local) if rank == 0 else None
+
     # ---- roofline of the dominant kernel: the coarse cross-term GEMM ----
     R = bundle.nr_classes * bundle.ndir * bundle.npsi
     T = bundle.ntrans
@@ -292,7 +294,83 @@ def run_ours(args, world, rank, local):
     }
     if rank == 0:
         out["clocks"] = clk.summary()
+        out["mstep"] = mstep
     return out, ds, batch, model
+
+
+def mstep_section(args, ds, model, bundle, worker, dev_batch, local):
+    """Reconstruction side of the iteration on the device, timed once per
+    call (host wall clock around each synchronous C-ABI call, map copies
+    included): symmetrise, updateSSNRarrays, reconstruct and
+    computeFourierTransformMap of this batch's volumes at the workload's
+    sizes, and reconstruct at the Nyquist-limited size (current 256).  Also
+    the equal-FSC check of the precision form: the same batch through the
+    plain FP32 path, both volumes reconstructed, FSC between the two maps."""
+    import time
+    from relion_gb300.estep import MlDeviceBundle, MlOptimiserCuda
+
+    ori, cur = model["ori_size"], model["current_size"]
+    ns = ori // 2 + 1
+    out = {}
+
+    def timed(name, fn):
+        t0 = time.perf_counter()
+        r = fn()
+        out[name] = round((time.perf_counter() - t0) * 1e3, 3)
+        return r
+
+    def chain(b, prefix):
+        b.symmetrise(0)
+        ws = b.get_wsum()
+        s = timed(prefix + "update_ssnr_ms", lambda: b.update_ssnr_arrays(0, 1.0, np.full(ns, 1.0)))
+        vol = timed(prefix + "reconstruct_ms", lambda: b.reconstruct(0, do_map=True, tau2=s["tau2"],
+                                                                    normalise=ws["pdf_class"][0]))
+        return vol
+
+    bundle.reset_wsum()
+    worker.do_expectation_some_particles(dev_batch)
+    timed("symmetrise_ms", lambda: bundle.symmetrise(0))
+    bundle.set_fourier_transform_map(0, bundle.reconstruct(0), cur)  # FFT plans outside the timed calls
+    vol = chain(bundle, "")
+    timed("projector_from_map_ms", lambda: bundle.set_fourier_transform_map(0, vol, cur))
+    out["sizes"] = "current %d: padded Fourier grid %d^3, real-space transform %d^3 (FP64 cuFFT)" % (
+        cur, bundle.backprojector_dims()[1], 2 * ori)
+    # restore the workload's projector for anything run after this section
+    r = ds.ref
+    bundle.setup_projector(0, r["data"], r["yinit"], r["zinit"], r["r_max"], r["pad"])
+
+    # the same batch through the plain FP32 path; FSC between the two maps
+    m32 = dict(model, precision=0)
+    b32 = MlDeviceBundle(m32, device=local)
+    b32.setup_projector(0, r["data"], r["yinit"], r["zinit"], r["r_max"], r["pad"])
+    w32 = MlOptimiserCuda(b32)
+    w32.do_expectation_some_particles(dev_batch)
+    vol32 = chain(b32, "fp32_path_")
+    f = bundle.fsc(vol, vol32)
+    w32.close()
+    b32.close()
+    rmax = cur // 2
+    out["equal_fsc"] = {"min_fsc_precision_vs_plain": round(float(np.min(f[1:rmax])), 6),
+                        "shells": "1..%d (inside the current size)" % (rmax - 1),
+                        "note": "maps reconstructed from the same %d particles: BF16 tensor-core coarse "
+                                "pass vs plain FP32 path" % dev_batch["n"]}
+    for k in ("fp32_path_update_ssnr_ms", "fp32_path_reconstruct_ms"):
+        out.pop(k, None)
+
+    # Nyquist-limited size: current 256 (padded grid 515^3, transform 512^3)
+    mn = dict(model, current_size=ori, coarse_size=model["coarse_size"])
+    bn = MlDeviceBundle(mn, device=local)
+    xd, yd, zd = bn.backprojector_dims()[:3]
+    rng = np.random.default_rng(1)
+    data = (rng.standard_normal((zd, yd, xd)) + 1j * rng.standard_normal((zd, yd, xd))) * 1e-3
+    bn.set_mdl_data(0, data, np.ones((zd, yd, xd)))
+    del data
+    bn.symmetrise(0)
+    bn.set_fourier_transform_map(0, bn.reconstruct(0), ori)  # FFT plans outside the timed calls
+    timed("nyquist_reconstruct_ms", lambda: bn.reconstruct(0))
+    timed("nyquist_projector_from_map_ms", lambda: bn.set_fourier_transform_map(0, vol, ori))
+    bn.close()
+    return out
 
 
 def measured_peaks():
