@@ -174,6 +174,7 @@ struct gbr_bundle {
     DevBuf<float2> phase_c, phase_f;
     DevBuf<float> proj_c, proj2_c;
     DevBuf<unsigned char> proj_c_tc;  // precision form: BF16 A tiles (tcgen05 smem image)
+    DevBuf<unsigned char> proj2_c_tf; // precision form: TF32 split tiles of |P|^2 (norm term)
     DevBuf<float> proj_f, proj2_f;  // all oversampled orientations: [RF][lda_f], [RF][ldk_f]
     int ldk_f = 0, lda_f = 0;
     DevBuf<float2> bpimg;
@@ -223,6 +224,7 @@ struct gbr_worker {
     DevBuf<unsigned int> ecode;
     DevBuf<double> shell, pacc;
     DevBuf<unsigned char> ytc;  // precision form: BF16 B tiles of the batch
+    DevBuf<unsigned char> wtf;  // precision form: TF32 split tiles of the norm weights
     // coarse significance candidates
     int cand_cap = 0;
     DevBuf<unsigned int> cand_idx, cand_cnt;
@@ -406,6 +408,8 @@ int build_tables(gbr_bundle *b) {
     if (d.precision == GBR_PREC_BF16) {
         GBR_CUDA(b->proj_c_tc.reserve(tc_a_bytes((int)R, 2 * b->nc)));
         GBR_CUDA(launch_tc_pack_a(b->proj_c.p, b->lda_c, (int)R, 2 * b->nc, b->proj_c_tc.p, 0));
+        GBR_CUDA(b->proj2_c_tf.reserve(tc_norm_a_bytes((int)R, b->nc)));
+        GBR_CUDA(launch_tc_norm_pack_a(b->proj2_c.p, b->ldk_c, (int)R, b->nc, b->proj2_c_tf.p, 0));
         int flag = 0;
         GBR_CUDA(tc_error_flag(&flag, 1));
     }
@@ -643,8 +647,15 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
     GBR_CUDA(cudaMemsetAsync(w->pacc.p, 0, sizeof(double) * n * 8, st));
     GBR_CUDA(cudaEventRecord(w->ev[1], st));
     // ---- coarse norm and cross GEMMs ----
-    GBR_CUDA(launch_gemm_rows(b->proj2_c.p, b->ldk_c, R, w->a_c.p, b->ldk_c, n, b->ldk_c, w->nrm.p, R, 1, st));
-    w->launches += 3;  // prep, pdf_offset, norms
+    if (d.precision == GBR_PREC_BF16) {
+        // tensor cores, TF32 three-term split (FP32-level accuracy)
+        GBR_CUDA(w->wtf.reserve(tc_norm_b_bytes(n, b->nc)));
+        GBR_CUDA(launch_tc_norm(b->proj2_c_tf.p, w->a_c.p, b->ldk_c, (int)R, b->nc, n, w->wtf.p, w->nrm.p, st));
+        w->launches += 4;  // prep, pdf_offset, norm operand packing, norms
+    } else {
+        GBR_CUDA(launch_gemm_rows(b->proj2_c.p, b->ldk_c, R, w->a_c.p, b->ldk_c, n, b->ldk_c, w->nrm.p, R, 1, st));
+        w->launches += 3;  // prep, pdf_offset, norms
+    }
     GBR_CUDA(cudaEventRecord(w->ev[2], st));
     const bool use_rowmin = d.precision == GBR_PREC_BF16 && T >= 32 && w->coarse_rows == 0;
     // sparse diff2 writes: only row segments near the running minimum are

@@ -88,6 +88,14 @@ cudaError_t launch_fp32_probe(float *ms, double *flops);
 
 // k_tc.cu: tcgen05 BF16 coarse cross term (precision form).  Operand tiles
 // are packed into [tiles][ktiles][bytes] images (sizes from tc_*_bytes).
+// Norm term of the precision form on the tensor cores (kind::tf32, three-term
+// split: FP32-level accuracy): A = |P|^2 table packed once per iteration,
+// w = per-particle noise-weighted CTF^2 [n][ldw]; out[p][M].
+size_t tc_norm_a_bytes(int M, int K);
+size_t tc_norm_b_bytes(int N, int K);
+cudaError_t launch_tc_norm_pack_a(const float *src, int lds, int M, int K, void *dst, cudaStream_t st);
+cudaError_t launch_tc_norm(const void *Ablk, const float *w, int ldw, int M, int K, int nparticles, void *Bblk,
+                           float *out, cudaStream_t st);
 size_t tc_a_bytes(int M, int K2);
 size_t tc_y_bytes(int N, int K2);
 cudaError_t launch_tc_pack_a(const float *src, int lds, int M, int K2, void *dst, cudaStream_t st);

@@ -63,6 +63,11 @@ __host__ __device__ constexpr uint32_t make_idesc() {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TN >> 3) << 17) | ((uint32_t)(TM >> 4) << 24);
 }
 
+// Instruction descriptor, kind::tf32: D = F32, A = B = TF32, both K-major.
+__host__ __device__ constexpr uint32_t make_idesc_tf32() {
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(TN >> 3) << 17) | ((uint32_t)(TM >> 4) << 24);
+}
+
 __device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
 }
@@ -85,6 +90,15 @@ __device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64
     asm volatile(
         "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
         " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
         "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
         : "memory");
 }
@@ -212,6 +226,11 @@ __device__ __forceinline__ void rowmin_flush(const TcArgs &a, int p, int m, floa
 // barrier and each finished tile to its accumulator's tfull barrier; warps
 // 4..11 drain the other accumulator meanwhile (warp w reads TMEM lanes
 // 32 (w & 3).. and columns 128 ((w - 4) >> 2)..) and release it on tempty.
+//
+// kNorm: the same pipeline on TF32 operands (kind::tf32, K tiles of 32) for
+// the norm term N(r,p) = sum_k |P_r(k)|^2 w_p(k); the epilogue stores the
+// accumulator as out[p][M] (T = 1).
+template <bool kNorm>
 __global__ void __launch_bounds__(THREADS, 1) k_tc_diff2(const TcArgs a) {
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ __align__(8) uint64_t full[STAGES];
@@ -273,7 +292,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_diff2(const TcArgs a) {
         }
     } else if (warp == 1 && lane == 0) {
         // MMA issuer
-        const uint32_t idesc = make_idesc();
+        const uint32_t idesc = kNorm ? make_idesc_tf32() : make_idesc();
         uint32_t g = 0, i = 0;
         for (int tidx = blockIdx.x; tidx < ntotal && !*vfail; tidx += gridDim.x, ++i) {
             const uint32_t b = i & 1u;
@@ -296,7 +315,10 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_diff2(const TcArgs a) {
                 for (int kk = 0; kk < TK / 16; ++kk) {
                     const uint64_t ad = make_desc(a0 + kk * 256, 128, 1024);
                     const uint64_t bd = make_desc(b0 + kk * 256, 128, 1024);
-                    mma_bf16(acc, ad, bd, idesc, (kt | kk) != 0 ? 1u : 0u);
+                    if (kNorm)
+                        mma_tf32(acc, ad, bd, idesc, (kt | kk) != 0 ? 1u : 0u);
+                    else
+                        mma_bf16(acc, ad, bd, idesc, (kt | kk) != 0 ? 1u : 0u);
                 }
                 mma_commit(smem_u32(&empty[s]));
             }
@@ -323,6 +345,27 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_diff2(const TcArgs a) {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const int m0 = mt * TM, n0 = nt * TN;
             const int m = m0 + q * 32 + lane;
+            if (kNorm) {
+                // lane = row m; for each column the 32 lanes store 32 consecutive m
+                for (int c = 0; c < 4; ++c) {
+                    const int col = h * 128 + c * 32, nb = n0 + col;
+                    if (nb >= a.N) break;  // warp-uniform
+                    float v[32];
+                    tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + b * (uint32_t)TN + (uint32_t)col, v);
+                    const int nvalid = min(32, a.N - nb);
+                    if (m < a.M) {
+#pragma unroll
+                        for (int jj = 0; jj < 32; ++jj)
+                            if (jj < nvalid) a.out[(size_t)(nb + jj) * a.M + m] = v[jj];
+                    }
+                }
+                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                __syncwarp();
+                if (lane == 0)
+                    asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tempty[b]))
+                                 : "memory");
+                continue;
+            }
             const bool skip = !(m < a.M) || !(a.pdf_orient[m] > 0.f);
             // running row minimum of the particle segment this lane is in
             const bool track_rows = a.rowmin != nullptr && a.T >= 32 && !skip;
@@ -510,7 +553,53 @@ __global__ void k_pack_y(const float2 *__restrict__ b, int ldb, const float2 *__
         make_uint4(pack_bf16(y[0], y[1]), pack_bf16(y[2], y[3]), pack_bf16(y[4], y[5]), pack_bf16(y[6], y[7]));
 }
 
+__device__ __forceinline__ uint32_t to_tf32(float x) {
+    uint32_t u;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(u) : "f"(x));
+    return u;
+}
+
+// TF32 operand tiles of the norm term, three-term split along K:
+// A = [hi | hi | lo], B = [hi | lo | hi] (x = hi + lo, both rounded to TF32),
+// so that one K loop accumulates hi*hi + hi*lo + lo*hi.  Tiles of `rows_t`
+// rows (128 for A, 256 for B) by 32 values, same shared-memory image as the
+// BF16 tiles (16-byte chunks of 4 values).
+__global__ void k_pack_tf32(const float *__restrict__ src, int lds, int rows, int K, int nk, int rows_t, int is_b,
+                            uint8_t *__restrict__ dst, long long nchunks) {
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nchunks) return;
+    const int per = rows_t * 8;  // chunks per tile
+    const long long blk = c / per;
+    const int within = (int)(c - blk * per), row = within >> 3, kg = within & 7;
+    const int ktot = 3 * nk;
+    const int rt = (int)(blk / ktot), kk = (int)(blk - (long long)rt * ktot);
+    const int part = kk / nk, kt = kk - part * nk;
+    const bool lo = is_b ? (part == 1) : (part == 2);
+    const int r = rt * rows_t + row, k0 = kt * 32 + kg * 4;
+    uint32_t u[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const float x = (r < rows && k0 + i < K) ? src[(size_t)r * lds + k0 + i] : 0.f;
+        const uint32_t hi = to_tf32(x);
+        u[i] = lo ? to_tf32(x - __uint_as_float(hi)) : hi;
+    }
+    *reinterpret_cast<uint4 *>(dst + blk * (long long)(rows_t * 128) + chunk_off(row, kg)) =
+        make_uint4(u[0], u[1], u[2], u[3]);
+}
+
 }  // namespace
+
+size_t tc_norm_a_bytes(int M, int K) { return (size_t)((M + TM - 1) / TM) * 3 * ((K + 31) / 32) * A_BYTES; }
+size_t tc_norm_b_bytes(int N, int K) { return (size_t)((N + TN - 1) / TN) * 3 * ((K + 31) / 32) * B_BYTES; }
+
+cudaError_t launch_tc_norm_pack_a(const float *src, int lds, int M, int K, void *dst, cudaStream_t st) {
+    const int nk = (K + 31) / 32, mtiles = (M + TM - 1) / TM;
+    const long long nchunks = (long long)mtiles * 3 * nk * (TM * 8);
+    if (nchunks <= 0) return cudaSuccess;
+    k_pack_tf32<<<(unsigned)((nchunks + 255) / 256), 256, 0, st>>>(src, lds, M, K, nk, TM, 0,
+                                                                   static_cast<uint8_t *>(dst), nchunks);
+    return cudaGetLastError();
+}
 
 size_t tc_a_bytes(int M, int K2) {
     return (size_t)((M + TM - 1) / TM) * ((K2 + TK - 1) / TK) * A_BYTES;
@@ -546,7 +635,9 @@ cudaError_t launch_tc_diff2(const void *Ablk, void *Yblk, int M, int K2, const f
         e = cudaGetDevice(&dev);
         if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
         if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(k_tc_diff2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            e = cudaFuncSetAttribute(k_tc_diff2<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_tc_diff2<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) {
             nsm = 0;
             return e;
@@ -558,7 +649,36 @@ cudaError_t launch_tc_diff2(const void *Ablk, void *Yblk, int M, int K2, const f
     TcArgs a{static_cast<const uint8_t *>(Ablk), static_cast<const uint8_t *>(Yblk), M, ktiles, T, N, nparticles,
              mtiles, ntiles, out, norm, pdf_orient, ps, T >= 32 ? rowmin : nullptr,
              (T >= 32 && T <= 960 && rowmin) ? segmask : nullptr};
-    k_tc_diff2<<<grid, THREADS, smem, st>>>(a);
+    k_tc_diff2<false><<<grid, THREADS, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tc_norm(const void *Ablk, const float *w, int ldw, int M, int K, int nparticles, void *Bblk,
+                           float *out, cudaStream_t st) {
+    if (nparticles <= 0 || M <= 0) return cudaSuccess;
+    const int nk = (K + 31) / 32, ntiles = (nparticles + TN - 1) / TN, mtiles = (M + TM - 1) / TM;
+    const long long bchunks = (long long)ntiles * 3 * nk * (TN * 8);
+    k_pack_tf32<<<(unsigned)((bchunks + 255) / 256), 256, 0, st>>>(w, ldw, nparticles, K, nk, TN, 1,
+                                                                   static_cast<uint8_t *>(Bblk), bchunks);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    static int nsm = 0;
+    if (!nsm) {
+        int dev = 0;
+        e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_tc_diff2<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+        if (e != cudaSuccess) {
+            nsm = 0;
+            return e;
+        }
+    }
+    const long long ntotal = (long long)mtiles * ntiles;
+    const int grid = (int)std::min<long long>(ntotal, nsm);
+    TcArgs a{static_cast<const uint8_t *>(Ablk), static_cast<const uint8_t *>(Bblk), M, 3 * nk, 1, nparticles,
+             nparticles, mtiles, ntiles, out, nullptr, nullptr, nullptr, nullptr, nullptr};
+    k_tc_diff2<true><<<grid, THREADS, SMEM_BYTES, st>>>(a);
     return cudaGetLastError();
 }
 
