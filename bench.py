@@ -319,8 +319,9 @@ def mstep_section(args, ds, model, bundle, worker, dev_batch, local):
         out[name] = round((time.perf_counter() - t0) * 1e3, 3)
         return r
 
-    def chain(b, prefix):
-        b.symmetrise(0)
+    def chain(b, prefix, sym):
+        if sym:
+            b.symmetrise(0)
         ws = b.get_wsum()
         s = timed(prefix + "update_ssnr_ms", lambda: b.update_ssnr_arrays(0, 1.0, np.full(ns, 1.0)))
         vol = timed(prefix + "reconstruct_ms", lambda: b.reconstruct(0, do_map=True, tau2=s["tau2"],
@@ -331,10 +332,22 @@ def mstep_section(args, ds, model, bundle, worker, dev_batch, local):
     worker.do_expectation_some_particles(dev_batch)
     timed("symmetrise_ms", lambda: bundle.symmetrise(0))
     bundle.set_fourier_transform_map(0, bundle.reconstruct(0), cur)  # FFT plans outside the timed calls
-    vol = chain(bundle, "")
+    vol = chain(bundle, "", False)  # symmetrised above
     timed("projector_from_map_ms", lambda: bundle.set_fourier_transform_map(0, vol, cur))
-    out["sizes"] = "current %d: padded Fourier grid %d^3, real-space transform %d^3 (FP64 cuFFT)" % (
+    out["sizes"] = "current %d: padded Fourier grid %d^3, real-space transform %d^3" % (
         cur, bundle.backprojector_dims()[1], 2 * ori)
+    # FP32 transforms, map kept on the device between the two calls
+    ws0 = bundle.get_wsum()
+    s0 = bundle.update_ssnr_arrays(0, 1.0, np.full(ns, 1.0))
+    kw = dict(do_map=True, tau2=s0["tau2"], normalise=ws0["pdf_class"][0])
+    bundle.set_recon_precision(True)
+    bundle.set_fourier_transform_map(0, bundle.reconstruct(0, **kw), cur)  # FP32 plans
+    vol_f = timed("fp32_reconstruct_ms", lambda: bundle.reconstruct(0, **kw))
+    timed("fp32_reconstruct_on_device_ms", lambda: bundle.reconstruct(0, to_host=False, **kw))
+    timed("fp32_projector_from_device_map_ms", lambda: bundle.set_fourier_transform_map(0, None, cur))
+    bundle.set_recon_precision(False)
+    out["fp32_map_rel_l2_vs_fp64"] = float(np.linalg.norm(vol_f - vol) / np.linalg.norm(vol))
+    out["transforms"] = "*_ms: FP64 cuFFT (the reference's precision); fp32_*: FP32 cuFFT, FP64 weights and sums"
     # restore the workload's projector for anything run after this section
     r = ds.ref
     bundle.setup_projector(0, r["data"], r["yinit"], r["zinit"], r["r_max"], r["pad"])
@@ -345,7 +358,7 @@ def mstep_section(args, ds, model, bundle, worker, dev_batch, local):
     b32.setup_projector(0, r["data"], r["yinit"], r["zinit"], r["r_max"], r["pad"])
     w32 = MlOptimiserCuda(b32)
     w32.do_expectation_some_particles(dev_batch)
-    vol32 = chain(b32, "fp32_path_")
+    vol32 = chain(b32, "fp32_path_", True)
     f = bundle.fsc(vol, vol32)
     w32.close()
     b32.close()

@@ -301,10 +301,17 @@ typedef struct {
     double normalise;       /* wsum_model.pdf_class[iclass] (used with gridding)         */
 } gbr_recon_params;
 
+/* Precision of the reconstruction-side transforms (gbr_reconstruct,
+ * gbr_projector_from_map, gbr_fsc): FP64 (the reference's precision, the
+ * default) or FP32 cuFFT; the weights, shell sums and maps stay FP64. */
+enum { GBR_RECON_FP64 = 0, GBR_RECON_FP32 = 1 };
+int gbr_recon_set_precision(gbr_bundle *b, int precision);
+
 /* BackProjector::reconstruct (src/backprojector.cpp:1379-1872) of one
  * class's device volumes into the real-space map vol_out [ori]^ref_dim
  * (z, y, x; mymodel.Iref[iclass]); tau2 [ori/2+1] is read when do_map.
- * Transforms are cuFFT double precision. */
+ * vol_out may be NULL: the map then stays on the device only, for a
+ * following gbr_projector_from_map with vol = NULL. */
 int gbr_reconstruct(gbr_bundle *b, int64_t iclass, const gbr_recon_params *p, const double *tau2, double *vol_out);
 
 /* Projector::computeFourierTransformMap (src/projector.cpp:116-593, called by
@@ -312,7 +319,9 @@ int gbr_reconstruct(gbr_bundle *b, int64_t iclass, const gbr_recon_params *p, co
  * vol [ori]^ref_dim straight into class iclass's device projector, in place
  * of gbr_projector_upload: gridding pre-correction, zero padding, forward
  * transform, r <= r_max(current_size) kept; power_spectrum [ori/2+1]
- * (tau2_class when updating it) or NULL; min_ires <= 0: no high-pass. */
+ * (tau2_class when updating it) or NULL; min_ires <= 0: no high-pass.
+ * vol = NULL: the device-resident map of the bundle's last gbr_reconstruct
+ * (no other reconstruction-side call in between). */
 int gbr_projector_from_map(gbr_bundle *b, int64_t iclass, const double *vol, int64_t current_size,
                            int do_gridding, int64_t min_ires, double *power_spectrum);
 

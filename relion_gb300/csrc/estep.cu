@@ -465,7 +465,7 @@ int ensure_capacity(gbr_worker *w, int n) {
     const int W = (int)((b->T + 31) / 32);
     GBR_CUDA(w->mask.reserve((size_t)n * b->R * W));
     GBR_CUDA(w->cnt.reserve((size_t)n * b->R));
-    GBR_CUDA(w->scan_tmp.reserve(2 * (((size_t)n * b->R + 1023) / 1024) + 2));
+    GBR_CUDA(w->scan_tmp.reserve(2 * (size_t)fine_jobs_nblocks((long long)n * b->R) + 2));
     GBR_CUDA(w->jobs.reserve((size_t)n * b->R));
     GBR_CUDA(w->need_r.reserve(b->R));
     GBR_CUDA(w->shell.reserve((size_t)n * b->nshell));
@@ -481,9 +481,14 @@ int ensure_capacity(gbr_worker *w, int n) {
 int threshold_search(gbr_worker *w, int n, float *vals, const long long *seg, long long max_len, int coarse,
                      const long long *seg_end = nullptr, long long n_total = 0) {
     gbr_bundle *b = w->b;
-    w->launches += 6;
     const double f = b->d.adaptive_fraction;
     const int pass = coarse ? 1 : 2;
+    if (max_len <= kSelectFusedMax) {
+        w->launches += 1;
+        GBR_CUDA(launch_select_fused(vals, seg, seg_end, n, n_total, pass, f, coarse, w->ps.p, w->st));
+        return GBR_OK;
+    }
+    w->launches += 6;
     GBR_CUDA(launch_hist_refine(vals, seg, n, max_len, 0, w->ps.p, w->hist.p, w->st, pass, f, seg_end, n_total));
     GBR_CUDA(launch_select(n, 0, f, coarse, w->ps.p, w->hist.p, w->st));
     GBR_CUDA(launch_hist_refine(vals, seg, n, max_len, 1, w->ps.p, w->hist.p, w->st, pass, f, seg_end, n_total));
@@ -728,7 +733,7 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
         GBR_CUDA(cudaMemcpyAsync(w->dbg_wcoarse.data(), dense_w, sizeof(float) * n * RT, cudaMemcpyDeviceToHost, st));
     }
     const long long nR = (long long)n * R;
-    const long long nbj = (nR + 1023) / 1024;
+    const long long nbj = fine_jobs_nblocks(nR);
     for (int attempt = 0;; ++attempt) {
         GBR_CUDA(cudaEventRecord(w->ev[4], st));
         GBR_CUDA(cudaMemsetAsync(w->need_r.p, 0, R, st));
@@ -1376,6 +1381,15 @@ int recon_begin(gbr_bundle *b, int64_t iclass) {
 }
 }  // namespace
 
+int gbr_recon_set_precision(gbr_bundle *b, int precision) {
+    int st = recon_begin(b, 0);
+    if (st) return st;
+    if (precision != GBR_RECON_FP64 && precision != GBR_RECON_FP32)
+        return fail(GBR_ERR_INVALID, "unknown reconstruction precision");
+    gbr::recon_set_fp32(b->recon, precision == GBR_RECON_FP32);
+    return GBR_OK;
+}
+
 int gbr_backprojector_symmetrise(gbr_bundle *b, int64_t iclass) {
     int st = recon_begin(b, iclass);
     if (st) return st;
@@ -1396,7 +1410,7 @@ int gbr_update_ssnr(gbr_bundle *b, int64_t iclass, double tau2_fudge, double *ta
 int gbr_reconstruct(gbr_bundle *b, int64_t iclass, const gbr_recon_params *p, const double *tau2, double *vol_out) {
     int st = recon_begin(b, iclass);
     if (st) return st;
-    if (!p || !vol_out) return fail(GBR_ERR_INVALID, "null argument");
+    if (!p) return fail(GBR_ERR_INVALID, "null argument");
     const gbr::ReconParams rp{p->max_iter_preweight, p->do_map, p->skip_gridding, p->minres_map, p->tau2_fudge,
                               p->normalise};
     return gbr::recon_reconstruct(b->recon, b->bp_data[iclass].p, b->bp_weight[iclass].p, b->bg,
@@ -1407,7 +1421,6 @@ int gbr_projector_from_map(gbr_bundle *b, int64_t iclass, const double *vol, int
                            int do_gridding, int64_t min_ires, double *power_spectrum) {
     int st = recon_begin(b, iclass);
     if (st) return st;
-    if (!vol) return fail(GBR_ERR_INVALID, "null map");
     const int dim = b->is2d ? 2 : 3;
     const gbr::VolGeom g = gbr::projector_geometry((int)b->d.ori_size, dim, (int)b->d.padding_factor,
                                                    (int)current_size);

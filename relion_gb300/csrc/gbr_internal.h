@@ -176,6 +176,12 @@ cudaError_t launch_weights_cand(const float *vals, int n, int R, int T, const fl
 cudaError_t launch_cand_masks(const unsigned int *cand_idx, const float *cand_w, const unsigned int *cand_cnt,
                               int cap, int n, int R, int T, int W, const ParticleState *ps, unsigned int *mask,
                               int *cnt, cudaStream_t st);
+// The three levels of the threshold search in one launch, one block per
+// particle (segments up to kSelectFusedMax elements).
+constexpr long long kSelectFusedMax = 1LL << 17;
+cudaError_t launch_select_fused(const float *vals, const long long *seg, const long long *seg_end, int n,
+                                long long n_total, int pass, double fraction, int coarse, ParticleState *ps,
+                                cudaStream_t st);
 cudaError_t launch_select(int n, int level, double adaptive_fraction, int coarse, ParticleState *ps,
                           HistBin *hist, cudaStream_t st);
 cudaError_t launch_sig_masks(const float *w, int n, int R, int T, int W, const ParticleState *ps,
@@ -183,6 +189,9 @@ cudaError_t launch_sig_masks(const float *w, int n, int R, int T, int W, const P
 // Fine-pass job list: jobs[] in (p, r) order for cnt > 0, seg[p] = first fine
 // entry of particle p, seg[n] = total; sums holds 2 * ceil(n R / 1024) + 2
 // values and ends with (number of jobs, number of fine entries).
+// blocks of the job-list scan for tot (particle, orientation) counts; the
+// totals (jobs, entries) land at sums[2 nblocks], sums[2 nblocks + 1]
+long long fine_jobs_nblocks(long long tot);
 cudaError_t launch_fine_jobs(const int *cnt, int n, int R, int per, long long *sums, FineJob *jobs, long long *seg,
                              unsigned char *need_r, cudaStream_t st);
 cudaError_t launch_fine_diff2(const FineJob *jobs, long long njobs, const unsigned int *mask,
@@ -261,6 +270,8 @@ namespace gbr {
 struct ReconWork;  // device scratch and cached double-precision FFT plans
 ReconWork *recon_work_create();
 void recon_work_destroy(ReconWork *w);
+// transforms in FP32 (1) or FP64 (0, default)
+void recon_set_fp32(ReconWork *w, int fp32);
 struct ReconParams {
     int max_iter_preweight, do_map, skip_gridding, minres_map;
     double tau2_fudge, normalise;

@@ -476,23 +476,40 @@ k_hist_refine(const float *__restrict__ vals, const long long *__restrict__ seg,
         }
 }
 
-// One block per particle: walk the histogram from the largest weights down
-// and find the bucket in which the cumulative weight first exceeds the
-// target (the break of the loop at src/ml_optimiser.cpp:8158-8179).  After
-// level 2 the bucket is a single float value: the significant weight.
-// The histogram is cleared for the next level.
-__global__ void k_select(int level, double fraction, int coarse, ParticleState *__restrict__ ps,
-                         HistBin *__restrict__ hist) {
-    const int p = blockIdx.x;
+// Histogram bins of the threshold search: in global memory (one HistBin per
+// bin, filled by k_hist_refine) or in shared memory (k_select_fused).
+struct GlobalBins {
+    const HistBin *hp;
+    __device__ double sum(int b) const { return hp[b].sum; }
+    __device__ unsigned int count(int b) const { return hp[b].count; }
+};
+struct SharedBins {
+    const double *hs;
+    const unsigned int *hc;
+    __device__ double sum(int b) const { return hs[b]; }
+    __device__ unsigned int count(int b) const { return hc[b]; }
+};
+
+// Scratch of select_level in shared memory: one (sum, count) per thread.
+struct SelectScratch {
+    double *ssum;
+    unsigned int *scnt;
+    int *found_bin;
+    double *found_above;
+    unsigned int *found_cnt_above;
+};
+
+// One level of the search for the block's particle: walk the histogram from
+// the largest weights down and find the bucket in which the cumulative
+// weight first exceeds the target (the break of the loop at
+// src/ml_optimiser.cpp:8158-8179).  After level 2 the bucket is a single
+// float value: the significant weight.  All threads of the block take part.
+template <class Bins>
+__device__ void select_level(int level, double fraction, int coarse, ParticleState &s, const Bins &bins,
+                             const SelectScratch &sc) {
     const int nb = level == 2 ? 128 : kHistBins;
-    const int per = (nb + blockDim.x - 1) / blockDim.x;   // bins per thread
-    __shared__ double ssum[256];
-    __shared__ unsigned int scnt[256];
-    __shared__ int found_bin;
-    __shared__ double found_above;
-    __shared__ unsigned int found_cnt_above;
-    HistBin *hp = hist + (size_t)p * kHistBins;
-    ParticleState &s = ps[p];
+    const int nt = (int)blockDim.x;
+    const int per = (nb + nt - 1) / nt;   // bins per thread
     if (level == 0) {
         if (threadIdx.x == 0) {
             s.target = fraction * (coarse ? s.sum_coarse : s.sum_fine);
@@ -510,76 +527,76 @@ __global__ void k_select(int level, double fraction, int coarse, ParticleState *
     for (int q = 0; q < per; ++q) {
         const int b = hi - q;
         if (b >= 0) {
-            my += hp[b].sum;
-            myc += hp[b].count;
+            my += bins.sum(b);
+            myc += bins.count(b);
         }
     }
-    ssum[threadIdx.x] = my;
-    scnt[threadIdx.x] = myc;
-    if (threadIdx.x == 0) found_bin = -1;
+    sc.ssum[threadIdx.x] = my;
+    sc.scnt[threadIdx.x] = myc;
+    if (threadIdx.x == 0) *sc.found_bin = -1;
     __syncthreads();
     // inclusive scan (Hillis-Steele) over threads in descending-bin order
-    for (int o = 1; o < (int)blockDim.x; o <<= 1) {
-        double v = threadIdx.x >= (unsigned)o ? ssum[threadIdx.x - o] : 0.;
-        unsigned int c = threadIdx.x >= (unsigned)o ? scnt[threadIdx.x - o] : 0u;
+    for (int o = 1; o < nt; o <<= 1) {
+        double v = threadIdx.x >= (unsigned)o ? sc.ssum[threadIdx.x - o] : 0.;
+        unsigned int c = threadIdx.x >= (unsigned)o ? sc.scnt[threadIdx.x - o] : 0u;
         __syncthreads();
-        ssum[threadIdx.x] += v;
-        scnt[threadIdx.x] += c;
+        sc.ssum[threadIdx.x] += v;
+        sc.scnt[threadIdx.x] += c;
         __syncthreads();
     }
-    const double incl = ssum[threadIdx.x];
+    const double incl = sc.ssum[threadIdx.x];
     const double excl = incl - my;
-    const unsigned int excl_c = scnt[threadIdx.x] - myc;
+    const unsigned int excl_c = sc.scnt[threadIdx.x] - myc;
     if (above0 + excl <= target && above0 + incl > target) {
         double cum = above0 + excl;
         unsigned int cc = excl_c;
         for (int q = 0; q < per; ++q) {
             const int b = hi - q;
             if (b < 0) break;
-            const double bs = hp[b].sum;
+            const double bs = bins.sum(b);
             if (cum + bs > target) {
-                found_bin = b;
-                found_above = cum;
-                found_cnt_above = cc;
+                *sc.found_bin = b;
+                *sc.found_above = cum;
+                *sc.found_cnt_above = cc;
                 break;
             }
             cum += bs;
-            cc += hp[b].count;
+            cc += bins.count(b);
         }
     }
     __syncthreads();
-    if (threadIdx.x == 0 && found_bin < 0) {
+    if (threadIdx.x == 0 && *sc.found_bin < 0) {
         // target not exceeded (fraction >= 1): the smallest positive weight
         double cum = above0;
         unsigned int cc = s.sel_count_above;
         int last = -1;
         for (int b = nb - 1; b >= 0; --b)
-            if (hp[b].count) {
+            if (bins.count(b)) {
                 if (last >= 0) {
-                    cum += hp[last].sum;
-                    cc += hp[last].count;
+                    cum += bins.sum(last);
+                    cc += bins.count(last);
                 }
                 last = b;
             }
-        found_bin = last < 0 ? 0 : last;
-        found_above = cum;
-        found_cnt_above = cc - s.sel_count_above;
+        *sc.found_bin = last < 0 ? 0 : last;
+        *sc.found_above = cum;
+        *sc.found_cnt_above = cc - s.sel_count_above;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        const int b = found_bin;
+        const int b = *sc.found_bin;
         const unsigned int prefix = (level == 0) ? (unsigned)b
                                   : (level == 1) ? ((s.sel_prefix << 12) | (unsigned)b)
                                                  : ((s.sel_prefix << 7) | (unsigned)b);
         s.sel_prefix = prefix;
-        s.sel_count_above += found_cnt_above;
-        s.sel_above = found_above;
+        s.sel_count_above += *sc.found_cnt_above;
+        s.sel_above = *sc.found_above;
         if (level == 2) {
             const float v = __uint_as_float(prefix);
             // ties: the loop stops inside the run of equal values
             const double need = (s.target - s.sel_above) / (double)v;
             unsigned int k = (need >= 0.) ? (unsigned int)floor(need) + 1u : 1u;
-            const unsigned int nb_cnt = hp[b].count;
+            const unsigned int nb_cnt = bins.count(b);
             if (k > nb_cnt) k = nb_cnt;
             if (k < 1u) k = 1u;
             if (coarse) {
@@ -591,9 +608,77 @@ __global__ void k_select(int level, double fraction, int coarse, ParticleState *
         }
     }
     __syncthreads();
+}
+
+// One block per particle, one level; the global histogram is cleared for
+// the next level.
+__global__ void k_select(int level, double fraction, int coarse, ParticleState *__restrict__ ps,
+                         HistBin *__restrict__ hist) {
+    __shared__ double ssum[256];
+    __shared__ unsigned int scnt[256];
+    __shared__ int found_bin;
+    __shared__ double found_above;
+    __shared__ unsigned int found_cnt_above;
+    HistBin *hp = hist + (size_t)blockIdx.x * kHistBins;
+    select_level(level, fraction, coarse, ps[blockIdx.x], GlobalBins{hp},
+                 SelectScratch{ssum, scnt, &found_bin, &found_above, &found_cnt_above});
     for (int i = threadIdx.x; i < kHistBins; i += blockDim.x) {
         hp[i].sum = 0.;
         hp[i].count = 0u;
+    }
+}
+
+// The whole three-level search of one particle in one block, histograms in
+// shared memory: for segments short enough that one block streams them
+// three times faster than six launches over many blocks (candidate lists,
+// sparse fine entries).  Same filters and arithmetic as k_hist_refine +
+// k_select.
+constexpr int kSelThreads = 512;
+__global__ void __launch_bounds__(kSelThreads)
+k_select_fused(const float *__restrict__ vals, const long long *__restrict__ seg, const long long *__restrict__ seg_end,
+               long long n_total, int pass, double fraction, int coarse, ParticleState *__restrict__ ps) {
+    extern __shared__ double dsm[];
+    double *hsum = dsm;
+    double *ssum = hsum + kHistBins;
+    unsigned int *hcnt = reinterpret_cast<unsigned int *>(ssum + kSelThreads);
+    unsigned int *scnt = hcnt + kHistBins;
+    __shared__ int found_bin;
+    __shared__ double found_above;
+    __shared__ unsigned int found_cnt_above;
+    const int p = blockIdx.x;
+    ParticleState &s = ps[p];
+    const long long b0 = seg[p], b1 = seg_end ? seg_end[p] : seg[p + 1];
+    float eps = 0.f;
+    if (pass) {
+        const double sum = pass == 1 ? s.sum_coarse : s.sum_fine;
+        eps = (float)((1.0 - fraction) * sum / (double)(n_total > 0 ? n_total : b1 - b0));
+    }
+    const SelectScratch sc{ssum, scnt, &found_bin, &found_above, &found_cnt_above};
+    for (int level = 0; level < 3; ++level) {
+        const int nb = level == 2 ? 128 : kHistBins;
+        const int shift = level == 0 ? 31 : (level == 1 ? 19 : 7);
+        const int fshift = level == 0 ? 19 : (level == 1 ? 7 : 0);
+        const unsigned int fmask = level == 2 ? 0x7Fu : 0xFFFu;
+        for (int i = threadIdx.x; i < kHistBins; i += blockDim.x) {
+            hsum[i] = 0.;
+            hcnt[i] = 0u;
+        }
+        __syncthreads();
+        const unsigned int prefix = level == 0 ? 0u : s.sel_prefix;
+        for (long long e = b0 + threadIdx.x; e < b1; e += blockDim.x) {
+            const float w = vals[e];
+            if (w > 0.f && w >= eps) {
+                const unsigned int u = __float_as_uint(w);
+                if ((u >> shift) == prefix) {
+                    const unsigned int bin = (u >> fshift) & fmask;
+                    atomicAdd(&hsum[bin], (double)w);
+                    atomicAdd(&hcnt[bin], 1u);
+                }
+            }
+        }
+        __syncthreads();
+        (void)nb;
+        select_level(level, fraction, coarse, s, SharedBins{hsum, hcnt}, sc);
     }
 }
 
@@ -671,12 +756,41 @@ __device__ __forceinline__ void block_excl_scan2(long long &a, long long &b, lon
     tb = wb[32];
 }
 
-__global__ void __launch_bounds__(kScanBlock) k_jobs_reduce(const int *__restrict__ cnt, long long n, int per,
-                                                           long long *__restrict__ sums) {
+// Job-list kernels: each thread takes kJobsPer consecutive (particle,
+// orientation) counts (vector loads; the array is mostly zeros), a block
+// kJobsThreads * kJobsPer of them.
+constexpr int kJobsThreads = 256, kJobsPer = 16;
+
+__device__ __forceinline__ void load_counts(const int *__restrict__ cnt, long long base, long long tot,
+                                            int (&c)[kJobsPer]) {
+    if (base + kJobsPer <= tot && (base & 3) == 0) {
+        const int4 *v = reinterpret_cast<const int4 *>(cnt + base);
+#pragma unroll
+        for (int q = 0; q < kJobsPer / 4; ++q) {
+            const int4 x = __ldg(v + q);
+            c[4 * q] = x.x;
+            c[4 * q + 1] = x.y;
+            c[4 * q + 2] = x.z;
+            c[4 * q + 3] = x.w;
+        }
+    } else {
+#pragma unroll
+        for (int q = 0; q < kJobsPer; ++q) c[q] = (base + q < tot) ? cnt[base + q] : 0;
+    }
+}
+
+__global__ void __launch_bounds__(kJobsThreads) k_jobs_reduce(const int *__restrict__ cnt, long long n, int per,
+                                                             long long *__restrict__ sums) {
     __shared__ long long wa[33], wb[33];
-    const long long i = (long long)blockIdx.x * kScanBlock + threadIdx.x;
-    const int c = i < n ? cnt[i] : 0;
-    long long f = c > 0 ? 1 : 0, e = (long long)c * per, tf, te;
+    const long long base = ((long long)blockIdx.x * kJobsThreads + threadIdx.x) * kJobsPer;
+    int c[kJobsPer];
+    load_counts(cnt, base, n, c);
+    long long f = 0, e = 0, tf, te;
+#pragma unroll
+    for (int q = 0; q < kJobsPer; ++q) {
+        f += c[q] > 0 ? 1 : 0;
+        e += (long long)c[q] * per;
+    }
     block_excl_scan2(f, e, wa, wb, tf, te);
     if (threadIdx.x == 0) {
         sums[2 * blockIdx.x] = tf;
@@ -710,33 +824,47 @@ __global__ void __launch_bounds__(kScanBlock) k_jobs_scan_sums(long long *__rest
     }
 }
 
-__global__ void __launch_bounds__(kScanBlock) k_jobs_emit(const int *__restrict__ cnt, int n, int R, int per,
-                                                         const long long *__restrict__ sums, int nb,
-                                                         FineJob *__restrict__ jobs, long long *__restrict__ seg,
-                                                         unsigned char *__restrict__ need_r) {
+__global__ void __launch_bounds__(kJobsThreads) k_jobs_emit(const int *__restrict__ cnt, int n, int R, int per,
+                                                           const long long *__restrict__ sums, int nb,
+                                                           FineJob *__restrict__ jobs, long long *__restrict__ seg,
+                                                           unsigned char *__restrict__ need_r) {
     __shared__ long long wa[33], wb[33];
     const long long tot = (long long)n * R;
-    const long long i = (long long)blockIdx.x * kScanBlock + threadIdx.x;
-    const int c = i < tot ? cnt[i] : 0;
-    long long f = c > 0 ? 1 : 0, e = (long long)c * per, tf, te;
+    const long long base = ((long long)blockIdx.x * kJobsThreads + threadIdx.x) * kJobsPer;
+    int c[kJobsPer];
+    load_counts(cnt, base, tot, c);
+    long long f = 0, e = 0, tf, te;
+#pragma unroll
+    for (int q = 0; q < kJobsPer; ++q) {
+        f += c[q] > 0 ? 1 : 0;
+        e += (long long)c[q] * per;
+    }
     block_excl_scan2(f, e, wa, wb, tf, te);
     f += sums[2 * blockIdx.x];
     e += sums[2 * blockIdx.x + 1];
-    if (i < tot) {
-        const int p = (int)(i / R), r = (int)(i - (long long)p * R);
-        if (c > 0) {
-            FineJob j;
-            j.p = p;
-            j.r = r;
-            j.n_t = c;
-            j.pad_ = 0;
-            j.off = e;
-            jobs[f] = j;
-            need_r[r] = 1;
+    if (base < tot) {
+        int p = (int)(base / R), r = (int)(base - (long long)p * R);
+        for (int q = 0; q < kJobsPer && base + q < tot; ++q) {
+            if (r == 0) seg[p] = e;
+            if (c[q] > 0) {
+                FineJob j;
+                j.p = p;
+                j.r = r;
+                j.n_t = c[q];
+                j.pad_ = 0;
+                j.off = e;
+                jobs[f] = j;
+                need_r[r] = 1;
+                ++f;
+                e += (long long)c[q] * per;
+            }
+            if (++r == R) {
+                r = 0;
+                ++p;
+            }
         }
-        if (r == 0) seg[p] = e;
     }
-    if (i == 0) seg[n] = sums[2 * nb + 1];
+    if (base == 0) seg[n] = sums[2 * nb + 1];
 }
 
 // ---------------------------------------------------------------------------
@@ -1360,6 +1488,25 @@ cudaError_t launch_hist_refine(const float *vals, const long long *seg, int n, l
     return cudaGetLastError();
 }
 
+size_t select_fused_smem() { return kHistBins * (sizeof(double) + sizeof(unsigned int)) +
+                                     kSelThreads * (sizeof(double) + sizeof(unsigned int)); }
+
+cudaError_t launch_select_fused(const float *vals, const long long *seg, const long long *seg_end, int n,
+                                long long n_total, int pass, double fraction, int coarse, ParticleState *ps,
+                                cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(k_select_fused, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)select_fused_smem());
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    k_select_fused<<<n, kSelThreads, select_fused_smem(), st>>>(vals, seg, seg_end, n_total, pass, fraction, coarse,
+                                                                 ps);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_select(int n, int level, double adaptive_fraction, int coarse, ParticleState *ps,
                           HistBin *hist, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
@@ -1380,12 +1527,17 @@ cudaError_t launch_fine_jobs(const int *cnt, int n, int R, int per, long long *s
                              unsigned char *need_r, cudaStream_t st) {
     const long long tot = (long long)n * R;
     if (tot <= 0) return cudaSuccess;
-    const long long nb = (tot + kScanBlock - 1) / kScanBlock;
+    const long long nb = fine_jobs_nblocks(tot);
     if (nb > 0x7fffffffLL) return cudaErrorInvalidValue;
-    k_jobs_reduce<<<(unsigned)nb, kScanBlock, 0, st>>>(cnt, tot, per, sums);
+    k_jobs_reduce<<<(unsigned)nb, kJobsThreads, 0, st>>>(cnt, tot, per, sums);
     k_jobs_scan_sums<<<1, kScanBlock, 0, st>>>(sums, (int)nb);
-    k_jobs_emit<<<(unsigned)nb, kScanBlock, 0, st>>>(cnt, n, R, per, sums, (int)nb, jobs, seg, need_r);
+    k_jobs_emit<<<(unsigned)nb, kJobsThreads, 0, st>>>(cnt, n, R, per, sums, (int)nb, jobs, seg, need_r);
     return cudaGetLastError();
+}
+
+long long fine_jobs_nblocks(long long tot) {
+    const long long per_block = (long long)kJobsThreads * kJobsPer;
+    return (tot + per_block - 1) / per_block;
 }
 
 cudaError_t launch_fine_diff2(const FineJob *jobs, long long njobs, const unsigned int *mask, int R,

@@ -15,6 +15,7 @@
 #include <algorithm>
 #include <cmath>
 #include <map>
+#include <type_traits>
 #include <string>
 #include <vector>
 
@@ -45,6 +46,18 @@ struct Half {
 };
 
 Half make_half(int N, int dim) { return Half{N, dim == 3 ? N : 1, N, N / 2 + 1, dim}; }
+
+// element types of the transformed arrays: FP64 (the reference's precision)
+// or FP32 (GB300's FP64 rate is a small fraction of its FP32 rate); weights,
+// shell sums and the final map stay FP64 either way
+template <class R> struct Cx;
+template <> struct Cx<double> { typedef double2 T; };
+template <> struct Cx<float> { typedef float2 T; };
+template <class R> __device__ __forceinline__ typename Cx<R>::T cmake(double a, double b);
+template <> __device__ __forceinline__ double2 cmake<double>(double a, double b) { return make_double2(a, b); }
+template <> __device__ __forceinline__ float2 cmake<float>(double a, double b) {
+    return make_float2((float)a, (float)b);
+}
 
 __host__ __device__ __forceinline__ int d_round(double x) { return (x > 0) ? (int)(x + 0.5) : (int)(x - 0.5); }
 
@@ -158,9 +171,10 @@ __global__ void k_radavg(const double *weight, VolGeom g, Half h, int max_r2, in
 // gridding weights (:1683-1694), and CenterFFTbySign (src/fftw.h:389-402).
 // mode 0: skip gridding (sums = radial sums [2][r_max]); mode 1: gridding
 // (fn = Fnewweight on hin, data divided by normalise).
+template <class R>
 __global__ void k_window(const double2 *data, const double *weight, VolGeom g, Half hin, Half hout, int max_r2,
                          MapTerm m, int mode, const double *sums, int r_max, const double *fn, double normalise,
-                         double2 *out, int *err) {
+                         typename Cx<R>::T *out, int *err) {
     extern __shared__ double ra[];
     if (mode == 0) {
         for (int b = threadIdx.x; b < r_max; b += blockDim.x) {
@@ -197,14 +211,19 @@ __global__ void k_window(const double2 *data, const double *weight, VolGeom g, H
             }
         }
         if ((k ^ i ^ j) & 1) v = make_double2(-v.x, -v.y);
-        out[n] = v;
+        // self-conjugate elements (every index 0 or N/2) are real: the
+        // half-complex inverse ignores their imaginary parts (FFTW's c2r does;
+        // cuFFT's FP32 C2R does not)
+        if ((k == 0 || 2 * k == hout.Z) && (i == 0 || 2 * i == hout.Y) && (j == 0 || 2 * j == hout.N)) v.y = 0.;
+        out[n] = cmake<R>(v.x, v.y);
     }
 }
 
 // gridding branch initialisation (:1571-1598): Fweight / normalise, the
 // Fnewweight indicator and the first convolution input Fnewweight * Fweight
+template <class R>
 __global__ void k_grid_init(const double *weight, VolGeom g, Half h, int max_r2, MapTerm m, double normalise,
-                            double *fw, double *fn, double2 *C) {
+                            double *fw, double *fn, typename Cx<R>::T *C) {
     for (long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x; n < h.size();
          n += (long long)gridDim.x * blockDim.x) {
         int k, i, j;
@@ -215,14 +234,15 @@ __global__ void k_grid_init(const double *weight, VolGeom g, Half h, int max_r2,
         const double f = (r2 < max_r2) ? 1. : 0.;
         fw[n] = w;
         fn[n] = f;
-        C[n] = make_double2(f * w, 0.);
+        C[n] = cmake<R>(f * w, 0.);
     }
 }
 
 // convoluteBlobRealSpace (:2483-2528) on the real array of an in-place
 // transform: multiply by the blob's Fourier value over its value at 0, and
 // by 1 / N^dim, the normalisation of the forward transform that follows
-__global__ void k_blob(double *M, Half h, const double *tab, double sampling, double inv_norm, double inv_scale,
+template <class R>
+__global__ void k_blob(R *M, Half h, const double *tab, double sampling, double inv_norm, double inv_scale,
                        double ori_pad) {
     const int padh = h.N / 2;
     const long long total = (long long)h.Z * h.Y * h.N;
@@ -236,13 +256,14 @@ __global__ void k_blob(double *M, Half h, const double *tab, double sampling, do
         const double rval = sqrt((double)(kp * kp + ip * ip + jp * jp)) / ori_pad;
         const int idx = (int)(fabs(rval) / sampling);
         const double b = (idx >= kBlobTab) ? 0. : tab[idx];
-        double &e = M[((long long)k * h.Y + i) * h.rowp() + j];
-        e = e * (b * inv_norm) * inv_scale;
+        R &e = M[((long long)k * h.Y + i) * h.rowp() + j];
+        e = (R)((double)e * (b * inv_norm) * inv_scale);
     }
 }
 
 // one gridding iteration's division (:1633-1649) and the next input
-__global__ void k_grid_update(double2 *C, const double *fw, double *fn, Half h, int max_r2) {
+template <class R>
+__global__ void k_grid_update(typename Cx<R>::T *C, const double *fw, double *fn, Half h, int max_r2) {
     for (long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x; n < h.size();
          n += (long long)gridDim.x * blockDim.x) {
         int k, i, j;
@@ -250,17 +271,18 @@ __global__ void k_grid_update(double2 *C, const double *fw, double *fn, Half h, 
         const int kp = h.kp(k), ip = h.ip(i);
         double f = fn[n];
         if (kp * kp + ip * ip + j * j < max_r2) {
-            const double2 c = C[n];
-            f /= fmax(1e-6, sqrt(c.x * c.x + c.y * c.y));
+            const double cx = C[n].x, cy = C[n].y;
+            f /= fmax(1e-6, sqrt(cx * cx + cy * cy));
             fn[n] = f;
         }
-        C[n] = make_double2(f * fw[n], 0.);
+        C[n] = cmake<R>(f * fw[n], 0.);
     }
 }
 
 // window the padded real box to ori (centred), divide by normfft and sum the
 // background of softMaskOutsideMap (radius ori/2, cosine width 3): bg [2]
-__global__ void k_crop_bg(const double *M, int No, int rowp, int ori, int dim, double normfft, double *vol,
+template <class R>
+__global__ void k_crop_bg(const R *M, int No, int rowp, int ori, int dim, double normfft, double *vol,
                           double *bg) {
     __shared__ double s_sum[kThreads / 32], s_bg[kThreads / 32];
     const int h = ori / 2, off = No / 2 - h;
@@ -273,7 +295,7 @@ __global__ void k_crop_bg(const double *M, int No, int rowp, int ori, int dim, d
         const long long t = n / ori;
         const int y = (int)(t % ori), z = (int)(t / ori);
         const int zo = dim == 3 ? z + off : 0;
-        const double v = M[((long long)zo * No + (y + off)) * rowp + (x + off)] / normfft;
+        const double v = (double)M[((long long)zo * No + (y + off)) * rowp + (x + off)] / normfft;
         vol[n] = v;
         const int k = dim == 3 ? z - h : 0, i = y - h, j = x - h;
         const double r = sqrt((double)(k * k + i * i + j * j));
@@ -340,8 +362,9 @@ __global__ void k_mask_gridcorr(double *vol, int ori, int dim, double ori_pad, c
 
 // computeFourierTransformMap: gridding pre-correction and zero padding into
 // the real rows of an in-place transform of size No
+template <class R>
 __global__ void k_pad_map(const double *vol, int ori, int dim, int No, int rowp, double ori_pad, int do_grid,
-                          double *M) {
+                          R *M) {
     const int h = ori / 2, ho = No / 2;
     const long long total = (long long)(dim == 3 ? No : 1) * No * rowp;
     for (long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x; n < total;
@@ -362,13 +385,14 @@ __global__ void k_pad_map(const double *vol, int ori, int dim, int No, int rowp,
                 }
             }
         }
-        M[n] = v;
+        M[n] = (R)v;
     }
 }
 
 // computeFourierTransformMap (:505-536): normalise, CenterFFTbySign, keep
 // r2 <= max_r2 in the projector layout, radial power [2][ns]
-__global__ void k_fill_projector(const double2 *F, Half h, VolGeom pg, int max_r2, int min_r2, double nreal,
+template <class R>
+__global__ void k_fill_projector(const typename Cx<R>::T *F, Half h, VolGeom pg, int max_r2, int min_r2, double nreal,
                                  double normfft, double pad, int ns, float2 *proj, double *power) {
     extern __shared__ double sh[];
     for (int b = threadIdx.x; b < 2 * ns; b += blockDim.x) sh[b] = 0.;
@@ -380,8 +404,7 @@ __global__ void k_fill_projector(const double2 *F, Half h, VolGeom pg, int max_r
         const int kp = h.kp(k), ip = h.ip(i);
         const int r2 = kp * kp + ip * ip + j * j;
         if (r2 > max_r2) continue;
-        double2 v = F[n];
-        v = make_double2(v.x / nreal, v.y / nreal);
+        double2 v = make_double2((double)F[n].x / nreal, (double)F[n].y / nreal);
         if ((k ^ i ^ j) & 1) v = make_double2(-v.x, -v.y);
         v = make_double2(v.x * normfft, v.y * normfft);
         const int ires = d_round(sqrt((double)r2) / pad);
@@ -396,7 +419,8 @@ __global__ void k_fill_projector(const double2 *F, Half h, VolGeom pg, int max_r
 }
 
 // getFSC shell sums [3][X]: Re(conj z1 z2), |z1|^2, |z2|^2
-__global__ void k_fsc(const double2 *F1, const double2 *F2, Half h, double nreal, double *sums) {
+template <class R>
+__global__ void k_fsc(const typename Cx<R>::T *F1, const typename Cx<R>::T *F2, Half h, double nreal, double *sums) {
     extern __shared__ double sh[];
     for (int b = threadIdx.x; b < 3 * h.X; b += blockDim.x) sh[b] = 0.;
     __syncthreads();
@@ -407,8 +431,8 @@ __global__ void k_fsc(const double2 *F1, const double2 *F2, Half h, double nreal
         const int kp = h.kp(k), ip = h.ip(i);
         const int idx = d_round(sqrt((double)(kp * kp + ip * ip + j * j)));
         if (idx >= h.X) continue;
-        const double2 a = F1[n], b = F2[n];
-        const double2 z1 = make_double2(a.x / nreal, a.y / nreal), z2 = make_double2(b.x / nreal, b.y / nreal);
+        const double2 z1 = make_double2((double)F1[n].x / nreal, (double)F1[n].y / nreal);
+        const double2 z2 = make_double2((double)F2[n].x / nreal, (double)F2[n].y / nreal);
         atomicAdd(&sh[idx], z1.x * z2.x + z1.y * z2.y);
         const double a1 = sqrt(z1.x * z1.x + z1.y * z1.y), a2 = sqrt(z2.x * z2.x + z2.y * z2.y);
         atomicAdd(&sh[h.X + idx], a1 * a1);
@@ -493,12 +517,13 @@ struct ReconWork {
     Scratch c1, c2, fw, fn, vol, small, tab;
     std::map<long long, cufftHandle> plans;
     bool have_tab = false;
+    bool fp32 = false;  // transforms in FP32 instead of FP64
     ~ReconWork() {
         for (auto &kv : plans) cufftDestroy(kv.second);
     }
-    // double-precision plan of an N^dim transform (in place)
+    // plan of an in-place N^dim transform of the given type, cached
     int plan(int N, int dim, cufftType type, cufftHandle *out) {
-        const long long key = ((long long)N << 8) | (dim << 4) | (type == CUFFT_D2Z ? 1 : 2);
+        const long long key = ((long long)N << 16) | (dim << 12) | (int)type;
         auto it = plans.find(key);
         if (it != plans.end()) {
             *out = it->second;
@@ -512,6 +537,32 @@ struct ReconWork {
         return 0;
     }
 };
+
+namespace {
+// in-place inverse (half -> real, unscaled) and forward (real -> half) transforms
+template <class R>
+int exec_inv(ReconWork *w, int N, int dim, void *buf) {
+    const bool f = std::is_same<R, float>::value;
+    cufftHandle h;
+    const int st = w->plan(N, dim, f ? CUFFT_C2R : CUFFT_Z2D, &h);
+    if (st) return st;
+    if (f) RC_FFT(cufftExecC2R(h, static_cast<cufftComplex *>(buf), static_cast<cufftReal *>(buf)));
+    else RC_FFT(cufftExecZ2D(h, static_cast<cufftDoubleComplex *>(buf), static_cast<cufftDoubleReal *>(buf)));
+    return 0;
+}
+template <class R>
+int exec_fwd(ReconWork *w, int N, int dim, void *buf) {
+    const bool f = std::is_same<R, float>::value;
+    cufftHandle h;
+    const int st = w->plan(N, dim, f ? CUFFT_R2C : CUFFT_D2Z, &h);
+    if (st) return st;
+    if (f) RC_FFT(cufftExecR2C(h, static_cast<cufftReal *>(buf), static_cast<cufftComplex *>(buf)));
+    else RC_FFT(cufftExecD2Z(h, static_cast<cufftDoubleReal *>(buf), static_cast<cufftDoubleComplex *>(buf)));
+    return 0;
+}
+}  // namespace
+
+void recon_set_fp32(ReconWork *w, int fp32) { w->fp32 = fp32 != 0; }
 
 ReconWork *recon_work_create() { return new ReconWork(); }
 void recon_work_destroy(ReconWork *w) { delete w; }
@@ -585,13 +636,17 @@ int recon_update_ssnr(ReconWork *w, const double *weight, const VolGeom &g, int 
     return 0;
 }
 
-int recon_reconstruct(ReconWork *w, const double2 *data, const double *weight, const VolGeom &g, int ori,
-                      const ReconParams &p, const double *tau2_host, double *vol_host) {
+namespace {
+
+template <class R>
+int reconstruct_impl(ReconWork *w, const double2 *data, const double *weight, const VolGeom &g, int ori,
+                     const ReconParams &p, const double *tau2_host, double *vol_host) {
+    typedef typename Cx<R>::T C2;
     const int dim = g.dim, N = g.ydim, r_max = g.r_max;
     const double pad = g.pad;
     if (r_max < 1 || N % 2 == 0) return fail_recon(kErrInvalid, "reconstruct: bad backprojector geometry");
-    if (!p.skip_gridding && p.max_iter_preweight > 0 && p.normalise == 0.)
-        return fail_recon(kErrInvalid, "reconstruct: normalise must be non-zero");
+    const bool grid = !p.skip_gridding && p.max_iter_preweight > 0;
+    if (grid && p.normalise == 0.) return fail_recon(kErrInvalid, "reconstruct: normalise must be non-zero");
     const Half hin = make_half(N, dim);
     int No = d_round(pad * ori);
     No += No % 2;
@@ -609,21 +664,21 @@ int recon_reconstruct(ReconWork *w, const double2 *data, const double *weight, c
         RC_CUDA(cudaMemcpy(tau2_d, tau2_host, sizeof(double) * ns, cudaMemcpyHostToDevice));
     }
     const MapTerm m{tau2_d, ovc * p.tau2_fudge, pad, p.minres_map, p.do_map ? 1 : 0};
-    RC_CUDA(w->c1.reserve(sizeof(double2) * hout.size()));
-    double2 *Fo = w->c1.as<double2>();
-    if (p.skip_gridding || p.max_iter_preweight <= 0) {
+    RC_CUDA(w->c1.reserve(sizeof(C2) * hout.size()));
+    C2 *Fo = w->c1.as<C2>();
+    if (!grid) {
         const int rm2 = d_round(r_max * pad * r_max * pad);
         k_radavg<<<grid_for(hin.size()), kThreads, sizeof(double) * 2 * r_max>>>(weight, g, hin, max_r2, rm2, m,
                                                                                 r_max, sums);
         RC_CUDA(cudaGetLastError());
-        k_window<<<grid_for(hout.size()), kThreads, sizeof(double) * r_max>>>(
+        k_window<R><<<grid_for(hout.size()), kThreads, sizeof(double) * r_max>>>(
             data, weight, g, hin, hout, max_r2, m, 0, sums, r_max, nullptr, 1., Fo, err);
         RC_CUDA(cudaGetLastError());
     } else {
-        RC_CUDA(w->c2.reserve(sizeof(double2) * hin.size()));
+        RC_CUDA(w->c2.reserve(sizeof(C2) * hin.size()));
         RC_CUDA(w->fw.reserve(sizeof(double) * hin.size()));
         RC_CUDA(w->fn.reserve(sizeof(double) * hin.size()));
-        double2 *C = w->c2.as<double2>();
+        C2 *C = w->c2.as<C2>();
         double *fw = w->fw.as<double>(), *fn = w->fn.as<double>();
         if (!w->have_tab) {
             const std::vector<double> t = blob_table();
@@ -633,67 +688,66 @@ int recon_reconstruct(ReconWork *w, const double2 *data, const double *weight, c
         }
         double tab0 = 0.;
         RC_CUDA(cudaMemcpy(&tab0, w->tab.p, sizeof(double), cudaMemcpyDeviceToHost));
-        cufftHandle inv, fwd;
-        int st = w->plan(N, dim, CUFFT_Z2D, &inv);
-        if (st) return st;
-        st = w->plan(N, dim, CUFFT_D2Z, &fwd);
-        if (st) return st;
-        k_grid_init<<<grid_for(hin.size()), kThreads>>>(weight, g, hin, max_r2, m, p.normalise, fw, fn, C);
+        k_grid_init<R><<<grid_for(hin.size()), kThreads>>>(weight, g, hin, max_r2, m, p.normalise, fw, fn, C);
         RC_CUDA(cudaGetLastError());
         const double nreal = (double)hin.Z * hin.Y * hin.N;
         for (int it = 0; it < p.max_iter_preweight; ++it) {
-            RC_FFT(cufftExecZ2D(inv, reinterpret_cast<cufftDoubleComplex *>(C), reinterpret_cast<cufftDoubleReal *>(C)));
-            k_blob<<<grid_for((long long)hin.Z * hin.Y * hin.N), kThreads>>>(
-                reinterpret_cast<double *>(C), hin, w->tab.as<double>(), 0.5 / kBlobTab, 1. / tab0, 1. / nreal,
+            int st = exec_inv<R>(w, N, dim, C);
+            if (st) return st;
+            k_blob<R><<<grid_for((long long)hin.Z * hin.Y * hin.N), kThreads>>>(
+                reinterpret_cast<R *>(C), hin, w->tab.as<double>(), 0.5 / kBlobTab, 1. / tab0, 1. / nreal,
                 (double)ori * pad);
             RC_CUDA(cudaGetLastError());
-            RC_FFT(cufftExecD2Z(fwd, reinterpret_cast<cufftDoubleReal *>(C), reinterpret_cast<cufftDoubleComplex *>(C)));
-            k_grid_update<<<grid_for(hin.size()), kThreads>>>(C, fw, fn, hin, max_r2);
+            st = exec_fwd<R>(w, N, dim, C);
+            if (st) return st;
+            k_grid_update<R><<<grid_for(hin.size()), kThreads>>>(C, fw, fn, hin, max_r2);
             RC_CUDA(cudaGetLastError());
         }
-        k_window<<<grid_for(hout.size()), kThreads, 0>>>(data, weight, g, hin, hout, max_r2, m, 1, sums, r_max, fn,
-                                                          p.normalise, Fo, err);
+        k_window<R><<<grid_for(hout.size()), kThreads, 0>>>(data, weight, g, hin, hout, max_r2, m, 1, sums, r_max, fn,
+                                                             p.normalise, Fo, err);
         RC_CUDA(cudaGetLastError());
     }
-    cufftHandle last;
-    int st = w->plan(No, dim, CUFFT_Z2D, &last);
+    int st = exec_inv<R>(w, No, dim, Fo);
     if (st) return st;
-    RC_FFT(cufftExecZ2D(last, reinterpret_cast<cufftDoubleComplex *>(Fo), reinterpret_cast<cufftDoubleReal *>(Fo)));
     const long long nv = (long long)(dim == 3 ? ori : 1) * ori * ori;
     RC_CUDA(w->vol.reserve(sizeof(double) * nv));
     double *vol = w->vol.as<double>();
     const double normfft = dim == 3 ? pad * pad * pad * ori : pad * pad;
-    k_crop_bg<<<grid_for(nv), kThreads>>>(reinterpret_cast<const double *>(Fo), No, hout.rowp(), ori, dim, normfft,
-                                          vol, bg);
+    k_crop_bg<R><<<grid_for(nv), kThreads>>>(reinterpret_cast<const R *>(Fo), No, hout.rowp(), ori, dim, normfft, vol,
+                                             bg);
     RC_CUDA(cudaGetLastError());
     k_mask_gridcorr<<<grid_for(nv), kThreads>>>(vol, ori, dim, (double)ori * pad, bg);
     RC_CUDA(cudaGetLastError());
     int herr = 0;
     RC_CUDA(cudaMemcpy(&herr, err, sizeof(int), cudaMemcpyDeviceToHost));
     if (herr) return fail_recon(kErrNumerical, "reconstruct: zeros in counter or radavg_weight");
-    RC_CUDA(cudaMemcpy(vol_host, vol, sizeof(double) * nv, cudaMemcpyDeviceToHost));
+    if (vol_host) RC_CUDA(cudaMemcpy(vol_host, vol, sizeof(double) * nv, cudaMemcpyDeviceToHost));
     return 0;
 }
 
-int recon_projector_from_map(ReconWork *w, const double *vol_host, int ori, int dim, int pad, const VolGeom &pg,
-                             int do_gridding, int min_ires, float2 *proj, double *power_host) {
+template <class R>
+int projector_impl(ReconWork *w, const double *vol_host, int ori, int dim, int pad, const VolGeom &pg,
+                   int do_gridding, int min_ires, float2 *proj, double *power_host) {
+    typedef typename Cx<R>::T C2;
     int No = d_round((double)pad * ori);
     No += No % 2;
     const Half ho = make_half(No, dim);
     const long long nv = (long long)(dim == 3 ? ori : 1) * ori * ori;
     const int ns = ori / 2 + 1;
-    RC_CUDA(w->vol.reserve(sizeof(double) * nv));
-    RC_CUDA(cudaMemcpy(w->vol.p, vol_host, sizeof(double) * nv, cudaMemcpyHostToDevice));
-    RC_CUDA(w->c1.reserve(sizeof(double2) * ho.size()));
-    double2 *F = w->c1.as<double2>();
+    if (vol_host) {
+        RC_CUDA(w->vol.reserve(sizeof(double) * nv));
+        RC_CUDA(cudaMemcpy(w->vol.p, vol_host, sizeof(double) * nv, cudaMemcpyHostToDevice));
+    } else if (w->vol.bytes < sizeof(double) * nv) {
+        return fail_recon(kErrInvalid, "no device-resident map of this size");
+    }
+    RC_CUDA(w->c1.reserve(sizeof(C2) * ho.size()));
+    C2 *F = w->c1.as<C2>();
     const long long nreal_p = (long long)ho.Z * ho.Y * ho.rowp();
-    k_pad_map<<<grid_for(nreal_p), kThreads>>>(w->vol.as<double>(), ori, dim, No, ho.rowp(), (double)ori * pad,
-                                               do_gridding, reinterpret_cast<double *>(F));
+    k_pad_map<R><<<grid_for(nreal_p), kThreads>>>(w->vol.as<double>(), ori, dim, No, ho.rowp(), (double)ori * pad,
+                                                  do_gridding, reinterpret_cast<R *>(F));
     RC_CUDA(cudaGetLastError());
-    cufftHandle fwd;
-    int st = w->plan(No, dim, CUFFT_D2Z, &fwd);
+    int st = exec_fwd<R>(w, No, dim, F);
     if (st) return st;
-    RC_FFT(cufftExecD2Z(fwd, reinterpret_cast<cufftDoubleReal *>(F), reinterpret_cast<cufftDoubleComplex *>(F)));
     RC_CUDA(cudaMemset(proj, 0, sizeof(float2) * (size_t)pg.xdim * pg.ydim * pg.zdim));
     RC_CUDA(w->small.reserve(sizeof(double) * 2 * ns));
     double *sums = w->small.as<double>();
@@ -702,7 +756,7 @@ int recon_projector_from_map(ReconWork *w, const double *vol_host, int ori, int 
     const int mn = d_round(min_ires * (double)pad), min_r2 = min_ires > 0 ? mn * mn : -1;
     const double normfft = dim == 3 ? (double)pad * pad * pad * ori : (double)pad * pad;
     const double nreal = (double)ho.Z * ho.Y * ho.N;
-    k_fill_projector<<<grid_for(ho.size()), kThreads, sizeof(double) * 2 * ns>>>(
+    k_fill_projector<R><<<grid_for(ho.size()), kThreads, sizeof(double) * 2 * ns>>>(
         F, ho, pg, max_r2, min_r2, nreal, normfft, (double)pad, ns, proj, sums);
     RC_CUDA(cudaGetLastError());
     std::vector<double> h(2 * ns);
@@ -712,30 +766,53 @@ int recon_projector_from_map(ReconWork *w, const double *vol_host, int ori, int 
     return 0;
 }
 
-int recon_fsc(ReconWork *w, const double *m1, const double *m2, int ori, int dim, double *fsc_host) {
+template <class R>
+int fsc_impl(ReconWork *w, const double *m1, const double *m2, int ori, int dim, double *fsc_host) {
+    typedef typename Cx<R>::T C2;
     const Half h = make_half(ori, dim);
-    RC_CUDA(w->c1.reserve(sizeof(double2) * h.size()));
-    RC_CUDA(w->c2.reserve(sizeof(double2) * h.size()));
-    const size_t rows = (size_t)h.Z * h.Y;
-    RC_CUDA(cudaMemcpy2D(w->c1.p, sizeof(double) * h.rowp(), m1, sizeof(double) * ori, sizeof(double) * ori, rows,
-                         cudaMemcpyHostToDevice));
-    RC_CUDA(cudaMemcpy2D(w->c2.p, sizeof(double) * h.rowp(), m2, sizeof(double) * ori, sizeof(double) * ori, rows,
-                         cudaMemcpyHostToDevice));
-    cufftHandle fwd;
-    int st = w->plan(ori, dim, CUFFT_D2Z, &fwd);
-    if (st) return st;
-    RC_FFT(cufftExecD2Z(fwd, w->c1.as<cufftDoubleReal>(), w->c1.as<cufftDoubleComplex>()));
-    RC_FFT(cufftExecD2Z(fwd, w->c2.as<cufftDoubleReal>(), w->c2.as<cufftDoubleComplex>()));
+    RC_CUDA(w->c1.reserve(sizeof(C2) * h.size()));
+    RC_CUDA(w->c2.reserve(sizeof(C2) * h.size()));
+    const long long nv = (long long)h.Z * h.Y * ori;
+    // maps in FP64 -> real rows of the in-place transforms
+    RC_CUDA(w->vol.reserve(sizeof(double) * nv));
+    for (int which = 0; which < 2; ++which) {
+        RC_CUDA(cudaMemcpy(w->vol.p, which ? m2 : m1, sizeof(double) * nv, cudaMemcpyHostToDevice));
+        R *dst = which ? w->c2.as<R>() : w->c1.as<R>();
+        // padding to the map's own size: a plain copy into the padded rows
+        k_pad_map<R><<<grid_for((long long)h.Z * h.Y * h.rowp()), kThreads>>>(w->vol.as<double>(), ori, dim, ori,
+                                                                               h.rowp(), 1., 0, dst);
+        RC_CUDA(cudaGetLastError());
+        const int st = exec_fwd<R>(w, ori, dim, dst);
+        if (st) return st;
+    }
     RC_CUDA(w->small.reserve(sizeof(double) * 3 * h.X));
     double *sums = w->small.as<double>();
     RC_CUDA(cudaMemset(sums, 0, sizeof(double) * 3 * h.X));
-    k_fsc<<<grid_for(h.size()), kThreads, sizeof(double) * 3 * h.X>>>(
-        w->c1.as<double2>(), w->c2.as<double2>(), h, (double)h.Z * h.Y * h.N, sums);
+    k_fsc<R><<<grid_for(h.size()), kThreads, sizeof(double) * 3 * h.X>>>(w->c1.as<C2>(), w->c2.as<C2>(), h,
+                                                                          (double)h.Z * h.Y * h.N, sums);
     RC_CUDA(cudaGetLastError());
     std::vector<double> s(3 * h.X);
     RC_CUDA(cudaMemcpy(s.data(), sums, sizeof(double) * 3 * h.X, cudaMemcpyDeviceToHost));
     for (int i = 0; i < h.X; ++i) fsc_host[i] = s[i] / std::sqrt(s[h.X + i] * s[2 * h.X + i]);
     return 0;
+}
+
+}  // namespace
+
+int recon_reconstruct(ReconWork *w, const double2 *data, const double *weight, const VolGeom &g, int ori,
+                      const ReconParams &p, const double *tau2_host, double *vol_host) {
+    return w->fp32 ? reconstruct_impl<float>(w, data, weight, g, ori, p, tau2_host, vol_host)
+                   : reconstruct_impl<double>(w, data, weight, g, ori, p, tau2_host, vol_host);
+}
+
+int recon_projector_from_map(ReconWork *w, const double *vol_host, int ori, int dim, int pad, const VolGeom &pg,
+                             int do_gridding, int min_ires, float2 *proj, double *power_host) {
+    return w->fp32 ? projector_impl<float>(w, vol_host, ori, dim, pad, pg, do_gridding, min_ires, proj, power_host)
+                   : projector_impl<double>(w, vol_host, ori, dim, pad, pg, do_gridding, min_ires, proj, power_host);
+}
+
+int recon_fsc(ReconWork *w, const double *m1, const double *m2, int ori, int dim, double *fsc_host) {
+    return w->fp32 ? fsc_impl<float>(w, m1, m2, ori, dim, fsc_host) : fsc_impl<double>(w, m1, m2, ori, dim, fsc_host);
 }
 
 }  // namespace gbr

@@ -113,28 +113,36 @@ class MlDeviceBundle:
                                        int(is_whole_instead_of_half)))
         return dict(tau2=t, sigma2=out[0], data_vs_prior=out[1], fourier_coverage=out[2])
 
+    def set_recon_precision(self, fp32):
+        """Reconstruction-side transforms in FP32 (True) or FP64 (False, default)."""
+        check(self.lib.gbr_recon_set_precision(self.h, 1 if fp32 else 0))
+
     # BackProjector::reconstruct
     def reconstruct(self, iclass, max_iter_preweight=10, do_map=False, tau2=None, tau2_fudge=1.0, normalise=1.0,
-                    minres_map=5, skip_gridding=True):
-        """Real-space map [ori]^ref_dim (mymodel.Iref[iclass])."""
+                    minres_map=5, skip_gridding=True, to_host=True):
+        """Real-space map [ori]^ref_dim (mymodel.Iref[iclass]); with
+        to_host=False the map stays on the device only (returns None)."""
         p = _lib.ReconParams(max_iter_preweight=int(max_iter_preweight), do_map=int(do_map),
                              skip_gridding=int(skip_gridding), minres_map=int(minres_map),
                              tau2_fudge=float(tau2_fudge), normalise=float(normalise))
-        vol = np.zeros((self.ori_size,) * self.ref_dim)
+        vol = np.zeros((self.ori_size,) * self.ref_dim) if to_host else None
         t = None if tau2 is None else np.ascontiguousarray(tau2, dtype=np.float64)
         check(self.lib.gbr_reconstruct(self.h, int(iclass), C.byref(p), None if t is None else t.ctypes.data,
-                                       vol.ctypes.data))
+                                       None if vol is None else vol.ctypes.data))
         return vol
 
     # Projector::computeFourierTransformMap (MlModel::setFourierTransformMaps)
     def set_fourier_transform_map(self, iclass, vol, current_size, do_gridding=True, min_ires=-1):
-        """Fill class iclass's projector from a real-space map; returns its power spectrum."""
-        v = np.ascontiguousarray(vol, dtype=np.float64)
-        if v.shape != (self.ori_size,) * self.ref_dim:
-            raise ValueError("map must be %s" % ((self.ori_size,) * self.ref_dim,))
+        """Fill class iclass's projector from a real-space map (None: the map
+        the last reconstruct left on the device); returns its power spectrum."""
+        v = None
+        if vol is not None:
+            v = np.ascontiguousarray(vol, dtype=np.float64)
+            if v.shape != (self.ori_size,) * self.ref_dim:
+                raise ValueError("map must be %s" % ((self.ori_size,) * self.ref_dim,))
         ps = np.zeros(self.ori_size // 2 + 1)
-        check(self.lib.gbr_projector_from_map(self.h, int(iclass), v.ctypes.data, int(current_size),
-                                              int(do_gridding), int(min_ires), ps.ctypes.data))
+        check(self.lib.gbr_projector_from_map(self.h, int(iclass), None if v is None else v.ctypes.data,
+                                              int(current_size), int(do_gridding), int(min_ires), ps.ctypes.data))
         return ps
 
     def get_projector(self, iclass):

@@ -169,3 +169,56 @@ def test_estep_then_reconstruct_then_project(po):
     assert _rel(vol, ovol) <= 1e-5, _rel(vol, ovol)
     assert _rel(P.astype(np.complex128), oP) <= 1e-5
     np.testing.assert_allclose(ps, ops, rtol=1e-4)
+
+
+@pytest.mark.parametrize("cur,do_map,skip,name", [
+    (None, True, True, "cfg0_box64"),
+    (64, True, True, "cfg0_box64"),
+    (None, True, False, "cfg0_box64"),
+    (None, True, True, "2d"),
+])
+def test_reconstruct_fp32_transforms(po, cur, do_map, skip, name):
+    # FP32 cuFFT transforms (weights, sums and maps FP64): within the
+    # volume tolerance of the path, 1e-5 relative L2
+    kw = {} if cur is None else dict(current_size=cur, coarse_size=min(cur, 28))
+    ds, m = _model(name, **kw)
+    b = _bundle(m)
+    b.set_recon_precision(True)
+    ori, dim = m["ori_size"], 2 if name == "2d" else 3
+    data, weight = _random_volumes(b, 17)
+    b.set_mdl_data(0, data, weight)
+    b.symmetrise(0)
+    data, weight = b.get_mdl_data(0)
+    tau2 = np.random.default_rng(18).uniform(0.05, 2.0, ori // 2 + 1)
+    kw = dict(do_map=do_map, tau2=tau2, tau2_fudge=1.3, normalise=2.5, minres_map=3, skip_gridding=skip,
+              max_iter_preweight=3)
+    g = b.reconstruct(0, **kw)
+    o = po.reconstruct(data if dim == 3 else data[0], weight if dim == 3 else weight[0], ori, m["current_size"],
+                       ref_dim=dim, **kw)
+    # the map kept on the device feeds the projector exactly like the host copy
+    b.reconstruct(0, to_host=False, **kw)
+    ps_dev = b.set_fourier_transform_map(0, None, m["current_size"])
+    P_dev, _ = b.get_projector(0)
+    ps_host = b.set_fourier_transform_map(0, g, m["current_size"])
+    P_host, _ = b.get_projector(0)
+    fg = b.fsc(g, o)
+    b.close()
+    assert _rel(g, o) <= 1e-5, _rel(g, o)
+    # (the two reconstructions differ only in the order of FP64 atomic sums)
+    assert _rel(P_dev.astype(np.complex128), P_host.astype(np.complex128)) <= 1e-7
+    np.testing.assert_allclose(ps_dev, ps_host, rtol=1e-12)
+    assert np.max(np.abs(fg[1:] - 1.)) <= 1e-6
+
+
+def test_projector_from_map_fp32_transforms(po):
+    ds, m = _model()
+    b = _bundle(m)
+    b.set_recon_precision(True)
+    ori = m["ori_size"]
+    vol = np.random.default_rng(5).normal(size=(ori,) * 3)
+    ps = b.set_fourier_transform_map(0, vol, 28)
+    P, _ = b.get_projector(0)
+    b.close()
+    oP, ops = po.projector_from_map(vol, 28)
+    assert _rel(P.astype(np.complex128), oP) <= 1e-5
+    np.testing.assert_allclose(ps, ops, rtol=1e-5)
