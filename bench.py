@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-mstep", action="store_true", help="skip the reconstruction-side section (profiling runs)")
     ap.add_argument("--precision", default="bf16", choices=["fp32", "bf16"],
                     help="coarse cross term: plain FP32 SIMT or tcgen05 BF16 (precision form)")
     return ap.parse_args()
@@ -226,7 +227,8 @@ def run_ours(args, world, rank, local):
         from relion_gb300.replicas import max_over_ranks
         total_ms, e2e_total, img_total = max_over_ranks([total_ms, e2e_total, img_total], device=dev)
 
-    mstep = mstep_section(args, ds, model, bundle, worker, dev_batch, local) if rank == 0 else None
+    mstep = mstep_section(args, ds, model, bundle, worker, dev_batch, local) if rank == 0 and not args.no_mstep \
+        else None
 
     # ---- roofline of the dominant kernel: the coarse cross-term GEMM ----
     R = bundle.nr_classes * bundle.ndir * bundle.npsi

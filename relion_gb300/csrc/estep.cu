@@ -824,7 +824,6 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
         }
     }
     // ---- per-particle finalisation (storeWeightedSums :8990-9150) ----
-    std::vector<double> fr(nOR), ft(nOR), fp(nOR);
     for (int p = 0; p < n; ++p) {
         const ParticleState &ps = psh[p];
         gbr_particle_result &o = res[p];
@@ -849,26 +848,27 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
         const long ior = (long)((idx / ((unsigned long long)nOT * T)) % nOR);
         const long r = (long)(idx / ((unsigned long long)nOT * T * nOR));
         const long ic = r / (b->ND * b->NP), id = (r / b->NP) % b->ND, is = r % b->NP;
-        b->grid.fine_orientations(id, is, fr.data(), ft.data(), fp.data());
-        o.rot = fr[ior];
-        o.tilt = ft[ior];
-        o.psi = fp[ior];
+        b->grid.fine_orientation(id, is, ior, o.rot, o.tilt, o.psi);
         o.xoff = pd[0] + b->otx_h[t * nOT + iot];
         o.yoff = pd[1] + b->oty_h[t * nOT + iot];
         o.cls = (double)ic + 1;
         o.pmax = (double)wmax / ps.sum_fine;
         o.best_ihidden_over = ((r * T + t) * nOR + ior) * nOT + iot;
         o.dLL = std::log(ps.sum_fine) - o.fine_min_diff2 - b->logsigma2;
-        double wnorm = 0.;
-        const double *sp = &shell[(size_t)p * b->nshell];
+        // four partial sums: no serial dependency chain through wnorm
+        double wn[4] = {0., 0., 0., 0.};
+        const double *__restrict__ sp = &shell[(size_t)p * b->nshell];
+        const double *__restrict__ pw = &power_h[(size_t)p * b->nshell];
+        double *__restrict__ wsig = b->w_sigma2.data();
         for (int i = 0; i < b->nshell; ++i) {
-            b->w_sigma2[i] += sp[i];
-            wnorm += sp[i];
+            wsig[i] += sp[i];
+            wn[i & 3] += sp[i];
         }
         for (int i = b->cur / 2 + 1; i < b->nshell; ++i) {
-            b->w_sigma2[i] += power_h[(size_t)p * b->nshell + i];
-            wnorm += power_h[(size_t)p * b->nshell + i];
+            wsig[i] += pw[i];
+            wn[i & 3] += pw[i];
         }
+        const double wnorm = (wn[0] + wn[1]) + (wn[2] + wn[3]);
         o.norm = pd[5];
         if (d.do_norm_correction) {
             o.norm = pd[5] / d.avg_norm_correction * std::sqrt(wnorm * 2.);

@@ -209,6 +209,24 @@ struct PoseGrid {
                 }
             }
     }
+    // One oversampled orientation (index ior of fine_orientations) of (idir, ipsi).
+    void fine_orientation(long idir, long ipsi, long ior, double &rot, double &tilt, double &ps) const {
+        const int npsi_over = iround(std::pow(2., oversampling));
+        const int k = (int)(ior % npsi_over);
+        ps = psi[ipsi] - 0.5 * psi_step + (0.5 + k) * psi_step / npsi_over;
+        if (!is3d) {
+            if (ps > 180.) ps -= 360.;
+            rot = 0.;
+            tilt = 0.;
+            return;
+        }
+        const HealpixNest base(order), fine(order + oversampling);
+        const int fact = fine.nside() / base.nside();
+        int x, y, face;
+        base.pix_to_xyf(dir_pix[idir], x, y, face);
+        const int c = (int)(ior / npsi_over);
+        healpix_angles(fine, fine.xyf_to_pix(fact * x + c % fact, fact * y + c / fact, face), rot, tilt);
+    }
     // Oversampled translations of itrans in pixels (ox-major, oy-minor).
     void fine_translations(long itrans, double pixel, double *tx, double *ty) const {
         const int n = iround(std::pow(2., oversampling));
