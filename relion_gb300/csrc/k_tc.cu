@@ -276,9 +276,14 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_diff2(const TcArgs a) {
         for (int tidx = blockIdx.x; tidx < ntotal && !*vfail; tidx += gridDim.x) {
             int mt, nt;
             tile_mn(tidx, a.mtiles, a.ntiles, mt, nt);
-            const uint8_t *ab = a.Ablk + (size_t)mt * nk * A_BYTES;
+            // norms: A holds [hi | lo] (2 nk/3 tiles per row tile), read in the
+            // order hi(0) hi(0) hi(1) hi(1) ... lo(0) lo(1) ... so that the
+            // second read of each hi tile follows the first (an L2 hit)
+            const int nkb = nk / 3;
+            const uint8_t *ab = a.Ablk + (size_t)mt * (kNorm ? 2 * nkb : nk) * A_BYTES;
             const uint8_t *yb = a.Yblk + (size_t)nt * nk * B_BYTES;
             for (int kt = 0; kt < nk; ++kt, ++g) {
+                const int ka = kNorm ? (kt < 2 * nkb ? kt >> 1 : kt - nkb) : kt;
                 const uint32_t s = g % STAGES;
                 if (g >= STAGES && !mbar_wait(smem_u32(&empty[s]), ((g / STAGES) - 1) & 1u)) {
                     *vfail = 1;
@@ -286,7 +291,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_diff2(const TcArgs a) {
                 }
                 const uint32_t st = sbase + s * STAGE_BYTES;
                 arrive_expect_tx(smem_u32(&full[s]), (uint32_t)STAGE_BYTES);
-                bulk_g2s(st, ab + (size_t)kt * A_BYTES, A_BYTES, smem_u32(&full[s]));
+                bulk_g2s(st, ab + (size_t)ka * A_BYTES, A_BYTES, smem_u32(&full[s]));
                 bulk_g2s(st + A_BYTES, yb + (size_t)kt * B_BYTES, B_BYTES, smem_u32(&full[s]));
             }
         }
@@ -559,11 +564,13 @@ __device__ __forceinline__ uint32_t to_tf32(float x) {
     return u;
 }
 
-// TF32 operand tiles of the norm term, three-term split along K:
-// A = [hi | hi | lo], B = [hi | lo | hi] (x = hi + lo, both rounded to TF32),
-// so that one K loop accumulates hi*hi + hi*lo + lo*hi.  Tiles of `rows_t`
-// rows (128 for A, 256 for B) by 32 values, same shared-memory image as the
-// BF16 tiles (16-byte chunks of 4 values).
+// TF32 operand tiles of the norm term, three-term split (x = hi + lo, both
+// rounded to TF32): one K loop of 3 nk tiles accumulates hi*hi and hi*lo
+// for every K tile kt (steps 2 kt and 2 kt + 1), then lo*hi (steps 2 nk + kt).
+// A (rows_t = 128) is stored [hi(0..nk-1) | lo(0..nk-1)]; B (rows_t = 256) in
+// step order [hi(0) lo(0) hi(1) lo(1) ... | hi(0) hi(1) ...].  Tiles of
+// rows_t rows by 32 values, same shared-memory image as the BF16 tiles
+// (16-byte chunks of 4 values).
 __global__ void k_pack_tf32(const float *__restrict__ src, int lds, int rows, int K, int nk, int rows_t, int is_b,
                             uint8_t *__restrict__ dst, long long nchunks) {
     const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -571,10 +578,17 @@ __global__ void k_pack_tf32(const float *__restrict__ src, int lds, int rows, in
     const int per = rows_t * 8;  // chunks per tile
     const long long blk = c / per;
     const int within = (int)(c - blk * per), row = within >> 3, kg = within & 7;
-    const int ktot = 3 * nk;
+    const int ktot = (is_b ? 3 : 2) * nk;
     const int rt = (int)(blk / ktot), kk = (int)(blk - (long long)rt * ktot);
-    const int part = kk / nk, kt = kk - part * nk;
-    const bool lo = is_b ? (part == 1) : (part == 2);
+    int kt;
+    bool lo;
+    if (is_b) {
+        lo = kk < 2 * nk && (kk & 1);
+        kt = kk < 2 * nk ? kk >> 1 : kk - 2 * nk;
+    } else {
+        lo = kk >= nk;
+        kt = lo ? kk - nk : kk;
+    }
     const int r = rt * rows_t + row, k0 = kt * 32 + kg * 4;
     uint32_t u[4];
 #pragma unroll
@@ -589,12 +603,12 @@ __global__ void k_pack_tf32(const float *__restrict__ src, int lds, int rows, in
 
 }  // namespace
 
-size_t tc_norm_a_bytes(int M, int K) { return (size_t)((M + TM - 1) / TM) * 3 * ((K + 31) / 32) * A_BYTES; }
+size_t tc_norm_a_bytes(int M, int K) { return (size_t)((M + TM - 1) / TM) * 2 * ((K + 31) / 32) * A_BYTES; }
 size_t tc_norm_b_bytes(int N, int K) { return (size_t)((N + TN - 1) / TN) * 3 * ((K + 31) / 32) * B_BYTES; }
 
 cudaError_t launch_tc_norm_pack_a(const float *src, int lds, int M, int K, void *dst, cudaStream_t st) {
     const int nk = (K + 31) / 32, mtiles = (M + TM - 1) / TM;
-    const long long nchunks = (long long)mtiles * 3 * nk * (TM * 8);
+    const long long nchunks = (long long)mtiles * 2 * nk * (TM * 8);
     if (nchunks <= 0) return cudaSuccess;
     k_pack_tf32<<<(unsigned)((nchunks + 255) / 256), 256, 0, st>>>(src, lds, M, K, nk, TM, 0,
                                                                    static_cast<uint8_t *>(dst), nchunks);
