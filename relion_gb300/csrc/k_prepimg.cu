@@ -8,6 +8,8 @@
 //   window to the current size with CenterFFTbySign,
 //   power spectrum and high-resolution power of the masked image,
 //   CTF image on the full-box frequencies (CTF::getFftwImage).
+#include <algorithm>
+
 #include "gbr_internal.h"
 
 #include <cufft.h>
@@ -39,6 +41,10 @@ __global__ void k_mask_weights(int N, double radius, double width, float *__rest
 // (translate with DONT_WRAP, src/transformations.h; V2(r) = V1(r - v)),
 // together with the weighted background sums of the soft mask (sum w A,
 // sum w): a few pixels per thread in FP32, FP64 across threads and blocks.
+// Each thread takes kImgPer pixels one block-width apart, loads all of them
+// before using any (memory-level parallelism), grid (N^2 / (256 kImgPer), n).
+constexpr int kImgPer = 8;
+
 __global__ void k_img_shift_bg(const float *__restrict__ in, int N, const int *__restrict__ shift,
                                const float *__restrict__ factor, const float *__restrict__ W,
                                float *__restrict__ A, double *__restrict__ sums) {
@@ -48,15 +54,30 @@ __global__ void k_img_shift_bg(const float *__restrict__ in, int N, const int *_
     const float f = factor[p];
     const float *src = in + (size_t)p * N * N;
     float *dst = A + (size_t)p * N * N;
+    const int NN = N * N, base = blockIdx.x * (blockDim.x * kImgPer) + threadIdx.x;
+    float v[kImgPer], wv[kImgPer];
+#pragma unroll
+    for (int k = 0; k < kImgPer; ++k) {
+        const int i = base + k * blockDim.x;
+        v[k] = 0.f;
+        wv[k] = 0.f;
+        if (i < NN) {
+            const int y = i / N, x = i - y * N;
+            const int sy = y - dy, sx = x - dx;
+            if (sy >= 0 && sy < N && sx >= 0 && sx < N) v[k] = src[(size_t)sy * N + sx];
+            wv[k] = W[i];
+        }
+    }
     float fw = 0.f, fv = 0.f;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N * N; i += gridDim.x * blockDim.x) {
-        const int y = i / N, x = i - y * N;
-        const int sy = y - dy, sx = x - dx;
-        const float v = (sy >= 0 && sy < N && sx >= 0 && sx < N) ? f * src[(size_t)sy * N + sx] : 0.f;
-        dst[i] = v;
-        const float w = W[i];
-        fw += w;
-        fv = fmaf(w, v, fv);
+#pragma unroll
+    for (int k = 0; k < kImgPer; ++k) {
+        const int i = base + k * blockDim.x;
+        if (i < NN) {
+            const float val = f * v[k];
+            dst[i] = val;
+            fw += wv[k];
+            fv = fmaf(wv[k], val, fv);
+        }
     }
     double sw = fw, sv = fv;
     for (int o = 16; o > 0; o >>= 1) {
@@ -86,9 +107,18 @@ __global__ void k_mask_apply(const float *__restrict__ A, int N, const float *__
     float *dst = B + (size_t)p * N * N;
     const double sw = sums[2 * p + 1];
     const float b = (float)(sw > 0. ? sums[2 * p] / sw : 0.);
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N * N; i += gridDim.x * blockDim.x) {
-        const float w = W[i];
-        dst[i] = (1.f - w) * src[i] + w * b;
+    const int NN = N * N, base = blockIdx.x * (blockDim.x * kImgPer) + threadIdx.x;
+    float a[kImgPer], w[kImgPer];
+#pragma unroll
+    for (int k = 0; k < kImgPer; ++k) {
+        const int i = base + k * blockDim.x;
+        a[k] = i < NN ? src[i] : 0.f;
+        w[k] = i < NN ? W[i] : 0.f;
+    }
+#pragma unroll
+    for (int k = 0; k < kImgPer; ++k) {
+        const int i = base + k * blockDim.x;
+        if (i < NN) dst[i] = (1.f - w[k]) * a[k] + w[k] * b;
     }
 }
 
@@ -189,11 +219,11 @@ __global__ void k_ctf_image(const double *__restrict__ ctf, int N, int cur, doub
     if (threadIdx.x == 0) sk = ctf_const(ctf + (size_t)p * 6, kV, Cs, Q0);
     __syncthreads();
     const CtfConst k = sk;
-    const double xs = (double)N * pixel;
+    const double inv_xs = 1. / ((double)N * pixel);
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < cur * X; e += gridDim.x * blockDim.x) {
         const int i = e / X, j = e - i * X;
         const int ip = i < X ? i : i - cur;
-        const double x = (double)j / xs, y = (double)ip / xs;
+        const double x = (double)j * inv_xs, y = (double)ip * inv_xs;
         const double u2 = x * x + y * y;
         double g = k.K1 * (k.Axx * x * x + 2.0 * k.Axy * x * y + k.Ayy * y * y) + k.K2 * u2 * u2 - k.K5 - k.K3;
         g -= 2. * kPiD * rint(g * (0.5 / kPiD));
@@ -210,8 +240,7 @@ cudaError_t launch_prepare_images(const PrepImagesArgs &a, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
     if (N <= 0 || (N & 1) || cur <= 0 || (cur & 1) || cur > N) return cudaErrorInvalidValue;
     const int X = cur / 2 + 1, half = N / 2 + 1;
-    const unsigned bx = (unsigned)((N * N + 255) / 256 < 64 ? (N * N + 255) / 256 : 64);
-    const dim3 gimg(bx, (unsigned)n);
+    const dim3 gimg((unsigned)((N * N + 256 * kImgPer - 1) / (256 * kImgPer)), (unsigned)n);
     if (a.mask_fresh) k_mask_weights<<<(N * N + 255) / 256, 256, 0, st>>>(N, a.mask_radius, a.mask_width, a.W);
     cudaError_t e = cudaMemsetAsync(a.bg, 0, sizeof(double) * 2 * n, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(a.power, 0, sizeof(double) * (size_t)n * half, st);
@@ -228,9 +257,11 @@ cudaError_t launch_prepare_images(const PrepImagesArgs &a, cudaStream_t st) {
     const dim3 gw((unsigned)((cur * X + 255) / 256), (unsigned)n);
     k_window_center<<<gw, 256, 0, st>>>(a.FA, N, cur, a.fimg_nomask);
     k_window_center<<<gw, 256, 0, st>>>(a.FB, N, cur, a.fimg);
-    const dim3 gs((unsigned)((N * half + 2047) / 2048 < 64 ? (N * half + 2047) / 2048 : 64), (unsigned)n);
+    // spectrum: 8 row chunks per particle (few FP64 atomics per shell)
+    const dim3 gs((unsigned)std::min(8, std::max(1, N / 32)), (unsigned)n);
     if (cur < N) k_img_spectrum<<<gs, 256, sizeof(float) * half, st>>>(a.FB, N, cur, a.power, a.xi2);
-    k_ctf_image<<<gw, 256, 0, st>>>(a.ctf, N, cur, a.pixel, a.kV, a.Cs, a.Q0, a.fctf);
+    // CTF: one block per particle, its constants formed once
+    k_ctf_image<<<dim3(1, (unsigned)n), 256, 0, st>>>(a.ctf, N, cur, a.pixel, a.kV, a.Cs, a.Q0, a.fctf);
     return cudaGetLastError();
 }
 
