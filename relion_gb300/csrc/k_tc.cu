@@ -546,13 +546,28 @@ __global__ void k_pack_y(const float2 *__restrict__ b, int ldb, const float2 *__
     if (n < N) {
         const int p = n / T, t = n - p * T;
         const int j = kt * (TK / 2) + kg * 4;
+        if (j + 4 <= ldb && j + 4 <= lde) {
+            // rows padded to 16 pixels: two 16-byte loads each (zeros beyond npix)
+            const float4 *bp = reinterpret_cast<const float4 *>(b + (size_t)p * ldb + j);
+            const float4 *ep = reinterpret_cast<const float4 *>(E + (size_t)t * lde + j);
+            const float4 x0 = __ldg(bp), x1 = __ldg(bp + 1), e0 = __ldg(ep), e1 = __ldg(ep + 1);
+            const float xr[4] = {x0.x, x0.z, x1.x, x1.z}, xi[4] = {x0.y, x0.w, x1.y, x1.w};
+            const float er[4] = {e0.x, e0.z, e1.x, e1.z}, ei[4] = {e0.y, e0.w, e1.y, e1.w};
 #pragma unroll
-        for (int q = 0; q < 4; ++q)
-            if (j + q < npix) {
-                const float2 x = __ldg(b + (size_t)p * ldb + j + q), e = __ldg(E + (size_t)t * lde + j + q);
-                y[2 * q] = x.x * e.x - x.y * e.y;
-                y[2 * q + 1] = x.x * e.y + x.y * e.x;
-            }
+            for (int q = 0; q < 4; ++q)
+                if (j + q < npix) {
+                    y[2 * q] = xr[q] * er[q] - xi[q] * ei[q];
+                    y[2 * q + 1] = xr[q] * ei[q] + xi[q] * er[q];
+                }
+        } else {
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                if (j + q < npix) {
+                    const float2 x = __ldg(b + (size_t)p * ldb + j + q), e = __ldg(E + (size_t)t * lde + j + q);
+                    y[2 * q] = x.x * e.x - x.y * e.y;
+                    y[2 * q + 1] = x.x * e.y + x.y * e.x;
+                }
+        }
     }
     *reinterpret_cast<uint4 *>(dst + blk * B_BYTES + chunk_off(row, kg)) =
         make_uint4(pack_bf16(y[0], y[1]), pack_bf16(y[2], y[3]), pack_bf16(y[4], y[5]), pack_bf16(y[6], y[7]));
