@@ -326,11 +326,22 @@ k_weights_cand(const float *__restrict__ vals, int R, int T, const float *__rest
     // for each pose: d >= rowmin gives d - mn >= rowmin - mn), and the warp
     // then walks the remaining rows in order, one warp per row so that
     // pdf_orient[r] is warp-uniform and the translation index is the lane.
-    for (int rb = r0 + 32 * warp; rb < r1; rb += 32 * nwarps) {
+    // each warp takes 4 x 32 rows per step: the four row-minimum loads of a
+    // lane are issued together
+    for (int rq = r0 + 128 * warp; rq < r1; rq += 128 * nwarps) {
+    unsigned int ru4[4];
+#pragma unroll
+    for (int kq = 0; kq < 4; ++kq) {
+        const int rr = rq + 32 * kq + lane;
+        ru4[kq] = (rowmin && rr < r1) ? rowmin[(size_t)p * R + rr] : 0u;
+    }
+#pragma unroll
+    for (int kq = 0; kq < 4; ++kq) {
+        const int rb = rq + 32 * kq;
         const int rr = rb + lane;
         bool keep = rr < r1;
         if (keep && rowmin) {
-            const unsigned int ru = rowmin[(size_t)p * R + rr];
+            const unsigned int ru = ru4[kq];
             keep = !(ru == 0xFFFFFFFFu || ord2f(ru) - mn > xs);
             if (!keep && dense_out)
                 for (int t = 0; t < T; ++t) dense_out[(size_t)p * RT + (size_t)rr * T + t] = 0.f;
@@ -401,6 +412,8 @@ k_weights_cand(const float *__restrict__ vals, int R, int T, const float *__rest
             }
         }
     }
+    }
+
     const double tot = block_sum(acc_c + (double)acc_f, sh);
     if (threadIdx.x == 0) atomicAdd(&ps[p].sum_coarse, tot);
 }

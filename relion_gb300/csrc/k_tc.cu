@@ -19,7 +19,7 @@
 // into one of two TMEM accumulators (2 x 256 columns) while eight warps drain
 // the other, so the epilogue of tile i overlaps the MMAs of tile i+1.  Every
 // mbarrier wait is bounded: on timeout the CTA records an error, waits
-// (bounded) for its own MMAs, frees its tensor memory and returns.
+// (bounded) for its own copies and MMAs, frees its tensor memory and returns.
 #include "gbr_internal.h"
 
 #include <cuda_bf16.h>
@@ -295,6 +295,11 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_diff2(const TcArgs a) {
                 bulk_g2s(st + A_BYTES, yb + (size_t)kt * B_BYTES, B_BYTES, smem_u32(&full[s]));
             }
         }
+        // copies still in flight (after a failure the MMA issuer stops
+        // consuming) land before the CTA may leave: wait (bounded) for the
+        // last filled phase of each stage; immediate when all were consumed
+        for (uint32_t q = g > (uint32_t)STAGES ? g - STAGES : 0u; q < g; ++q)
+            if (!mbar_wait(smem_u32(&full[q % STAGES]), (q / STAGES) & 1u)) *vfail = 1;
     } else if (warp == 1 && lane == 0) {
         // MMA issuer
         const uint32_t idesc = kNorm ? make_idesc_tf32() : make_idesc();
