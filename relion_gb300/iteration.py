@@ -70,6 +70,38 @@ def maximization_other_parameters(model, wsum, npix, do_norm_correction, min_sig
     model["ave_Pmax"] = wsum["ave_Pmax"] / sum_weight
 
 
+def update_image_sizes(model, data_vs_prior, angular_sampling_deg, particle_diameter, minres_map=5, incr_size=10,
+                       split_halves=True):
+    """MlOptimiser::updateCurrentResolution (src/ml_optimiser.cpp:5579-5682,
+    do_map, one body, after the first iteration) and the sizes of
+    updateImageSizeAndResolutionPointers (:5684-5777, incr_size, one optics
+    group of the model's size): the last shell with data_vs_prior >= 1 (with
+    the split-halves rule for a later rise above 1), the current size
+    2 (maxres + incr_size) and the coarse size from the angular sampling.
+    Updates model["current_size"], ["coarse_size"], ["current_resolution"]."""
+    ori, pix = int(model["ori_size"]), float(model["pixel_size"])
+    maxres = 0
+    for dvp in data_vs_prior:
+        ires = 1
+        while ires < ori // 2 and dvp[ires] >= 1.:
+            ires += 1
+        ires -= 1
+        if split_halves:
+            ires2 = ori // 2 - 1
+            while ires2 >= ires and not dvp[ires2] > 1.:
+                ires2 -= 1
+            if ires2 > ires + 3:
+                ires = ires2
+        maxres = max(maxres, ires)
+    maxres = max(maxres, minres_map)
+    model["current_resolution"] = maxres / (ori * pix)          # getResolution (1/Angstrom)
+    cur = min(2 * (maxres + incr_size), ori)
+    keepsafe = 1.2 if int(model.get("ref_dim", 3) or 3) == 3 else 1.5
+    coarse_res = (angular_sampling_deg / 360.) * math.pi * particle_diameter / keepsafe
+    coarse = min(2 * int(math.ceil(pix * ori / coarse_res)), cur)
+    model["current_size"], model["coarse_size"] = cur, coarse
+
+
 def resolution_at(fsc, ori_size, pixel_size, threshold=0.143):
     """Resolution (Angstrom) of the last shell before the FSC first drops
     below the threshold (shell 0 excluded)."""
@@ -83,11 +115,17 @@ def resolution_at(fsc, ori_size, pixel_size, threshold=0.143):
 class HalfSet:
     """One half of the particle set with its own model and maps."""
 
-    def __init__(self, model, maps, batches, device=0):
+    def __init__(self, model, maps, batches, device=0, optics=None):
+        """batches: prepared particle batches (gbr_particle_batch fields), or,
+        with `optics` (kV, Cs, Q0, particle_diameter, width_mask_edge),
+        raw real-space image batches prepared on the device at each
+        iteration's current size."""
         self.model = dict(model)
         self.maps = [np.array(m, np.float64) for m in maps]
         self.batches = batches
         self.device = device
+        self.optics = optics
+        self.dvp = None
         K = int(model["nr_classes"])
         self.tau2 = [None] * K
         self.wsum = None
@@ -105,7 +143,11 @@ class HalfSet:
             if self.tau2[k] is None:
                 self.tau2[k] = ps
         w = MlOptimiserCuda(b)
-        self.last_results = [w.do_expectation_some_particles(bt) for bt in self.batches]
+        if self.optics is not None:
+            b.set_optics(**self.optics)
+            self.last_results = [w.do_expectation_images(bt) for bt in self.batches]
+        else:
+            self.last_results = [w.do_expectation_some_particles(bt) for bt in self.batches]
         w.close()
         self.wsum = b.get_wsum()
         return b
@@ -114,10 +156,12 @@ class HalfSet:
         """Per class: symmetrise, updateSSNRarrays (with the FSC when given),
         reconstruct with the MAP term; then the scalar model update."""
         m = self.model
+        self.dvp = []
         for k in range(len(self.maps)):
             b.symmetrise(k)
             s = b.update_ssnr_arrays(k, tau2_fudge, self.tau2[k], fsc, fsc is not None)
             self.tau2[k] = s["tau2"]
+            self.dvp.append(s["data_vs_prior"])
             self.maps[k] = b.reconstruct(k, max_iter_preweight=gridding_iter, do_map=True, tau2=s["tau2"],
                                          tau2_fudge=tau2_fudge, normalise=self.wsum["pdf_class"][k],
                                          minres_map=minres_map)
@@ -126,20 +170,28 @@ class HalfSet:
         b.close()
 
 
-def refine(halves, iterations, pixel_size):
+def refine(halves, iterations, pixel_size, adapt_sizes=None):
     """Gold-standard iterations over two HalfSet objects; returns the FSC
-    curve and the FSC-0.143 resolution after each iteration."""
+    curve and the FSC-0.143 resolution after each iteration.  With
+    adapt_sizes = dict(angular_sampling_deg=..., particle_diameter=...) the
+    current and coarse sizes follow the resolution between iterations (the
+    half-sets must then hold raw image batches)."""
     out = []
     fsc = None
     for _ in range(iterations):
+        sizes = (int(halves[0].model["current_size"]), int(halves[0].model["coarse_size"]))
         bundles = [h.expectation() for h in halves]
         for h, b in zip(halves, bundles):
             h.maximization(b, fsc)
         b0 = MlDeviceBundle(halves[0].model, device=halves[0].device)
         fsc = b0.fsc(halves[0].maps[0], halves[1].maps[0])
         b0.close()
+        if adapt_sizes is not None:
+            # both halves take the sizes of the joint data_vs_prior (FSC-based after the first pass)
+            for h in halves:
+                update_image_sizes(h.model, halves[0].dvp + halves[1].dvp, **adapt_sizes)
         out.append(dict(fsc=fsc, resolution=resolution_at(fsc, int(halves[0].model["ori_size"]), pixel_size),
-                        LL=[h.model["LL"] for h in halves]))
+                        LL=[h.model["LL"] for h in halves], sizes=sizes))
     return out
 
 

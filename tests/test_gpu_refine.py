@@ -42,3 +42,28 @@ def test_refinement_equal_fsc():
     assert bf[-1]["resolution"] == fp[-1]["resolution"]
     # the half maps agree at low resolution: the refinement found a common structure
     assert bf[-1]["fsc"][1:4].min() > 0.5
+
+
+def test_refinement_adaptive_sizes_from_raw_images():
+    # raw real-space images prepared on the device at each iteration's
+    # current size; the sizes follow data_vs_prior between iterations
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from relion_gb300 import datagen, iteration
+    ds = datagen.Dataset("cfg0_box64", seed=23, n_particles=128, healpix_order=1, psi_step=30.0)
+    m = ds.model(precision=1)
+    box, pix = m["ori_size"], m["pixel_size"]
+    ini = iteration.gaussian_map(ds.vol, box, lowpass_px=box * pix / ds.cfg["ini_high"])
+    optics = dict(kV=300.0, Cs=2.7, Q0=0.1, particle_diameter=ds.cfg["diameter"], width_mask_edge=5.0)
+    halves = [iteration.HalfSet(m, [ini], [ds.particle_images(h * 64, 64)], optics=optics) for h in range(2)]
+    out = iteration.refine(halves, 3, pix, adapt_sizes=dict(angular_sampling_deg=360.0 / (6 * 2),
+                                                            particle_diameter=ds.cfg["diameter"]))
+    for it in out:
+        print("sizes", it["sizes"], "resolution %.2f A" % it["resolution"])
+        assert np.all(np.isfinite(it["fsc"][1:it["sizes"][0] // 2]))
+    cur0 = m["current_size"]
+    assert all(it["sizes"][0] % 2 == 0 and it["sizes"][1] <= it["sizes"][0] <= box for it in out)
+    assert out[0]["sizes"][0] == cur0
+    assert halves[0].model["current_size"] == halves[1].model["current_size"]
+    assert out[-1]["fsc"][1:4].min() > 0.5
