@@ -229,6 +229,7 @@ def run_ours(args, world, rank, local):
 
     mstep = mstep_section(args, ds, model, bundle, worker, dev_batch, local) if rank == 0 and not args.no_mstep \
         else None
+    io = io_section(ds, ib, model) if rank == 0 and not args.no_mstep else None
 
     # ---- roofline of the dominant kernel: the coarse cross-term GEMM ----
     R = bundle.nr_classes * bundle.ndir * bundle.npsi
@@ -297,7 +298,48 @@ def run_ours(args, world, rank, local):
     if rank == 0:
         out["clocks"] = clk.summary()
         out["mstep"] = mstep
+        out["io"] = io
     return out, ds, batch, model
+
+
+def io_section(ds, ib, model):
+    """Data formats: the batch's raw images written as an MRC stack with a
+    RELION 3.1 STAR file, then read back through the native reader (page
+    cache warm: the second of two reads is timed)."""
+    import shutil
+    import tempfile
+    import time
+    from relion_gb300 import io as gio
+    d = tempfile.mkdtemp()
+    try:
+        n, box, pix = ib["images"].shape[0], model["ori_size"], model["pixel_size"]
+        stack = os.path.join(d, "parts.mrcs")
+        gio.write_mrc_stack(stack, ib["images"], pix)
+        star = os.path.join(d, "parts.star")
+        gio.write_star(star, {"optics": {"rlnOpticsGroup": [1], "rlnVoltage": [300.0],
+                                         "rlnSphericalAberration": [2.7], "rlnAmplitudeContrast": [0.1],
+                                         "rlnImagePixelSize": [pix], "rlnImageSize": [box]},
+                              "particles": {"rlnImageName": ["%06d@parts.mrcs" % (i + 1) for i in range(n)],
+                                            "rlnDefocusU": list(ib["ctf"][:, 0]), "rlnDefocusV": list(ib["ctf"][:, 1]),
+                                            "rlnDefocusAngle": list(ib["ctf"][:, 2]),
+                                            "rlnOriginXAngst": [0.0] * n, "rlnOriginYAngst": [0.0] * n,
+                                            "rlnOpticsGroup": [1] * n}})
+        out = np.empty((n, box, box), np.float32)
+        threads = min(16, os.cpu_count() or 1)
+        for _ in range(2):
+            t0 = time.perf_counter()
+            gio.read_mrc_images(stack, out=out, nthreads=threads)
+            t_mrc = time.perf_counter() - t0
+        for _ in range(2):
+            t0 = time.perf_counter()
+            lb = gio.load_particles(star, nthreads=threads)
+            t_load = time.perf_counter() - t0
+        assert np.array_equal(lb["images"], ib["images"])
+        return {"mrc_read_GBps": round(out.nbytes / t_mrc / 1e9, 2), "load_particles_per_s": round(n / t_load),
+                "threads": threads, "note": "%d images of %d^2 float32 (%.0f MB), page cache warm; "
+                "load_particles = STAR parse + MRC read into the image batch" % (n, box, out.nbytes / 1e6)}
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
 
 
 def mstep_section(args, ds, model, bundle, worker, dev_batch, local):

@@ -140,14 +140,6 @@ __device__ __forceinline__ uint32_t chunk_off(int row, int kg) {
     return (uint32_t)((((row >> 3) * (TK / 8) + kg) << 7) + ((row & 7) << 4));
 }
 
-// Chunk c of a tile -> (row, kg): each warp writes 512 contiguous bytes
-// (8 rows x 4 K-groups), so the shared-memory stores are conflict-free.
-__device__ __forceinline__ void chunk_rc(int c, int &row, int &kg) {
-    const int lane = c & 31, wi = c >> 5;
-    kg = (lane >> 3) + 4 * (wi & 1);
-    row = (wi >> 1) * 8 + (lane & 7);
-}
-
 __device__ __forceinline__ bool arrive_expect_tx(uint32_t bar, uint32_t bytes) {
     uint64_t state;
     asm volatile("mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 %0, [%1], %2;"
