@@ -14,6 +14,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <array>
 #include <map>
 #include <type_traits>
 #include <string>
@@ -72,6 +73,17 @@ struct MapTerm {
     double ovc_fudge;  // oversampling_correction * tau2_fudge
     double pad;
     int minres, on;
+    const int *iround;  // ROUND(sqrt(r2) / pad) by r2
+};
+
+// Per-r2 tables, built once on the host in double precision (GB300's FP64
+// rate makes a sqrt / sin / cos per voxel the bottleneck of these passes):
+// shell indices ROUND(sqrt(r2) / p) and FLOOR(sqrt(r2) / p), and for the
+// real-space box the gridding correction 1 / sinc^2 and the soft-mask
+// weight (< 0 inside the radius, > 1.5 beyond the cosine edge).
+struct RealTab {
+    const double *inv_sinc2;
+    const double *rc;
 };
 
 // decenter(weight) (src/projector.h:249-260) plus the MAP term
@@ -79,7 +91,7 @@ __device__ __forceinline__ double fweight_at(const double *weight, const VolGeom
                                              int max_r2, const MapTerm &m) {
     double fw = (r2 <= max_r2) ? weight[cidx(g, kp, ip, jp)] : 0.;
     if (m.on && r2 < max_r2) {
-        const int ires = d_round(sqrt((double)r2) / m.pad);
+        const int ires = m.iround[r2];
         const double t = m.tau2[ires];
         const double inv = (t > 0.) ? 1. / (m.ovc_fudge * t) : ((fw > 1e-20) ? 1. / (0.001 * fw) : 0.);
         if (ires >= m.minres) fw = fw + inv;
@@ -111,7 +123,7 @@ __global__ void k_hermitian(double2 *data, double *weight, VolGeom g) {
 
 // updateSSNRarrays, pass 0: sigma2 and counter; pass 1: data_vs_prior,
 // coverage and counter with the final tau2.  sums [3][ns]
-__global__ void k_ssnr(const double *weight, VolGeom g, int max_r2, double pad, double ovc, int pass,
+__global__ void k_ssnr(const double *weight, VolGeom g, int max_r2, const int *iround, double ovc, int pass,
                        const double *tau2, double ovc_fudge, int upd, int ns, double *sums) {
     extern __shared__ double sh[];
     for (int b = threadIdx.x; b < 3 * ns; b += blockDim.x) sh[b] = 0.;
@@ -124,7 +136,7 @@ __global__ void k_ssnr(const double *weight, VolGeom g, int max_r2, double pad, 
         const int i = g.yinit + (int)(t % g.ydim), k = g.zinit + (int)(t / g.ydim);
         const int r2 = k * k + i * i + j * j;
         if (r2 >= max_r2) continue;
-        const int ires = d_round(sqrt((double)r2) / pad);
+        const int ires = iround[r2];
         const double w = weight[n];
         if (pass == 0) {
             atomicAdd(&sh[ires], ovc * w);
@@ -144,20 +156,40 @@ __global__ void k_ssnr(const double *weight, VolGeom g, int max_r2, double pad, 
 
 // skip-gridding branch: radial sums of Fweight (FLOOR shells) [2][r_max]
 __global__ void k_radavg(const double *weight, VolGeom g, Half h, int max_r2, int round_max_r2, MapTerm m,
-                         int r_max, double *sums) {
+                         const int *ifloor, int r_max, double *sums) {
     extern __shared__ double sh[];
     for (int b = threadIdx.x; b < 2 * r_max; b += blockDim.x) sh[b] = 0.;
     __syncthreads();
-    for (long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x; n < h.size();
-         n += (long long)gridDim.x * blockDim.x) {
-        int k, i, j;
-        h.at(n, k, i, j);
-        const int kp = h.kp(k), ip = h.ip(i);
-        const int r2 = kp * kp + ip * ip + j * j;
-        if (r2 >= round_max_r2) continue;
-        const int ires = (int)(sqrt((double)r2) / m.pad);
-        atomicAdd(&sh[ires], fweight_at(weight, g, kp, ip, j, r2, max_r2, m));
-        atomicAdd(&sh[r_max + ires], 1.);
+    // runs of kRunR consecutive elements per thread, neighbours of one shell
+    // summed before the shared-memory atomic
+    constexpr int kRunR = 8;
+    for (long long n0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * kRunR; n0 < h.size();
+         n0 += (long long)gridDim.x * blockDim.x * kRunR) {
+        int cur = -1;
+        double acc = 0., cnt = 0.;
+        for (int q = 0; q < kRunR && n0 + q < h.size(); ++q) {
+            int k, i, j;
+            h.at(n0 + q, k, i, j);
+            const int kp = h.kp(k), ip = h.ip(i);
+            const int r2 = kp * kp + ip * ip + j * j;
+            if (r2 >= round_max_r2) continue;
+            const int ires = ifloor[r2];
+            if (ires != cur) {
+                if (cur >= 0) {
+                    atomicAdd(&sh[cur], acc);
+                    atomicAdd(&sh[r_max + cur], cnt);
+                }
+                cur = ires;
+                acc = 0.;
+                cnt = 0.;
+            }
+            acc += fweight_at(weight, g, kp, ip, j, r2, max_r2, m);
+            cnt += 1.;
+        }
+        if (cur >= 0) {
+            atomicAdd(&sh[cur], acc);
+            atomicAdd(&sh[r_max + cur], cnt);
+        }
     }
     __syncthreads();
     for (int b = threadIdx.x; b < 2 * r_max; b += blockDim.x)
@@ -173,8 +205,8 @@ __global__ void k_radavg(const double *weight, VolGeom g, Half h, int max_r2, in
 // (fn = Fnewweight on hin, data divided by normalise).
 template <class R>
 __global__ void k_window(const double2 *data, const double *weight, VolGeom g, Half hin, Half hout, int max_r2,
-                         MapTerm m, int mode, const double *sums, int r_max, const double *fn, double normalise,
-                         typename Cx<R>::T *out, int *err) {
+                         MapTerm m, const int *ifloor, int mode, const double *sums, int r_max, const double *fn,
+                         double normalise, typename Cx<R>::T *out, int *err) {
     extern __shared__ double ra[];
     if (mode == 0) {
         for (int b = threadIdx.x; b < r_max; b += blockDim.x) {
@@ -201,7 +233,7 @@ __global__ void k_window(const double2 *data, const double *weight, VolGeom g, H
             v = data[cidx(g, kp, ip, j)];
             if (mode == 0) {
                 const double fw = fweight_at(weight, g, kp, ip, j, r2, max_r2, m);
-                const int ires = (int)(sqrt((double)r2) / m.pad);
+                const int ires = ifloor[r2];
                 const double w = fmax(fw, ra[(ires < r_max) ? ires : (r_max - 1)]);
                 if (w != 0.) v = make_double2(v.x / w, v.y / w);
             } else {
@@ -282,12 +314,11 @@ __global__ void k_grid_update(typename Cx<R>::T *C, const double *fw, double *fn
 // window the padded real box to ori (centred), divide by normfft and sum the
 // background of softMaskOutsideMap (radius ori/2, cosine width 3): bg [2]
 template <class R>
-__global__ void k_crop_bg(const R *M, int No, int rowp, int ori, int dim, double normfft, double *vol,
+__global__ void k_crop_bg(const R *M, int No, int rowp, int ori, int dim, double normfft, RealTab tab, double *vol,
                           double *bg) {
     __shared__ double s_sum[kThreads / 32], s_bg[kThreads / 32];
     const int h = ori / 2, off = No / 2 - h;
     const long long total = (long long)(dim == 3 ? ori : 1) * ori * ori;
-    const double radius = (double)ori / 2., radius_p = radius + 3.;
     double sum = 0., sbg = 0.;
     for (long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x; n < total;
          n += (long long)gridDim.x * blockDim.x) {
@@ -298,13 +329,12 @@ __global__ void k_crop_bg(const R *M, int No, int rowp, int ori, int dim, double
         const double v = (double)M[((long long)zo * No + (y + off)) * rowp + (x + off)] / normfft;
         vol[n] = v;
         const int k = dim == 3 ? z - h : 0, i = y - h, j = x - h;
-        const double r = sqrt((double)(k * k + i * i + j * j));
-        if (r < radius) continue;
-        if (r > radius_p) {
+        const double rc = tab.rc[k * k + i * i + j * j];
+        if (rc < 0.) continue;
+        if (rc > 1.5) {
             sum += 1.;
             sbg += v;
         } else {
-            const double rc = 0.5 + 0.5 * cos(kPi * (radius_p - r) / 3.);
             sum += rc;
             sbg += rc * v;
         }
@@ -331,39 +361,28 @@ __global__ void k_crop_bg(const R *M, int No, int rowp, int ori, int dim, double
 
 // apply softMaskOutsideMap with the background average, then
 // griddingCorrect (trilinear: divide by sinc^2 for r > 0)
-__global__ void k_mask_gridcorr(double *vol, int ori, int dim, double ori_pad, const double *bg) {
+__global__ void k_mask_gridcorr(double *vol, int ori, int dim, RealTab tab, const double *bg) {
     const int h = ori / 2;
     const long long total = (long long)(dim == 3 ? ori : 1) * ori * ori;
-    const double radius = (double)ori / 2., radius_p = radius + 3., avg = bg[1] / bg[0];
+    const double avg = bg[1] / bg[0];
     for (long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x; n < total;
          n += (long long)gridDim.x * blockDim.x) {
         const int x = (int)(n % ori);
         const long long t = n / ori;
         const int y = (int)(t % ori), z = (int)(t / ori);
         const int k = dim == 3 ? z - h : 0, i = y - h, j = x - h;
-        const double r = sqrt((double)(k * k + i * i + j * j));
+        const int r2 = k * k + i * i + j * j;
+        const double rc = tab.rc[r2];
         double v = vol[n];
-        if (r >= radius) {
-            if (r > radius_p) {
-                v = avg;
-            } else {
-                const double rc = 0.5 + 0.5 * cos(kPi * (radius_p - r) / 3.);
-                v = (1 - rc) * v + rc * avg;
-            }
-        }
-        if (r > 0.) {
-            const double rv = r / ori_pad;
-            const double sinc = sin(kPi * rv) / (kPi * rv);
-            v /= sinc * sinc;
-        }
-        vol[n] = v;
+        if (rc >= 0.) v = rc > 1.5 ? avg : (1 - rc) * v + rc * avg;
+        vol[n] = v * tab.inv_sinc2[r2];
     }
 }
 
 // computeFourierTransformMap: gridding pre-correction and zero padding into
 // the real rows of an in-place transform of size No
 template <class R>
-__global__ void k_pad_map(const double *vol, int ori, int dim, int No, int rowp, double ori_pad, int do_grid,
+__global__ void k_pad_map(const double *vol, int ori, int dim, int No, int rowp, const double *inv_sinc2,
                           R *M) {
     const int h = ori / 2, ho = No / 2;
     const long long total = (long long)(dim == 3 ? No : 1) * No * rowp;
@@ -376,14 +395,7 @@ __global__ void k_pad_map(const double *vol, int ori, int dim, int No, int rowp,
         double v = 0.;
         if (x < No && k >= -h && k < ori - h && i >= -h && i < ori - h && j >= -h && j < ori - h) {
             v = vol[((long long)(dim == 3 ? k + h : 0) * ori + (i + h)) * ori + (j + h)];
-            if (do_grid) {
-                const double r = sqrt((double)(k * k + i * i + j * j));
-                if (r > 0.) {
-                    const double rv = r / ori_pad;
-                    const double sinc = sin(kPi * rv) / (kPi * rv);
-                    v /= sinc * sinc;
-                }
-            }
+            if (inv_sinc2) v *= inv_sinc2[k * k + i * i + j * j];
         }
         M[n] = (R)v;
     }
@@ -393,25 +405,44 @@ __global__ void k_pad_map(const double *vol, int ori, int dim, int No, int rowp,
 // r2 <= max_r2 in the projector layout, radial power [2][ns]
 template <class R>
 __global__ void k_fill_projector(const typename Cx<R>::T *F, Half h, VolGeom pg, int max_r2, int min_r2, double nreal,
-                                 double normfft, double pad, int ns, float2 *proj, double *power) {
+                                 double normfft, const int *iround, int ns, float2 *proj, double *power) {
     extern __shared__ double sh[];
     for (int b = threadIdx.x; b < 2 * ns; b += blockDim.x) sh[b] = 0.;
     __syncthreads();
-    for (long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x; n < h.size();
-         n += (long long)gridDim.x * blockDim.x) {
-        int k, i, j;
-        h.at(n, k, i, j);
-        const int kp = h.kp(k), ip = h.ip(i);
-        const int r2 = kp * kp + ip * ip + j * j;
-        if (r2 > max_r2) continue;
-        double2 v = make_double2((double)F[n].x / nreal, (double)F[n].y / nreal);
-        if ((k ^ i ^ j) & 1) v = make_double2(-v.x, -v.y);
-        v = make_double2(v.x * normfft, v.y * normfft);
-        const int ires = d_round(sqrt((double)r2) / pad);
-        atomicAdd(&sh[ires], (v.x * v.x + v.y * v.y) / 2.);
-        atomicAdd(&sh[ns + ires], 1.);
-        if (r2 <= min_r2) v = make_double2(0., 0.);
-        proj[cidx(pg, kp, ip, j)] = make_float2((float)v.x, (float)v.y);
+    constexpr int kRunF = 8;  // consecutive elements per thread, one shell summed before its atomic
+    for (long long n0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * kRunF; n0 < h.size();
+         n0 += (long long)gridDim.x * blockDim.x * kRunF) {
+        int cur = -1;
+        double acc = 0., cnt = 0.;
+        for (int q = 0; q < kRunF && n0 + q < h.size(); ++q) {
+            const long long n = n0 + q;
+            int k, i, j;
+            h.at(n, k, i, j);
+            const int kp = h.kp(k), ip = h.ip(i);
+            const int r2 = kp * kp + ip * ip + j * j;
+            if (r2 > max_r2) continue;
+            double2 v = make_double2((double)F[n].x / nreal, (double)F[n].y / nreal);
+            if ((k ^ i ^ j) & 1) v = make_double2(-v.x, -v.y);
+            v = make_double2(v.x * normfft, v.y * normfft);
+            const int ires = iround[r2];
+            if (ires != cur) {
+                if (cur >= 0) {
+                    atomicAdd(&sh[cur], acc);
+                    atomicAdd(&sh[ns + cur], cnt);
+                }
+                cur = ires;
+                acc = 0.;
+                cnt = 0.;
+            }
+            acc += (v.x * v.x + v.y * v.y) / 2.;
+            cnt += 1.;
+            if (r2 <= min_r2) v = make_double2(0., 0.);
+            proj[cidx(pg, kp, ip, j)] = make_float2((float)v.x, (float)v.y);
+        }
+        if (cur >= 0) {
+            atomicAdd(&sh[cur], acc);
+            atomicAdd(&sh[ns + cur], cnt);
+        }
     }
     __syncthreads();
     for (int b = threadIdx.x; b < 2 * ns; b += blockDim.x)
@@ -420,7 +451,8 @@ __global__ void k_fill_projector(const typename Cx<R>::T *F, Half h, VolGeom pg,
 
 // getFSC shell sums [3][X]: Re(conj z1 z2), |z1|^2, |z2|^2
 template <class R>
-__global__ void k_fsc(const typename Cx<R>::T *F1, const typename Cx<R>::T *F2, Half h, double nreal, double *sums) {
+__global__ void k_fsc(const typename Cx<R>::T *F1, const typename Cx<R>::T *F2, Half h, double nreal, const int *iround1,
+                      double *sums) {
     extern __shared__ double sh[];
     for (int b = threadIdx.x; b < 3 * h.X; b += blockDim.x) sh[b] = 0.;
     __syncthreads();
@@ -429,7 +461,7 @@ __global__ void k_fsc(const typename Cx<R>::T *F1, const typename Cx<R>::T *F2, 
         int k, i, j;
         h.at(n, k, i, j);
         const int kp = h.kp(k), ip = h.ip(i);
-        const int idx = d_round(sqrt((double)(kp * kp + ip * ip + j * j)));
+        const int idx = iround1[kp * kp + ip * ip + j * j];
         if (idx >= h.X) continue;
         const double2 z1 = make_double2((double)F1[n].x / nreal, (double)F1[n].y / nreal);
         const double2 z2 = make_double2((double)F2[n].x / nreal, (double)F2[n].y / nreal);
@@ -516,6 +548,7 @@ std::vector<double> blob_table() {
 struct ReconWork {
     Scratch c1, c2, fw, fn, vol, small, tab;
     std::map<long long, cufftHandle> plans;
+    std::map<std::array<int, 4>, Scratch> tabs;  // per-r2 tables by (kind, a, b, entries)
     bool have_tab = false;
     bool fp32 = false;  // transforms in FP32 instead of FP64
     ~ReconWork() {
@@ -564,6 +597,57 @@ int exec_fwd(ReconWork *w, int N, int dim, void *buf) {
 
 void recon_set_fp32(ReconWork *w, int fp32) { w->fp32 = fp32 != 0; }
 
+namespace {
+// Device table of n entries of type T built by fill(r2) on the host, cached.
+template <class T, class F>
+const T *cached_table(ReconWork *w, int kind, int a, int b, int n, F fill, int &st) {
+    const std::array<int, 4> key{kind, a, b, n};
+    auto it = w->tabs.find(key);
+    if (it != w->tabs.end()) return it->second.as<T>();
+    std::vector<T> h((size_t)n);
+    for (int r2 = 0; r2 < n; ++r2) h[(size_t)r2] = fill(r2);
+    Scratch &sc = w->tabs[key];
+    cudaError_t e = sc.reserve(sizeof(T) * (size_t)n);
+    if (e == cudaSuccess) e = cudaMemcpy(sc.p, h.data(), sizeof(T) * (size_t)n, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        set_error_text(std::string("reconstruction table: ") + cudaGetErrorString(e));
+        st = e == cudaErrorMemoryAllocation ? kErrOom : kErrCuda;
+        w->tabs.erase(key);
+        return nullptr;
+    }
+    return sc.as<T>();
+}
+
+// ROUND(sqrt(r2) / p) (floor_mode 0) or FLOOR(sqrt(r2) / p) for r2 < n
+const int *shell_table(ReconWork *w, int p, int n, int floor_mode, int &st) {
+    return cached_table<int>(w, floor_mode ? 1 : 0, p, 0, n, [&](int r2) {
+        const double x = std::sqrt((double)r2) / p;
+        return floor_mode ? (int)x : d_round(x);
+    }, st);
+}
+
+// gridding correction and soft-mask weights of the real box (ori, pad)
+RealTab real_tables(ReconWork *w, int ori, int pad, int &st) {
+    const int n = 3 * (ori / 2) * (ori / 2) + 1;
+    RealTab t{};
+    t.inv_sinc2 = cached_table<double>(w, 2, ori, pad, n, [&](int r2) {
+        const double r = std::sqrt((double)r2);
+        if (!(r > 0.)) return 1.;
+        const double rval = r / ((double)ori * pad);
+        const double sinc = std::sin(kPi * rval) / (kPi * rval);
+        return 1. / (sinc * sinc);
+    }, st);
+    if (!t.inv_sinc2) return t;
+    t.rc = cached_table<double>(w, 3, ori, 0, n, [&](int r2) {
+        const double r = std::sqrt((double)r2), radius = (double)ori / 2., radius_p = radius + 3.;
+        if (r < radius) return -1.;
+        if (r > radius_p) return 2.;
+        return 0.5 + 0.5 * std::cos(kPi * (radius_p - r) / 3.);
+    }, st);
+    return t;
+}
+}  // namespace
+
 ReconWork *recon_work_create() { return new ReconWork(); }
 void recon_work_destroy(ReconWork *w) { delete w; }
 
@@ -595,7 +679,10 @@ int recon_update_ssnr(ReconWork *w, const double *weight, const VolGeom &g, int 
     std::vector<double> h(3 * ns);
     const size_t smem = sizeof(double) * 3 * ns;
     RC_CUDA(cudaMemset(sums, 0, smem));
-    k_ssnr<<<grid_for(nvox), kThreads, smem>>>(weight, g, max_r2, pad, ovc, 0, nullptr, 0., upd, ns, sums);
+    int tst = 0;
+    const int *iround = shell_table(w, g.pad, mr * mr + 1, 0, tst);
+    if (!iround) return tst;
+    k_ssnr<<<grid_for(nvox), kThreads, smem>>>(weight, g, max_r2, iround, ovc, 0, nullptr, 0., upd, ns, sums);
     RC_CUDA(cudaGetLastError());
     RC_CUDA(cudaMemcpy(h.data(), sums, smem, cudaMemcpyDeviceToHost));
     std::vector<double> sigma2(ns), tau2(tau2_io, tau2_io + ns), dvp(ns, 0.), cov(ns, 0.);
@@ -620,7 +707,7 @@ int recon_update_ssnr(ReconWork *w, const double *weight, const VolGeom &g, int 
         if (tau2[i] < 0.) return fail_recon(kErrNumerical, "updateSSNRarrays: negative tau2 spectrum");
     RC_CUDA(cudaMemcpy(tau2_d, tau2.data(), sizeof(double) * ns, cudaMemcpyHostToDevice));
     RC_CUDA(cudaMemset(sums, 0, smem));
-    k_ssnr<<<grid_for(nvox), kThreads, smem>>>(weight, g, max_r2, pad, ovc, 1, tau2_d, ovc * tau2_fudge, upd, ns,
+    k_ssnr<<<grid_for(nvox), kThreads, smem>>>(weight, g, max_r2, iround, ovc, 1, tau2_d, ovc * tau2_fudge, upd, ns,
                                                 sums);
     RC_CUDA(cudaGetLastError());
     RC_CUDA(cudaMemcpy(h.data(), sums, smem, cudaMemcpyDeviceToHost));
@@ -663,16 +750,21 @@ int reconstruct_impl(ReconWork *w, const double2 *data, const double *weight, co
         if (!tau2_host) return fail_recon(kErrInvalid, "reconstruct: do_map needs tau2");
         RC_CUDA(cudaMemcpy(tau2_d, tau2_host, sizeof(double) * ns, cudaMemcpyHostToDevice));
     }
-    const MapTerm m{tau2_d, ovc * p.tau2_fudge, pad, p.minres_map, p.do_map ? 1 : 0};
+    int tst = 0;
+    const int *iround = shell_table(w, g.pad, max_r2 + 1, 0, tst);
+    const int *ifloor = iround ? shell_table(w, g.pad, max_r2 + 1, 1, tst) : nullptr;
+    const RealTab rtab = ifloor ? real_tables(w, ori, g.pad, tst) : RealTab{};
+    if (!rtab.rc) return tst;
+    const MapTerm m{tau2_d, ovc * p.tau2_fudge, pad, p.minres_map, p.do_map ? 1 : 0, iround};
     RC_CUDA(w->c1.reserve(sizeof(C2) * hout.size()));
     C2 *Fo = w->c1.as<C2>();
     if (!grid) {
         const int rm2 = d_round(r_max * pad * r_max * pad);
-        k_radavg<<<grid_for(hin.size()), kThreads, sizeof(double) * 2 * r_max>>>(weight, g, hin, max_r2, rm2, m,
-                                                                                r_max, sums);
+        k_radavg<<<grid_for(hin.size() / 8 + 1), kThreads, sizeof(double) * 2 * r_max>>>(
+            weight, g, hin, max_r2, rm2, m, ifloor, r_max, sums);
         RC_CUDA(cudaGetLastError());
         k_window<R><<<grid_for(hout.size()), kThreads, sizeof(double) * r_max>>>(
-            data, weight, g, hin, hout, max_r2, m, 0, sums, r_max, nullptr, 1., Fo, err);
+            data, weight, g, hin, hout, max_r2, m, ifloor, 0, sums, r_max, nullptr, 1., Fo, err);
         RC_CUDA(cudaGetLastError());
     } else {
         RC_CUDA(w->c2.reserve(sizeof(C2) * hin.size()));
@@ -703,8 +795,8 @@ int reconstruct_impl(ReconWork *w, const double2 *data, const double *weight, co
             k_grid_update<R><<<grid_for(hin.size()), kThreads>>>(C, fw, fn, hin, max_r2);
             RC_CUDA(cudaGetLastError());
         }
-        k_window<R><<<grid_for(hout.size()), kThreads, 0>>>(data, weight, g, hin, hout, max_r2, m, 1, sums, r_max, fn,
-                                                             p.normalise, Fo, err);
+        k_window<R><<<grid_for(hout.size()), kThreads, 0>>>(data, weight, g, hin, hout, max_r2, m, ifloor, 1, sums,
+                                                             r_max, fn, p.normalise, Fo, err);
         RC_CUDA(cudaGetLastError());
     }
     int st = exec_inv<R>(w, No, dim, Fo);
@@ -713,10 +805,10 @@ int reconstruct_impl(ReconWork *w, const double2 *data, const double *weight, co
     RC_CUDA(w->vol.reserve(sizeof(double) * nv));
     double *vol = w->vol.as<double>();
     const double normfft = dim == 3 ? pad * pad * pad * ori : pad * pad;
-    k_crop_bg<R><<<grid_for(nv), kThreads>>>(reinterpret_cast<const R *>(Fo), No, hout.rowp(), ori, dim, normfft, vol,
-                                             bg);
+    k_crop_bg<R><<<grid_for(nv), kThreads>>>(reinterpret_cast<const R *>(Fo), No, hout.rowp(), ori, dim, normfft, rtab,
+                                             vol, bg);
     RC_CUDA(cudaGetLastError());
-    k_mask_gridcorr<<<grid_for(nv), kThreads>>>(vol, ori, dim, (double)ori * pad, bg);
+    k_mask_gridcorr<<<grid_for(nv), kThreads>>>(vol, ori, dim, rtab, bg);
     RC_CUDA(cudaGetLastError());
     int herr = 0;
     RC_CUDA(cudaMemcpy(&herr, err, sizeof(int), cudaMemcpyDeviceToHost));
@@ -743,8 +835,11 @@ int projector_impl(ReconWork *w, const double *vol_host, int ori, int dim, int p
     RC_CUDA(w->c1.reserve(sizeof(C2) * ho.size()));
     C2 *F = w->c1.as<C2>();
     const long long nreal_p = (long long)ho.Z * ho.Y * ho.rowp();
-    k_pad_map<R><<<grid_for(nreal_p), kThreads>>>(w->vol.as<double>(), ori, dim, No, ho.rowp(), (double)ori * pad,
-                                                  do_gridding, reinterpret_cast<R *>(F));
+    int tst = 0;
+    const RealTab rtab = real_tables(w, ori, pad, tst);
+    if (!rtab.rc) return tst;
+    k_pad_map<R><<<grid_for(nreal_p), kThreads>>>(w->vol.as<double>(), ori, dim, No, ho.rowp(),
+                                                  do_gridding ? rtab.inv_sinc2 : nullptr, reinterpret_cast<R *>(F));
     RC_CUDA(cudaGetLastError());
     int st = exec_fwd<R>(w, No, dim, F);
     if (st) return st;
@@ -756,8 +851,10 @@ int projector_impl(ReconWork *w, const double *vol_host, int ori, int dim, int p
     const int mn = d_round(min_ires * (double)pad), min_r2 = min_ires > 0 ? mn * mn : -1;
     const double normfft = dim == 3 ? (double)pad * pad * pad * ori : (double)pad * pad;
     const double nreal = (double)ho.Z * ho.Y * ho.N;
-    k_fill_projector<R><<<grid_for(ho.size()), kThreads, sizeof(double) * 2 * ns>>>(
-        F, ho, pg, max_r2, min_r2, nreal, normfft, (double)pad, ns, proj, sums);
+    const int *iround = shell_table(w, pad, max_r2 + 1, 0, tst);
+    if (!iround) return tst;
+    k_fill_projector<R><<<grid_for(ho.size() / 8 + 1), kThreads, sizeof(double) * 2 * ns>>>(
+        F, ho, pg, max_r2, min_r2, nreal, normfft, iround, ns, proj, sums);
     RC_CUDA(cudaGetLastError());
     std::vector<double> h(2 * ns);
     RC_CUDA(cudaMemcpy(h.data(), sums, sizeof(double) * 2 * ns, cudaMemcpyDeviceToHost));
@@ -780,7 +877,7 @@ int fsc_impl(ReconWork *w, const double *m1, const double *m2, int ori, int dim,
         R *dst = which ? w->c2.as<R>() : w->c1.as<R>();
         // padding to the map's own size: a plain copy into the padded rows
         k_pad_map<R><<<grid_for((long long)h.Z * h.Y * h.rowp()), kThreads>>>(w->vol.as<double>(), ori, dim, ori,
-                                                                               h.rowp(), 1., 0, dst);
+                                                                               h.rowp(), nullptr, dst);
         RC_CUDA(cudaGetLastError());
         const int st = exec_fwd<R>(w, ori, dim, dst);
         if (st) return st;
@@ -788,8 +885,11 @@ int fsc_impl(ReconWork *w, const double *m1, const double *m2, int ori, int dim,
     RC_CUDA(w->small.reserve(sizeof(double) * 3 * h.X));
     double *sums = w->small.as<double>();
     RC_CUDA(cudaMemset(sums, 0, sizeof(double) * 3 * h.X));
+    int tst = 0;
+    const int *iround1 = shell_table(w, 1, 3 * (ori / 2) * (ori / 2) + 1, 0, tst);
+    if (!iround1) return tst;
     k_fsc<R><<<grid_for(h.size()), kThreads, sizeof(double) * 3 * h.X>>>(w->c1.as<C2>(), w->c2.as<C2>(), h,
-                                                                          (double)h.Z * h.Y * h.N, sums);
+                                                                          (double)h.Z * h.Y * h.N, iround1, sums);
     RC_CUDA(cudaGetLastError());
     std::vector<double> s(3 * h.X);
     RC_CUDA(cudaMemcpy(s.data(), sums, sizeof(double) * 3 * h.X, cudaMemcpyDeviceToHost));
