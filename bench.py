@@ -55,6 +55,9 @@ def parse():
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mstep", action="store_true", help="skip the reconstruction-side section (profiling runs)")
+    ap.add_argument("--workload", default=CONFIG,
+                    choices=["cfg1_box256", "cfg4_box256_K4", "cfg3_box128_2d", "cfg0_box64"],
+                    help="dataset shape (the headline line is cfg1_box256; the others for reference figures)")
     ap.add_argument("--precision", default="bf16", choices=["fp32", "bf16"],
                     help="coarse cross term: plain FP32 SIMT or tcgen05 BF16 (precision form)")
     return ap.parse_args()
@@ -126,12 +129,12 @@ def run_ours(args, world, rank, local):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     B = args.batch
-    ds = datagen.Dataset(CONFIG, seed=args.seed + rank, n_particles=B, device=str(dev))
+    ds = datagen.Dataset(args.workload, seed=args.seed + rank, n_particles=B, device=str(dev))
     model = ds.model(precision=1 if args.precision == "bf16" else 0)
     batch = ds.particles(0, B)
     bundle = MlDeviceBundle(model, device=local)
-    r = ds.ref
-    bundle.setup_projector(0, r["data"], r["yinit"], r["zinit"], r["r_max"], r["pad"])
+    for k, r in enumerate(ds.refs):
+        bundle.setup_projector(k, r["data"], r["yinit"], r["zinit"], r["r_max"], r["pad"])
     bundle.reserve(64 << 30)
     worker = MlOptimiserCuda(bundle)
 
@@ -227,9 +230,9 @@ def run_ours(args, world, rank, local):
         from relion_gb300.replicas import max_over_ranks
         total_ms, e2e_total, img_total = max_over_ranks([total_ms, e2e_total, img_total], device=dev)
 
-    mstep = mstep_section(args, ds, model, bundle, worker, dev_batch, local) if rank == 0 and not args.no_mstep \
-        else None
-    io = io_section(ds, ib, model) if rank == 0 and not args.no_mstep else None
+    extra = rank == 0 and not args.no_mstep and args.workload == CONFIG  # sections of the headline workload
+    mstep = mstep_section(args, ds, model, bundle, worker, dev_batch, local) if extra else None
+    io = io_section(ds, ib, model) if extra else None
 
     # ---- roofline of the dominant kernel: the coarse cross-term GEMM ----
     R = bundle.nr_classes * bundle.ndir * bundle.npsi
@@ -263,8 +266,7 @@ def run_ours(args, world, rank, local):
         "dtype": "bf16 (coarse cross term) / fp32 (fine pass) / f64 (sums, volumes)"
                  if args.precision == "bf16" else "fp32 / f64 (sums, volumes)",
         "data": "synthetic (seeded Gaussian-blob volume, analytic Fourier slices, CTF, white noise)",
-        "config": {"workload": "box256 E-step, iteration-1 sizes (current 46 px), HEALPix order 3 x 48 psi, "
-                               "113 translations, oversampling 1, 1 class",
+        "config": {"workload": workload_text(args.workload, bundle, model),
                    "batch_particles": B,
                    "precision": "precision form: tcgen05 BF16 coarse pass, FP32 fine pass"
                                 if args.precision == "bf16" else "plain FP32 path",
@@ -285,7 +287,8 @@ def run_ours(args, world, rank, local):
                      "peak_source": peak_src,
                      "traffic": (NCU_CROSS_B16["read"] + NCU_CROSS_B16["write"] * B / NCU_CROSS_B16["batch"])
                      if args.precision == "fp32" else
-                     ((NCU_TC_B256["read"] + NCU_TC_B256["write"]) if B == NCU_TC_B256["batch"] else None),
+                     ((NCU_TC_B256["read"] + NCU_TC_B256["write"])
+                      if B == NCU_TC_B256["batch"] and args.workload == CONFIG else None),
                      "traffic_note": "ncu dram read+write of a 16-particle launch, write scaled to the batch"
                      if args.precision == "fp32" else
                      "ncu dram read+write of one full-size launch at batch 256 (one-pass metrics); "
@@ -428,6 +431,16 @@ def mstep_section(args, ds, model, bundle, worker, dev_batch, local):
     timed("nyquist_projector_from_map_ms", lambda: bn.set_fourier_transform_map(0, vol, ori))
     bn.close()
     return out
+
+
+def workload_text(name, bundle, model):
+    """One line naming the workload with its sizes."""
+    box = model["ori_size"]
+    grid = ("%d classes x %d psi" % (bundle.nr_classes, bundle.npsi) if int(model.get("ref_dim", 3) or 3) == 2
+            else "HEALPix %d directions x %d psi, %d class%s" % (bundle.ndir, bundle.npsi, bundle.nr_classes,
+                                                                 "" if bundle.nr_classes == 1 else "es"))
+    return ("%s: box%d E-step, iteration-1 sizes (current %d px, coarse %d px), %s, %d translations, "
+            "oversampling 1" % (name, box, model["current_size"], model["coarse_size"], grid, bundle.ntrans))
 
 
 def measured_peaks():

@@ -36,6 +36,13 @@ struct Half {
     __host__ __device__ long long size() const { return (long long)Z * Y * X; }
     __host__ __device__ int rowp() const { return 2 * X; }  // padded real row (in-place transforms)
     __device__ void at(long long n, int &k, int &i, int &j) const {
+        if (n <= 0x7fffffffLL) {  // 32-bit divisions (several times cheaper than 64-bit)
+            const unsigned u = (unsigned)n, t = u / (unsigned)X;
+            j = (int)(u - t * (unsigned)X);
+            i = (int)(t % (unsigned)Y);
+            k = (int)(t / (unsigned)Y);
+            return;
+        }
         j = (int)(n % X);
         const long long t = n / X;
         i = (int)(t % Y);
@@ -58,6 +65,21 @@ template <class R> __device__ __forceinline__ typename Cx<R>::T cmake(double a, 
 template <> __device__ __forceinline__ double2 cmake<double>(double a, double b) { return make_double2(a, b); }
 template <> __device__ __forceinline__ float2 cmake<float>(double a, double b) {
     return make_float2((float)a, (float)b);
+}
+
+// n -> (z, y, x) of a [.][B][A] array, 32-bit divisions when n fits
+__device__ __forceinline__ void decode3(long long n, int A, int B, int &z, int &y, int &x) {
+    if (n <= 0x7fffffffLL) {
+        const unsigned u = (unsigned)n, t = u / (unsigned)A;
+        x = (int)(u - t * (unsigned)A);
+        y = (int)(t % (unsigned)B);
+        z = (int)(t / (unsigned)B);
+        return;
+    }
+    x = (int)(n % A);
+    const long long t = n / A;
+    y = (int)(t % B);
+    z = (int)(t / B);
 }
 
 __host__ __device__ __forceinline__ int d_round(double x) { return (x > 0) ? (int)(x + 0.5) : (int)(x - 0.5); }
@@ -131,9 +153,10 @@ __global__ void k_ssnr(const double *weight, VolGeom g, int max_r2, const int *i
     const long long nvox = (long long)g.zdim * g.ydim * g.xdim;
     for (long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x; n < nvox;
          n += (long long)gridDim.x * blockDim.x) {
-        const int j = (int)(n % g.xdim);
-        const long long t = n / g.xdim;
-        const int i = g.yinit + (int)(t % g.ydim), k = g.zinit + (int)(t / g.ydim);
+        int k, i, j;
+        decode3(n, g.xdim, g.ydim, k, i, j);
+        i += g.yinit;
+        k += g.zinit;
         const int r2 = k * k + i * i + j * j;
         if (r2 >= max_r2) continue;
         const int ires = iround[r2];
@@ -280,9 +303,8 @@ __global__ void k_blob(R *M, Half h, const double *tab, double sampling, double 
     const long long total = (long long)h.Z * h.Y * h.N;
     for (long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x; n < total;
          n += (long long)gridDim.x * blockDim.x) {
-        const int j = (int)(n % h.N);
-        const long long t = n / h.N;
-        const int i = (int)(t % h.Y), k = (int)(t / h.Y);
+        int k, i, j;
+        decode3(n, h.N, h.Y, k, i, j);
         const int kp = (h.dim == 3) ? ((k < padh) ? k : k - h.N) : 0;
         const int ip = (i < padh) ? i : i - h.N, jp = (j < padh) ? j : j - h.N;
         const double rval = sqrt((double)(kp * kp + ip * ip + jp * jp)) / ori_pad;
@@ -322,9 +344,8 @@ __global__ void k_crop_bg(const R *M, int No, int rowp, int ori, int dim, double
     double sum = 0., sbg = 0.;
     for (long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x; n < total;
          n += (long long)gridDim.x * blockDim.x) {
-        const int x = (int)(n % ori);
-        const long long t = n / ori;
-        const int y = (int)(t % ori), z = (int)(t / ori);
+        int z, y, x;
+        decode3(n, ori, ori, z, y, x);
         const int zo = dim == 3 ? z + off : 0;
         const double v = (double)M[((long long)zo * No + (y + off)) * rowp + (x + off)] / normfft;
         vol[n] = v;
@@ -367,9 +388,8 @@ __global__ void k_mask_gridcorr(double *vol, int ori, int dim, RealTab tab, cons
     const double avg = bg[1] / bg[0];
     for (long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x; n < total;
          n += (long long)gridDim.x * blockDim.x) {
-        const int x = (int)(n % ori);
-        const long long t = n / ori;
-        const int y = (int)(t % ori), z = (int)(t / ori);
+        int z, y, x;
+        decode3(n, ori, ori, z, y, x);
         const int k = dim == 3 ? z - h : 0, i = y - h, j = x - h;
         const int r2 = k * k + i * i + j * j;
         const double rc = tab.rc[r2];
@@ -388,9 +408,8 @@ __global__ void k_pad_map(const double *vol, int ori, int dim, int No, int rowp,
     const long long total = (long long)(dim == 3 ? No : 1) * No * rowp;
     for (long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x; n < total;
          n += (long long)gridDim.x * blockDim.x) {
-        const int x = (int)(n % rowp);
-        const long long t = n / rowp;
-        const int y = (int)(t % No), z = (int)(t / No);
+        int z, y, x;
+        decode3(n, rowp, No, z, y, x);
         const int k = dim == 3 ? z - ho : 0, i = y - ho, j = x - ho;
         double v = 0.;
         if (x < No && k >= -h && k < ori - h && i >= -h && i < ori - h && j >= -h && j < ori - h) {
