@@ -51,6 +51,7 @@ struct ParticleState {
     float eps;                      // weights below eps cannot reach the threshold
     float xs;                       // coarse diff2 - min beyond which the weights of all
                                     // poses together stay below 1e-10 of the weight sum
+    float po_min;                   // smallest normalised offset prior of the particle
 };
 
 // Fine-pass job: one (particle, significant coarse orientation).

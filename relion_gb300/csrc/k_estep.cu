@@ -127,20 +127,40 @@ __global__ void k_pdf_offset(const double *__restrict__ pdat, const double *__re
     extern __shared__ double vals[];  // [KP][T]
     const int p = blockIdx.x;
     const double *pd = pdat + (size_t)p * 8;
-    const double norm = 2. * 3.14159265358979323846 * sqrt(s2) * sqrt(s2);
     const int KT = KP * T;
-    double acc = 0.;
+    // The Gaussian's normalisation and any common factor cancel in the
+    // normalisation by the mean below, so the exponent is taken relative to
+    // its maximum over the particle's (class, translation) pairs, in FP32
+    // (FP64 exponentials are slow on this GPU; the values are stored in FP32).
+    double tmax = -DBL_MAX;
+    const double neg_inv_2s2 = 1. / (-2. * s2);
     for (int i = threadIdx.x; i < KT; i += blockDim.x) {
         const int kc = i / T, t = i - kc * T;
         // 2D classification: the offset prior is the class's (:7829-7833)
         const double prx = class_prior ? class_prior[2 * kc] : pd[2];
         const double pry = class_prior ? class_prior[2 * kc + 1] : pd[3];
         const double ox = pd[0] + tx[t], oy = pd[1] + ty[t];
-        double td = 0.;
-        td += (ox - prx) * (ox - prx) / (-2. * s2);
-        td += (oy - pry) * (oy - pry) / (-2. * s2);
-        td *= pixel * pixel;
-        const double v = (s2 < 0.0001) ? ((td > 0.) ? 0. : 1.) : exp(td) / norm;
+        // (x^2 + y^2) / (-2 s2) pixel^2, with one reciprocal per block
+        const double td = ((ox - prx) * (ox - prx) + (oy - pry) * (oy - pry)) * neg_inv_2s2 * (pixel * pixel);
+        vals[i] = td;
+        tmax = fmax(tmax, td);
+    }
+    __shared__ double s_tmax;
+    {
+        for (int o = 16; o > 0; o >>= 1) tmax = fmax(tmax, __shfl_xor_sync(0xffffffffu, tmax, o));
+        if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = tmax;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double m = -DBL_MAX;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = fmax(m, sh[w]);
+            s_tmax = m;
+        }
+        __syncthreads();
+    }
+    double acc = 0.;
+    for (int i = threadIdx.x; i < KT; i += blockDim.x) {
+        const double td = vals[i];
+        const double v = (s2 < 0.0001) ? ((td > 0.) ? 0. : 1.) : (double)expf((float)(td - s_tmax));
         vals[i] = v;
         acc += v;
     }
@@ -149,8 +169,9 @@ __global__ void k_pdf_offset(const double *__restrict__ pdat, const double *__re
     if (threadIdx.x == 0) mean = tot / (double)KT;
     __syncthreads();
     float vmax = 0.f, vmin = FLT_MAX;
+    const double inv_mean = mean > 0. ? 1. / mean : 1.;
     for (int i = threadIdx.x; i < KT; i += blockDim.x) {
-        const float v = (float)(mean > 0. ? vals[i] / mean : vals[i]);
+        const float v = (float)(vals[i] * inv_mean);
         out[(size_t)p * KT + i] = v;
         vmax = fmaxf(vmax, v);
         vmin = fminf(vmin, v);
@@ -178,6 +199,7 @@ __global__ void k_pdf_offset(const double *__restrict__ pdat, const double *__re
         if (vmin > 0.f && vmax < FLT_MAX && isfinite(log_rt_orient))
             xs = (float)(log_rt_orient + log((double)vmax / (double)vmin) + 1.0);
         ps[p].xs = xs;
+        ps[p].po_min = vmin;
     }
 }
 
@@ -291,7 +313,7 @@ k_weights_cand(const float *__restrict__ vals, int R, int T, const float *__rest
                float *__restrict__ cand_w, unsigned int *__restrict__ cand_cnt, int cap,
                float *__restrict__ dense_out, const unsigned int *__restrict__ rowmin, int KP, int rpc,
                const unsigned int *__restrict__ segmask) {
-    extern __shared__ float s_po[];  // pdf_offset rows of the particle [KP][T]
+    extern __shared__ float s_po[];  // pdf_offset rows of the classes of this block's orientations
     __shared__ double sh[32];
     __shared__ float s_eps;
     const int p = blockIdx.y;
@@ -299,15 +321,11 @@ k_weights_cand(const float *__restrict__ vals, int R, int T, const float *__rest
     if (r0 >= R) return;
     const int r1 = min(r0 + kWRowsPerBlock, R);
     const long long RT = (long long)R * T;
-    for (int t = threadIdx.x; t < KP * T; t += blockDim.x) s_po[t] = pdf_off[(size_t)p * KP * T + t];
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        float m = FLT_MAX;
-        for (int t = threadIdx.x; t < KP * T; t += 32) m = fminf(m, s_po[t]);
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) m = fminf(m, __shfl_xor_sync(0xffffffffu, m, o));
-        if (threadIdx.x == 0) s_eps = (float)((1.0 - fraction) * (double)pdf_orient_min * (double)m / (double)RT);
-    }
+    const int c0 = KP > 1 ? r0 / rpc : 0, c1 = KP > 1 ? (r1 - 1) / rpc : 0;
+    for (int t = threadIdx.x; t < (c1 - c0 + 1) * T; t += blockDim.x)
+        s_po[t] = pdf_off[((size_t)p * KP + c0) * T + t];
+    if (threadIdx.x == 0)
+        s_eps = (float)((1.0 - fraction) * (double)pdf_orient_min * (double)ps[p].po_min / (double)RT);
     __syncthreads();
     const float eps_lo = s_eps;
     const float mn = ord2f(ps[p].min_coarse);
@@ -351,7 +369,7 @@ k_weights_cand(const float *__restrict__ vals, int R, int T, const float *__rest
             const int r = rb + __ffs(rows_left) - 1;
             rows_left &= rows_left - 1u;
             const float pr = pdf_orient[r];
-            const float *po_r = s_po + (KP > 1 ? (r / rpc) * T : 0);
+            const float *po_r = s_po + (KP > 1 ? (r / rpc - c0) * T : 0);
             const float *row = rows + (size_t)r * T;
             // segments of the row the coarse pass stored (sparse writes); the
             // others lie beyond the skip distance and are not read
@@ -1692,7 +1710,9 @@ cudaError_t launch_weights_cand(const float *vals, int n, int R, int T, const fl
                                 const unsigned int *rowmin, int KP, int rpc, const unsigned int *segmask,
                                 cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    const size_t smem = (size_t)KP * T * sizeof(float);
+    // the classes a block of kWRowsPerBlock orientations can touch
+    const int ncls = KP > 1 ? std::min(KP, (kWRowsPerBlock - 1) / std::max(rpc, 1) + 2) : 1;
+    const size_t smem = (size_t)ncls * T * sizeof(float);
     if (smem > 48 * 1024) return cudaErrorInvalidValue;
     dim3 grid((unsigned)((R + kWRowsPerBlock - 1) / kWRowsPerBlock), n);
     k_weights_cand<<<grid, kWThreads, smem, st>>>(vals, R, T, pdf_orient, pdf_orient_min, pdf_off, fraction, ps,
