@@ -250,6 +250,7 @@ struct gbr_worker {
     int fine_mode = 0;  // 0: by significant density, 1: always dense, 2: always sparse
     int coarse_rows = 0;  // 0: skip far coarse rows by their minimum (tensor-core pass), 1: read all rows
     int cand_cap_max = 1 << 16;  // candidate-list entries per particle (GBR_CAND_CAP)
+    int cand_buf = 0;            // block-local candidate buffer used (GBR_CAND_BUF; 0 = all of it)
     int last_dense = 0;
     DevBuf<float> Wt, Wp, Zt, CM, S2P, fnrm;
     DevBuf<float2> G;
@@ -711,7 +712,7 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
     GBR_CUDA(launch_weights_cand(w->vals.p, n, R, T, b->pdf_orient.p, b->pdf_orient_min, w->pdf_off.p,
                                  d.adaptive_fraction, w->ps.p, w->cand_idx.p, w->cand_w.p, w->cand_cnt.p, cap,
                                  dense_w, use_rowmin ? w->rowmin.p : nullptr, b->KP, (int)(b->ND * b->NP), segmask,
-                                 st));
+                                 w->cand_buf, st));
     w->launches += 1;
     GBR_CUDA(w->h_ccnt.reserve(n));
     GBR_CUDA(w->h_totals.reserve(2));
@@ -1047,6 +1048,8 @@ int gbr_worker_create(gbr_bundle *b, gbr_worker **out) {
     if (nm && std::strcmp(nm, "full") == 0) w->coarse_rows = 1;
     const char *cc = std::getenv("GBR_CAND_CAP");
     if (cc && std::atoi(cc) > 0) w->cand_cap_max = std::atoi(cc);
+    const char *cb = std::getenv("GBR_CAND_BUF");
+    if (cb && std::atoi(cb) > 0) w->cand_buf = std::atoi(cb);
     *out = w.release();
     return GBR_OK;
 }

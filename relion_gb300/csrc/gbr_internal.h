@@ -173,7 +173,7 @@ cudaError_t launch_weights_cand(const float *vals, int n, int R, int T, const fl
                                 const float *pdf_off, double fraction, ParticleState *ps, unsigned int *cand_idx,
                                 float *cand_w, unsigned int *cand_cnt, int cap, float *dense_out,
                                 const unsigned int *rowmin, int KP, int rpc, const unsigned int *segmask,
-                                cudaStream_t st);
+                                int cand_buf, cudaStream_t st);
 cudaError_t launch_cand_masks(const unsigned int *cand_idx, const float *cand_w, const unsigned int *cand_cnt,
                               int cap, int n, int R, int T, int W, const ParticleState *ps, unsigned int *mask,
                               int *cnt, cudaStream_t st);

@@ -213,6 +213,7 @@ constexpr int kWThreads = 512;
 // k_weights_cand: orientation rows per block and loads in flight per lane
 constexpr int kWRowsPerBlock = 2048;
 constexpr int kWUnroll = 4;
+constexpr int kCandBuf = 2048;  // block-local candidate buffer of k_weights_cand
 
 __global__ void __launch_bounds__(kWThreads)
 k_weights(float *__restrict__ vals, const long long *__restrict__ seg, int coarse, int T,
@@ -312,13 +313,22 @@ k_weights_cand(const float *__restrict__ vals, int R, int T, const float *__rest
                ParticleState *__restrict__ ps, unsigned int *__restrict__ cand_idx,
                float *__restrict__ cand_w, unsigned int *__restrict__ cand_cnt, int cap,
                float *__restrict__ dense_out, const unsigned int *__restrict__ rowmin, int KP, int rpc,
-               const unsigned int *__restrict__ segmask) {
+               const unsigned int *__restrict__ segmask, int cbuf) {
     extern __shared__ float s_po[];  // pdf_offset rows of the classes of this block's orientations
     __shared__ double sh[32];
     __shared__ float s_eps;
+    // candidates are gathered in a block-local buffer (shared-memory atomics)
+    // and appended to the particle's list with one global atomic per flush
+    __shared__ unsigned int s_ci[kCandBuf];
+    __shared__ float s_cw[kCandBuf];
+    __shared__ unsigned int s_n, s_cut;  // slots taken; first slot of an overflowing warp
     const int p = blockIdx.y;
     const int r0 = blockIdx.x * kWRowsPerBlock;
     if (r0 >= R) return;
+    if (threadIdx.x == 0) {
+        s_n = 0u;
+        s_cut = (unsigned)cbuf;
+    }
     const int r1 = min(r0 + kWRowsPerBlock, R);
     const long long RT = (long long)R * T;
     const int c0 = KP > 1 ? r0 / rpc : 0, c1 = KP > 1 ? (r1 - 1) / rpc : 0;
@@ -415,14 +425,29 @@ k_weights_cand(const float *__restrict__ vals, int R, int T, const float *__rest
                     if (!is_c) acc_f += w;
                     if (ball) {  // warp-uniform: the FP64 add runs only where candidates are
                         if (is_c) acc_c += (double)w;
+                        const unsigned int nb = (unsigned)__popc(ball);
                         unsigned int base = 0;
-                        if (lane == 0) base = atomicAdd(&cand_cnt[p], (unsigned)__popc(ball));
+                        if (lane == 0) base = atomicAdd(&s_n, nb);
                         base = __shfl_sync(0xffffffffu, base, 0);
-                        if (is_c) {
-                            const unsigned int pos = base + __popc(ball & ((1u << lane) - 1u));
-                            if (pos < (unsigned)cap) {
-                                ci[pos] = (unsigned int)((long long)r * T + t);
-                                cw[pos] = w;
+                        if (base + nb <= (unsigned)cbuf) {
+                            if (is_c) {
+                                const unsigned int pos = base + __popc(ball & ((1u << lane) - 1u));
+                                s_ci[pos] = (unsigned int)((long long)r * T + t);
+                                s_cw[pos] = w;
+                            }
+                        } else {
+                            // buffer full: straight to the particle's list (the
+                            // buffer keeps the slots below the first overflow)
+                            if (lane == 0) atomicMin(&s_cut, base);
+                            unsigned int gb = 0;
+                            if (lane == 0) gb = atomicAdd(&cand_cnt[p], nb);
+                            gb = __shfl_sync(0xffffffffu, gb, 0);
+                            if (is_c) {
+                                const unsigned int pos = gb + __popc(ball & ((1u << lane) - 1u));
+                                if (pos < (unsigned)cap) {
+                                    ci[pos] = (unsigned int)((long long)r * T + t);
+                                    cw[pos] = w;
+                                }
                             }
                         }
                     }
@@ -432,6 +457,20 @@ k_weights_cand(const float *__restrict__ vals, int R, int T, const float *__rest
     }
     }
 
+    __syncthreads();
+    {
+        __shared__ unsigned int s_gbase;
+        const unsigned int nbuf = min(s_n, s_cut);
+        if (threadIdx.x == 0) s_gbase = nbuf ? atomicAdd(&cand_cnt[p], nbuf) : 0u;
+        __syncthreads();
+        for (unsigned int i = threadIdx.x; i < nbuf; i += blockDim.x) {
+            const unsigned int pos = s_gbase + i;
+            if (pos < (unsigned)cap) {
+                ci[pos] = s_ci[i];
+                cw[pos] = s_cw[i];
+            }
+        }
+    }
     const double tot = block_sum(acc_c + (double)acc_f, sh);
     if (threadIdx.x == 0) atomicAdd(&ps[p].sum_coarse, tot);
 }
@@ -1708,16 +1747,16 @@ cudaError_t launch_weights_cand(const float *vals, int n, int R, int T, const fl
                                 const float *pdf_off, double fraction, ParticleState *ps, unsigned int *cand_idx,
                                 float *cand_w, unsigned int *cand_cnt, int cap, float *dense_out,
                                 const unsigned int *rowmin, int KP, int rpc, const unsigned int *segmask,
-                                cudaStream_t st) {
+                                int cand_buf, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
     // the classes a block of kWRowsPerBlock orientations can touch
     const int ncls = KP > 1 ? std::min(KP, (kWRowsPerBlock - 1) / std::max(rpc, 1) + 2) : 1;
     const size_t smem = (size_t)ncls * T * sizeof(float);
-    if (smem > 48 * 1024) return cudaErrorInvalidValue;
+    if (smem > 30 * 1024) return cudaErrorInvalidValue;  // with the 17 KB static candidate buffer
     dim3 grid((unsigned)((R + kWRowsPerBlock - 1) / kWRowsPerBlock), n);
     k_weights_cand<<<grid, kWThreads, smem, st>>>(vals, R, T, pdf_orient, pdf_orient_min, pdf_off, fraction, ps,
                                                   cand_idx, cand_w, cand_cnt, cap, dense_out, rowmin, KP, rpc,
-                                                  segmask);
+                                                  segmask, (cand_buf > 0 && cand_buf < kCandBuf) ? cand_buf : kCandBuf);
     return cudaGetLastError();
 }
 

@@ -13,7 +13,8 @@ of the dense coarse weights must be identical too.  Without the debug
 read-back the coarse pass also stores only the row segments near the running
 minimum (sparse diff2 writes); the same bounds hold then, also when the
 candidate lists overflow and the significance search reruns on the full
-(partly unwritten) array (GBR_CAND_CAP small).
+(partly unwritten) array (GBR_CAND_CAP small), and when the block-local
+candidate buffers overflow into direct appends (GBR_CAND_BUF small).
 """
 import numpy as np
 import pytest
@@ -21,10 +22,13 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def _run(monkeypatch, ds, model, batch, mode=None, debug=True, cand_cap=None):
+def _run(monkeypatch, ds, model, batch, mode=None, debug=True, cand_cap=None, cand_buf=None):
     from relion_gb300.estep import MlDeviceBundle, MlOptimiserCuda
     monkeypatch.delenv("GBR_COARSE_WEIGHTS", raising=False)
     monkeypatch.delenv("GBR_CAND_CAP", raising=False)
+    monkeypatch.delenv("GBR_CAND_BUF", raising=False)
+    if cand_buf:
+        monkeypatch.setenv("GBR_CAND_BUF", str(cand_buf))
     if mode:
         monkeypatch.setenv("GBR_COARSE_WEIGHTS", mode)
     if cand_cap:
@@ -73,8 +77,8 @@ def test_row_skip_matches_full_coarse_pass(monkeypatch, seed):
     assert _rel(gn, gf) <= 1e-6
 
 
-@pytest.mark.parametrize("cand_cap", [None, 16])
-def test_sparse_writes_match_full_coarse_pass(monkeypatch, cand_cap):
+@pytest.mark.parametrize("cand_cap,cand_buf", [(None, None), (16, None), (None, 8)])
+def test_sparse_writes_match_full_coarse_pass(monkeypatch, cand_cap, cand_buf):
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
@@ -84,7 +88,7 @@ def test_sparse_writes_match_full_coarse_pass(monkeypatch, cand_cap):
     model = ds.model(precision=1)
     batch = ds.particles(0, 12)
     rf, _, wf, df, gf = _run(monkeypatch, ds, model, batch, mode="full", debug=False)
-    rn, _, wn, dn, gn = _run(monkeypatch, ds, model, batch, debug=False, cand_cap=cand_cap)
+    rn, _, wn, dn, gn = _run(monkeypatch, ds, model, batch, debug=False, cand_cap=cand_cap, cand_buf=cand_buf)
     assert np.array_equal(rf["nr_sign"], rn["nr_sign"])
     assert np.array_equal(rf["best_ihidden_over"], rn["best_ihidden_over"])
     for k in ("coarse_sum_weight", "coarse_significant_weight", "pmax", "dLL", "fine_sum_weight"):
