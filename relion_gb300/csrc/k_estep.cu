@@ -313,7 +313,7 @@ k_weights_cand(const float *__restrict__ vals, int R, int T, const float *__rest
                ParticleState *__restrict__ ps, unsigned int *__restrict__ cand_idx,
                float *__restrict__ cand_w, unsigned int *__restrict__ cand_cnt, int cap,
                float *__restrict__ dense_out, const unsigned int *__restrict__ rowmin, int KP, int rpc,
-               const unsigned int *__restrict__ segmask, int cbuf) {
+               const unsigned int *__restrict__ segmask, int cbuf, int rpb) {
     extern __shared__ float s_po[];  // pdf_offset rows of the classes of this block's orientations
     __shared__ double sh[32];
     __shared__ float s_eps;
@@ -323,13 +323,13 @@ k_weights_cand(const float *__restrict__ vals, int R, int T, const float *__rest
     __shared__ float s_cw[kCandBuf];
     __shared__ unsigned int s_n, s_cut;  // slots taken; first slot of an overflowing warp
     const int p = blockIdx.y;
-    const int r0 = blockIdx.x * kWRowsPerBlock;
+    const int r0 = blockIdx.x * rpb;
     if (r0 >= R) return;
     if (threadIdx.x == 0) {
         s_n = 0u;
         s_cut = (unsigned)cbuf;
     }
-    const int r1 = min(r0 + kWRowsPerBlock, R);
+    const int r1 = min(r0 + rpb, R);
     const long long RT = (long long)R * T;
     const int c0 = KP > 1 ? r0 / rpc : 0, c1 = KP > 1 ? (r1 - 1) / rpc : 0;
     for (int t = threadIdx.x; t < (c1 - c0 + 1) * T; t += blockDim.x)
@@ -1749,14 +1749,18 @@ cudaError_t launch_weights_cand(const float *vals, int n, int R, int T, const fl
                                 const unsigned int *rowmin, int KP, int rpc, const unsigned int *segmask,
                                 int cand_buf, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    // the classes a block of kWRowsPerBlock orientations can touch
-    const int ncls = KP > 1 ? std::min(KP, (kWRowsPerBlock - 1) / std::max(rpc, 1) + 2) : 1;
+    // orientations per block: up to kWRowsPerBlock, fewer when the prior rows
+    // of the classes a block touches ((rpb - 1) / rpc + 2 of them) would not
+    // fit next to the 17 KB static candidate buffer
+    const int max_cls = (int)((30 * 1024) / (sizeof(float) * (size_t)std::max(T, 1)));
+    if (KP > 1 && max_cls < 2) return cudaErrorInvalidValue;
+    const int rpb = KP > 1 ? std::max(1, std::min(kWRowsPerBlock, (max_cls - 1) * std::max(rpc, 1))) : kWRowsPerBlock;
+    const int ncls = KP > 1 ? std::min(KP, (rpb - 1) / std::max(rpc, 1) + 2) : 1;
     const size_t smem = (size_t)ncls * T * sizeof(float);
-    if (smem > 30 * 1024) return cudaErrorInvalidValue;  // with the 17 KB static candidate buffer
-    dim3 grid((unsigned)((R + kWRowsPerBlock - 1) / kWRowsPerBlock), n);
+    dim3 grid((unsigned)((R + rpb - 1) / rpb), n);
     k_weights_cand<<<grid, kWThreads, smem, st>>>(vals, R, T, pdf_orient, pdf_orient_min, pdf_off, fraction, ps,
                                                   cand_idx, cand_w, cand_cnt, cap, dense_out, rowmin, KP, rpc,
-                                                  segmask, (cand_buf > 0 && cand_buf < kCandBuf) ? cand_buf : kCandBuf);
+                                                  segmask, (cand_buf > 0 && cand_buf < kCandBuf) ? cand_buf : kCandBuf, rpb);
     return cudaGetLastError();
 }
 
