@@ -217,6 +217,19 @@ int gbr_prepare_images(gbr_worker *w, const gbr_image_batch *in, void *fimg, voi
  * plus accDoExpectationOneParticle). */
 int gbr_expect_images(gbr_worker *w, const gbr_image_batch *in, gbr_particle_result *res);
 
+/* Stage a host image batch (page-locked memory, for the copy to run
+ * asynchronously) into the next of the worker's two device slots.  The copy
+ * runs on a copy stream of the worker's own; it is issued by the next
+ * gbr_expect_images once that call has queued its own small input copies
+ * (the host-to-device copy engine serves copies in the order they were
+ * queued, across streams), so it uploads during that call's E-step.  A later
+ * gbr_expect_images with the same batch (same images pointer and count)
+ * prepares it from the slot instead of copying it then.  Staging batch i + 1
+ * before gbr_expect_images(batch i) overlaps its upload with batch i's
+ * compute (the pinned-memory reader feeding the batch queue).  The caller
+ * keeps the host batch unchanged until it is used. */
+int gbr_stage_images(gbr_worker *w, const gbr_image_batch *in);
+
 /* ---- data formats (MRC image stacks, STAR metadata) --------------------- */
 
 /* MRC header fields (src/rwMRC.h): sizes, data mode, extended-header bytes,
@@ -346,8 +359,10 @@ int gbr_bundle_reset_wsum(gbr_bundle *b);
  * (CUDA events on the worker's stream: prep, norm, cross term, coarse
  * weights, significance + job list, fine diff2, fine weights, weighted sums,
  * backprojection, read-back), then the input copies of each batch (device
- * time before the first stage), the host finalisation of the results, and
- * for gbr_expect_images the image upload and the image preparation. */
+ * time before the first stage), the host finalisation of the results, for
+ * gbr_expect_images the image upload and the image preparation, and for
+ * batches staged by gbr_stage_images the staging copy (copy stream) and the
+ * compute stream's wait for it at the start of the call. */
 int gbr_worker_stage_times(const gbr_worker *w, double *ms, int64_t n, int64_t *n_written);
 
 /* Number of CUDA kernels this worker has launched (all batches so far). */

@@ -110,6 +110,7 @@ EXPORTS = {
     "gbr_reconstruct": (C.c_int, [P, I64, P, P, P]),
     "gbr_projector_from_map": (C.c_int, [P, I64, P, I64, C.c_int, I64, P]),
     "gbr_fsc": (C.c_int, [P, P, P, P]),
+    "gbr_stage_images": (C.c_int, [P, P]),
     "gbr_recon_set_precision": (C.c_int, [P, C.c_int]),
     "gbr_projector_download": (C.c_int, [P, I64, P, P]),
     "gbr_wsum_download": (C.c_int, [P, C.POINTER(Wsum)]),

@@ -195,10 +195,28 @@ struct gbr_worker {
     gbr_bundle *b = nullptr;
     cudaStream_t st = nullptr;
     cudaEvent_t ev[ST_N + 1] = {};
-    double stage_ms[ST_N + 4] = {};  // device stages, input copies, host finalisation,
+    double stage_ms[ST_N + 6] = {};  // device stages, input copies, host finalisation,
                                      // image upload and image preparation
     cudaEvent_t ev_in = nullptr;     // start of the batch's input copies
     cudaEvent_t ev_img[3] = {};      // image upload start, preparation start, end
+    // image batches staged ahead (gbr_stage_images): two device slots filled on
+    // a copy stream while the compute stream works on the previous batch
+    struct StageSlot {
+        DevBuf<float> img;
+        cudaEvent_t start = nullptr, ready = nullptr, consumed = nullptr;
+        const float *host = nullptr;
+        int64_t n = 0;
+        size_t npx = 0;
+        long long seq = 0;  // staging order: matching slots are used oldest first
+        bool valid = false;    // holds (or will hold) the images of (host, n)
+        bool pending = false;  // requested, copy not yet issued
+        bool used = false;     // consumed has been recorded at least once
+    } stage[2];
+    int stage_next = 0;
+    long long stage_seq = 0;
+    cudaEvent_t ev_call = nullptr;  // start of a gbr_expect_images call using a staged slot
+    cudaEvent_t ev_inputs = nullptr;  // the call's host-to-device input copies are done
+    cudaStream_t st_copy = nullptr;
     int debug = 0;
     int cap = 0;  // particles the batch buffers hold
     long long launches = 0;  // kernels launched by this worker
@@ -236,6 +254,7 @@ struct gbr_worker {
     // the host copies of device-resident metadata
     PinnedBuf<unsigned int> h_ccnt;
     PinnedBuf<long long> h_totals, h_segf;
+    PinnedBuf<int> h_tcflag;  // tensor-core pipeline error flag of the call
     PinnedBuf<ParticleState> h_ps;
     PinnedBuf<double> h_shell, h_pacc, h_pdat, h_power;
     // image preparation: inputs, scratch, FFT plan and the prepared batch
@@ -479,6 +498,21 @@ int ensure_capacity(gbr_worker *w, int n) {
     return GBR_OK;
 }
 
+// Worker buffers for a call of n_all particles: the tables of the bundle and
+// the batch capacity (particles per pass, bounded by the device budget).
+int call_capacity(gbr_worker *w, int n_all) {
+    gbr_bundle *b = w->b;
+    int s = build_tables(b);
+    if (s) return s;
+    // device bytes per particle of the coarse pass (the dense fine pass is
+    // only chosen when its array also fits, see run_batch)
+    const long long per_part = (long long)b->R * b->T * 4 + (1LL << 20);
+    const long long mem_cap = (b->budget ? (long long)b->budget : (48LL << 30)) / 2;
+    int cap = (int)std::max<long long>(1, std::min<long long>(1024, mem_cap / per_part));
+    if (w->debug) cap = n_all;  // debug read-back covers the whole call
+    return ensure_capacity(w, std::min(cap, n_all));
+}
+
 int threshold_search(gbr_worker *w, int n, float *vals, const long long *seg, long long max_len, int coarse,
                      const long long *seg_end = nullptr, long long n_total = 0) {
     gbr_bundle *b = w->b;
@@ -717,6 +751,7 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
     GBR_CUDA(w->h_ccnt.reserve(n));
     GBR_CUDA(w->h_totals.reserve(2));
     GBR_CUDA(w->h_segf.reserve(n + 1));
+    GBR_CUDA(w->h_tcflag.reserve(1));
     // Speculative: the candidate lists are taken as complete and the host
     // checks their counts at the job-list read-back; if one overflowed
     // (flat posterior), the threshold search reruns on the full weight array.
@@ -742,14 +777,13 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
         GBR_CUDA(cudaMemcpyAsync(w->h_totals.p, w->scan_tmp.p + 2 * nbj, sizeof(long long) * 2, cudaMemcpyDeviceToHost,
                                  st));
         GBR_CUDA(cudaMemcpyAsync(w->h_segf.p, w->seg_f.p, sizeof(long long) * (n + 1), cudaMemcpyDeviceToHost, st));
+        const bool tc_check = attempt == 0 && d.precision == GBR_PREC_BF16;
+        if (tc_check) GBR_CUDA(tc_error_flag_async(w->h_tcflag.p, st));
         GBR_CUDA(cudaStreamSynchronize(st));
         w->launches += 3;
+        if (tc_check && w->h_tcflag.p[0])
+            return fail(GBR_ERR_CUDA, "tensor-core pipeline timed out waiting for its MMAs");
         if (attempt > 0) break;
-        if (d.precision == GBR_PREC_BF16) {
-            int flag = 0;
-            GBR_CUDA(tc_error_flag(&flag, 1));
-            if (flag) return fail(GBR_ERR_CUDA, "tensor-core pipeline timed out waiting for its MMAs");
-        }
         unsigned int cmax = 0;
         for (int p = 0; p < n; ++p) cmax = std::max(cmax, w->h_ccnt.p[p]);
         if (cmax <= (unsigned int)cap) break;
@@ -1039,6 +1073,14 @@ int gbr_worker_create(gbr_bundle *b, gbr_worker **out) {
     for (int i = 0; i <= ST_N; ++i) GBR_CUDA(cudaEventCreate(&w->ev[i]));
     GBR_CUDA(cudaEventCreate(&w->ev_in));
     for (auto &ev : w->ev_img) GBR_CUDA(cudaEventCreate(&ev));
+    GBR_CUDA(cudaStreamCreateWithFlags(&w->st_copy, cudaStreamNonBlocking));
+    for (auto &sl : w->stage) {
+        GBR_CUDA(cudaEventCreate(&sl.start));
+        GBR_CUDA(cudaEventCreate(&sl.ready));
+        GBR_CUDA(cudaEventCreateWithFlags(&sl.consumed, cudaEventDisableTiming));
+    }
+    GBR_CUDA(cudaEventCreate(&w->ev_call));
+    GBR_CUDA(cudaEventCreateWithFlags(&w->ev_inputs, cudaEventDisableTiming));
     const char *dbg = std::getenv("GBR_DEBUG_FETCH");
     w->debug = dbg && dbg[0] == '1';
     const char *fm = std::getenv("GBR_FINE_MODE");
@@ -1068,25 +1110,24 @@ int gbr_expect_batch(gbr_worker *w, const gbr_particle_batch *batch, gbr_particl
         return fail(GBR_ERR_INVALID, "null particle array");
     gbr_bundle *b = w->b;
     GBR_CUDA(cudaSetDevice(b->device));
-    int s = build_tables(b);
-    if (s) return s;
-    // device bytes per particle of the coarse pass (the dense fine pass is
-    // only chosen when its array also fits, see run_batch)
-    const long long per_part = (long long)b->R * b->T * 4 + (1LL << 20);
-    const long long mem_cap = (b->budget ? (long long)b->budget : (48LL << 30)) / 2;
-    int cap = (int)std::max<long long>(1, std::min<long long>(1024, mem_cap / per_part));
     const int n_all = (int)batch->n;
-    if (w->debug) cap = n_all;  // debug read-back covers the whole call
-    s = ensure_capacity(w, std::min(cap, n_all));
+    int s = call_capacity(w, n_all);
     if (s) return s;
     const size_t full = (size_t)b->full_npix;
     const cudaMemcpyKind kind = batch->device_resident ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     for (int p0 = 0; p0 < n_all; p0 += w->cap) {
         const int n = std::min(w->cap, n_all - p0);
         GBR_CUDA(cudaEventRecord(w->ev_in, w->st));
-        GBR_CUDA(cudaMemcpyAsync(w->X.p, batch->fimg + 2 * full * p0, sizeof(float2) * full * n, kind, w->st));
-        GBR_CUDA(cudaMemcpyAsync(w->Xn.p, batch->fimg_nomask + 2 * full * p0, sizeof(float2) * full * n, kind, w->st));
-        GBR_CUDA(cudaMemcpyAsync(w->C.p, batch->fctf + full * p0, sizeof(float) * full * n, kind, w->st));
+        // inputs already in the worker's buffers (gbr_expect_images prepares
+        // into them) are not copied
+        const float *xs = batch->fimg + 2 * full * p0, *xns = batch->fimg_nomask + 2 * full * p0;
+        const float *cs = batch->fctf + full * p0;
+        if ((const void *)xs != (const void *)w->X.p)
+            GBR_CUDA(cudaMemcpyAsync(w->X.p, xs, sizeof(float2) * full * n, kind, w->st));
+        if ((const void *)xns != (const void *)w->Xn.p)
+            GBR_CUDA(cudaMemcpyAsync(w->Xn.p, xns, sizeof(float2) * full * n, kind, w->st));
+        if ((const void *)cs != (const void *)w->C.p)
+            GBR_CUDA(cudaMemcpyAsync(w->C.p, cs, sizeof(float) * full * n, kind, w->st));
         GBR_CUDA(w->h_pdat.reserve((size_t)n * 8));
         GBR_CUDA(w->h_power.reserve((size_t)n * b->nshell));
         double *pdat = w->h_pdat.p, *power = w->h_power.p;
@@ -1134,7 +1175,7 @@ namespace {
 
 // getFourierTransformsAndCtfs for a whole batch into the given device arrays.
 int prepare_images(gbr_worker *w, const gbr_image_batch *in, float2 *fimg, float2 *fnm, float *fctf, double *power,
-                   double *xi2, double *off_out) {
+                   double *xi2, double *off_out, const float *staged_images = nullptr) {
     gbr_bundle *b = w->b;
     if (!b->have_optics) return fail(GBR_ERR_STATE, "optics not set (gbr_bundle_set_optics)");
     const int n = (int)in->n, N = (int)b->d.ori_size, cur = b->cur;
@@ -1155,9 +1196,13 @@ int prepare_images(gbr_worker *w, const gbr_image_batch *in, float2 *fimg, float
     GBR_CUDA(w->pi_factor.reserve(n));
     // rounded old offsets (selfROUND, src/ml_optimiser.cpp:6054) and norm factors on the host
     std::vector<double> off((size_t)n * 2), nc(n);
-    const cudaMemcpyKind kind = in->device_resident ? cudaMemcpyDeviceToHost : cudaMemcpyHostToHost;
-    GBR_CUDA(cudaMemcpy(off.data(), in->old_offset, sizeof(double) * 2 * n, kind));
-    GBR_CUDA(cudaMemcpy(nc.data(), in->norm_correction, sizeof(double) * n, kind));
+    if (in->device_resident) {
+        GBR_CUDA(cudaMemcpy(off.data(), in->old_offset, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost));
+        GBR_CUDA(cudaMemcpy(nc.data(), in->norm_correction, sizeof(double) * n, cudaMemcpyDeviceToHost));
+    } else {
+        std::memcpy(off.data(), in->old_offset, sizeof(double) * 2 * n);
+        std::memcpy(nc.data(), in->norm_correction, sizeof(double) * n);
+    }
     std::vector<int> sh((size_t)n * 2);
     std::vector<float> fac(n);
     std::vector<double> offr((size_t)n * 2);
@@ -1174,9 +1219,9 @@ int prepare_images(gbr_worker *w, const gbr_image_batch *in, float2 *fimg, float
     GBR_CUDA(cudaMemcpyAsync(off_out, offr.data(), sizeof(double) * offr.size(), cudaMemcpyHostToDevice, st));
     GBR_CUDA(cudaMemcpyAsync(w->pi_ctf.p, in->ctf, sizeof(double) * 6 * n,
                              in->device_resident ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st));
-    const float *imgs = in->images;
+    const float *imgs = staged_images ? staged_images : in->images;
     GBR_CUDA(cudaEventRecord(w->ev_img[0], st));
-    if (!in->device_resident) {
+    if (!in->device_resident && !staged_images) {
         GBR_CUDA(w->pi_images.reserve(npx));
         GBR_CUDA(cudaMemcpyAsync(w->pi_images.p, in->images, sizeof(float) * npx, cudaMemcpyHostToDevice, st));
         imgs = w->pi_images.p;
@@ -1239,6 +1284,66 @@ int gbr_prepare_images(gbr_worker *w, const gbr_image_batch *in, void *fimg, voi
     return GBR_OK;
 }
 
+namespace {
+
+// Issue a requested staging copy on the copy stream, after the previous
+// batch in the slot has been read.
+int issue_stage(gbr_worker *w, gbr_worker::StageSlot &sl, cudaEvent_t after = nullptr) {
+    if (sl.used) GBR_CUDA(cudaStreamWaitEvent(w->st_copy, sl.consumed, 0));
+    if (after) GBR_CUDA(cudaStreamWaitEvent(w->st_copy, after, 0));
+    GBR_CUDA(cudaEventRecord(sl.start, w->st_copy));
+    GBR_CUDA(cudaMemcpyAsync(sl.img.p, sl.host, sizeof(float) * sl.npx, cudaMemcpyHostToDevice, w->st_copy));
+    GBR_CUDA(cudaEventRecord(sl.ready, w->st_copy));
+    sl.pending = false;
+    return GBR_OK;
+}
+
+// Issue every requested staging copy, oldest first, to start once the event
+// `after` (recorded on the compute stream behind the current call's host-to-
+// device copies) has completed.  The device's host-to-device copies run one
+// after the other across streams: a batch copy issued ahead of the call's
+// small input copies held them, and the E-step behind them, for the whole
+// upload (measured).
+int pump_stages(gbr_worker *w, cudaEvent_t after) {
+    gbr_worker::StageSlot *a = &w->stage[0], *b = &w->stage[1];
+    if (b->seq < a->seq) std::swap(a, b);
+    for (gbr_worker::StageSlot *sl : {a, b})
+        if (sl->pending) {
+            int s = issue_stage(w, *sl, after);
+            if (s) return s;
+        }
+    return GBR_OK;
+}
+
+}  // namespace
+
+int gbr_stage_images(gbr_worker *w, const gbr_image_batch *in) {
+    if (!w || !in || !in->images) return fail(GBR_ERR_INVALID, "null argument");
+    if (in->device_resident) return fail(GBR_ERR_INVALID, "gbr_stage_images: host batches only");
+    gbr_bundle *b = w->b;
+    GBR_CUDA(cudaSetDevice(b->device));
+    const int N = (int)b->d.ori_size;
+    if (in->n <= 0 || in->n > 4096) return fail(GBR_ERR_INVALID, "gbr_stage_images: 1 to 4096 images");
+    gbr_worker::StageSlot &sl = w->stage[w->stage_next];
+    w->stage_next ^= 1;
+    const size_t npx = (size_t)in->n * N * N;
+    if (sl.img.n < npx) {
+        // a larger slot: the previous copy into it and its readers must be done
+        GBR_CUDA(cudaStreamSynchronize(w->st_copy));
+        GBR_CUDA(cudaStreamSynchronize(w->st));
+        GBR_CUDA(sl.img.reserve(npx));
+    }
+    // the copy itself is issued by the next gbr_expect_images once that call's
+    // own input copies are queued (or at once if it asks for this batch)
+    sl.host = in->images;
+    sl.n = in->n;
+    sl.npx = npx;
+    sl.seq = ++w->stage_seq;
+    sl.valid = true;
+    sl.pending = true;
+    return GBR_OK;
+}
+
 int gbr_expect_images(gbr_worker *w, const gbr_image_batch *in, gbr_particle_result *res) {
     if (!w || !in || !res) return fail(GBR_ERR_INVALID, "null argument");
     if (in->n == 0) return GBR_OK;
@@ -1246,33 +1351,74 @@ int gbr_expect_images(gbr_worker *w, const gbr_image_batch *in, gbr_particle_res
     gbr_bundle *b = w->b;
     GBR_CUDA(cudaSetDevice(b->device));
     const size_t n = (size_t)in->n, cur = (size_t)b->cur, X = cur / 2 + 1, half = (size_t)b->nshell;
-    GBR_CUDA(w->pi_fimg.reserve(n * cur * X));
-    GBR_CUDA(w->pi_fnm.reserve(n * cur * X));
-    GBR_CUDA(w->pi_fctf.reserve(n * cur * X));
+    int s = call_capacity(w, (int)n);
+    if (s) return s;
+    // a call that fits one pass prepares straight into the E-step's input
+    // buffers (no device-to-device copies of the Fourier images)
+    const bool in_place = (size_t)w->cap >= n;
+    if (!in_place) {
+        GBR_CUDA(w->pi_fimg.reserve(n * cur * X));
+        GBR_CUDA(w->pi_fnm.reserve(n * cur * X));
+        GBR_CUDA(w->pi_fctf.reserve(n * cur * X));
+    }
+    float2 *fimg = in_place ? w->X.p : w->pi_fimg.p, *fnm = in_place ? w->Xn.p : w->pi_fnm.p;
+    float *fctf = in_place ? w->C.p : w->pi_fctf.p;
     GBR_CUDA(w->pi_power.reserve(n * half));
     GBR_CUDA(w->pi_xi2.reserve(n));
     GBR_CUDA(w->pi_off.reserve(2 * n));
     GBR_CUDA(w->pi_prior.reserve(2 * n));
     GBR_CUDA(w->pi_norm.reserve(n));
     GBR_CUDA(w->pi_scale.reserve(n));
-    int s = prepare_images(w, in, w->pi_fimg.p, w->pi_fnm.p, w->pi_fctf.p, w->pi_power.p, w->pi_xi2.p, w->pi_off.p);
+    gbr_worker::StageSlot *slot = nullptr;
+    for (auto &sl : w->stage)
+        if (sl.valid && !in->device_resident && sl.host == in->images && sl.n == in->n &&
+            (!slot || sl.seq < slot->seq))
+            slot = &sl;
+    if (slot) {
+        if (slot->pending) {
+            int s = issue_stage(w, *slot);
+            if (s) return s;
+        }
+        GBR_CUDA(cudaEventRecord(w->ev_call, w->st));
+        GBR_CUDA(cudaStreamWaitEvent(w->st, slot->ready, 0));
+    }
+    s = prepare_images(w, in, fimg, fnm, fctf, w->pi_power.p, w->pi_xi2.p, w->pi_off.p, slot ? slot->img.p : nullptr);
     if (s) return s;
+    if (slot) {
+        // the preparation kernels have read the slot: it may be refilled
+        GBR_CUDA(cudaEventRecord(slot->consumed, w->st));
+        slot->valid = false;
+        slot->used = true;
+    }
     GBR_CUDA(cudaEventSynchronize(w->ev_img[2]));
     float t0 = 0.f, t1 = 0.f;
     cudaEventElapsedTime(&t0, w->ev_img[0], w->ev_img[1]);
     cudaEventElapsedTime(&t1, w->ev_img[1], w->ev_img[2]);
     w->stage_ms[ST_N + 2] += t0;
     w->stage_ms[ST_N + 3] += t1;
+    if (slot) {
+        // the preparation waited for the slot: both intervals have ended
+        float tc = 0.f, tw = 0.f;
+        cudaEventElapsedTime(&tc, slot->start, slot->ready);
+        cudaEventElapsedTime(&tw, w->ev_call, w->ev_img[0]);
+        w->stage_ms[ST_N + 4] += tc;
+        w->stage_ms[ST_N + 5] += tw;
+    }
     const cudaMemcpyKind kind = in->device_resident ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     GBR_CUDA(cudaMemcpyAsync(w->pi_prior.p, in->prior, sizeof(double) * 2 * n, kind, w->st));
     GBR_CUDA(cudaMemcpyAsync(w->pi_norm.p, in->norm_correction, sizeof(double) * n, kind, w->st));
     GBR_CUDA(cudaMemcpyAsync(w->pi_scale.p, in->scale, sizeof(double) * n, kind, w->st));
+    // batches staged for the next calls upload during this call's E-step,
+    // behind the call's own host-to-device copies
+    GBR_CUDA(cudaEventRecord(w->ev_inputs, w->st));
+    s = pump_stages(w, w->ev_inputs);
+    if (s) return s;
     gbr_particle_batch pb{};
     pb.n = in->n;
     pb.device_resident = 1;
-    pb.fimg = reinterpret_cast<const float *>(w->pi_fimg.p);
-    pb.fimg_nomask = reinterpret_cast<const float *>(w->pi_fnm.p);
-    pb.fctf = w->pi_fctf.p;
+    pb.fimg = reinterpret_cast<const float *>(fimg);
+    pb.fimg_nomask = reinterpret_cast<const float *>(fnm);
+    pb.fctf = fctf;
     pb.power_img = w->pi_power.p;
     pb.old_offset = w->pi_off.p;
     pb.prior = w->pi_prior.p;
@@ -1527,7 +1673,7 @@ int gbr_bundle_reset_wsum(gbr_bundle *b) {
 
 int gbr_worker_stage_times(const gbr_worker *w, double *ms, int64_t n, int64_t *n_written) {
     if (!w || !ms) return fail(GBR_ERR_INVALID, "null argument");
-    const int64_t m = std::min<int64_t>(n, ST_N + 4);
+    const int64_t m = std::min<int64_t>(n, ST_N + 6);
     for (int64_t i = 0; i < m; ++i) ms[i] = w->stage_ms[i];
     if (n_written) *n_written = m;
     return GBR_OK;
@@ -1558,6 +1704,15 @@ int gbr_worker_destroy(gbr_worker *w) {
     if (w->ev_in) cudaEventDestroy(w->ev_in);
     for (auto &ev : w->ev_img)
         if (ev) cudaEventDestroy(ev);
+    if (w->st_copy) cudaStreamSynchronize(w->st_copy);
+    if (w->ev_call) cudaEventDestroy(w->ev_call);
+    if (w->ev_inputs) cudaEventDestroy(w->ev_inputs);
+    for (auto &sl : w->stage) {
+        if (sl.start) cudaEventDestroy(sl.start);
+        if (sl.ready) cudaEventDestroy(sl.ready);
+        if (sl.consumed) cudaEventDestroy(sl.consumed);
+    }
+    if (w->st_copy) cudaStreamDestroy(w->st_copy);
     if (w->fft_plan >= 0) destroy_fft_plan(w->fft_plan);
     if (w->st) cudaStreamDestroy(w->st);
     delete w;

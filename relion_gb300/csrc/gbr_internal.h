@@ -111,6 +111,7 @@ cudaError_t launch_tc_diff2(const void *Ablk, void *Yblk, int M, int K2, const f
                             ParticleState *ps, unsigned int *rowmin, unsigned int *segmask, cudaStream_t st);
 // Read (and optionally clear) the tensor-core pipeline error flag.
 cudaError_t tc_error_flag(int *flag, int reset);
+cudaError_t tc_error_flag_async(int *host_flag, cudaStream_t st);
 
 // k_gemm.cu: C[m][n] = sum_k A[m][k] * Bop[n][k], FP32 SIMT.
 // Cross term + diff2 epilogue; output [p][M][T] relative to c_p, +inf where

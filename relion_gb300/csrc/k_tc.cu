@@ -708,6 +708,18 @@ cudaError_t launch_tc_norm(const void *Ablk, const float *w, int ldw, int M, int
     return cudaGetLastError();
 }
 
+// The same, queued on a stream: the flag is copied into page-locked host
+// memory (valid after the caller's next synchronisation) and cleared.  No
+// synchronous host-to-device copy: those wait behind any batch copy the
+// host-to-device engine is serving for another stream.
+cudaError_t tc_error_flag_async(int *host_flag, cudaStream_t st) {
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_tc_error);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(host_flag, p, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(p, 0, sizeof(int), st);
+    return e;
+}
+
 cudaError_t tc_error_flag(int *flag, int reset) {
     cudaError_t e = cudaMemcpyFromSymbol(flag, g_tc_error, sizeof(int));
     if (e == cudaSuccess && reset) {

@@ -287,6 +287,19 @@ class MlOptimiserCuda:
         check(self.lib.gbr_expect_images(self.h, C.byref(b), out.ctypes.data))
         return out
 
+    def stage_images(self, batch):
+        """Start the upload of a host image batch into the worker's next
+        staging slot (gbr_stage_images); a following do_expectation_images
+        with the same batch uses it.  The images must already be a
+        C-contiguous float32 array (ideally page-locked) that stays unchanged
+        until then."""
+        img = batch["images"]
+        if not (isinstance(img, np.ndarray) and img.dtype == np.float32 and img.flags.c_contiguous):
+            raise ValueError("stage_images needs C-contiguous float32 images (no temporary copy)")
+        keep = []
+        b = self._image_batch(batch, keep)
+        check(self.lib.gbr_stage_images(self.h, C.byref(b)))
+
     def debug_fetch(self, what, i):
         cap = self.bundle.nr_classes * self.bundle.ndir * self.bundle.npsi * self.bundle.ntrans * \
             self.bundle.nover_rot * self.bundle.nover_trans
@@ -320,7 +333,7 @@ class MlOptimiserCuda:
 
 STAGES = ["prep", "norm_gemm", "cross_gemm", "weights_coarse", "sig_jobs", "diff2_fine",
           "weights_fine", "wsum", "backproject", "readback", "inputs", "host_final",
-          "image_upload", "image_prep"]
+          "image_upload", "image_prep", "image_stage_copy", "image_stage_wait"]
 
 
 def measure_fp32_peak(device=0):

@@ -128,3 +128,33 @@ def test_expect_images_from_star_and_mrc(tmp_path):
     assert np.array_equal(r_file["best_ihidden_over"], r_mem["best_ihidden_over"])
     assert np.array_equal(r_file["nr_sign"], r_mem["nr_sign"])
     np.testing.assert_allclose(r_file["pmax"], r_mem["pmax"], rtol=1e-5)
+
+
+def test_staged_images_equal_direct():
+    # gbr_stage_images: batches copied ahead on the copy stream (two slots,
+    # reused) give the results of the direct calls
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from relion_gb300.estep import MlOptimiserCuda
+    ds, m, _ = _setup(seed=11, n=12, norm=False)
+    batches = []
+    for k in range(3):
+        bi = ds.particle_images(k * 4, 4)
+        bi["images"] = torch.from_numpy(np.ascontiguousarray(bi["images"], np.float32)).pin_memory().numpy()
+        batches.append(bi)
+    b = _bundle(ds, m)
+    w = MlOptimiserCuda(b)
+    direct = [w.do_expectation_images(bi) for bi in batches]
+    w.stage_images(batches[0])
+    staged = []
+    for k in range(3):
+        if k + 1 < 3:
+            w.stage_images(batches[k + 1])
+        staged.append(w.do_expectation_images(batches[k]))
+    w.close()
+    b.close()
+    for r1, r2 in zip(direct, staged):
+        assert np.array_equal(r1["best_ihidden_over"], r2["best_ihidden_over"])
+        assert np.array_equal(r1["nr_sign"], r2["nr_sign"])
+        np.testing.assert_allclose(r2["pmax"], r1["pmax"], rtol=1e-6)
