@@ -393,6 +393,56 @@ int gbr_significance_threshold_noalloc(const float *weights, int64_t n, int64_t 
                                        double adaptive_fraction, float *threshold,
                                        uint32_t *nr_significant, void *stream);
 
+/* ---- learned pose proposal ---------------------------------------------
+ * No counterpart in the reference (its coarse search is exhaustive): a small
+ * convolutional network that proposes the top-M coarse viewing directions of
+ * a particle, trained on the device by the library's own forward, backward
+ * and Adam kernels on views it generates from the bundle's current
+ * reference (coarse projection table, one row per coarse orientation, so the
+ * direction label is exact) with CTFs drawn from a pool and the model's noise.
+ * Features: whitened coarse power |X|^2 / sigma2 over the active coarse
+ * pixels in polar bins (nring rings x nangle angle bins over [0, pi)),
+ * log(1 + mean) - log 2.  Layers: conv 3x5 (1 -> c1, ReLU), conv 3x5
+ * (c1 -> c2, ReLU), both zero-padded along rings and circular along angles;
+ * mean over angles; linear to one logit per HEALPix direction; softmax.
+ * Parameters (float): W1 [c1][1][3][5], b1 [c1], W2 [c2][c1][3][5], b2 [c2],
+ * W3 [c2*nring][ndir], b3 [ndir]. */
+typedef struct gbr_posenet gbr_posenet;
+typedef struct {
+    int32_t nring;      /* rings 1..nring of the coarse image (<= coarse size / 2) */
+    int32_t nangle;     /* angle bins over [0, pi) */
+    int32_t c1, c2;     /* channels of the two convolutions */
+    int32_t max_batch;  /* particles or training views per launch */
+    int32_t reserved;
+    uint64_t seed;      /* weight initialisation and training views */
+} gbr_posenet_desc;
+
+/* The bundle must have its model arrays and projectors (the pose tables are
+ * built here if needed); the network keeps a pointer to it. */
+int gbr_posenet_create(gbr_bundle *b, const gbr_posenet_desc *d, gbr_posenet **out);
+int gbr_posenet_destroy(gbr_posenet *n);
+/* parameter count, features per particle (nring * nangle), directions, active coarse pixels */
+int gbr_posenet_sizes(const gbr_posenet *n, int64_t *nparams, int64_t *nfeat, int64_t *ndir, int64_t *npix);
+/* active coarse pixels: (x, y) pairs [npix][2] and noise weights 1 / (2 sigma2) [npix] */
+int gbr_posenet_pixels(const gbr_posenet *n, int32_t *xy, float *minv);
+int gbr_posenet_get_params(const gbr_posenet *n, float *out);
+int gbr_posenet_set_params(gbr_posenet *n, const float *in);
+/* features [count][nfeat] of prepared images fimg (host, complex float
+ * [count][current_size][current_size/2+1], the layout of gbr_particle_batch) */
+int gbr_posenet_features(gbr_posenet *n, const float *fimg, int64_t count, float *feat_out);
+/* mean loss and its gradient for given features [count][nfeat] and target
+ * distributions [count][ndir] (host; each target row sums to 1) */
+int gbr_posenet_loss_grad(gbr_posenet *n, const float *feat, const float *target, int64_t count, double *loss,
+                          float *grad_out);
+/* `steps` Adam steps (learning rate lr) on `batch` generated views each; CTFs
+ * drawn from ctf_pool (host, [n_pool][current_size][current_size/2+1], the
+ * fctf layout); *loss_out = mean loss over the last min(steps, 20) steps */
+int gbr_posenet_train(gbr_posenet *n, const float *ctf_pool, int64_t n_pool, int64_t steps, int64_t batch,
+                      double lr, double *loss_out);
+/* top-m directions [count][m] (most probable first) and their probabilities */
+int gbr_posenet_propose(gbr_posenet *n, const float *fimg, int64_t count, int64_t m, int32_t *dir_out,
+                        float *prob_out);
+
 /* delete MlOptimiserCuda / MlDeviceBundle (src/ml_optimiser.cpp:3840-3868). */
 int gbr_worker_destroy(gbr_worker *w);
 int gbr_bundle_destroy(gbr_bundle *b);

@@ -75,6 +75,11 @@ class ReconParams(C.Structure):
         [(n, F64) for n in ("tau2_fudge", "normalise")]
 
 
+class PosenetDesc(C.Structure):
+    _fields_ = [(n, C.c_int32) for n in ("nring", "nangle", "c1", "c2", "max_batch", "reserved")] + \
+        [("seed", C.c_uint64)]
+
+
 EXPORTS = {
     "gbr_last_error": (C.c_size_t, [C.c_char_p, C.c_size_t]),
     "gbr_version": (C.c_char_p, []),
@@ -111,6 +116,16 @@ EXPORTS = {
     "gbr_projector_from_map": (C.c_int, [P, I64, P, I64, C.c_int, I64, P]),
     "gbr_fsc": (C.c_int, [P, P, P, P]),
     "gbr_stage_images": (C.c_int, [P, P]),
+    "gbr_posenet_create": (C.c_int, [P, C.POINTER(PosenetDesc), C.POINTER(P)]),
+    "gbr_posenet_destroy": (C.c_int, [P]),
+    "gbr_posenet_sizes": (C.c_int, [P, P, P, P, P]),
+    "gbr_posenet_pixels": (C.c_int, [P, P, P]),
+    "gbr_posenet_get_params": (C.c_int, [P, P]),
+    "gbr_posenet_set_params": (C.c_int, [P, P]),
+    "gbr_posenet_features": (C.c_int, [P, P, I64, P]),
+    "gbr_posenet_loss_grad": (C.c_int, [P, P, P, I64, P, P]),
+    "gbr_posenet_train": (C.c_int, [P, P, I64, I64, I64, F64, P]),
+    "gbr_posenet_propose": (C.c_int, [P, P, I64, I64, P, P]),
     "gbr_recon_set_precision": (C.c_int, [P, C.c_int]),
     "gbr_projector_download": (C.c_int, [P, I64, P, P]),
     "gbr_wsum_download": (C.c_int, [P, C.POINTER(Wsum)]),

@@ -1,6 +1,6 @@
 """Build libgbrelion (the sm_103a CUDA E-step) in-tree with nvcc.
 
-The four translation units are compiled in parallel and linked into
+The translation units are compiled in parallel and linked into
 relion_gb300/_build/libgbrelion.so.  Host code is compiled with
 -ffp-contract=off so that the pose enumeration is bit-identical to the
 reference's double-precision arithmetic.
@@ -14,7 +14,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libgbrelion.so")
-SOURCES = ["k_project.cu", "k_gemm.cu", "k_estep.cu", "estep.cu", "k_noalloc.cu", "k_tc.cu", "k_prepimg.cu", "k_recon.cu", "io.cpp"]
+SOURCES = ["k_project.cu", "k_gemm.cu", "k_estep.cu", "estep.cu", "k_noalloc.cu", "k_tc.cu", "k_prepimg.cu", "k_recon.cu",
+           "k_posenet.cu", "io.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -1727,4 +1727,274 @@ int gbr_bundle_destroy(gbr_bundle *b) {
     return GBR_OK;
 }
 
+// ---- learned pose proposal (k_posenet.cu) --------------------------------
+struct gbr_posenet {
+    gbr_bundle *b = nullptr;
+    gbr::PnDims d;  // d.B = batch capacity
+    int nbins = 0;
+    uint64_t seed = 0;
+    long long t = 0;  // Adam steps taken
+    cudaStream_t st = nullptr;
+    DevBuf<float> params, grad, m, v;
+    DevBuf<int> bin;
+    DevBuf<float> inv_cnt;
+    DevBuf<float> pw, feat, a1, a2, h, logits, dl, d1, d2, loss, target, ctf_pool, prob;
+    DevBuf<int> label, idx;
+    DevBuf<float2> fimg;
+    ~gbr_posenet() {
+        if (st) cudaStreamDestroy(st);
+    }
+};
+
+namespace {
+
+uint64_t host_mix64(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+// features of count prepared images (host) into n->feat (device), count <= d.B
+int pn_features_dev(gbr_posenet *n, const float *fimg, int count) {
+    gbr_bundle *b = n->b;
+    const size_t full = (size_t)b->full_npix;
+    GBR_CUDA(cudaMemcpyAsync(n->fimg.p, fimg, sizeof(float2) * full * count, cudaMemcpyHostToDevice, n->st));
+    GBR_CUDA(gbr::pn_power(n->fimg.p, (int)full, b->pc.p, b->nc, b->minv_c.p, count, n->pw.p, n->st));
+    GBR_CUDA(gbr::pn_bin(n->pw.p, b->nc, n->bin.p, n->inv_cnt.p, n->nbins, count, n->feat.p, n->st));
+    return GBR_OK;
+}
+
+}  // namespace
+
+int gbr_posenet_create(gbr_bundle *b, const gbr_posenet_desc *desc, gbr_posenet **out) {
+    if (!b || !desc || !out) return fail(GBR_ERR_INVALID, "null argument");
+    GBR_CUDA(cudaSetDevice(b->device));
+    int s = build_tables(b);
+    if (s) return s;
+    if (desc->nring < 1 || desc->nring > b->crs / 2 || desc->nangle < 5 || desc->nangle > 256 || desc->c1 < 1 ||
+        desc->c1 > 256 || desc->c2 < 1 || desc->c2 > 256 || desc->max_batch < 1 || desc->max_batch > 65536)
+        return fail(GBR_ERR_INVALID, "gbr_posenet_create: invalid sizes (nring <= coarse size / 2, nangle >= 5)");
+    if ((size_t)desc->nring * desc->nangle * sizeof(float) > 48 * 1024 || b->ND > 8192)
+        return fail(GBR_ERR_UNSUPPORTED, "gbr_posenet_create: nring x nangle <= 12288 bins, <= 8192 directions");
+    std::unique_ptr<gbr_posenet> n(new gbr_posenet);
+    n->b = b;
+    n->seed = desc->seed;
+    gbr::PnDims &d = n->d;
+    d.B = desc->max_batch;
+    d.H = desc->nring;
+    d.W = desc->nangle;
+    d.C1 = desc->c1;
+    d.C2 = desc->c2;
+    d.ND = (int)b->ND;
+    const long long F = (long long)d.C2 * d.H;
+    d.o_w1 = 0;
+    d.o_b1 = d.o_w1 + (long long)d.C1 * 15;
+    d.o_w2 = d.o_b1 + d.C1;
+    d.o_b2 = d.o_w2 + (long long)d.C2 * d.C1 * 15;
+    d.o_w3 = d.o_b2 + d.C2;
+    d.o_b3 = d.o_w3 + F * d.ND;
+    d.nparams = d.o_b3 + d.ND;
+    n->nbins = d.H * d.W;
+    // polar bin of every active coarse pixel: ring = shell, angle of (x, y) modulo pi
+    const double kPi = 3.14159265358979323846;
+    std::vector<int> bin(b->nc, -1);
+    std::vector<int> cnt(n->nbins, 0);
+    for (int j = 0; j < b->nc; ++j) {
+        const PixelRef &pr = b->pc_h[j];
+        if (pr.shell < 1 || pr.shell > d.H) continue;
+        const double a = std::atan2((double)pr.y, (double)pr.x) + 0.5 * kPi;  // [0, pi]
+        int t = (int)std::floor(a / kPi * d.W);
+        if (t >= d.W) t -= d.W;
+        if (t < 0) t = 0;
+        bin[j] = (pr.shell - 1) * d.W + t;
+        cnt[bin[j]] += 1;
+    }
+    std::vector<float> inv(n->nbins);
+    for (int k = 0; k < n->nbins; ++k) inv[k] = cnt[k] ? 1.f / (float)cnt[k] : 0.f;
+    GBR_CUDA(n->bin.upload(bin.data(), bin.size()));
+    GBR_CUDA(n->inv_cnt.upload(inv.data(), inv.size()));
+    // He-uniform initial weights, zero biases
+    std::vector<float> p(d.nparams, 0.f);
+    uint64_t z = host_mix64(desc->seed ^ 0x5EEDull);
+    auto fill = [&](long long off, long long count, double fan_in) {
+        const double a = std::sqrt(6.0 / fan_in);
+        for (long long i = 0; i < count; ++i) {
+            z = host_mix64(z);
+            p[off + i] = (float)(a * (2.0 * ((double)(z >> 11) * (1.0 / 9007199254740992.0)) - 1.0));
+        }
+    };
+    fill(d.o_w1, (long long)d.C1 * 15, 15.0);
+    fill(d.o_w2, (long long)d.C2 * d.C1 * 15, 15.0 * d.C1);
+    fill(d.o_w3, F * d.ND, (double)F);
+    GBR_CUDA(n->params.upload(p.data(), p.size()));
+    GBR_CUDA(n->grad.reserve(d.nparams));
+    GBR_CUDA(n->m.reserve(d.nparams));
+    GBR_CUDA(n->v.reserve(d.nparams));
+    GBR_CUDA(n->m.zero());
+    GBR_CUDA(n->v.zero());
+    const size_t B = (size_t)d.B;
+    GBR_CUDA(n->pw.reserve(B * b->nc));
+    GBR_CUDA(n->feat.reserve(B * n->nbins));
+    GBR_CUDA(n->a1.reserve(B * d.C1 * n->nbins));
+    GBR_CUDA(n->d1.reserve(B * d.C1 * n->nbins));
+    GBR_CUDA(n->a2.reserve(B * d.C2 * n->nbins));
+    GBR_CUDA(n->d2.reserve(B * d.C2 * n->nbins));
+    GBR_CUDA(n->h.reserve(B * F));
+    GBR_CUDA(n->logits.reserve(B * d.ND));
+    GBR_CUDA(n->dl.reserve(B * d.ND));
+    GBR_CUDA(n->target.reserve(B * d.ND));
+    GBR_CUDA(n->loss.reserve(B));
+    GBR_CUDA(n->label.reserve(B));
+    GBR_CUDA(n->fimg.reserve(B * b->full_npix));
+    GBR_CUDA(cudaStreamCreateWithFlags(&n->st, cudaStreamNonBlocking));
+    GBR_CUDA(cudaDeviceSynchronize());
+    *out = n.release();
+    return GBR_OK;
+}
+
+int gbr_posenet_destroy(gbr_posenet *n) {
+    if (!n) return GBR_OK;
+    cudaSetDevice(n->b->device);
+    if (n->st) cudaStreamSynchronize(n->st);
+    delete n;
+    return GBR_OK;
+}
+
+int gbr_posenet_sizes(const gbr_posenet *n, int64_t *nparams, int64_t *nfeat, int64_t *ndir, int64_t *npix) {
+    if (!n) return fail(GBR_ERR_INVALID, "null network");
+    if (nparams) *nparams = n->d.nparams;
+    if (nfeat) *nfeat = n->nbins;
+    if (ndir) *ndir = n->d.ND;
+    if (npix) *npix = n->b->nc;
+    return GBR_OK;
+}
+
+int gbr_posenet_pixels(const gbr_posenet *n, int32_t *xy, float *minv) {
+    if (!n || !xy || !minv) return fail(GBR_ERR_INVALID, "null argument");
+    const gbr_bundle *b = n->b;
+    for (int j = 0; j < b->nc; ++j) {
+        xy[2 * j] = b->pc_h[j].x;
+        xy[2 * j + 1] = b->pc_h[j].y;
+    }
+    GBR_CUDA(cudaSetDevice(b->device));
+    GBR_CUDA(cudaMemcpy(minv, b->minv_c.p, sizeof(float) * b->nc, cudaMemcpyDeviceToHost));
+    return GBR_OK;
+}
+
+int gbr_posenet_get_params(const gbr_posenet *n, float *out) {
+    if (!n || !out) return fail(GBR_ERR_INVALID, "null argument");
+    GBR_CUDA(cudaSetDevice(n->b->device));
+    GBR_CUDA(cudaStreamSynchronize(n->st));
+    GBR_CUDA(cudaMemcpy(out, n->params.p, sizeof(float) * n->d.nparams, cudaMemcpyDeviceToHost));
+    return GBR_OK;
+}
+
+int gbr_posenet_set_params(gbr_posenet *n, const float *in) {
+    if (!n || !in) return fail(GBR_ERR_INVALID, "null argument");
+    GBR_CUDA(cudaSetDevice(n->b->device));
+    GBR_CUDA(cudaStreamSynchronize(n->st));
+    GBR_CUDA(cudaMemcpy(n->params.p, in, sizeof(float) * n->d.nparams, cudaMemcpyHostToDevice));
+    return GBR_OK;
+}
+
+int gbr_posenet_features(gbr_posenet *n, const float *fimg, int64_t count, float *feat_out) {
+    if (!n || (count > 0 && (!fimg || !feat_out))) return fail(GBR_ERR_INVALID, "null argument");
+    GBR_CUDA(cudaSetDevice(n->b->device));
+    const size_t full = (size_t)n->b->full_npix;
+    for (int64_t c0 = 0; c0 < count; c0 += n->d.B) {
+        const int c = (int)std::min<int64_t>(n->d.B, count - c0);
+        int s = pn_features_dev(n, fimg + 2 * full * c0, c);
+        if (s) return s;
+        GBR_CUDA(cudaMemcpyAsync(feat_out + (size_t)n->nbins * c0, n->feat.p, sizeof(float) * n->nbins * c,
+                                 cudaMemcpyDeviceToHost, n->st));
+        GBR_CUDA(cudaStreamSynchronize(n->st));
+    }
+    return GBR_OK;
+}
+
+int gbr_posenet_loss_grad(gbr_posenet *n, const float *feat, const float *target, int64_t count, double *loss,
+                          float *grad_out) {
+    if (!n || !feat || !target || !loss || !grad_out) return fail(GBR_ERR_INVALID, "null argument");
+    if (count < 1 || count > n->d.B) return fail(GBR_ERR_INVALID, "gbr_posenet_loss_grad: 1 <= count <= max_batch");
+    GBR_CUDA(cudaSetDevice(n->b->device));
+    gbr::PnDims d = n->d;
+    d.B = (int)count;
+    GBR_CUDA(cudaMemcpyAsync(n->feat.p, feat, sizeof(float) * n->nbins * count, cudaMemcpyHostToDevice, n->st));
+    GBR_CUDA(cudaMemcpyAsync(n->target.p, target, sizeof(float) * d.ND * count, cudaMemcpyHostToDevice, n->st));
+    GBR_CUDA(gbr::pn_forward(d, n->params.p, n->feat.p, n->a1.p, n->a2.p, n->h.p, n->logits.p, n->st));
+    GBR_CUDA(gbr::pn_loss_backward(d, n->params.p, n->feat.p, n->a1.p, n->a2.p, n->h.p, n->logits.p, nullptr,
+                                   n->target.p, n->dl.p, n->loss.p, n->d2.p, n->d1.p, n->grad.p, n->st));
+    std::vector<float> ls(count);
+    GBR_CUDA(cudaMemcpyAsync(ls.data(), n->loss.p, sizeof(float) * count, cudaMemcpyDeviceToHost, n->st));
+    GBR_CUDA(cudaMemcpyAsync(grad_out, n->grad.p, sizeof(float) * d.nparams, cudaMemcpyDeviceToHost, n->st));
+    GBR_CUDA(cudaStreamSynchronize(n->st));
+    double sum = 0.;
+    for (float x : ls) sum += x;
+    *loss = sum / (double)count;
+    return GBR_OK;
+}
+
+int gbr_posenet_train(gbr_posenet *n, const float *ctf_pool, int64_t n_pool, int64_t steps, int64_t batch,
+                      double lr, double *loss_out) {
+    if (!n || !ctf_pool || n_pool < 1) return fail(GBR_ERR_INVALID, "null argument or empty CTF pool");
+    if (batch < 1 || batch > n->d.B) return fail(GBR_ERR_INVALID, "gbr_posenet_train: 1 <= batch <= max_batch");
+    if (steps < 0 || !(lr > 0.)) return fail(GBR_ERR_INVALID, "gbr_posenet_train: steps >= 0, lr > 0");
+    gbr_bundle *b = n->b;
+    GBR_CUDA(cudaSetDevice(b->device));
+    const size_t full = (size_t)b->full_npix;
+    GBR_CUDA(n->ctf_pool.reserve((size_t)n_pool * full));
+    GBR_CUDA(cudaMemcpyAsync(n->ctf_pool.p, ctf_pool, sizeof(float) * full * n_pool, cudaMemcpyHostToDevice, n->st));
+    gbr::PnDims d = n->d;
+    d.B = (int)batch;
+    std::vector<float> ls(batch);
+    double acc = 0.;
+    long long nacc = 0;
+    for (int64_t k = 0; k < steps; ++k) {
+        ++n->t;
+        const uint64_t sd = host_mix64(n->seed ^ host_mix64((uint64_t)n->t));
+        GBR_CUDA(gbr::pn_gen(b->proj_c.p, b->lda_c, b->pc.p, b->nc, b->minv_c.p, n->ctf_pool.p, (int)full,
+                             (int)n_pool, b->R, (int)b->NP, (int)b->ND, sd, d.B, n->pw.p, n->label.p, n->st));
+        GBR_CUDA(gbr::pn_bin(n->pw.p, b->nc, n->bin.p, n->inv_cnt.p, n->nbins, d.B, n->feat.p, n->st));
+        GBR_CUDA(gbr::pn_forward(d, n->params.p, n->feat.p, n->a1.p, n->a2.p, n->h.p, n->logits.p, n->st));
+        GBR_CUDA(gbr::pn_loss_backward(d, n->params.p, n->feat.p, n->a1.p, n->a2.p, n->h.p, n->logits.p,
+                                       n->label.p, nullptr, n->dl.p, n->loss.p, n->d2.p, n->d1.p, n->grad.p,
+                                       n->st));
+        GBR_CUDA(gbr::pn_adam(n->params.p, n->grad.p, n->m.p, n->v.p, d.nparams, (float)lr, (int)n->t, n->st));
+        if (k >= steps - 20) {
+            GBR_CUDA(cudaMemcpyAsync(ls.data(), n->loss.p, sizeof(float) * batch, cudaMemcpyDeviceToHost, n->st));
+            GBR_CUDA(cudaStreamSynchronize(n->st));
+            for (float x : ls) acc += x;
+            nacc += batch;
+        }
+    }
+    GBR_CUDA(cudaStreamSynchronize(n->st));
+    if (loss_out) *loss_out = nacc ? acc / (double)nacc : 0.;
+    return GBR_OK;
+}
+
+int gbr_posenet_propose(gbr_posenet *n, const float *fimg, int64_t count, int64_t m, int32_t *dir_out,
+                        float *prob_out) {
+    if (!n || (count > 0 && (!fimg || !dir_out || !prob_out))) return fail(GBR_ERR_INVALID, "null argument");
+    if (m < 1 || m > n->d.ND) return fail(GBR_ERR_INVALID, "gbr_posenet_propose: 1 <= m <= number of directions");
+    GBR_CUDA(cudaSetDevice(n->b->device));
+    const size_t full = (size_t)n->b->full_npix;
+    GBR_CUDA(n->idx.reserve((size_t)n->d.B * m));
+    GBR_CUDA(n->prob.reserve((size_t)n->d.B * m));
+    for (int64_t c0 = 0; c0 < count; c0 += n->d.B) {
+        const int c = (int)std::min<int64_t>(n->d.B, count - c0);
+        int s = pn_features_dev(n, fimg + 2 * full * c0, c);
+        if (s) return s;
+        gbr::PnDims d = n->d;
+        d.B = c;
+        GBR_CUDA(gbr::pn_forward(d, n->params.p, n->feat.p, n->a1.p, n->a2.p, n->h.p, n->logits.p, n->st));
+        GBR_CUDA(gbr::pn_topm(n->logits.p, d.ND, (int)m, c, n->idx.p, n->prob.p, n->st));
+        GBR_CUDA(cudaMemcpyAsync(dir_out + m * c0, n->idx.p, sizeof(int32_t) * m * c, cudaMemcpyDeviceToHost, n->st));
+        GBR_CUDA(cudaMemcpyAsync(prob_out + m * c0, n->prob.p, sizeof(float) * m * c, cudaMemcpyDeviceToHost, n->st));
+        GBR_CUDA(cudaStreamSynchronize(n->st));
+    }
+    return GBR_OK;
+}
+
+
 }  // extern "C"

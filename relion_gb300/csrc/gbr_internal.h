@@ -290,3 +290,27 @@ int recon_projector_from_map(ReconWork *w, const double *vol_host, int ori, int 
                              int do_gridding, int min_ires, float2 *proj, double *power_host);
 int recon_fsc(ReconWork *w, const double *m1, const double *m2, int ori, int dim, double *fsc_host);
 }  // namespace gbr
+
+// Pose-proposal network (k_posenet.cu).  Parameter offsets into one float
+// array; activations [B][C][H][W] with H rings and W angle bins.
+namespace gbr {
+struct PnDims {
+    int B = 0, H = 0, W = 0, C1 = 0, C2 = 0, ND = 0;
+    long long o_w1 = 0, o_b1 = 0, o_w2 = 0, o_b2 = 0, o_w3 = 0, o_b3 = 0, nparams = 0;
+};
+cudaError_t pn_gen(const float *proj, int lda, const PixelRef *pix, int npix, const float *minv,
+                   const float *ctf_pool, int full_npix, int n_pool, long long R, int NP, int ND, uint64_t seed,
+                   int B, float *v, int *label, cudaStream_t st);
+cudaError_t pn_power(const float2 *fimg, int full_npix, const PixelRef *pix, int npix, const float *minv, int B,
+                     float *v, cudaStream_t st);
+cudaError_t pn_bin(const float *v, int npix, const int *bin, const float *inv_cnt, int nbins, int B, float *feat,
+                   cudaStream_t st);
+cudaError_t pn_forward(const PnDims &d, const float *params, const float *feat, float *a1, float *a2, float *h,
+                       float *logits, cudaStream_t st);
+cudaError_t pn_loss_backward(const PnDims &d, const float *params, const float *feat, const float *a1,
+                             const float *a2, const float *h, const float *logits, const int *label,
+                             const float *target, float *dl, float *loss, float *d2, float *d1, float *grad,
+                             cudaStream_t st);
+cudaError_t pn_adam(float *p, const float *g, float *m, float *v, long long n, float lr, int t, cudaStream_t st);
+cudaError_t pn_topm(const float *logits, int N, int M, int B, int *idx, float *prob, cudaStream_t st);
+}  // namespace gbr

@@ -1,0 +1,432 @@
+// Pose-proposal network: a small convolutional classifier of the viewing
+// direction, trained and run by the kernels below (no library calls).
+//
+// Input features of a particle: its whitened coarse power |X_j|^2 / sigma2_j
+// over the active coarse pixels (the pixels the E-step scores), averaged in
+// polar bins (ring = the pixel's shell 1..H, angle = atan2(y, x) modulo pi in
+// W bins) and mapped to log(1 + mean) - log 2 (0 for pure noise, 0 in empty
+// bins).  Power removes the translation; an in-plane rotation becomes a
+// circular shift along the angle axis.
+//
+// Layers ([B][C][H][W] row-major, angle fastest):
+//   conv1  1 -> C1, 3 x 5 kernel (zero padding along rings, circular along
+//          angles), bias, ReLU
+//   conv2  C1 -> C2, same, ReLU
+//   pool   mean over angles  -> h [B][C2*H]   (invariant to in-plane rotation)
+//   linear h W3 + b3         -> logits [B][ND] (one per HEALPix direction)
+//   softmax cross entropy against a target distribution (one-hot labels of
+//   the synthetic training views, or E-step posteriors)
+// Parameters in one array: W1 [C1][1][3][5], b1 [C1], W2 [C2][C1][3][5],
+// b2 [C2], W3 [C2*H][ND], b3 [ND].
+//
+// Training views are projections of the current reference taken from the
+// coarse projection table (one row per coarse orientation, so the direction
+// label is exact), multiplied by the CTF of a particle drawn from a pool and
+// given complex Gaussian noise of the model's sigma2 per pixel.  Random
+// numbers: SplitMix64 (Steele, Lea, Flood 2014) of (seed, step, sample,
+// pixel), Box-Muller for the normals.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "gbr_internal.h"
+
+namespace gbr {
+namespace {
+
+constexpr int KH = 3, KW = 5;
+constexpr float kLn2 = 0.6931471805599453f;
+
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+// uniform in (0, 1]
+__device__ __forceinline__ float unit(uint64_t h) { return ((float)(h >> 40) + 1.f) * (1.f / 16777216.f); }
+
+// Training views: whitened power of CTF * P_r + noise at the active pixels.
+__global__ void k_pn_gen(const float *__restrict__ proj, int lda, const PixelRef *__restrict__ pix, int npix,
+                         const float *__restrict__ minv, const float *__restrict__ ctf_pool, int full_npix,
+                         int n_pool, long long R, int NP, int ND, uint64_t seed, float *__restrict__ v,
+                         int *__restrict__ label) {
+    const int b = blockIdx.x;
+    __shared__ long long s_r;
+    __shared__ int s_k;
+    if (threadIdx.x == 0) {
+        const uint64_t h = mix64(seed ^ mix64((uint64_t)b * 0x100000001B3ull));
+        s_r = (long long)(h % (uint64_t)R);
+        s_k = (int)(mix64(h) % (uint64_t)n_pool);
+        label[b] = (int)((s_r / NP) % ND);
+    }
+    __syncthreads();
+    const float *row = proj + (size_t)s_r * lda;
+    const float *ctf = ctf_pool + (size_t)s_k * full_npix;
+    for (int j = threadIdx.x; j < npix; j += blockDim.x) {
+        const float c = ctf[pix[j].full];
+        const float s2 = 0.5f / minv[j];  // minv = 1 / (2 sigma2)
+        const uint64_t h = mix64(seed ^ mix64(((uint64_t)b << 32) ^ (uint64_t)j ^ 0xA5A5A5A5ull));
+        const float u1 = unit(h), u2 = unit(mix64(h));
+        const float rad = sqrtf(-2.f * logf(u1) * 0.5f * s2);
+        float sn, cs;
+        sincospif(2.f * u2, &sn, &cs);
+        const float xr = c * row[2 * j] + rad * cs, xi = c * row[2 * j + 1] + rad * sn;
+        v[(size_t)b * npix + j] = (xr * xr + xi * xi) / s2;
+    }
+}
+
+// Whitened power of prepared particle images (fimg [B][full_npix] complex).
+__global__ void k_pn_power(const float2 *__restrict__ fimg, int full_npix, const PixelRef *__restrict__ pix,
+                           int npix, const float *__restrict__ minv, int B, float *__restrict__ v) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)B * npix) return;
+    const int b = (int)(i / npix), j = (int)(i % npix);
+    const float2 x = fimg[(size_t)b * full_npix + pix[j].full];
+    v[i] = (x.x * x.x + x.y * x.y) * 2.f * minv[j];
+}
+
+// Polar bins: one block per sample, shared-memory sums.
+__global__ void k_pn_bin(const float *__restrict__ v, int npix, const int *__restrict__ bin,
+                         const float *__restrict__ inv_cnt, int nbins, float *__restrict__ feat) {
+    extern __shared__ float acc[];
+    const int b = blockIdx.x;
+    for (int i = threadIdx.x; i < nbins; i += blockDim.x) acc[i] = 0.f;
+    __syncthreads();
+    for (int j = threadIdx.x; j < npix; j += blockDim.x) {
+        const int k = bin[j];
+        if (k >= 0) atomicAdd(&acc[k], v[(size_t)b * npix + j]);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nbins; i += blockDim.x)
+        feat[(size_t)b * nbins + i] = inv_cnt[i] > 0.f ? log1pf(acc[i] * inv_cnt[i]) - kLn2 : 0.f;
+}
+
+// out[b][co][y][x] = relu(bias[co] + sum W[co][ci][ky][kx] in[b][ci][y+ky-1][(x+kx-2) mod W])
+__global__ void k_pn_conv_fwd(const float *__restrict__ in, int Ci, const float *__restrict__ w,
+                              const float *__restrict__ bias, int Co, int H, int W, int B, float *__restrict__ out) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)B * Co * H * W) return;
+    const int x = (int)(i % W), y = (int)((i / W) % H), co = (int)((i / ((long long)W * H)) % Co);
+    const int b = (int)(i / ((long long)W * H * Co));
+    float s = bias[co];
+    for (int ci = 0; ci < Ci; ++ci) {
+        const float *src = in + ((size_t)b * Ci + ci) * H * W;
+        const float *wk = w + ((size_t)co * Ci + ci) * KH * KW;
+        for (int ky = 0; ky < KH; ++ky) {
+            const int yy = y + ky - 1;
+            if (yy < 0 || yy >= H) continue;
+            for (int kx = 0; kx < KW; ++kx) {
+                int xx = x + kx - 2;
+                xx += (xx < 0) ? W : 0;
+                xx -= (xx >= W) ? W : 0;
+                s += wk[ky * KW + kx] * src[yy * W + xx];
+            }
+        }
+    }
+    out[i] = s > 0.f ? s : 0.f;
+}
+
+// h[b][c*H + y] = mean over x of a[b][c][y][x]
+__global__ void k_pn_pool(const float *__restrict__ a, int C, int H, int W, int B, float *__restrict__ h) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)B * C * H) return;
+    const float *src = a + (size_t)i * W;
+    float s = 0.f;
+    for (int x = 0; x < W; ++x) s += src[x];
+    h[i] = s / (float)W;
+}
+
+// logits[b][n] = b3[n] + sum_f h[b][f] W3[f][n]
+__global__ void k_pn_linear(const float *__restrict__ h, int F, const float *__restrict__ w,
+                            const float *__restrict__ bias, int N, int B, float *__restrict__ out) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)B * N) return;
+    const int n = (int)(i % N), b = (int)(i / N);
+    const float *hb = h + (size_t)b * F;
+    float s = bias[n];
+    for (int f = 0; f < F; ++f) s += hb[f] * w[(size_t)f * N + n];
+    out[i] = s;
+}
+
+__device__ float block_reduce(float v, float *sh, bool is_max) {
+    for (int o = 16; o > 0; o >>= 1) {
+        const float u = __shfl_xor_sync(0xffffffffu, v, o);
+        v = is_max ? fmaxf(v, u) : v + u;
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    __syncthreads();
+    if (lane == 0) sh[wid] = v;
+    __syncthreads();
+    float r = is_max ? -3.4e38f : 0.f;
+    for (int k = 0; k < nw; ++k) r = is_max ? fmaxf(r, sh[k]) : r + sh[k];
+    return r;
+}
+
+// Softmax cross entropy, one block per sample.  Target: one-hot `label` if
+// given, else the distribution `target` [B][N].  dl = (softmax - t) / B.
+__global__ void k_pn_xent(const float *__restrict__ logits, int N, const int *__restrict__ label,
+                          const float *__restrict__ target, int B, float *__restrict__ dl, float *__restrict__ loss) {
+    __shared__ float sh[32];
+    const int b = blockIdx.x;
+    const float *l = logits + (size_t)b * N;
+    float m = -3.4e38f;
+    for (int n = threadIdx.x; n < N; n += blockDim.x) m = fmaxf(m, l[n]);
+    m = block_reduce(m, sh, true);
+    float se = 0.f;
+    for (int n = threadIdx.x; n < N; n += blockDim.x) se += expf(l[n] - m);
+    se = block_reduce(se, sh, false);
+    const float lse = m + logf(se);
+    float ls = 0.f;
+    for (int n = threadIdx.x; n < N; n += blockDim.x) {
+        const float t = label ? (n == label[b] ? 1.f : 0.f) : target[(size_t)b * N + n];
+        const float p = expf(l[n] - lse);
+        dl[(size_t)b * N + n] = (p - t) / (float)B;
+        ls += t * (lse - l[n]);
+    }
+    ls = block_reduce(ls, sh, false);
+    if (threadIdx.x == 0) loss[b] = ls;
+}
+
+// dW3[f][n] = sum_b h[b][f] dl[b][n]; row f = F holds db3[n] = sum_b dl[b][n]
+__global__ void k_pn_linear_bwd_w(const float *__restrict__ h, const float *__restrict__ dl, int F, int N, int B,
+                                  float *__restrict__ dw, float *__restrict__ db) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)(F + 1) * N) return;
+    const int n = (int)(i % N), f = (int)(i / N);
+    float s = 0.f;
+    if (f < F) {
+        for (int b = 0; b < B; ++b) s += h[(size_t)b * F + f] * dl[(size_t)b * N + n];
+        dw[(size_t)f * N + n] = s;
+    } else {
+        for (int b = 0; b < B; ++b) s += dl[(size_t)b * N + n];
+        db[n] = s;
+    }
+}
+
+// dh[b][f] = sum_n dl[b][n] W3[f][n]; through the mean pool and the ReLU of
+// a2: d2[b][c][y][x] = dh[b][c*H + y] / W * (a2 > 0)
+__global__ void k_pn_linear_bwd_x(const float *__restrict__ dl, const float *__restrict__ w, int F, int N, int B,
+                                  const float *__restrict__ a2, int W, float *__restrict__ d2) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)B * F) return;
+    const int f = (int)(i % F), b = (int)(i / F);
+    const float *dlb = dl + (size_t)b * N;
+    const float *wf = w + (size_t)f * N;
+    float s = 0.f;
+    for (int n = 0; n < N; ++n) s += dlb[n] * wf[n];
+    s /= (float)W;
+    const float *ab = a2 + (size_t)i * W;
+    float *db = d2 + (size_t)i * W;
+    for (int x = 0; x < W; ++x) db[x] = ab[x] > 0.f ? s : 0.f;
+}
+
+// Weight gradient of a convolution: one block per (co, ci, ky, kx), blocks
+// Co*Ci*KH*KW .. +Co hold the bias gradients.
+__global__ void k_pn_conv_bwd_w(const float *__restrict__ in, int Ci, const float *__restrict__ d, int Co, int H,
+                                int W, int B, float *__restrict__ dw, float *__restrict__ db) {
+    __shared__ float sh[32];
+    const int nw = Co * Ci * KH * KW;
+    const int k = blockIdx.x;
+    const long long tot = (long long)B * H * W;
+    float s = 0.f;
+    if (k < nw) {
+        const int kx = k % KW, ky = (k / KW) % KH, ci = (k / (KW * KH)) % Ci, co = k / (KW * KH * Ci);
+        for (long long e = threadIdx.x; e < tot; e += blockDim.x) {
+            const int x = (int)(e % W), y = (int)((e / W) % H), b = (int)(e / ((long long)W * H));
+            const int yy = y + ky - 1;
+            if (yy < 0 || yy >= H) continue;
+            int xx = x + kx - 2;
+            xx += (xx < 0) ? W : 0;
+            xx -= (xx >= W) ? W : 0;
+            s += d[(((size_t)b * Co + co) * H + y) * W + x] * in[(((size_t)b * Ci + ci) * H + yy) * W + xx];
+        }
+    } else {
+        const int co = k - nw;
+        for (long long e = threadIdx.x; e < tot; e += blockDim.x) {
+            const int x = (int)(e % W), y = (int)((e / W) % H), b = (int)(e / ((long long)W * H));
+            s += d[(((size_t)b * Co + co) * H + y) * W + x];
+        }
+    }
+    s = block_reduce(s, sh, false);
+    if (threadIdx.x == 0) {
+        if (k < nw)
+            dw[k] = s;
+        else
+            db[k - nw] = s;
+    }
+}
+
+// Input gradient of a convolution through the ReLU of its input a:
+// din[b][ci][y][x] = (a > 0) * sum d[b][co][y-ky+1][(x-kx+2) mod W] W[co][ci][ky][kx]
+__global__ void k_pn_conv_bwd_x(const float *__restrict__ d, int Co, const float *__restrict__ w, int Ci, int H,
+                                int W, int B, const float *__restrict__ a, float *__restrict__ din) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)B * Ci * H * W) return;
+    if (!(a[i] > 0.f)) {
+        din[i] = 0.f;
+        return;
+    }
+    const int x = (int)(i % W), y = (int)((i / W) % H), ci = (int)((i / ((long long)W * H)) % Ci);
+    const int b = (int)(i / ((long long)W * H * Ci));
+    float s = 0.f;
+    for (int co = 0; co < Co; ++co) {
+        const float *src = d + ((size_t)b * Co + co) * H * W;
+        const float *wk = w + ((size_t)co * Ci + ci) * KH * KW;
+        for (int ky = 0; ky < KH; ++ky) {
+            const int yy = y - ky + 1;
+            if (yy < 0 || yy >= H) continue;
+            for (int kx = 0; kx < KW; ++kx) {
+                int xx = x - kx + 2;
+                xx += (xx < 0) ? W : 0;
+                xx -= (xx >= W) ? W : 0;
+                s += wk[ky * KW + kx] * src[yy * W + xx];
+            }
+        }
+    }
+    din[i] = s;
+}
+
+// Adam (Kingma & Ba 2015) with bias corrections c1 = 1 - beta1^t, c2 = 1 - beta2^t.
+__global__ void k_pn_adam(float *__restrict__ p, const float *__restrict__ g, float *__restrict__ m,
+                          float *__restrict__ v, long long n, float lr, float b1, float b2, float eps, float c1,
+                          float c2) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.f - b1) * gi, vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+}
+
+// Top-M directions by logit and their softmax probabilities, one block per
+// sample (M passes of a block arg-max over a shared copy).
+__global__ void k_pn_topm(const float *__restrict__ logits, int N, int M, int *__restrict__ idx,
+                          float *__restrict__ prob) {
+    extern __shared__ float s_l[];
+    __shared__ float sh[32];
+    __shared__ float s_bv[32];
+    __shared__ int s_bi[32];
+    const int b = blockIdx.x;
+    const float *l = logits + (size_t)b * N;
+    float m = -3.4e38f;
+    for (int n = threadIdx.x; n < N; n += blockDim.x) {
+        s_l[n] = l[n];
+        m = fmaxf(m, l[n]);
+    }
+    m = block_reduce(m, sh, true);
+    float se = 0.f;
+    for (int n = threadIdx.x; n < N; n += blockDim.x) se += expf(s_l[n] - m);
+    se = block_reduce(se, sh, false);
+    const float lse = m + logf(se);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    for (int k = 0; k < M; ++k) {
+        float bv = -3.4e38f;
+        int bi = 0x7fffffff;
+        for (int n = threadIdx.x; n < N; n += blockDim.x)
+            if (s_l[n] > bv || (s_l[n] == bv && n < bi)) {
+                bv = s_l[n];
+                bi = n;
+            }
+        for (int o = 16; o > 0; o >>= 1) {
+            const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
+            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            if (ov > bv || (ov == bv && oi < bi)) {
+                bv = ov;
+                bi = oi;
+            }
+        }
+        if (lane == 0) {
+            s_bv[wid] = bv;
+            s_bi[wid] = bi;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            float v0 = s_bv[0];
+            int i0 = s_bi[0];
+            for (int q = 1; q < nw; ++q)
+                if (s_bv[q] > v0 || (s_bv[q] == v0 && s_bi[q] < i0)) {
+                    v0 = s_bv[q];
+                    i0 = s_bi[q];
+                }
+            if (i0 < 0 || i0 >= N) i0 = 0;  // every logit NaN
+            idx[(size_t)b * M + k] = i0;
+            prob[(size_t)b * M + k] = expf(v0 - lse);
+            s_l[i0] = -3.4e38f;
+        }
+        __syncthreads();
+    }
+}
+
+inline unsigned nblk(long long n, int t) { return (unsigned)((n + t - 1) / t); }
+
+}  // namespace
+
+cudaError_t pn_gen(const float *proj, int lda, const PixelRef *pix, int npix, const float *minv,
+                   const float *ctf_pool, int full_npix, int n_pool, long long R, int NP, int ND, uint64_t seed,
+                   int B, float *v, int *label, cudaStream_t st) {
+    k_pn_gen<<<B, 128, 0, st>>>(proj, lda, pix, npix, minv, ctf_pool, full_npix, n_pool, R, NP, ND, seed, v, label);
+    return cudaGetLastError();
+}
+
+cudaError_t pn_power(const float2 *fimg, int full_npix, const PixelRef *pix, int npix, const float *minv, int B,
+                     float *v, cudaStream_t st) {
+    k_pn_power<<<nblk((long long)B * npix, 256), 256, 0, st>>>(fimg, full_npix, pix, npix, minv, B, v);
+    return cudaGetLastError();
+}
+
+cudaError_t pn_bin(const float *v, int npix, const int *bin, const float *inv_cnt, int nbins, int B, float *feat,
+                   cudaStream_t st) {
+    k_pn_bin<<<B, 128, sizeof(float) * nbins, st>>>(v, npix, bin, inv_cnt, nbins, feat);
+    return cudaGetLastError();
+}
+
+cudaError_t pn_forward(const PnDims &d, const float *params, const float *feat, float *a1, float *a2, float *h,
+                       float *logits, cudaStream_t st) {
+    const int H = d.H, W = d.W, B = d.B;
+    const float *w1 = params + d.o_w1, *b1 = params + d.o_b1, *w2 = params + d.o_w2, *b2 = params + d.o_b2;
+    const float *w3 = params + d.o_w3, *b3 = params + d.o_b3;
+    k_pn_conv_fwd<<<nblk((long long)B * d.C1 * H * W, 256), 256, 0, st>>>(feat, 1, w1, b1, d.C1, H, W, B, a1);
+    k_pn_conv_fwd<<<nblk((long long)B * d.C2 * H * W, 256), 256, 0, st>>>(a1, d.C1, w2, b2, d.C2, H, W, B, a2);
+    k_pn_pool<<<nblk((long long)B * d.C2 * H, 256), 256, 0, st>>>(a2, d.C2, H, W, B, h);
+    k_pn_linear<<<nblk((long long)B * d.ND, 256), 256, 0, st>>>(h, d.C2 * H, w3, b3, d.ND, B, logits);
+    return cudaGetLastError();
+}
+
+cudaError_t pn_loss_backward(const PnDims &d, const float *params, const float *feat, const float *a1,
+                             const float *a2, const float *h, const float *logits, const int *label,
+                             const float *target, float *dl, float *loss, float *d2, float *d1, float *grad,
+                             cudaStream_t st) {
+    const int H = d.H, W = d.W, B = d.B, F = d.C2 * d.H;
+    k_pn_xent<<<B, 256, 0, st>>>(logits, d.ND, label, target, B, dl, loss);
+    k_pn_linear_bwd_w<<<nblk((long long)(F + 1) * d.ND, 256), 256, 0, st>>>(h, dl, F, d.ND, B, grad + d.o_w3,
+                                                                             grad + d.o_b3);
+    k_pn_linear_bwd_x<<<nblk((long long)B * F, 256), 256, 0, st>>>(dl, params + d.o_w3, F, d.ND, B, a2, W, d2);
+    k_pn_conv_bwd_w<<<d.C2 * d.C1 * KH * KW + d.C2, 256, 0, st>>>(a1, d.C1, d2, d.C2, H, W, B, grad + d.o_w2,
+                                                                   grad + d.o_b2);
+    k_pn_conv_bwd_x<<<nblk((long long)B * d.C1 * H * W, 256), 256, 0, st>>>(d2, d.C2, params + d.o_w2, d.C1, H, W,
+                                                                             B, a1, d1);
+    k_pn_conv_bwd_w<<<d.C1 * 1 * KH * KW + d.C1, 256, 0, st>>>(feat, 1, d1, d.C1, H, W, B, grad + d.o_w1,
+                                                                grad + d.o_b1);
+    return cudaGetLastError();
+}
+
+cudaError_t pn_adam(float *p, const float *g, float *m, float *v, long long n, float lr, int t, cudaStream_t st) {
+    const float b1 = 0.9f, b2 = 0.999f;
+    double p1 = 1., p2 = 1.;
+    for (int k = 0; k < t; ++k) {
+        p1 *= b1;
+        p2 *= b2;
+    }
+    k_pn_adam<<<nblk(n, 256), 256, 0, st>>>(p, g, m, v, n, lr, b1, b2, 1e-8f, (float)(1. - p1), (float)(1. - p2));
+    return cudaGetLastError();
+}
+
+cudaError_t pn_topm(const float *logits, int N, int M, int B, int *idx, float *prob, cudaStream_t st) {
+    k_pn_topm<<<B, 256, sizeof(float) * N, st>>>(logits, N, M, idx, prob);
+    return cudaGetLastError();
+}
+
+}  // namespace gbr

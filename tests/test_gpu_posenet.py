@@ -1,0 +1,117 @@
+"""Learned pose proposal on the device (gbr_posenet_*) against the numpy
+oracle, and what training buys.
+
+Tolerances: features (FP32 bin sums in shared memory, FP32 log1p) to 1e-5
+relative / absolute; loss to 1e-5 relative and each parameter block's
+gradient to 1e-4 relative L2 (FP32 kernels against the float64 oracle).
+Gain: after training on views generated from the bundle's reference, the
+network's top-M directions (M = 1/8 of the directions) hold the exhaustive
+E-step's best direction for at least 1.5x the fraction that M random
+directions would (M / ndir), and clearly more often than the untrained
+network.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _bundle(ds, m):
+    from relion_gb300.estep import MlDeviceBundle
+    b = MlDeviceBundle(m, device=0)
+    for k, r in enumerate(ds.refs):
+        b.setup_projector(k, r["data"], r["yinit"], r["zinit"], r["r_max"], r["pad"])
+    return b
+
+
+def _need_cuda():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+
+
+def test_features_match_oracle():
+    _need_cuda()
+    from oracle import posenet_oracle as po
+    from relion_gb300 import datagen
+    from relion_gb300.posenet import PoseProposer
+    ds = datagen.Dataset("cfg0_box64", seed=3, n_particles=16)
+    m = ds.model(precision=1)
+    b = _bundle(ds, m)
+    net = PoseProposer(b, nangle=24, max_batch=8, seed=2)  # two chunks of 8
+    batch = ds.particles(0, 16)
+    fg = net.features(batch["fimg"])
+    xy, minv = net.pixels()
+    fo = po.features(batch["fimg"], xy, minv, net.nring, net.nangle)
+    net.close()
+    b.close()
+    assert np.count_nonzero(fo) > fo.size // 2
+    np.testing.assert_allclose(fg, fo, rtol=1e-5, atol=1e-5)
+
+
+def test_loss_grad_match_oracle():
+    _need_cuda()
+    from oracle import posenet_oracle as po
+    from relion_gb300 import datagen
+    from relion_gb300.posenet import PoseProposer
+    ds = datagen.Dataset("cfg0_box64", seed=4, n_particles=4)
+    m = ds.model(precision=1)
+    b = _bundle(ds, m)
+    net = PoseProposer(b, nangle=24, c1=8, c2=12, max_batch=8, seed=5)
+    H, W, C1, C2, ND = net.nring, net.nangle, net.c1, net.c2, net.ndir
+    g = np.random.default_rng(9)
+    p = net.get_params().astype(np.float64)
+    o = po.layout(H, W, C1, C2, ND)
+    p[o["b1"]:o["w2"]] = 0.1
+    p[o["b2"]:o["w3"]] = 0.1
+    p[o["b3"]:] = g.normal(0, 0.1, ND)
+    net.set_params(p.astype(np.float32))
+    p32 = net.get_params().astype(np.float64)
+    feat = g.normal(0, 1, (8, H * W)).astype(np.float32)
+    t = (g.random((8, ND)) ** 4).astype(np.float32)
+    t /= t.sum(axis=1, keepdims=True)
+    lg, gg = net.loss_grad(feat, t)
+    lo, go = po.loss_grad(p32, feat.astype(np.float64), t.astype(np.float64), H, W, C1, C2, ND)
+    net.close()
+    b.close()
+    assert abs(lg - lo) <= 1e-5 * abs(lo)
+    names = ["w1", "b1", "w2", "b2", "w3", "b3", "n"]
+    for k, nxt in zip(names[:-1], names[1:]):
+        a, r = gg[o[k]:o[nxt]], go[o[k]:o[nxt]]
+        err = np.linalg.norm(a - r) / max(np.linalg.norm(r), 1e-30)
+        assert err <= 1e-4, (k, err)
+
+
+def _best_dirs(b, res):
+    ih = np.asarray(res["best_ihidden_over"]) // (b.nover_rot * b.nover_trans)
+    return (ih // b.ntrans // b.npsi) % b.ndir
+
+
+def test_training_gain():
+    _need_cuda()
+    from relion_gb300 import datagen
+    from relion_gb300.estep import MlOptimiserCuda
+    from relion_gb300.posenet import PoseProposer
+    ds = datagen.Dataset("cfg0_box64", seed=7, n_particles=512)
+    m = ds.model(precision=1)
+    b = _bundle(ds, m)
+    pool = ds.particles(0, 256)["fctf"]
+    test = ds.particles(256, 256)
+    w = MlOptimiserCuda(b)
+    best = _best_dirs(b, w.do_expectation_some_particles(test))
+    w.close()
+    net = PoseProposer(b, nangle=24, max_batch=256, seed=1)
+    M = net.ndir // 8
+    idx0, _ = net.propose(test["fimg"], M)
+    loss = net.train(pool, steps=1500, batch=256, lr=2e-3)
+    idx1, prob1 = net.propose(test["fimg"], M)
+    ndir = net.ndir
+    net.close()
+    b.close()
+    r0 = float(np.mean([best[i] in idx0[i] for i in range(len(best))]))
+    r1 = float(np.mean([best[i] in idx1[i] for i in range(len(best))]))
+    print("posenet: M %d of %d directions, recall untrained %.3f trained %.3f (uniform %.3f), loss %.3f" %
+          (M, ndir, r0, r1, M / ndir, loss))
+    assert np.all(np.diff(prob1, axis=1) <= 0)
+    assert r1 >= 1.5 * M / ndir
+    assert r1 >= r0 + 0.1
