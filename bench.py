@@ -257,6 +257,7 @@ def run_ours(args, world, rank, local):
     extra = rank == 0 and not args.no_mstep and args.workload == CONFIG  # sections of the headline workload
     mstep = mstep_section(args, ds, model, bundle, worker, dev_batch, local) if extra else None
     io = io_section(ds, ib, model) if extra else None
+    learned = learned_section(batch, bundle, res) if extra else None
 
     # ---- roofline of the dominant kernel: the coarse cross-term GEMM ----
     R = bundle.nr_classes * bundle.ndir * bundle.npsi
@@ -334,7 +335,40 @@ def run_ours(args, world, rank, local):
         out["clocks"] = clk.summary()
         out["mstep"] = mstep
         out["io"] = io
+        out["learned"] = learned
     return out, ds, batch, model
+
+
+def learned_section(batch, bundle, res, steps=2000):
+    """Learned pose proposal on this workload: the network trained on the
+    device on views generated from the current reference (CTFs of this batch,
+    the model's noise), then asked for the top-M directions of this batch's
+    particles; recall = fraction whose exhaustive E-step best direction (the
+    timed steps' result) is among them, against M / ndir for M directions
+    taken without the network."""
+    from relion_gb300.posenet import PoseProposer
+    n_over = bundle.nover_rot * bundle.nover_trans
+    best = (np.asarray(res["best_ihidden_over"]) // n_over // bundle.ntrans // bundle.npsi) % bundle.ndir
+    net = PoseProposer(bundle, nangle=24, max_batch=256, seed=1)
+    t0 = time.perf_counter()
+    loss = net.train(batch["fctf"], steps=steps, batch=256, lr=2e-3)
+    t_train = time.perf_counter() - t0
+    recall = {}
+    for k in (16, 8, 4):
+        M = net.ndir // k
+        idx, _ = net.propose(batch["fimg"], M)
+        recall["ndir/%d" % k] = {"M": int(M), "recall": round(float(np.mean([best[i] in idx[i] for i in range(len(best))])), 4),
+                                 "uniform": round(M / net.ndir, 4)}
+    t0 = time.perf_counter()
+    net.propose(batch["fimg"], net.ndir // 8)
+    t_prop = time.perf_counter() - t0
+    ndir = net.ndir
+    net.close()
+    return {"ndir": int(ndir), "train_steps": steps, "views_per_step": 256, "train_s": round(t_train, 2),
+            "final_loss": round(float(loss), 4), "propose_ms": round(1e3 * t_prop, 3),
+            "particles": int(len(best)), "recall": recall,
+            "note": "proposals are not yet used to restrict the coarse pass: the line's value is the exhaustive "
+                    "precision-form E-step"}
 
 
 def io_section(ds, ib, model):

@@ -81,3 +81,15 @@ def test_star_errors(lib, tmp_path):
     # an absent label reads as the given default
     np.testing.assert_array_equal(st.column("particles", "rlnDefocusV", float, 7.0), [7.0])
     assert os.path.exists(str(p))
+
+
+def test_posenet_null_arguments(lib):
+    L = lib.load()
+    h = C.c_void_p()
+    d = lib.PosenetDesc(4, 12, 4, 4, 8, 0, 1)
+    assert L.gbr_posenet_create(None, C.byref(d), C.byref(h)) == GBR_ERR_INVALID
+    assert L.gbr_posenet_sizes(None, None, None, None, None) == GBR_ERR_INVALID
+    assert L.gbr_posenet_train(None, None, 0, 1, 1, 1e-3, None) == GBR_ERR_INVALID
+    assert L.gbr_posenet_propose(None, None, 0, 1, None, None) == GBR_ERR_INVALID
+    assert L.gbr_posenet_loss_grad(None, None, None, 1, None, None) == GBR_ERR_INVALID
+    assert L.gbr_posenet_destroy(None) == 0
