@@ -38,14 +38,12 @@ sys.path.insert(0, ROOT)
 METRIC = "E-step particles/s @box256, 1 GB300: learned+batched vs plain GPU at equal FSC"
 CONFIG = "cfg1_box256"
 
-# DRAM bytes of one coarse cross-term GEMM launch from the ncu capture of a
-# 16-particle batch (profiles/coarse_cross_gemm_box256_b16.md): the
-# projection-table read is independent of the batch, the diff2 write grows
-# with it.
+# DRAM bytes of one coarse cross-term GEMM launch (plain FP32 path) from an
+# ncu capture of a 16-particle batch: the projection-table read is independent
+# of the batch, the diff2 write grows with it.
 NCU_CROSS_B16 = {"read": 262.75e6, "write": 222.41e6, "batch": 16}
 # dram__bytes_read.sum / dram__bytes_write.sum of one k_tc_diff2<0> launch at
-# the bench's batch of 768 (one-pass metrics, full-size capture;
-# profiles/launches_box256_b768.md)
+# the bench's batch of 768 (ncu, one-pass metrics, full-size capture)
 NCU_TC = {"read": 3.326e9, "write": 0.755e9, "batch": 768}
 
 

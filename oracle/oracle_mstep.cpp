@@ -2,7 +2,7 @@
  * oracle_mstep.cpp -- TEST INFRASTRUCTURE ONLY (the oracle).
  *
  * Double-precision restatement of the reference's reconstruction side of an
- * iteration, for the checker of relion_gb300/csrc/k_recon.cu:
+ * iteration, which the tests compare relion_gb300/csrc/k_recon.cu with:
  *   BackProjector::enforceHermitianSymmetry   src/backprojector.cpp:2148-2165
  *   BackProjector::updateSSNRarrays           src/backprojector.cpp:1041-1204
  *   BackProjector::reconstruct                src/backprojector.cpp:1379-1872

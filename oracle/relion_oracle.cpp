@@ -4,8 +4,8 @@
  * A single-threaded, double-precision restatement of the CPU expectation
  * step of relion_refine (no --gpu, RFLOAT = double, exact Fourier shifts,
  * i.e. without --onthefly_shifts).  Each function cites the reference
- * file:line it follows.  This file is the checker for the CUDA path in
- * relion_gb300/csrc; the product never links it.
+ * file:line it follows.  The tests compare the CUDA path in
+ * relion_gb300/csrc with it (test infrastructure); the product never links it.
  *
  * Scope (the configurations' case): one optics group whose pixel and box
  * size equal the model's, one image per particle, C1, NOPRIOR orientational

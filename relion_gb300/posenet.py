@@ -2,7 +2,7 @@
 top-M coarse viewing directions of each particle (gbr_posenet_* in
 libgbrelion).  No counterpart in the reference, whose coarse search is
 exhaustive (src/acc/acc_ml_optimiser_impl.h:1016-1414 scores every coarse
-orientation); the exhaustive search stays the fallback and the judge of the
+orientation); the exhaustive search stays the fallback and the measure of the
 proposals.
 
 The network is trained on the device by the library's own forward, backward
