@@ -27,6 +27,7 @@
 // pixel), Box-Muller for the normals.
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdint>
 
 #include "gbr_internal.h"
@@ -415,11 +416,7 @@ cudaError_t pn_loss_backward(const PnDims &d, const float *params, const float *
 
 cudaError_t pn_adam(float *p, const float *g, float *m, float *v, long long n, float lr, int t, cudaStream_t st) {
     const float b1 = 0.9f, b2 = 0.999f;
-    double p1 = 1., p2 = 1.;
-    for (int k = 0; k < t; ++k) {
-        p1 *= b1;
-        p2 *= b2;
-    }
+    const double p1 = std::pow((double)b1, (double)t), p2 = std::pow((double)b2, (double)t);
     k_pn_adam<<<nblk(n, 256), 256, 0, st>>>(p, g, m, v, n, lr, b1, b2, 1e-8f, (float)(1. - p1), (float)(1. - p2));
     return cudaGetLastError();
 }
