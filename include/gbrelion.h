@@ -418,7 +418,9 @@ typedef struct {
 } gbr_posenet_desc;
 
 /* The bundle must have its model arrays and projectors (the pose tables are
- * built here if needed); the network keeps a pointer to it. */
+ * built here if needed); the network keeps a pointer to it and reads the
+ * bundle's current tables, so destroy the network before the bundle.  3D
+ * bundles only (GBR_ERR_UNSUPPORTED for 2D classification). */
 int gbr_posenet_create(gbr_bundle *b, const gbr_posenet_desc *d, gbr_posenet **out);
 int gbr_posenet_destroy(gbr_posenet *n);
 /* parameter count, features per particle (nring * nangle), directions, active coarse pixels */
