@@ -37,6 +37,9 @@ sys.path.insert(0, ROOT)
 
 METRIC = "E-step particles/s @box256, 1 GB300: learned+batched vs plain GPU at equal FSC"
 CONFIG = "cfg1_box256"
+# reference arm: particles of the batch per step (the oracle takes ~1 s per
+# box-256 particle on 16 host threads)
+REF_PARTICLES_PER_STEP = 2
 
 # DRAM bytes of one coarse cross-term GEMM launch (plain FP32 path) from an
 # ncu capture of a 16-particle batch: the projection-table read is independent
@@ -57,6 +60,7 @@ def parse():
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mstep", action="store_true", help="skip the reconstruction-side section (profiling runs)")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain FP32 path leg (profiling runs)")
     ap.add_argument("--workload", default=CONFIG,
                     choices=["cfg1_box256", "cfg4_box256_K4", "cfg3_box128_2d", "cfg0_box64"],
                     help="dataset shape (the headline line is cfg1_box256; the others for reference figures)")
@@ -252,6 +256,15 @@ def run_ours(args, world, rank, local):
         total_ms, e2e_total, img_total, stream_total = max_over_ranks([total_ms, e2e_total, img_total, stream_total],
                                                                       device=dev)
 
+    # ---- the plain FP32 path on the same batch (the metric's denominator) ----
+    plain = None
+    if args.precision == "bf16" and not args.no_plain:
+        plain = plain_section(args, ds, model, dev_batch, host_batch, h2d, flush, local)
+        if world > 1:
+            from relion_gb300.replicas import max_over_ranks
+            plain["total_ms"], plain["e2e_total_ms"] = max_over_ranks([plain["total_ms"], plain["e2e_total_ms"]],
+                                                                      device=dev)
+
     extra = rank == 0 and not args.no_mstep and args.workload == CONFIG  # sections of the headline workload
     mstep = mstep_section(args, ds, model, bundle, worker, dev_batch, local) if extra else None
     io = io_section(ds, ib, model) if extra else None
@@ -289,12 +302,13 @@ def run_ours(args, world, rank, local):
         "dtype": "bf16 (coarse cross term) / fp32 (fine pass) / f64 (sums, volumes)"
                  if args.precision == "bf16" else "fp32 / f64 (sums, volumes)",
         "data": "synthetic (seeded Gaussian-blob volume, analytic Fourier slices, CTF, white noise)",
-        "config": {"workload": workload_text(args.workload, bundle, model),
-                   "batch_particles": B,
-                   "precision": "precision form: tcgen05 BF16 coarse pass, FP32 fine pass"
-                                if args.precision == "bf16" else "plain FP32 path",
-                   "l2": "flushed (512 MB write) before every timed step",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "config": {"workload": workload_text(args.workload, model, bundle.nr_classes, bundle.ndir, bundle.npsi,
+                                             bundle.ntrans)},
+        "run": {"batch_particles": B,
+                "precision": "precision form: tcgen05 BF16 coarse pass, FP32 fine pass"
+                             if args.precision == "bf16" else "plain FP32 path",
+                "l2": "flushed (512 MB write) before every timed step",
+                "parallelism": "replicas" if world > 1 else "single GPU"},
         "e2e": {"value": world * B * args.steps / (e2e_total * 1e-3), "unit": "particles/s",
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "e2e_from_images": {"value": world * B * args.steps / (img_total * 1e-3), "unit": "particles/s",
@@ -329,12 +343,87 @@ def run_ours(args, world, rank, local):
         "mean_nr_sign": float(np.mean(res["nr_sign"])),
         "mean_fine_poses": float(np.mean(res["n_fine"])),
     }
+    if plain is not None:
+        pv = world * B * args.steps / (plain.pop("total_ms") * 1e-3)
+        pe = world * B * args.steps / (plain.pop("e2e_total_ms") * 1e-3)
+        plain["value"], plain["e2e"]["value"] = pv, pe
+        out["plain"] = plain
+        out["vs_plain"] = {"value": out["value"] / pv, "e2e": out["e2e"]["value"] / pe,
+                           "note": "this line's value / the plain FP32 path's, same batch and timing"}
     if rank == 0:
         out["clocks"] = clk.summary()
         out["mstep"] = mstep
         out["io"] = io
         out["learned"] = learned
     return out, ds, batch, model
+
+
+def plain_section(args, ds, model, dev_batch, host_batch, h2d, flush, local):
+    """The plain FP32 path (FP32 SIMT cross term and norms, every coarse row
+    read, full diff2 stores) on the same batch, timed like the headline:
+    device-resident steps, then host-buffer (e2e) steps, L2 flushed before
+    each.  Its roofline: the FP32 cross-term GEMM against the live-measured
+    FP32 FMA peak (the bound of this path), next to the HBM byte model of the
+    reference's unfused plain path (bytes per particle below)."""
+    import torch
+    from relion_gb300.estep import MlDeviceBundle, MlOptimiserCuda, STAGES, measure_fp32_peak
+    B = dev_batch["n"]
+    b = MlDeviceBundle(dict(model, precision=0), device=local)
+    for k, r in enumerate(ds.refs):
+        b.setup_projector(k, r["data"], r["yinit"], r["zinit"], r["r_max"], r["pad"])
+    b.reserve(64 << 30)
+    w = MlOptimiserCuda(b)
+    for _ in range(max(1, min(args.warmup, 2))):
+        w.do_expectation_some_particles(dev_batch)
+    torch.cuda.synchronize()
+
+    def timed(batch):
+        ms = []
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ev0.record()
+            w.do_expectation_some_particles(batch)
+            ev1.record()
+            ev1.synchronize()
+            ms.append(ev0.elapsed_time(ev1))
+        return float(sum(ms))
+    st0 = w.stage_times().copy()
+    total = timed(dev_batch)
+    stage = (w.stage_times() - st0) / args.steps
+    e2e_total = timed(host_batch)
+    R = b.nr_classes * b.ndir * b.npsi
+    T = b.ntrans
+    nc = active_coarse_pixels(model)
+    cross_ms = float(stage[STAGES.index("cross_gemm")])
+    achieved = 2.0 * R * (B * T) * (2 * nc) / (cross_ms * 1e-3) / 1e12
+    peak = measure_fp32_peak(local)
+    # HBM byte model of the reference's plain path per particle (unfused):
+    # image, CTF and noise weights; the coarse diff2 / weight array written and
+    # read ~8 times (min, exp, max, filter, sort, scan, threshold); the coarse
+    # projections shared by the batch
+    npix_f = model["current_size"] * (model["current_size"] // 2 + 1)
+    per_part = npix_f * 16 + 8 * R * T * 4 + R * nc * 8 / B
+    step_s = total * 1e-3 / args.steps
+    hbm = measured_peaks().get("hbm_gbs")
+    w.close()
+    b.close()
+    return {"total_ms": total, "e2e_total_ms": e2e_total,
+            "ms_per_step": total / args.steps,
+            "unit": "particles/s", "dtype": "fp32 (cross term, norms, fine pass) / f64 (weight sums, volumes)",
+            "e2e": {"unit": "particles/s", "h2d_bytes_per_step": int(h2d)},
+            "stage_ms": {k: round(float(v), 4) for k, v in zip(STAGES, stage) if v > 0},
+            "roofline": {"bound": "fp32", "kernel": "coarse cross-term GEMM, FP32 SIMT (k_gemm<RowsK,CrossY,Diff2Epi>)",
+                         "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                         "peak_source": "measured live (gbr_measure_fp32_peak: FMA chains on all SMs)"},
+            "hbm_model": {"bytes_per_particle": per_part,
+                          "achieved_GBps": per_part * B / step_s / 1e9,
+                          "peak_GBps": hbm, "frac": (per_part * B / step_s / 1e9 / hbm) if hbm else None,
+                          "note": "the reference's unfused plain-path byte model (image + CTF + noise weights, "
+                                  "coarse diff2 array written and read 8 times, projections shared by the batch) "
+                                  "over this path's step time; this path stores the diff2 array once and reads it "
+                                  "once, and its time goes to the FP32 contraction"}}
 
 
 def learned_section(batch, bundle, res, steps=2000):
@@ -497,14 +586,14 @@ def mstep_section(args, ds, model, bundle, worker, dev_batch, local):
     return out
 
 
-def workload_text(name, bundle, model):
-    """One line naming the workload with its sizes."""
+def workload_text(name, model, nr_classes, ndir, npsi, ntrans):
+    """One line naming the workload with its sizes (both arms print it)."""
     box = model["ori_size"]
-    grid = ("%d classes x %d psi" % (bundle.nr_classes, bundle.npsi) if int(model.get("ref_dim", 3) or 3) == 2
-            else "HEALPix %d directions x %d psi, %d class%s" % (bundle.ndir, bundle.npsi, bundle.nr_classes,
-                                                                 "" if bundle.nr_classes == 1 else "es"))
+    grid = ("%d classes x %d psi" % (nr_classes, npsi) if int(model.get("ref_dim", 3) or 3) == 2
+            else "HEALPix %d directions x %d psi, %d class%s" % (ndir, npsi, nr_classes,
+                                                                 "" if nr_classes == 1 else "es"))
     return ("%s: box%d E-step, iteration-1 sizes (current %d px, coarse %d px), %s, %d translations, "
-            "oversampling 1" % (name, box, model["current_size"], model["coarse_size"], grid, bundle.ntrans))
+            "oversampling 1" % (name, box, model["current_size"], model["coarse_size"], grid, ntrans))
 
 
 def measured_peaks():
@@ -530,16 +619,19 @@ def active_coarse_pixels(model):
 
 
 def cpu_particles_per_s(ds, batch, model, n_particles, threads):
-    """Oracle (CPU restatement of the reference's CPU E-step) on n particles."""
-    os.environ["OMP_NUM_THREADS"] = str(threads)
+    """Oracle (CPU restatement of the reference's CPU E-step) on n particles
+    with `threads` host threads; returns (particles/s, threads in effect).
+    The thread count is set through the OpenMP runtime itself: torch has
+    started it already, so OMP_NUM_THREADS would no longer be read."""
     from oracle import build as obuild
     obuild.build()
     from oracle import pyoracle
+    used = pyoracle.set_threads(threads)
     sub = {k: (v[:n_particles] if isinstance(v, np.ndarray) else v) for k, v in batch.items()}
     sub["n"] = n_particles
     t0 = time.perf_counter()
-    pyoracle.run(model, [ds.ref], sub)
-    return n_particles / (time.perf_counter() - t0)
+    pyoracle.run(model, ds.refs, sub)
+    return n_particles / (time.perf_counter() - t0), used
 
 
 def run_reference(args, world, rank):
@@ -549,28 +641,37 @@ def run_reference(args, world, rank):
     if rank != 0:
         return None
     from relion_gb300 import datagen
+    from oracle import pyoracle
     cores = os.cpu_count() or 1
-    per_step = 2
-    ds = datagen.Dataset(CONFIG, seed=args.seed, n_particles=per_step)
+    per_step = REF_PARTICLES_PER_STEP
+    # the GPU arm's workload (same generator and seed); each step is a bounded
+    # sample of its batch: the first particles of it
+    ds = datagen.Dataset(args.workload, seed=args.seed, n_particles=per_step)
     model = ds.model()
     batch = ds.particles(0, per_step)
     for _ in range(args.warmup if args.warmup < 1 else 1):
         cpu_particles_per_s(ds, batch, model, 1, cores)
-    t_total, n_total = 0.0, 0
+    t_total, n_total, used = 0.0, 0, 0
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        cpu_particles_per_s(ds, batch, model, per_step, cores)
+        _, used = cpu_particles_per_s(ds, batch, model, per_step, cores)
         t_total += time.perf_counter() - t0
         n_total += per_step
     v = n_total / t_total
+    ndir, npsi, ntr = pyoracle.sampling_sizes(int(model["healpix_order"]), float(model["psi_step"]),
+                                             float(model["offset_range"]), float(model["offset_step"]),
+                                             int(model.get("ref_dim", 3) or 3))
     return {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "particles/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic", "config": {"workload": "box256 E-step (same as the GPU arm)",
-                                        "batch_particles": per_step},
-        "cpu_baseline": {"value": v, "unit": "particles/s", "cores": cores, "kind": "port",
-                         "sample": "%d particles per step, all host threads (OpenMP)" % per_step},
+        "data": "synthetic (seeded Gaussian-blob volume, analytic Fourier slices, CTF, white noise)",
+        "config": {"workload": workload_text(args.workload, model, int(model["nr_classes"]), ndir, npsi, ntr)},
+        "particles_per_step": per_step,
+        "cpu_baseline": {"value": v, "unit": "particles/s", "cores": used, "kind": "port",
+                         "sample": "%d particles of the GPU arm's batch per step (its first ones), the oracle "
+                                   "(FP64 restatement of the reference's CPU E-step) on %d host threads "
+                                   "(OpenMP over orientations; %d cores on the host)" % (per_step, used, cores)},
         "e2e": {"value": v, "unit": "particles/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
@@ -591,9 +692,10 @@ def main():
     if rank == 0:
         if not args.no_cpu_baseline:
             # bounded sample: one particle on one host thread (~10-30 s)
-            v = cpu_particles_per_s(ds, batch, model, 1, 1)
-            out["cpu_baseline"] = {"value": v, "unit": "particles/s", "cores": 1, "kind": "port",
-                                   "sample": "1 particle of the same batch, oracle on 1 host thread"}
+            v, used = cpu_particles_per_s(ds, batch, model, 1, 1)
+            out["cpu_baseline"] = {"value": v, "unit": "particles/s", "cores": used, "kind": "port",
+                                   "sample": "1 particle of the same batch, the oracle (FP64 restatement of the "
+                                             "reference's CPU E-step) on %d host thread(s)" % used}
         print(json.dumps(out))
     if world > 1:
         import torch.distributed as dist

@@ -157,10 +157,27 @@ int gbr_bundle_reserve(gbr_bundle *b, size_t bytes);
 /* new MlOptimiserCuda(MlOptimiser*, bundle, name) (src/ml_optimiser.cpp:3587). */
 int gbr_worker_create(gbr_bundle *b, gbr_worker **out);
 
-/* Keep device copies of the last batch's intermediate arrays for
+/* Keep host copies of the last call's intermediate arrays for
  * gbr_worker_debug_fetch (the RELION_TESTING dumps of
- * src/ml_optimiser.cpp:4600-4700 serve the same purpose). */
+ * src/ml_optimiser.cpp:4600-4700 serve the same purpose).  The read-back
+ * does not change the computation: the call runs the same passes, kernels
+ * and sparse stores as without it, and the copies are taken per pass. */
 int gbr_worker_set_debug(gbr_worker *w, int on);
+
+/* Worker settings for tests and tuning (the reference has no counterpart;
+ * its equivalents are compile-time constants).  The library reads no
+ * environment variable: every setting is made through this call. */
+typedef enum {
+    GBR_OPT_DEBUG = 1,        /* as gbr_worker_set_debug                             */
+    GBR_OPT_FINE_MODE = 2,    /* fine pass: 0 by significant density (default),
+                                 1 always dense, 2 always sparse                      */
+    GBR_OPT_COARSE_ROWS = 3,  /* precision form: 0 skip coarse rows far above the
+                                 minimum (default), 1 read every row                  */
+    GBR_OPT_CAND_CAP = 4,     /* coarse candidate-list entries per particle (65536)   */
+    GBR_OPT_CAND_BUF = 5,     /* block-local candidate buffer entries (0: all)        */
+    GBR_OPT_BATCH_CAP = 6     /* particles per pass of a call (0: from the budget)    */
+} gbr_worker_option;
+int gbr_worker_set_option(gbr_worker *w, int option, int64_t value);
 
 /* MlOptimiserCuda::doThreadExpectationSomeParticles(thread_id)
  * (cuda_ml_optimiser.cu:250-299 -> accDoExpectationOneParticle,
@@ -384,11 +401,15 @@ int gbr_measure_fp32_peak(int device, double *tflops);
  * src/ml_optimiser.cpp:8120-8200 without --maxsig), in device arrays
  * threshold[n] and nr_significant[n]; work is queued on `stream` (a
  * cudaStream_t, NULL for the default stream) and runs asynchronously.
- * Limit: n <= 64 rows per call (larger n: GBR_ERR_INVALID).  Its working
+ * Limit: n <= 64 rows per call (larger n: GBR_ERR_INVALID).  A row with no
+ * positive weight gets nr_significant 0 and threshold +inf.  Its working
  * memory is one fixed array of about 4.3 MB per GPU, held until the process
  * exits and shared by all calls: calls that overlap on the GPU race and must
  * be ordered by the caller.  The first call on a device looks up that
- * array's address; make it before any stream capture. */
+ * array's address and, with lazy module loading (the CUDA default), loads
+ * the library's device code, which may allocate: make the first call on
+ * each device before any stream capture and outside any region that must
+ * not allocate; every later call allocates nothing. */
 int gbr_significance_threshold_noalloc(const float *weights, int64_t n, int64_t len,
                                        double adaptive_fraction, float *threshold,
                                        uint32_t *nr_significant, void *stream);

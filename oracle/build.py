@@ -1,9 +1,9 @@
 """Build the oracle (TEST INFRASTRUCTURE ONLY).
 
 Compiles oracle/relion_oracle.cpp and oracle/oracle_mstep.cpp into
-oracle/_build/liboracle.so and, when
-the reference tree is present, the reference's own HEALPix sources into
-oracle/_ref/libref_healpix.so (oracle/build_ref.sh).
+oracle/_build/liboracle.so and, when the environment variable
+RELION_REFERENCE names the reference source tree, the reference's own HEALPix
+sources into oracle/_ref/libref_healpix.so (oracle/build_ref.sh).
 """
 import os
 import subprocess
@@ -22,8 +22,8 @@ def build(force=False):
         subprocess.run(["g++", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-std=c++17", "-fopenmp"]
                        + srcs + ["-o", LIB + ".tmp"], check=True)
         os.replace(LIB + ".tmp", LIB)
-    ref = os.environ.get("RELION_REFERENCE", "/root/reference")
-    if os.path.isdir(os.path.join(ref, "src", "Healpix_2.15a")) and (force or not os.path.exists(REF_LIB)):
+    ref = os.environ.get("RELION_REFERENCE", "")
+    if ref and os.path.isdir(os.path.join(ref, "src", "Healpix_2.15a")) and (force or not os.path.exists(REF_LIB)):
         subprocess.run(["sh", os.path.join(HERE, "build_ref.sh")], check=True)
     return LIB
 

@@ -1,10 +1,10 @@
 #!/bin/sh
 # Build the reference's own HEALPix sources (src/Healpix_2.15a) into
 # oracle/_ref/libref_healpix.so for the enumeration parity tests.
-# Needs the reference tree (default /root/reference, or $RELION_REFERENCE);
-# compiles the two .cc files where they lie, copies nothing into this repo.
+# Needs the reference tree in $RELION_REFERENCE; compiles the two .cc files
+# where they lie and copies nothing into this repository.
 set -e
-REF=${RELION_REFERENCE:-/root/reference}
+REF=${RELION_REFERENCE:?set RELION_REFERENCE to the reference source tree}
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 if [ ! -f "$REF/src/Healpix_2.15a/healpix_base.cc" ]; then

@@ -17,12 +17,14 @@ TOL = dict(
 )
 
 
-def run_gpu(model, refs, batch, device=0):
+def run_gpu(model, refs, batch, device=0, **options):
+    """The CUDA E-step with the debug read-back; `options` are worker
+    options (relion_gb300.estep.MlOptimiserCuda), e.g. batch_cap."""
     from relion_gb300.estep import MlDeviceBundle, MlOptimiserCuda
     b = MlDeviceBundle(model, device=device)
     for k, r in enumerate(refs):
         b.setup_projector(k, r["data"], r["yinit"], r["zinit"], r["r_max"], r["pad"])
-    w = MlOptimiserCuda(b, debug=True)
+    w = MlOptimiserCuda(b, debug=True, **options)
     res = w.do_expectation_some_particles(batch)
     n = len(res)
     dbg = []
@@ -40,22 +42,41 @@ def run_gpu(model, refs, batch, device=0):
     return res, dbg, ws, vols, times
 
 
-def compare(model, refs, batch, device=0):
-    gres, gdbg, gws, gvols, _ = run_gpu(model, refs, batch, device)
-    ores, odbg, ows, obpd, obpw = pyoracle.run(model, refs, batch, debug=True)
+def compare(model, refs, batch, device=0, oracle_out=None, **options):
+    """Error statistics of the CUDA E-step against the oracle on one batch.
+
+    The GPU side may store only part of the coarse diff2 array (sparse
+    stores of the precision form): `coarse_stored_subset` says whether its
+    stored poses are among those the oracle computed, `coarse_unstored_mass`
+    is the oracle's normalised weight on the poses it left out, and the
+    diff2 error is taken over the stored poses.  `fine_missing_mass` /
+    `fine_extra_mass` are the normalised fine weights of the oracle on poses
+    the GPU did not evaluate and of the GPU on poses the oracle did not.
+    `oracle_out` reuses an earlier pyoracle.run(..., debug=True) result."""
+    gres, gdbg, gws, gvols, _ = run_gpu(model, refs, batch, device, **options)
+    if oracle_out is None:
+        oracle_out = pyoracle.run(model, refs, batch, debug=True)
+    ores, odbg, ows, obpd, obpw = oracle_out
     n = len(gres)
     st = dict(coarse_diff2_rel=0.0, coarse_w_abs=0.0, sig_mismatch=0, nr_sign_diff=0,
               fine_set_mismatch=0, fine_diff2_rel=0.0, fine_w_abs=0.0, pmax_rel=0.0,
-              argmax_agree=0.0, dLL_abs=0.0, sig_weight_rel=0.0)
+              argmax_agree=0.0, dLL_abs=0.0, sig_weight_rel=0.0, coarse_stored_subset=True,
+              coarse_stored_all=True, coarse_unstored_mass=0.0, fine_missing_mass=0.0,
+              fine_extra_mass=0.0, coarse_sum_rel=0.0)
     for i in range(n):
         od, gd = odbg[i]["coarse_diff2"], gdbg[i]["coarse_diff2"]
         comp = od != -999.0
-        assert np.array_equal(comp, np.isfinite(gd)), "coarse computed sets differ"
-        st["coarse_diff2_rel"] = max(st["coarse_diff2_rel"],
-                                     float(np.max(np.abs(gd[comp] - od[comp]) / np.abs(od[comp]))))
+        stored = np.isfinite(gd)
+        st["coarse_stored_subset"] &= bool(np.all(comp[stored]))
+        st["coarse_stored_all"] &= bool(np.array_equal(comp, stored))
         ow = odbg[i]["coarse_weight"] / ores["coarse_sum_weight"][i]
+        st["coarse_unstored_mass"] = max(st["coarse_unstored_mass"], float(np.sum(ow[comp & ~stored])))
+        st["coarse_diff2_rel"] = max(st["coarse_diff2_rel"],
+                                     float(np.max(np.abs(gd[stored] - od[stored]) / np.abs(od[stored]))))
         gw = gdbg[i]["coarse_weight"] / gres["coarse_sum_weight"][i]
         st["coarse_w_abs"] = max(st["coarse_w_abs"], float(np.max(np.abs(ow - gw))))
+        st["coarse_sum_rel"] = max(st["coarse_sum_rel"], abs(gres["coarse_sum_weight"][i] /
+                                                             ores["coarse_sum_weight"][i] - 1.0))
         osig = odbg[i]["coarse_significant"].astype(bool)
         gsig = gdbg[i]["coarse_weight"] >= gres["coarse_significant_weight"][i]
         gsig &= gdbg[i]["coarse_weight"] > 0
@@ -67,6 +88,11 @@ def compare(model, refs, batch, device=0):
         gidx = gdbg[i]["fine_idx"]
         common, oi, gi = np.intersect1d(ocomp, gidx, return_indices=True)
         st["fine_set_mismatch"] = max(st["fine_set_mismatch"], len(ocomp) + len(gidx) - 2 * len(common))
+        ofw = odbg[i]["fine_weight"] / ores["fine_sum_weight"][i]
+        gfw = gdbg[i]["fine_weight"] / gres["fine_sum_weight"][i]
+        st["fine_missing_mass"] = max(st["fine_missing_mass"],
+                                      float(np.sum(ofw[ocomp]) - np.sum(ofw[common])))
+        st["fine_extra_mass"] = max(st["fine_extra_mass"], float(np.sum(gfw) - np.sum(gfw[gi])))
         if len(common):
             o = ofd[common]
             g = gdbg[i]["fine_diff2"][gi]

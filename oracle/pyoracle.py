@@ -68,6 +68,8 @@ def load():
             raise RuntimeError("oracle not built: %s (run oracle/build.py)" % path)
         lib = C.CDLL(path)
         lib.oracle_expectation.restype = C.c_int
+        lib.oracle_set_threads.restype = C.c_int
+        lib.oracle_set_threads.argtypes = [C.c_int]
         lib.oracle_prepare_images.restype = C.c_int
         lib.oracle_prepare_images.argtypes = [P, I64, P, P, P, P, P, P, P, P]
         lib.oracle_ctf.restype = F64
@@ -87,6 +89,13 @@ def load():
         lib.oracle_fsc.argtypes = [I64, I64, P, P, P]
         _O = lib
     return _O
+
+
+def set_threads(n):
+    """Host threads of the oracle's OpenMP loops (0: leave unchanged); returns
+    the number in effect.  Works after another library (torch) has started
+    the OpenMP runtime, where OMP_NUM_THREADS is no longer read."""
+    return int(load().oracle_set_threads(int(n)))
 
 
 def load_ref():

@@ -23,6 +23,8 @@
 #include <cstring>
 #include <vector>
 
+#include <omp.h>
+
 namespace {
 
 const double kPI = 3.14159265358979323846;          // src/macros.h:104
@@ -531,6 +533,14 @@ struct PassOut {
 }  // namespace
 
 extern "C" {
+
+/* Host threads of the oracle's parallel loops (omp_set_num_threads on the
+ * calling thread, which is what counts even when the OpenMP runtime was
+ * started earlier by another library); returns the number now in effect. */
+int oracle_set_threads(int n) {
+    if (n > 0) omp_set_num_threads(n);
+    return omp_get_max_threads();
+}
 
 double oracle_ctf(double defU, double defV, double defAng, double kV, double Cs, double Q0,
                   double Bfac, double scale, double phase_shift, double X, double Y) {

@@ -26,6 +26,9 @@ extern "C" {
 
 /* Model and sampling state read by the E-step (MlOptimiser / MlModel /
  * HealpixSampling members).  All lengths in pixels unless stated. */
+/* Host threads of the oracle's OpenMP loops; returns the number in effect. */
+int oracle_set_threads(int n);
+
 typedef struct {
     int64_t ori_size;            /* mymodel.ori_size                               */
     int64_t nr_classes;          /* mymodel.nr_classes                             */

@@ -90,6 +90,7 @@ EXPORTS = {
     "gbr_bundle_reserve": (C.c_int, [P, C.c_size_t]),
     "gbr_worker_create": (C.c_int, [P, C.POINTER(P)]),
     "gbr_worker_set_debug": (C.c_int, [P, C.c_int]),
+    "gbr_worker_set_option": (C.c_int, [P, C.c_int, I64]),
     "gbr_expect_batch": (C.c_int, [P, C.POINTER(ParticleBatch), P]),
     "gbr_bundle_set_optics": (C.c_int, [P, C.POINTER(OpticsDesc)]),
     "gbr_prepare_images": (C.c_int, [P, C.POINTER(ImageBatch), P, P, P, P, P, P]),

@@ -268,21 +268,30 @@ struct gbr_worker {
     // dense fine pass
     int fine_mode = 0;  // 0: by significant density, 1: always dense, 2: always sparse
     int coarse_rows = 0;  // 0: skip far coarse rows by their minimum (tensor-core pass), 1: read all rows
-    int cand_cap_max = 1 << 16;  // candidate-list entries per particle (GBR_CAND_CAP)
-    int cand_buf = 0;            // block-local candidate buffer used (GBR_CAND_BUF; 0 = all of it)
+    int cand_cap_max = 1 << 16;  // candidate-list entries per particle (GBR_OPT_CAND_CAP)
+    int cand_buf = 0;            // block-local candidate buffer used (GBR_OPT_CAND_BUF; 0 = all of it)
     int last_dense = 0;
     DevBuf<float> Wt, Wp, Zt, CM, S2P, fnrm;
     DevBuf<float2> G;
-    // debug copies of the last batch
-    int dbg_n = 0;
-    std::vector<float> dbg_coarse;   // relative diff2
-    std::vector<float> dbg_wcoarse;
-    std::vector<double> dbg_cc, dbg_cf;
-    std::vector<float> dbg_fine, dbg_wfine;
-    std::vector<int> dbg_ejob;
-    std::vector<unsigned int> dbg_ecode;
-    std::vector<FineJob> dbg_jobs;
-    std::vector<long long> dbg_segf;
+    int batch_cap = 0;           // particles per pass (GBR_OPT_BATCH_CAP; 0 = from the budget)
+    int pass_cap = 0;            // particles per pass of the current call
+    // debug copies of the last call, one entry per pass (gbr_worker_debug_fetch)
+    struct DbgPass {
+        int n = 0;                        // particles of the pass
+        int dense = 0;                    // fine pass ran as dense contractions
+        int sparse = 0;                   // coarse diff2 stored only near the running minimum
+        std::vector<float> coarse;        // relative coarse diff2 [n][R*T]
+        std::vector<unsigned int> segmask;  // [n][R] stored 32-column segments (sparse)
+        std::vector<float> wcoarse;       // coarse weights [n][R*T]
+        std::vector<double> cc, cf;       // per-particle diff2 constants (coarse, fine)
+        std::vector<float> fine, wfine;
+        std::vector<int> ejob;
+        std::vector<unsigned int> ecode;
+        std::vector<FineJob> jobs;
+        std::vector<long long> segf;
+    };
+    std::vector<DbgPass> dbg;
+    int dbg_n = 0;                        // particles of the last call
 };
 
 namespace {
@@ -509,8 +518,16 @@ int call_capacity(gbr_worker *w, int n_all) {
     const long long per_part = (long long)b->R * b->T * 4 + (1LL << 20);
     const long long mem_cap = (b->budget ? (long long)b->budget : (48LL << 30)) / 2;
     int cap = (int)std::max<long long>(1, std::min<long long>(1024, mem_cap / per_part));
-    if (w->debug) cap = n_all;  // debug read-back covers the whole call
-    return ensure_capacity(w, std::min(cap, n_all));
+    if (w->batch_cap > 0) cap = std::min(cap, w->batch_cap);
+    if (w->debug) {
+        w->dbg.clear();
+        w->dbg_n = 0;
+    }
+    s = ensure_capacity(w, std::min(cap, n_all));
+    if (s) return s;
+    // passes of this call: at most `cap` particles each (the buffers may hold more)
+    w->pass_cap = std::min(cap, n_all);
+    return GBR_OK;
 }
 
 int threshold_search(gbr_worker *w, int n, float *vals, const long long *seg, long long max_len, int coarse,
@@ -551,15 +568,16 @@ int fine_sparse(gbr_worker *w, int n, long long njobs, long long nfine, const st
                                b->nf, b->phase_f.p, w->fd.p, w->ejob.p, w->ecode.p, w->ps.p, st));
     GBR_CUDA(cudaEventRecord(w->ev[6], st));
     if (w->debug) {
-        w->dbg_fine.resize(nfine);
-        w->dbg_ejob.resize(nfine);
-        w->dbg_ecode.resize(nfine);
-        w->dbg_jobs.resize(njobs);
-        GBR_CUDA(cudaMemcpyAsync(w->dbg_fine.data(), w->fd.p, sizeof(float) * nfine, cudaMemcpyDeviceToHost, st));
-        GBR_CUDA(cudaMemcpyAsync(w->dbg_ejob.data(), w->ejob.p, sizeof(int) * nfine, cudaMemcpyDeviceToHost, st));
-        GBR_CUDA(cudaMemcpyAsync(w->dbg_ecode.data(), w->ecode.p, sizeof(unsigned) * nfine, cudaMemcpyDeviceToHost, st));
-        GBR_CUDA(cudaMemcpyAsync(w->dbg_jobs.data(), w->jobs.p, sizeof(FineJob) * njobs, cudaMemcpyDeviceToHost, st));
-        w->dbg_segf = segf;
+        gbr_worker::DbgPass &D = w->dbg.back();
+        D.fine.resize(nfine);
+        D.ejob.resize(nfine);
+        D.ecode.resize(nfine);
+        D.jobs.resize(njobs);
+        GBR_CUDA(cudaMemcpyAsync(D.fine.data(), w->fd.p, sizeof(float) * nfine, cudaMemcpyDeviceToHost, st));
+        GBR_CUDA(cudaMemcpyAsync(D.ejob.data(), w->ejob.p, sizeof(int) * nfine, cudaMemcpyDeviceToHost, st));
+        GBR_CUDA(cudaMemcpyAsync(D.ecode.data(), w->ecode.p, sizeof(unsigned) * nfine, cudaMemcpyDeviceToHost, st));
+        GBR_CUDA(cudaMemcpyAsync(D.jobs.data(), w->jobs.p, sizeof(FineJob) * njobs, cudaMemcpyDeviceToHost, st));
+        D.segf = segf;
     }
     GBR_CUDA(launch_weights(w->fd.p, w->seg_f.p, n, max_seg, 0, T, w->ejob.p, w->ecode.p, w->jobs.p, nOR, nOT,
                             b->pdf_orient.p, w->pdf_off.p, w->ps.p, w->hist.p, st, 1, b->KP, (int)(b->ND * b->NP)));
@@ -567,8 +585,9 @@ int fine_sparse(gbr_worker *w, int n, long long njobs, long long nfine, const st
     if (s) return s;
     GBR_CUDA(cudaEventRecord(w->ev[7], st));
     if (w->debug) {
-        w->dbg_wfine.resize(nfine);
-        GBR_CUDA(cudaMemcpyAsync(w->dbg_wfine.data(), w->fd.p, sizeof(float) * nfine, cudaMemcpyDeviceToHost, st));
+        gbr_worker::DbgPass &D = w->dbg.back();
+        D.wfine.resize(nfine);
+        GBR_CUDA(cudaMemcpyAsync(D.wfine.data(), w->fd.p, sizeof(float) * nfine, cudaMemcpyDeviceToHost, st));
     }
     WsumArgs wa{};
     wa.jobs = w->jobs.p;
@@ -619,9 +638,10 @@ int fine_dense(gbr_worker *w, int n, long long &seg_len) {
                                w->fd.p, w->fnrm.p, b->pdf_orient.p, w->mask.p, nOR, nOT, W, w->ps.p, 1, st));
     GBR_CUDA(cudaEventRecord(w->ev[6], st));
     if (w->debug) {
-        w->dbg_fine.resize((size_t)n * per);
-        GBR_CUDA(cudaMemcpyAsync(w->dbg_fine.data(), w->fd.p, sizeof(float) * n * per, cudaMemcpyDeviceToHost, st));
-        w->dbg_segf = seg;
+        gbr_worker::DbgPass &D = w->dbg.back();
+        D.fine.resize((size_t)n * per);
+        GBR_CUDA(cudaMemcpyAsync(D.fine.data(), w->fd.p, sizeof(float) * n * per, cudaMemcpyDeviceToHost, st));
+        D.segf = seg;
     }
     GBR_CUDA(launch_weights(w->fd.p, w->seg_f.p, n, per, 2, T, nullptr, nullptr, nullptr, nOR, nOT,
                             b->pdf_orient.p, w->pdf_off.p, w->ps.p, w->hist.p, st, 1, b->KP, (int)(b->ND * b->NP)));
@@ -629,8 +649,9 @@ int fine_dense(gbr_worker *w, int n, long long &seg_len) {
     if (s) return s;
     GBR_CUDA(cudaEventRecord(w->ev[7], st));
     if (w->debug) {
-        w->dbg_wfine.resize((size_t)n * per);
-        GBR_CUDA(cudaMemcpyAsync(w->dbg_wfine.data(), w->fd.p, sizeof(float) * n * per, cudaMemcpyDeviceToHost, st));
+        gbr_worker::DbgPass &D = w->dbg.back();
+        D.wfine.resize((size_t)n * per);
+        GBR_CUDA(cudaMemcpyAsync(D.wfine.data(), w->fd.p, sizeof(float) * n * per, cudaMemcpyDeviceToHost, st));
     }
     // normalised weights, row sums, scalar sums
     const int ldwt = pad16(n);
@@ -699,8 +720,13 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
     GBR_CUDA(cudaEventRecord(w->ev[2], st));
     const bool use_rowmin = d.precision == GBR_PREC_BF16 && T >= 32 && w->coarse_rows == 0;
     // sparse diff2 writes: only row segments near the running minimum are
-    // stored (the debug read-back needs the whole array)
-    const bool sparse = use_rowmin && !w->debug && T <= 960;
+    // stored (the debug read-back reports the others as not computed)
+    const bool sparse = use_rowmin && T <= 960;
+    if (w->debug) {
+        w->dbg.emplace_back();
+        w->dbg.back().n = n;
+        w->dbg.back().sparse = sparse ? 1 : 0;
+    }
     if (use_rowmin) {
         GBR_CUDA(w->rowmin.reserve((size_t)n * R));
         GBR_CUDA(cudaMemsetAsync(w->rowmin.p, 0xFF, sizeof(unsigned int) * (size_t)n * R, st));
@@ -723,8 +749,14 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
     }
     GBR_CUDA(cudaEventRecord(w->ev[3], st));
     if (w->debug) {
-        w->dbg_coarse.resize((size_t)n * RT);
-        GBR_CUDA(cudaMemcpyAsync(w->dbg_coarse.data(), w->vals.p, sizeof(float) * n * RT, cudaMemcpyDeviceToHost, st));
+        gbr_worker::DbgPass &D = w->dbg.back();
+        D.coarse.resize((size_t)n * RT);
+        GBR_CUDA(cudaMemcpyAsync(D.coarse.data(), w->vals.p, sizeof(float) * n * RT, cudaMemcpyDeviceToHost, st));
+        if (sparse) {
+            D.segmask.resize((size_t)n * R);
+            GBR_CUDA(cudaMemcpyAsync(D.segmask.data(), w->segmask.p, sizeof(unsigned int) * n * R,
+                                     cudaMemcpyDeviceToHost, st));
+        }
     }
     // ---- coarse weights and significance ----
     // one read of the diff2 array: weights, FP64 sums and the candidate lists;
@@ -765,8 +797,9 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
     GBR_CUDA(cudaMemcpyAsync(w->h_ccnt.p, w->cand_cnt.p, sizeof(unsigned int) * n, cudaMemcpyDeviceToHost, st));
     w->launches += 2;
     if (w->debug) {
-        w->dbg_wcoarse.resize((size_t)n * RT);
-        GBR_CUDA(cudaMemcpyAsync(w->dbg_wcoarse.data(), dense_w, sizeof(float) * n * RT, cudaMemcpyDeviceToHost, st));
+        gbr_worker::DbgPass &D = w->dbg.back();
+        D.wcoarse.resize((size_t)n * RT);
+        GBR_CUDA(cudaMemcpyAsync(D.wcoarse.data(), dense_w, sizeof(float) * n * RT, cudaMemcpyDeviceToHost, st));
     }
     const long long nR = (long long)n * R;
     const long long nbj = fine_jobs_nblocks(nR);
@@ -850,13 +883,15 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
     }
     const auto t_final = std::chrono::steady_clock::now();
     if (w->debug) {
-        w->dbg_n = n;
-        w->dbg_cc.resize(n);
-        w->dbg_cf.resize(n);
+        gbr_worker::DbgPass &D = w->dbg.back();
+        D.dense = w->last_dense;
+        D.cc.resize(n);
+        D.cf.resize(n);
         for (int p = 0; p < n; ++p) {
-            w->dbg_cc[p] = psh[p].c_coarse;
-            w->dbg_cf[p] = psh[p].c_fine;
+            D.cc[p] = psh[p].c_coarse;
+            D.cf[p] = psh[p].c_fine;
         }
+        w->dbg_n += n;
     }
     // ---- per-particle finalisation (storeWeightedSums :8990-9150) ----
     for (int p = 0; p < n; ++p) {
@@ -1081,17 +1116,6 @@ int gbr_worker_create(gbr_bundle *b, gbr_worker **out) {
     }
     GBR_CUDA(cudaEventCreate(&w->ev_call));
     GBR_CUDA(cudaEventCreateWithFlags(&w->ev_inputs, cudaEventDisableTiming));
-    const char *dbg = std::getenv("GBR_DEBUG_FETCH");
-    w->debug = dbg && dbg[0] == '1';
-    const char *fm = std::getenv("GBR_FINE_MODE");
-    if (fm && std::strcmp(fm, "dense") == 0) w->fine_mode = 1;
-    if (fm && std::strcmp(fm, "sparse") == 0) w->fine_mode = 2;
-    const char *nm = std::getenv("GBR_COARSE_WEIGHTS");
-    if (nm && std::strcmp(nm, "full") == 0) w->coarse_rows = 1;
-    const char *cc = std::getenv("GBR_CAND_CAP");
-    if (cc && std::atoi(cc) > 0) w->cand_cap_max = std::atoi(cc);
-    const char *cb = std::getenv("GBR_CAND_BUF");
-    if (cb && std::atoi(cb) > 0) w->cand_buf = std::atoi(cb);
     *out = w.release();
     return GBR_OK;
 }
@@ -1099,6 +1123,27 @@ int gbr_worker_create(gbr_bundle *b, gbr_worker **out) {
 int gbr_worker_set_debug(gbr_worker *w, int on) {
     if (!w) return fail(GBR_ERR_INVALID, "null worker");
     w->debug = on ? 1 : 0;
+    return GBR_OK;
+}
+
+int gbr_worker_set_option(gbr_worker *w, int option, int64_t value) {
+    if (!w) return fail(GBR_ERR_INVALID, "null worker");
+    if (value < 0 || value > (1LL << 30)) return fail(GBR_ERR_INVALID, "option value out of range");
+    switch (option) {
+        case GBR_OPT_DEBUG: w->debug = value ? 1 : 0; break;
+        case GBR_OPT_FINE_MODE:
+            if (value > 2) return fail(GBR_ERR_INVALID, "fine mode must be 0 (auto), 1 (dense) or 2 (sparse)");
+            w->fine_mode = (int)value;
+            break;
+        case GBR_OPT_COARSE_ROWS:
+            if (value > 1) return fail(GBR_ERR_INVALID, "coarse rows must be 0 (skip far rows) or 1 (all)");
+            w->coarse_rows = (int)value;
+            break;
+        case GBR_OPT_CAND_CAP: w->cand_cap_max = value > 0 ? (int)value : (1 << 16); break;
+        case GBR_OPT_CAND_BUF: w->cand_buf = (int)value; break;
+        case GBR_OPT_BATCH_CAP: w->batch_cap = (int)value; break;
+        default: return fail(GBR_ERR_INVALID, "unknown worker option " + std::to_string(option));
+    }
     return GBR_OK;
 }
 
@@ -1115,8 +1160,8 @@ int gbr_expect_batch(gbr_worker *w, const gbr_particle_batch *batch, gbr_particl
     if (s) return s;
     const size_t full = (size_t)b->full_npix;
     const cudaMemcpyKind kind = batch->device_resident ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
-    for (int p0 = 0; p0 < n_all; p0 += w->cap) {
-        const int n = std::min(w->cap, n_all - p0);
+    for (int p0 = 0; p0 < n_all; p0 += w->pass_cap) {
+        const int n = std::min(w->pass_cap, n_all - p0);
         GBR_CUDA(cudaEventRecord(w->ev_in, w->st));
         // inputs already in the worker's buffers (gbr_expect_images prepares
         // into them) are not copied
@@ -1355,7 +1400,7 @@ int gbr_expect_images(gbr_worker *w, const gbr_image_batch *in, gbr_particle_res
     if (s) return s;
     // a call that fits one pass prepares straight into the E-step's input
     // buffers (no device-to-device copies of the Fourier images)
-    const bool in_place = (size_t)w->cap >= n;
+    const bool in_place = (size_t)w->pass_cap >= n;
     if (!in_place) {
         GBR_CUDA(w->pi_fimg.reserve(n * cur * X));
         GBR_CUDA(w->pi_fnm.reserve(n * cur * X));
@@ -1441,32 +1486,51 @@ int gbr_sampling_sizes(const gbr_bundle *b, int64_t *ndir, int64_t *npsi, int64_
 
 int64_t gbr_worker_debug_fetch(gbr_worker *w, int what, int64_t i, void *host, int64_t capacity) {
     if (!w || !host) return fail(GBR_ERR_INVALID, "null argument");
-    if (!w->debug) return fail(GBR_ERR_STATE, "debug read-back needs GBR_DEBUG_FETCH=1 at worker creation");
+    if (!w->debug) return fail(GBR_ERR_STATE, "debug read-back needs gbr_worker_set_debug before the call");
     if (i < 0 || i >= w->dbg_n) return fail(GBR_ERR_INVALID, "particle index out of range");
+    // the pass that held particle i of the call
+    size_t ip = 0;
+    while (i >= w->dbg[ip].n) i -= w->dbg[ip++].n;
+    const gbr_worker::DbgPass &D = w->dbg[ip];
     gbr_bundle *b = w->b;
     const long long RT = (long long)b->R * b->T;
+    const int nOR = (int)b->nOR, nOT = (int)b->nOT, T = (int)b->T;
     if (what == 0 || what == 1) {
         if (capacity < RT) return fail(GBR_ERR_INVALID, "capacity too small");
         double *o = static_cast<double *>(host);
-        const float *src = (what == 0 ? w->dbg_coarse.data() : w->dbg_wcoarse.data()) + (size_t)i * RT;
-        for (long long e = 0; e < RT; ++e)
-            o[e] = (what == 0) ? (std::isfinite(src[e]) ? w->dbg_cc[i] + (double)src[e] : INFINITY) : (double)src[e];
+        const float *src = (what == 0 ? D.coarse.data() : D.wcoarse.data()) + (size_t)i * RT;
+        if (what == 1) {
+            for (long long e = 0; e < RT; ++e) o[e] = (double)src[e];
+            return RT;
+        }
+        // sparse stores: the segments (32 consecutive columns of the pass's
+        // [particle][translation] axis) the coarse pass did not store are
+        // reported as +inf (poses beyond the skip distance)
+        const long long c0 = ((long long)i * T) >> 5;
+        for (long long e = 0; e < RT; ++e) {
+            const long long r = e / T, t = e % T;
+            bool stored = true;
+            if (D.sparse) {
+                const unsigned int seg = D.segmask[(size_t)i * b->R + r];
+                stored = (seg >> ((((long long)i * T + t) >> 5) - c0)) & 1u;
+            }
+            o[e] = (stored && std::isfinite(src[e])) ? D.cc[i] + (double)src[e] : INFINITY;
+        }
         return RT;
     }
-    const long long b0 = w->dbg_segf[i], b1 = w->dbg_segf[i + 1];
+    const long long b0 = D.segf[i], b1 = D.segf[i + 1];
     if (capacity < b1 - b0) return fail(GBR_ERR_INVALID, "capacity too small");
-    const int nOR = (int)b->nOR, nOT = (int)b->nOT, T = (int)b->T;
-    if (w->last_dense) {
+    if (D.dense) {
         // dense layout [rf][tf]: report the computed (finite diff2) entries
         const long long TF = (long long)T * nOT;
         long long m = 0;
         for (long long e = b0; e < b1; ++e) {
-            if (!std::isfinite(w->dbg_fine[e])) continue;
+            if (!std::isfinite(D.fine[e])) continue;
             const long long loc = e - b0, rf = loc / TF, tf = loc % TF;
             const long long r = rf / nOR, ior = rf % nOR, t = tf / nOT, iot = tf % nOT;
             if (what == 2) static_cast<int64_t *>(host)[m] = ((r * T + t) * nOR + ior) * nOT + iot;
-            else if (what == 3) static_cast<double *>(host)[m] = w->dbg_cf[i] + (double)w->dbg_fine[e];
-            else if (what == 4) static_cast<double *>(host)[m] = (double)w->dbg_wfine[e];
+            else if (what == 3) static_cast<double *>(host)[m] = D.cf[i] + (double)D.fine[e];
+            else if (what == 4) static_cast<double *>(host)[m] = (double)D.wfine[e];
             else return fail(GBR_ERR_INVALID, "unknown debug selector");
             ++m;
         }
@@ -1475,14 +1539,14 @@ int64_t gbr_worker_debug_fetch(gbr_worker *w, int what, int64_t i, void *host, i
     for (long long e = b0; e < b1; ++e) {
         const long long k = e - b0;
         if (what == 2) {
-            const FineJob &j = w->dbg_jobs[w->dbg_ejob[e]];
-            const unsigned code = w->dbg_ecode[e];
+            const FineJob &j = D.jobs[D.ejob[e]];
+            const unsigned code = D.ecode[e];
             const long long t = code / (nOR * nOT), ior = (code / nOT) % nOR, iot = code % nOT;
             static_cast<int64_t *>(host)[k] = (((long long)j.r * T + t) * nOR + ior) * nOT + iot;
         } else if (what == 3) {
-            static_cast<double *>(host)[k] = w->dbg_cf[i] + (double)w->dbg_fine[e];
+            static_cast<double *>(host)[k] = D.cf[i] + (double)D.fine[e];
         } else if (what == 4) {
-            static_cast<double *>(host)[k] = (double)w->dbg_wfine[e];
+            static_cast<double *>(host)[k] = (double)D.wfine[e];
         } else {
             return fail(GBR_ERR_INVALID, "unknown debug selector");
         }

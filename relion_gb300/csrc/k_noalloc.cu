@@ -19,8 +19,15 @@
 //     on the GPU (different streams, or different host threads, without
 //     ordering between them) race on it and give wrong results;
 //   * the first call on each device looks up the array's device address
-//     (cudaGetSymbolAddress) with that device current; make that first call
-//     before any stream capture.
+//     (cudaGetSymbolAddress) with that device current; with lazy module
+//     loading (the CUDA default) that lookup, or the first kernel launch,
+//     loads the library's device code, which may itself allocate device
+//     memory.  Make the first call on each device before any stream capture
+//     and outside any region that must not allocate; the guarantee holds for
+//     every call after it;
+//   * a row without a positive weight gets nr_significant 0 and threshold
+//     +inf (gbr_expect_batch reports such a particle as "zero sum of
+//     weights").
 #include "../../include/gbrelion.h"
 #include "gbr_internal.h"
 
@@ -99,11 +106,14 @@ __global__ void k_noalloc_hist0(const float *__restrict__ w, long long len, NoAl
         }
 }
 
+// A row without a positive weight has no threshold: nr_significant 0 and
+// threshold +inf (no weight passes w >= threshold).
 __global__ void k_noalloc_out(const NoAllocScratch *s, int n, float *thr, unsigned int *nsig) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p < n) {
-        thr[p] = s->ps[p].thr_coarse;
-        nsig[p] = s->ps[p].nr_sign;
+        const bool any = s->ps[p].sum_coarse > 0.;
+        thr[p] = any ? s->ps[p].thr_coarse : __int_as_float(0x7f800000);
+        nsig[p] = any ? s->ps[p].nr_sign : 0u;
     }
 }
 

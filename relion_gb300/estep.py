@@ -196,10 +196,20 @@ RESULT_DTYPE = np.dtype([(n, np.int64 if t is _lib.I64 else np.float64)
 assert RESULT_DTYPE.itemsize == C.sizeof(_lib.ParticleResult)
 
 
-class MlOptimiserCuda:
-    """One E-step worker (stream + batch buffers) on a bundle."""
+# gbr_worker_set_option selectors (include/gbrelion.h, gbr_worker_option)
+WORKER_OPTIONS = dict(debug=1, fine_mode=2, coarse_rows=3, cand_cap=4, cand_buf=5, batch_cap=6)
+FINE_MODES = dict(auto=0, dense=1, sparse=2)
+COARSE_ROWS = dict(skip=0, full=1)
 
-    def __init__(self, bundle, debug=False):
+
+class MlOptimiserCuda:
+    """One E-step worker (stream + batch buffers) on a bundle.
+
+    Keyword options (gbr_worker_set_option): fine_mode ("auto", "dense",
+    "sparse"), coarse_rows ("skip", "full"), cand_cap, cand_buf, batch_cap
+    (particles per pass of a call)."""
+
+    def __init__(self, bundle, debug=False, **options):
         self.bundle = bundle
         self.lib = bundle.lib
         h = C.c_void_p()
@@ -207,6 +217,18 @@ class MlOptimiserCuda:
         self.h = h
         if debug:
             check(self.lib.gbr_worker_set_debug(h, 1))
+        for k, v in options.items():
+            if v is not None:
+                self.set_option(k, v)
+
+    def set_option(self, name, value):
+        if name not in WORKER_OPTIONS:
+            raise ValueError("unknown worker option %r" % name)
+        if name == "fine_mode" and isinstance(value, str):
+            value = FINE_MODES[value]
+        if name == "coarse_rows" and isinstance(value, str):
+            value = COARSE_ROWS[value]
+        check(self.lib.gbr_worker_set_option(self.h, WORKER_OPTIONS[name], int(value)))
 
     def do_expectation_some_particles(self, batch):
         """Run the E-step on a batch (dict of host arrays, or device pointers).

@@ -5,16 +5,16 @@ orientation) row, and the coarse weight pass then reads only the rows whose
 minimum lies within xs of the particle's minimum.  Every pose left out
 weighs so little that all of them together stay below 1e-10 of the weight
 sum (xs = ln(R T) + ln(pmax / pmin) + ln(1e10)), so the E-step results must
-agree with the pass over all rows (GBR_COARSE_WEIGHTS=full): per-particle
+agree with the pass over all rows (worker option coarse_rows="full"): per-particle
 results to 1e-9 relative with identical significant counts and best poses,
 and the accumulated sums (sigma2 noise, backprojection), whose FP64 atomics
 run in a different order on every run, to 1e-6 relative L2.  The debug copy
-of the dense coarse weights must be identical too.  Without the debug
-read-back the coarse pass also stores only the row segments near the running
-minimum (sparse diff2 writes); the same bounds hold then, also when the
-candidate lists overflow and the significance search reruns on the full
-(partly unwritten) array (GBR_CAND_CAP small), and when the block-local
-candidate buffers overflow into direct appends (GBR_CAND_BUF small).
+of the dense coarse weights must be identical too.  The coarse pass also
+stores only the row segments near the running minimum (sparse diff2 writes,
+with or without the debug read-back); the same bounds hold then, also when
+the candidate lists overflow and the significance search reruns on the full
+(partly unwritten) array (option cand_cap small), and when the block-local
+candidate buffers overflow into direct appends (option cand_buf small).
 """
 import numpy as np
 import pytest
@@ -22,21 +22,12 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def _run(monkeypatch, ds, model, batch, mode=None, debug=True, cand_cap=None, cand_buf=None):
+def _run(ds, model, batch, mode=None, debug=True, cand_cap=None, cand_buf=None):
     from relion_gb300.estep import MlDeviceBundle, MlOptimiserCuda
-    monkeypatch.delenv("GBR_COARSE_WEIGHTS", raising=False)
-    monkeypatch.delenv("GBR_CAND_CAP", raising=False)
-    monkeypatch.delenv("GBR_CAND_BUF", raising=False)
-    if cand_buf:
-        monkeypatch.setenv("GBR_CAND_BUF", str(cand_buf))
-    if mode:
-        monkeypatch.setenv("GBR_COARSE_WEIGHTS", mode)
-    if cand_cap:
-        monkeypatch.setenv("GBR_CAND_CAP", str(cand_cap))
     b = MlDeviceBundle(model, device=0)
     r = ds.ref
     b.setup_projector(0, r["data"], r["yinit"], r["zinit"], r["r_max"], r["pad"])
-    w = MlOptimiserCuda(b, debug=debug)
+    w = MlOptimiserCuda(b, debug=debug, coarse_rows=mode, cand_cap=cand_cap, cand_buf=cand_buf)
     res = w.do_expectation_some_particles(batch)
     cw = [w.debug_fetch(1, i) for i in range(len(res))] if debug else None
     wsum = b.get_wsum()
@@ -53,7 +44,7 @@ def _rel(a, b):
 
 
 @pytest.mark.parametrize("seed", [17, 18])
-def test_row_skip_matches_full_coarse_pass(monkeypatch, seed):
+def test_row_skip_matches_full_coarse_pass(seed):
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
@@ -63,8 +54,8 @@ def test_row_skip_matches_full_coarse_pass(monkeypatch, seed):
                          offset_range_px=4.0, offset_step_px=1.0)
     model = ds.model(precision=1)
     batch = ds.particles(0, 12)
-    rf, cf, wf, df, gf = _run(monkeypatch, ds, model, batch, mode="full")
-    rn, cn, wn, dn, gn = _run(monkeypatch, ds, model, batch)
+    rf, cf, wf, df, gf = _run(ds, model, batch, mode="full")
+    rn, cn, wn, dn, gn = _run(ds, model, batch)
     assert np.array_equal(rf["nr_sign"], rn["nr_sign"])
     assert np.array_equal(rf["best_ihidden_over"], rn["best_ihidden_over"])
     for k in ("coarse_sum_weight", "coarse_significant_weight", "pmax", "dLL", "fine_sum_weight"):
@@ -78,7 +69,7 @@ def test_row_skip_matches_full_coarse_pass(monkeypatch, seed):
 
 
 @pytest.mark.parametrize("cand_cap,cand_buf", [(None, None), (16, None), (None, 8)])
-def test_sparse_writes_match_full_coarse_pass(monkeypatch, cand_cap, cand_buf):
+def test_sparse_writes_match_full_coarse_pass(cand_cap, cand_buf):
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
@@ -87,8 +78,8 @@ def test_sparse_writes_match_full_coarse_pass(monkeypatch, cand_cap, cand_buf):
                          offset_range_px=4.0, offset_step_px=1.0)
     model = ds.model(precision=1)
     batch = ds.particles(0, 12)
-    rf, _, wf, df, gf = _run(monkeypatch, ds, model, batch, mode="full", debug=False)
-    rn, _, wn, dn, gn = _run(monkeypatch, ds, model, batch, debug=False, cand_cap=cand_cap, cand_buf=cand_buf)
+    rf, _, wf, df, gf = _run(ds, model, batch, mode="full", debug=False)
+    rn, _, wn, dn, gn = _run(ds, model, batch, debug=False, cand_cap=cand_cap, cand_buf=cand_buf)
     assert np.array_equal(rf["nr_sign"], rn["nr_sign"])
     assert np.array_equal(rf["best_ihidden_over"], rn["best_ihidden_over"])
     for k in ("coarse_sum_weight", "coarse_significant_weight", "pmax", "dLL", "fine_sum_weight"):

@@ -28,6 +28,7 @@ def _case(name, seed, n, **kw):
 
 def _check(st, tol):
     print(st)
+    assert st["coarse_stored_all"], "coarse computed sets differ"
     assert st["coarse_diff2_rel"] <= tol["coarse_diff2_rel"]
     assert st["coarse_w_abs"] <= tol["weight_norm_abs"]
     assert st["fine_diff2_rel"] <= tol["fine_diff2_rel"]
@@ -41,15 +42,10 @@ def _check(st, tol):
     assert st["dLL_abs"] <= 1e-2
 
 
-@pytest.fixture(params=["dense", "sparse"])
-def fine_mode(request, monkeypatch):
-    monkeypatch.setenv("GBR_FINE_MODE", request.param)
-    return request.param
-
-
+@pytest.mark.parametrize("fine_mode", ["dense", "sparse"])
 def test_parity_order1(cmp, fine_mode):
     m, refs, b = _case("cfg0_box64", 11, 6, healpix_order=1, psi_step=30.0)
-    st = cmp.compare(m, refs, b)
+    st = cmp.compare(m, refs, b, fine_mode=fine_mode)
     assert st["sig_mismatch"] == 0 and st["fine_set_mismatch"] == 0
     _check(st, cmp.TOL)
 

@@ -1,0 +1,120 @@
+"""GPU parity at the box-256 workload, on the path the benchmark times.
+
+Box 256 px, 1.0 A/px, HEALPix order 3 (768 directions x 48 psi = 36,864
+coarse orientations), offsets +/-6 px step 1 (113 translations), first
+iteration sizes (current and coarse size 46 px), three seeded particles of
+the box-256 generator, against the FP64 oracle (the reference's CPU E-step,
+src/ml_optimiser.cpp:7098-9157).  The oracle runs once per module; every GPU
+run goes through the C ABI with the debug read-back, which copies the
+intermediate arrays per pass and changes nothing of the computation.
+
+(a) plain FP32 path: relative diff2 <= 1e-5 (coarse and fine), max
+    normalised-weight difference <= 1e-4, backprojected volumes relative
+    L2 <= 1e-5, identical significance and fine hidden-index sets, best pose
+    equal for every particle.
+(b) precision form exactly as timed: BF16 tcgen05 coarse cross term, coarse
+    rows skipped by their minimum, diff2 stored only near each particle's
+    running minimum, candidate lists and the radix-select threshold; the
+    fine pass in FP32.  The errors against the FP64 oracle are measured and
+    bounded: relative coarse diff2 <= 2e-5 on the stored poses, the oracle's
+    weight on unstored poses < 1e-9, normalised coarse weights within 0.05,
+    fine diff2 <= 1e-5 relative on the common fine poses, the oracle's fine
+    weight on poses the GPU did not evaluate <= 1e-3 (and the converse),
+    volumes within 1e-3 relative L2, best pose equal for every particle.
+(c) a call larger than the worker's pass capacity (one particle per pass):
+    per-particle results equal to the one-pass call (FP64 atomic sums in
+    another order: 1e-9 relative) and the same oracle bounds as (b).
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+N = 3
+
+
+@pytest.fixture(scope="module")
+def case(oracle_lib):
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from relion_gb300 import datagen
+    from oracle import pyoracle
+    ds = datagen.Dataset("cfg1_box256", seed=41, n_particles=N)
+    batch = ds.particles(0, N)
+    model = ds.model(precision=0)
+    ora = pyoracle.run(model, ds.refs, batch, debug=True)
+    return ds, batch, ora
+
+
+def _stats(case, precision, **opts):
+    from oracle import compare
+    ds, batch, ora = case
+    st = compare.compare(ds.model(precision=precision), ds.refs, batch, oracle_out=ora, **opts)
+    print(precision, opts, st)
+    return st
+
+
+def test_box256_plain_fp32(case):
+    from oracle import compare
+    st = _stats(case, 0)
+    tol = compare.TOL
+    assert st["coarse_stored_all"]
+    assert st["coarse_diff2_rel"] <= tol["coarse_diff2_rel"]
+    assert st["coarse_w_abs"] <= tol["weight_norm_abs"]
+    assert st["sig_mismatch"] == 0 and st["nr_sign_diff"] == 0
+    assert st["fine_set_mismatch"] == 0
+    assert st["fine_diff2_rel"] <= tol["fine_diff2_rel"]
+    assert st["fine_w_abs"] <= tol["weight_norm_abs"]
+    assert st["bp_data_rel_l2"] <= tol["bp_rel_l2"]
+    assert st["bp_weight_rel_l2"] <= tol["bp_rel_l2"]
+    assert st["argmax_agree"] == 1.0
+    assert st["sigma2_noise_rel"] <= 1e-5
+    assert st["pdf_direction_abs"] <= 1e-5
+
+
+def _check_precision_form(st):
+    assert st["coarse_stored_subset"]
+    assert st["coarse_diff2_rel"] <= 2e-5
+    assert st["coarse_unstored_mass"] < 1e-9
+    assert st["coarse_w_abs"] <= 0.05
+    assert st["fine_diff2_rel"] <= 1e-5
+    assert st["fine_missing_mass"] <= 1e-3
+    assert st["fine_extra_mass"] <= 1e-3
+    assert st["bp_data_rel_l2"] <= 1e-3
+    assert st["bp_weight_rel_l2"] <= 1e-3
+    assert st["argmax_agree"] == 1.0
+    assert st["sigma2_noise_rel"] <= 1e-3
+
+
+def test_box256_precision_form_as_timed(case):
+    st = _stats(case, 1)
+    # the timed configuration stores diff2 only near the running minimum
+    assert not st["coarse_stored_all"]
+    _check_precision_form(st)
+
+
+def _results(case, precision, **opts):
+    from relion_gb300.estep import MlDeviceBundle, MlOptimiserCuda
+    ds, batch, _ = case
+    b = MlDeviceBundle(ds.model(precision=precision), device=0)
+    r = ds.ref
+    b.setup_projector(0, r["data"], r["yinit"], r["zinit"], r["r_max"], r["pad"])
+    w = MlOptimiserCuda(b, **opts)
+    res = w.do_expectation_some_particles(batch)
+    data, weight = b.get_mdl_data(0)
+    w.close()
+    b.close()
+    return res, data, weight
+
+
+def test_box256_multi_pass_call(case):
+    one, d1, w1 = _results(case, 1)
+    multi, dm, wm = _results(case, 1, batch_cap=1)
+    assert np.array_equal(one["nr_sign"], multi["nr_sign"])
+    assert np.array_equal(one["best_ihidden_over"], multi["best_ihidden_over"])
+    for k in ("coarse_sum_weight", "coarse_significant_weight", "pmax", "dLL", "fine_sum_weight"):
+        np.testing.assert_allclose(multi[k], one[k], rtol=1e-9, err_msg=k)
+    assert np.linalg.norm(dm - d1) <= 1e-6 * np.linalg.norm(d1)
+    assert np.linalg.norm(wm - w1) <= 1e-6 * np.linalg.norm(w1)
+    _check_precision_form(_stats(case, 1, batch_cap=1))
