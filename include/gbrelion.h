@@ -186,6 +186,33 @@ int gbr_worker_set_option(gbr_worker *w, int option, int64_t value);
  * backprojection into the bundle's volumes.  `res` has batch->n entries. */
 int gbr_expect_batch(gbr_worker *w, const gbr_particle_batch *batch, gbr_particle_result *res);
 
+/* ---- coarse pass restricted to proposed orientations ------------------
+ * No counterpart in the reference: its coarse pass scores every orientation
+ * (getAllSquaredDifferencesCoarse, src/acc/acc_ml_optimiser_impl.h:1016-1414;
+ * CPU src/ml_optimiser.cpp:7098-7700).  Here each particle may score only a
+ * set of orientation blocks, e.g. the ones a pose-proposal network puts its
+ * mass on, with the exhaustive search kept for particles whose list starts
+ * with GBR_ALL_BLOCKS.  A block is one parent HEALPix pixel: the four sibling
+ * directions 4 j .. 4 j + 3 of the coarse NEST grid (of class
+ * block / (ndir / 4)), with every psi angle and every translation.  Poses in
+ * blocks a particle does not score get weight zero; significance, the fine
+ * pass, the weighted sums and the backprojection then run as in
+ * gbr_expect_batch.  Precision form only (tcgen05), 3D grids with
+ * 4 x npsi a multiple of 32 and at most 256, at most 128 translations;
+ * GBR_ERR_UNSUPPORTED otherwise. */
+#define GBR_ALL_BLOCKS (-2)
+
+/* Number of orientation blocks (K x ndir / 4), directions per block (4) and
+ * projection-table rows per block (4 npsi). */
+int gbr_orientation_blocks(const gbr_bundle *b, int64_t *nblocks, int64_t *dirs_per_block, int64_t *rows_per_block);
+
+/* gbr_expect_batch with the coarse pass restricted per particle: blocks is
+ * host int32 [batch->n][m]; row i lists the blocks particle i scores
+ * (negative entries are ignored, repeats scored once), or starts with
+ * GBR_ALL_BLOCKS for the exhaustive search. */
+int gbr_expect_batch_blocks(gbr_worker *w, const gbr_particle_batch *batch, const int32_t *blocks, int64_t m,
+                            gbr_particle_result *res);
+
 /* ---- image preparation (the step before the search) ------------------- */
 
 /* Optics and masking of MlOptimiser::getFourierTransformsAndCtfs. */

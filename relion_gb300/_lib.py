@@ -92,6 +92,8 @@ EXPORTS = {
     "gbr_worker_set_debug": (C.c_int, [P, C.c_int]),
     "gbr_worker_set_option": (C.c_int, [P, C.c_int, I64]),
     "gbr_expect_batch": (C.c_int, [P, C.POINTER(ParticleBatch), P]),
+    "gbr_orientation_blocks": (C.c_int, [P, C.POINTER(I64), C.POINTER(I64), C.POINTER(I64)]),
+    "gbr_expect_batch_blocks": (C.c_int, [P, C.POINTER(ParticleBatch), P, I64, P]),
     "gbr_bundle_set_optics": (C.c_int, [P, C.POINTER(OpticsDesc)]),
     "gbr_prepare_images": (C.c_int, [P, C.POINTER(ImageBatch), P, P, P, P, P, P]),
     "gbr_expect_images": (C.c_int, [P, C.POINTER(ImageBatch), P]),

@@ -175,6 +175,8 @@ struct gbr_bundle {
     DevBuf<float> proj_c, proj2_c;
     DevBuf<unsigned char> proj_c_tc;  // precision form: BF16 A tiles (tcgen05 smem image)
     DevBuf<unsigned char> proj2_c_tf; // precision form: TF32 split tiles of |P|^2 (norm term)
+    DevBuf<unsigned char> proj_c_blk; // orientation-block tiles of the BF16 table (restricted coarse pass)
+    bool blk_ready = false;
     DevBuf<float> proj_f, proj2_f;  // all oversampled orientations: [RF][lda_f], [RF][ldk_f]
     int ldk_f = 0, lda_f = 0;
     DevBuf<float2> bpimg;
@@ -273,6 +275,16 @@ struct gbr_worker {
     int last_dense = 0;
     DevBuf<float> Wt, Wp, Zt, CM, S2P, fnrm;
     DevBuf<float2> G;
+    // coarse pass restricted to orientation blocks (gbr_expect_batch_blocks):
+    // the caller's [n_all][restrict_m] block lists, the first particle of the
+    // current pass and the pass's (particle, block) work items
+    const int32_t *restrict_blocks = nullptr;
+    int64_t restrict_m = 0;
+    int pass_p0 = 0;
+    long long last_items = 0;  // work items of the last restricted pass
+    PinnedBuf<int2> items_h;
+    DevBuf<int2> items_d;
+    DevBuf<unsigned char> ytp;  // per-particle BF16 Y tiles of the restricted pass
     int batch_cap = 0;           // particles per pass (GBR_OPT_BATCH_CAP; 0 = from the budget)
     int pass_cap = 0;            // particles per pass of the current call
     // debug copies of the last call, one entry per pass (gbr_worker_debug_fetch)
@@ -298,6 +310,7 @@ namespace {
 
 int build_tables(gbr_bundle *b) {
     if (b->tables_ready) return GBR_OK;
+    b->blk_ready = false;
     if (!b->have_arrays) return fail(GBR_ERR_STATE, "model arrays not set (gbr_model_set_arrays)");
     for (long k = 0; k < b->K; ++k)
         if (!b->have_vol[k]) return fail(GBR_ERR_STATE, "reference of class " + std::to_string(k) + " not uploaded");
@@ -684,6 +697,78 @@ int fine_dense(gbr_worker *w, int n, long long &seg_len) {
     return GBR_OK;
 }
 
+// Orientation blocks of the restricted coarse pass: four sibling HEALPix
+// directions (one parent pixel in NEST order) with every psi angle, i.e.
+// NB = 4 npsi consecutive rows of the projection table.
+constexpr int kDirsPerBlock = 4;
+
+int restricted_supported(const gbr_bundle *b) {
+    if (b->d.precision != GBR_PREC_BF16)
+        return fail(GBR_ERR_UNSUPPORTED, "restricted coarse pass needs the precision form (tcgen05)");
+    if (b->is2d || b->ND % kDirsPerBlock != 0)
+        return fail(GBR_ERR_UNSUPPORTED, "restricted coarse pass needs a 3D HEALPix grid of order >= 1");
+    const long NB = kDirsPerBlock * b->NP;
+    if (NB % 32 != 0 || NB > 256)
+        return fail(GBR_ERR_UNSUPPORTED, "restricted coarse pass needs 4 x psi samples = a multiple of 32, <= 256");
+    if (b->T > 128) return fail(GBR_ERR_UNSUPPORTED, "restricted coarse pass needs at most 128 translations");
+    return GBR_OK;
+}
+
+// The coarse cross term of the pass's particles over their own blocks: one
+// (particle, block) work item per block a particle scores, in chunks of 64
+// particles and block-major inside a chunk (a block's tiles are read from HBM
+// once per chunk, the chunk's particle tiles stay in L2).
+int restricted_coarse(gbr_worker *w, int n, unsigned int *segmask) {
+    gbr_bundle *b = w->b;
+    const int R = (int)b->R, T = (int)b->T, NB = kDirsPerBlock * (int)b->NP;
+    const int nblk = R / NB;
+    const int K2 = 2 * b->nc;
+    if (!b->blk_ready) {
+        GBR_CUDA(b->proj_c_blk.reserve(tc_blocks_bytes(R, K2, NB)));
+        GBR_CUDA(launch_tc_pack_blocks(b->proj_c.p, b->lda_c, R, K2, NB, b->proj_c_blk.p, w->st));
+        b->blk_ready = true;
+        w->launches += 1;
+    }
+    std::vector<std::vector<int>> by_block(nblk);
+    std::vector<char> seen(nblk);
+    GBR_CUDA(w->items_h.reserve((size_t)n * nblk));
+    long long ni = 0;
+    for (int c0 = 0; c0 < n; c0 += 64) {
+        const int c1 = std::min(n, c0 + 64);
+        for (auto &v : by_block) v.clear();
+        for (int p = c0; p < c1; ++p) {
+            const int32_t *row = w->restrict_blocks + (size_t)(w->pass_p0 + p) * w->restrict_m;
+            if (w->restrict_m > 0 && row[0] == GBR_ALL_BLOCKS) {
+                for (int o = 0; o < nblk; ++o) by_block[o].push_back(p);
+                continue;
+            }
+            std::fill(seen.begin(), seen.end(), 0);
+            for (int64_t j = 0; j < w->restrict_m; ++j) {
+                const int32_t o = row[j];
+                if (o < 0) continue;
+                if (o >= nblk) return fail(GBR_ERR_INVALID, "orientation block " + std::to_string(o) +
+                                                                " out of range (" + std::to_string(nblk) + " blocks)");
+                if (!seen[o]) {
+                    seen[o] = 1;
+                    by_block[o].push_back(p);
+                }
+            }
+        }
+        for (int o = 0; o < nblk; ++o)
+            for (int p : by_block[o]) w->items_h.p[ni++] = make_int2(p, o);
+    }
+    w->last_items = ni;
+    if (ni == 0) return fail(GBR_ERR_NUMERICAL, "no orientation block to score in this batch");
+    GBR_CUDA(w->items_d.reserve(ni));
+    GBR_CUDA(cudaMemcpyAsync(w->items_d.p, w->items_h.p, sizeof(int2) * ni, cudaMemcpyHostToDevice, w->st));
+    GBR_CUDA(w->ytp.reserve(tc_yp_bytes(n, K2)));
+    GBR_CUDA(launch_tc_blocks(b->proj_c_blk.p, NB, w->ytp.p, R, K2, w->b_c.p, b->ldk_c, b->phase_c.p, b->ldk_c, n, T,
+                              w->items_d.p, (int)ni, w->vals.p, w->nrm.p, b->pdf_orient.p, w->ps.p, w->rowmin.p,
+                              segmask, w->st));
+    w->launches += 2;  // particle tiles + tensor-core kernel
+    return GBR_OK;
+}
+
 // One sub-batch of n <= cap particles whose inputs are already in w->X etc.
 int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h, gbr_particle_result *res) {
     gbr_bundle *b = w->b;
@@ -718,10 +803,12 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
         w->launches += 3;  // prep, pdf_offset, norms
     }
     GBR_CUDA(cudaEventRecord(w->ev[2], st));
-    const bool use_rowmin = d.precision == GBR_PREC_BF16 && T >= 32 && w->coarse_rows == 0;
+    const bool restricted = w->restrict_blocks != nullptr;
+    const bool use_rowmin = d.precision == GBR_PREC_BF16 && (restricted || (T >= 32 && w->coarse_rows == 0));
     // sparse diff2 writes: only row segments near the running minimum are
-    // stored (the debug read-back reports the others as not computed)
-    const bool sparse = use_rowmin && T <= 960;
+    // stored (the debug read-back reports the others as not computed); the
+    // restricted pass stores the rows of the blocks it scores
+    const bool sparse = use_rowmin && (restricted || T <= 960);
     if (w->debug) {
         w->dbg.emplace_back();
         w->dbg.back().n = n;
@@ -736,7 +823,10 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
         GBR_CUDA(cudaMemsetAsync(w->segmask.p, 0, sizeof(unsigned int) * (size_t)n * R, st));
     }
     unsigned int *segmask = sparse ? w->segmask.p : nullptr;
-    if (d.precision == GBR_PREC_BF16) {
+    if (restricted) {
+        int s2 = restricted_coarse(w, n, segmask);
+        if (s2) return s2;
+    } else if (d.precision == GBR_PREC_BF16) {
         GBR_CUDA(w->ytc.reserve(tc_y_bytes(n * T, 2 * b->nc)));
         GBR_CUDA(launch_tc_diff2(b->proj_c_tc.p, w->ytc.p, R, 2 * b->nc, w->b_c.p, b->ldk_c, b->phase_c.p, b->ldk_c, n,
                                  T, w->vals.p, w->nrm.p, b->pdf_orient.p, w->ps.p,
@@ -1200,10 +1290,34 @@ int gbr_expect_batch(gbr_worker *w, const gbr_particle_batch *batch, gbr_particl
             std::memcpy(power, batch->power_img + (size_t)b->nshell * p0, sizeof(double) * b->nshell * n);
             GBR_CUDA(cudaMemcpyAsync(w->pdat.p, pdat, sizeof(double) * n * 8, cudaMemcpyHostToDevice, w->st));
         }
+        w->pass_p0 = p0;
         s = run_batch(w, n, power, pdat, res + p0);
         if (s) return s;
     }
     return GBR_OK;
+}
+
+int gbr_orientation_blocks(const gbr_bundle *b, int64_t *nblocks, int64_t *dirs_per_block, int64_t *rows_per_block) {
+    if (!b) return fail(GBR_ERR_INVALID, "null bundle");
+    int s = restricted_supported(b);
+    if (s) return s;
+    if (nblocks) *nblocks = b->R / (kDirsPerBlock * b->NP);
+    if (dirs_per_block) *dirs_per_block = kDirsPerBlock;
+    if (rows_per_block) *rows_per_block = kDirsPerBlock * b->NP;
+    return GBR_OK;
+}
+
+int gbr_expect_batch_blocks(gbr_worker *w, const gbr_particle_batch *batch, const int32_t *blocks, int64_t m,
+                            gbr_particle_result *res) {
+    if (!w || !batch || !blocks || m <= 0) return fail(GBR_ERR_INVALID, "null argument or empty block lists");
+    int s = restricted_supported(w->b);
+    if (s) return s;
+    w->restrict_blocks = blocks;
+    w->restrict_m = m;
+    s = gbr_expect_batch(w, batch, res);
+    w->restrict_blocks = nullptr;
+    w->restrict_m = 0;
+    return s;
 }
 
 int gbr_bundle_set_optics(gbr_bundle *b, const gbr_optics_desc *optics) {

@@ -109,6 +109,20 @@ cudaError_t launch_tc_pack_a(const float *src, int lds, int M, int K2, void *dst
 cudaError_t launch_tc_diff2(const void *Ablk, void *Yblk, int M, int K2, const float2 *b, int ldb, const float2 *E,
                             int lde, int nparticles, int T, float *out, const float *norm, const float *pdf_orient,
                             ParticleState *ps, unsigned int *rowmin, unsigned int *segmask, cudaStream_t st);
+// Coarse cross term restricted to orientation blocks (precision form):
+// blocks of NB consecutive rows of the projection table (NB % 32 == 0,
+// NB <= 256, M % NB == 0) packed once per iteration; one work item per
+// (particle, block) pair of `items`; needs T <= 128.  Scored rows are stored
+// whole with their row minimum (rowmin, set to ~0 by the caller) and all
+// segments marked in segmask (zeroed by the caller); other rows stay
+// unscored.
+size_t tc_blocks_bytes(int M, int K2, int NB);
+size_t tc_yp_bytes(int nparticles, int K2);
+cudaError_t launch_tc_pack_blocks(const float *src, int lds, int M, int K2, int NB, void *dst, cudaStream_t st);
+cudaError_t launch_tc_blocks(const void *Bblk, int NB, void *Yp, int M, int K2, const float2 *b, int ldb,
+                             const float2 *E, int lde, int nparticles, int T, const int2 *items, int nitems,
+                             float *out, const float *norm, const float *pdf_orient, ParticleState *ps,
+                             unsigned int *rowmin, unsigned int *segmask, cudaStream_t st);
 // Read (and optionally clear) the tensor-core pipeline error flag.
 cudaError_t tc_error_flag(int *flag, int reset);
 cudaError_t tc_error_flag_async(int *host_flag, cudaStream_t st);

@@ -527,21 +527,11 @@ __global__ void k_pack_a(const float *__restrict__ src, int lds, int M, int K2, 
         make_uint4(pack_bf16(f[0], f[1]), pack_bf16(f[2], f[3]), pack_bf16(f[4], f[5]), pack_bf16(f[6], f[7]));
 }
 
-// B operand tiles: Y[(p,t)][2j+c] = Re/Im(b[p][j] E[t][j]) in BF16, blocked
-// per (N tile, K tile) in the same image.
-__global__ void k_pack_y(const float2 *__restrict__ b, int ldb, const float2 *__restrict__ E, int lde, int npix,
-                         int T, int N, int ktiles, uint8_t *__restrict__ dst, long long nchunks) {
-    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= nchunks) return;
-    const long long blk = c >> 11;  // 2048 chunks per B block
-    const int within = (int)(c & 2047), row = within >> 3, kg = within & 7;
-    const int nt = (int)(blk / ktiles), kt = (int)(blk - (long long)nt * ktiles);
-    const int n = nt * TN + row;
-    float y[8];
-#pragma unroll
-    for (int i = 0; i < 8; ++i) y[i] = 0.f;
-    if (n < N) {
-        const int p = n / T, t = n - p * T;
+// Eight BF16-bound values Y[(p,t)][8 kg .. 8 kg + 7] of K tile kt:
+// Re/Im(b[p][j] E[t][j]) for the four pixels j of the chunk (zeros beyond npix).
+__device__ __forceinline__ void y_chunk(const float2 *__restrict__ b, int ldb, const float2 *__restrict__ E,
+                                        int lde, int npix, int p, int t, int kt, int kg, float (&y)[8]) {
+    {
         const int j = kt * (TK / 2) + kg * 4;
         if (j + 4 <= ldb && j + 4 <= lde) {
             // rows padded to 16 pixels: two 16-byte loads each (zeros beyond npix)
@@ -565,6 +555,25 @@ __global__ void k_pack_y(const float2 *__restrict__ b, int ldb, const float2 *__
                     y[2 * q + 1] = x.x * e.y + x.y * e.x;
                 }
         }
+    }
+}
+
+// B operand tiles: Y[(p,t)][2j+c] = Re/Im(b[p][j] E[t][j]) in BF16, blocked
+// per (N tile, K tile) in the same image.
+__global__ void k_pack_y(const float2 *__restrict__ b, int ldb, const float2 *__restrict__ E, int lde, int npix,
+                         int T, int N, int ktiles, uint8_t *__restrict__ dst, long long nchunks) {
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nchunks) return;
+    const long long blk = c >> 11;  // 2048 chunks per B block
+    const int within = (int)(c & 2047), row = within >> 3, kg = within & 7;
+    const int nt = (int)(blk / ktiles), kt = (int)(blk - (long long)nt * ktiles);
+    const int n = nt * TN + row;
+    float y[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) y[i] = 0.f;
+    if (n < N) {
+        const int p = n / T, t = n - p * T;
+        y_chunk(b, ldb, E, lde, npix, p, t, kt, kg, y);
     }
     *reinterpret_cast<uint4 *>(dst + blk * B_BYTES + chunk_off(row, kg)) =
         make_uint4(pack_bf16(y[0], y[1]), pack_bf16(y[2], y[3]), pack_bf16(y[4], y[5]), pack_bf16(y[6], y[7]));
@@ -611,6 +620,255 @@ __global__ void k_pack_tf32(const float *__restrict__ src, int lds, int rows, in
     }
     *reinterpret_cast<uint4 *>(dst + blk * (long long)(rows_t * 128) + chunk_off(row, kg)) =
         make_uint4(u[0], u[1], u[2], u[3]);
+}
+
+// ---- coarse pass restricted to orientation blocks -------------------------
+// The same contraction with the roles of the operands exchanged, so that
+// every particle can score its own set of orientations: the MMA's M axis is
+// one particle's translations (T <= 128, rows beyond T zero) and its N axis
+// one orientation block of NB consecutive rows of the projection table (the
+// four sibling HEALPix directions of one parent pixel, every psi: NB = 4
+// npsi).  A work item is one (particle, block) pair; the item list holds
+// each particle's proposed blocks (all blocks for a particle that falls back
+// to the exhaustive search), so restricted and exhaustive particles share
+// one launch.  TMEM holds [translation][orientation]: for one accumulator
+// column (an orientation row r) the 32 lanes of a warp are 32 consecutive
+// translations, stored as one 128-byte segment of out[p][r][t].  Every
+// scored row is stored whole, its row minimum recorded in rowmin and all of
+// its 32-column segments marked in segmask; rows of blocks a particle did
+// not score keep rowmin = ~0 and segmask = 0 (weight zero downstream).
+constexpr int PB_MAX_N = 256;
+constexpr int PB_A_BYTES = TM * TK * 2;                          // 16 KB: 128 translations x 64 K
+constexpr int PB_STAGE_BYTES = PB_A_BYTES + PB_MAX_N * TK * 2;   // 48 KB
+constexpr int PB_SMEM_BYTES = STAGES * PB_STAGE_BYTES;
+
+struct TbArgs {
+    const uint8_t *Yp;      // [nparticles][ktiles][PB_A_BYTES] per-particle Y tiles (rows = translations)
+    const uint8_t *Bblk;    // [nblocks][ktiles][NB * 128] projection rows of each block
+    const int2 *items;      // (particle, block) pairs
+    int nitems, ktiles, NB, M, T;
+    float *out;             // [p][M][T]
+    const float *norm;      // [p][M]
+    const float *pdf_orient;
+    ParticleState *ps;
+    unsigned int *rowmin;   // [p][M]
+    unsigned int *segmask;  // [p][M]
+};
+
+__host__ __device__ constexpr uint32_t make_idesc_n(int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(TM >> 4) << 24);
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// Persistent CTA per SM over the item list (items blockIdx.x + i gridDim.x),
+// with the warp roles, stage ring, double-buffered accumulators and bounded
+// waits of k_tc_diff2.
+__global__ void __launch_bounds__(THREADS, 1) k_tc_blocks(const TbArgs a) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ __align__(8) uint64_t full[STAGES];
+    __shared__ __align__(8) uint64_t empty[STAGES];
+    __shared__ __align__(8) uint64_t tfull[2];
+    __shared__ __align__(8) uint64_t tempty[2];
+    __shared__ __align__(8) uint64_t done;
+    __shared__ uint32_t tmem_slot;
+    __shared__ int sfail;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int nk = a.ktiles;
+    const uint32_t bbytes = (uint32_t)a.NB * (TK * 2);
+    volatile int *vfail = &sfail;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                     "r"(TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        for (int s = 0; s < STAGES; ++s) {
+            mbar_init(smem_u32(&full[s]), 1);
+            mbar_init(smem_u32(&empty[s]), 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(smem_u32(&tfull[b]), 1);
+            mbar_init(smem_u32(&tempty[b]), EPI_WARPS);
+        }
+        mbar_init(smem_u32(&done), 1);
+        sfail = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_slot;
+    const uint32_t sbase = smem_u32(smem);
+
+    if (warp == 0 && lane == 0) {
+        uint32_t g = 0;
+        for (int it = blockIdx.x; it < a.nitems && !*vfail; it += gridDim.x) {
+            const int2 item = a.items[it];
+            const uint8_t *yb = a.Yp + (size_t)item.x * nk * PB_A_BYTES;
+            const uint8_t *bb = a.Bblk + (size_t)item.y * nk * bbytes;
+            for (int kt = 0; kt < nk; ++kt, ++g) {
+                const uint32_t s = g % STAGES;
+                if (g >= STAGES && !mbar_wait(smem_u32(&empty[s]), ((g / STAGES) - 1) & 1u)) {
+                    *vfail = 1;
+                    break;
+                }
+                const uint32_t st = sbase + s * PB_STAGE_BYTES;
+                arrive_expect_tx(smem_u32(&full[s]), (uint32_t)PB_A_BYTES + bbytes);
+                bulk_g2s(st, yb + (size_t)kt * PB_A_BYTES, PB_A_BYTES, smem_u32(&full[s]));
+                bulk_g2s(st + PB_A_BYTES, bb + (size_t)kt * bbytes, bbytes, smem_u32(&full[s]));
+            }
+        }
+        for (uint32_t q = g > (uint32_t)STAGES ? g - STAGES : 0u; q < g; ++q)
+            if (!mbar_wait(smem_u32(&full[q % STAGES]), (q / STAGES) & 1u)) *vfail = 1;
+    } else if (warp == 1 && lane == 0) {
+        const uint32_t idesc = make_idesc_n(a.NB);
+        uint32_t g = 0, i = 0;
+        for (int it = blockIdx.x; it < a.nitems && !*vfail; it += gridDim.x, ++i) {
+            const uint32_t b = i & 1u;
+            if (i >= 2 && !mbar_wait(smem_u32(&tempty[b]), ((i >> 1) - 1) & 1u)) {
+                *vfail = 1;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t acc = tmem + b * (uint32_t)PB_MAX_N;
+            bool ok = true;
+            for (int kt = 0; kt < nk; ++kt, ++g) {
+                const uint32_t s = g % STAGES;
+                if (!mbar_wait(smem_u32(&full[s]), (g / STAGES) & 1u)) {
+                    ok = false;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t a0 = sbase + s * PB_STAGE_BYTES, b0 = a0 + PB_A_BYTES;
+#pragma unroll
+                for (int kk = 0; kk < TK / 16; ++kk) {
+                    const uint64_t ad = make_desc(a0 + kk * 256, 128, 1024);
+                    const uint64_t bd = make_desc(b0 + kk * 256, 128, 1024);
+                    mma_bf16(acc, ad, bd, idesc, (kt | kk) != 0 ? 1u : 0u);
+                }
+                mma_commit(smem_u32(&empty[s]));
+            }
+            if (!ok) {
+                *vfail = 1;
+                break;
+            }
+            mma_commit(smem_u32(&tfull[b]));
+        }
+        mma_commit(smem_u32(&done));
+    } else if (warp >= 4) {
+        // warp (q, h): TMEM lanes 32 q.. (translations), columns h NB/2.. (rows)
+        const int q = warp & 3, h = (warp - 4) >> 2;
+        const int t = q * 32 + lane;
+        const bool tv = t < a.T;
+        const int half = a.NB >> 1;
+        uint32_t i = 0;
+        for (int it = blockIdx.x; it < a.nitems && !*vfail; it += gridDim.x, ++i) {
+            const uint32_t b = i & 1u;
+            if (!mbar_wait(smem_u32(&tfull[b]), (i >> 1) & 1u)) {
+                *vfail = 1;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const int2 item = a.items[it];
+            const int p = item.x;
+            const size_t prow = (size_t)p * a.M;
+            const int rbase = item.y * a.NB;
+            // all 32-column segments of a row of particle p
+            const int c0 = (p * a.T) >> 5, nch = ((p * a.T + a.T - 1) >> 5) - c0 + 1;
+            const unsigned int segbits = nch >= 32 ? 0xFFFFFFFFu : ((1u << nch) - 1u);
+            float pmin = __int_as_float(0x7f800000);
+            for (int col = h * half; col < (h + 1) * half; col += 16) {
+                float v[16];
+                tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + b * (uint32_t)PB_MAX_N + (uint32_t)col, v);
+                unsigned int myrow = 0xFFFFFFFFu;
+#pragma unroll
+                for (int jj = 0; jj < 16; ++jj) {
+                    const int r = rbase + col + jj;
+                    const float pdf = __ldg(&a.pdf_orient[r]);
+                    const float nrm = __ldg(&a.norm[prow + r]);
+                    const float d = (tv && pdf > 0.f) ? nrm - 2.f * v[jj] : __int_as_float(0x7f800000);
+                    if (tv) a.out[(prow + r) * a.T + t] = d;
+                    pmin = fminf(pmin, d);
+                    const unsigned int u = d < __int_as_float(0x7f800000) ? f2ord(d) : 0xFFFFFFFFu;
+                    const unsigned int m = __reduce_min_sync(0xffffffffu, u);
+                    if (lane == jj) myrow = m;
+                }
+                if (lane < 16) {
+                    const size_t e = prow + rbase + col + lane;
+                    if (myrow != 0xFFFFFFFFu) atomicMin(&a.rowmin[e], myrow);
+                    if (q == 0) a.segmask[e] = segbits;
+                }
+            }
+            warp_min_flush(pmin, &a.ps[p].min_coarse);
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0)
+                asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tempty[b]))
+                             : "memory");
+        }
+    }
+    __syncwarp();
+    if (warp == 0) {
+        bool ok = true;
+        if (lane == 0) ok = mbar_wait(smem_u32(&done), 0u);
+        ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+        if (!ok && lane == 0) *vfail = 1;
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (tid == 0 && *vfail) atomicCAS(&g_tc_error, 0, 1);
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+    }
+}
+
+// Per-particle Y tiles: rows = translations t < T of particle p (zero rows
+// up to 128), [p][kt] tiles of PB_A_BYTES in the shared-memory image.
+__global__ void k_pack_yp(const float2 *__restrict__ b, int ldb, const float2 *__restrict__ E, int lde, int npix,
+                          int T, int ktiles, uint8_t *__restrict__ dst, long long nchunks) {
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nchunks) return;
+    const long long blk = c >> 10;  // 1024 chunks per 128-row tile
+    const int within = (int)(c & 1023), row = within >> 3, kg = within & 7;
+    const int p = (int)(blk / ktiles), kt = (int)(blk - (long long)p * ktiles);
+    float y[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) y[i] = 0.f;
+    if (row < T) y_chunk(b, ldb, E, lde, npix, p, row, kt, kg, y);
+    *reinterpret_cast<uint4 *>(dst + blk * PB_A_BYTES + chunk_off(row, kg)) =
+        make_uint4(pack_bf16(y[0], y[1]), pack_bf16(y[2], y[3]), pack_bf16(y[4], y[5]), pack_bf16(y[6], y[7]));
+}
+
+// Projection rows in tiles of rows_t rows (one orientation block) x 64 K.
+__global__ void k_pack_rows(const float *__restrict__ src, int lds, int M, int K2, int ktiles, int rows_t,
+                            uint8_t *__restrict__ dst, long long nchunks) {
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nchunks) return;
+    const int per = rows_t * 8;
+    const long long blk = c / per;
+    const int within = (int)(c - blk * per), row = within >> 3, kg = within & 7;
+    const int mt = (int)(blk / ktiles), kt = (int)(blk - (long long)mt * ktiles);
+    const int m = mt * rows_t + row, k0 = kt * TK + kg * 8;
+    float f[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) f[i] = (m < M && k0 + i < K2) ? src[(size_t)m * lds + k0 + i] : 0.f;
+    *reinterpret_cast<uint4 *>(dst + blk * (long long)(rows_t * TK * 2) + chunk_off(row, kg)) =
+        make_uint4(pack_bf16(f[0], f[1]), pack_bf16(f[2], f[3]), pack_bf16(f[4], f[5]), pack_bf16(f[6], f[7]));
 }
 
 }  // namespace
@@ -705,6 +963,54 @@ cudaError_t launch_tc_norm(const void *Ablk, const float *w, int ldw, int M, int
     TcArgs a{static_cast<const uint8_t *>(Ablk), static_cast<const uint8_t *>(Bblk), M, 3 * nk, 1, nparticles,
              nparticles, mtiles, ntiles, out, nullptr, nullptr, nullptr, nullptr, nullptr};
     k_tc_diff2<true><<<grid, THREADS, SMEM_BYTES, st>>>(a);
+    return cudaGetLastError();
+}
+
+// ---- orientation-block restricted coarse pass ------------------------------
+size_t tc_blocks_bytes(int M, int K2, int NB) {
+    return (size_t)((M + NB - 1) / NB) * ((K2 + TK - 1) / TK) * (size_t)NB * TK * 2;
+}
+size_t tc_yp_bytes(int nparticles, int K2) { return (size_t)nparticles * ((K2 + TK - 1) / TK) * PB_A_BYTES; }
+
+cudaError_t launch_tc_pack_blocks(const float *src, int lds, int M, int K2, int NB, void *dst, cudaStream_t st) {
+    if (NB < 32 || NB > PB_MAX_N || NB % 32 != 0) return cudaErrorInvalidValue;
+    const int ktiles = (K2 + TK - 1) / TK, nblk = (M + NB - 1) / NB;
+    const long long nchunks = (long long)nblk * ktiles * NB * 8;
+    if (nchunks <= 0) return cudaSuccess;
+    k_pack_rows<<<(unsigned)((nchunks + 255) / 256), 256, 0, st>>>(src, lds, M, K2, ktiles, NB,
+                                                                  static_cast<uint8_t *>(dst), nchunks);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tc_blocks(const void *Bblk, int NB, void *Yp, int M, int K2, const float2 *b, int ldb,
+                             const float2 *E, int lde, int nparticles, int T, const int2 *items, int nitems,
+                             float *out, const float *norm, const float *pdf_orient, ParticleState *ps,
+                             unsigned int *rowmin, unsigned int *segmask, cudaStream_t st) {
+    if (nitems <= 0 || nparticles <= 0 || M <= 0) return cudaSuccess;
+    if (T < 1 || T > TM || NB < 32 || NB > PB_MAX_N || NB % 32 != 0 || M % NB != 0 || !rowmin || !segmask)
+        return cudaErrorInvalidValue;
+    const int ktiles = (K2 + TK - 1) / TK;
+    const long long ychunks = (long long)nparticles * ktiles * (PB_A_BYTES / 16);
+    k_pack_yp<<<(unsigned)((ychunks + 255) / 256), 256, 0, st>>>(b, ldb, E, lde, K2 / 2, T, ktiles,
+                                                                static_cast<uint8_t *>(Yp), ychunks);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    static int nsm = 0;
+    if (!nsm) {
+        int dev = 0;
+        e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_tc_blocks, cudaFuncAttributeMaxDynamicSharedMemorySize, PB_SMEM_BYTES);
+        if (e != cudaSuccess) {
+            nsm = 0;
+            return e;
+        }
+    }
+    const int grid = std::min(nitems, nsm);
+    TbArgs a{static_cast<const uint8_t *>(Yp), static_cast<const uint8_t *>(Bblk), items, nitems, ktiles, NB, M, T,
+             out, norm, pdf_orient, ps, rowmin, segmask};
+    k_tc_blocks<<<grid, THREADS, PB_SMEM_BYTES, st>>>(a);
     return cudaGetLastError();
 }
 

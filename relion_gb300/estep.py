@@ -73,6 +73,13 @@ class MlDeviceBundle:
         check(self.lib.gbr_projector_upload(self.h, int(iclass), data.ctypes.data, xdim, ydim, zdim,
                                             int(yinit), int(zinit), int(r_max), int(padding_factor)))
 
+    def orientation_blocks(self):
+        """(number of blocks, directions per block, projection rows per block)
+        of the restricted coarse pass (gbr_orientation_blocks)."""
+        v = [C.c_int64() for _ in range(3)]
+        check(self.lib.gbr_orientation_blocks(self.h, *[C.byref(x) for x in v]))
+        return tuple(x.value for x in v)
+
     def reserve(self, nbytes):
         check(self.lib.gbr_bundle_reserve(self.h, int(nbytes)))
 
@@ -196,6 +203,9 @@ RESULT_DTYPE = np.dtype([(n, np.int64 if t is _lib.I64 else np.float64)
 assert RESULT_DTYPE.itemsize == C.sizeof(_lib.ParticleResult)
 
 
+# gbr_expect_batch_blocks: a block list starting with this scores every block
+ALL_BLOCKS = -2
+
 # gbr_worker_set_option selectors (include/gbrelion.h, gbr_worker_option)
 WORKER_OPTIONS = dict(debug=1, fine_mode=2, coarse_rows=3, cand_cap=4, cand_buf=5, batch_cap=6)
 FINE_MODES = dict(auto=0, dense=1, sparse=2)
@@ -230,12 +240,15 @@ class MlOptimiserCuda:
             value = COARSE_ROWS[value]
         check(self.lib.gbr_worker_set_option(self.h, WORKER_OPTIONS[name], int(value)))
 
-    def do_expectation_some_particles(self, batch):
+    def do_expectation_some_particles(self, batch, blocks=None):
         """Run the E-step on a batch (dict of host arrays, or device pointers).
 
         Host batch keys: fimg, fimg_nomask (complex [n][cur][cur/2+1]), fctf
         (float [n][cur][cur/2+1]), power_img [n][ori/2+1], old_offset [n][2],
         prior [n][2], highres_Xi2 [n], norm_correction [n], scale [n].
+        blocks: optional int32 [n][m] orientation blocks each particle scores
+        in the coarse pass (gbr_expect_batch_blocks; a row starting with
+        ALL_BLOCKS is searched exhaustively).
         Returns a structured numpy array of gbr_particle_result rows.
         """
         n = int(batch["n"]) if "n" in batch else len(batch["fimg"])
@@ -263,7 +276,14 @@ class MlOptimiserCuda:
             for k in ("power_img", "old_offset", "prior", "highres_Xi2", "norm_correction", "scale"):
                 setattr(b, k, arr(batch[k], np.float64))
         out = np.zeros(n, dtype=RESULT_DTYPE)
-        check(self.lib.gbr_expect_batch(self.h, C.byref(b), out.ctypes.data))
+        if blocks is None:
+            check(self.lib.gbr_expect_batch(self.h, C.byref(b), out.ctypes.data))
+        else:
+            bl = np.ascontiguousarray(blocks, dtype=np.int32)
+            if bl.ndim != 2 or bl.shape[0] != n:
+                raise ValueError("blocks must be [n][m]")
+            check(self.lib.gbr_expect_batch_blocks(self.h, C.byref(b), bl.ctypes.data, bl.shape[1],
+                                                   out.ctypes.data))
         return out
 
     def _image_batch(self, batch, keep):
