@@ -268,7 +268,9 @@ def run_ours(args, world, rank, local):
     extra = rank == 0 and not args.no_mstep and args.workload == CONFIG  # sections of the headline workload
     mstep = mstep_section(args, ds, model, bundle, worker, dev_batch, local) if extra else None
     io = io_section(ds, ib, model) if extra else None
-    learned = learned_section(batch, bundle, res) if extra else None
+    learned = (learned_section(args, ds, model, bundle, worker, batch, dev_batch, res, flush, local,
+                               world * B * args.steps / (total_ms * 1e-3))
+               if extra and args.precision == "bf16" else None)
 
     # ---- roofline of the dominant kernel: the coarse cross-term GEMM ----
     R = bundle.nr_classes * bundle.ndir * bundle.npsi
@@ -426,36 +428,191 @@ def plain_section(args, ds, model, dev_batch, host_batch, h2d, flush, local):
                                   "once, and its time goes to the FP32 contraction"}}
 
 
-def learned_section(batch, bundle, res, steps=2000):
-    """Learned pose proposal on this workload: the network trained on the
-    device on views generated from the current reference (CTFs of this batch,
-    the model's noise), then asked for the top-M directions of this batch's
-    particles; recall = fraction whose exhaustive E-step best direction (the
-    timed steps' result) is among them, against M / ndir for M directions
-    taken without the network."""
-    from relion_gb300.posenet import PoseProposer
-    n_over = bundle.nover_rot * bundle.nover_trans
-    best = (np.asarray(res["best_ihidden_over"]) // n_over // bundle.ntrans // bundle.npsi) % bundle.ndir
+def _slice_batch(batch, sl, n):
+    out = {k: (v[sl] if isinstance(v, np.ndarray) and v.ndim >= 1 and v.shape[0] == n else v)
+           for k, v in batch.items()}
+    out["n"] = len(range(n)[sl])
+    return out
+
+
+def _half_set_maps(model, ds, batch, local, blocks=None):
+    """Gold-standard check of one path: the batch split into two halves, each
+    half's E-step (optionally restricted to `blocks`) and reconstruction
+    (updateSSNRarrays, MAP) in its own bundle; returns the half maps and
+    their FSC."""
+    from relion_gb300.estep import MlDeviceBundle, MlOptimiserCuda
+    n = batch["n"]
+    ns = model["ori_size"] // 2 + 1
+    maps = []
+    for h in range(2):
+        sl = slice(h * n // 2, (h + 1) * n // 2)
+        b = MlDeviceBundle(model, device=local)
+        r = ds.ref
+        b.setup_projector(0, r["data"], r["yinit"], r["zinit"], r["r_max"], r["pad"])
+        w = MlOptimiserCuda(b)
+        w.do_expectation_some_particles(_slice_batch(batch, sl, n), blocks=None if blocks is None else blocks[sl])
+        ws = b.get_wsum()
+        b.symmetrise(0)
+        s = b.update_ssnr_arrays(0, 1.0, np.full(ns, 1.0))
+        maps.append(b.reconstruct(0, do_map=True, tau2=s["tau2"], normalise=ws["pdf_class"][0]))
+        w.close()
+        b.close()
+    b = MlDeviceBundle(model, device=local)
+    fsc = b.fsc(maps[0], maps[1])
+    b.close()
+    return maps, fsc
+
+
+def _angles_between(ra, rb):
+    """Angle (degrees) between rotation matrices [n, 3, 3]."""
+    tr = np.einsum("nij,nij->n", ra, rb)
+    return np.degrees(np.arccos(np.clip((tr - 1.0) / 2.0, -1.0, 1.0)))
+
+
+def learned_section(args, ds, model, bundle, worker, batch, dev_batch, res_ex, flush, local, value_ex,
+                    train_steps=2000, posterior_steps=400, blocks_per_particle=24, mass_threshold=0.9):
+    """Learned pose proposal on this workload, judged by the exhaustive search.
+
+    The network is trained on the device on views of the current reference
+    (CTFs of this batch, the model's noise), then on the E-step's own
+    posteriors (the exhaustive E-step's best directions) of a second batch
+    of the workload.  For the timed batch it proposes orientation blocks
+    (four sibling directions x every psi): each particle scores its
+    `blocks_per_particle` most probable blocks, or everything when they hold
+    less than `mass_threshold` of its probability.  A timed learned step is
+    the proposal (features, network, top blocks) plus the restricted E-step
+    (gbr_expect_batch_blocks), L2 flushed before each.  Judged against the
+    exhaustive precision form on the same batch: best-pose agreement and
+    angular error, the fine-posterior mass the restriction leaves out on a
+    seeded subset (its total-variation distance to the exhaustive
+    posterior), and the FSC and gold-standard FSC-0.143 resolution of
+    half-set maps reconstructed from each path."""
+    import torch
+    from relion_gb300 import datagen
+    from relion_gb300.estep import MlDeviceBundle, MlOptimiserCuda
+    from relion_gb300.iteration import resolution_at
+    from relion_gb300.posenet import BlockProposer, PoseProposer, best_directions, direction_targets
+    B = dev_batch["n"]
+    out = {}
     net = PoseProposer(bundle, nangle=24, max_batch=256, seed=1)
     t0 = time.perf_counter()
-    loss = net.train(batch["fctf"], steps=steps, batch=256, lr=2e-3)
-    t_train = time.perf_counter() - t0
+    loss = net.train(batch["fctf"], steps=train_steps, batch=256, lr=2e-3)
+    out["train_views_s"] = round(time.perf_counter() - t0, 2)
+    out["train_views_steps"] = train_steps
+    out["loss_views"] = round(float(loss), 4)
+    # the E-step's own posteriors of a second batch (untimed exhaustive E-step)
+    b2 = ds.particles(B, B)
+    w2 = MlOptimiserCuda(bundle)
+    r2 = w2.do_expectation_some_particles(b2)
+    w2.close()
+    t0 = time.perf_counter()
+    loss2 = net.train_targets(b2["fimg"], direction_targets(bundle, r2), steps=posterior_steps, batch=256, lr=1e-3)
+    out["train_posteriors_s"] = round(time.perf_counter() - t0, 2)
+    out["train_posteriors_steps"] = posterior_steps
+    out["loss_posteriors"] = round(float(loss2), 4)
+    best = best_directions(bundle, res_ex)
     recall = {}
     for k in (16, 8, 4):
         M = net.ndir // k
         idx, _ = net.propose(batch["fimg"], M)
-        recall["ndir/%d" % k] = {"M": int(M), "recall": round(float(np.mean([best[i] in idx[i] for i in range(len(best))])), 4),
+        recall["ndir/%d" % k] = {"M": int(M), "recall": round(float(np.mean([best[i] in idx[i] for i in range(B)])), 4),
                                  "uniform": round(M / net.ndir, 4)}
-    t0 = time.perf_counter()
-    net.propose(batch["fimg"], net.ndir // 8)
-    t_prop = time.perf_counter() - t0
-    ndir = net.ndir
+    out["recall_exhaustive_best_direction"] = recall
+    prop = BlockProposer(net, bundle, blocks_per_particle, mass_threshold)
+    nblk, dpb, rows = bundle.orientation_blocks()
+    blocks = prop(batch["fimg"])
+    fallback = prop.last["fallback"]
+    scored = np.where(fallback, nblk, np.minimum(blocks_per_particle, nblk) * bundle.nr_classes)
+    out.update(blocks_per_particle=int(blocks_per_particle), mass_threshold=mass_threshold,
+               blocks_total=int(nblk), fallback_fraction=round(float(np.mean(fallback)), 4),
+               scored_orientation_fraction=round(float(np.sum(scored)) / (B * nblk), 4),
+               proposal_mass_median=round(float(np.median(prop.last["mass"])), 4))
+    # ---- timed learned steps: proposal + restricted E-step ----
+    for _ in range(max(1, min(args.warmup, 3))):
+        worker.do_expectation_some_particles(dev_batch, blocks=prop(batch["fimg"]))
+    torch.cuda.synchronize()
+    ms, prop_ms = [], []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record()
+        t0 = time.perf_counter()
+        blk = prop(batch["fimg"])
+        prop_ms.append(1e3 * (time.perf_counter() - t0))
+        res_l = worker.do_expectation_some_particles(dev_batch, blocks=blk)
+        ev1.record()
+        ev1.synchronize()
+        ms.append(ev0.elapsed_time(ev1))
+    v_learned = B * args.steps / (sum(ms) * 1e-3)
+    out["value"] = v_learned
+    out["unit"] = "particles/s"
+    out["ms_per_step"] = sum(ms) / args.steps
+    out["propose_ms"] = round(float(np.mean(prop_ms)), 3)
+    out["vs_exhaustive"] = v_learned / value_ex
+    # training per iteration amortised over the configuration's particle count
+    n_cfg = int(datagen.CONFIGS[args.workload]["n_particles"])
+    t_tr = out["train_views_s"] + out["train_posteriors_s"]
+    out["amortised"] = {"particles_per_iteration": n_cfg, "training_s": round(t_tr, 2),
+                        "value": n_cfg / (n_cfg / v_learned + t_tr),
+                        "note": "particles/s of one iteration over the configuration's particle set with the "
+                                "network trained once in it"}
+    # ---- judged by the exhaustive search ----
+    eq = res_l["best_ihidden_over"] == res_ex["best_ihidden_over"]
+    ra = datagen.euler_matrices(res_l["rot"], res_l["tilt"], res_l["psi"]).numpy()
+    rb = datagen.euler_matrices(res_ex["rot"], res_ex["tilt"], res_ex["psi"]).numpy()
+    ang = _angles_between(ra, rb)
+    rt = np.asarray(batch["true_rot"])
+    out["pose"] = {"best_pose_agreement": round(float(np.mean(eq)), 4),
+                   "angle_to_exhaustive_deg_mean": round(float(np.mean(ang)), 3),
+                   "angle_to_exhaustive_deg_p99": round(float(np.percentile(ang, 99)), 3),
+                   "angle_to_truth_deg_median_learned": round(float(np.median(_angles_between(ra, rt))), 3),
+                   "angle_to_truth_deg_median_exhaustive": round(float(np.median(_angles_between(rb, rt))), 3),
+                   "pmax_abs_diff_mean": round(float(np.mean(np.abs(res_l["pmax"] - res_ex["pmax"]))), 6)}
+    # weight divergence on a seeded subset: exhaustive fine posterior mass in unscored blocks
+    nsub = min(24, B)
+    sub = _slice_batch(batch, slice(0, nsub), B)
+    bd = MlDeviceBundle(model, device=local)
+    r = ds.ref
+    bd.setup_projector(0, r["data"], r["yinit"], r["zinit"], r["r_max"], r["pad"])
+    wd = MlOptimiserCuda(bd, debug=True)
+    wd.do_expectation_some_particles(sub)
+    tv = []
+    per = bd.nover_rot * bd.nover_trans * bd.ntrans
+    for i in range(nsub):
+        idx = wd.debug_fetch(2, i)
+        wf = wd.debug_fetch(4, i)
+        fblk = (idx // per // bd.npsi) // dpb
+        if fallback[i]:
+            tv.append(0.0)
+            continue
+        keep = np.isin(fblk, blocks[i][blocks[i] >= 0])
+        tv.append(float(np.sum(wf[~keep]) / max(np.sum(wf), 1e-300)))
+    wd.close()
+    bd.close()
+    out["weight_divergence"] = {"particles": nsub, "tv_mean": float(np.mean(tv)), "tv_max": float(np.max(tv)),
+                                "note": "exhaustive fine-posterior mass outside the scored blocks (total-variation "
+                                        "distance of the restricted posterior to the exhaustive one)"}
+    # FSC: half-set maps of each path, same particles
+    m_l, f_l = _half_set_maps(model, ds, batch, local, blocks=blk)
+    m_e, f_e = _half_set_maps(model, ds, batch, local)
+    m_p, f_p = _half_set_maps(dict(model, precision=0), ds, batch, local)
+    cur = model["current_size"]
+    rmax = cur // 2
+    b = MlDeviceBundle(model, device=local)
+    f_le = b.fsc(m_l[0], m_e[0])
+    b.close()
+    ori, pix = model["ori_size"], model["pixel_size"]
+    out["fsc"] = {"resolution_A_learned": resolution_at(f_l, ori, pix),
+                  "resolution_A_exhaustive": resolution_at(f_e, ori, pix),
+                  "resolution_A_plain": resolution_at(f_p, ori, pix),
+                  "half_map_fsc_max_abs_diff_learned_vs_plain": round(float(np.max(np.abs(f_l[1:rmax] - f_p[1:rmax]))), 5),
+                  "min_fsc_learned_vs_exhaustive_map": round(float(np.min(f_le[1:rmax])), 6),
+                  "shells": "1..%d (inside the current size)" % (rmax - 1),
+                  "note": "gold-standard FSC-0.143 of two half-set maps (%d particles each) per path; first "
+                          "iteration, so the current size bounds the resolution" % (B // 2)}
     net.close()
-    return {"ndir": int(ndir), "train_steps": steps, "views_per_step": 256, "train_s": round(t_train, 2),
-            "final_loss": round(float(loss), 4), "propose_ms": round(1e3 * t_prop, 3),
-            "particles": int(len(best)), "recall": recall,
-            "note": "proposals are not yet used to restrict the coarse pass: the line's value is the exhaustive "
-                    "precision-form E-step"}
+    return out
 
 
 def io_section(ds, ib, model):

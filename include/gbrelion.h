@@ -489,6 +489,13 @@ int gbr_posenet_loss_grad(gbr_posenet *n, const float *feat, const float *target
  * fctf layout); *loss_out = mean loss over the last min(steps, 20) steps */
 int gbr_posenet_train(gbr_posenet *n, const float *ctf_pool, int64_t n_pool, int64_t steps, int64_t batch,
                       double lr, double *loss_out);
+/* `steps` Adam steps on particle images with given target distributions:
+ * fimg prepared images [count] (host, gbr_particle_batch layout), target
+ * [count][ndir] (host; each row sums to 1), e.g. the E-step's own
+ * posteriors over directions; mini-batches of `batch` consecutive particles,
+ * cycling through the set; *loss_out as gbr_posenet_train */
+int gbr_posenet_train_targets(gbr_posenet *n, const float *fimg, const float *target, int64_t count, int64_t steps,
+                              int64_t batch, double lr, double *loss_out);
 /* top-m directions [count][m] (most probable first) and their probabilities */
 int gbr_posenet_propose(gbr_posenet *n, const float *fimg, int64_t count, int64_t m, int32_t *dir_out,
                         float *prob_out);

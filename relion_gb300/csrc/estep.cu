@@ -1917,6 +1917,7 @@ struct gbr_posenet {
     DevBuf<int> bin;
     DevBuf<float> inv_cnt;
     DevBuf<float> pw, feat, a1, a2, h, logits, dl, d1, d2, loss, target, ctf_pool, prob;
+    DevBuf<float> feat_all, target_all;  // training on particle images with given targets
     DevBuf<int> label, idx;
     DevBuf<float2> fimg;
     ~gbr_posenet() {
@@ -2139,6 +2140,55 @@ int gbr_posenet_train(gbr_posenet *n, const float *ctf_pool, int64_t n_pool, int
         GBR_CUDA(gbr::pn_loss_backward(d, n->params.p, n->feat.p, n->a1.p, n->a2.p, n->h.p, n->logits.p,
                                        n->label.p, nullptr, n->dl.p, n->loss.p, n->d2.p, n->d1.p, n->grad.p,
                                        n->st));
+        GBR_CUDA(gbr::pn_adam(n->params.p, n->grad.p, n->m.p, n->v.p, d.nparams, (float)lr, (int)n->t, n->st));
+        if (k >= steps - 20) {
+            GBR_CUDA(cudaMemcpyAsync(ls.data(), n->loss.p, sizeof(float) * batch, cudaMemcpyDeviceToHost, n->st));
+            GBR_CUDA(cudaStreamSynchronize(n->st));
+            for (float x : ls) acc += x;
+            nacc += batch;
+        }
+    }
+    GBR_CUDA(cudaStreamSynchronize(n->st));
+    if (loss_out) *loss_out = nacc ? acc / (double)nacc : 0.;
+    return GBR_OK;
+}
+
+int gbr_posenet_train_targets(gbr_posenet *n, const float *fimg, const float *target, int64_t count, int64_t steps,
+                              int64_t batch, double lr, double *loss_out) {
+    if (!n || !fimg || !target || count < 1) return fail(GBR_ERR_INVALID, "null argument or empty particle set");
+    if (batch < 1 || batch > n->d.B || batch > count)
+        return fail(GBR_ERR_INVALID, "gbr_posenet_train_targets: 1 <= batch <= min(max_batch, count)");
+    if (steps < 0 || !(lr > 0.)) return fail(GBR_ERR_INVALID, "gbr_posenet_train_targets: steps >= 0, lr > 0");
+    gbr_bundle *b = n->b;
+    GBR_CUDA(cudaSetDevice(b->device));
+    const size_t full = (size_t)b->full_npix;
+    const int nb = n->nbins, ND = n->d.ND;
+    // features of every particle once, then targets; mini-batches are
+    // consecutive windows of the set, cycling
+    GBR_CUDA(n->feat_all.reserve((size_t)count * nb));
+    GBR_CUDA(n->target_all.reserve((size_t)count * ND));
+    for (int64_t c0 = 0; c0 < count; c0 += n->d.B) {
+        const int c = (int)std::min<int64_t>(n->d.B, count - c0);
+        int s = pn_features_dev(n, fimg + 2 * full * c0, c);
+        if (s) return s;
+        GBR_CUDA(cudaMemcpyAsync(n->feat_all.p + (size_t)nb * c0, n->feat.p, sizeof(float) * nb * c,
+                                 cudaMemcpyDeviceToDevice, n->st));
+    }
+    GBR_CUDA(cudaMemcpyAsync(n->target_all.p, target, sizeof(float) * ND * count, cudaMemcpyHostToDevice, n->st));
+    gbr::PnDims d = n->d;
+    d.B = (int)batch;
+    std::vector<float> ls(batch);
+    double acc = 0.;
+    long long nacc = 0;
+    const int64_t nwin = count - batch + 1;
+    for (int64_t k = 0; k < steps; ++k) {
+        ++n->t;
+        const int64_t s0 = (k * batch) % nwin;
+        const float *f = n->feat_all.p + (size_t)nb * s0;
+        const float *tg = n->target_all.p + (size_t)ND * s0;
+        GBR_CUDA(gbr::pn_forward(d, n->params.p, f, n->a1.p, n->a2.p, n->h.p, n->logits.p, n->st));
+        GBR_CUDA(gbr::pn_loss_backward(d, n->params.p, f, n->a1.p, n->a2.p, n->h.p, n->logits.p, nullptr, tg,
+                                       n->dl.p, n->loss.p, n->d2.p, n->d1.p, n->grad.p, n->st));
         GBR_CUDA(gbr::pn_adam(n->params.p, n->grad.p, n->m.p, n->v.p, d.nparams, (float)lr, (int)n->t, n->st));
         if (k >= steps - 20) {
             GBR_CUDA(cudaMemcpyAsync(ls.data(), n->loss.p, sizeof(float) * batch, cudaMemcpyDeviceToHost, n->st));

@@ -115,16 +115,21 @@ def resolution_at(fsc, ori_size, pixel_size, threshold=0.143):
 class HalfSet:
     """One half of the particle set with its own model and maps."""
 
-    def __init__(self, model, maps, batches, device=0, optics=None):
+    def __init__(self, model, maps, batches, device=0, optics=None, proposer=None):
         """batches: prepared particle batches (gbr_particle_batch fields), or,
         with `optics` (kV, Cs, Q0, particle_diameter, width_mask_edge),
         raw real-space image batches prepared on the device at each
-        iteration's current size."""
+        iteration's current size.  proposer: optional callable
+        (bundle, batch) -> int32 [n][m] orientation blocks (or None) that
+        restricts each batch's coarse pass (prepared batches only)."""
         self.model = dict(model)
         self.maps = [np.array(m, np.float64) for m in maps]
         self.batches = batches
         self.device = device
         self.optics = optics
+        self.proposer = proposer
+        if proposer is not None and optics is not None:
+            raise ValueError("a proposer needs prepared particle batches")
         self.dvp = None
         K = int(model["nr_classes"])
         self.tau2 = [None] * K
@@ -146,6 +151,11 @@ class HalfSet:
         if self.optics is not None:
             b.set_optics(**self.optics)
             self.last_results = [w.do_expectation_images(bt) for bt in self.batches]
+        elif self.proposer is not None:
+            self.last_results = [w.do_expectation_some_particles(bt, blocks=self.proposer(b, bt))
+                                 for bt in self.batches]
+            if hasattr(self.proposer, "release"):
+                self.proposer.release()  # a network reading this bundle goes before the bundle
         else:
             self.last_results = [w.do_expectation_some_particles(bt) for bt in self.batches]
         w.close()

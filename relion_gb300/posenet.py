@@ -82,6 +82,20 @@ class PoseProposer:
                                          C.byref(loss)))
         return loss.value
 
+    def train_targets(self, fimg, target, steps, batch=256, lr=1e-3):
+        """Adam steps on particle images with target distributions over the
+        directions (e.g. the E-step's own posteriors); returns the mean loss
+        of the last steps."""
+        f = self._fimg(fimg)
+        t = np.ascontiguousarray(target, dtype=np.float32)
+        if t.shape != (len(f), self.ndir):
+            raise ValueError("target must be [n][ndir]")
+        loss = C.c_double()
+        check(self.lib.gbr_posenet_train_targets(self.h, f.ctypes.data, t.ctypes.data, len(f), int(steps),
+                                                 int(min(batch, len(f), self.max_batch)), float(lr),
+                                                 C.byref(loss)))
+        return loss.value
+
     def propose(self, fimg, m):
         """Top-m directions [n][m] (most probable first) and their probabilities."""
         f = self._fimg(fimg)
@@ -90,3 +104,100 @@ class PoseProposer:
         check(self.lib.gbr_posenet_propose(self.h, f.ctypes.data, len(f), int(m), idx.ctypes.data,
                                            prob.ctypes.data))
         return idx, prob
+
+
+def best_directions(bundle, results):
+    """Coarse direction (within its class) of each particle's best fine pose
+    (gbr_particle_result.best_ihidden_over, the hidden-index packing of
+    HealpixSampling::getPositionOversampledSamplingPoint)."""
+    h = np.asarray(results["best_ihidden_over"], np.int64)
+    r = h // (bundle.nover_rot * bundle.nover_trans) // bundle.ntrans
+    return (r // bundle.npsi) % bundle.ndir
+
+
+def direction_targets(bundle, results, smoothing=0.0):
+    """Target distributions over the directions from an E-step's results:
+    the posterior's mode (best pose's direction), optionally with a uniform
+    share `smoothing`."""
+    d = best_directions(bundle, results)
+    t = np.full((len(d), bundle.ndir), smoothing / bundle.ndir, np.float32)
+    t[np.arange(len(d)), d] += 1.0 - smoothing
+    return t
+
+
+class BlockProposer:
+    """Orientation blocks of the restricted coarse pass from the network.
+
+    The network's probabilities over directions are summed per block (the
+    four sibling directions of one parent HEALPix pixel); each particle
+    scores its `blocks` most probable blocks (in every class), and falls
+    back to the exhaustive search (ALL_BLOCKS) when those carry less than
+    `mass_threshold` of its probability.  Called with a batch's prepared
+    images, returns the int32 [n][m] block lists of
+    MlOptimiserCuda.do_expectation_some_particles(batch, blocks=...)."""
+
+    def __init__(self, net, bundle, blocks, mass_threshold=0.9):
+        self.net = net
+        self.nblk, self.dpb, _ = bundle.orientation_blocks()
+        self.K = bundle.nr_classes
+        self.ndir = bundle.ndir
+        self.per_class = self.ndir // self.dpb
+        self.blocks = int(min(blocks, self.per_class))
+        self.mass_threshold = float(mass_threshold)
+        self.last = None
+
+    def block_probabilities(self, fimg):
+        idx, prob = self.net.propose(fimg, self.ndir)
+        bp = np.zeros((len(idx), self.per_class), np.float64)
+        rows = np.repeat(np.arange(len(idx)), idx.shape[1])
+        np.add.at(bp, (rows, (idx // self.dpb).ravel()), prob.astype(np.float64).ravel())
+        return bp
+
+    def __call__(self, fimg):
+        from .estep import ALL_BLOCKS
+        bp = self.block_probabilities(fimg)
+        order = np.argsort(-bp, axis=1, kind="stable")[:, :self.blocks]
+        mass = np.take_along_axis(bp, order, axis=1).sum(axis=1)
+        out = np.concatenate([order + c * self.per_class for c in range(self.K)], axis=1).astype(np.int32)
+        fallback = mass < self.mass_threshold
+        out[fallback, 0] = ALL_BLOCKS
+        self.last = dict(mass=mass, fallback=fallback)
+        return out
+
+
+class LearnedBlocks:
+    """Proposer for relion_gb300.iteration.HalfSet: on each iteration's
+    bundle the network is trained on views of the current reference (the
+    first time `train_steps` Adam steps, later `finetune_steps` from the
+    previous iteration's parameters), then each batch gets the blocks of a
+    BlockProposer.  release() (called by HalfSet after its E-step) keeps the
+    parameters and frees the network before its bundle is closed."""
+
+    def __init__(self, blocks, mass_threshold=0.9, train_steps=1500, finetune_steps=300, lr=2e-3, **net_kw):
+        self.blocks, self.mass_threshold = blocks, mass_threshold
+        self.train_steps, self.finetune_steps, self.lr = train_steps, finetune_steps, lr
+        self.net_kw = dict(nangle=24, max_batch=256, seed=1)
+        self.net_kw.update(net_kw)
+        self.net = self.bundle = self.params = self.bp = None
+        self.fallback = []
+
+    def __call__(self, bundle, batch):
+        if self.bundle is not bundle:
+            self.release()
+            self.net = PoseProposer(bundle, **self.net_kw)
+            steps = self.train_steps
+            if self.params is not None:
+                self.net.set_params(self.params)
+                steps = self.finetune_steps
+            self.net.train(batch["fctf"], steps=steps, batch=min(256, self.net.max_batch), lr=self.lr)
+            self.bundle = bundle
+            self.bp = BlockProposer(self.net, bundle, self.blocks, self.mass_threshold)
+        out = self.bp(batch["fimg"])
+        self.fallback.append(float(np.mean(self.bp.last["fallback"])))
+        return out
+
+    def release(self):
+        if self.net is not None:
+            self.params = self.net.get_params()
+            self.net.close()
+        self.net = self.bundle = self.bp = None

@@ -3,7 +3,8 @@
 The precision form evaluates the coarse diff2 with BF16 operands on the
 tensor cores; it is compared with the plain FP32 path on the same inputs
 through the C ABI.  Tolerance: the coarse relative diff2 (diff2 minus the
-per-particle constant) agrees to 2 % of its range (BF16 has an 8-bit
+per-particle constant) agrees to 2 % of its range on the poses the tensor-core
+pass stores (BF16 has an 8-bit
 significand); every significant pose of the FP32 coarse pass is also
 significant in BF16 for at least 95 % of the particles' weight, and the
 FP32 fine pass gives the same best pose for at least 90 % of particles.
@@ -76,8 +77,11 @@ def test_tcgen05_coarse_2d_classification():
     for i in range(8):
         a, b = d32[i], d16[i]
         fin = np.isfinite(a)
-        assert np.array_equal(fin, np.isfinite(b))
-        ra, rb = a[fin] - a[fin].min(), b[fin] - b[fin].min()
-        assert np.max(np.abs(ra - rb)) <= 0.02 * np.ptp(ra) + 1e-3
+        # the tensor-core pass stores diff2 only near the particle's running
+        # minimum (sparse stores; its minimum is always stored)
+        st = np.isfinite(b)
+        assert np.all(fin[st])
+        ra, rb = a[st] - a[fin].min(), b[st] - b[st].min()
+        assert np.max(np.abs(ra - rb)) <= 0.02 * np.ptp(a[fin] - a[fin].min()) + 1e-3
     assert np.mean(r32["best_ihidden_over"] == r16["best_ihidden_over"]) >= 0.9
     assert np.mean(r16["cls"] - 1 == batch["true_class"]) >= 0.75
