@@ -500,15 +500,20 @@ def learned_section(args, ds, model, bundle, worker, batch, dev_batch, res_ex, f
     out["train_views_s"] = round(time.perf_counter() - t0, 2)
     out["train_views_steps"] = train_steps
     out["loss_views"] = round(float(loss), 4)
-    # the E-step's own posteriors of a second batch (untimed exhaustive E-step)
+    # the E-step's own posteriors of a second batch of the workload (untimed
+    # exhaustive E-step): the first half trains the network, the second half
+    # (held out) calibrates its softmax temperature
     b2 = ds.particles(B, B)
     w2 = MlOptimiserCuda(bundle)
     r2 = w2.do_expectation_some_particles(b2)
     w2.close()
+    h = B // 2
     t0 = time.perf_counter()
-    loss2 = net.train_targets(b2["fimg"], direction_targets(bundle, r2), steps=posterior_steps, batch=256, lr=1e-3)
+    loss2 = net.train_targets(b2["fimg"][:h], direction_targets(bundle, r2[:h], smoothing=0.1),
+                              steps=posterior_steps, batch=min(256, h), lr=5e-4)
     out["train_posteriors_s"] = round(time.perf_counter() - t0, 2)
     out["train_posteriors_steps"] = posterior_steps
+    out["train_posteriors_particles"] = h
     out["loss_posteriors"] = round(float(loss2), 4)
     best = best_directions(bundle, res_ex)
     recall = {}
@@ -519,6 +524,8 @@ def learned_section(args, ds, model, bundle, worker, batch, dev_batch, res_ex, f
                                  "uniform": round(M / net.ndir, 4)}
     out["recall_exhaustive_best_direction"] = recall
     prop = BlockProposer(net, bundle, blocks_per_particle, mass_threshold)
+    out["temperature"] = prop.calibrate(b2["fimg"][h:], best_directions(bundle, r2[h:]))
+    out["calibration_particles"] = B - h
     nblk, dpb, rows = bundle.orientation_blocks()
     blocks = prop(batch["fimg"])
     fallback = prop.last["fallback"]
@@ -599,6 +606,9 @@ def learned_section(args, ds, model, bundle, worker, batch, dev_batch, res_ex, f
     m_p, f_p = _half_set_maps(dict(model, precision=0), ds, batch, local)
     cur = model["current_size"]
     rmax = cur // 2
+    # resolution over the shells inside the current size (beyond it the maps
+    # hold no data)
+    f_l, f_e, f_p = f_l[:rmax + 1], f_e[:rmax + 1], f_p[:rmax + 1]
     b = MlDeviceBundle(model, device=local)
     f_le = b.fsc(m_l[0], m_e[0])
     b.close()

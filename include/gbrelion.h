@@ -496,6 +496,11 @@ int gbr_posenet_train(gbr_posenet *n, const float *ctf_pool, int64_t n_pool, int
  * cycling through the set; *loss_out as gbr_posenet_train */
 int gbr_posenet_train_targets(gbr_posenet *n, const float *fimg, const float *target, int64_t count, int64_t steps,
                               int64_t batch, double lr, double *loss_out);
+/* probability of each block of dirs_per_block consecutive directions
+ * [count][ndir / dirs_per_block] under softmax(logits / temperature), for
+ * prepared images fimg [count] (host) */
+int gbr_posenet_block_probs(gbr_posenet *n, const float *fimg, int64_t count, int64_t dirs_per_block,
+                            double temperature, float *out);
 /* top-m directions [count][m] (most probable first) and their probabilities */
 int gbr_posenet_propose(gbr_posenet *n, const float *fimg, int64_t count, int64_t m, int32_t *dir_out,
                         float *prob_out);

@@ -130,6 +130,7 @@ EXPORTS = {
     "gbr_posenet_train": (C.c_int, [P, P, I64, I64, I64, F64, P]),
     "gbr_posenet_propose": (C.c_int, [P, P, I64, I64, P, P]),
     "gbr_posenet_train_targets": (C.c_int, [P, P, P, I64, I64, I64, F64, P]),
+    "gbr_posenet_block_probs": (C.c_int, [P, P, I64, I64, F64, P]),
     "gbr_recon_set_precision": (C.c_int, [P, C.c_int]),
     "gbr_projector_download": (C.c_int, [P, I64, P, P]),
     "gbr_wsum_download": (C.c_int, [P, C.POINTER(Wsum)]),

@@ -2202,6 +2202,31 @@ int gbr_posenet_train_targets(gbr_posenet *n, const float *fimg, const float *ta
     return GBR_OK;
 }
 
+int gbr_posenet_block_probs(gbr_posenet *n, const float *fimg, int64_t count, int64_t dirs_per_block,
+                            double temperature, float *out) {
+    if (!n || (count > 0 && (!fimg || !out))) return fail(GBR_ERR_INVALID, "null argument");
+    if (dirs_per_block < 1 || n->d.ND % dirs_per_block != 0 || !(temperature > 0.))
+        return fail(GBR_ERR_INVALID, "gbr_posenet_block_probs: dirs_per_block must divide ndir, temperature > 0");
+    GBR_CUDA(cudaSetDevice(n->b->device));
+    const size_t full = (size_t)n->b->full_npix;
+    const int nb = n->d.ND / (int)dirs_per_block;
+    GBR_CUDA(n->prob.reserve((size_t)n->d.B * nb));
+    for (int64_t c0 = 0; c0 < count; c0 += n->d.B) {
+        const int c = (int)std::min<int64_t>(n->d.B, count - c0);
+        int s = pn_features_dev(n, fimg + 2 * full * c0, c);
+        if (s) return s;
+        gbr::PnDims d = n->d;
+        d.B = c;
+        GBR_CUDA(gbr::pn_forward(d, n->params.p, n->feat.p, n->a1.p, n->a2.p, n->h.p, n->logits.p, n->st));
+        GBR_CUDA(gbr::pn_block_probs(n->logits.p, d.ND, (int)dirs_per_block, (float)temperature, c, n->prob.p,
+                                     n->st));
+        GBR_CUDA(cudaMemcpyAsync(out + (size_t)nb * c0, n->prob.p, sizeof(float) * nb * c, cudaMemcpyDeviceToHost,
+                                 n->st));
+    }
+    GBR_CUDA(cudaStreamSynchronize(n->st));
+    return GBR_OK;
+}
+
 int gbr_posenet_propose(gbr_posenet *n, const float *fimg, int64_t count, int64_t m, int32_t *dir_out,
                         float *prob_out) {
     if (!n || (count > 0 && (!fimg || !dir_out || !prob_out))) return fail(GBR_ERR_INVALID, "null argument");

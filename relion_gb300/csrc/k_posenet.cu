@@ -421,6 +421,35 @@ cudaError_t pn_adam(float *p, const float *g, float *m, float *v, long long n, f
     return cudaGetLastError();
 }
 
+// Probability of each block of `dpb` consecutive directions under the
+// tempered softmax softmax(logits / temperature): one CTA per particle.
+__global__ void k_pn_block_probs(const float *__restrict__ logits, int N, int dpb, float inv_t,
+                                 float *__restrict__ out) {
+    __shared__ float sh[32];
+    const int b = blockIdx.x;
+    const float *l = logits + (size_t)b * N;
+    float m = -3.4e38f;
+    for (int n = threadIdx.x; n < N; n += blockDim.x) m = fmaxf(m, l[n] * inv_t);
+    m = block_reduce(m, sh, true);
+    float se = 0.f;
+    for (int n = threadIdx.x; n < N; n += blockDim.x) se += expf(l[n] * inv_t - m);
+    se = block_reduce(se, sh, false);
+    const float inv_se = se > 0.f ? 1.f / se : 0.f;
+    const int nb = N / dpb;
+    for (int j = threadIdx.x; j < nb; j += blockDim.x) {
+        float acc = 0.f;
+        for (int q = 0; q < dpb; ++q) acc += expf(l[j * dpb + q] * inv_t - m);
+        out[(size_t)b * nb + j] = acc * inv_se;
+    }
+}
+
+cudaError_t pn_block_probs(const float *logits, int N, int dpb, float temperature, int B, float *out,
+                           cudaStream_t st) {
+    if (dpb < 1 || N % dpb != 0 || !(temperature > 0.f)) return cudaErrorInvalidValue;
+    k_pn_block_probs<<<B, 256, 0, st>>>(logits, N, dpb, 1.f / temperature, out);
+    return cudaGetLastError();
+}
+
 cudaError_t pn_topm(const float *logits, int N, int M, int B, int *idx, float *prob, cudaStream_t st) {
     k_pn_topm<<<B, 256, sizeof(float) * N, st>>>(logits, N, M, idx, prob);
     return cudaGetLastError();

@@ -96,6 +96,15 @@ class PoseProposer:
                                                  C.byref(loss)))
         return loss.value
 
+    def block_probs(self, fimg, dirs_per_block, temperature=1.0):
+        """Probability of each block of dirs_per_block consecutive directions
+        [n][ndir / dirs_per_block] under softmax(logits / temperature)."""
+        f = self._fimg(fimg)
+        out = np.zeros((len(f), self.ndir // int(dirs_per_block)), np.float32)
+        check(self.lib.gbr_posenet_block_probs(self.h, f.ctypes.data, len(f), int(dirs_per_block),
+                                               float(temperature), out.ctypes.data))
+        return out
+
     def propose(self, fimg, m):
         """Top-m directions [n][m] (most probable first) and their probabilities."""
         f = self._fimg(fimg)
@@ -136,7 +145,7 @@ class BlockProposer:
     images, returns the int32 [n][m] block lists of
     MlOptimiserCuda.do_expectation_some_particles(batch, blocks=...)."""
 
-    def __init__(self, net, bundle, blocks, mass_threshold=0.9):
+    def __init__(self, net, bundle, blocks, mass_threshold=0.9, temperature=1.0):
         self.net = net
         self.nblk, self.dpb, _ = bundle.orientation_blocks()
         self.K = bundle.nr_classes
@@ -144,14 +153,33 @@ class BlockProposer:
         self.per_class = self.ndir // self.dpb
         self.blocks = int(min(blocks, self.per_class))
         self.mass_threshold = float(mass_threshold)
+        self.temperature = float(temperature)
         self.last = None
 
     def block_probabilities(self, fimg):
-        idx, prob = self.net.propose(fimg, self.ndir)
-        bp = np.zeros((len(idx), self.per_class), np.float64)
-        rows = np.repeat(np.arange(len(idx)), idx.shape[1])
-        np.add.at(bp, (rows, (idx // self.dpb).ravel()), prob.astype(np.float64).ravel())
-        return bp
+        return self.net.block_probs(fimg, self.dpb, self.temperature)
+
+    def calibrate(self, fimg, best_dirs, temperatures=None):
+        """Temperature of the network's softmax judged by the exhaustive
+        search: the value minimising the negative log-likelihood of the
+        blocks holding the exhaustive E-step's best directions on a held-out
+        set of particles (temperature scaling; the network's ranking is
+        unchanged, its probabilities, and with them the fallback decision,
+        become calibrated).  Returns the chosen temperature."""
+        if temperatures is None:
+            temperatures = np.geomspace(0.25, 32.0, 29)
+        logp = np.log(np.maximum(self.net.block_probs(fimg, 1, 1.0).astype(np.float64), 1e-38))
+        best_blk = np.asarray(best_dirs) // self.dpb
+        nll = []
+        for t in temperatures:
+            z = logp / t
+            z -= z.max(axis=1, keepdims=True)
+            p = np.exp(z)
+            p /= p.sum(axis=1, keepdims=True)
+            bp = p.reshape(len(p), self.per_class, self.dpb).sum(axis=2)
+            nll.append(-np.mean(np.log(np.maximum(bp[np.arange(len(bp)), best_blk], 1e-300))))
+        self.temperature = float(temperatures[int(np.argmin(nll))])
+        return self.temperature
 
     def __call__(self, fimg):
         from .estep import ALL_BLOCKS

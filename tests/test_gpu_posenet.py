@@ -115,3 +115,37 @@ def test_training_gain():
     assert np.all(np.diff(prob1, axis=1) <= 0)
     assert r1 >= 1.5 * M / ndir
     assert r1 >= r0 + 0.1
+
+
+def test_block_probs_and_target_training():
+    # tempered block probabilities against the oracle's softmax of the
+    # network's logits, and a few steps on given target distributions lower
+    # the loss on them (training on the E-step's own posteriors)
+    _need_cuda()
+    from oracle import posenet_oracle as po
+    from relion_gb300 import datagen
+    from relion_gb300.posenet import PoseProposer
+    ds = datagen.Dataset("cfg0_box64", seed=5, n_particles=32)
+    m = ds.model(precision=1)
+    b = _bundle(ds, m)
+    net = PoseProposer(b, nangle=12, c1=4, c2=6, max_batch=32, seed=2)
+    batch = ds.particles(0, 32)
+    feat = net.features(batch["fimg"])
+    H, W, C1, C2, ND = net.nring, net.nangle, net.c1, net.c2, net.ndir
+    params = net.get_params().astype(np.float64)
+    for t, dpb in ((1.0, 1), (2.5, 4)):
+        got = net.block_probs(batch["fimg"], dpb, t)
+        logits = po.forward(params, feat.astype(np.float64), H, W, C1, C2, ND)["logits"] / t
+        p = np.exp(logits - logits.max(axis=1, keepdims=True))
+        p /= p.sum(axis=1, keepdims=True)
+        want = p.reshape(len(p), ND // dpb, dpb).sum(axis=2)
+        assert np.max(np.abs(got - want)) <= 1e-5
+    target = np.zeros((32, ND), np.float32)
+    target[np.arange(32), np.arange(32) % ND] = 1.0
+    l0, _ = net.loss_grad(feat, target)
+    net.train_targets(batch["fimg"], target, steps=50, batch=16, lr=1e-2)
+    l1, _ = net.loss_grad(feat, target)
+    print("target loss", l0, "->", l1)
+    assert l1 < 0.5 * l0
+    net.close()
+    b.close()
