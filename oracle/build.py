@@ -2,8 +2,9 @@
 
 Compiles oracle/relion_oracle.cpp and oracle/oracle_mstep.cpp into
 oracle/_build/liboracle.so and, when the environment variable
-RELION_REFERENCE names the reference source tree, the reference's own HEALPix
-sources into oracle/_ref/libref_healpix.so (oracle/build_ref.sh).
+RELION_REFERENCE names the reference source tree, the reference's own code
+into oracle/_ref (oracle/build_ref.sh): its HEALPix sources as
+libref_healpix.so and the ref_pin driver over its CPU sources.
 """
 import os
 import subprocess
@@ -11,6 +12,7 @@ import subprocess
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "liboracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libref_healpix.so")
+REF_PIN = os.path.join(HERE, "_ref", "ref_pin")
 
 
 def build(force=False):
@@ -23,7 +25,11 @@ def build(force=False):
                        + srcs + ["-o", LIB + ".tmp"], check=True)
         os.replace(LIB + ".tmp", LIB)
     ref = os.environ.get("RELION_REFERENCE", "")
-    if ref and os.path.isdir(os.path.join(ref, "src", "Healpix_2.15a")) and (force or not os.path.exists(REF_LIB)):
+    deps = [os.path.join(HERE, "build_ref.sh")] + [os.path.join(HERE, "ref", f) for f in os.listdir(os.path.join(HERE, "ref"))
+                                                  if f.endswith(".cpp")]
+    stale = not os.path.exists(REF_PIN) or os.path.getmtime(REF_PIN) < max(os.path.getmtime(d) for d in deps)
+    if ref and os.path.isdir(os.path.join(ref, "src", "Healpix_2.15a")) and (force or stale or
+                                                                          not os.path.exists(REF_LIB)):
         subprocess.run(["sh", os.path.join(HERE, "build_ref.sh")], check=True)
     return LIB
 

@@ -68,6 +68,10 @@ def load():
             raise RuntimeError("oracle not built: %s (run oracle/build.py)" % path)
         lib = C.CDLL(path)
         lib.oracle_expectation.restype = C.c_int
+        lib.oracle_project.restype = None
+        lib.oracle_backproject.restype = None
+        lib.oracle_shift_ft.restype = None
+        lib.oracle_euler.restype = None
         lib.oracle_set_threads.restype = C.c_int
         lib.oracle_set_threads.argtypes = [C.c_int]
         lib.oracle_prepare_images.restype = C.c_int
@@ -134,6 +138,69 @@ def directions(order):
     load().oracle_directions(I64(order), rot.ctypes.data_as(P), tilt.ctypes.data_as(P),
                              ipix.ctypes.data_as(P))
     return rot, tilt, ipix
+
+
+def _geometry_model(ori, pad, ref=None, bp=None):
+    """An OracleModel holding only the projector / backprojector geometry
+    (for the building-block entry points)."""
+    m = OracleModel()
+    m.ori_size, m.nr_classes, m.padding_factor, m.ref_dim = ori, 1, pad, 3
+    keep = []
+    if ref is not None:
+        d = np.ascontiguousarray(ref["data"], np.complex128)
+        keep.append(d)
+        m.proj_r_max = ref["r_max"]
+        m.proj_zdim, m.proj_ydim, m.proj_xdim = d.shape
+        m.proj_yinit, m.proj_zinit = ref["yinit"], ref["zinit"]
+        m.ppref = d.ctypes.data
+    if bp is not None:
+        m.bp_r_max, m.bp_xdim, m.bp_ydim, m.bp_zdim = bp["r_max"], bp["xdim"], bp["ydim"], bp["zdim"]
+        m.bp_yinit, m.bp_zinit = bp["yinit"], bp["zinit"]
+    return m, keep
+
+
+def project(ref, ori, pad, size, A):
+    """The oracle's Projector::project of one 3x3 matrix -> [size][size/2+1]."""
+    o = load()
+    m, keep = _geometry_model(ori, pad, ref=ref)
+    out = np.zeros((size, size // 2 + 1), np.complex128)
+    a = np.ascontiguousarray(A, np.float64)
+    o.oracle_project(C.byref(m), I64(0), a.ctypes.data_as(P), I64(size), out.ctypes.data_as(P))
+    del keep
+    return out
+
+
+def backproject(ori, pad, current_size, size, mats, images, weights):
+    """The oracle's backprojection of (matrix, image, weight) triplets into
+    volumes of bp_geometry(current_size) -> (data complex, weight)."""
+    o = load()
+    g = bp_geometry(current_size, ori, pad)
+    m, keep = _geometry_model(ori, pad, bp=g)
+    data = np.zeros((g["zdim"], g["ydim"], g["xdim"]), np.complex128)
+    wt = np.zeros((g["zdim"], g["ydim"], g["xdim"]))
+    for A, f, w in zip(mats, images, weights):
+        a = np.ascontiguousarray(A, np.float64)
+        fi = np.ascontiguousarray(f, np.complex128)
+        wi = np.ascontiguousarray(w, np.float64)
+        o.oracle_backproject(C.byref(m), I64(0), a.ctypes.data_as(P), I64(size), fi.ctypes.data_as(P),
+                             wi.ctypes.data_as(P), data.ctypes.data_as(P), wt.ctypes.data_as(P))
+    del keep
+    return data, wt
+
+
+def shift(image, oridim, xshift, yshift):
+    """The oracle's phase shift of a [size][size/2+1] image."""
+    f = np.ascontiguousarray(image, np.complex128)
+    out = np.zeros_like(f)
+    load().oracle_shift_ft(f.ctypes.data_as(P), I64(f.shape[0]), F64(oridim), F64(xshift), F64(yshift),
+                           out.ctypes.data_as(P))
+    return out
+
+
+def euler(rot, tilt, psi):
+    A = np.zeros(9)
+    load().oracle_euler(F64(rot), F64(tilt), F64(psi), A.ctypes.data_as(P))
+    return A.reshape(3, 3)
 
 
 def bp_geometry(current_size, ori_size, pad=2, ref_dim=3):

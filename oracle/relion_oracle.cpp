@@ -554,10 +554,13 @@ double oracle_ctf(double defU, double defV, double defAng, double kV, double Cs,
     double K4 = -Bfac / 4.;
     double K5 = deg2rad(phase_shift);
     double s = std::sin(rad_az), c = std::cos(rad_az);
-    // A = Q^T D Q with Q = [[c, s], [-s, c]], D = diag(-defU, -defV)
-    double Axx = c * c * (-defU) + s * s * (-defV);
-    double Axy = c * s * (-defU) - s * c * (-defV);
-    double Ayy = s * s * (-defU) + c * c * (-defV);
+    // A = (Q^T D) Q with Q = [[c, s], [-s, c]], D = diag(-defU, -defV),
+    // multiplied in that order as the reference's 2x2 products do
+    // (src/ctf.cpp:251-257; src/jaz/gravis/t2Matrix.h operator*)
+    const double M00 = c * (-defU), M01 = (-s) * (-defV), M10 = s * (-defU), M11 = c * (-defV);
+    double Axx = M00 * c + M01 * (-s);
+    double Axy = M00 * s + M01 * c;
+    double Ayy = M10 * s + M11 * c;
     double u2 = X * X + Y * Y, u4 = u2 * u2;
     double gamma = K1 * (Axx * X * X + 2.0 * Axy * X * Y + Ayy * Y * Y) + K2 * u4 - K5 - K3;
     double ret = -std::sin(gamma);
@@ -640,6 +643,15 @@ void oracle_euler(double rot, double tilt, double psi, double *A) { euler_matrix
 
 void oracle_project(const oracle_model *m, int64_t iclass, const double *A, int64_t size, double *out) {
     project(*m, iclass, A, size, reinterpret_cast<Cplx *>(out));
+}
+
+void oracle_backproject(const oracle_model *m, int64_t iclass, const double *A, int64_t size, const double *f2d,
+                        const double *Mw, double *bp_data, double *bp_weight) {
+    backproject(*m, iclass, A, size, reinterpret_cast<const Cplx *>(f2d), Mw, bp_data, bp_weight);
+}
+
+void oracle_shift_ft(const double *in, int64_t size, double oridim, double xshift, double yshift, double *out) {
+    shift_ft(reinterpret_cast<const Cplx *>(in), size, oridim, xshift, yshift, reinterpret_cast<Cplx *>(out));
 }
 
 /*

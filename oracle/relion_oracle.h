@@ -197,8 +197,16 @@ void oracle_hpx_nest2xyf(int64_t order, int64_t pix, int64_t *ix, int64_t *iy, i
 int64_t oracle_hpx_xyf2nest(int64_t order, int64_t ix, int64_t iy, int64_t face);
 /* Euler (rot,tilt,psi) -> 3x3 row-major */
 void oracle_euler(double rot, double tilt, double psi, double *A);
-/* Fourier slice of one class at the given size, A row-major 3x3; out [size][size/2+1][2] */
+/* Building blocks, for checks against the reference's own code: the
+ * projection of class iclass of m->ppref at the Euler matrix A (row-major)
+ * into a [size][size/2+1] complex image; the backprojection of such an
+ * image with weights Mw into volumes of the m->bp_* geometry (added to
+ * bp_data complex / bp_weight); the phase shift of an image by (x, y)
+ * pixels of a box of oridim. */
 void oracle_project(const oracle_model *m, int64_t iclass, const double *A, int64_t size, double *out);
+void oracle_backproject(const oracle_model *m, int64_t iclass, const double *A, int64_t size, const double *f2d,
+                        const double *Mw, double *bp_data, double *bp_weight);
+void oracle_shift_ft(const double *in, int64_t size, double oridim, double xshift, double yshift, double *out);
 
 #ifdef __cplusplus
 }
