@@ -13,6 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "liboracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libref_healpix.so")
 REF_PIN = os.path.join(HERE, "_ref", "ref_pin")
+REF_ESTEP = os.path.join(HERE, "_ref", "ref_estep")
 
 
 def build(force=False):
@@ -27,7 +28,8 @@ def build(force=False):
     ref = os.environ.get("RELION_REFERENCE", "")
     deps = [os.path.join(HERE, "build_ref.sh")] + [os.path.join(HERE, "ref", f) for f in os.listdir(os.path.join(HERE, "ref"))
                                                   if f.endswith(".cpp")]
-    stale = not os.path.exists(REF_PIN) or os.path.getmtime(REF_PIN) < max(os.path.getmtime(d) for d in deps)
+    newest = max(os.path.getmtime(d) for d in deps)
+    stale = any(not os.path.exists(f) or os.path.getmtime(f) < newest for f in (REF_PIN, REF_ESTEP))
     if ref and os.path.isdir(os.path.join(ref, "src", "Healpix_2.15a")) and (force or stale or
                                                                           not os.path.exists(REF_LIB)):
         subprocess.run(["sh", os.path.join(HERE, "build_ref.sh")], check=True)

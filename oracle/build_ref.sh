@@ -9,9 +9,13 @@
 #                      CTF images, HEALPix sampling, shifts, Euler matrices,
 #                      reconstruction and the Fourier map of a reference, over
 #                      the shims of oracle/ref/shim (FFTW API on our own FFT,
-#                      TIFF / PNG declarations) and oracle/ref/stubs.cpp.
-# Paths the driver never takes (helical geometry, optics-group models, plots)
-# stay unresolved (--unresolved-symbols=ignore-all).
+#                      TIFF / PNG declarations) and oracle/ref/stubs.cpp;
+#   ref_estep          a driver (oracle/ref/ref_estep_driver.cpp) running the
+#                      reference's MlOptimiser E-step (getAllSquaredDifferences,
+#                      convertAllSquaredDifferencesToWeights, storeWeightedSums)
+#                      with its model, sampling, particle and optics classes.
+# Paths the drivers never take (helical geometry, aberrations, tomography
+# I/O, atomic models, plots) stay unresolved (--unresolved-symbols=ignore-all).
 set -e
 REF=${RELION_REFERENCE:?set RELION_REFERENCE to the reference source tree}
 HERE=$(cd "$(dirname "$0")" && pwd)
@@ -41,12 +45,24 @@ g++ $FLAGS -c "$REF/src/Healpix_2.15a/healpix_base.cc" -o "$OUT/obj/healpix_base
 pids="$pids $!"
 g++ $FLAGS -c "$REF/src/Healpix_2.15a/cxxutils.cc" -o "$OUT/obj/cxxutils.o" &
 pids="$pids $!"
-g++ $FLAGS -c "$HERE/ref/ref_pin_driver.cpp" -o "$OUT/obj/ref_pin_driver.o" &
+for f in ml_optimiser ml_model exp_model parallel helix jaz/single_particle/obs_model jaz/optics/optics_data \
+         jaz/tomography/tomogram_set jaz/tomography/particle_set jaz/tomography/tomogram; do
+  g++ $FLAGS -c "$REF/src/$f.cpp" -o "$OUT/obj/$(basename $f).o" &
+  pids="$pids $!"
+done
+mkdir -p "$OUT/drv"
+g++ $FLAGS -c "$HERE/ref/ref_pin_driver.cpp" -o "$OUT/drv/ref_pin_driver.o" &
+pids="$pids $!"
+g++ $FLAGS -c "$HERE/ref/ref_estep_driver.cpp" -o "$OUT/drv/ref_estep_driver.o" &
 pids="$pids $!"
 g++ -std=c++14 -O2 -w -I"$HERE/ref/shim" -c "$HERE/ref/fftw_shim.cpp" -o "$OUT/obj/fftw_shim.o" &
 pids="$pids $!"
 g++ -std=c++14 -O2 -w -I"$HERE/ref/shim" -c "$HERE/ref/stubs.cpp" -o "$OUT/obj/stubs.o" &
 pids="$pids $!"
 for p in $pids; do wait $p; done
-g++ -fopenmp -o "$OUT/ref_pin" "$OUT"/obj/*.o -lpthread -Wl,--unresolved-symbols=ignore-all
+g++ -fopenmp -o "$OUT/ref_pin" "$OUT/drv/ref_pin_driver.o" "$OUT"/obj/*.o -lpthread \
+    -Wl,--unresolved-symbols=ignore-all 2>/dev/null
 echo "built $OUT/ref_pin"
+g++ -fopenmp -o "$OUT/ref_estep" "$OUT/drv/ref_estep_driver.o" "$OUT"/obj/*.o -lpthread \
+    -Wl,--unresolved-symbols=ignore-all 2>/dev/null
+echo "built $OUT/ref_estep"

@@ -128,3 +128,82 @@ def fourier_map(ori, pad, current_size, vol, do_gridding=True, min_ires=-1):
     data = out[6:6 + 2 * n].view(np.complex128).reshape(zd, yd, xd)
     power = out[6 + 2 * n:]
     return data, (yi, zi, rmax), power
+
+
+ESTEP_BIN = os.path.join(HERE, "_ref", "ref_estep")
+METADATA = ("rot", "tilt", "psi", "xoff", "yoff", "cls", "dLL", "pmax", "nr_sign", "norm")
+SCALARS = ("coarse_min_diff2", "coarse_sum_weight", "coarse_significant_weight", "fine_min_diff2",
+           "fine_sum_weight", "fine_significant_weight", "max_weight")
+
+
+def estep_available():
+    return os.path.exists(ESTEP_BIN) and os.access(ESTEP_BIN, os.X_OK)
+
+
+def estep(model, ref, batch):
+    """The reference's CPU E-step (MlOptimiser::getAllSquaredDifferences,
+    convertAllSquaredDifferencesToWeights for both passes, storeWeightedSums)
+    on a prepared batch of one class, through oracle/_ref/ref_estep.
+    Returns (per-particle list of dicts: coarse_diff2, coarse_weight,
+    coarse_significant, fine_diff2, fine_weight and the scalars / metadata of
+    SCALARS / METADATA; wsum dict; bp_data [z][y][x] complex; bp_weight)."""
+    if not estep_available():
+        return None
+    d = np.asarray(ref["data"], np.complex128)
+    z, y, x = d.shape
+    n = int(batch["n"])
+    m = model
+    req = [[m["ori_size"], m["current_size"], m["coarse_size"], m["padding_factor"], m["healpix_order"],
+            m["psi_step"], m["offset_range"], m["offset_step"], m["pixel_size"], m["adaptive_fraction"],
+            m["sigma2_fudge"], m["sigma2_offset"], n, x, y, z, ref["yinit"], ref["zinit"], ref["r_max"]],
+           _cplx(d), np.asarray(m["sigma2_noise"], np.float64), np.asarray(m["pdf_direction"], np.float64)]
+    for i in range(n):
+        req += [_cplx(batch["fimg"][i]), _cplx(batch["fimg_nomask"][i]), np.asarray(batch["fctf"][i], np.float64),
+                np.asarray(batch["power_img"][i], np.float64), batch["old_offset"][i], batch["prior"][i],
+                [batch["highres_Xi2"][i], batch["norm_correction"][i]]]
+    with tempfile.TemporaryDirectory() as td:
+        rq, rs = os.path.join(td, "req.bin"), os.path.join(td, "out.bin")
+        np.concatenate([np.ravel(np.asarray(q, np.float64)) for q in req]).tofile(rq)
+        p = subprocess.run([ESTEP_BIN, rq, rs], stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)
+        if p.returncode != 0:
+            raise RuntimeError("ref_estep failed: %s" % p.stderr.strip())
+        out = np.fromfile(rs, np.float64)
+    k = 0
+    parts = []
+    for i in range(n):
+        rec = {}
+        for ipass, tag in ((0, "coarse"), (1, "fine")):
+            cnt = int(out[k])
+            k += 1
+            rec[tag + "_diff2"] = out[k:k + cnt]
+            k += cnt
+            rec[tag + "_weight"] = out[k:k + cnt]
+            k += cnt
+            if ipass == 0:
+                rec["coarse_significant"] = out[k:k + cnt].astype(bool)
+                k += cnt
+        for s in SCALARS:
+            rec[s] = out[k]
+            k += 1
+        for s in METADATA:
+            rec[s] = out[k]
+            k += 1
+        parts.append(rec)
+    half = int(m["ori_size"]) // 2 + 1
+    ndir = len(m["pdf_direction"])
+    ws = dict(sigma2_noise=out[k:k + half])
+    k += half
+    ws["pdf_class"] = out[k:k + 1]
+    k += 1
+    ws["pdf_direction"] = out[k:k + ndir]
+    k += ndir
+    for s in ("sigma2_offset", "sumw_group", "LL", "ave_Pmax", "avg_norm_correction"):
+        ws[s] = out[k]
+        k += 1
+    xd, yd, zd = [int(v) for v in out[k:k + 3]]
+    k += 3
+    nv = xd * yd * zd
+    bp_data = out[k:k + 2 * nv].view(np.complex128).reshape(zd, yd, xd)
+    k += 2 * nv
+    bp_weight = out[k:k + nv].reshape(zd, yd, xd)
+    return parts, ws, bp_data, bp_weight

@@ -280,13 +280,40 @@ double class_prior(const oracle_model &m, long iclass, int axis) {
 // The inverse of the rotation is taken as its transpose (A.inv() in the
 // reference; the two agree to rounding).  `out` is zero-filled first: points
 // outside r_max stay zero, as in a freshly resized MultidimArray.
+// Matrix2D<RFLOAT>::inv of a 3x3 matrix (src/matrix2d.h:1098-1125: the
+// adjugate divided by the determinant, in the reference's order of
+// operations), then *= padding factor (src/projector.cpp:638,
+// src/backprojector.cpp:80-81).  The reference decides whether pixels exactly
+// on the r_max circle are projected / inserted from this matrix in double
+// precision, so the oracle uses the same matrix and the same tests.
+void ref_inverse_pad(const double A[9], double pad, double Ai[9]) {
+    const double a00 = A[0], a01 = A[1], a02 = A[2], a10 = A[3], a11 = A[4], a12 = A[5], a20 = A[6], a21 = A[7],
+                 a22 = A[8];
+    double r[9];
+    r[0] = a22 * a11 - a21 * a12;
+    r[1] = -(a22 * a01 - a21 * a02);
+    r[2] = a12 * a01 - a11 * a02;
+    r[3] = -(a22 * a10 - a20 * a12);
+    r[4] = a22 * a00 - a20 * a02;
+    r[5] = -(a12 * a00 - a10 * a02);
+    r[6] = a21 * a10 - a20 * a11;
+    r[7] = -(a21 * a00 - a20 * a01);
+    r[8] = a11 * a00 - a10 * a01;
+    const double tmp = a00 * r[0] + a10 * r[1] + a20 * r[2];
+    for (int k = 0; k < 9; ++k) Ai[k] = (r[k] / tmp) * pad;
+}
+
 void project(const oracle_model &m, long iclass, const double A[9], long size, Cplx *out) {
     const long X = size / 2 + 1, Y = size;
     std::memset(out, 0, sizeof(Cplx) * X * Y);
     const double pad = (double)m.padding_factor;
     double Ai[9];
-    for (int r = 0; r < 3; ++r)
-        for (int c = 0; c < 3; ++c) Ai[r * 3 + c] = A[c * 3 + r] * pad;
+    if (m.ref_dim == 2) {
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) Ai[r * 3 + c] = A[c * 3 + r] * pad;
+    } else {
+        ref_inverse_pad(A, pad, Ai);
+    }
     const int r_max_out = (int)X - 1;
     const int r_max_out_2 = r_max_out * r_max_out;
     const int r_max_ref = (int)(m.proj_r_max * m.padding_factor);
@@ -328,11 +355,9 @@ void project(const oracle_model &m, long iclass, const double A[9], long size, C
                 out[i * X + x] = v;
                 continue;
             }
-            // r_ref_2 > r_max_ref_2 in the reference (:672).  For a rotation
-            // |Ainv (x,y,0)|^2 = pad^2 (x^2+y^2) exactly; the test is made in
-            // integers so that pixels on the circle itself are decided
-            // independently of the last bit of the rotation matrix.
-            if ((long)m.padding_factor * m.padding_factor * (x * x + y2) > r_max_ref_2) continue;
+            // r_ref_2 > r_max_ref_2 (:672), in double precision as the reference
+            const double r_ref_2 = xp * xp + yp * yp + zp * zp;
+            if (r_ref_2 > r_max_ref_2) continue;
             bool neg = (xp < 0);
             if (neg) {
                 xp = -xp;
@@ -374,9 +399,18 @@ void backproject(const oracle_model &m, long iclass, const double A[9], long siz
                  const double *Mw, double *bp_data, double *bp_weight) {
     const double pad = (double)m.padding_factor;
     double Ai[9];
-    for (int r = 0; r < 3; ++r)
-        for (int c = 0; c < 3; ++c) Ai[r * 3 + c] = A[c * 3 + r] * pad;
+    if (m.ref_dim == 2) {
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) Ai[r * 3 + c] = A[c * 3 + r] * pad;
+    } else {
+        ref_inverse_pad(A, pad, Ai);
+    }
     const int max_r2 = r_round(m.bp_r_max * pad) * r_round(m.bp_r_max * pad);
+    // the ellipse |Ainv (x, y)|^2 <= max_r2 bounding x per row (:84-92, :150-160)
+    const double AtA_xx = Ai[0] * Ai[0] + Ai[3] * Ai[3] + Ai[6] * Ai[6];
+    const double AtA_xy = Ai[0] * Ai[1] + Ai[3] * Ai[4] + Ai[6] * Ai[7];
+    const double AtA_yy = Ai[1] * Ai[1] + Ai[4] * Ai[4] + Ai[7] * Ai[7];
+    const double AtA_xy2 = AtA_xy * AtA_xy;
     const long s = size, sh = size / 2 + 1;
     const long xd = m.bp_xdim, yd = m.bp_ydim, zd = m.bp_zdim;
     const size_t vox = (size_t)xd * yd * zd;
@@ -391,18 +425,29 @@ void backproject(const oracle_model &m, long iclass, const double A[9], long siz
             y = (int)(i - s);
             first_allowed_x = 1;
         }
-        // The reference bounds x by the ellipse |Ainv (x,y)|^2 <= max_r2
-        // (:150-160) and re-checks r2_3D > max_r2 (:188).  For a rotation the
-        // ellipse is the circle pad^2 (x^2+y^2) <= max_r2; it is evaluated in
-        // integers so that pixels on the circle are decided exactly.
-        for (int x = first_allowed_x; x <= (int)(sh - 1); ++x) {
-            if ((long)m.padding_factor * m.padding_factor * ((long)x * x + (long)y * y) > max_r2) continue;
+        // x bounded by the ellipse of this row (:150-160) and r2_3D > max_r2
+        // re-checked per pixel (:188), in double precision as the reference;
+        // 2D: the integer circle test of backrotate2D
+        int first_x = first_allowed_x, last_x = (int)(sh - 1);
+        if (m.ref_dim != 2) {
+            const double discr = AtA_xy2 * y * y - AtA_xx * (AtA_yy * y * y - max_r2);
+            if (discr < 0.) continue;
+            const double d = std::sqrt(discr) / AtA_xx;
+            const double q = -AtA_xy * y / AtA_xx;
+            first_x = std::max(first_x, r_ceil(q - d));
+            last_x = std::min(last_x, r_floor(q + d));
+        }
+        for (int x = first_x; x <= last_x; ++x) {
+            if (m.ref_dim == 2 &&
+                (long)m.padding_factor * m.padding_factor * ((long)x * x + (long)y * y) > max_r2)
+                continue;
             Cplx val = f2d[i * sh + x];
             double w = Mw[i * sh + x];
             if (w <= 0.) continue;
             double xp = Ai[0] * x + Ai[1] * y;
             double yp = Ai[3] * x + Ai[4] * y;
             double zp = Ai[6] * x + Ai[7] * y;
+            if (m.ref_dim != 2 && xp * xp + yp * yp + zp * zp > max_r2) continue;
             bool neg = xp < 0;
             if (neg) {
                 xp = -xp;

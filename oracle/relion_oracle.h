@@ -7,15 +7,22 @@
  * arm may load the library built from relion_oracle.cpp; the product path
  * (libgbrelion) never links or calls it.
  *
- * Parity pins:
+ * Parity pins (the reference's own code, built from its sources by
+ * oracle/build_ref.sh into oracle/_ref, and golden vectors of it under
+ * tests/golden):
  *   - CTF value: reference tests/ctf.cpp:8-9 (getCTF(10,10) = 0.59154).
- *   - HEALPix NEST enumeration: compared index-for-index and bit-for-bit
- *     against the reference's own src/Healpix_2.15a/healpix_base.cc, compiled
- *     from its source files into oracle/_ref (see oracle/build_ref.sh).
- *   - Everything downstream of the enumeration (projection, diff2, weights,
- *     significance, weighted sums, backprojection) is a restatement of
- *     src/ml_optimiser.cpp, src/projector.cpp and src/backprojector.cpp
- *     that the reference's tests do not pin (no golden vectors exist).
+ *   - HEALPix NEST enumeration: bit-for-bit against
+ *     src/Healpix_2.15a/healpix_base.cc.
+ *   - The E-step itself: MlOptimiser::getAllSquaredDifferences,
+ *     convertAllSquaredDifferencesToWeights and storeWeightedSums of the
+ *     reference (oracle/_ref/ref_estep) on the same prepared particles give
+ *     the same coarse and fine diff2, weights, significance sets, fine pose
+ *     sets, best poses, PMAX, dLL, weighted sums and backprojected volumes
+ *     (bit-identical on x86-64 with this build's flags).
+ *   - Building blocks: Projector::project, BackProjector::backproject2Dto3D,
+ *     CTF::getFftwImage, HealpixSampling, shiftImageInFourierTransform,
+ *     Euler_angles2matrix, BackProjector::reconstruct and
+ *     Projector::computeFourierTransformMap (oracle/_ref/ref_pin).
  */
 #ifndef RELION_ORACLE_H
 #define RELION_ORACLE_H

@@ -165,6 +165,12 @@ struct gbr_bundle {
     DevBuf<PixelRef> pc, pf;
     DevBuf<float> minv_c, minv_f, minv_store;
     DevBuf<float> eul_c, eul_f;
+    // pixels exactly on the r_max circle: bit index per pixel (-1 elsewhere)
+    // and per orientation the bits of those the reference projects /
+    // backprojects (3D; decided on the host as the reference decides them)
+    DevBuf<int> pcirc_c, pcirc_f, bcirc_f;
+    DevBuf<unsigned long long> pmask_c, pmask_f, bmask_f;
+    bool use_circ = false;
     DevBuf<int> cls_c, cls_f, cls_of_r;
     DevBuf<float> pdf_orient;
     float pdf_orient_min = 0.f;  // smallest non-zero normalised pdf_orient
@@ -308,6 +314,81 @@ struct gbr_worker {
 
 namespace {
 
+// ---- the reference's inside-r_max decisions, in double precision ---------
+// Pixels strictly inside or outside the r_max circle are decided exactly by
+// integers (|Ainv (x, y, 0)|^2 = pad^2 (x^2 + y^2) for a rotation); for the
+// few pixels exactly on the circle the reference's double-precision tests
+// decide, by the last bits of its inverted rotation matrix, and are restated
+// here with the same operations (this file is compiled without contraction
+// of multiply-adds).
+inline int r_ceil(double x) { return (x == (int)x) ? (int)x : ((x > 0) ? (int)(x + 1) : (int)x); }
+inline int r_floor(double x) { return (x == (int)x) ? (int)x : ((x > 0) ? (int)x : (int)(x - 1)); }
+
+// Matrix2D<RFLOAT>::inv of a 3x3 matrix (src/matrix2d.h:1098-1125: adjugate
+// over determinant) times the padding factor (src/projector.cpp:638).
+void ref_inverse_pad(const double A[9], double pad, double Ai[9]) {
+    const double a00 = A[0], a01 = A[1], a02 = A[2], a10 = A[3], a11 = A[4], a12 = A[5], a20 = A[6], a21 = A[7],
+                 a22 = A[8];
+    double r[9];
+    r[0] = a22 * a11 - a21 * a12;
+    r[1] = -(a22 * a01 - a21 * a02);
+    r[2] = a12 * a01 - a11 * a02;
+    r[3] = -(a22 * a10 - a20 * a12);
+    r[4] = a22 * a00 - a20 * a02;
+    r[5] = -(a12 * a00 - a10 * a02);
+    r[6] = a21 * a10 - a20 * a11;
+    r[7] = -(a21 * a00 - a20 * a01);
+    r[8] = a11 * a00 - a10 * a01;
+    const double tmp = a00 * r[0] + a10 * r[1] + a20 * r[2];
+    for (int k = 0; k < 9; ++k) Ai[k] = (r[k] / tmp) * pad;
+}
+
+// Projector::project keeps pixel (x, y) unless r_ref_2 > r_max_ref_2
+// (src/projector.cpp:665-672).
+bool ref_projects(const double Ai[9], int x, int y, int r_max_ref_2) {
+    const double xp = Ai[0] * x + Ai[1] * y, yp = Ai[3] * x + Ai[4] * y, zp = Ai[6] * x + Ai[7] * y;
+    return !(xp * xp + yp * yp + zp * zp > r_max_ref_2);
+}
+
+// BackProjector::backproject2Dto3D inserts pixel (x, y) when x lies within
+// the row's ellipse bounds (src/backprojector.cpp:84-92, :150-160) and
+// r2_3D <= max_r2 (:188); no Ewald sphere, identity magnification.
+bool ref_inserts(const double Ai[9], int x, int y, int max_r2, int sh) {
+    const double AtA_xx = Ai[0] * Ai[0] + Ai[3] * Ai[3] + Ai[6] * Ai[6];
+    const double AtA_xy = Ai[0] * Ai[1] + Ai[3] * Ai[4] + Ai[6] * Ai[7];
+    const double AtA_yy = Ai[1] * Ai[1] + Ai[4] * Ai[4] + Ai[7] * Ai[7];
+    const double AtA_xy2 = AtA_xy * AtA_xy;
+    const double discr = AtA_xy2 * y * y - AtA_xx * (AtA_yy * y * y - max_r2);
+    if (discr < 0.) return false;
+    const double dd = std::sqrt(discr) / AtA_xx;
+    const double q = -AtA_xy * y / AtA_xx;
+    const int first_allowed_x = y < 0 ? 1 : 0;
+    const int first_x = std::max(r_ceil(q - dd), first_allowed_x), last_x = std::min(r_floor(q + dd), sh - 1);
+    if (x < first_x || x > last_x) return false;
+    const double xp = Ai[0] * x + Ai[1] * y, yp = Ai[3] * x + Ai[4] * y, zp = Ai[6] * x + Ai[7] * y;
+    return !(xp * xp + yp * yp + zp * zp > max_r2);
+}
+
+// Bit index of each pixel of a list that lies exactly on the circle
+// pad^2 (x^2 + y^2) == r2 (-1 elsewhere); the number of such pixels.
+int circle_bits(const std::vector<PixelRef> &px, long pad, long r2, std::vector<int> &bit) {
+    bit.assign(px.size(), -1);
+    int nb = 0;
+    for (size_t j = 0; j < px.size(); ++j)
+        if (pad * pad * ((long)px[j].x * px[j].x + (long)px[j].y * px[j].y) == r2) bit[j] = nb++;
+    return nb;
+}
+
+unsigned long long circle_mask(const std::vector<PixelRef> &px, const std::vector<int> &bit, const double Ai[9],
+                               bool backproject, int r2, int sh) {
+    unsigned long long m = 0ull;
+    for (size_t j = 0; j < px.size(); ++j)
+        if (bit[j] >= 0 &&
+            (backproject ? ref_inserts(Ai, px[j].x, px[j].y, r2, sh) : ref_projects(Ai, px[j].x, px[j].y, r2)))
+            m |= 1ull << bit[j];
+    return m;
+}
+
 int build_tables(gbr_bundle *b) {
     if (b->tables_ready) return GBR_OK;
     b->blk_ready = false;
@@ -376,7 +457,20 @@ int build_tables(gbr_bundle *b) {
             for (long is = 0; is < b->NP; ++is) mean += b->pdf_dir[ic * b->ND + id];
     mean /= (double)R;
     std::vector<double> fr(b->nOR), ft(b->nOR), fp(b->nOR);
-    double A[9];
+    double A[9], Ai[9];
+    // r_max-circle pixels of the coarse / fine lists (projector geometry) and
+    // of the fine list (backprojector geometry)
+    std::vector<int> pcc, pcf, bcf;
+    const long pr2 = (long)b->pg.r_max * b->pg.pad * b->pg.r_max * b->pg.pad;
+    const long brr = iround((double)b->bg.r_max * b->bg.pad);
+    const long br2 = brr * brr;
+    b->use_circ = !b->is2d;
+    const int nbc = circle_bits(b->pc_h, b->pg.pad, pr2, pcc), nbf = circle_bits(b->pf_h, b->pg.pad, pr2, pcf),
+              nbb = circle_bits(b->pf_h, b->bg.pad, br2, bcf);
+    if (b->use_circ && (nbc > 64 || nbf > 64 || nbb > 64))
+        return fail(GBR_ERR_UNSUPPORTED, "more than 64 pixels on the r_max circle");
+    std::vector<unsigned long long> pmc(b->use_circ ? R : 0), pmf(b->use_circ ? RF : 0), bmf(b->use_circ ? RF : 0);
+    const int shf = b->cur / 2 + 1;
     for (long ic = 0; ic < b->K; ++ic)
         for (long id = 0; id < b->ND; ++id)
             for (long is = 0; is < b->NP; ++is) {
@@ -384,6 +478,10 @@ int build_tables(gbr_bundle *b) {
                 euler_to_matrix(b->grid.dir_rot[id], b->grid.dir_tilt[id], b->grid.psi[is], A);
                 for (int a = 0; a < 3; ++a)
                     for (int c = 0; c < 3; ++c) ec[(size_t)r * 9 + a * 3 + c] = (float)(A[c * 3 + a] * d.padding_factor);
+                if (b->use_circ && nbc) {
+                    ref_inverse_pad(A, (double)b->pg.pad, Ai);
+                    pmc[r] = circle_mask(b->pc_h, pcc, Ai, false, (int)pr2, 0);
+                }
                 double pdf = b->pdf_dir[ic * b->ND + id];
                 if (mean != 0.) pdf /= mean;
                 po[r] = (b->pdf_class[ic] > 0. && b->pdf_dir[ic * b->ND + id] > 0.) ? (float)pdf : 0.f;
@@ -396,6 +494,12 @@ int build_tables(gbr_bundle *b) {
                     for (int a = 0; a < 3; ++a)
                         for (int c = 0; c < 3; ++c)
                             ef[(size_t)rf * 9 + a * 3 + c] = (float)(A[c * 3 + a] * d.padding_factor);
+                    if (b->use_circ && (nbf || nbb)) {
+                        ref_inverse_pad(A, (double)b->pg.pad, Ai);
+                        if (nbf) pmf[rf] = circle_mask(b->pf_h, pcf, Ai, false, (int)pr2, 0);
+                        if (b->bg.pad != b->pg.pad) ref_inverse_pad(A, (double)b->bg.pad, Ai);
+                        if (nbb) bmf[rf] = circle_mask(b->pf_h, bcf, Ai, true, (int)br2, shf);
+                    }
                     cf[rf] = (int)ic;
                 }
             }
@@ -405,6 +509,14 @@ int build_tables(gbr_bundle *b) {
     GBR_CUDA(b->cls_f.upload(cf.data(), cf.size()));
     GBR_CUDA(b->cls_of_r.upload(cr.data(), cr.size()));
     GBR_CUDA(b->pdf_orient.upload(po.data(), po.size()));
+    if (b->use_circ) {
+        GBR_CUDA(b->pcirc_c.upload(pcc.data(), pcc.size()));
+        GBR_CUDA(b->pcirc_f.upload(pcf.data(), pcf.size()));
+        GBR_CUDA(b->bcirc_f.upload(bcf.data(), bcf.size()));
+        GBR_CUDA(b->pmask_c.upload(pmc.data(), pmc.size()));
+        GBR_CUDA(b->pmask_f.upload(pmf.data(), pmf.size()));
+        GBR_CUDA(b->bmask_f.upload(bmf.data(), bmf.size()));
+    }
     b->pdf_orient_min = 0.f;
     b->pdf_orient_max = 0.f;
     for (float v : po) {
@@ -446,7 +558,8 @@ int build_tables(gbr_bundle *b) {
     GBR_CUDA(b->proj_c.zero());
     GBR_CUDA(b->proj2_c.zero());
     GBR_CUDA(launch_project_rows(b->vols_d.p, b->pg, b->eul_c.p, b->cls_c.p, nullptr, (int)R, b->pc.p, b->nc,
-                                 b->proj_c.p, b->lda_c, b->proj2_c.p, b->ldk_c, nullptr, 0));
+                                 b->proj_c.p, b->lda_c, b->proj2_c.p, b->ldk_c, nullptr, 0,
+                                 b->use_circ ? b->pcirc_c.p : nullptr, b->use_circ ? b->pmask_c.p : nullptr));
     if (d.precision == GBR_PREC_BF16) {
         GBR_CUDA(b->proj_c_tc.reserve(tc_a_bytes((int)R, 2 * b->nc)));
         GBR_CUDA(launch_tc_pack_a(b->proj_c.p, b->lda_c, (int)R, 2 * b->nc, b->proj_c_tc.p, 0));
@@ -463,7 +576,8 @@ int build_tables(gbr_bundle *b) {
     GBR_CUDA(b->proj_f.zero());
     GBR_CUDA(b->proj2_f.zero());
     GBR_CUDA(launch_project_rows(b->vols_d.p, b->pg, b->eul_f.p, b->cls_f.p, nullptr, (int)RF, b->pf.p, b->nf,
-                                 b->proj_f.p, b->lda_f, b->proj2_f.p, b->ldk_f, nullptr, 0));
+                                 b->proj_f.p, b->lda_f, b->proj2_f.p, b->ldk_f, nullptr, 0,
+                                 b->use_circ ? b->pcirc_f.p : nullptr, b->use_circ ? b->pmask_f.p : nullptr));
     // ---- slice accumulators ----
     GBR_CUDA(b->bpimg.reserve((size_t)RF * b->nf));
     GBR_CUDA(b->bpw.reserve((size_t)RF * b->nf));
@@ -947,7 +1061,8 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
     GBR_CUDA(launch_compact_flags(b->active.p, (int)b->RF, w->act_list.p, w->act_count.p, st));
     GBR_CUDA(launch_backproject(w->act_list.p, w->act_count.p, (int)b->RF, b->eul_f.p, nOR, b->cls_of_r.p,
                                 b->bpimg.p, b->bpw.p, b->pf.p, b->nf, b->bg, b->bpd_ptrs.p, b->bpw_ptrs.p,
-                                b->active.p, st));
+                                b->active.p, st, b->use_circ ? b->bcirc_f.p : nullptr,
+                                b->use_circ ? b->bmask_f.p : nullptr));
     GBR_CUDA(cudaEventRecord(w->ev[9], st));
     w->launches += 2;
     // ---- results ----

@@ -79,10 +79,14 @@ cudaError_t launch_phase_table(float2 *out, const double *tx, const double *ty, 
 // Project n orientations (matrices Ainv*pad, row-major float[9]) of class
 // volumes; orientation o uses class cls[o].  Output either interleaved
 // (re,im) rows of `ld` floats (+ |P|^2 rows of `ld2` floats) or float2 rows.
+// circ / mask (optional): per pixel the bit index of pixels exactly on the
+// r_max circle (-1 elsewhere) and per orientation the bits of those the
+// reference projects (Projector::project decides them in double precision).
 cudaError_t launch_project_rows(const float2 *const *vols, const VolGeom &g, const float *eul,
                                 const int *cls, const int *orient_ids, int n_orient,
                                 const PixelRef *pix, int npix, float *out_ri, int ld, float *out_p2,
-                                int ld2, float2 *out_c, cudaStream_t st);
+                                int ld2, float2 *out_c, cudaStream_t st, const int *circ = nullptr,
+                                const unsigned long long *mask = nullptr);
 
 // FP32 FMA throughput probe (ms of one timed launch and its flop count).
 cudaError_t launch_fp32_probe(float *ms, double *flops);
@@ -269,10 +273,14 @@ void destroy_fft_plan(long long plan);
 
 cudaError_t launch_compact_flags(const unsigned char *flags, int n, int *list, int *count,
                                  cudaStream_t st);
+// circ / mask: as launch_project_rows, for the backprojection's own test
+// (BackProjector::backproject2Dto3D decides the r_max-circle pixels in double
+// precision by its per-row ellipse bounds and its 3D radius check).
 cudaError_t launch_backproject(const int *list, const int *count, int max_list, const float *eul_f, int nOR,
                                const int *cls_of_r, float2 *bpimg, float *bpw, const PixelRef *pf, int nf,
                                const VolGeom &g, double2 *const *data, double *const *weight,
-                               unsigned char *active, cudaStream_t st);
+                               unsigned char *active, cudaStream_t st, const int *circ = nullptr,
+                               const unsigned long long *mask = nullptr);
 cudaError_t launch_gather_pdat(const double *old_offset, const double *prior, const double *xi2,
                                const double *norm, const double *scale, int n, double *pdat, cudaStream_t st);
 cudaError_t launch_cand_seg(const unsigned int *cnt, int n, int cap, long long *seg, cudaStream_t st);

@@ -1240,7 +1240,8 @@ __global__ void k_backproject(const int *__restrict__ list, const float *__restr
                               float *__restrict__ bpw, const PixelRef *__restrict__ pf, int nf,
                               const VolGeom g, double2 *const *__restrict__ data,
                               double *const *__restrict__ weight, unsigned char *__restrict__ active,
-                              const int *__restrict__ count) {
+                              const int *__restrict__ count, const int *__restrict__ circ,
+                              const unsigned long long *__restrict__ cmask) {
     const int nlist = *count;
     for (int li = blockIdx.x; li < nlist; li += gridDim.x) {
     const int rf = list[li];
@@ -1263,6 +1264,9 @@ __global__ void k_backproject(const int *__restrict__ list, const float *__restr
         if (!(w > 0.f)) continue;
         const PixelRef pr = pf[k];
         if (g.pad * g.pad * (pr.x * pr.x + pr.y * pr.y) > max_r2) continue;
+        // pixels on the r_max circle: inserted where the reference inserts them
+        const int cb = circ ? circ[k] : -1;
+        if (cb >= 0 && !((cmask[rf] >> cb) & 1ull)) continue;
         float xp = fmaf(Ai[0], (float)pr.x, Ai[1] * (float)pr.y);
         float yp = fmaf(Ai[3], (float)pr.x, Ai[4] * (float)pr.y);
         if (g.dim == 2) {
@@ -1659,8 +1663,10 @@ cudaError_t launch_compact_flags(const unsigned char *flags, int n, int *list, i
 cudaError_t launch_backproject(const int *list, const int *count, int max_list, const float *eul_f, int nOR,
                                const int *cls_of_r, float2 *bpimg, float *bpw, const PixelRef *pf, int nf,
                                const VolGeom &g, double2 *const *data, double *const *weight,
-                               unsigned char *active, cudaStream_t st) {
+                               unsigned char *active, cudaStream_t st, const int *circ,
+                               const unsigned long long *mask) {
     if (max_list <= 0) return cudaSuccess;
+    if ((circ == nullptr) != (mask == nullptr)) return cudaErrorInvalidValue;
     // slices are read from the device-side list; the grid covers the device
     // a few times over and loops over the slices present
     int dev = 0, nsm = 148;
@@ -1668,7 +1674,7 @@ cudaError_t launch_backproject(const int *list, const int *count, int max_list, 
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     const int grid = std::min(max_list, 8 * nsm);
     k_backproject<<<grid, 256, 0, st>>>(list, eul_f, nOR, cls_of_r, bpimg, bpw, pf, nf, g, data, weight,
-                                        active, count);
+                                        active, count, circ, mask);
     return cudaGetLastError();
 }
 

@@ -79,11 +79,16 @@ __device__ __forceinline__ float2 sample_slice(const float2 *__restrict__ vol, c
     return v;
 }
 
+// circ[j] >= 0 marks the pixels exactly on the r_max circle; bit circ[j] of
+// mask[orientation] says whether the reference projects it for that
+// orientation (decided on the host in double precision as
+// Projector::project does, src/projector.cpp:638-672).
 __global__ void k_project_rows(const float2 *const *__restrict__ vols, const VolGeom g,
                                const float *__restrict__ eul, const int *__restrict__ cls,
                                const int *__restrict__ orient_ids, int n_orient,
                                const PixelRef *__restrict__ pix, int npix, float *__restrict__ out_ri,
-                               int ld, float *__restrict__ out_p2, int ld2, float2 *__restrict__ out_c) {
+                               int ld, float *__restrict__ out_p2, int ld2, float2 *__restrict__ out_c,
+                               const int *__restrict__ circ, const unsigned long long *__restrict__ mask) {
     const int o = blockIdx.y;
     if (o >= n_orient) return;
     const int oid = orient_ids ? orient_ids[o] : o;
@@ -91,9 +96,11 @@ __global__ void k_project_rows(const float2 *const *__restrict__ vols, const Vol
     if (threadIdx.x < 9) Ai[threadIdx.x] = eul[(size_t)oid * 9 + threadIdx.x];
     __syncthreads();
     const float2 *vol = vols[cls[oid]];
+    const unsigned long long cm = mask ? mask[oid] : ~0ull;
     for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < npix; j += gridDim.x * blockDim.x) {
         const PixelRef pr = pix[j];
-        const float2 v = sample_slice(vol, g, Ai, pr.x, pr.y);
+        const int cb = circ ? circ[j] : -1;
+        const float2 v = (cb >= 0 && !((cm >> cb) & 1ull)) ? make_float2(0.f, 0.f) : sample_slice(vol, g, Ai, pr.x, pr.y);
         if (out_ri) {
             float *row = out_ri + (size_t)oid * ld;
             row[2 * j] = v.x;
@@ -130,7 +137,8 @@ __global__ void k_phase_table(float2 *__restrict__ out, const double *__restrict
 cudaError_t launch_project_rows(const float2 *const *vols, const VolGeom &g, const float *eul,
                                 const int *cls, const int *orient_ids, int n_orient,
                                 const PixelRef *pix, int npix, float *out_ri, int ld, float *out_p2,
-                                int ld2, float2 *out_c, cudaStream_t st) {
+                                int ld2, float2 *out_c, cudaStream_t st, const int *circ,
+                                const unsigned long long *mask) {
     if (n_orient <= 0 || npix <= 0) return cudaSuccess;
     const int threads = 128;
     const int bx = (npix + threads - 1) / threads;
@@ -140,11 +148,13 @@ cudaError_t launch_project_rows(const float2 *const *vols, const VolGeom &g, con
         k_project_rows<<<grid, threads, 0, st>>>(vols, g, eul, cls, orient_ids ? orient_ids + o0 : nullptr,
                                                  n, pix, npix, out_ri ? out_ri + (orient_ids ? 0 : (size_t)o0 * ld) : nullptr,
                                                  ld, out_p2 ? out_p2 + (orient_ids ? 0 : (size_t)o0 * ld2) : nullptr,
-                                                 ld2, out_c ? out_c + (orient_ids ? 0 : (size_t)o0 * npix) : nullptr);
+                                                 ld2, out_c ? out_c + (orient_ids ? 0 : (size_t)o0 * npix) : nullptr,
+                                                 circ, mask);
         if (!orient_ids) {
-            // rows are addressed by the orientation index; shift eul/cls too
+            // rows are addressed by the orientation index; shift eul/cls/mask too
             eul += (size_t)n * 9;
             cls += n;
+            if (mask) mask += n;
         }
     }
     return cudaGetLastError();

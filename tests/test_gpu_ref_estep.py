@@ -1,0 +1,65 @@
+"""GPU parity against the reference's own E-step.
+
+The plain FP32 path, through the C ABI, on the seeded prepared particles of
+tests/golden/ref_estep_golden.npz, against the results the reference's
+MlOptimiser E-step (getAllSquaredDifferences,
+convertAllSquaredDifferencesToWeights, storeWeightedSums; built from its
+sources, tests/golden/make_ref_estep_golden.py) gave on the same inputs:
+best pose and offsets equal, significant-sample count equal, PMAX within
+1e-4 relative, dLL within 1e-2, sigma2 noise and pdf_direction within 1e-5
+relative, and the backprojected volumes within 1e-5 relative L2 (outer shell
+included: the pixels on the r_max circle are inserted where the reference
+inserts them) and their norms within 1e-5.
+"""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "golden"))
+import make_ref_estep_golden as G  # noqa: E402
+
+GOLD = os.path.join(HERE, "golden", "ref_estep_golden.npz")
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(np.ravel(np.asarray(a) - np.asarray(b))) / max(np.linalg.norm(np.ravel(b)), 1e-300))
+
+
+@pytest.mark.parametrize("case", G.CASES, ids=[c[0] for c in G.CASES])
+def test_plain_path_matches_reference_estep(case):
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from relion_gb300.estep import MlDeviceBundle, MlOptimiserCuda
+    g = np.load(GOLD)
+    name, _, _, n, _ = case
+    ds = G.dataset(case)
+    m = ds.model(precision=0)
+    b = MlDeviceBundle(m, device=0)
+    r = ds.ref
+    b.setup_projector(0, r["data"], r["yinit"], r["zinit"], r["r_max"], r["pad"])
+    w = MlOptimiserCuda(b)
+    res = w.do_expectation_some_particles(ds.particles(0, n))
+    ws = b.get_wsum()
+    bd, bw = b.get_mdl_data(0)
+    w.close()
+    b.close()
+    print(name, {k: (np.asarray(res[k]).tolist(), g["%s/%s" % (name, k)].tolist()) for k in ("pmax", "nr_sign")})
+    for k in ("rot", "tilt", "psi", "xoff", "yoff", "nr_sign"):
+        np.testing.assert_allclose(np.asarray(res[k]), g["%s/%s" % (name, k)], rtol=0, atol=1e-9, err_msg=k)
+    np.testing.assert_allclose(res["pmax"], g["%s/pmax" % name], rtol=1e-4)
+    np.testing.assert_allclose(res["dLL"], g["%s/dLL" % name], atol=1e-2)
+    assert _rel(ws["sigma2_noise"], g["%s/wsum_sigma2_noise" % name]) <= 1e-5
+    assert _rel(np.ravel(ws["pdf_direction"]), g["%s/wsum_pdf_direction" % name]) <= 1e-5
+    idx = g["%s/bp_idx" % name]
+    d_rel = _rel(bd.ravel()[idx], g["%s/bp_data_sub" % name])
+    w_rel = _rel(bw.ravel()[idx], g["%s/bp_weight_sub" % name])
+    print(name, "volume sample rel L2: data %.2e weight %.2e" % (d_rel, w_rel))
+    assert d_rel <= 1e-5 and w_rel <= 1e-5
+    np.testing.assert_allclose(np.linalg.norm(bd), g["%s/bp_data_norm" % name], rtol=1e-5)
+    np.testing.assert_allclose(np.linalg.norm(bw), g["%s/bp_weight_norm" % name], rtol=1e-5)
