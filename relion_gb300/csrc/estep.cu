@@ -917,7 +917,16 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
         w->launches += 3;  // prep, pdf_offset, norms
     }
     GBR_CUDA(cudaEventRecord(w->ev[2], st));
-    const bool restricted = w->restrict_blocks != nullptr;
+    // a pass whose particles all fall back to the exhaustive search runs the
+    // exhaustive kernel (no work-item list)
+    bool restricted = w->restrict_blocks != nullptr;
+    if (restricted) {
+        bool all = true;
+        for (int p = 0; p < n && all; ++p)
+            all = w->restrict_blocks[(size_t)(w->pass_p0 + p) * w->restrict_m] == GBR_ALL_BLOCKS;
+        if (all) restricted = false;
+        w->last_items = all ? (long long)n * (R / (kDirsPerBlock * (int)b->NP)) : 0;
+    }
     const bool use_rowmin = d.precision == GBR_PREC_BF16 && (restricted || (T >= 32 && w->coarse_rows == 0));
     // sparse diff2 writes: only row segments near the running minimum are
     // stored (the debug read-back reports the others as not computed); the
