@@ -175,7 +175,13 @@ typedef enum {
                                  minimum (default), 1 read every row                  */
     GBR_OPT_CAND_CAP = 4,     /* coarse candidate-list entries per particle (65536)   */
     GBR_OPT_CAND_BUF = 5,     /* block-local candidate buffer entries (0: all)        */
-    GBR_OPT_BATCH_CAP = 6     /* particles per pass of a call (0: from the budget)    */
+    GBR_OPT_BATCH_CAP = 6,    /* particles per pass of a call (0: from the budget)    */
+    GBR_OPT_TILE_GROUP = 7,   /* precision form: orientation tiles of 128 rows per
+                                 group of the coarse kernel's tile order (0: 32)     */
+    GBR_OPT_KEEP_A = 8,       /* precision form: 1 reads the projection tiles with
+                                 an L2 keep policy (default 0)                        */
+    GBR_OPT_PAIR = 9          /* precision form: 1 runs the coarse cross term on SM
+                                 pairs (tcgen05 cta_group::2; default 0)             */
 } gbr_worker_option;
 int gbr_worker_set_option(gbr_worker *w, int option, int64_t value);
 

@@ -14,6 +14,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libgbrelion.so")
+ACC = os.path.join(HERE, "acc")
+ACC_LIB = os.path.join(BUILD, "libgbrelion_acc.so")
+INCLUDE = os.path.join(HERE, "..", "include")
 SOURCES = ["k_project.cu", "k_gemm.cu", "k_estep.cu", "estep.cu", "k_noalloc.cu", "k_tc.cu", "k_prepimg.cu", "k_recon.cu",
            "k_posenet.cu", "io.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -33,9 +36,34 @@ def _run(cmd):
     return proc.stdout
 
 
+def build_acc(force=False):
+    """Compile the C++ façade (relion_gb300/acc: AccProjector, AccBackprojector,
+    MlDeviceBundle, MlOptimiserCuda over the C ABI) into libgbrelion_acc.so,
+    linked against libgbrelion.so; return its path."""
+    srcs = [os.path.join(ACC, f) for f in sorted(os.listdir(ACC)) if f.endswith(".cpp")]
+    deps = [os.path.join(ACC, f) for f in os.listdir(ACC)] + [os.path.join(INCLUDE, "gbrelion.h"), LIB]
+    if (not force and os.path.exists(ACC_LIB)
+            and os.path.getmtime(ACC_LIB) >= max(os.path.getmtime(d) for d in deps)):
+        return ACC_LIB
+    tmp = ACC_LIB + ".tmp"
+    _run(["g++", "-std=c++17", "-O2", "-Wall", "-fPIC", "-shared", "-I", INCLUDE, "-I", ACC] + srcs +
+         ["-o", tmp, "-L", BUILD, "-lgbrelion", "-Wl,-rpath,$ORIGIN"])
+    os.replace(tmp, ACC_LIB)
+    return ACC_LIB
+
+
 def build(verbose=False, force=False):
-    """Compile libgbrelion.so if any source is newer than it; return its path."""
+    """Compile libgbrelion.so if any source is newer than it, then the C++
+    façade library; return the path of libgbrelion.so."""
     os.makedirs(BUILD, exist_ok=True)
+    _build_lib(verbose, force)
+    build_acc(force)
+    if verbose:
+        print("built", ACC_LIB)
+    return LIB
+
+
+def _build_lib(verbose, force):
     deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
     deps.append(os.path.join(HERE, "..", "include", "gbrelion.h"))
     if (not force and os.path.exists(LIB)

@@ -292,6 +292,7 @@ struct gbr_worker {
     DevBuf<int2> items_d;
     DevBuf<unsigned char> ytp;  // per-particle BF16 Y tiles of the restricted pass
     int batch_cap = 0;           // particles per pass (GBR_OPT_BATCH_CAP; 0 = from the budget)
+    TcTuning tc_tune;            // GBR_OPT_TILE_GROUP, GBR_OPT_KEEP_A, GBR_OPT_PAIR
     int pass_cap = 0;            // particles per pass of the current call
     // debug copies of the last call, one entry per pass (gbr_worker_debug_fetch)
     struct DbgPass {
@@ -953,7 +954,7 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
         GBR_CUDA(w->ytc.reserve(tc_y_bytes(n * T, 2 * b->nc)));
         GBR_CUDA(launch_tc_diff2(b->proj_c_tc.p, w->ytc.p, R, 2 * b->nc, w->b_c.p, b->ldk_c, b->phase_c.p, b->ldk_c, n,
                                  T, w->vals.p, w->nrm.p, b->pdf_orient.p, w->ps.p,
-                                 use_rowmin ? w->rowmin.p : nullptr, segmask, st));
+                                 use_rowmin ? w->rowmin.p : nullptr, segmask, st, w->tc_tune));
         w->launches += 2;  // operand packing + tensor-core kernel
     } else {
         GBR_CUDA(launch_gemm_diff2(b->proj_c.p, b->lda_c, R, 2 * b->nc, w->b_c.p, b->ldk_c, b->phase_c.p, b->ldk_c,
@@ -1356,6 +1357,15 @@ int gbr_worker_set_option(gbr_worker *w, int option, int64_t value) {
         case GBR_OPT_CAND_CAP: w->cand_cap_max = value > 0 ? (int)value : (1 << 16); break;
         case GBR_OPT_CAND_BUF: w->cand_buf = (int)value; break;
         case GBR_OPT_BATCH_CAP: w->batch_cap = (int)value; break;
+        case GBR_OPT_TILE_GROUP: w->tc_tune.group_m = (int)value; break;
+        case GBR_OPT_KEEP_A:
+            if (value > 1) return fail(GBR_ERR_INVALID, "keep_a must be 0 or 1");
+            w->tc_tune.keep_a = (int)value;
+            break;
+        case GBR_OPT_PAIR:
+            if (value > 1) return fail(GBR_ERR_INVALID, "pair must be 0 or 1");
+            w->tc_tune.pair = (int)value;
+            break;
         default: return fail(GBR_ERR_INVALID, "unknown worker option " + std::to_string(option));
     }
     return GBR_OK;

@@ -110,9 +110,19 @@ cudaError_t launch_tc_pack_a(const float *src, int lds, int M, int K2, void *dst
 // caller); with segmask non-null too (and T <= 960) it stores only the row
 // segments within ps[p].xs of the running minimum and marks them in segmask
 // (zeroed by the caller); the rest of `out` is left unwritten.
+// Tile order and cache use of the coarse tensor-core kernel: group_m
+// orientation tiles of 128 rows per group (0 = 32), keep_a reads the
+// projection tiles with an L2 keep policy, pair runs the SM-pair kernel
+// (cta_group::2, tiles of 256 orientations).
+struct TcTuning {
+    int group_m = 0;
+    int keep_a = 0;
+    int pair = 0;
+};
 cudaError_t launch_tc_diff2(const void *Ablk, void *Yblk, int M, int K2, const float2 *b, int ldb, const float2 *E,
                             int lde, int nparticles, int T, float *out, const float *norm, const float *pdf_orient,
-                            ParticleState *ps, unsigned int *rowmin, unsigned int *segmask, cudaStream_t st);
+                            ParticleState *ps, unsigned int *rowmin, unsigned int *segmask, cudaStream_t st,
+                            const TcTuning &tune = TcTuning());
 // Coarse cross term restricted to orientation blocks (precision form):
 // blocks of NB consecutive rows of the projection table (NB % 32 == 0,
 // NB <= 256, M % NB == 0) packed once per iteration; one work item per

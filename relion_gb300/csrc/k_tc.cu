@@ -38,7 +38,7 @@ constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
 constexpr int TRANSPOSE_BYTES = EPI_WARPS * 32 * 33 * 4;
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + TRANSPOSE_BYTES;
 constexpr int TMEM_COLS = 2 * TN;             // two accumulators
-constexpr int kGroupM = 32;
+constexpr int kGroupMDefault = 32;
 constexpr unsigned int kWaitLimit = 1u << 22;
 
 __device__ int g_tc_error;  // first failure code of the last launches (0 = ok)
@@ -155,6 +155,23 @@ __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t
                  : "memory");
 }
 
+// The same copy with an L2 cache policy (createpolicy) attached to its reads.
+__device__ __forceinline__ void bulk_g2s_hint(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar,
+                                              uint64_t policy) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(
+            dst),
+        "l"(src), "r"(bytes), "r"(bar), "l"(policy)
+        : "memory");
+}
+
+// L2 policy that keeps the lines it reads ahead of normal lines on eviction.
+__device__ __forceinline__ uint64_t policy_keep() {
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+
 struct TcArgs {
     const uint8_t *Ablk;     // [mtiles][ktiles][A_BYTES] BF16 tiles in shared-memory image
     const uint8_t *Yblk;     // [ntiles][ktiles][B_BYTES]
@@ -170,16 +187,19 @@ struct TcArgs {
     // within ps[p].xs of the particle's running minimum are stored, and bit
     // (chunk - first chunk of the row) of segmask[p][M] records them
     unsigned int *segmask;
+    int group_m;             // orientation tiles per group of the tile order (>= 1)
+    int keep_a;              // read the A tiles with an L2 keep policy
 };
 
-// Tile order of the persistent loop: groups of kGroupM orientation tiles,
+// Tile order of the persistent loop: groups of group_m orientation tiles,
 // orientation tile fastest inside a group, so that the CTAs running at the
-// same time share a few A tiles and sweep the Y tiles once per group.
-__device__ __forceinline__ void tile_mn(int tidx, int mtiles, int ntiles, int &mt, int &nt) {
-    const int per_group = kGroupM * ntiles;
+// same time share the group's A tiles (held in L2) and sweep the Y tiles
+// once per group: DRAM reads A once and Y ceil(mtiles / group_m) times.
+__device__ __forceinline__ void tile_mn(int tidx, int group_m, int mtiles, int ntiles, int &mt, int &nt) {
+    const int per_group = group_m * ntiles;
     const int g = tidx / per_group, r = tidx - g * per_group;
-    const int gm = min(kGroupM, mtiles - g * kGroupM);
-    mt = g * kGroupM + r % gm;
+    const int gm = min(group_m, mtiles - g * group_m);
+    mt = g * group_m + r % gm;
     nt = r / gm;
 }
 
@@ -208,6 +228,133 @@ __device__ __forceinline__ float near_cut(unsigned int run, float xs) {
 // lane and particle segment of the tile half).
 __device__ __forceinline__ void rowmin_flush(const TcArgs &a, int p, int m, float v) {
     if (p >= 0 && v < FLT_MAX) atomicMin(&a.rowmin[(size_t)p * a.M + m], f2ord(v));
+}
+
+// Epilogue of one cross-term tile: drains the 128 x 256 FP32 accumulator at
+// TMEM address acc (rows m0.., columns n0..) into diff2 = N(r,p) - 2 C with
+// the particles' running minima, row minima and sparse segment stores.  Warp
+// q = warp & 3 reads TMEM lanes 32 q.. (rows m0 + 32 q + lane), h the column
+// half 128 h..; tb is the warp's 32 x 33 transpose buffer.
+__device__ __forceinline__ void drain_cross(const TcArgs &a, uint32_t acc, int m0, int n0, int q, int h, int lane,
+                                            float *tb) {
+    const int m = m0 + q * 32 + lane;
+        const bool skip = !(m < a.M) || !(a.pdf_orient[m] > 0.f);
+        // running row minimum of the particle segment this lane is in
+        const bool track_rows = a.rowmin != nullptr && a.T >= 32 && !skip;
+        int acc_p = -1;
+        float acc_m = __int_as_float(0x7f800000);
+        for (int c = 0; c < 4; ++c) {
+            const int col = h * 128 + c * 32;
+            const int nb = n0 + col;
+            if (nb >= a.N) break;  // warp-uniform
+            const int nvalid = min(32, a.N - nb);
+            // rows whose segments of this chunk are stored (bit r = lane r's row)
+            unsigned int lo_rows = 0xFFFFFFFFu, hi_rows = 0xFFFFFFFFu;
+            int bnd_st = 32;
+            const int p_lo = nb / a.T;
+            // operands of the epilogue that do not depend on the accumulator
+            // are loaded before the TMEM read so their latency overlaps it:
+            // at most two particles in these 32 columns (T >= 32), p_lo for jj < bnd
+            const int bnd = (p_lo + 1) * a.T - nb;
+            float n_lo = 0.f, n_hi = 0.f, xs_lo = 0.f, xs_hi = 0.f;
+            unsigned int run_lo = 0xFFFFFFFFu, run_hi = 0xFFFFFFFFu;
+            if (a.T >= 32) {
+                if (!skip) n_lo = a.norm[(size_t)p_lo * a.M + m];
+                if (!skip && bnd < nvalid) n_hi = a.norm[(size_t)(p_lo + 1) * a.M + m];
+                if (a.segmask) {
+                    run_lo = __ldcg(&a.ps[p_lo].min_coarse);
+                    xs_lo = __ldg(&a.ps[p_lo].xs);
+                    if (bnd < nvalid) {
+                        run_hi = __ldcg(&a.ps[p_lo + 1].min_coarse);
+                        xs_hi = __ldg(&a.ps[p_lo + 1].xs);
+                    }
+                }
+            }
+            float v[32];
+            tmem_ld32(acc + ((uint32_t)(q * 32) << 16) + (uint32_t)col, v);
+            if (a.T >= 32) {
+                bnd_st = bnd;
+                float min_lo = __int_as_float(0x7f800000), min_hi = min_lo;
+#pragma unroll
+                for (int jj = 0; jj < 32; ++jj) {
+                    float d = __int_as_float(0x7f800000);
+                    if (!skip && jj < nvalid) {
+                        d = (jj < bnd ? n_lo : n_hi) - 2.f * v[jj];
+                        if (jj < bnd)
+                            min_lo = fminf(min_lo, d);
+                        else
+                            min_hi = fminf(min_hi, d);
+                    }
+                    v[jj] = d;
+                }
+                const bool two = bnd < nvalid;
+                const unsigned int u_lo = warp_min_flush(min_lo, &a.ps[p_lo].min_coarse);
+                const unsigned int u_hi = two ? warp_min_flush(min_hi, &a.ps[p_lo + 1].min_coarse) : 0xFFFFFFFFu;
+                if (a.segmask) {
+                    const bool near_lo = min_lo <= near_cut(min(u_lo, run_lo), xs_lo);
+                    const bool near_hi = two && min_hi <= near_cut(min(u_hi, run_hi), xs_hi);
+                    lo_rows = __ballot_sync(0xffffffffu, near_lo);
+                    hi_rows = __ballot_sync(0xffffffffu, near_hi);
+                    if (near_lo)
+                        atomicOr(&a.segmask[(size_t)p_lo * a.M + m], 1u << ((nb >> 5) - ((p_lo * a.T) >> 5)));
+                    if (near_hi) atomicOr(&a.segmask[(size_t)(p_lo + 1) * a.M + m], 1u);
+                }
+                if (lo_rows | hi_rows) {
+#pragma unroll
+                    for (int jj = 0; jj < 32; ++jj) tb[lane * 33 + jj] = v[jj];
+                }
+                if (track_rows) {
+                    if (p_lo != acc_p) {
+                        rowmin_flush(a, acc_p, m, acc_m);
+                        acc_p = p_lo;
+                        acc_m = min_lo;
+                    } else {
+                        acc_m = fminf(acc_m, min_lo);
+                    }
+                    if (two) {
+                        rowmin_flush(a, acc_p, m, acc_m);
+                        acc_p = p_lo + 1;
+                        acc_m = min_hi;
+                    }
+                }
+            } else {
+                // short translation lists: one particle index per column
+                int p = p_lo, t = nb - p_lo * a.T;
+                float lmin = __int_as_float(0x7f800000);
+#pragma unroll
+                for (int jj = 0; jj < 32; ++jj) {
+                    float d = __int_as_float(0x7f800000);
+                    if (jj < nvalid) {
+                        if (!skip) {
+                            d = a.norm[(size_t)p * a.M + m] - 2.f * v[jj];
+                            lmin = fminf(lmin, d);
+                        }
+                        if (++t == a.T || jj + 1 == nvalid) {
+                            warp_min_flush(lmin, &a.ps[p].min_coarse);
+                            lmin = __int_as_float(0x7f800000);
+                            t = 0;
+                            ++p;
+                        }
+                    }
+                    tb[lane * 33 + jj] = d;
+                }
+            }
+            __syncwarp();
+            // lane = column: each store writes 32 consecutive translations
+            // of one row; rows whose segment is not kept are not stored
+            const int n = nb + lane;
+            if ((lo_rows | hi_rows) && lane < nvalid) {
+                const int pn = n / a.T, tn = n - pn * a.T;
+                float *dst = a.out + (size_t)pn * a.M * a.T + tn;
+                const int rows = min(32, a.M - (m0 + q * 32));
+                const unsigned int my_rows = lane < bnd_st ? lo_rows : hi_rows;
+#pragma unroll 8
+                for (int r = 0; r < 32; ++r)
+                    if (r < rows && ((my_rows >> r) & 1u)) dst[(size_t)(m0 + q * 32 + r) * a.T] = tb[r * 33 + lane];
+            }
+            __syncwarp();
+        }
+        if (track_rows) rowmin_flush(a, acc_p, m, acc_m);
 }
 
 // Persistent warp-specialised CTA, one per SM, tiles tidx = blockIdx.x +
@@ -265,9 +412,10 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_diff2(const TcArgs a) {
     if (warp == 0 && lane == 0) {
         // producer: one running stage counter over all tiles of this CTA
         uint32_t g = 0;
+        const uint64_t keep = policy_keep();
         for (int tidx = blockIdx.x; tidx < ntotal && !*vfail; tidx += gridDim.x) {
             int mt, nt;
-            tile_mn(tidx, a.mtiles, a.ntiles, mt, nt);
+            tile_mn(tidx, a.group_m, a.mtiles, a.ntiles, mt, nt);
             // norms: A holds [hi | lo] (2 nk/3 tiles per row tile), read in the
             // order hi(0) hi(0) hi(1) hi(1) ... lo(0) lo(1) ... so that the
             // second read of each hi tile follows the first (an L2 hit)
@@ -283,7 +431,10 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_diff2(const TcArgs a) {
                 }
                 const uint32_t st = sbase + s * STAGE_BYTES;
                 arrive_expect_tx(smem_u32(&full[s]), (uint32_t)STAGE_BYTES);
-                bulk_g2s(st, ab + (size_t)ka * A_BYTES, A_BYTES, smem_u32(&full[s]));
+                if (a.keep_a)
+                    bulk_g2s_hint(st, ab + (size_t)ka * A_BYTES, A_BYTES, smem_u32(&full[s]), keep);
+                else
+                    bulk_g2s(st, ab + (size_t)ka * A_BYTES, A_BYTES, smem_u32(&full[s]));
                 bulk_g2s(st + A_BYTES, yb + (size_t)kt * B_BYTES, B_BYTES, smem_u32(&full[s]));
             }
         }
@@ -338,7 +489,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_diff2(const TcArgs a) {
         uint32_t i = 0;
         for (int tidx = blockIdx.x; tidx < ntotal && !*vfail; tidx += gridDim.x, ++i) {
             int mt, nt;
-            tile_mn(tidx, a.mtiles, a.ntiles, mt, nt);
+            tile_mn(tidx, a.group_m, a.mtiles, a.ntiles, mt, nt);
             const uint32_t b = i & 1u;
             if (!mbar_wait(smem_u32(&tfull[b]), (i >> 1) & 1u)) {
                 *vfail = 1;
@@ -368,123 +519,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_diff2(const TcArgs a) {
                                  : "memory");
                 continue;
             }
-            const bool skip = !(m < a.M) || !(a.pdf_orient[m] > 0.f);
-            // running row minimum of the particle segment this lane is in
-            const bool track_rows = a.rowmin != nullptr && a.T >= 32 && !skip;
-            int acc_p = -1;
-            float acc_m = __int_as_float(0x7f800000);
-            for (int c = 0; c < 4; ++c) {
-                const int col = h * 128 + c * 32;
-                const int nb = n0 + col;
-                if (nb >= a.N) break;  // warp-uniform
-                const int nvalid = min(32, a.N - nb);
-                // rows whose segments of this chunk are stored (bit r = lane r's row)
-                unsigned int lo_rows = 0xFFFFFFFFu, hi_rows = 0xFFFFFFFFu;
-                int bnd_st = 32;
-                const int p_lo = nb / a.T;
-                // operands of the epilogue that do not depend on the accumulator
-                // are loaded before the TMEM read so their latency overlaps it:
-                // at most two particles in these 32 columns (T >= 32), p_lo for jj < bnd
-                const int bnd = (p_lo + 1) * a.T - nb;
-                float n_lo = 0.f, n_hi = 0.f, xs_lo = 0.f, xs_hi = 0.f;
-                unsigned int run_lo = 0xFFFFFFFFu, run_hi = 0xFFFFFFFFu;
-                if (a.T >= 32) {
-                    if (!skip) n_lo = a.norm[(size_t)p_lo * a.M + m];
-                    if (!skip && bnd < nvalid) n_hi = a.norm[(size_t)(p_lo + 1) * a.M + m];
-                    if (a.segmask) {
-                        run_lo = __ldcg(&a.ps[p_lo].min_coarse);
-                        xs_lo = __ldg(&a.ps[p_lo].xs);
-                        if (bnd < nvalid) {
-                            run_hi = __ldcg(&a.ps[p_lo + 1].min_coarse);
-                            xs_hi = __ldg(&a.ps[p_lo + 1].xs);
-                        }
-                    }
-                }
-                float v[32];
-                tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + b * (uint32_t)TN + (uint32_t)col, v);
-                if (a.T >= 32) {
-                    bnd_st = bnd;
-                    float min_lo = __int_as_float(0x7f800000), min_hi = min_lo;
-#pragma unroll
-                    for (int jj = 0; jj < 32; ++jj) {
-                        float d = __int_as_float(0x7f800000);
-                        if (!skip && jj < nvalid) {
-                            d = (jj < bnd ? n_lo : n_hi) - 2.f * v[jj];
-                            if (jj < bnd)
-                                min_lo = fminf(min_lo, d);
-                            else
-                                min_hi = fminf(min_hi, d);
-                        }
-                        v[jj] = d;
-                    }
-                    const bool two = bnd < nvalid;
-                    const unsigned int u_lo = warp_min_flush(min_lo, &a.ps[p_lo].min_coarse);
-                    const unsigned int u_hi = two ? warp_min_flush(min_hi, &a.ps[p_lo + 1].min_coarse) : 0xFFFFFFFFu;
-                    if (a.segmask) {
-                        const bool near_lo = min_lo <= near_cut(min(u_lo, run_lo), xs_lo);
-                        const bool near_hi = two && min_hi <= near_cut(min(u_hi, run_hi), xs_hi);
-                        lo_rows = __ballot_sync(0xffffffffu, near_lo);
-                        hi_rows = __ballot_sync(0xffffffffu, near_hi);
-                        if (near_lo)
-                            atomicOr(&a.segmask[(size_t)p_lo * a.M + m], 1u << ((nb >> 5) - ((p_lo * a.T) >> 5)));
-                        if (near_hi) atomicOr(&a.segmask[(size_t)(p_lo + 1) * a.M + m], 1u);
-                    }
-                    if (lo_rows | hi_rows) {
-#pragma unroll
-                        for (int jj = 0; jj < 32; ++jj) tb[lane * 33 + jj] = v[jj];
-                    }
-                    if (track_rows) {
-                        if (p_lo != acc_p) {
-                            rowmin_flush(a, acc_p, m, acc_m);
-                            acc_p = p_lo;
-                            acc_m = min_lo;
-                        } else {
-                            acc_m = fminf(acc_m, min_lo);
-                        }
-                        if (two) {
-                            rowmin_flush(a, acc_p, m, acc_m);
-                            acc_p = p_lo + 1;
-                            acc_m = min_hi;
-                        }
-                    }
-                } else {
-                    // short translation lists: one particle index per column
-                    int p = p_lo, t = nb - p_lo * a.T;
-                    float lmin = __int_as_float(0x7f800000);
-#pragma unroll
-                    for (int jj = 0; jj < 32; ++jj) {
-                        float d = __int_as_float(0x7f800000);
-                        if (jj < nvalid) {
-                            if (!skip) {
-                                d = a.norm[(size_t)p * a.M + m] - 2.f * v[jj];
-                                lmin = fminf(lmin, d);
-                            }
-                            if (++t == a.T || jj + 1 == nvalid) {
-                                warp_min_flush(lmin, &a.ps[p].min_coarse);
-                                lmin = __int_as_float(0x7f800000);
-                                t = 0;
-                                ++p;
-                            }
-                        }
-                        tb[lane * 33 + jj] = d;
-                    }
-                }
-                __syncwarp();
-                // lane = column: each store writes 32 consecutive translations
-                // of one row; rows whose segment is not kept are not stored
-                const int n = nb + lane;
-                if ((lo_rows | hi_rows) && lane < nvalid) {
-                    const int pn = n / a.T, tn = n - pn * a.T;
-                    float *dst = a.out + (size_t)pn * a.M * a.T + tn;
-                    const int rows = min(32, a.M - (m0 + q * 32));
-                    const unsigned int my_rows = lane < bnd_st ? lo_rows : hi_rows;
-#pragma unroll 8
-                    for (int r = 0; r < 32; ++r)
-                        if (r < rows && ((my_rows >> r) & 1u)) dst[(size_t)(m0 + q * 32 + r) * a.T] = tb[r * 33 + lane];
-                }
-                __syncwarp();
-            }
-            if (track_rows) rowmin_flush(a, acc_p, m, acc_m);
+            drain_cross(a, tmem + b * (uint32_t)TN, m0, n0, q, h, lane, tb);
             // accumulator drained: hand it back to the MMA issuer
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             __syncwarp();
@@ -507,6 +542,286 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_diff2(const TcArgs a) {
     if (warp == 0) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+    }
+}
+
+// ---- cross term on SM pairs (cta_group::2) ----------------------------------
+// A cluster of two CTAs on a pair of SMs computes output tiles of 256
+// orientations x 256 columns.  Each CTA streams its own 128 orientation rows
+// (A tile 2 mp + rank) and one half of the tile's particle columns (Y rows
+// 128 rank ..); the MMA issued by the even CTA (M = 256, N = 256, K = 16)
+// reads both CTAs' shared memory and writes each CTA's 128 x 256 half of the
+// accumulator into that CTA's tensor memory.  Per SM and K tile that is 32 KB
+// of operands instead of 48 KB for the same MMA work, which is what bounds
+// the one-SM kernel (its operand feed from L2).
+//
+// Synchronisation: the odd CTA forwards the completion of each of its stages
+// to the even CTA's pfull barrier (st.async of one word, which completes 4
+// transaction bytes there without blocking the forwarding thread -- a
+// blocking remote arrive per stage took longer than the stage's MMAs); the
+// even CTA's commits
+// release both CTAs' stages (empty) and accumulators (tfull, done); the
+// epilogue warps of both CTAs hand an accumulator back on the even CTA's
+// tempty barrier (16 arrivals).  Every mbarrier wait is bounded; both CTAs
+// meet at a cluster barrier after their last wait, before the tensor memory
+// (allocated by both CTAs together) is freed.
+constexpr int P_STAGES = 6;
+constexpr int P_HALF_BYTES = (TN / 2) * TK * 2;        // 16 KB: 128 Y rows x 64 K
+constexpr int P_STAGE_BYTES = A_BYTES + P_HALF_BYTES;  // 32 KB
+constexpr int P_SMEM_BYTES = P_STAGES * P_STAGE_BYTES + TRANSPOSE_BYTES;
+
+__device__ __forceinline__ uint32_t cluster_rank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+
+__device__ __forceinline__ uint32_t cluster_id() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%clusterid.x;" : "=r"(r));
+    return r;
+}
+
+__device__ __forceinline__ uint32_t cluster_count() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%nclusterid.x;" : "=r"(r));
+    return r;
+}
+
+// Shared::cluster address of the variable at local shared address `local`
+// in the CTA of cluster rank `rank`.
+__device__ __forceinline__ uint32_t rank_addr(uint32_t local, uint32_t rank) {
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(local), "r"(rank));
+    return r;
+}
+
+__device__ __forceinline__ void arrive_cluster(uint32_t cluster_addr) {
+    asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(cluster_addr) : "memory");
+}
+
+// Non-blocking signal to another CTA of the cluster: a 4-byte store into its
+// shared memory (word) that completes 4 transaction bytes on its barrier bar
+// (both shared::cluster addresses in that CTA).
+__device__ __forceinline__ void signal_tx4(uint32_t word, uint32_t value, uint32_t bar) {
+    asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b32 [%0], %1, [%2];" ::"r"(word), "r"(value),
+                 "r"(bar)
+                 : "memory");
+}
+
+// Bounded wait that acquires at cluster scope (arrivals from the peer CTA).
+__device__ __forceinline__ bool mbar_wait_cl(uint32_t bar, uint32_t parity) {
+    for (unsigned int it = 0; it < kWaitLimit; ++it) {
+        uint32_t ok;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n"
+            " selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(ok)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void mma_bf16_pair(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                              uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+// Arrive on the barrier at shared::cluster address bar (either CTA of the
+// pair) when every pair MMA issued so far by this thread has completed.
+__device__ __forceinline__ void mma_commit_pair(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void cluster_sync_all() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+// Instruction descriptor, kind::f16, M = 256 over the pair, N = TN.
+__host__ __device__ constexpr uint32_t make_idesc_pair() {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TN >> 3) << 17) | ((uint32_t)(2 * TM >> 4) << 24);
+}
+
+__global__ void __launch_bounds__(THREADS, 1) k_tc_pair(const TcArgs a) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ __align__(8) uint64_t full[P_STAGES];
+    __shared__ __align__(8) uint64_t pfull[P_STAGES];
+    __shared__ __align__(8) uint64_t empty[P_STAGES];
+    __shared__ __align__(8) uint64_t tfull[2];
+    __shared__ __align__(8) uint64_t tempty[2];
+    __shared__ __align__(8) uint64_t done;
+    __shared__ uint32_t pword[P_STAGES];  // targets of the odd CTA's stage signals
+    __shared__ uint32_t tmem_slot;
+    __shared__ int sfail;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t rank = cluster_rank();
+    const int cid = (int)cluster_id(), ncl = (int)cluster_count();
+    const int nk = a.ktiles;
+    const int mpairs = (a.mtiles + 1) >> 1;  // the A table holds an even number of row tiles
+    const int ntotal = mpairs * a.ntiles;
+    const int gp = max(1, a.group_m >> 1);
+    volatile int *vfail = &sfail;
+
+    if (warp == 0) {
+        // one warp of each CTA of the pair allocates (the same columns in both)
+        asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                     "r"(TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        for (int s = 0; s < P_STAGES; ++s) {
+            mbar_init(smem_u32(&full[s]), 1);
+            mbar_init(smem_u32(&pfull[s]), 1);
+            mbar_init(smem_u32(&empty[s]), 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(smem_u32(&tfull[b]), 1);
+            mbar_init(smem_u32(&tempty[b]), 2 * EPI_WARPS);
+        }
+        mbar_init(smem_u32(&done), 1);
+        sfail = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    // both CTAs' barriers are initialised before either CTA signals the other
+    cluster_sync_all();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_slot;
+    const uint32_t sbase = smem_u32(smem);
+
+    if (warp == 0 && lane == 0) {
+        // producer (both CTAs): this CTA's A rows and Y half of every stage
+        uint32_t g = 0;
+        const uint64_t keep = policy_keep();
+        for (int tidx = cid; tidx < ntotal && !*vfail; tidx += ncl) {
+            int mp, nt;
+            tile_mn(tidx, gp, mpairs, a.ntiles, mp, nt);
+            const uint8_t *ab = a.Ablk + (size_t)(2 * mp + (int)rank) * nk * A_BYTES;
+            const uint8_t *yb = a.Yblk + (size_t)nt * nk * B_BYTES + rank * P_HALF_BYTES;
+            for (int kt = 0; kt < nk; ++kt, ++g) {
+                const uint32_t s = g % P_STAGES;
+                if (g >= P_STAGES && !mbar_wait(smem_u32(&empty[s]), ((g / P_STAGES) - 1) & 1u)) {
+                    *vfail = 1;
+                    break;
+                }
+                const uint32_t st = sbase + s * P_STAGE_BYTES;
+                arrive_expect_tx(smem_u32(&full[s]), (uint32_t)P_STAGE_BYTES);
+                if (a.keep_a)
+                    bulk_g2s_hint(st, ab + (size_t)kt * A_BYTES, A_BYTES, smem_u32(&full[s]), keep);
+                else
+                    bulk_g2s(st, ab + (size_t)kt * A_BYTES, A_BYTES, smem_u32(&full[s]));
+                bulk_g2s(st + A_BYTES, yb + (size_t)kt * B_BYTES, P_HALF_BYTES, smem_u32(&full[s]));
+            }
+        }
+        for (uint32_t q = g > (uint32_t)P_STAGES ? g - P_STAGES : 0u; q < g; ++q)
+            if (!mbar_wait(smem_u32(&full[q % P_STAGES]), (q / P_STAGES) & 1u)) *vfail = 1;
+    } else if (warp == 1 && lane == 0 && rank == 0) {
+        // MMA issuer (even CTA)
+        const uint32_t idesc = make_idesc_pair();
+        uint32_t g = 0, i = 0;
+        for (int tidx = cid; tidx < ntotal && !*vfail; tidx += ncl, ++i) {
+            const uint32_t b = i & 1u;
+            if (i >= 2 && !mbar_wait_cl(smem_u32(&tempty[b]), ((i >> 1) - 1) & 1u)) {
+                *vfail = 1;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t acc = tmem + b * (uint32_t)TN;
+            bool ok = true;
+            for (int kt = 0; kt < nk; ++kt, ++g) {
+                const uint32_t s = g % P_STAGES, par = (g / P_STAGES) & 1u;
+                // this thread's arrival on pfull and the 4 bytes the odd CTA's
+                // signal completes (the bytes may land first)
+                arrive_expect_tx(smem_u32(&pfull[s]), 4u);
+                if (!mbar_wait(smem_u32(&full[s]), par) || !mbar_wait_cl(smem_u32(&pfull[s]), par)) {
+                    ok = false;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t a0 = sbase + s * P_STAGE_BYTES, b0 = a0 + A_BYTES;
+#pragma unroll
+                for (int kk = 0; kk < TK / 16; ++kk) {
+                    const uint64_t ad = make_desc(a0 + kk * 256, 128, 1024);
+                    const uint64_t bd = make_desc(b0 + kk * 256, 128, 1024);
+                    mma_bf16_pair(acc, ad, bd, idesc, (kt | kk) != 0 ? 1u : 0u);
+                }
+                mma_commit_pair(smem_u32(&empty[s]));
+                mma_commit_pair(rank_addr(smem_u32(&empty[s]), 1));
+            }
+            if (!ok) {
+                *vfail = 1;
+                break;
+            }
+            mma_commit_pair(smem_u32(&tfull[b]));
+            mma_commit_pair(rank_addr(smem_u32(&tfull[b]), 1));
+        }
+        // completion of every MMA issued above, in both CTAs (also after a failure)
+        mma_commit_pair(smem_u32(&done));
+        mma_commit_pair(rank_addr(smem_u32(&done), 1));
+    } else if (warp == 1 && lane == 0) {
+        // odd CTA: forward each filled stage to the even CTA's pfull barrier
+        uint32_t g = 0;
+        const uint32_t lead_pfull = rank_addr(smem_u32(&pfull[0]), 0);
+        const uint32_t lead_pword = rank_addr(smem_u32(&pword[0]), 0);
+        for (int tidx = cid; tidx < ntotal && !*vfail; tidx += ncl) {
+            bool ok = true;
+            for (int kt = 0; kt < nk; ++kt, ++g) {
+                const uint32_t s = g % P_STAGES;
+                if (!mbar_wait(smem_u32(&full[s]), (g / P_STAGES) & 1u)) {
+                    ok = false;
+                    break;
+                }
+                signal_tx4(lead_pword + s * 4u, g, lead_pfull + s * 8u);
+            }
+            if (!ok) {
+                *vfail = 1;
+                break;
+            }
+        }
+    } else if (warp >= 4) {
+        const int ew = warp - 4, q = warp & 3, h = ew >> 2;
+        float *tb = reinterpret_cast<float *>(smem + P_STAGES * P_STAGE_BYTES) + ew * 32 * 33;
+        uint32_t i = 0;
+        for (int tidx = cid; tidx < ntotal && !*vfail; tidx += ncl, ++i) {
+            int mp, nt;
+            tile_mn(tidx, gp, mpairs, a.ntiles, mp, nt);
+            const uint32_t b = i & 1u;
+            if (!mbar_wait(smem_u32(&tfull[b]), (i >> 1) & 1u)) {
+                *vfail = 1;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            drain_cross(a, tmem + b * (uint32_t)TN, (2 * mp + (int)rank) * TM, nt * TN, q, h, lane, tb);
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) arrive_cluster(rank_addr(smem_u32(&tempty[b]), 0));
+        }
+    }
+    __syncwarp();
+    if (warp == 0) {
+        // every MMA writing this CTA's tensor memory has completed
+        bool ok = true;
+        if (lane == 0) ok = mbar_wait(smem_u32(&done), 0u);
+        ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+        if (!ok && lane == 0) *vfail = 1;
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    // neither CTA leaves (or frees its tensor memory) while the other may
+    // still signal it or read its shared memory
+    cluster_sync_all();
+    if (tid == 0 && *vfail) atomicCAS(&g_tc_error, 0, 1);
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
     }
 }
 
@@ -885,15 +1200,19 @@ cudaError_t launch_tc_norm_pack_a(const float *src, int lds, int M, int K, void 
     return cudaGetLastError();
 }
 
+// Row tiles of the packed projection table: an even count (the SM-pair
+// kernel reads row tiles two at a time; a padding tile holds zeros).
+static int a_row_tiles(int M) { return (((M + TM - 1) / TM) + 1) & ~1; }
+
 size_t tc_a_bytes(int M, int K2) {
-    return (size_t)((M + TM - 1) / TM) * ((K2 + TK - 1) / TK) * A_BYTES;
+    return (size_t)a_row_tiles(M) * ((K2 + TK - 1) / TK) * A_BYTES;
 }
 size_t tc_y_bytes(int N, int K2) {
     return (size_t)((N + TN - 1) / TN) * ((K2 + TK - 1) / TK) * B_BYTES;
 }
 
 cudaError_t launch_tc_pack_a(const float *src, int lds, int M, int K2, void *dst, cudaStream_t st) {
-    const int ktiles = (K2 + TK - 1) / TK, mtiles = (M + TM - 1) / TM;
+    const int ktiles = (K2 + TK - 1) / TK, mtiles = a_row_tiles(M);
     const long long nchunks = (long long)mtiles * ktiles * (A_BYTES / 16);
     if (nchunks <= 0) return cudaSuccess;
     k_pack_a<<<(unsigned)((nchunks + 255) / 256), 256, 0, st>>>(src, lds, M, K2, ktiles, static_cast<uint8_t *>(dst),
@@ -903,7 +1222,8 @@ cudaError_t launch_tc_pack_a(const float *src, int lds, int M, int K2, void *dst
 
 cudaError_t launch_tc_diff2(const void *Ablk, void *Yblk, int M, int K2, const float2 *b, int ldb, const float2 *E,
                             int lde, int nparticles, int T, float *out, const float *norm, const float *pdf_orient,
-                            ParticleState *ps, unsigned int *rowmin, unsigned int *segmask, cudaStream_t st) {
+                            ParticleState *ps, unsigned int *rowmin, unsigned int *segmask, cudaStream_t st,
+                            const TcTuning &tune) {
     const int N = nparticles * T;
     if (N <= 0 || M <= 0) return cudaSuccess;
     const int ktiles = (K2 + TK - 1) / TK, ntiles = (N + TN - 1) / TN, mtiles = (M + TM - 1) / TM;
@@ -929,10 +1249,41 @@ cudaError_t launch_tc_diff2(const void *Ablk, void *Yblk, int M, int K2, const f
     }
     const long long ntotal = (long long)mtiles * ntiles;
     if (ntotal > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-    const int grid = (int)std::min<long long>(ntotal, nsm);
     TcArgs a{static_cast<const uint8_t *>(Ablk), static_cast<const uint8_t *>(Yblk), M, ktiles, T, N, nparticles,
              mtiles, ntiles, out, norm, pdf_orient, ps, T >= 32 ? rowmin : nullptr,
-             (T >= 32 && T <= 960 && rowmin) ? segmask : nullptr};
+             (T >= 32 && T <= 960 && rowmin) ? segmask : nullptr,
+             tune.group_m > 0 ? tune.group_m : kGroupMDefault, tune.keep_a ? 1 : 0};
+    if (tune.pair) {
+        // clusters of two CTAs, as many as can be resident at once
+        static int max_clusters = 0;
+        cudaLaunchConfig_t cfg = {};
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = 2;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.blockDim = dim3(THREADS);
+        cfg.dynamicSmemBytes = P_SMEM_BYTES;
+        cfg.stream = st;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        if (!max_clusters) {
+            e = cudaFuncSetAttribute(k_tc_pair, cudaFuncAttributeMaxDynamicSharedMemorySize, P_SMEM_BYTES);
+            cfg.gridDim = dim3(2 * (unsigned)(nsm / 2));
+            if (e == cudaSuccess) e = cudaOccupancyMaxActiveClusters(&max_clusters, k_tc_pair, &cfg);
+            if (e != cudaSuccess) {
+                max_clusters = 0;
+                return e;
+            }
+            if (max_clusters <= 0) return cudaErrorInvalidConfiguration;
+        }
+        const long long npairs = (long long)((mtiles + 1) / 2) * ntiles;
+        cfg.gridDim = dim3(2 * (unsigned)std::min<long long>(npairs, max_clusters));
+        e = cudaLaunchKernelEx(&cfg, k_tc_pair, a);
+        if (e != cudaSuccess) return e;
+        return cudaGetLastError();
+    }
+    const int grid = (int)std::min<long long>(ntotal, nsm);
     k_tc_diff2<false><<<grid, THREADS, smem, st>>>(a);
     return cudaGetLastError();
 }
@@ -961,7 +1312,7 @@ cudaError_t launch_tc_norm(const void *Ablk, const float *w, int ldw, int M, int
     const long long ntotal = (long long)mtiles * ntiles;
     const int grid = (int)std::min<long long>(ntotal, nsm);
     TcArgs a{static_cast<const uint8_t *>(Ablk), static_cast<const uint8_t *>(Bblk), M, 3 * nk, 1, nparticles,
-             nparticles, mtiles, ntiles, out, nullptr, nullptr, nullptr, nullptr, nullptr};
+             nparticles, mtiles, ntiles, out, nullptr, nullptr, nullptr, nullptr, nullptr, kGroupMDefault, 0};
     k_tc_diff2<true><<<grid, THREADS, SMEM_BYTES, st>>>(a);
     return cudaGetLastError();
 }

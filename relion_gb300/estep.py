@@ -207,7 +207,8 @@ assert RESULT_DTYPE.itemsize == C.sizeof(_lib.ParticleResult)
 ALL_BLOCKS = -2
 
 # gbr_worker_set_option selectors (include/gbrelion.h, gbr_worker_option)
-WORKER_OPTIONS = dict(debug=1, fine_mode=2, coarse_rows=3, cand_cap=4, cand_buf=5, batch_cap=6)
+WORKER_OPTIONS = dict(debug=1, fine_mode=2, coarse_rows=3, cand_cap=4, cand_buf=5, batch_cap=6, tile_group=7,
+                      keep_a=8, pair=9)
 FINE_MODES = dict(auto=0, dense=1, sparse=2)
 COARSE_ROWS = dict(skip=0, full=1)
 
@@ -217,7 +218,10 @@ class MlOptimiserCuda:
 
     Keyword options (gbr_worker_set_option): fine_mode ("auto", "dense",
     "sparse"), coarse_rows ("skip", "full"), cand_cap, cand_buf, batch_cap
-    (particles per pass of a call)."""
+    (particles per pass of a call), tile_group (orientation tiles of 128 rows
+    per group of the coarse tensor-core kernel's tile order), keep_a (1:
+    projection tiles read with an L2 keep policy) and pair (1: the coarse
+    cross term on SM pairs, tcgen05 cta_group::2)."""
 
     def __init__(self, bundle, debug=False, **options):
         self.bundle = bundle
