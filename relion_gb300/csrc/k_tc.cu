@@ -22,7 +22,9 @@
 // (bounded) for its own copies and MMAs, frees its tensor memory and returns.
 #include "gbr_internal.h"
 
+#include <cuda.h>
 #include <cuda_bf16.h>
+#include <cudaTypedefs.h>
 #include <cfloat>
 #include <algorithm>
 #include <cstdint>
@@ -230,6 +232,28 @@ __device__ __forceinline__ void rowmin_flush(const TcArgs &a, int p, int m, floa
     if (p >= 0 && v < FLT_MAX) atomicMin(&a.rowmin[(size_t)p * a.M + m], f2ord(v));
 }
 
+// Particles a warp's 128 columns can touch when T >= 32.
+constexpr int kTileParticles = 128 / 32 + 1;
+
+// Five per-particle values of a tile held in registers (selects, not an
+// indexed array, which would live in local memory); get(i) of i outside
+// 0..4 returns the last.
+template <typename V>
+struct TileOps {
+    V v0, v1, v2, v3, v4;
+    __device__ __forceinline__ void set(int i, V x) {
+        if (i == 0) v0 = x;
+        else if (i == 1) v1 = x;
+        else if (i == 2) v2 = x;
+        else if (i == 3) v3 = x;
+        else v4 = x;
+    }
+    __device__ __forceinline__ V get(int i) const {
+        return i == 0 ? v0 : i == 1 ? v1 : i == 2 ? v2 : i == 3 ? v3 : v4;
+    }
+};
+static_assert(kTileParticles == 5, "TileOps holds five values");
+
 // Epilogue of one cross-term tile: drains the 128 x 256 FP32 accumulator at
 // TMEM address acc (rows m0.., columns n0..) into diff2 = N(r,p) - 2 C with
 // the particles' running minima, row minima and sparse segment stores.  Warp
@@ -238,123 +262,129 @@ __device__ __forceinline__ void rowmin_flush(const TcArgs &a, int p, int m, floa
 __device__ __forceinline__ void drain_cross(const TcArgs &a, uint32_t acc, int m0, int n0, int q, int h, int lane,
                                             float *tb) {
     const int m = m0 + q * 32 + lane;
-        const bool skip = !(m < a.M) || !(a.pdf_orient[m] > 0.f);
-        // running row minimum of the particle segment this lane is in
-        const bool track_rows = a.rowmin != nullptr && a.T >= 32 && !skip;
-        int acc_p = -1;
-        float acc_m = __int_as_float(0x7f800000);
-        for (int c = 0; c < 4; ++c) {
-            const int col = h * 128 + c * 32;
-            const int nb = n0 + col;
-            if (nb >= a.N) break;  // warp-uniform
-            const int nvalid = min(32, a.N - nb);
-            // rows whose segments of this chunk are stored (bit r = lane r's row)
-            unsigned int lo_rows = 0xFFFFFFFFu, hi_rows = 0xFFFFFFFFu;
-            int bnd_st = 32;
-            const int p_lo = nb / a.T;
-            // operands of the epilogue that do not depend on the accumulator
-            // are loaded before the TMEM read so their latency overlaps it:
-            // at most two particles in these 32 columns (T >= 32), p_lo for jj < bnd
+    const bool skip = !(m < a.M) || !(a.pdf_orient[m] > 0.f);
+    // running row minimum of the particle segment this lane is in
+    const bool track_rows = a.rowmin != nullptr && a.T >= 32 && !skip;
+    int acc_p = -1;
+    float acc_m = __int_as_float(0x7f800000);
+    // the operands that do not depend on the accumulator -- this row's norm
+    // and the running minimum and skip distance of every particle in the
+    // warp's 128 columns -- loaded once per tile, before the first TMEM read
+    // (a running minimum read early is only larger: more segments stored)
+    const int nh = n0 + h * 128, pbase = nh / a.T;
+    const int nend = min(a.N, nh + 128);
+    const bool hoist = a.T >= 32;
+    TileOps<float> nrm;
+    TileOps<float> xsv;
+    TileOps<unsigned int> run;
+#pragma unroll
+    for (int i = 0; i < kTileParticles; ++i) {
+        const int p = pbase + i;
+        const bool in = hoist && p * a.T < nend;
+        nrm.set(i, (in && !skip) ? a.norm[(size_t)p * a.M + m] : 0.f);
+        run.set(i, (in && a.segmask) ? __ldcg(&a.ps[p].min_coarse) : 0xFFFFFFFFu);
+        xsv.set(i, (in && a.segmask) ? __ldg(&a.ps[p].xs) : 0.f);
+    }
+    for (int c = 0; c < 4; ++c) {
+        const int col = h * 128 + c * 32;
+        const int nb = n0 + col;
+        if (nb >= a.N) break;  // warp-uniform
+        const int nvalid = min(32, a.N - nb);
+        // rows whose segments of this chunk are stored (bit r = lane r's row)
+        unsigned int lo_rows = 0xFFFFFFFFu, hi_rows = 0xFFFFFFFFu;
+        int bnd_st = 32;
+        const int p_lo = nb / a.T;
+        float v[32];
+        tmem_ld32(acc + ((uint32_t)(q * 32) << 16) + (uint32_t)col, v);
+        if (a.T >= 32) {
+            // at most two particles in these 32 columns: p_lo for jj < bnd
             const int bnd = (p_lo + 1) * a.T - nb;
-            float n_lo = 0.f, n_hi = 0.f, xs_lo = 0.f, xs_hi = 0.f;
-            unsigned int run_lo = 0xFFFFFFFFu, run_hi = 0xFFFFFFFFu;
-            if (a.T >= 32) {
-                if (!skip) n_lo = a.norm[(size_t)p_lo * a.M + m];
-                if (!skip && bnd < nvalid) n_hi = a.norm[(size_t)(p_lo + 1) * a.M + m];
-                if (a.segmask) {
-                    run_lo = __ldcg(&a.ps[p_lo].min_coarse);
-                    xs_lo = __ldg(&a.ps[p_lo].xs);
-                    if (bnd < nvalid) {
-                        run_hi = __ldcg(&a.ps[p_lo + 1].min_coarse);
-                        xs_hi = __ldg(&a.ps[p_lo + 1].xs);
-                    }
+            const int il = p_lo - pbase;
+            const float n_lo = nrm.get(il), n_hi = nrm.get(il + 1);
+            const float xs_lo = xsv.get(il), xs_hi = xsv.get(il + 1);
+            const unsigned int run_lo = run.get(il), run_hi = run.get(il + 1);
+            bnd_st = bnd;
+            float min_lo = __int_as_float(0x7f800000), min_hi = min_lo;
+#pragma unroll
+            for (int jj = 0; jj < 32; ++jj) {
+                float d = __int_as_float(0x7f800000);
+                if (!skip && jj < nvalid) {
+                    d = (jj < bnd ? n_lo : n_hi) - 2.f * v[jj];
+                    if (jj < bnd)
+                        min_lo = fminf(min_lo, d);
+                    else
+                        min_hi = fminf(min_hi, d);
+                }
+                v[jj] = d;
+            }
+            const bool two = bnd < nvalid;
+            const unsigned int u_lo = warp_min_flush(min_lo, &a.ps[p_lo].min_coarse);
+            const unsigned int u_hi = two ? warp_min_flush(min_hi, &a.ps[p_lo + 1].min_coarse) : 0xFFFFFFFFu;
+            if (a.segmask) {
+                const bool near_lo = min_lo <= near_cut(min(u_lo, run_lo), xs_lo);
+                const bool near_hi = two && min_hi <= near_cut(min(u_hi, run_hi), xs_hi);
+                lo_rows = __ballot_sync(0xffffffffu, near_lo);
+                hi_rows = __ballot_sync(0xffffffffu, near_hi);
+                if (near_lo)
+                    atomicOr(&a.segmask[(size_t)p_lo * a.M + m], 1u << ((nb >> 5) - ((p_lo * a.T) >> 5)));
+                if (near_hi) atomicOr(&a.segmask[(size_t)(p_lo + 1) * a.M + m], 1u);
+            }
+            if (lo_rows | hi_rows) {
+#pragma unroll
+                for (int jj = 0; jj < 32; ++jj) tb[lane * 33 + jj] = v[jj];
+            }
+            if (track_rows) {
+                if (p_lo != acc_p) {
+                    rowmin_flush(a, acc_p, m, acc_m);
+                    acc_p = p_lo;
+                    acc_m = min_lo;
+                } else {
+                    acc_m = fminf(acc_m, min_lo);
+                }
+                if (two) {
+                    rowmin_flush(a, acc_p, m, acc_m);
+                    acc_p = p_lo + 1;
+                    acc_m = min_hi;
                 }
             }
-            float v[32];
-            tmem_ld32(acc + ((uint32_t)(q * 32) << 16) + (uint32_t)col, v);
-            if (a.T >= 32) {
-                bnd_st = bnd;
-                float min_lo = __int_as_float(0x7f800000), min_hi = min_lo;
+        } else {
+            // short translation lists: one particle index per column
+            int p = p_lo, t = nb - p_lo * a.T;
+            float lmin = __int_as_float(0x7f800000);
 #pragma unroll
-                for (int jj = 0; jj < 32; ++jj) {
-                    float d = __int_as_float(0x7f800000);
-                    if (!skip && jj < nvalid) {
-                        d = (jj < bnd ? n_lo : n_hi) - 2.f * v[jj];
-                        if (jj < bnd)
-                            min_lo = fminf(min_lo, d);
-                        else
-                            min_hi = fminf(min_hi, d);
+            for (int jj = 0; jj < 32; ++jj) {
+                float d = __int_as_float(0x7f800000);
+                if (jj < nvalid) {
+                    if (!skip) {
+                        d = a.norm[(size_t)p * a.M + m] - 2.f * v[jj];
+                        lmin = fminf(lmin, d);
                     }
-                    v[jj] = d;
-                }
-                const bool two = bnd < nvalid;
-                const unsigned int u_lo = warp_min_flush(min_lo, &a.ps[p_lo].min_coarse);
-                const unsigned int u_hi = two ? warp_min_flush(min_hi, &a.ps[p_lo + 1].min_coarse) : 0xFFFFFFFFu;
-                if (a.segmask) {
-                    const bool near_lo = min_lo <= near_cut(min(u_lo, run_lo), xs_lo);
-                    const bool near_hi = two && min_hi <= near_cut(min(u_hi, run_hi), xs_hi);
-                    lo_rows = __ballot_sync(0xffffffffu, near_lo);
-                    hi_rows = __ballot_sync(0xffffffffu, near_hi);
-                    if (near_lo)
-                        atomicOr(&a.segmask[(size_t)p_lo * a.M + m], 1u << ((nb >> 5) - ((p_lo * a.T) >> 5)));
-                    if (near_hi) atomicOr(&a.segmask[(size_t)(p_lo + 1) * a.M + m], 1u);
-                }
-                if (lo_rows | hi_rows) {
-#pragma unroll
-                    for (int jj = 0; jj < 32; ++jj) tb[lane * 33 + jj] = v[jj];
-                }
-                if (track_rows) {
-                    if (p_lo != acc_p) {
-                        rowmin_flush(a, acc_p, m, acc_m);
-                        acc_p = p_lo;
-                        acc_m = min_lo;
-                    } else {
-                        acc_m = fminf(acc_m, min_lo);
-                    }
-                    if (two) {
-                        rowmin_flush(a, acc_p, m, acc_m);
-                        acc_p = p_lo + 1;
-                        acc_m = min_hi;
+                    if (++t == a.T || jj + 1 == nvalid) {
+                        warp_min_flush(lmin, &a.ps[p].min_coarse);
+                        lmin = __int_as_float(0x7f800000);
+                        t = 0;
+                        ++p;
                     }
                 }
-            } else {
-                // short translation lists: one particle index per column
-                int p = p_lo, t = nb - p_lo * a.T;
-                float lmin = __int_as_float(0x7f800000);
-#pragma unroll
-                for (int jj = 0; jj < 32; ++jj) {
-                    float d = __int_as_float(0x7f800000);
-                    if (jj < nvalid) {
-                        if (!skip) {
-                            d = a.norm[(size_t)p * a.M + m] - 2.f * v[jj];
-                            lmin = fminf(lmin, d);
-                        }
-                        if (++t == a.T || jj + 1 == nvalid) {
-                            warp_min_flush(lmin, &a.ps[p].min_coarse);
-                            lmin = __int_as_float(0x7f800000);
-                            t = 0;
-                            ++p;
-                        }
-                    }
-                    tb[lane * 33 + jj] = d;
-                }
+                tb[lane * 33 + jj] = d;
             }
-            __syncwarp();
-            // lane = column: each store writes 32 consecutive translations
-            // of one row; rows whose segment is not kept are not stored
-            const int n = nb + lane;
-            if ((lo_rows | hi_rows) && lane < nvalid) {
-                const int pn = n / a.T, tn = n - pn * a.T;
-                float *dst = a.out + (size_t)pn * a.M * a.T + tn;
-                const int rows = min(32, a.M - (m0 + q * 32));
-                const unsigned int my_rows = lane < bnd_st ? lo_rows : hi_rows;
-#pragma unroll 8
-                for (int r = 0; r < 32; ++r)
-                    if (r < rows && ((my_rows >> r) & 1u)) dst[(size_t)(m0 + q * 32 + r) * a.T] = tb[r * 33 + lane];
-            }
-            __syncwarp();
         }
-        if (track_rows) rowmin_flush(a, acc_p, m, acc_m);
+        __syncwarp();
+        // lane = column: each store writes 32 consecutive translations
+        // of one row; rows whose segment is not kept are not stored
+        const int n = nb + lane;
+        if ((lo_rows | hi_rows) && lane < nvalid) {
+            const int pn = n / a.T, tn = n - pn * a.T;
+            float *dst = a.out + (size_t)pn * a.M * a.T + tn;
+            const int rows = min(32, a.M - (m0 + q * 32));
+            const unsigned int my_rows = lane < bnd_st ? lo_rows : hi_rows;
+#pragma unroll 8
+            for (int r = 0; r < 32; ++r)
+                if (r < rows && ((my_rows >> r) & 1u)) dst[(size_t)(m0 + q * 32 + r) * a.T] = tb[r * 33 + lane];
+        }
+        __syncwarp();
+    }
+    if (track_rows) rowmin_flush(a, acc_p, m, acc_m);
 }
 
 // Persistent warp-specialised CTA, one per SM, tiles tidx = blockIdx.x +
@@ -552,23 +582,24 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_diff2(const TcArgs a) {
 // 128 rank ..); the MMA issued by the even CTA (M = 256, N = 256, K = 16)
 // reads both CTAs' shared memory and writes each CTA's 128 x 256 half of the
 // accumulator into that CTA's tensor memory.  Per SM and K tile that is 32 KB
-// of operands instead of 48 KB for the same MMA work, which is what bounds
-// the one-SM kernel (its operand feed from L2).
+// of operands instead of 48 KB for the same MMA work.
 //
-// Synchronisation: the odd CTA forwards the completion of each of its stages
-// to the even CTA's pfull barrier (st.async of one word, which completes 4
-// transaction bytes there without blocking the forwarding thread -- a
-// blocking remote arrive per stage took longer than the stage's MMAs); the
-// even CTA's commits
-// release both CTAs' stages (empty) and accumulators (tfull, done); the
-// epilogue warps of both CTAs hand an accumulator back on the even CTA's
-// tempty barrier (16 arrivals).  Every mbarrier wait is bounded; both CTAs
-// meet at a cluster barrier after their last wait, before the tensor memory
-// (allocated by both CTAs together) is freed.
+// Synchronisation: both CTAs' tensor copies (cp.async.bulk.tensor with
+// .cta_group::2, over 2D byte views of the packed operands) complete their
+// bytes on the even CTA's full barrier, whose producer expects both CTAs'
+// bytes; the even CTA's commits release both CTAs' stages (empty) and
+// accumulators (tfull, done); the epilogue warps of both CTAs hand an
+// accumulator back on the even CTA's tempty barrier (16 arrivals).  Every
+// mbarrier wait is bounded; both CTAs meet at a cluster barrier after their
+// last wait, before the tensor memory (allocated by both CTAs together) is
+// freed.
 constexpr int P_STAGES = 6;
 constexpr int P_HALF_BYTES = (TN / 2) * TK * 2;        // 16 KB: 128 Y rows x 64 K
 constexpr int P_STAGE_BYTES = A_BYTES + P_HALF_BYTES;  // 32 KB
 constexpr int P_SMEM_BYTES = P_STAGES * P_STAGE_BYTES + TRANSPOSE_BYTES;
+// tensor-map view of a packed operand: rows of 256 bytes, boxes of 64 rows
+constexpr int P_ROW_BYTES = 256, P_BOX_ROWS = 64;
+static_assert(A_BYTES == P_ROW_BYTES * P_BOX_ROWS && P_HALF_BYTES == P_ROW_BYTES * P_BOX_ROWS, "16 KB boxes");
 
 __device__ __forceinline__ uint32_t cluster_rank() {
     uint32_t r;
@@ -596,17 +627,12 @@ __device__ __forceinline__ uint32_t rank_addr(uint32_t local, uint32_t rank) {
     return r;
 }
 
+// Arrive on a barrier of either CTA of the cluster (default semantics:
+// release at CTA scope; the TMEM reads it orders are complete, waited for by
+// tcgen05.wait::ld).  The cluster-scope form blocked the arriving warp for
+// ~1,700 clocks per arrival.
 __device__ __forceinline__ void arrive_cluster(uint32_t cluster_addr) {
-    asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(cluster_addr) : "memory");
-}
-
-// Non-blocking signal to another CTA of the cluster: a 4-byte store into its
-// shared memory (word) that completes 4 transaction bytes on its barrier bar
-// (both shared::cluster addresses in that CTA).
-__device__ __forceinline__ void signal_tx4(uint32_t word, uint32_t value, uint32_t bar) {
-    asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b32 [%0], %1, [%2];" ::"r"(word), "r"(value),
-                 "r"(bar)
-                 : "memory");
+    asm volatile("mbarrier.arrive.shared::cluster.b64 _, [%0];" ::"r"(cluster_addr) : "memory");
 }
 
 // Bounded wait that acquires at cluster scope (arrivals from the peer CTA).
@@ -622,6 +648,17 @@ __device__ __forceinline__ bool mbar_wait_cl(uint32_t bar, uint32_t parity) {
         if (ok) return true;
     }
     return false;
+}
+
+// One 16 KB box (64 rows of 256 bytes, starting at row `row`) of a packed
+// operand into this CTA's shared memory at dst; its bytes complete on the
+// barrier at shared::cluster address bar (the even CTA's).  x = 0 always.
+__device__ __forceinline__ void tma_box_pair(uint32_t dst, const CUtensorMap *map, int row, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cta.global.tile.mbarrier::complete_tx::bytes.cta_group::2 [%0], [%1, {%2, "
+        "%3}], [%4];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(0), "r"(row), "r"(bar)
+        : "memory");
 }
 
 __device__ __forceinline__ void mma_bf16_pair(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
@@ -649,15 +686,14 @@ __host__ __device__ constexpr uint32_t make_idesc_pair() {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TN >> 3) << 17) | ((uint32_t)(2 * TM >> 4) << 24);
 }
 
-__global__ void __launch_bounds__(THREADS, 1) k_tc_pair(const TcArgs a) {
+__global__ void __launch_bounds__(THREADS, 1)
+    k_tc_pair(const TcArgs a, const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapY) {
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ __align__(8) uint64_t full[P_STAGES];
-    __shared__ __align__(8) uint64_t pfull[P_STAGES];
     __shared__ __align__(8) uint64_t empty[P_STAGES];
     __shared__ __align__(8) uint64_t tfull[2];
     __shared__ __align__(8) uint64_t tempty[2];
     __shared__ __align__(8) uint64_t done;
-    __shared__ uint32_t pword[P_STAGES];  // targets of the odd CTA's stage signals
     __shared__ uint32_t tmem_slot;
     __shared__ int sfail;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -679,7 +715,6 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_pair(const TcArgs a) {
     if (tid == 0) {
         for (int s = 0; s < P_STAGES; ++s) {
             mbar_init(smem_u32(&full[s]), 1);
-            mbar_init(smem_u32(&pfull[s]), 1);
             mbar_init(smem_u32(&empty[s]), 1);
         }
         for (int b = 0; b < 2; ++b) {
@@ -698,14 +733,17 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_pair(const TcArgs a) {
     const uint32_t sbase = smem_u32(smem);
 
     if (warp == 0 && lane == 0) {
-        // producer (both CTAs): this CTA's A rows and Y half of every stage
+        // producer (both CTAs): this CTA's A rows and Y half of every stage,
+        // completing on the even CTA's full barrier
         uint32_t g = 0;
-        const uint64_t keep = policy_keep();
+        const uint32_t lead_full = rank_addr(smem_u32(&full[0]), 0);
+        asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mapA)) : "memory");
+        asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mapY)) : "memory");
         for (int tidx = cid; tidx < ntotal && !*vfail; tidx += ncl) {
             int mp, nt;
             tile_mn(tidx, gp, mpairs, a.ntiles, mp, nt);
-            const uint8_t *ab = a.Ablk + (size_t)(2 * mp + (int)rank) * nk * A_BYTES;
-            const uint8_t *yb = a.Yblk + (size_t)nt * nk * B_BYTES + rank * P_HALF_BYTES;
+            const int rowA = (2 * mp + (int)rank) * nk * P_BOX_ROWS;
+            const int rowY = nt * nk * (2 * P_BOX_ROWS) + (int)rank * P_BOX_ROWS;
             for (int kt = 0; kt < nk; ++kt, ++g) {
                 const uint32_t s = g % P_STAGES;
                 if (g >= P_STAGES && !mbar_wait(smem_u32(&empty[s]), ((g / P_STAGES) - 1) & 1u)) {
@@ -713,16 +751,18 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_pair(const TcArgs a) {
                     break;
                 }
                 const uint32_t st = sbase + s * P_STAGE_BYTES;
-                arrive_expect_tx(smem_u32(&full[s]), (uint32_t)P_STAGE_BYTES);
-                if (a.keep_a)
-                    bulk_g2s_hint(st, ab + (size_t)kt * A_BYTES, A_BYTES, smem_u32(&full[s]), keep);
-                else
-                    bulk_g2s(st, ab + (size_t)kt * A_BYTES, A_BYTES, smem_u32(&full[s]));
-                bulk_g2s(st + A_BYTES, yb + (size_t)kt * B_BYTES, P_HALF_BYTES, smem_u32(&full[s]));
+                // the even CTA's arrival announces both CTAs' bytes (the odd
+                // CTA's may land first)
+                if (rank == 0) arrive_expect_tx(smem_u32(&full[s]), 2u * P_STAGE_BYTES);
+                tma_box_pair(st, &mapA, rowA + kt * P_BOX_ROWS, lead_full + s * 8u);
+                tma_box_pair(st + A_BYTES, &mapY, rowY + kt * (2 * P_BOX_ROWS), lead_full + s * 8u);
             }
         }
-        for (uint32_t q = g > (uint32_t)P_STAGES ? g - P_STAGES : 0u; q < g; ++q)
-            if (!mbar_wait(smem_u32(&full[q % P_STAGES]), (q / P_STAGES) & 1u)) *vfail = 1;
+        // the even CTA waits (bounded) for the last filled phase of each stage:
+        // every copy of both CTAs that it announced has landed
+        if (rank == 0)
+            for (uint32_t q = g > (uint32_t)P_STAGES ? g - P_STAGES : 0u; q < g; ++q)
+                if (!mbar_wait(smem_u32(&full[q % P_STAGES]), (q / P_STAGES) & 1u)) *vfail = 1;
     } else if (warp == 1 && lane == 0 && rank == 0) {
         // MMA issuer (even CTA)
         const uint32_t idesc = make_idesc_pair();
@@ -737,11 +777,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_pair(const TcArgs a) {
             const uint32_t acc = tmem + b * (uint32_t)TN;
             bool ok = true;
             for (int kt = 0; kt < nk; ++kt, ++g) {
-                const uint32_t s = g % P_STAGES, par = (g / P_STAGES) & 1u;
-                // this thread's arrival on pfull and the 4 bytes the odd CTA's
-                // signal completes (the bytes may land first)
-                arrive_expect_tx(smem_u32(&pfull[s]), 4u);
-                if (!mbar_wait(smem_u32(&full[s]), par) || !mbar_wait_cl(smem_u32(&pfull[s]), par)) {
+                const uint32_t s = g % P_STAGES;
+                if (!mbar_wait(smem_u32(&full[s]), (g / P_STAGES) & 1u)) {
                     ok = false;
                     break;
                 }
@@ -766,26 +803,6 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_pair(const TcArgs a) {
         // completion of every MMA issued above, in both CTAs (also after a failure)
         mma_commit_pair(smem_u32(&done));
         mma_commit_pair(rank_addr(smem_u32(&done), 1));
-    } else if (warp == 1 && lane == 0) {
-        // odd CTA: forward each filled stage to the even CTA's pfull barrier
-        uint32_t g = 0;
-        const uint32_t lead_pfull = rank_addr(smem_u32(&pfull[0]), 0);
-        const uint32_t lead_pword = rank_addr(smem_u32(&pword[0]), 0);
-        for (int tidx = cid; tidx < ntotal && !*vfail; tidx += ncl) {
-            bool ok = true;
-            for (int kt = 0; kt < nk; ++kt, ++g) {
-                const uint32_t s = g % P_STAGES;
-                if (!mbar_wait(smem_u32(&full[s]), (g / P_STAGES) & 1u)) {
-                    ok = false;
-                    break;
-                }
-                signal_tx4(lead_pword + s * 4u, g, lead_pfull + s * 8u);
-            }
-            if (!ok) {
-                *vfail = 1;
-                break;
-            }
-        }
     } else if (warp >= 4) {
         const int ew = warp - 4, q = warp & 3, h = ew >> 2;
         float *tb = reinterpret_cast<float *>(smem + P_STAGES * P_STAGE_BYTES) + ew * 32 * 33;
@@ -1254,6 +1271,30 @@ cudaError_t launch_tc_diff2(const void *Ablk, void *Yblk, int M, int K2, const f
              (T >= 32 && T <= 960 && rowmin) ? segmask : nullptr,
              tune.group_m > 0 ? tune.group_m : kGroupMDefault, tune.keep_a ? 1 : 0};
     if (tune.pair) {
+        // 2D byte views of the packed operands for the tensor copies
+        static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+        if (!encode) {
+            void *fn = nullptr;
+            cudaDriverEntryPointQueryResult q;
+            e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+            if (e != cudaSuccess) return e;
+            if (!fn || q != cudaDriverEntryPointSuccess) return cudaErrorNotSupported;
+            encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+        }
+        CUtensorMap maps[2];
+        const void *bases[2] = {Ablk, Yblk};
+        const size_t bytes[2] = {tc_a_bytes(M, K2), tc_y_bytes(N, K2)};
+        for (int i = 0; i < 2; ++i) {
+            if (((uintptr_t)bases[i] & 15u) != 0 || bytes[i] % P_ROW_BYTES != 0) return cudaErrorInvalidValue;
+            const cuuint64_t dims[2] = {(cuuint64_t)P_ROW_BYTES, (cuuint64_t)(bytes[i] / P_ROW_BYTES)};
+            const cuuint64_t strides[1] = {(cuuint64_t)P_ROW_BYTES};
+            const cuuint32_t box[2] = {(cuuint32_t)P_ROW_BYTES, (cuuint32_t)P_BOX_ROWS};
+            const cuuint32_t estr[2] = {1, 1};
+            if (encode(&maps[i], CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, const_cast<void *>(bases[i]), dims, strides, box,
+                       estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                       CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+                return cudaErrorInvalidValue;
+        }
         // clusters of two CTAs, as many as can be resident at once
         static int max_clusters = 0;
         cudaLaunchConfig_t cfg = {};
@@ -1278,8 +1319,11 @@ cudaError_t launch_tc_diff2(const void *Ablk, void *Yblk, int M, int K2, const f
             if (max_clusters <= 0) return cudaErrorInvalidConfiguration;
         }
         const long long npairs = (long long)((mtiles + 1) / 2) * ntiles;
+        // the row coordinates of the tensor copies are 32-bit
+        if ((long long)(bytes[0] / P_ROW_BYTES) > 0x7fffffffLL || (long long)(bytes[1] / P_ROW_BYTES) > 0x7fffffffLL)
+            return cudaErrorInvalidConfiguration;
         cfg.gridDim = dim3(2 * (unsigned)std::min<long long>(npairs, max_clusters));
-        e = cudaLaunchKernelEx(&cfg, k_tc_pair, a);
+        e = cudaLaunchKernelEx(&cfg, k_tc_pair, a, maps[0], maps[1]);
         if (e != cudaSuccess) return e;
         return cudaGetLastError();
     }

@@ -38,6 +38,15 @@ CONFIGS = {
                            blob_radius=30.0, max_shift=4.0, defocus=(8000.0, 30000.0), snr=0.02,
                            ini_high=20.0, healpix_order=0, psi_step=6.0, offset_range_px=5.0,
                            offset_step_px=1.0, diameter=150.0, classes=100, ref_dim=2),
+    # the box-256 refinement in a late iteration: the map has reached Nyquist
+    # (reference low-passed at 2 A), so the current size is the whole box
+    # (256 px: 33,024 Fourier pixels per image against 1,104 in the first
+    # iteration) while the coarse pass stays at 48 px; search as box 256
+    "cfg1_box256_late": dict(box=256, pixel=1.0, n_particles=20000, n_blobs=5000, blob_sigma=1.5,
+                             blob_radius=90.0, max_shift=3.0, defocus=(8000.0, 25000.0), snr=0.03,
+                             ini_high=2.0, healpix_order=3, psi_step=-1.0, offset_range_px=6.0,
+                             offset_step_px=1.0, diameter=200.0, classes=1, current_size=256,
+                             coarse_size=48),
     "cfg4_box256_K4": dict(box=256, pixel=1.0, n_particles=50000, n_blobs=4000, blob_sigma=1.5,
                            blob_radius=90.0, max_shift=3.0, defocus=(8000.0, 25000.0), snr=0.03,
                            ini_high=20.0, healpix_order=3, psi_step=-1.0, offset_range_px=6.0,
@@ -298,6 +307,9 @@ class Dataset:
         self.is2d = int(c.get("ref_dim", 3)) == 2
         self.current, self.coarse = estep_sizes(box, pix, c["ini_high"], c["healpix_order"], c["diameter"],
                                                 psi_step_2d=c["psi_step"] if self.is2d else None)
+        # a later iteration's sizes, where the configuration gives them
+        self.current = int(c.get("current_size", self.current))
+        self.coarse = int(c.get("coarse_size", self.coarse))
         self.vol = GaussianVolume(c["n_blobs"], c["blob_sigma"], c["blob_radius"], self.gen, device)
         K = int(c.get("classes", 1))
         self.vols = [self.vol]
