@@ -585,7 +585,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_diff2(const TcArgs a) {
 // of operands instead of 48 KB for the same MMA work.
 //
 // Synchronisation: both CTAs' tensor copies (cp.async.bulk.tensor with
-// .cta_group::2, over 2D byte views of the packed operands) complete their
+// .cta_group::2, over 2D views of the packed operands) complete their
 // bytes on the even CTA's full barrier, whose producer expects both CTAs'
 // bytes; the even CTA's commits release both CTAs' stages (empty) and
 // accumulators (tfull, done); the epilogue warps of both CTAs hand an
@@ -597,8 +597,10 @@ constexpr int P_STAGES = 6;
 constexpr int P_HALF_BYTES = (TN / 2) * TK * 2;        // 16 KB: 128 Y rows x 64 K
 constexpr int P_STAGE_BYTES = A_BYTES + P_HALF_BYTES;  // 32 KB
 constexpr int P_SMEM_BYTES = P_STAGES * P_STAGE_BYTES + TRANSPOSE_BYTES;
-// tensor-map view of a packed operand: rows of 256 bytes, boxes of 64 rows
-constexpr int P_ROW_BYTES = 256, P_BOX_ROWS = 64;
+// tensor-map view of a packed operand: rows of 2 KB (256 elements of 8
+// bytes, the widest box row; a tensor copy costs about 9 clocks per box row,
+// so 256-byte rows made the copies, not the MMAs, the limit), boxes of 8 rows
+constexpr int P_ROW_BYTES = 2048, P_BOX_ROWS = 8;
 static_assert(A_BYTES == P_ROW_BYTES * P_BOX_ROWS && P_HALF_BYTES == P_ROW_BYTES * P_BOX_ROWS, "16 KB boxes");
 
 __device__ __forceinline__ uint32_t cluster_rank() {
@@ -1237,6 +1239,37 @@ cudaError_t launch_tc_pack_a(const float *src, int lds, int M, int K2, void *dst
     return cudaGetLastError();
 }
 
+// 2D view of a packed operand for tensor copies: rows of row_bytes bytes of
+// 1-, 2- or 8-byte elements (elem), boxes of box_x elements x box_y rows.
+static cudaError_t encode_view(const void *base, size_t bytes, int row_bytes, int elem, int box_x, int box_y,
+                               CUtensorMap *out) {
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    if (!encode) {
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+        if (e != cudaSuccess) return e;
+        if (!fn || q != cudaDriverEntryPointSuccess) return cudaErrorNotSupported;
+        encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    }
+    if (((uintptr_t)base & 15u) != 0 || bytes % (size_t)row_bytes != 0 || (bytes / row_bytes) > 0x7fffffffULL)
+        return cudaErrorInvalidValue;
+    const cuuint64_t dims[2] = {(cuuint64_t)(row_bytes / elem), (cuuint64_t)(bytes / row_bytes)};
+    const cuuint64_t strides[1] = {(cuuint64_t)row_bytes};
+    const cuuint32_t box[2] = {(cuuint32_t)box_x, (cuuint32_t)box_y};
+    const cuuint32_t estr[2] = {1, 1};
+    if (elem != 1 && elem != 2 && elem != 8) return cudaErrorInvalidValue;
+    const CUtensorMapDataType type = elem == 1   ? CU_TENSOR_MAP_DATA_TYPE_UINT8
+                                     : elem == 2 ? CU_TENSOR_MAP_DATA_TYPE_UINT16
+                                                 : CU_TENSOR_MAP_DATA_TYPE_UINT64;
+    if (encode(out, type, 2,
+               const_cast<void *>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return cudaErrorInvalidValue;
+    return cudaSuccess;
+}
+
 cudaError_t launch_tc_diff2(const void *Ablk, void *Yblk, int M, int K2, const float2 *b, int ldb, const float2 *E,
                             int lde, int nparticles, int T, float *out, const float *norm, const float *pdf_orient,
                             ParticleState *ps, unsigned int *rowmin, unsigned int *segmask, cudaStream_t st,
@@ -1272,29 +1305,11 @@ cudaError_t launch_tc_diff2(const void *Ablk, void *Yblk, int M, int K2, const f
              tune.group_m > 0 ? tune.group_m : kGroupMDefault, tune.keep_a ? 1 : 0};
     if (tune.pair) {
         // 2D byte views of the packed operands for the tensor copies
-        static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
-        if (!encode) {
-            void *fn = nullptr;
-            cudaDriverEntryPointQueryResult q;
-            e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
-            if (e != cudaSuccess) return e;
-            if (!fn || q != cudaDriverEntryPointSuccess) return cudaErrorNotSupported;
-            encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
-        }
         CUtensorMap maps[2];
-        const void *bases[2] = {Ablk, Yblk};
         const size_t bytes[2] = {tc_a_bytes(M, K2), tc_y_bytes(N, K2)};
-        for (int i = 0; i < 2; ++i) {
-            if (((uintptr_t)bases[i] & 15u) != 0 || bytes[i] % P_ROW_BYTES != 0) return cudaErrorInvalidValue;
-            const cuuint64_t dims[2] = {(cuuint64_t)P_ROW_BYTES, (cuuint64_t)(bytes[i] / P_ROW_BYTES)};
-            const cuuint64_t strides[1] = {(cuuint64_t)P_ROW_BYTES};
-            const cuuint32_t box[2] = {(cuuint32_t)P_ROW_BYTES, (cuuint32_t)P_BOX_ROWS};
-            const cuuint32_t estr[2] = {1, 1};
-            if (encode(&maps[i], CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, const_cast<void *>(bases[i]), dims, strides, box,
-                       estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                       CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-                return cudaErrorInvalidValue;
-        }
+        e = encode_view(Ablk, bytes[0], P_ROW_BYTES, 8, P_ROW_BYTES / 8, P_BOX_ROWS, &maps[0]);
+        if (e == cudaSuccess) e = encode_view(Yblk, bytes[1], P_ROW_BYTES, 8, P_ROW_BYTES / 8, P_BOX_ROWS, &maps[1]);
+        if (e != cudaSuccess) return e;
         // clusters of two CTAs, as many as can be resident at once
         static int max_clusters = 0;
         cudaLaunchConfig_t cfg = {};
@@ -1319,9 +1334,6 @@ cudaError_t launch_tc_diff2(const void *Ablk, void *Yblk, int M, int K2, const f
             if (max_clusters <= 0) return cudaErrorInvalidConfiguration;
         }
         const long long npairs = (long long)((mtiles + 1) / 2) * ntiles;
-        // the row coordinates of the tensor copies are 32-bit
-        if ((long long)(bytes[0] / P_ROW_BYTES) > 0x7fffffffLL || (long long)(bytes[1] / P_ROW_BYTES) > 0x7fffffffLL)
-            return cudaErrorInvalidConfiguration;
         cfg.gridDim = dim3(2 * (unsigned)std::min<long long>(npairs, max_clusters));
         e = cudaLaunchKernelEx(&cfg, k_tc_pair, a, maps[0], maps[1]);
         if (e != cudaSuccess) return e;
