@@ -303,95 +303,169 @@ void ref_inverse_pad(const double A[9], double pad, double Ai[9]) {
     for (int k = 0; k < 9; ++k) Ai[k] = (r[k] / tmp) * pad;
 }
 
-void project(const oracle_model &m, long iclass, const double A[9], long size, Cplx *out) {
-    const long X = size / 2 + 1, Y = size;
-    std::memset(out, 0, sizeof(Cplx) * X * Y);
+// The inverse-and-pad matrix of Projector::project (3D) / rotate2D (2D).
+void projection_inverse(const oracle_model &m, const double A[9], double Ai[9]) {
     const double pad = (double)m.padding_factor;
-    double Ai[9];
     if (m.ref_dim == 2) {
         for (int r = 0; r < 3; ++r)
             for (int c = 0; c < 3; ++c) Ai[r * 3 + c] = A[c * 3 + r] * pad;
     } else {
         ref_inverse_pad(A, pad, Ai);
     }
-    const int r_max_out = (int)X - 1;
-    const int r_max_out_2 = r_max_out * r_max_out;
+}
+
+// One pixel (x, y) of Projector::project (3D, src/projector.cpp:664-733) or
+// rotate2D (2D, :1048-1100) of class volume vol; false where the reference
+// skips the pixel (radius test or outside the volume) and writes nothing.
+bool project_pixel(const oracle_model &m, const Cplx *vol, const double Ai[9], int x, int y, Cplx &out) {
     const int r_max_ref = (int)(m.proj_r_max * m.padding_factor);
     const int r_max_ref_2 = r_max_ref * r_max_ref;
     const long xd = m.proj_xdim, yd = m.proj_ydim, zd = m.proj_zdim;
-    const Cplx *vol = reinterpret_cast<const Cplx *>(m.ppref) + (size_t)iclass * xd * yd * zd;
+    double xp = Ai[0] * x + Ai[1] * y;
+    double yp = Ai[3] * x + Ai[4] * y;
+    double zp = Ai[6] * x + Ai[7] * y;
+    if (m.ref_dim == 2) {
+        // the radius test (:1055-1057) is made in integers as below
+        if ((long)m.padding_factor * m.padding_factor * (x * x + y * y) > r_max_ref_2) return false;
+        const bool neg2 = xp < 0;
+        if (neg2) {
+            xp = -xp;
+            yp = -yp;
+        }
+        const int x0 = r_floor(xp);
+        const double fx = xp - x0;
+        int y0 = r_floor(yp);
+        const double fy = yp - y0;
+        y0 -= (int)m.proj_yinit;
+        if (x0 < 0 || x0 + 1 >= xd || y0 < 0 || y0 + 1 >= yd) return false;
+        auto at2 = [&](int yy, int xx) { return vol[(size_t)yy * xd + xx]; };
+        auto lerp2 = [](double a, Cplx l, Cplx h) {  // LIN_INTERP, src/macros.h:373
+            return Cplx{l.re + (h.re - l.re) * a, l.im + (h.im - l.im) * a};
+        };
+        Cplx dx0 = lerp2(fx, at2(y0, x0), at2(y0, x0 + 1));
+        Cplx dx1 = lerp2(fx, at2(y0 + 1, x0), at2(y0 + 1, x0 + 1));
+        Cplx v = lerp2(fy, dx0, dx1);
+        if (neg2) v.im = -v.im;
+        out = v;
+        return true;
+    }
+    // r_ref_2 > r_max_ref_2 (:672), in double precision as the reference
+    const double r_ref_2 = xp * xp + yp * yp + zp * zp;
+    if (r_ref_2 > r_max_ref_2) return false;
+    bool neg = (xp < 0);
+    if (neg) {
+        xp = -xp;
+        yp = -yp;
+        zp = -zp;
+    }
+    const int x0 = r_floor(xp);
+    const double fx = xp - x0;
+    const int x1 = x0 + 1;
+    int y0 = r_floor(yp);
+    const double fy = yp - y0;
+    y0 -= (int)m.proj_yinit;
+    const int y1 = y0 + 1;
+    int z0 = r_floor(zp);
+    const double fz = zp - z0;
+    z0 -= (int)m.proj_zinit;
+    const int z1 = z0 + 1;
+    if (x0 < 0 || x0 + 1 >= xd || y0 < 0 || y0 + 1 >= yd || z0 < 0 || z0 + 1 >= zd) return false;
+    auto at = [&](int zz, int yy, int xx) { return vol[((size_t)zz * yd + yy) * xd + xx]; };
+    auto lerp = [](double a, Cplx l, Cplx h) {  // LIN_INTERP, src/macros.h:373
+        return Cplx{l.re + (h.re - l.re) * a, l.im + (h.im - l.im) * a};
+    };
+    Cplx dx00 = lerp(fx, at(z0, y0, x0), at(z0, y0, x1));
+    Cplx dx01 = lerp(fx, at(z1, y0, x0), at(z1, y0, x1));
+    Cplx dx10 = lerp(fx, at(z0, y1, x0), at(z0, y1, x1));
+    Cplx dx11 = lerp(fx, at(z1, y1, x0), at(z1, y1, x1));
+    Cplx dxy0 = lerp(fy, dx00, dx10);
+    Cplx dxy1 = lerp(fy, dx01, dx11);
+    Cplx v = lerp(fz, dxy0, dxy1);
+    if (neg) v.im = -v.im;
+    out = v;
+    return true;
+}
+
+const Cplx *class_volume(const oracle_model &m, long iclass) {
+    return reinterpret_cast<const Cplx *>(m.ppref) + (size_t)iclass * m.proj_xdim * m.proj_ydim * m.proj_zdim;
+}
+
+// Projector::project / rotate2D of class iclass into out [size][size/2+1]:
+// only the pixels inside the output image's circle (radius size / 2) that
+// the reference does not skip are written; with clear, out is zeroed first
+// (a fresh f2d), otherwise the other pixels keep their values, as the
+// reference's projection buffer does between orientations.
+void project(const oracle_model &m, long iclass, const double A[9], long size, Cplx *out, bool clear = true) {
+    const long X = size / 2 + 1, Y = size;
+    if (clear) std::memset(out, 0, sizeof(Cplx) * X * Y);
+    double Ai[9];
+    projection_inverse(m, A, Ai);
+    const Cplx *vol = class_volume(m, iclass);
+    const int r_max_out = (int)X - 1;
+    const int r_max_out_2 = r_max_out * r_max_out;
     for (long i = 0; i < Y; ++i) {
         const int y = (i <= r_max_out) ? (int)i : (int)(i - Y);
         const int y2 = y * y;
         const int x_max = r_floor(std::sqrt((double)(r_max_out_2 - y2)));
         for (int x = 0; x <= x_max; ++x) {
-            double xp = Ai[0] * x + Ai[1] * y;
-            double yp = Ai[3] * x + Ai[4] * y;
-            double zp = Ai[6] * x + Ai[7] * y;
-            if (m.ref_dim == 2) {
-                // Projector::rotate2D (src/projector.cpp:1010-1100): bilinear
-                // interpolation in the padded 2D reference (one z plane); the
-                // radius test (:1055-1057) is made in integers as below
-                if ((long)m.padding_factor * m.padding_factor * (x * x + y2) > r_max_ref_2) continue;
-                const bool neg2 = xp < 0;
-                if (neg2) {
-                    xp = -xp;
-                    yp = -yp;
-                }
-                const int x0 = r_floor(xp);
-                const double fx = xp - x0;
-                int y0 = r_floor(yp);
-                const double fy = yp - y0;
-                y0 -= (int)m.proj_yinit;
-                if (x0 < 0 || x0 + 1 >= xd || y0 < 0 || y0 + 1 >= yd) continue;
-                auto at2 = [&](int yy, int xx) { return vol[(size_t)yy * xd + xx]; };
-                auto lerp2 = [](double a, Cplx l, Cplx h) {  // LIN_INTERP, src/macros.h:373
-                    return Cplx{l.re + (h.re - l.re) * a, l.im + (h.im - l.im) * a};
-                };
-                Cplx dx0 = lerp2(fx, at2(y0, x0), at2(y0, x0 + 1));
-                Cplx dx1 = lerp2(fx, at2(y0 + 1, x0), at2(y0 + 1, x0 + 1));
-                Cplx v = lerp2(fy, dx0, dx1);
-                if (neg2) v.im = -v.im;
-                out[i * X + x] = v;
-                continue;
-            }
-            // r_ref_2 > r_max_ref_2 (:672), in double precision as the reference
-            const double r_ref_2 = xp * xp + yp * yp + zp * zp;
-            if (r_ref_2 > r_max_ref_2) continue;
-            bool neg = (xp < 0);
-            if (neg) {
-                xp = -xp;
-                yp = -yp;
-                zp = -zp;
-            }
-            const int x0 = r_floor(xp);
-            const double fx = xp - x0;
-            const int x1 = x0 + 1;
-            int y0 = r_floor(yp);
-            const double fy = yp - y0;
-            y0 -= (int)m.proj_yinit;
-            const int y1 = y0 + 1;
-            int z0 = r_floor(zp);
-            const double fz = zp - z0;
-            z0 -= (int)m.proj_zinit;
-            const int z1 = z0 + 1;
-            if (x0 < 0 || x0 + 1 >= xd || y0 < 0 || y0 + 1 >= yd || z0 < 0 || z0 + 1 >= zd) continue;
-            auto at = [&](int zz, int yy, int xx) { return vol[((size_t)zz * yd + yy) * xd + xx]; };
-            auto lerp = [](double a, Cplx l, Cplx h) {  // LIN_INTERP, src/macros.h:373
-                return Cplx{l.re + (h.re - l.re) * a, l.im + (h.im - l.im) * a};
-            };
-            Cplx dx00 = lerp(fx, at(z0, y0, x0), at(z0, y0, x1));
-            Cplx dx01 = lerp(fx, at(z1, y0, x0), at(z1, y0, x1));
-            Cplx dx10 = lerp(fx, at(z0, y1, x0), at(z0, y1, x1));
-            Cplx dx11 = lerp(fx, at(z1, y1, x0), at(z1, y1, x1));
-            Cplx dxy0 = lerp(fy, dx00, dx10);
-            Cplx dxy1 = lerp(fy, dx01, dx11);
-            Cplx v = lerp(fz, dxy0, dxy1);
-            if (neg) v.im = -v.im;
-            out[i * X + x] = v;
+            Cplx v;
+            if (project_pixel(m, vol, Ai, x, y, v)) out[i * X + x] = v;
         }
     }
 }
+
+// The reference projects every orientation of one call of
+// getAllSquaredDifferences or storeWeightedSums into one buffer (Fref,
+// src/ml_optimiser.cpp:7269, 8431) that is never cleared between
+// orientations: Projector::project does not zero its output
+// (src/projector.cpp:632-634), so a pixel it skips for one orientation keeps
+// the value of the last orientation that wrote it.  In 3D the only pixels
+// skipped for some orientations and written for others are those exactly
+// on the r_max circle, decided by the last bits of the rotated radius.
+// StaleCircle records, along one call's sequence of projected orientations,
+// the value each such pixel holds when an orientation skips it.
+struct StaleCircle {
+    std::vector<long> idx;  // flat index of each r_max-circle pixel in the image
+    std::vector<int> xs, ys;
+    std::vector<Cplx> last;
+    std::vector<std::vector<std::pair<long, Cplx>>> patches;  // per sequence element
+
+    StaleCircle(const oracle_model &m, long size) {
+        if (m.ref_dim == 2) return;
+        const long X = size / 2 + 1, Y = size;
+        const int r_max_out = (int)X - 1, r2 = (int)(m.proj_r_max * m.proj_r_max);
+        for (long i = 0; i < Y; ++i) {
+            const int y = (i <= r_max_out) ? (int)i : (int)(i - Y);
+            const int x_max = r_floor(std::sqrt((double)(r_max_out * r_max_out - y * y)));
+            for (int x = 0; x <= x_max; ++x)
+                if (x * x + y * y == r2) {
+                    idx.push_back(i * X + x);
+                    xs.push_back(x);
+                    ys.push_back(y);
+                }
+        }
+        last.assign(idx.size(), Cplx{0, 0});
+    }
+    // the next orientation of the sequence: returns its element index
+    long add(const oracle_model &m, long iclass, const double A[9]) {
+        patches.emplace_back();
+        if (idx.empty()) return (long)patches.size() - 1;
+        double Ai[9];
+        projection_inverse(m, A, Ai);
+        const Cplx *vol = class_volume(m, iclass);
+        for (size_t c = 0; c < idx.size(); ++c) {
+            Cplx v;
+            if (project_pixel(m, vol, Ai, xs[c], ys[c], v))
+                last[c] = v;
+            else
+                patches.back().push_back({idx[c], last[c]});
+        }
+        return (long)patches.size() - 1;
+    }
+    void apply(long e, Cplx *out) const {
+        for (const auto &pv : patches[(size_t)e]) out[pv.first] = pv.second;
+    }
+};
 
 // Trilinear insertion: src/backprojector.cpp:55-296 (no Ewald sphere,
 // identity magnification).  Data/weight accumulate in double.
@@ -758,8 +832,34 @@ int oracle_expectation(const oracle_model *mp, int64_t n, const oracle_particle 
             Mw.assign(nW, -999.);
             min_diff2 = 99e99;  // LARGE_NUMBER, src/macros.h:78
             // orientations are independent: threads split (class, direction,
-            // psi); each writes its own hidden indices and a private minimum
+            // psi); each writes its own hidden indices and a private minimum.
+            // The reference projects them in this order into one buffer; the
+            // values it leaves at skipped r_max-circle pixels are found first
+            // along that order (StaleCircle).
             const long n_orient = K * ND * NP;
+            StaleCircle stale(m, size);
+            std::vector<long> elem_of(n_orient, -1);
+            {
+                std::vector<double> ro, ti, ps;
+                double A[9];
+                for (long ioc = 0; ioc < n_orient; ++ioc) {
+                    const long ic = ioc / (ND * NP), id = (ioc / NP) % ND, is = ioc % NP;
+                    if (!(m.pdf_class[ic] > 0.)) continue;
+                    bool proceed = true;
+                    if (ipass > 0) {
+                        proceed = false;
+                        for (long it = 0; it < NT; ++it)
+                            if (coarse_sig[ioc * NT + it]) { proceed = true; break; }
+                    }
+                    if (!(proceed && m.pdf_direction[ic * ND + id] > 0.)) continue;
+                    S.orientations(id, is, cov, ro, ti, ps);
+                    for (long ior = 0; ior < nor; ++ior) {
+                        euler_matrix(ro[ior], ti[ior], ps[ior], A);
+                        const long e = stale.add(m, ic, A);
+                        if (ior == 0) elem_of[ioc] = e;
+                    }
+                }
+            }
 #pragma omp parallel
             {
                 std::vector<Cplx> Fref(npix), Frefctf(npix);
@@ -782,6 +882,7 @@ int oracle_expectation(const oracle_model *mp, int64_t n, const oracle_particle 
                     for (long ior = 0; ior < nor; ++ior) {
                         euler_matrix(ro[ior], ti[ior], ps[ior], A);
                         project(m, ic, A, size, reinterpret_cast<Cplx *>(Fref.data()));
+                        stale.apply(elem_of[ioc] + ior, Fref.data());
                         for (long k = 0; k < npix; ++k) {
                             Frefctf[k].re = Fref[k].re * Fctf[k] * myscale_d2;
                             Frefctf[k].im = Fref[k].im * Fctf[k] * myscale_d2;
@@ -953,7 +1054,8 @@ int oracle_expectation(const oracle_model *mp, int64_t n, const oracle_particle 
                     S.orientations(id, is, ov, ro, ti, ps);
                     for (long ior = 0; ior < nOR; ++ior) {
                         euler_matrix(ro[ior], ti[ior], ps[ior], A);
-                        project(m, ic, A, cur, Fref.data());
+                        // one buffer along the loop, as the reference's Fref
+                        project(m, ic, A, cur, Fref.data(), false);
                         std::fill(Fimg.begin(), Fimg.end(), Cplx{0, 0});
                         std::fill(Fweight.begin(), Fweight.end(), 0.);
                         double myscale = 1.;

@@ -560,7 +560,8 @@ int build_tables(gbr_bundle *b) {
     GBR_CUDA(b->proj2_c.zero());
     GBR_CUDA(launch_project_rows(b->vols_d.p, b->pg, b->eul_c.p, b->cls_c.p, nullptr, (int)R, b->pc.p, b->nc,
                                  b->proj_c.p, b->lda_c, b->proj2_c.p, b->ldk_c, nullptr, 0,
-                                 b->use_circ ? b->pcirc_c.p : nullptr, b->use_circ ? b->pmask_c.p : nullptr));
+                                 b->use_circ ? b->pcirc_c.p : nullptr, b->use_circ ? b->pmask_c.p : nullptr,
+                                 (b->crs / 2) * (b->crs / 2)));
     if (d.precision == GBR_PREC_BF16) {
         GBR_CUDA(b->proj_c_tc.reserve(tc_a_bytes((int)R, 2 * b->nc)));
         GBR_CUDA(launch_tc_pack_a(b->proj_c.p, b->lda_c, (int)R, 2 * b->nc, b->proj_c_tc.p, 0));
@@ -578,7 +579,8 @@ int build_tables(gbr_bundle *b) {
     GBR_CUDA(b->proj2_f.zero());
     GBR_CUDA(launch_project_rows(b->vols_d.p, b->pg, b->eul_f.p, b->cls_f.p, nullptr, (int)RF, b->pf.p, b->nf,
                                  b->proj_f.p, b->lda_f, b->proj2_f.p, b->ldk_f, nullptr, 0,
-                                 b->use_circ ? b->pcirc_f.p : nullptr, b->use_circ ? b->pmask_f.p : nullptr));
+                                 b->use_circ ? b->pcirc_f.p : nullptr, b->use_circ ? b->pmask_f.p : nullptr,
+                                 (b->cur / 2) * (b->cur / 2)));
     // ---- slice accumulators ----
     GBR_CUDA(b->bpimg.reserve((size_t)RF * b->nf));
     GBR_CUDA(b->bpw.reserve((size_t)RF * b->nf));

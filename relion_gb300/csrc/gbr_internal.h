@@ -82,11 +82,13 @@ cudaError_t launch_phase_table(float2 *out, const double *tx, const double *ty, 
 // circ / mask (optional): per pixel the bit index of pixels exactly on the
 // r_max circle (-1 elsewhere) and per orientation the bits of those the
 // reference projects (Projector::project decides them in double precision).
+// rout2 >= 0: pixels with x^2 + y^2 > rout2 are zero (the output image's
+// circle, radius size / 2, as the reference fills it).
 cudaError_t launch_project_rows(const float2 *const *vols, const VolGeom &g, const float *eul,
                                 const int *cls, const int *orient_ids, int n_orient,
                                 const PixelRef *pix, int npix, float *out_ri, int ld, float *out_p2,
                                 int ld2, float2 *out_c, cudaStream_t st, const int *circ = nullptr,
-                                const unsigned long long *mask = nullptr);
+                                const unsigned long long *mask = nullptr, int rout2 = -1);
 
 // FP32 FMA throughput probe (ms of one timed launch and its flop count).
 cudaError_t launch_fp32_probe(float *ms, double *flops);

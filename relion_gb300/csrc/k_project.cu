@@ -82,13 +82,17 @@ __device__ __forceinline__ float2 sample_slice(const float2 *__restrict__ vol, c
 // circ[j] >= 0 marks the pixels exactly on the r_max circle; bit circ[j] of
 // mask[orientation] says whether the reference projects it for that
 // orientation (decided on the host in double precision as
-// Projector::project does, src/projector.cpp:638-672).
+// Projector::project does, src/projector.cpp:638-672).  Pixels with
+// x^2 + y^2 > rout2 (rout2 >= 0) are not projected: the reference fills only
+// the circle of the output image, radius XSIZE - 1 = size / 2 (:641-660,
+// rotate2D :1020-1048), which for the coarse pass is smaller than r_max.
 __global__ void k_project_rows(const float2 *const *__restrict__ vols, const VolGeom g,
                                const float *__restrict__ eul, const int *__restrict__ cls,
                                const int *__restrict__ orient_ids, int n_orient,
                                const PixelRef *__restrict__ pix, int npix, float *__restrict__ out_ri,
                                int ld, float *__restrict__ out_p2, int ld2, float2 *__restrict__ out_c,
-                               const int *__restrict__ circ, const unsigned long long *__restrict__ mask) {
+                               const int *__restrict__ circ, const unsigned long long *__restrict__ mask,
+                               int rout2) {
     const int o = blockIdx.y;
     if (o >= n_orient) return;
     const int oid = orient_ids ? orient_ids[o] : o;
@@ -100,7 +104,9 @@ __global__ void k_project_rows(const float2 *const *__restrict__ vols, const Vol
     for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < npix; j += gridDim.x * blockDim.x) {
         const PixelRef pr = pix[j];
         const int cb = circ ? circ[j] : -1;
-        const float2 v = (cb >= 0 && !((cm >> cb) & 1ull)) ? make_float2(0.f, 0.f) : sample_slice(vol, g, Ai, pr.x, pr.y);
+        const bool outside = rout2 >= 0 && pr.x * pr.x + pr.y * pr.y > rout2;
+        const float2 v = (outside || (cb >= 0 && !((cm >> cb) & 1ull))) ? make_float2(0.f, 0.f)
+                                                                        : sample_slice(vol, g, Ai, pr.x, pr.y);
         if (out_ri) {
             float *row = out_ri + (size_t)oid * ld;
             row[2 * j] = v.x;
@@ -138,7 +144,7 @@ cudaError_t launch_project_rows(const float2 *const *vols, const VolGeom &g, con
                                 const int *cls, const int *orient_ids, int n_orient,
                                 const PixelRef *pix, int npix, float *out_ri, int ld, float *out_p2,
                                 int ld2, float2 *out_c, cudaStream_t st, const int *circ,
-                                const unsigned long long *mask) {
+                                const unsigned long long *mask, int rout2) {
     if (n_orient <= 0 || npix <= 0) return cudaSuccess;
     const int threads = 128;
     const int bx = (npix + threads - 1) / threads;
@@ -149,7 +155,7 @@ cudaError_t launch_project_rows(const float2 *const *vols, const VolGeom &g, con
                                                  n, pix, npix, out_ri ? out_ri + (orient_ids ? 0 : (size_t)o0 * ld) : nullptr,
                                                  ld, out_p2 ? out_p2 + (orient_ids ? 0 : (size_t)o0 * ld2) : nullptr,
                                                  ld2, out_c ? out_c + (orient_ids ? 0 : (size_t)o0 * npix) : nullptr,
-                                                 circ, mask);
+                                                 circ, mask, rout2);
         if (!orient_ids) {
             // rows are addressed by the orientation index; shift eul/cls/mask too
             eul += (size_t)n * 9;

@@ -24,6 +24,10 @@ sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 CASES = [
     ("box32_hp1", "small32", 5, 4, dict(healpix_order=1, psi_step=30.0)),
     ("box32_hp2", "small32", 6, 2, dict(healpix_order=2, psi_step=15.0, offset_range_px=3.0, offset_step_px=1.0)),
+    # a late iteration: the whole box as current size, a small coarse size and
+    # a reference sharp to Nyquist (the coarse projection fills only the
+    # coarse image's own circle, inside the reference's r_max)
+    ("box32_late", "small32_late", 7, 3, dict(healpix_order=1, psi_step=30.0)),
 ]
 PER_PARTICLE = ("rot", "tilt", "psi", "xoff", "yoff", "pmax", "dLL", "nr_sign", "coarse_min_diff2",
                 "coarse_sum_weight", "coarse_significant_weight", "fine_min_diff2", "fine_sum_weight",
@@ -31,10 +35,14 @@ PER_PARTICLE = ("rot", "tilt", "psi", "xoff", "yoff", "pmax", "dLL", "nr_sign", 
 
 
 def config(name):
-    """A box-32 shape of the box-64 generator (2 A pixels halved in count)."""
+    """A box-32 shape of the box-64 generator (2 A pixels halved in count);
+    "small32_late": the same in a late iteration (current size 32, coarse
+    size 12, reference low-passed at Nyquist, 8 A)."""
     from relion_gb300 import datagen
     c = dict(datagen.CONFIGS["cfg0_box64"])
     c.update(box=32, pixel=4.0, n_blobs=150, blob_radius=10.0, max_shift=2.0, diameter=100.0, ini_high=24.0)
+    if name == "small32_late":
+        c.update(current_size=32, coarse_size=12, ini_high=8.0)
     return c
 
 
