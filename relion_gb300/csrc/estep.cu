@@ -157,8 +157,8 @@ struct gbr_bundle {
     // backprojector (FP64)
     std::vector<DevBuf<double2>> bp_data;
     std::vector<DevBuf<double>> bp_weight;
-    DevBuf<double2 *> bpd_ptrs;
-    DevBuf<double *> bpw_ptrs;
+    std::vector<DevBuf<float4>> bp_stage;  // one batch's insertions (FP32), flushed into bp_data / bp_weight
+    DevBuf<float4 *> bps_ptrs;
     size_t bp_vox = 0;
     // iteration tables
     bool tables_ready = false;
@@ -1072,11 +1072,12 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
     GBR_CUDA(cudaMemsetAsync(w->act_count.p, 0, sizeof(int), st));
     GBR_CUDA(launch_compact_flags(b->active.p, (int)b->RF, w->act_list.p, w->act_count.p, st));
     GBR_CUDA(launch_backproject(w->act_list.p, w->act_count.p, (int)b->RF, b->eul_f.p, nOR, b->cls_of_r.p,
-                                b->bpimg.p, b->bpw.p, b->pf.p, b->nf, b->bg, b->bpd_ptrs.p, b->bpw_ptrs.p,
-                                b->active.p, st, b->use_circ ? b->bcirc_f.p : nullptr,
-                                b->use_circ ? b->bmask_f.p : nullptr));
+                                b->bpimg.p, b->bpw.p, b->pf.p, b->nf, b->bg, b->bps_ptrs.p, b->active.p, st,
+                                b->use_circ ? b->bcirc_f.p : nullptr, b->use_circ ? b->bmask_f.p : nullptr));
+    for (long k = 0; k < b->K; ++k)
+        GBR_CUDA(launch_bp_flush(b->bp_stage[k].p, b->bp_data[k].p, b->bp_weight[k].p, b->bp_vox, st));
     GBR_CUDA(cudaEventRecord(w->ev[9], st));
-    w->launches += 2;
+    w->launches += 2 + (int)b->K;
     // ---- results ----
     GBR_CUDA(w->h_ps.reserve(n));
     GBR_CUDA(w->h_shell.reserve((size_t)n * b->nshell));
@@ -1246,18 +1247,18 @@ int gbr_bundle_create(const gbr_model_desc *desc, int device, gbr_bundle **out) 
     b->bp_vox = (size_t)b->bg.xdim * b->bg.ydim * b->bg.zdim;
     b->bp_data.resize(b->K);
     b->bp_weight.resize(b->K);
-    std::vector<double2 *> dp(b->K);
-    std::vector<double *> wp(b->K);
+    b->bp_stage.resize(b->K);
+    std::vector<float4 *> sp(b->K);
     for (long k = 0; k < b->K; ++k) {
         GBR_CUDA(b->bp_data[k].reserve(b->bp_vox));
         GBR_CUDA(b->bp_weight[k].reserve(b->bp_vox));
+        GBR_CUDA(b->bp_stage[k].reserve(b->bp_vox));
         GBR_CUDA(b->bp_data[k].zero());
         GBR_CUDA(b->bp_weight[k].zero());
-        dp[k] = b->bp_data[k].p;
-        wp[k] = b->bp_weight[k].p;
+        GBR_CUDA(b->bp_stage[k].zero());
+        sp[k] = b->bp_stage[k].p;
     }
-    GBR_CUDA(b->bpd_ptrs.upload(dp.data(), dp.size()));
-    GBR_CUDA(b->bpw_ptrs.upload(wp.data(), wp.size()));
+    GBR_CUDA(b->bps_ptrs.upload(sp.data(), sp.size()));
     GBR_CUDA(b->w_pdf_cls.reserve(b->K));
     GBR_CUDA(b->w_pdf_dir.reserve((size_t)b->K * b->ND));
     GBR_CUDA(b->w_pdf_cls.zero());

@@ -288,11 +288,14 @@ cudaError_t launch_compact_flags(const unsigned char *flags, int n, int *list, i
 // circ / mask: as launch_project_rows, for the backprojection's own test
 // (BackProjector::backproject2Dto3D decides the r_max-circle pixels in double
 // precision by its per-row ellipse bounds and its 3D radius check).
+// Trilinear insertion of the active slices into the FP32 staging volumes
+// (float4 re, im, weight, 0 per voxel, one per class); launch_bp_flush adds
+// a staging volume into the FP64 data / weight volumes and clears it.
 cudaError_t launch_backproject(const int *list, const int *count, int max_list, const float *eul_f, int nOR,
                                const int *cls_of_r, float2 *bpimg, float *bpw, const PixelRef *pf, int nf,
-                               const VolGeom &g, double2 *const *data, double *const *weight,
-                               unsigned char *active, cudaStream_t st, const int *circ = nullptr,
-                               const unsigned long long *mask = nullptr);
+                               const VolGeom &g, float4 *const *stage, unsigned char *active, cudaStream_t st,
+                               const int *circ = nullptr, const unsigned long long *mask = nullptr);
+cudaError_t launch_bp_flush(float4 *stage, double2 *data, double *weight, size_t nvox, cudaStream_t st);
 cudaError_t launch_gather_pdat(const double *old_offset, const double *prior, const double *xi2,
                                const double *norm, const double *scale, int n, double *pdat, cudaStream_t st);
 cudaError_t launch_cand_seg(const unsigned int *cnt, int n, int cap, long long *seg, cudaStream_t st);

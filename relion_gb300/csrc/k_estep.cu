@@ -1232,16 +1232,19 @@ __global__ void k_compact_flags(const unsigned char *__restrict__ flags, int n, 
 }
 
 // Trilinear insertion of the accumulated 2D slices of the active fine
-// orientations into the FP64 data and weight volumes
-// (backproject2Dto3D, src/backprojector.cpp:55-296).  Each block handles
-// one slice; the slice accumulators are cleared for the next batch.
+// orientations (backproject2Dto3D, src/backprojector.cpp:55-296) into the
+// batch's FP32 staging volume: one float4 (re, im, weight, 0) per voxel, one
+// vector atomic per corner (8 per pixel instead of 24 FP64 atomics);
+// k_bp_flush adds the staging volume into the FP64 data and weight volumes
+// after every batch, so the volumes accumulate across batches in FP64 and a
+// staging sum holds one batch at most.  Each block handles one slice; the
+// slice accumulators are cleared for the next batch.
 __global__ void k_backproject(const int *__restrict__ list, const float *__restrict__ eul_f, int nOR,
                               const int *__restrict__ cls_of_r, float2 *__restrict__ bpimg,
                               float *__restrict__ bpw, const PixelRef *__restrict__ pf, int nf,
-                              const VolGeom g, double2 *const *__restrict__ data,
-                              double *const *__restrict__ weight, unsigned char *__restrict__ active,
-                              const int *__restrict__ count, const int *__restrict__ circ,
-                              const unsigned long long *__restrict__ cmask) {
+                              const VolGeom g, float4 *const *__restrict__ stage,
+                              unsigned char *__restrict__ active, const int *__restrict__ count,
+                              const int *__restrict__ circ, const unsigned long long *__restrict__ cmask) {
     const int nlist = *count;
     for (int li = blockIdx.x; li < nlist; li += gridDim.x) {
     const int rf = list[li];
@@ -1250,8 +1253,7 @@ __global__ void k_backproject(const int *__restrict__ list, const float *__restr
     if (threadIdx.x < 9) Ai[threadIdx.x] = eul_f[(size_t)rf * 9 + threadIdx.x];
     __syncthreads();
     const int ic = cls_of_r[rf / nOR];
-    double2 *dv = data[ic];
-    double *wv = weight[ic];
+    float4 *sv = stage[ic];
     const int rr = (int)lrintf((float)g.r_max * g.pad);   // ROUND(r_max * pad)
     const int max_r2 = rr * rr;
     const size_t sy = (size_t)g.xdim, sz = (size_t)g.xdim * g.ydim;
@@ -1287,12 +1289,8 @@ __global__ void k_backproject(const int *__restrict__ list, const float *__restr
             const size_t base = (size_t)y0 * g.xdim + x0;
             const size_t off4[4] = {0, 1, (size_t)g.xdim, (size_t)g.xdim + 1};
 #pragma unroll
-            for (int c = 0; c < 4; ++c) {
-                const double dc = (double)d4[c];
-                atomicAdd(&dv[base + off4[c]].x, dc * v2.x);
-                atomicAdd(&dv[base + off4[c]].y, dc * v2.y);
-                atomicAdd(&wv[base + off4[c]], dc * w);
-            }
+            for (int c = 0; c < 4; ++c)
+                atomicAdd(&sv[base + off4[c]], make_float4(d4[c] * v2.x, d4[c] * v2.y, d4[c] * w, 0.f));
             continue;
         }
         float zp = fmaf(Ai[6], (float)pr.x, Ai[7] * (float)pr.y);
@@ -1314,14 +1312,27 @@ __global__ void k_backproject(const int *__restrict__ list, const float *__restr
         const size_t base = (size_t)z0 * sz + (size_t)y0 * sy + x0;
         const size_t off[8] = {0, 1, sy, sy + 1, sz, sz + 1, sz + sy, sz + sy + 1};
 #pragma unroll
-        for (int c = 0; c < 8; ++c) {
-            const double dc = (double)dd[c];
-            atomicAdd(&dv[base + off[c]].x, dc * val.x);
-            atomicAdd(&dv[base + off[c]].y, dc * val.y);
-            atomicAdd(&wv[base + off[c]], dc * w);
-        }
+        for (int c = 0; c < 8; ++c)
+            atomicAdd(&sv[base + off[c]], make_float4(dd[c] * val.x, dd[c] * val.y, dd[c] * w, 0.f));
     }
     if (threadIdx.x == 0) active[rf] = 0;
+    }
+}
+
+// Adds one batch's FP32 staging volume into the FP64 data and weight
+// volumes and clears it (voxels no slice touched are only read).
+__global__ void k_bp_flush(float4 *__restrict__ stage, double2 *__restrict__ data, double *__restrict__ weight,
+                           size_t nvox) {
+    for (size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < nvox; v += (size_t)gridDim.x * blockDim.x) {
+        const float4 s = stage[v];
+        if (s.x != 0.f || s.y != 0.f || s.z != 0.f) {
+            double2 dv = data[v];
+            dv.x += (double)s.x;
+            dv.y += (double)s.y;
+            data[v] = dv;
+            weight[v] += (double)s.z;
+            stage[v] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
     }
 }
 
@@ -1660,11 +1671,20 @@ cudaError_t launch_compact_flags(const unsigned char *flags, int n, int *list, i
     return cudaGetLastError();
 }
 
+cudaError_t launch_bp_flush(float4 *stage, double2 *data, double *weight, size_t nvox, cudaStream_t st) {
+    if (nvox == 0) return cudaSuccess;
+    int dev = 0, nsm = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const size_t blocks = std::min<size_t>((nvox + 255) / 256, (size_t)nsm * 16);
+    k_bp_flush<<<(unsigned)blocks, 256, 0, st>>>(stage, data, weight, nvox);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_backproject(const int *list, const int *count, int max_list, const float *eul_f, int nOR,
                                const int *cls_of_r, float2 *bpimg, float *bpw, const PixelRef *pf, int nf,
-                               const VolGeom &g, double2 *const *data, double *const *weight,
-                               unsigned char *active, cudaStream_t st, const int *circ,
-                               const unsigned long long *mask) {
+                               const VolGeom &g, float4 *const *stage, unsigned char *active, cudaStream_t st,
+                               const int *circ, const unsigned long long *mask) {
     if (max_list <= 0) return cudaSuccess;
     if ((circ == nullptr) != (mask == nullptr)) return cudaErrorInvalidValue;
     // slices are read from the device-side list; the grid covers the device
@@ -1673,8 +1693,8 @@ cudaError_t launch_backproject(const int *list, const int *count, int max_list, 
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     const int grid = std::min(max_list, 8 * nsm);
-    k_backproject<<<grid, 256, 0, st>>>(list, eul_f, nOR, cls_of_r, bpimg, bpw, pf, nf, g, data, weight,
-                                        active, count, circ, mask);
+    k_backproject<<<grid, 256, 0, st>>>(list, eul_f, nOR, cls_of_r, bpimg, bpw, pf, nf, g, stage, active, count,
+                                        circ, mask);
     return cudaGetLastError();
 }
 
