@@ -163,6 +163,11 @@ def run_ours(args, world, rank, local):
 
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
 
+    # tile order, coarse-kernel form and fine-pass form picked on this batch
+    # (the autotuner clears the sums its own runs added)
+    from relion_gb300 import autotune
+    tuned = autotune.tune(bundle, worker, dev_batch, repeats=2)
+
     def barrier():
         if world > 1:
             import torch.distributed as dist
@@ -328,6 +333,11 @@ def run_ours(args, world, rank, local):
                                               "worker's copy stream during the previous step (gbr_stage_images); "
                                               "one timed region over all steps"},
         "gpu_launches": int(launches),
+        "autotune": {"options": tuned["options"],
+                     "cross_term_ms": [[o, round(float(v), 4)] for o, v in tuned["coarse"]],
+                     "fine_stages_ms": [[o, round(float(v), 4)] for o, v in tuned["fine"]],
+                     "note": "measured on the bench batch before the warm-up steps; each candidate on the "
+                             "stages it changes"},
         "roofline": {"bound": bound, "kernel": kname,
                      "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                      "peak_source": peak_src,

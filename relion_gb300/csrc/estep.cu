@@ -1075,7 +1075,7 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
                                 b->bpimg.p, b->bpw.p, b->pf.p, b->nf, b->bg, b->bps_ptrs.p, b->active.p, st,
                                 b->use_circ ? b->bcirc_f.p : nullptr, b->use_circ ? b->bmask_f.p : nullptr));
     for (long k = 0; k < b->K; ++k)
-        GBR_CUDA(launch_bp_flush(b->bp_stage[k].p, b->bp_data[k].p, b->bp_weight[k].p, b->bp_vox, st));
+        GBR_CUDA(launch_bp_flush(b->bp_stage[k].p, b->bp_data[k].p, b->bp_weight[k].p, b->bg, st));
     GBR_CUDA(cudaEventRecord(w->ev[9], st));
     w->launches += 2 + (int)b->K;
     // ---- results ----

@@ -295,7 +295,7 @@ cudaError_t launch_backproject(const int *list, const int *count, int max_list, 
                                const int *cls_of_r, float2 *bpimg, float *bpw, const PixelRef *pf, int nf,
                                const VolGeom &g, float4 *const *stage, unsigned char *active, cudaStream_t st,
                                const int *circ = nullptr, const unsigned long long *mask = nullptr);
-cudaError_t launch_bp_flush(float4 *stage, double2 *data, double *weight, size_t nvox, cudaStream_t st);
+cudaError_t launch_bp_flush(float4 *stage, double2 *data, double *weight, const VolGeom &g, cudaStream_t st);
 cudaError_t launch_gather_pdat(const double *old_offset, const double *prior, const double *xi2,
                                const double *norm, const double *scale, int n, double *pdat, cudaStream_t st);
 cudaError_t launch_cand_seg(const unsigned int *cnt, int n, int cap, long long *seg, cudaStream_t st);

@@ -1320,10 +1320,18 @@ __global__ void k_backproject(const int *__restrict__ list, const float *__restr
 }
 
 // Adds one batch's FP32 staging volume into the FP64 data and weight
-// volumes and clears it (voxels no slice touched are only read).
+// volumes and clears it.  Only voxels within r_max pad + 2 of the origin can
+// hold insertions (pixels inside r_max, trilinear corners one voxel out); the
+// others are not read, and voxels no slice touched are only read.
 __global__ void k_bp_flush(float4 *__restrict__ stage, double2 *__restrict__ data, double *__restrict__ weight,
-                           size_t nvox) {
+                           const VolGeom g) {
+    const size_t nvox = (size_t)g.xdim * g.ydim * g.zdim;
+    const int rlim = g.r_max * g.pad + 2;
     for (size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < nvox; v += (size_t)gridDim.x * blockDim.x) {
+        const int x = (int)(v % g.xdim);
+        const size_t yz = v / g.xdim;
+        const int y = (int)(yz % g.ydim) + g.yinit, z = (int)(yz / g.ydim) + g.zinit;
+        if (x * x + y * y + z * z > rlim * rlim) continue;
         const float4 s = stage[v];
         if (s.x != 0.f || s.y != 0.f || s.z != 0.f) {
             double2 dv = data[v];
@@ -1671,13 +1679,14 @@ cudaError_t launch_compact_flags(const unsigned char *flags, int n, int *list, i
     return cudaGetLastError();
 }
 
-cudaError_t launch_bp_flush(float4 *stage, double2 *data, double *weight, size_t nvox, cudaStream_t st) {
+cudaError_t launch_bp_flush(float4 *stage, double2 *data, double *weight, const VolGeom &g, cudaStream_t st) {
+    const size_t nvox = (size_t)g.xdim * g.ydim * g.zdim;
     if (nvox == 0) return cudaSuccess;
     int dev = 0, nsm = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     const size_t blocks = std::min<size_t>((nvox + 255) / 256, (size_t)nsm * 16);
-    k_bp_flush<<<(unsigned)blocks, 256, 0, st>>>(stage, data, weight, nvox);
+    k_bp_flush<<<(unsigned)blocks, 256, 0, st>>>(stage, data, weight, g);
     return cudaGetLastError();
 }
 
