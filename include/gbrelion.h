@@ -180,8 +180,13 @@ typedef enum {
                                  group of the coarse kernel's tile order (0: 32)     */
     GBR_OPT_KEEP_A = 8,       /* precision form: 1 reads the projection tiles with
                                  an L2 keep policy (default 0)                        */
-    GBR_OPT_PAIR = 9          /* precision form: 1 runs the coarse cross term on SM
+    GBR_OPT_PAIR = 9,         /* precision form: 1 runs the coarse cross term on SM
                                  pairs (tcgen05 cta_group::2; default 0)             */
+    GBR_OPT_BP_FLUSH = 10     /* particles collected in the FP32 staging volumes
+                                 before they are added into the FP64 volumes
+                                 (default 2048; 0: after every pass).  Reading,
+                                 replacing or reconstructing the volumes flushes
+                                 first.                                               */
 } gbr_worker_option;
 int gbr_worker_set_option(gbr_worker *w, int option, int64_t value);
 

@@ -28,6 +28,13 @@ namespace {
 
 thread_local std::string g_last_error;
 
+// Particles whose backprojected insertions the FP32 staging volumes collect
+// before they are added into the FP64 volumes (GBR_OPT_BP_FLUSH).  Each voxel
+// inside the insertion sphere takes ~70 insertions per 512 particles at
+// current size 256, so an FP32 sum of 2048 particles carries ~1e-6 relative
+// rounding; the FP64 volumes accumulate the flushes.
+constexpr int kBpFlushDefault = 2048;
+
 int fail(int status, const std::string &msg) {
     g_last_error = msg;
     return status;
@@ -157,8 +164,9 @@ struct gbr_bundle {
     // backprojector (FP64)
     std::vector<DevBuf<double2>> bp_data;
     std::vector<DevBuf<double>> bp_weight;
-    std::vector<DevBuf<float4>> bp_stage;  // one batch's insertions (FP32), flushed into bp_data / bp_weight
+    std::vector<DevBuf<float4>> bp_stage;  // insertions since the last flush (FP32), flushed into bp_data / bp_weight
     DevBuf<float4 *> bps_ptrs;
+    long long staged = 0;                  // particles inserted into bp_stage since the last flush
     size_t bp_vox = 0;
     // iteration tables
     bool tables_ready = false;
@@ -292,6 +300,7 @@ struct gbr_worker {
     DevBuf<int2> items_d;
     DevBuf<unsigned char> ytp;  // per-particle BF16 Y tiles of the restricted pass
     int batch_cap = 0;           // particles per pass (GBR_OPT_BATCH_CAP; 0 = from the budget)
+    int bp_flush = kBpFlushDefault;  // flush the staging volumes at this many particles (GBR_OPT_BP_FLUSH)
     TcTuning tc_tune;            // GBR_OPT_TILE_GROUP, GBR_OPT_KEEP_A, GBR_OPT_PAIR
     int pass_cap = 0;            // particles per pass of the current call
     // debug copies of the last call, one entry per pass (gbr_worker_debug_fetch)
@@ -887,6 +896,18 @@ int restricted_coarse(gbr_worker *w, int n, unsigned int *segmask) {
 }
 
 // One sub-batch of n <= cap particles whose inputs are already in w->X etc.
+// Adds the staged insertions of every class into the FP64 volumes (after
+// all work queued on the device), before the volumes are read or replaced.
+int flush_staged(gbr_bundle *b) {
+    GBR_CUDA(cudaDeviceSynchronize());
+    if (b->staged == 0) return GBR_OK;
+    for (long k = 0; k < b->K; ++k)
+        GBR_CUDA(launch_bp_flush(b->bp_stage[k].p, b->bp_data[k].p, b->bp_weight[k].p, b->bg, 0));
+    GBR_CUDA(cudaDeviceSynchronize());
+    b->staged = 0;
+    return GBR_OK;
+}
+
 int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h, gbr_particle_result *res) {
     gbr_bundle *b = w->b;
     const gbr_model_desc &d = b->d;
@@ -1074,10 +1095,17 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
     GBR_CUDA(launch_backproject(w->act_list.p, w->act_count.p, (int)b->RF, b->eul_f.p, nOR, b->cls_of_r.p,
                                 b->bpimg.p, b->bpw.p, b->pf.p, b->nf, b->bg, b->bps_ptrs.p, b->active.p, st,
                                 b->use_circ ? b->bcirc_f.p : nullptr, b->use_circ ? b->bmask_f.p : nullptr));
-    for (long k = 0; k < b->K; ++k)
-        GBR_CUDA(launch_bp_flush(b->bp_stage[k].p, b->bp_data[k].p, b->bp_weight[k].p, b->bg, st));
+    // the FP32 staging volumes are added into the FP64 volumes once they hold
+    // bp_flush particles (and before anything reads the FP64 volumes)
+    b->staged += n;
+    if (b->staged >= w->bp_flush) {
+        for (long k = 0; k < b->K; ++k)
+            GBR_CUDA(launch_bp_flush(b->bp_stage[k].p, b->bp_data[k].p, b->bp_weight[k].p, b->bg, st));
+        b->staged = 0;
+        w->launches += (int)b->K;
+    }
     GBR_CUDA(cudaEventRecord(w->ev[9], st));
-    w->launches += 2 + (int)b->K;
+    w->launches += 2;
     // ---- results ----
     GBR_CUDA(w->h_ps.reserve(n));
     GBR_CUDA(w->h_shell.reserve((size_t)n * b->nshell));
@@ -1369,6 +1397,7 @@ int gbr_worker_set_option(gbr_worker *w, int option, int64_t value) {
             if (value > 1) return fail(GBR_ERR_INVALID, "pair must be 0 or 1");
             w->tc_tune.pair = (int)value;
             break;
+        case GBR_OPT_BP_FLUSH: w->bp_flush = (int)value; break;
         default: return fail(GBR_ERR_INVALID, "unknown worker option " + std::to_string(option));
     }
     return GBR_OK;
@@ -1820,7 +1849,8 @@ int gbr_backprojector_dims(const gbr_bundle *b, int64_t *xdim, int64_t *ydim, in
 int gbr_backprojector_download(gbr_bundle *b, int64_t iclass, double *data, double *weight) {
     if (!b || iclass < 0 || iclass >= b->K) return fail(GBR_ERR_INVALID, "bad class");
     GBR_CUDA(cudaSetDevice(b->device));
-    GBR_CUDA(cudaDeviceSynchronize());
+    int s = flush_staged(b);
+    if (s) return s;
     if (data) GBR_CUDA(cudaMemcpy(data, b->bp_data[iclass].p, sizeof(double2) * b->bp_vox, cudaMemcpyDeviceToHost));
     if (weight) GBR_CUDA(cudaMemcpy(weight, b->bp_weight[iclass].p, sizeof(double) * b->bp_vox, cudaMemcpyDeviceToHost));
     return GBR_OK;
@@ -1829,7 +1859,8 @@ int gbr_backprojector_download(gbr_bundle *b, int64_t iclass, double *data, doub
 int gbr_backprojector_upload(gbr_bundle *b, int64_t iclass, const double *data, const double *weight) {
     if (!b || !data || !weight || iclass < 0 || iclass >= b->K) return fail(GBR_ERR_INVALID, "bad class or data");
     GBR_CUDA(cudaSetDevice(b->device));
-    GBR_CUDA(cudaDeviceSynchronize());
+    int s = flush_staged(b);
+    if (s) return s;
     GBR_CUDA(cudaMemcpy(b->bp_data[iclass].p, data, sizeof(double2) * b->bp_vox, cudaMemcpyHostToDevice));
     GBR_CUDA(cudaMemcpy(b->bp_weight[iclass].p, weight, sizeof(double) * b->bp_vox, cudaMemcpyHostToDevice));
     return GBR_OK;
@@ -1839,7 +1870,8 @@ namespace {
 int recon_begin(gbr_bundle *b, int64_t iclass) {
     if (!b || iclass < 0 || iclass >= b->K) return fail(GBR_ERR_INVALID, "bad class");
     GBR_CUDA(cudaSetDevice(b->device));
-    GBR_CUDA(cudaDeviceSynchronize());
+    int s = flush_staged(b);
+    if (s) return s;
     if (!b->recon) b->recon = gbr::recon_work_create();
     return GBR_OK;
 }
@@ -1973,10 +2005,13 @@ int gbr_model_set_class_offsets(gbr_bundle *b, const double *prior_offset_class)
 int gbr_bundle_reset_wsum(gbr_bundle *b) {
     if (!b) return fail(GBR_ERR_INVALID, "null bundle");
     GBR_CUDA(cudaSetDevice(b->device));
+    GBR_CUDA(cudaDeviceSynchronize());
     for (long k = 0; k < b->K; ++k) {
         GBR_CUDA(b->bp_data[k].zero());
         GBR_CUDA(b->bp_weight[k].zero());
+        if (b->staged) GBR_CUDA(b->bp_stage[k].zero());
     }
+    b->staged = 0;
     GBR_CUDA(b->w_pdf_cls.zero());
     GBR_CUDA(b->w_pdf_dir.zero());
     if (b->is2d) GBR_CUDA(b->w_prior_off.zero());

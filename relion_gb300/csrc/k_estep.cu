@@ -1233,12 +1233,12 @@ __global__ void k_compact_flags(const unsigned char *__restrict__ flags, int n, 
 
 // Trilinear insertion of the accumulated 2D slices of the active fine
 // orientations (backproject2Dto3D, src/backprojector.cpp:55-296) into the
-// batch's FP32 staging volume: one float4 (re, im, weight, 0) per voxel, one
-// vector atomic per corner (8 per pixel instead of 24 FP64 atomics);
-// k_bp_flush adds the staging volume into the FP64 data and weight volumes
-// after every batch, so the volumes accumulate across batches in FP64 and a
-// staging sum holds one batch at most.  Each block handles one slice; the
-// slice accumulators are cleared for the next batch.
+// FP32 staging volume: one float4 (re, im, weight, 0) per voxel, one vector
+// atomic per corner (8 per pixel instead of 24 FP64 atomics); k_bp_flush adds
+// the staging volume into the FP64 data and weight volumes once it holds a
+// set number of particles (a few batches), so the volumes accumulate in FP64
+// and a staging sum holds a bounded number of particles.  Each block handles
+// one slice; the slice accumulators are cleared for the next batch.
 __global__ void k_backproject(const int *__restrict__ list, const float *__restrict__ eul_f, int nOR,
                               const int *__restrict__ cls_of_r, float2 *__restrict__ bpimg,
                               float *__restrict__ bpw, const PixelRef *__restrict__ pf, int nf,

@@ -208,7 +208,7 @@ ALL_BLOCKS = -2
 
 # gbr_worker_set_option selectors (include/gbrelion.h, gbr_worker_option)
 WORKER_OPTIONS = dict(debug=1, fine_mode=2, coarse_rows=3, cand_cap=4, cand_buf=5, batch_cap=6, tile_group=7,
-                      keep_a=8, pair=9)
+                      keep_a=8, pair=9, bp_flush=10)
 FINE_MODES = dict(auto=0, dense=1, sparse=2)
 COARSE_ROWS = dict(skip=0, full=1)
 
@@ -220,8 +220,10 @@ class MlOptimiserCuda:
     "sparse"), coarse_rows ("skip", "full"), cand_cap, cand_buf, batch_cap
     (particles per pass of a call), tile_group (orientation tiles of 128 rows
     per group of the coarse tensor-core kernel's tile order), keep_a (1:
-    projection tiles read with an L2 keep policy) and pair (1: the coarse
-    cross term on SM pairs, tcgen05 cta_group::2)."""
+    projection tiles read with an L2 keep policy), pair (1: the coarse
+    cross term on SM pairs, tcgen05 cta_group::2) and bp_flush (particles
+    collected in the FP32 staging volumes before they are added into the
+    FP64 volumes; 0: after every pass)."""
 
     def __init__(self, bundle, debug=False, **options):
         self.bundle = bundle

@@ -6,7 +6,8 @@ ctypes on the same raw particle images.  The façade only marshals: best pose,
 offsets, class and significant-sample count are bit-identical to the ctypes
 path's; PMAX, dLL, norm, the weighted sums and the backprojected volumes agree
 within the library's own run-to-run spread (atomic additions in the image
-preparation and in the sums: last bits; 1e-6 relative allowed)."""
+preparation and in the sums: last bits, 1e-6 relative allowed; FP32 staging of
+the volumes: 1e-5)."""
 import subprocess
 
 import numpy as np
@@ -139,6 +140,9 @@ def test_facade_matches_ctypes_path(facade_driver, tmp_path, precision):
     for k in ("sigma2_noise", "pdf_class", "pdf_direction", "sigma2_offset", "LL", "ave_Pmax", "avg_norm_correction",
               "sumw_group"):
         errs[k] = close(fws[k], ws[k], k, 1e-6)
-    errs["bp_data"] = close(vols[0][0].view(np.float64), bd.view(np.float64), "bp_data", 1e-6)
-    errs["bp_weight"] = close(vols[0][1], bw, "bp_weight", 1e-6)
+    # the volumes are summed in FP32 staging volumes (vector atomics, in an
+    # order that differs between runs) before they reach the FP64 volumes:
+    # ~1e-6 of the maximum between two runs; the oracle's tolerance applies
+    errs["bp_data"] = close(vols[0][0].view(np.float64), bd.view(np.float64), "bp_data", 1e-5)
+    errs["bp_weight"] = close(vols[0][1], bw, "bp_weight", 1e-5)
     print("relative difference to the ctypes path:", errs)
