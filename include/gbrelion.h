@@ -10,6 +10,13 @@
  * the last error of the calling thread is available from gbr_last_error().
  * No entry point takes or returns a PyTorch or C++ type.
  *
+ * Threads: like the reference's threads, each with its MlOptimiserCuda on
+ * one MlDeviceBundle, several threads may drive their own workers of one
+ * bundle at once.  Calls that run work on the bundle's shared state (E-step,
+ * image preparation, volumes, model arrays, reconstruction) hold a
+ * bundle-wide lock and are serialised; one worker is used by one thread at a
+ * time.
+ *
  * Layout conventions (FFTW half-transform, as in the reference):
  *   a 2D Fourier image of size s is stored row-major as [s][s/2+1]; row i
  *   holds frequency y = i for i <= s/2 and y = i - s otherwise.

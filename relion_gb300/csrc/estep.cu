@@ -19,6 +19,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -48,6 +49,8 @@ int fail(int status, const std::string &msg) {
             return fail(st_, std::string(#expr) + ": " + cudaGetErrorString(e_));          \
         }                                                                                  \
     } while (0)
+
+#define GBR_LOCK(bundle) std::lock_guard<std::recursive_mutex> lock_((bundle)->mu)
 
 template <class T>
 struct DevBuf {
@@ -134,6 +137,12 @@ enum Stage { ST_PREP = 0, ST_NORM, ST_CROSS, ST_WCOARSE, ST_SIG, ST_PROJF, ST_FI
 void gbr::set_error_text(const std::string &msg) { g_last_error = msg; }
 
 struct gbr_bundle {
+    // every call that runs work on the bundle's shared state (E-step,
+    // image preparation, volumes, model arrays) holds this lock, so workers
+    // of one bundle may be driven from several threads (as the reference's
+    // threads drive their MlOptimiserCuda on one MlDeviceBundle): their
+    // calls are serialised
+    std::recursive_mutex mu;
     gbr_model_desc d{};
     int device = 0;
     PoseGrid grid;
@@ -1306,6 +1315,7 @@ int gbr_bundle_create(const gbr_model_desc *desc, int device, gbr_bundle **out) 
 int gbr_projector_upload(gbr_bundle *b, int64_t iclass, const float *data, int64_t xdim, int64_t ydim,
                          int64_t zdim, int64_t yinit, int64_t zinit, int64_t r_max, int64_t padding_factor) {
     if (!b || !data || iclass < 0 || iclass >= b->K) return fail(GBR_ERR_INVALID, "bad class or data");
+    GBR_LOCK(b);
     if (xdim <= 1 || ydim <= 1 || padding_factor != b->d.padding_factor ||
         (b->is2d ? (zdim != 1 || zinit != 0) : zdim <= 1))
         return fail(GBR_ERR_INVALID, "bad projector dimensions");
@@ -1328,6 +1338,7 @@ int gbr_projector_upload(gbr_bundle *b, int64_t iclass, const float *data, int64
 int gbr_model_set_arrays(gbr_bundle *b, const double *sigma2_noise, const double *pdf_class,
                          const double *pdf_direction, const double *data_vs_prior) {
     if (!b || !sigma2_noise || !pdf_class || !pdf_direction) return fail(GBR_ERR_INVALID, "null array");
+    GBR_LOCK(b);
     if (b->d.do_scale_correction && !data_vs_prior)
         return fail(GBR_ERR_INVALID, "data_vs_prior needed with scale correction");
     b->sigma2.assign(sigma2_noise, sigma2_noise + b->d.sigma2_len);
@@ -1341,6 +1352,7 @@ int gbr_model_set_arrays(gbr_bundle *b, const double *sigma2_noise, const double
 
 int gbr_bundle_reserve(gbr_bundle *b, size_t bytes) {
     if (!b) return fail(GBR_ERR_INVALID, "null bundle");
+    GBR_LOCK(b);
     b->budget = bytes;
     return GBR_OK;
 }
@@ -1405,6 +1417,7 @@ int gbr_worker_set_option(gbr_worker *w, int option, int64_t value) {
 
 int gbr_expect_batch(gbr_worker *w, const gbr_particle_batch *batch, gbr_particle_result *res) {
     if (!w || !batch || !res || batch->n < 0) return fail(GBR_ERR_INVALID, "null argument");
+    GBR_LOCK(w->b);
     if (batch->n == 0) return GBR_OK;
     if (!batch->fimg || !batch->fimg_nomask || !batch->fctf || !batch->power_img || !batch->old_offset ||
         !batch->prior || !batch->highres_Xi2 || !batch->norm_correction || !batch->scale)
@@ -1476,6 +1489,7 @@ int gbr_orientation_blocks(const gbr_bundle *b, int64_t *nblocks, int64_t *dirs_
 int gbr_expect_batch_blocks(gbr_worker *w, const gbr_particle_batch *batch, const int32_t *blocks, int64_t m,
                             gbr_particle_result *res) {
     if (!w || !batch || !blocks || m <= 0) return fail(GBR_ERR_INVALID, "null argument or empty block lists");
+    GBR_LOCK(w->b);
     int s = restricted_supported(w->b);
     if (s) return s;
     w->restrict_blocks = blocks;
@@ -1488,6 +1502,7 @@ int gbr_expect_batch_blocks(gbr_worker *w, const gbr_particle_batch *batch, cons
 
 int gbr_bundle_set_optics(gbr_bundle *b, const gbr_optics_desc *optics) {
     if (!b || !optics) return fail(GBR_ERR_INVALID, "null argument");
+    GBR_LOCK(b);
     if (!(optics->kV > 0.) || optics->Q0 < 0. || optics->Q0 >= 1. || !(optics->particle_diameter > 0.) ||
         !(optics->width_mask_edge > 0.))
         return fail(GBR_ERR_INVALID, "invalid optics / mask parameters");
@@ -1601,6 +1616,7 @@ int gbr_prepare_images(gbr_worker *w, const gbr_image_batch *in, void *fimg, voi
                        double *power_img, double *highres_Xi2, double *old_offset_rounded) {
     if (!w || !in || !fimg || !fimg_nomask || !fctf || !power_img || !highres_Xi2 || !old_offset_rounded)
         return fail(GBR_ERR_INVALID, "null argument");
+    GBR_LOCK(w->b);
     GBR_CUDA(cudaSetDevice(w->b->device));
     int s = prepare_images(w, in, static_cast<float2 *>(fimg), static_cast<float2 *>(fimg_nomask), fctf, power_img,
                            highres_Xi2, old_offset_rounded);
@@ -1644,6 +1660,7 @@ int pump_stages(gbr_worker *w, cudaEvent_t after) {
 
 int gbr_stage_images(gbr_worker *w, const gbr_image_batch *in) {
     if (!w || !in || !in->images) return fail(GBR_ERR_INVALID, "null argument");
+    GBR_LOCK(w->b);
     if (in->device_resident) return fail(GBR_ERR_INVALID, "gbr_stage_images: host batches only");
     gbr_bundle *b = w->b;
     GBR_CUDA(cudaSetDevice(b->device));
@@ -1671,6 +1688,7 @@ int gbr_stage_images(gbr_worker *w, const gbr_image_batch *in) {
 
 int gbr_expect_images(gbr_worker *w, const gbr_image_batch *in, gbr_particle_result *res) {
     if (!w || !in || !res) return fail(GBR_ERR_INVALID, "null argument");
+    GBR_LOCK(w->b);
     if (in->n == 0) return GBR_OK;
     if (!in->prior || !in->scale) return fail(GBR_ERR_INVALID, "null image batch array");
     gbr_bundle *b = w->b;
@@ -1848,6 +1866,7 @@ int gbr_backprojector_dims(const gbr_bundle *b, int64_t *xdim, int64_t *ydim, in
 
 int gbr_backprojector_download(gbr_bundle *b, int64_t iclass, double *data, double *weight) {
     if (!b || iclass < 0 || iclass >= b->K) return fail(GBR_ERR_INVALID, "bad class");
+    GBR_LOCK(b);
     GBR_CUDA(cudaSetDevice(b->device));
     int s = flush_staged(b);
     if (s) return s;
@@ -1858,6 +1877,7 @@ int gbr_backprojector_download(gbr_bundle *b, int64_t iclass, double *data, doub
 
 int gbr_backprojector_upload(gbr_bundle *b, int64_t iclass, const double *data, const double *weight) {
     if (!b || !data || !weight || iclass < 0 || iclass >= b->K) return fail(GBR_ERR_INVALID, "bad class or data");
+    GBR_LOCK(b);
     GBR_CUDA(cudaSetDevice(b->device));
     int s = flush_staged(b);
     if (s) return s;
@@ -1878,6 +1898,8 @@ int recon_begin(gbr_bundle *b, int64_t iclass) {
 }  // namespace
 
 int gbr_recon_set_precision(gbr_bundle *b, int precision) {
+    if (!b) return fail(GBR_ERR_INVALID, "null bundle");
+    GBR_LOCK(b);
     int st = recon_begin(b, 0);
     if (st) return st;
     if (precision != GBR_RECON_FP64 && precision != GBR_RECON_FP32)
@@ -1887,6 +1909,8 @@ int gbr_recon_set_precision(gbr_bundle *b, int precision) {
 }
 
 int gbr_backprojector_symmetrise(gbr_bundle *b, int64_t iclass) {
+    if (!b) return fail(GBR_ERR_INVALID, "null bundle");
+    GBR_LOCK(b);
     int st = recon_begin(b, iclass);
     if (st) return st;
     return gbr::recon_symmetrise(b->bp_data[iclass].p, b->bp_weight[iclass].p, b->bg);
@@ -1895,6 +1919,8 @@ int gbr_backprojector_symmetrise(gbr_bundle *b, int64_t iclass) {
 int gbr_update_ssnr(gbr_bundle *b, int64_t iclass, double tau2_fudge, double *tau2_io, double *sigma2_out,
                     double *data_vs_prior_out, double *fourier_coverage_out, const double *fsc,
                     int update_tau2_with_fsc, int is_whole_instead_of_half) {
+    if (!b) return fail(GBR_ERR_INVALID, "null bundle");
+    GBR_LOCK(b);
     int st = recon_begin(b, iclass);
     if (st) return st;
     if (!tau2_io || (update_tau2_with_fsc && !fsc)) return fail(GBR_ERR_INVALID, "null tau2 / fsc");
@@ -1904,6 +1930,8 @@ int gbr_update_ssnr(gbr_bundle *b, int64_t iclass, double tau2_fudge, double *ta
 }
 
 int gbr_reconstruct(gbr_bundle *b, int64_t iclass, const gbr_recon_params *p, const double *tau2, double *vol_out) {
+    if (!b) return fail(GBR_ERR_INVALID, "null bundle");
+    GBR_LOCK(b);
     int st = recon_begin(b, iclass);
     if (st) return st;
     if (!p) return fail(GBR_ERR_INVALID, "null argument");
@@ -1915,6 +1943,8 @@ int gbr_reconstruct(gbr_bundle *b, int64_t iclass, const gbr_recon_params *p, co
 
 int gbr_projector_from_map(gbr_bundle *b, int64_t iclass, const double *vol, int64_t current_size,
                            int do_gridding, int64_t min_ires, double *power_spectrum) {
+    if (!b) return fail(GBR_ERR_INVALID, "null bundle");
+    GBR_LOCK(b);
     int st = recon_begin(b, iclass);
     if (st) return st;
     const int dim = b->is2d ? 2 : 3;
@@ -1936,6 +1966,7 @@ int gbr_projector_from_map(gbr_bundle *b, int64_t iclass, const double *vol, int
 
 int gbr_projector_download(gbr_bundle *b, int64_t iclass, float *data, int64_t *dims) {
     if (!b || !dims || iclass < 0 || iclass >= b->K) return fail(GBR_ERR_INVALID, "bad class");
+    GBR_LOCK(b);
     if (!b->have_vol[iclass]) return fail(GBR_ERR_STATE, "no projector for this class");
     const gbr::VolGeom &g = b->pg;
     const int64_t v[7] = {g.xdim, g.ydim, g.zdim, g.yinit, g.zinit, g.r_max, g.pad};
@@ -1950,6 +1981,8 @@ int gbr_projector_download(gbr_bundle *b, int64_t iclass, float *data, int64_t *
 }
 
 int gbr_fsc(gbr_bundle *b, const double *map1, const double *map2, double *fsc) {
+    if (!b) return fail(GBR_ERR_INVALID, "null bundle");
+    GBR_LOCK(b);
     int st = recon_begin(b, 0);
     if (st) return st;
     if (!map1 || !map2 || !fsc) return fail(GBR_ERR_INVALID, "null argument");
@@ -1958,6 +1991,7 @@ int gbr_fsc(gbr_bundle *b, const double *map1, const double *map2, double *fsc) 
 
 int gbr_wsum_download(gbr_bundle *b, gbr_wsum *out) {
     if (!b || !out) return fail(GBR_ERR_INVALID, "null argument");
+    GBR_LOCK(b);
     GBR_CUDA(cudaSetDevice(b->device));
     GBR_CUDA(cudaDeviceSynchronize());
     if (out->sigma2_noise)
@@ -1984,6 +2018,7 @@ int gbr_wsum_download(gbr_bundle *b, gbr_wsum *out) {
 
 int gbr_wsum_download_class_offsets(gbr_bundle *b, double *out) {
     if (!b || !out) return fail(GBR_ERR_INVALID, "null argument");
+    GBR_LOCK(b);
     if (!b->is2d) return fail(GBR_ERR_STATE, "class offset priors exist only for 2D classification");
     GBR_CUDA(cudaSetDevice(b->device));
     GBR_CUDA(cudaDeviceSynchronize());
@@ -1995,6 +2030,7 @@ int gbr_wsum_download_class_offsets(gbr_bundle *b, double *out) {
 
 int gbr_model_set_class_offsets(gbr_bundle *b, const double *prior_offset_class) {
     if (!b || !prior_offset_class) return fail(GBR_ERR_INVALID, "null argument");
+    GBR_LOCK(b);
     if (!b->is2d) return fail(GBR_ERR_STATE, "class offset priors exist only for 2D classification");
     GBR_CUDA(cudaSetDevice(b->device));
     b->class_prior_h.assign(prior_offset_class, prior_offset_class + 2 * b->K);
@@ -2004,6 +2040,7 @@ int gbr_model_set_class_offsets(gbr_bundle *b, const double *prior_offset_class)
 
 int gbr_bundle_reset_wsum(gbr_bundle *b) {
     if (!b) return fail(GBR_ERR_INVALID, "null bundle");
+    GBR_LOCK(b);
     GBR_CUDA(cudaSetDevice(b->device));
     GBR_CUDA(cudaDeviceSynchronize());
     for (long k = 0; k < b->K; ++k) {
