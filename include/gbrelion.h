@@ -189,11 +189,16 @@ typedef enum {
                                  an L2 keep policy (default 0)                        */
     GBR_OPT_PAIR = 9,         /* precision form: 1 runs the coarse cross term on SM
                                  pairs (tcgen05 cta_group::2; default 0)             */
-    GBR_OPT_BP_FLUSH = 10     /* particles collected in the FP32 staging volumes
+    GBR_OPT_BP_FLUSH = 10,    /* particles collected in the FP32 staging volumes
                                  before they are added into the FP64 volumes
                                  (default 2048; 0: after every pass).  Reading,
                                  replacing or reconstructing the volumes flushes
                                  first.                                               */
+    GBR_OPT_GRAPH = 11        /* 1 (default): the coarse part of a pass (up to the
+                                 read-back of the fine job lists) is captured as
+                                 a CUDA graph on the second pass of a batch size
+                                 and replayed while buffers, model and settings
+                                 are unchanged; 0: always launched directly      */
 } gbr_worker_option;
 int gbr_worker_set_option(gbr_worker *w, int option, int64_t value);
 
@@ -429,6 +434,11 @@ int gbr_worker_stage_times(const gbr_worker *w, double *ms, int64_t n, int64_t *
 
 /* Number of CUDA kernels this worker has launched (all batches so far). */
 int gbr_worker_launch_count(const gbr_worker *w, int64_t *count);
+
+/* CUDA graphs of the worker's coarse segment (GBR_OPT_GRAPH): how many were
+ * captured and how many passes replayed one.  No counterpart in the
+ * reference. */
+int gbr_worker_graph_stats(const gbr_worker *w, int64_t *captures, int64_t *replays);
 
 /* Measured FP32 FMA throughput of the device (TFLOP/s, register-resident
  * FMA chains on every SM): the roofline peak of the FP32 SIMT kernels.

@@ -138,6 +138,7 @@ EXPORTS = {
     "gbr_bundle_reset_wsum": (C.c_int, [P]),
     "gbr_worker_stage_times": (C.c_int, [P, P, I64, C.POINTER(I64)]),
     "gbr_worker_launch_count": (C.c_int, [P, C.POINTER(I64)]),
+    "gbr_worker_graph_stats": (C.c_int, [P, C.POINTER(I64), C.POINTER(I64)]),
     "gbr_measure_fp32_peak": (C.c_int, [C.c_int, C.POINTER(F64)]),
     "gbr_significance_threshold_noalloc": (C.c_int, [P, I64, I64, F64, P, P, P]),
     "gbr_worker_destroy": (C.c_int, [P]),

@@ -20,6 +20,7 @@
 #include <cstring>
 #include <memory>
 #include <mutex>
+#include <atomic>
 #include <string>
 #include <vector>
 
@@ -52,6 +53,15 @@ int fail(int status, const std::string &msg) {
 
 #define GBR_LOCK(bundle) std::lock_guard<std::recursive_mutex> lock_((bundle)->mu)
 
+// Keys of the CUDA graph of a worker's coarse segment (run_coarse): a graph
+// replays only while the kernels' pointers and by-value arguments are the
+// captured ones.  g_api_gen is bumped by every call that changes model,
+// tables, optics or worker settings; g_alloc_count by every (re)allocation
+// or release of a device or pinned buffer (a segment run that allocated is
+// not captured on its next call).
+std::atomic<unsigned long long> g_api_gen{0};
+std::atomic<unsigned long long> g_alloc_count{0};
+
 template <class T>
 struct DevBuf {
     T *p = nullptr;
@@ -65,7 +75,10 @@ struct DevBuf {
     }
     ~DevBuf() { release(); }
     void release() {
-        if (p) cudaFree(p);
+        if (p) {
+            cudaFree(p);
+            ++g_alloc_count;
+        }
         p = nullptr;
         n = 0;
     }
@@ -76,6 +89,7 @@ struct DevBuf {
         size_t bytes = std::max<size_t>(m, 1) * sizeof(T);
         cudaError_t e = cudaMalloc(&p, bytes);
         if (e == cudaSuccess) n = std::max<size_t>(m, 1);
+        ++g_alloc_count;
         return e;
     }
     cudaError_t upload(const T *h, size_t m) {
@@ -96,7 +110,10 @@ struct PinnedBuf {
     PinnedBuf &operator=(const PinnedBuf &) = delete;
     ~PinnedBuf() { release(); }
     void release() {
-        if (p) cudaFreeHost(p);
+        if (p) {
+            cudaFreeHost(p);
+            ++g_alloc_count;
+        }
         p = nullptr;
         n = 0;
     }
@@ -104,6 +121,7 @@ struct PinnedBuf {
         if (m <= n && p) return cudaSuccess;
         release();
         void *q = nullptr;
+        ++g_alloc_count;
         cudaError_t e = cudaMallocHost(&q, std::max<size_t>(m, 1) * sizeof(T));
         if (e == cudaSuccess) {
             p = static_cast<T *>(q);
@@ -310,6 +328,17 @@ struct gbr_worker {
     DevBuf<unsigned char> ytp;  // per-particle BF16 Y tiles of the restricted pass
     int batch_cap = 0;           // particles per pass (GBR_OPT_BATCH_CAP; 0 = from the budget)
     int bp_flush = kBpFlushDefault;  // flush the staging volumes at this many particles (GBR_OPT_BP_FLUSH)
+    // CUDA graph of the coarse segment (run_coarse; GBR_OPT_GRAPH)
+    int use_graph = 1;
+    cudaGraphExec_t gexec = nullptr;
+    unsigned long long buf_gen = 0;  // bumped when the worker's batch buffers are reallocated
+    struct GraphKey {
+        int n = -1;
+        unsigned long long api = 0, buf = 0;
+        bool operator==(const GraphKey &o) const { return n == o.n && api == o.api && buf == o.buf; }
+    } g_key, warm_key;
+    int g_launches = 0;
+    long long g_captures = 0, g_replays = 0;
     TcTuning tc_tune;            // GBR_OPT_TILE_GROUP, GBR_OPT_KEEP_A, GBR_OPT_PAIR
     int pass_cap = 0;            // particles per pass of the current call
     // debug copies of the last call, one entry per pass (gbr_worker_debug_fetch)
@@ -410,6 +439,7 @@ unsigned long long circle_mask(const std::vector<PixelRef> &px, const std::vecto
 
 int build_tables(gbr_bundle *b) {
     if (b->tables_ready) return GBR_OK;
+    ++g_api_gen;
     b->blk_ready = false;
     if (!b->have_arrays) return fail(GBR_ERR_STATE, "model arrays not set (gbr_model_set_arrays)");
     for (long k = 0; k < b->K; ++k)
@@ -619,6 +649,7 @@ int build_tables(gbr_bundle *b) {
 int ensure_capacity(gbr_worker *w, int n) {
     gbr_bundle *b = w->b;
     if (n <= w->cap) return GBR_OK;
+    ++w->buf_gen;
     const size_t full = (size_t)b->full_npix;
     GBR_CUDA(w->X.reserve(n * full));
     GBR_CUDA(w->Xn.reserve(n * full));
@@ -917,14 +948,80 @@ int flush_staged(gbr_bundle *b) {
     return GBR_OK;
 }
 
-int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h, gbr_particle_result *res) {
+// Host-side choices of a coarse pass (no device work): the restricted form,
+// row skip, sparse diff2 writes, the candidate-list capacity.
+struct CoarseFlags {
+    bool restricted = false, use_rowmin = false, sparse = false;
+    int cap = 0;
+    long long nbj = 0;
+};
+
+CoarseFlags coarse_flags(gbr_worker *w, int n) {
+    gbr_bundle *b = w->b;
+    const gbr_model_desc &d = b->d;
+    const int R = (int)b->R, T = (int)b->T;
+    const long long RT = (long long)R * T;
+    CoarseFlags cf;
+    // a pass whose particles all fall back to the exhaustive search runs the
+    // exhaustive kernel (no work-item list)
+    cf.restricted = w->restrict_blocks != nullptr;
+    if (cf.restricted) {
+        bool all = true;
+        for (int p = 0; p < n && all; ++p)
+            all = w->restrict_blocks[(size_t)(w->pass_p0 + p) * w->restrict_m] == GBR_ALL_BLOCKS;
+        if (all) cf.restricted = false;
+        w->last_items = all ? (long long)n * (R / (kDirsPerBlock * (int)b->NP)) : 0;
+    }
+    cf.use_rowmin = d.precision == GBR_PREC_BF16 && (cf.restricted || (T >= 32 && w->coarse_rows == 0));
+    // sparse diff2 writes: only row segments near the running minimum are
+    // stored (the debug read-back reports the others as not computed); the
+    // restricted pass stores the rows of the blocks it scores
+    cf.sparse = cf.use_rowmin && (cf.restricted || T <= 960);
+    cf.cap = (int)std::min<long long>(RT, w->cand_cap_max);
+    cf.nbj = fine_jobs_nblocks((long long)n * R);
+    return cf;
+}
+
+// Event record that stream capture turns into an event node of the graph,
+// so that the stage times stay measurable when the graph is replayed.
+cudaError_t record(cudaEvent_t ev, cudaStream_t st) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaError_t e = cudaStreamIsCapturing(st, &cs);
+    if (e != cudaSuccess) return e;
+    return cs == cudaStreamCaptureStatusActive ? cudaEventRecordWithFlags(ev, st, cudaEventRecordExternal)
+                                               : cudaEventRecord(ev, st);
+}
+
+// Fine-pass job lists from the significance counts, and their read-back
+// (with the tensor-core pipeline's error flag on the first try).
+int jobs_readback(gbr_worker *w, int n, long long nbj, bool tc_check) {
+    gbr_bundle *b = w->b;
+    cudaStream_t st = w->st;
+    const int R = (int)b->R;
+    GBR_CUDA(record(w->ev[4], st));
+    GBR_CUDA(cudaMemsetAsync(w->need_r.p, 0, R, st));
+    GBR_CUDA(launch_fine_jobs(w->cnt.p, n, R, (int)(b->nOR * b->nOT), w->scan_tmp.p, w->jobs.p, w->seg_f.p,
+                              w->need_r.p, st));
+    GBR_CUDA(cudaMemcpyAsync(w->h_totals.p, w->scan_tmp.p + 2 * nbj, sizeof(long long) * 2, cudaMemcpyDeviceToHost,
+                             st));
+    GBR_CUDA(cudaMemcpyAsync(w->h_segf.p, w->seg_f.p, sizeof(long long) * (n + 1), cudaMemcpyDeviceToHost, st));
+    if (tc_check) GBR_CUDA(tc_error_flag_async(w->h_tcflag.p, st));
+    w->launches += 3;
+    return GBR_OK;
+}
+
+// The coarse pass of a batch up to the read-back of its fine job lists:
+// preparation, norms, cross term, weights, significance, job lists.  It
+// holds no host synchronisation, which makes it the part of a call that is
+// captured as a CUDA graph and replayed (run_coarse).
+int coarse_segment(gbr_worker *w, int n, const CoarseFlags &cf) {
     gbr_bundle *b = w->b;
     const gbr_model_desc &d = b->d;
     cudaStream_t st = w->st;
     const int R = (int)b->R, T = (int)b->T, nOR = (int)b->nOR, nOT = (int)b->nOT;
     const int W = (T + 31) / 32;
     const long long RT = (long long)R * T;
-    GBR_CUDA(cudaEventRecord(w->ev[0], st));
+    GBR_CUDA(record(w->ev[0], st));
     // ---- prep ----
     GBR_CUDA(launch_prep(w->X.p, w->C.p, w->pdat.p, n, b->full_npix, b->pc.p, b->nc, b->minv_c.p, b->ldk_c,
                          b->pf.p, b->nf, b->ldk_f, b->minv_f.p, w->a_c.p, w->b_c.p, w->a_f.p, w->b_f.p, w->Xf.p,
@@ -938,7 +1035,7 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
                                log_rt_orient, w->ps.p, b->KP, b->is2d ? b->class_prior.p : nullptr, st));
     GBR_CUDA(cudaMemsetAsync(w->shell.p, 0, sizeof(double) * n * b->nshell, st));
     GBR_CUDA(cudaMemsetAsync(w->pacc.p, 0, sizeof(double) * n * 8, st));
-    GBR_CUDA(cudaEventRecord(w->ev[1], st));
+    GBR_CUDA(record(w->ev[1], st));
     // ---- coarse norm and cross GEMMs ----
     if (d.precision == GBR_PREC_BF16) {
         // tensor cores, TF32 three-term split (FP32-level accuracy)
@@ -949,22 +1046,8 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
         GBR_CUDA(launch_gemm_rows(b->proj2_c.p, b->ldk_c, R, w->a_c.p, b->ldk_c, n, b->ldk_c, w->nrm.p, R, 1, st));
         w->launches += 3;  // prep, pdf_offset, norms
     }
-    GBR_CUDA(cudaEventRecord(w->ev[2], st));
-    // a pass whose particles all fall back to the exhaustive search runs the
-    // exhaustive kernel (no work-item list)
-    bool restricted = w->restrict_blocks != nullptr;
-    if (restricted) {
-        bool all = true;
-        for (int p = 0; p < n && all; ++p)
-            all = w->restrict_blocks[(size_t)(w->pass_p0 + p) * w->restrict_m] == GBR_ALL_BLOCKS;
-        if (all) restricted = false;
-        w->last_items = all ? (long long)n * (R / (kDirsPerBlock * (int)b->NP)) : 0;
-    }
-    const bool use_rowmin = d.precision == GBR_PREC_BF16 && (restricted || (T >= 32 && w->coarse_rows == 0));
-    // sparse diff2 writes: only row segments near the running minimum are
-    // stored (the debug read-back reports the others as not computed); the
-    // restricted pass stores the rows of the blocks it scores
-    const bool sparse = use_rowmin && (restricted || T <= 960);
+    GBR_CUDA(record(w->ev[2], st));
+    const bool restricted = cf.restricted, use_rowmin = cf.use_rowmin, sparse = cf.sparse;
     if (w->debug) {
         w->dbg.emplace_back();
         w->dbg.back().n = n;
@@ -993,7 +1076,7 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
                                    n, T, w->vals.p, w->nrm.p, b->pdf_orient.p, nullptr, 1, 1, W, w->ps.p, 0, st));
         w->launches += 1;
     }
-    GBR_CUDA(cudaEventRecord(w->ev[3], st));
+    GBR_CUDA(record(w->ev[3], st));
     if (w->debug) {
         gbr_worker::DbgPass &D = w->dbg.back();
         D.coarse.resize((size_t)n * RT);
@@ -1007,7 +1090,7 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
     // ---- coarse weights and significance ----
     // one read of the diff2 array: weights, FP64 sums and the candidate lists;
     // the threshold search and the significance masks then run on the lists
-    const int cap = (int)std::min<long long>(RT, w->cand_cap_max);
+    const int cap = cf.cap;
     if (w->cand_cap < cap || w->cand_idx.n < (size_t)n * cap) {
         GBR_CUDA(w->cand_idx.reserve((size_t)n * cap));
         GBR_CUDA(w->cand_w.reserve((size_t)n * cap));
@@ -1047,26 +1130,82 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
         D.wcoarse.resize((size_t)n * RT);
         GBR_CUDA(cudaMemcpyAsync(D.wcoarse.data(), dense_w, sizeof(float) * n * RT, cudaMemcpyDeviceToHost, st));
     }
-    const long long nR = (long long)n * R;
-    const long long nbj = fine_jobs_nblocks(nR);
-    for (int attempt = 0;; ++attempt) {
-        GBR_CUDA(cudaEventRecord(w->ev[4], st));
-        GBR_CUDA(cudaMemsetAsync(w->need_r.p, 0, R, st));
-        GBR_CUDA(launch_fine_jobs(w->cnt.p, n, R, nOR * nOT, w->scan_tmp.p, w->jobs.p, w->seg_f.p, w->need_r.p, st));
-        GBR_CUDA(cudaMemcpyAsync(w->h_totals.p, w->scan_tmp.p + 2 * nbj, sizeof(long long) * 2, cudaMemcpyDeviceToHost,
-                                 st));
-        GBR_CUDA(cudaMemcpyAsync(w->h_segf.p, w->seg_f.p, sizeof(long long) * (n + 1), cudaMemcpyDeviceToHost, st));
-        const bool tc_check = attempt == 0 && d.precision == GBR_PREC_BF16;
-        if (tc_check) GBR_CUDA(tc_error_flag_async(w->h_tcflag.p, st));
-        GBR_CUDA(cudaStreamSynchronize(st));
-        w->launches += 3;
-        if (tc_check && w->h_tcflag.p[0])
-            return fail(GBR_ERR_CUDA, "tensor-core pipeline timed out waiting for its MMAs");
-        if (attempt > 0) break;
-        unsigned int cmax = 0;
-        for (int p = 0; p < n; ++p) cmax = std::max(cmax, w->h_ccnt.p[p]);
-        if (cmax <= (unsigned int)cap) break;
-        // a list overflowed: significance from the full weight array
+    return jobs_readback(w, n, cf.nbj, d.precision == GBR_PREC_BF16);
+}
+
+// Runs coarse_segment directly, or captured as a CUDA graph, or replays the
+// captured graph.  A pass of the same batch size as a previous direct pass
+// that allocated nothing, with no model, table, option or buffer change
+// since (the graph key), is captured; later such passes replay the graph.
+// Debug read-backs and the restricted pass (host-built work items) always
+// run directly.
+int run_coarse(gbr_worker *w, int n, const CoarseFlags &cf) {
+    const bool graphable = w->use_graph && !w->debug && !cf.restricted;
+    gbr_worker::GraphKey key;
+    key.n = n;
+    key.api = g_api_gen.load();
+    key.buf = w->buf_gen;
+    if (graphable && w->gexec && w->g_key == key) {
+        GBR_CUDA(cudaGraphLaunch(w->gexec, w->st));
+        w->launches += w->g_launches;
+        ++w->g_replays;
+        return GBR_OK;
+    }
+    if (!graphable || !(w->warm_key == key)) {
+        const unsigned long long a0 = g_alloc_count.load();
+        const int s = coarse_segment(w, n, cf);
+        if (g_alloc_count.load() != a0) ++w->buf_gen;  // the segment (re)allocated: not yet stable
+        w->warm_key = key;
+        w->warm_key.buf = w->buf_gen;
+        return s;
+    }
+    // capture: nothing runs until the graph is launched; an allocation in
+    // the segment ends the capture with an error (thread-local capture mode)
+    const int l0 = w->launches;
+    GBR_CUDA(cudaStreamBeginCapture(w->st, cudaStreamCaptureModeThreadLocal));
+    const int s = coarse_segment(w, n, cf);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(w->st, &g);
+    cudaGraphExec_t ex = nullptr;
+    if (s == GBR_OK && e == cudaSuccess && g)
+        e = cudaGraphInstantiate(&ex, g, 0);
+    else if (e == cudaSuccess)
+        e = cudaErrorStreamCaptureInvalidated;
+    if (g) cudaGraphDestroy(g);
+    if (e != cudaSuccess || !ex) {
+        // not capturable this time: run directly
+        (void)cudaGetLastError();
+        w->launches = l0;
+        w->warm_key = gbr_worker::GraphKey();
+        return coarse_segment(w, n, cf);
+    }
+    if (w->gexec) cudaGraphExecDestroy(w->gexec);
+    w->gexec = ex;
+    w->g_key = key;
+    w->g_launches = w->launches - l0;
+    ++w->g_captures;
+    GBR_CUDA(cudaGraphLaunch(ex, w->st));
+    return GBR_OK;
+}
+
+int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h, gbr_particle_result *res) {
+    gbr_bundle *b = w->b;
+    const gbr_model_desc &d = b->d;
+    cudaStream_t st = w->st;
+    const int R = (int)b->R, T = (int)b->T, nOR = (int)b->nOR, nOT = (int)b->nOT;
+    const int W = (T + 31) / 32;
+    const long long RT = (long long)R * T;
+    const CoarseFlags cf = coarse_flags(w, n);
+    int s = run_coarse(w, n, cf);
+    if (s) return s;
+    GBR_CUDA(cudaStreamSynchronize(st));
+    if (d.precision == GBR_PREC_BF16 && w->h_tcflag.p[0])
+        return fail(GBR_ERR_CUDA, "tensor-core pipeline timed out waiting for its MMAs");
+    unsigned int cmax = 0;
+    for (int p = 0; p < n; ++p) cmax = std::max(cmax, w->h_ccnt.p[p]);
+    if (cmax > (unsigned int)cf.cap) {
+        // a candidate list overflowed: significance from the full weight array
+        unsigned int *segmask = cf.sparse ? w->segmask.p : nullptr;
         GBR_CUDA(launch_weights(w->vals.p, w->seg_c.p, n, RT, 1, T, nullptr, nullptr, nullptr, nOR, nOT,
                                 b->pdf_orient.p, w->pdf_off.p, w->ps.p, w->hist.p, st, 0, b->KP, (int)(b->ND * b->NP),
                                 segmask));
@@ -1074,6 +1213,9 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
         if (s) return s;
         GBR_CUDA(launch_sig_masks(w->vals.p, n, R, T, W, w->ps.p, w->mask.p, w->cnt.p, st));
         w->launches += 2;
+        s = jobs_readback(w, n, cf.nbj, false);
+        if (s) return s;
+        GBR_CUDA(cudaStreamSynchronize(st));
     }
     const long long njobs = w->h_totals.p[0], nfine = w->h_totals.p[1];
     const std::vector<long long> segf(w->h_segf.p, w->h_segf.p + n + 1);
@@ -1316,6 +1458,7 @@ int gbr_projector_upload(gbr_bundle *b, int64_t iclass, const float *data, int64
                          int64_t zdim, int64_t yinit, int64_t zinit, int64_t r_max, int64_t padding_factor) {
     if (!b || !data || iclass < 0 || iclass >= b->K) return fail(GBR_ERR_INVALID, "bad class or data");
     GBR_LOCK(b);
+    ++g_api_gen;
     if (xdim <= 1 || ydim <= 1 || padding_factor != b->d.padding_factor ||
         (b->is2d ? (zdim != 1 || zinit != 0) : zdim <= 1))
         return fail(GBR_ERR_INVALID, "bad projector dimensions");
@@ -1339,6 +1482,7 @@ int gbr_model_set_arrays(gbr_bundle *b, const double *sigma2_noise, const double
                          const double *pdf_direction, const double *data_vs_prior) {
     if (!b || !sigma2_noise || !pdf_class || !pdf_direction) return fail(GBR_ERR_INVALID, "null array");
     GBR_LOCK(b);
+    ++g_api_gen;
     if (b->d.do_scale_correction && !data_vs_prior)
         return fail(GBR_ERR_INVALID, "data_vs_prior needed with scale correction");
     b->sigma2.assign(sigma2_noise, sigma2_noise + b->d.sigma2_len);
@@ -1353,6 +1497,7 @@ int gbr_model_set_arrays(gbr_bundle *b, const double *sigma2_noise, const double
 int gbr_bundle_reserve(gbr_bundle *b, size_t bytes) {
     if (!b) return fail(GBR_ERR_INVALID, "null bundle");
     GBR_LOCK(b);
+    ++g_api_gen;
     b->budget = bytes;
     return GBR_OK;
 }
@@ -1380,12 +1525,14 @@ int gbr_worker_create(gbr_bundle *b, gbr_worker **out) {
 
 int gbr_worker_set_debug(gbr_worker *w, int on) {
     if (!w) return fail(GBR_ERR_INVALID, "null worker");
+    ++g_api_gen;
     w->debug = on ? 1 : 0;
     return GBR_OK;
 }
 
 int gbr_worker_set_option(gbr_worker *w, int option, int64_t value) {
     if (!w) return fail(GBR_ERR_INVALID, "null worker");
+    ++g_api_gen;
     if (value < 0 || value > (1LL << 30)) return fail(GBR_ERR_INVALID, "option value out of range");
     switch (option) {
         case GBR_OPT_DEBUG: w->debug = value ? 1 : 0; break;
@@ -1410,6 +1557,10 @@ int gbr_worker_set_option(gbr_worker *w, int option, int64_t value) {
             w->tc_tune.pair = (int)value;
             break;
         case GBR_OPT_BP_FLUSH: w->bp_flush = (int)value; break;
+        case GBR_OPT_GRAPH:
+            if (value > 1) return fail(GBR_ERR_INVALID, "graph must be 0 or 1");
+            w->use_graph = (int)value;
+            break;
         default: return fail(GBR_ERR_INVALID, "unknown worker option " + std::to_string(option));
     }
     return GBR_OK;
@@ -1503,6 +1654,7 @@ int gbr_expect_batch_blocks(gbr_worker *w, const gbr_particle_batch *batch, cons
 int gbr_bundle_set_optics(gbr_bundle *b, const gbr_optics_desc *optics) {
     if (!b || !optics) return fail(GBR_ERR_INVALID, "null argument");
     GBR_LOCK(b);
+    ++g_api_gen;
     if (!(optics->kV > 0.) || optics->Q0 < 0. || optics->Q0 >= 1. || !(optics->particle_diameter > 0.) ||
         !(optics->width_mask_edge > 0.))
         return fail(GBR_ERR_INVALID, "invalid optics / mask parameters");
@@ -1945,6 +2097,7 @@ int gbr_projector_from_map(gbr_bundle *b, int64_t iclass, const double *vol, int
                            int do_gridding, int64_t min_ires, double *power_spectrum) {
     if (!b) return fail(GBR_ERR_INVALID, "null bundle");
     GBR_LOCK(b);
+    ++g_api_gen;
     int st = recon_begin(b, iclass);
     if (st) return st;
     const int dim = b->is2d ? 2 : 3;
@@ -2031,6 +2184,7 @@ int gbr_wsum_download_class_offsets(gbr_bundle *b, double *out) {
 int gbr_model_set_class_offsets(gbr_bundle *b, const double *prior_offset_class) {
     if (!b || !prior_offset_class) return fail(GBR_ERR_INVALID, "null argument");
     GBR_LOCK(b);
+    ++g_api_gen;
     if (!b->is2d) return fail(GBR_ERR_STATE, "class offset priors exist only for 2D classification");
     GBR_CUDA(cudaSetDevice(b->device));
     b->class_prior_h.assign(prior_offset_class, prior_offset_class + 2 * b->K);
@@ -2072,6 +2226,13 @@ int gbr_worker_launch_count(const gbr_worker *w, int64_t *count) {
     return GBR_OK;
 }
 
+int gbr_worker_graph_stats(const gbr_worker *w, int64_t *captures, int64_t *replays) {
+    if (!w) return fail(GBR_ERR_INVALID, "null worker");
+    if (captures) *captures = w->g_captures;
+    if (replays) *replays = w->g_replays;
+    return GBR_OK;
+}
+
 int gbr_measure_fp32_peak(int device, double *tflops) {
     if (!tflops) return fail(GBR_ERR_INVALID, "null argument");
     GBR_CUDA(cudaSetDevice(device));
@@ -2101,6 +2262,7 @@ int gbr_worker_destroy(gbr_worker *w) {
     }
     if (w->st_copy) cudaStreamDestroy(w->st_copy);
     if (w->fft_plan >= 0) destroy_fft_plan(w->fft_plan);
+    if (w->gexec) cudaGraphExecDestroy(w->gexec);
     if (w->st) cudaStreamDestroy(w->st);
     delete w;
     return GBR_OK;

@@ -208,7 +208,7 @@ ALL_BLOCKS = -2
 
 # gbr_worker_set_option selectors (include/gbrelion.h, gbr_worker_option)
 WORKER_OPTIONS = dict(debug=1, fine_mode=2, coarse_rows=3, cand_cap=4, cand_buf=5, batch_cap=6, tile_group=7,
-                      keep_a=8, pair=9, bp_flush=10)
+                      keep_a=8, pair=9, bp_flush=10, graph=11)
 FINE_MODES = dict(auto=0, dense=1, sparse=2)
 COARSE_ROWS = dict(skip=0, full=1)
 
@@ -223,7 +223,9 @@ class MlOptimiserCuda:
     projection tiles read with an L2 keep policy), pair (1: the coarse
     cross term on SM pairs, tcgen05 cta_group::2) and bp_flush (particles
     collected in the FP32 staging volumes before they are added into the
-    FP64 volumes; 0: after every pass)."""
+    FP64 volumes; 0: after every pass) and graph (1, default: the coarse
+    segment of a pass captured as a CUDA graph and replayed; 0: launched
+    directly)."""
 
     def __init__(self, bundle, debug=False, **options):
         self.bundle = bundle
@@ -366,6 +368,12 @@ class MlOptimiserCuda:
         n = C.c_int64()
         check(self.lib.gbr_worker_launch_count(self.h, C.byref(n)))
         return n.value
+
+    def graph_stats(self):
+        """(captures, replays) of the coarse segment's CUDA graph."""
+        c, r = C.c_int64(), C.c_int64()
+        check(self.lib.gbr_worker_graph_stats(self.h, C.byref(c), C.byref(r)))
+        return c.value, r.value
 
     def close(self):
         if self.h:
