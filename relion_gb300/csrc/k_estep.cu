@@ -943,21 +943,43 @@ __global__ void __launch_bounds__(kJobsThreads) k_jobs_emit(const int *__restric
 // translation t with its oversampled shifts iot:
 //   diff2 - c_fine = N_ior - 2 sum_k Re(Q_ior,k conj(E_(t,iot),k)),
 //   Q = P_(r,ior) conj(m C X),  N_ior = sum_k m C^2 |P|^2.
-// Q is staged in shared memory per pixel chunk; one warp per (t, iot) row.
+// Q is staged in shared memory per pixel chunk.  A warp takes kFineRows
+// rows (t, iot) at a time: each Q value read from shared memory serves
+// kFineRows rows (shared-memory reads, not FMAs, bounded the one-row form),
+// and the warp's 32 partial sums (kFineRows rows x 8 orientations) are
+// reduced across the lanes in one 31-shuffle transpose-reduction.
 // Entries are written in hidden-index order (t, ior, iot) within the job.
 // ---------------------------------------------------------------------------
 constexpr int kFineChunk = 512;
 constexpr int kFineThreads = 256;
+constexpr int kFineRows = 4;  // rows per warp pass; kFineRows x 8 orientations = 32 lanes
 
-__global__ void __launch_bounds__(kFineThreads)
+// v[i] summed over the warp's lanes, the sum of index i left on lane i
+// (recursive halving: at offset o each lane keeps the half whose index bit
+// equals its own lane bit and adds the partner's copy of it).
+__device__ __forceinline__ float warp_transpose_sum32(float (&v)[32], int lane) {
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) {
+        const bool upper = (lane & o) != 0;
+#pragma unroll
+        for (int i = 0; i < o; ++i) {
+            const float send = upper ? v[i] : v[i + o];
+            const float keep = upper ? v[i + o] : v[i];
+            v[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+        }
+    }
+    return v[0];
+}
+
+__global__ void __launch_bounds__(kFineThreads, 4)
 k_fine_diff2(const FineJob *__restrict__ jobs, const unsigned int *__restrict__ mask, int R, int T,
              int W, int nOR, int nOT, const float2 *__restrict__ projf, int ldpf, const float2 *__restrict__ b_f,
              const float *__restrict__ a_f, int nf, const float2 *__restrict__ phase_f,
              float *__restrict__ d, int *__restrict__ ejob, unsigned int *__restrict__ ecode,
              ParticleState *__restrict__ ps) {
     extern __shared__ float4 fsm[];
-    float2 *Q = reinterpret_cast<float2 *>(fsm);                   // [nOR][kFineChunk]
-    float *acc = reinterpret_cast<float *>(Q + nOR * kFineChunk);  // [rows][nOR]
+    float2 *Q = reinterpret_cast<float2 *>(fsm);                   // [8][kFineChunk]
+    float *acc = reinterpret_cast<float *>(Q + 8 * kFineChunk);    // [rows][nOR]
     int *tlist = reinterpret_cast<int *>(acc + T * nOT * nOR);     // [T]
     float *norm = reinterpret_cast<float *>(tlist + T);            // [nOR]
     __shared__ unsigned int smin;
@@ -981,6 +1003,8 @@ k_fine_diff2(const FineJob *__restrict__ jobs, const unsigned int *__restrict__ 
     }
     for (int i = threadIdx.x; i < rows * nOR; i += blockDim.x) acc[i] = 0.f;
     for (int i = threadIdx.x; i < nOR; i += blockDim.x) norm[i] = 0.f;
+    // orientations nOR..7 of Q stay zero (their sums are not stored)
+    for (int i = nOR * kFineChunk + threadIdx.x; i < 8 * kFineChunk; i += blockDim.x) Q[i] = make_float2(0.f, 0.f);
     __syncthreads();
     const float2 *bp = b_f + (size_t)p * ldpf;
     const float *ap = a_f + (size_t)p * ldpf;
@@ -999,31 +1023,31 @@ k_fine_diff2(const FineJob *__restrict__ jobs, const unsigned int *__restrict__ 
             if (lane == 0) norm[ior] += nacc;
         }
         __syncthreads();
-        for (int row = warp; row < rows; row += nwarp) {
-            const int tr = row / nOT, iot = row - tr * nOT;
-            const int tf = tlist[tr] * nOT + iot;
-            const float2 *E = phase_f + (size_t)tf * nf + c0;
-            float s[8];
+        for (int row0 = warp * kFineRows; row0 < rows; row0 += nwarp * kFineRows) {
+            const float2 *E[kFineRows];
 #pragma unroll
-            for (int i = 0; i < 8; ++i) s[i] = 0.f;
+            for (int j = 0; j < kFineRows; ++j) {
+                const int row = min(row0 + j, rows - 1);  // rows past the end repeat the last (not stored)
+                const int tr = row / nOT, iot = row - tr * nOT;
+                E[j] = phase_f + (size_t)(tlist[tr] * nOT + iot) * nf + c0;
+            }
+            float s[32];
+#pragma unroll
+            for (int i = 0; i < 32; ++i) s[i] = 0.f;
             for (int k = lane; k < cl; k += 32) {
-                const float2 e = E[k];
+                float2 q[8];
 #pragma unroll
-                for (int i = 0; i < 8; ++i)
-                    if (i < nOR) {
-                        const float2 q = Q[i * kFineChunk + k];
-                        s[i] = fmaf(q.x, e.x, fmaf(q.y, e.y, s[i]));
-                    }
+                for (int i = 0; i < 8; ++i) q[i] = Q[i * kFineChunk + k];
+#pragma unroll
+                for (int j = 0; j < kFineRows; ++j) {
+                    const float2 e = E[j][k];
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) s[j * 8 + i] = fmaf(q[i].x, e.x, fmaf(q[i].y, e.y, s[j * 8 + i]));
+                }
             }
-#pragma unroll
-            for (int i = 0; i < 8; ++i) s[i] = warp_sum(s[i]);
-            if (lane < nOR && lane < 8) {
-                float v = s[0];
-#pragma unroll
-                for (int i = 1; i < 8; ++i)
-                    if (lane == i) v = s[i];
-                acc[row * nOR + lane] += v;
-            }
+            const float v = warp_transpose_sum32(s, lane);
+            const int row = row0 + (lane >> 3), ior = lane & 7;
+            if (row < rows && ior < nOR) acc[row * nOR + ior] += v;
         }
         __syncthreads();
     }
@@ -1639,7 +1663,7 @@ cudaError_t launch_fine_diff2(const FineJob *jobs, long long njobs, const unsign
                               unsigned int *ecode, ParticleState *ps, cudaStream_t st) {
     if (njobs <= 0) return cudaSuccess;
     if (nOR > 8) return cudaErrorInvalidValue;
-    const size_t smem = sizeof(float2) * nOR * kFineChunk + sizeof(float) * T * nOT * nOR +
+    const size_t smem = sizeof(float2) * 8 * kFineChunk + sizeof(float) * T * nOT * nOR +
                         sizeof(int) * T + sizeof(float) * nOR + 16;
     static size_t attr = 0;
     if (smem > attr) {

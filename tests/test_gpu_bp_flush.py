@@ -2,7 +2,8 @@
 FP64 volumes once they hold GBR_OPT_BP_FLUSH particles, and before the
 volumes are read, replaced or reconstructed.  Three batches with a flush
 after every batch and with the flush deferred to the download give the same
-volumes to FP32 rounding; clearing the weighted sums clears what is staged."""
+volumes to the FP32 staging's run-to-run spread (1e-5, the oracle's volume
+tolerance); clearing the weighted sums clears what is staged."""
 import numpy as np
 import pytest
 
@@ -38,7 +39,8 @@ def test_deferred_flush_equals_flush_per_batch():
         b.close()
     (d0, w0), (d1, w1) = out["each"], out["deferred"]
     assert np.linalg.norm(np.ravel(w0)) > 0
-    assert _rel(d1, d0) <= 1e-6 and _rel(w1, w0) <= 1e-6
+    # FP32 staging sums in atomic (run-dependent) order: ~1e-6 between runs
+    assert _rel(d1, d0) <= 1e-5 and _rel(w1, w0) <= 1e-5
 
 
 def test_reset_clears_staged_insertions():
@@ -56,6 +58,6 @@ def test_reset_clears_staged_insertions():
     b.reset_wsum()
     w.do_expectation_some_particles(second)
     got = b.get_mdl_data(0)
-    assert _rel(got[0], want[0]) <= 1e-6 and _rel(got[1], want[1]) <= 1e-6
+    assert _rel(got[0], want[0]) <= 1e-5 and _rel(got[1], want[1]) <= 1e-5
     w.close()
     b.close()
