@@ -1088,7 +1088,9 @@ __global__ void __launch_bounds__(kWsumPix) k_wsum(WsumArgs a) {
     double *shell = wsm;                                            // [nshell]
     float *wt = reinterpret_cast<float *>(shell + a.nshell);        // [rows][kMaxOR]
     int *tlist = reinterpret_cast<int *>(wt + a.T * a.nOT * kMaxOR); // [T]
+    int *rlist = tlist + a.T;                                       // [rows] rows with a significant weight
     __shared__ double red[6];  // sumw, sigma2_offset, XA, AA, 2D class offset sums x / y
+    __shared__ int wcount[kWsumPix / 32], nnz;
     const FineJob job = a.jobs[blockIdx.x];
     const int p = job.p, r = job.r, n_t = job.n_t;
     const int nOR = a.nOR, nOT = a.nOT;
@@ -1112,6 +1114,7 @@ __global__ void __launch_bounds__(kWsumPix) k_wsum(WsumArgs a) {
         }
     }
     if (threadIdx.x < 6) red[threadIdx.x] = 0.;
+    if (threadIdx.x == 0) nnz = 0;
     for (int i = threadIdx.x; i < a.nshell; i += blockDim.x) shell[i] = 0.;
     __syncthreads();
     // 2D classification: the offset prior is the class's (:8449-8456)
@@ -1155,6 +1158,29 @@ __global__ void __launch_bounds__(kWsumPix) k_wsum(WsumArgs a) {
         }
     }
     __syncthreads();
+    // the rows (t, iot) with a significant weight for some orientation, in
+    // row order (the sums below skip rows whose weights are all zero; adding
+    // zero terms would not change them)
+    {
+        const int wp = threadIdx.x >> 5, ln = threadIdx.x & 31;
+        for (int base = 0; base < rows; base += blockDim.x) {
+            const int row = base + threadIdx.x;
+            bool f = false;
+            if (row < rows)
+                for (int i = 0; i < nOR; ++i) f = f || wt[row * kMaxOR + i] != 0.f;
+            const unsigned int bal = __ballot_sync(0xffffffffu, f);
+            if (ln == 0) wcount[wp] = __popc(bal);
+            __syncthreads();
+            int off = nnz;
+            for (int w2 = 0; w2 < wp; ++w2) off += wcount[w2];
+            if (f) rlist[off + __popc(bal & ((1u << ln) - 1u))] = row;
+            __syncthreads();
+            if (threadIdx.x == 0)
+                for (int w2 = 0; w2 < (int)(blockDim.x >> 5); ++w2) nnz += wcount[w2];
+            __syncthreads();
+        }
+    }
+    const int nrz = nnz;
     const int k = blockIdx.y * kWsumPix + threadIdx.x;
     double l_xa = 0., l_aa = 0.;
     if (k < a.nf) {
@@ -1171,21 +1197,20 @@ __global__ void __launch_bounds__(kWsumPix) k_wsum(WsumArgs a) {
             s2[ior] = 0.f;
             W[ior] = 0.f;
         }
-        for (int tr = 0; tr < n_t; ++tr) {
-            const float2 *ph = a.phase_f + (size_t)tlist[tr] * nOT * a.nf + k;
-            for (int iot = 0; iot < nOT; ++iot) {
-                const float2 e = ph[(size_t)iot * a.nf];
-                const float xr = x.x * e.x - x.y * e.y, xi = x.x * e.y + x.y * e.x;
-                const float *wr = wt + (tr * nOT + iot) * kMaxOR;
+        for (int q = 0; q < nrz; ++q) {
+            const int row = rlist[q];
+            const int tr = row / nOT, iot = row - tr * nOT;
+            const float2 e = a.phase_f[((size_t)tlist[tr] * nOT + iot) * a.nf + k];
+            const float xr = x.x * e.x - x.y * e.y, xi = x.x * e.y + x.y * e.x;
+            const float *wr = wt + row * kMaxOR;
 #pragma unroll
-                for (int ior = 0; ior < kMaxOR; ++ior) {
-                    const float wv = wr[ior];
-                    const float dr = fmaf(cs, pv[ior].x, -xr), di = fmaf(cs, pv[ior].y, -xi);
-                    s2[ior] = fmaf(wv, dr * dr + di * di, s2[ior]);
-                    phi[ior].x = fmaf(wv, e.x, phi[ior].x);
-                    phi[ior].y = fmaf(wv, e.y, phi[ior].y);
-                    W[ior] += wv;
-                }
+            for (int ior = 0; ior < kMaxOR; ++ior) {
+                const float wv = wr[ior];
+                const float dr = fmaf(cs, pv[ior].x, -xr), di = fmaf(cs, pv[ior].y, -xi);
+                s2[ior] = fmaf(wv, dr * dr + di * di, s2[ior]);
+                phi[ior].x = fmaf(wv, e.x, phi[ior].x);
+                phi[ior].y = fmaf(wv, e.y, phi[ior].y);
+                W[ior] += wv;
             }
         }
         const int sh = a.pf[k].shell;
@@ -1683,8 +1708,8 @@ cudaError_t launch_wsum(const WsumArgs &a, cudaStream_t st) {
     if (a.njobs <= 0) return cudaSuccess;
     if (a.nOR > kMaxOR) return cudaErrorInvalidValue;
     if (a.njobs > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-    const size_t smem =
-        sizeof(double) * a.nshell + sizeof(float) * (size_t)kMaxOR * a.T * a.nOT + sizeof(int) * a.T + 16;
+    const size_t smem = sizeof(double) * a.nshell + sizeof(float) * (size_t)kMaxOR * a.T * a.nOT +
+                        sizeof(int) * (a.T + (size_t)a.T * a.nOT) + 16;
     static size_t attr = 0;
     if (smem > attr) {
         cudaError_t e = cudaFuncSetAttribute(k_wsum, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
