@@ -1280,6 +1280,55 @@ __global__ void k_compact_flags(const unsigned char *__restrict__ flags, int n, 
     }
 }
 
+// One slice pixel's trilinear (3D) or bilinear (2D) insertion: value val,
+// weight w, pixel (px, py), rotation Ai.
+__device__ __forceinline__ void bp_insert(const float *Ai, int px, int py, float2 val, float w, const VolGeom &g,
+                                          float4 *sv) {
+    float xp = fmaf(Ai[0], (float)px, Ai[1] * (float)py);
+    float yp = fmaf(Ai[3], (float)px, Ai[4] * (float)py);
+    if (g.dim == 2) {
+        // BackProjector::backrotate2D (src/backprojector.cpp:471-660):
+        // bilinear insertion into the 2D data / weight planes
+        if (xp < 0.f) {
+            xp = -xp;
+            yp = -yp;
+            val.y = -val.y;
+        }
+        const float fx0 = floorf(xp), fy0 = floorf(yp);
+        const float fx = xp - fx0, fy = yp - fy0;
+        const int x0 = (int)fx0, y0 = (int)fy0 - g.yinit;
+        if (x0 < 0 || x0 + 1 >= g.xdim || y0 < 0 || y0 + 1 >= g.ydim) return;
+        const float mfx = 1.f - fx, mfy = 1.f - fy;
+        const float d4[4] = {mfy * mfx, mfy * fx, fy * mfx, fy * fx};
+        const size_t base = (size_t)y0 * g.xdim + x0;
+        const size_t off4[4] = {0, 1, (size_t)g.xdim, (size_t)g.xdim + 1};
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+            atomicAdd(&sv[base + off4[c]], make_float4(d4[c] * val.x, d4[c] * val.y, d4[c] * w, 0.f));
+        return;
+    }
+    float zp = fmaf(Ai[6], (float)px, Ai[7] * (float)py);
+    if (xp < 0.f) {
+        xp = -xp;
+        yp = -yp;
+        zp = -zp;
+        val.y = -val.y;
+    }
+    const float fx0 = floorf(xp), fy0 = floorf(yp), fz0 = floorf(zp);
+    const float fx = xp - fx0, fy = yp - fy0, fz = zp - fz0;
+    const int x0 = (int)fx0, y0 = (int)fy0 - g.yinit, z0 = (int)fz0 - g.zinit;
+    if (x0 < 0 || x0 + 1 >= g.xdim || y0 < 0 || y0 + 1 >= g.ydim || z0 < 0 || z0 + 1 >= g.zdim) return;
+    const float mfx = 1.f - fx, mfy = 1.f - fy, mfz = 1.f - fz;
+    const float dd[8] = {mfz * mfy * mfx, mfz * mfy * fx, mfz * fy * mfx, mfz * fy * fx,
+                         fz * mfy * mfx,  fz * mfy * fx,  fz * fy * mfx,  fz * fy * fx};
+    const size_t sy = (size_t)g.xdim, sz = (size_t)g.xdim * g.ydim;
+    const size_t base = (size_t)z0 * sz + (size_t)y0 * sy + x0;
+    const size_t off[8] = {0, 1, sy, sy + 1, sz, sz + 1, sz + sy, sz + sy + 1};
+#pragma unroll
+    for (int c = 0; c < 8; ++c)
+        atomicAdd(&sv[base + off[c]], make_float4(dd[c] * val.x, dd[c] * val.y, dd[c] * w, 0.f));
+}
+
 // Trilinear insertion of the accumulated 2D slices of the active fine
 // orientations (backproject2Dto3D, src/backprojector.cpp:55-296) into the
 // FP32 staging volume: one float4 (re, im, weight, 0) per voxel, one vector
@@ -1287,84 +1336,65 @@ __global__ void k_compact_flags(const unsigned char *__restrict__ flags, int n, 
 // the staging volume into the FP64 data and weight volumes once it holds a
 // set number of particles (a few batches), so the volumes accumulate in FP64
 // and a staging sum holds a bounded number of particles.  Each block handles
-// one slice; the slice accumulators are cleared for the next batch.
-__global__ void k_backproject(const int *__restrict__ list, const float *__restrict__ eul_f, int nOR,
-                              const int *__restrict__ cls_of_r, float2 *__restrict__ bpimg,
-                              float *__restrict__ bpw, const PixelRef *__restrict__ pf, int nf,
-                              const VolGeom g, float4 *const *__restrict__ stage,
-                              unsigned char *__restrict__ active, const int *__restrict__ count,
-                              const int *__restrict__ circ, const unsigned long long *__restrict__ cmask) {
+// one slice at a time; the slice accumulators are cleared for the next batch.
+// A thread takes kBpUnroll pixels per step and issues their loads first: the
+// kernel waits on those loads (slices scattered over the accumulator array),
+// not on the atomics, so loads in flight per thread set its speed.
+constexpr int kBpThreads = 256, kBpUnroll = 4;
+
+__global__ void __launch_bounds__(kBpThreads)
+k_backproject(const int *__restrict__ list, const float *__restrict__ eul_f, int nOR,
+              const int *__restrict__ cls_of_r, float2 *__restrict__ bpimg, float *__restrict__ bpw,
+              const PixelRef *__restrict__ pf, int nf, const VolGeom g, float4 *const *__restrict__ stage,
+              unsigned char *__restrict__ active, const int *__restrict__ count, const int *__restrict__ circ,
+              const unsigned long long *__restrict__ cmask) {
     const int nlist = *count;
-    for (int li = blockIdx.x; li < nlist; li += gridDim.x) {
-    const int rf = list[li];
     __shared__ float Ai[9];
-    __syncthreads();  // the previous slice's readers of Ai are done
-    if (threadIdx.x < 9) Ai[threadIdx.x] = eul_f[(size_t)rf * 9 + threadIdx.x];
-    __syncthreads();
-    const int ic = cls_of_r[rf / nOR];
-    float4 *sv = stage[ic];
     const int rr = (int)lrintf((float)g.r_max * g.pad);   // ROUND(r_max * pad)
     const int max_r2 = rr * rr;
-    const size_t sy = (size_t)g.xdim, sz = (size_t)g.xdim * g.ydim;
-    for (int k = threadIdx.x; k < nf; k += blockDim.x) {
-        const size_t idx = (size_t)rf * nf + k;
-        const float w = bpw[idx];
-        const float2 val0 = bpimg[idx];
-        bpw[idx] = 0.f;
-        bpimg[idx] = make_float2(0.f, 0.f);
-        if (!(w > 0.f)) continue;
-        const PixelRef pr = pf[k];
-        if (g.pad * g.pad * (pr.x * pr.x + pr.y * pr.y) > max_r2) continue;
-        // pixels on the r_max circle: inserted where the reference inserts them
-        const int cb = circ ? circ[k] : -1;
-        if (cb >= 0 && !((cmask[rf] >> cb) & 1ull)) continue;
-        float xp = fmaf(Ai[0], (float)pr.x, Ai[1] * (float)pr.y);
-        float yp = fmaf(Ai[3], (float)pr.x, Ai[4] * (float)pr.y);
-        if (g.dim == 2) {
-            // BackProjector::backrotate2D (src/backprojector.cpp:471-660):
-            // bilinear insertion into the 2D data / weight planes
-            float2 v2 = val0;
-            if (xp < 0.f) {
-                xp = -xp;
-                yp = -yp;
-                v2.y = -v2.y;
+    for (int li = blockIdx.x; li < nlist; li += gridDim.x) {
+        const int rf = list[li];
+        __syncthreads();  // the previous slice's readers of Ai are done
+        if (threadIdx.x < 9) Ai[threadIdx.x] = eul_f[(size_t)rf * 9 + threadIdx.x];
+        __syncthreads();
+        float4 *sv = stage[cls_of_r[rf / nOR]];
+        const unsigned long long cm = circ ? cmask[rf] : 0ull;
+        for (int k0 = threadIdx.x; k0 < nf; k0 += kBpThreads * kBpUnroll) {
+            float wv[kBpUnroll];
+            float2 vv[kBpUnroll];
+            int2 xy[kBpUnroll];
+            int cb[kBpUnroll];
+#pragma unroll
+            for (int u = 0; u < kBpUnroll; ++u) {
+                const int k = k0 + u * kBpThreads;
+                wv[u] = 0.f;
+                if (k < nf) {
+                    const size_t idx = (size_t)rf * nf + k;
+                    wv[u] = bpw[idx];
+                    vv[u] = bpimg[idx];
+                    xy[u] = *reinterpret_cast<const int2 *>(&pf[k]);
+                    cb[u] = circ ? circ[k] : -1;
+                }
             }
-            const float fx0 = floorf(xp), fy0 = floorf(yp);
-            const float fx = xp - fx0, fy = yp - fy0;
-            const int x0 = (int)fx0, y0 = (int)fy0 - g.yinit;
-            if (x0 < 0 || x0 + 1 >= g.xdim || y0 < 0 || y0 + 1 >= g.ydim) continue;
-            const float mfx = 1.f - fx, mfy = 1.f - fy;
-            const float d4[4] = {mfy * mfx, mfy * fx, fy * mfx, fy * fx};
-            const size_t base = (size_t)y0 * g.xdim + x0;
-            const size_t off4[4] = {0, 1, (size_t)g.xdim, (size_t)g.xdim + 1};
 #pragma unroll
-            for (int c = 0; c < 4; ++c)
-                atomicAdd(&sv[base + off4[c]], make_float4(d4[c] * v2.x, d4[c] * v2.y, d4[c] * w, 0.f));
-            continue;
-        }
-        float zp = fmaf(Ai[6], (float)pr.x, Ai[7] * (float)pr.y);
-        float2 val = val0;
-        if (xp < 0.f) {
-            xp = -xp;
-            yp = -yp;
-            zp = -zp;
-            val.y = -val.y;
-        }
-        const float fx0 = floorf(xp), fy0 = floorf(yp), fz0 = floorf(zp);
-        const float fx = xp - fx0, fy = yp - fy0, fz = zp - fz0;
-        const int x0 = (int)fx0, y0 = (int)fy0 - g.yinit, z0 = (int)fz0 - g.zinit;
-        if (x0 < 0 || x0 + 1 >= g.xdim || y0 < 0 || y0 + 1 >= g.ydim || z0 < 0 || z0 + 1 >= g.zdim)
-            continue;
-        const float mfx = 1.f - fx, mfy = 1.f - fy, mfz = 1.f - fz;
-        const float dd[8] = {mfz * mfy * mfx, mfz * mfy * fx, mfz * fy * mfx, mfz * fy * fx,
-                             fz * mfy * mfx,  fz * mfy * fx,  fz * fy * mfx,  fz * fy * fx};
-        const size_t base = (size_t)z0 * sz + (size_t)y0 * sy + x0;
-        const size_t off[8] = {0, 1, sy, sy + 1, sz, sz + 1, sz + sy, sz + sy + 1};
+            for (int u = 0; u < kBpUnroll; ++u) {
+                const int k = k0 + u * kBpThreads;
+                if (k < nf) {
+                    const size_t idx = (size_t)rf * nf + k;
+                    bpw[idx] = 0.f;
+                    bpimg[idx] = make_float2(0.f, 0.f);
+                }
+            }
 #pragma unroll
-        for (int c = 0; c < 8; ++c)
-            atomicAdd(&sv[base + off[c]], make_float4(dd[c] * val.x, dd[c] * val.y, dd[c] * w, 0.f));
-    }
-    if (threadIdx.x == 0) active[rf] = 0;
+            for (int u = 0; u < kBpUnroll; ++u) {
+                if (!(wv[u] > 0.f)) continue;
+                if (g.pad * g.pad * (xy[u].x * xy[u].x + xy[u].y * xy[u].y) > max_r2) continue;
+                // pixels on the r_max circle: inserted where the reference inserts them
+                if (cb[u] >= 0 && !((cm >> cb[u]) & 1ull)) continue;
+                bp_insert(Ai, xy[u].x, xy[u].y, vv[u], wv[u], g, sv);
+            }
+        }
+        if (threadIdx.x == 0) active[rf] = 0;
     }
 }
 
@@ -1751,8 +1781,8 @@ cudaError_t launch_backproject(const int *list, const int *count, int max_list, 
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     const int grid = std::min(max_list, 8 * nsm);
-    k_backproject<<<grid, 256, 0, st>>>(list, eul_f, nOR, cls_of_r, bpimg, bpw, pf, nf, g, stage, active, count,
-                                        circ, mask);
+    k_backproject<<<grid, kBpThreads, 0, st>>>(list, eul_f, nOR, cls_of_r, bpimg, bpw, pf, nf, g, stage, active,
+                                                count, circ, mask);
     return cudaGetLastError();
 }
 
