@@ -63,9 +63,11 @@ def parse():
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP32 path leg (profiling runs)")
     ap.add_argument("--no-late", action="store_true", help="skip the late-iteration section (profiling runs)")
     ap.add_argument("--workload", default=CONFIG,
-                    choices=["cfg1_box256", "cfg1_box256_late", "cfg4_box256_K4", "cfg3_box128_2d", "cfg0_box64"],
+                    choices=["cfg1_box256", "cfg1_box256_late", "cfg1_box128_late", "cfg4_box256_K4", "cfg3_box128_2d",
+                             "cfg0_box64"],
                     help="dataset shape (the headline line is cfg1_box256; the others for reference figures; "
-                         "cfg1_box256_late: the same refinement in a late iteration, current size 256)")
+                         "cfg1_box256_late: the same refinement in a late iteration, current size 256; "
+                         "cfg1_box128_late: the late shape at box 128, small enough for profiler captures)")
     ap.add_argument("--precision", default="bf16", choices=["fp32", "bf16"],
                     help="coarse cross term: plain FP32 SIMT or tcgen05 BF16 (precision form)")
     return ap.parse_args()

@@ -277,6 +277,10 @@ struct gbr_worker {
     DevBuf<unsigned int> mask;
     DevBuf<int> cnt;
     DevBuf<long long> scan_tmp;
+    // fine-pass work queue: head counter, per-job arrivals, partial sums
+    DevBuf<unsigned long long> fq_head;
+    DevBuf<int> fq_arrive;
+    DevBuf<float> fq_part, fq_npart;
     DevBuf<FineJob> jobs;
     DevBuf<unsigned char> need_r;
     DevBuf<int> proj_ids, act_list, act_count;
@@ -743,8 +747,16 @@ int fine_sparse(gbr_worker *w, int n, long long njobs, long long nfine, const st
     GBR_CUDA(w->ecode.reserve(nfine));
     GBR_CUDA(cudaEventRecord(w->ev[5], st));
     const float2 *projf = reinterpret_cast<const float2 *>(b->proj_f.p);
-    GBR_CUDA(launch_fine_diff2(w->jobs.p, njobs, w->mask.p, R, T, W, nOR, nOT, projf, b->ldk_f, w->b_f.p, w->a_f.p,
-                               b->nf, b->phase_f.p, w->fd.p, w->ejob.p, w->ecode.p, w->ps.p, st));
+    // work queue of (job, pixel range) items; the job count is read on the device
+    const int nsplit = fine_diff2_nsplit(b->nf);
+    GBR_CUDA(w->fq_part.reserve((size_t)nfine * nsplit));
+    GBR_CUDA(w->fq_npart.reserve((size_t)njobs * 8 * nsplit));
+    GBR_CUDA(w->fq_arrive.reserve(njobs));
+    GBR_CUDA(w->fq_head.reserve(1));
+    GBR_CUDA(launch_fine_diff2(w->jobs.p, w->scan_tmp.p + 2 * fine_jobs_nblocks((long long)n * R), njobs, nsplit,
+                               w->fq_head.p, w->fq_arrive.p, w->fq_part.p, w->fq_npart.p, w->mask.p, R, T, W, nOR,
+                               nOT, projf, b->ldk_f, w->b_f.p, w->a_f.p, b->nf, b->phase_f.p, w->fd.p, w->ejob.p,
+                               w->ecode.p, w->ps.p, st));
     GBR_CUDA(cudaEventRecord(w->ev[6], st));
     if (w->debug) {
         gbr_worker::DbgPass &D = w->dbg.back();

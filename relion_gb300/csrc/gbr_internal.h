@@ -226,11 +226,17 @@ cudaError_t launch_sig_masks(const float *w, int n, int R, int T, int W, const P
 long long fine_jobs_nblocks(long long tot);
 cudaError_t launch_fine_jobs(const int *cnt, int n, int R, int per, long long *sums, FineJob *jobs, long long *seg,
                              unsigned char *need_r, cudaStream_t st);
-cudaError_t launch_fine_diff2(const FineJob *jobs, long long njobs, const unsigned int *mask,
-                              int R, int T, int W, int nOR, int nOT, const float2 *projf, int ldpf,
-                              const float2 *b_f, const float *a_f, int nf, const float2 *phase_f,
-                              float *d, int *ejob, unsigned int *ecode, ParticleState *ps,
-                              cudaStream_t st);
+// Fine diff2 over a device work queue of (job, pixel range) items: the job
+// count is read on the device (njobs_dev; njobs_max sizes the arrival
+// counters), nsplit = fine_diff2_nsplit(nf) ranges per job, head / arrive
+// are zeroed by the launcher, part holds [nfine][nsplit] and npart
+// [njobs][8][nsplit] floats.
+int fine_diff2_nsplit(int nf);
+cudaError_t launch_fine_diff2(const FineJob *jobs, const long long *njobs_dev, long long njobs_max, int nsplit,
+                              unsigned long long *head, int *arrive, float *part, float *npart,
+                              const unsigned int *mask, int R, int T, int W, int nOR, int nOT, const float2 *projf,
+                              int ldpf, const float2 *b_f, const float *a_f, int nf, const float2 *phase_f, float *d,
+                              int *ejob, unsigned int *ecode, ParticleState *ps, cudaStream_t st);
 struct WsumArgs {
     const FineJob *jobs;
     long long njobs;

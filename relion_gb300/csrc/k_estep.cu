@@ -938,19 +938,25 @@ __global__ void __launch_bounds__(kJobsThreads) k_jobs_emit(const int *__restric
 }
 
 // ---------------------------------------------------------------------------
-// Fine pass: one block per job (particle p, coarse orientation r).
-// For every oversampled orientation ior and every significant coarse
-// translation t with its oversampled shifts iot:
+// Fine pass over a device work queue: a work item is one job (particle p,
+// coarse orientation r) and one range of kFineSplit fine pixels; jobs with
+// many significant translations and jobs with few share one persistent
+// launch whose blocks take the next item from a device counter.  For every
+// oversampled orientation ior and every significant coarse translation t
+// with its oversampled shifts iot:
 //   diff2 - c_fine = N_ior - 2 sum_k Re(Q_ior,k conj(E_(t,iot),k)),
 //   Q = P_(r,ior) conj(m C X),  N_ior = sum_k m C^2 |P|^2.
-// Q is staged in shared memory per pixel chunk.  A warp takes kFineRows
-// rows (t, iot) at a time: each Q value read from shared memory serves
-// kFineRows rows (shared-memory reads, not FMAs, bounded the one-row form),
-// and the warp's 32 partial sums (kFineRows rows x 8 orientations) are
-// reduced across the lanes in one 31-shuffle transpose-reduction.
-// Entries are written in hidden-index order (t, ior, iot) within the job.
+// Q is staged in shared memory per chunk of kFineChunk pixels.  A warp takes
+// kFineRows rows (t, iot) at a time: each Q value read from shared memory
+// serves kFineRows rows, and the warp's 32 partial sums (kFineRows rows x 8
+// orientations) are reduced across the lanes in one 31-shuffle
+// transpose-reduction.  Each item stores its partial sums; the job's last
+// item to finish (arrival counter) adds the partials in range order (the
+// result does not depend on which block ran which range), writes the entries
+// in hidden-index order (t, ior, iot) and the particle's minimum.
 // ---------------------------------------------------------------------------
 constexpr int kFineChunk = 512;
+constexpr int kFineSplit = 4 * kFineChunk;  // fine pixels per work item
 constexpr int kFineThreads = 256;
 constexpr int kFineRows = 4;  // rows per warp pass; kFineRows x 8 orientations = 32 lanes
 
@@ -971,101 +977,147 @@ __device__ __forceinline__ float warp_transpose_sum32(float (&v)[32], int lane) 
     return v[0];
 }
 
+struct FineQueue {
+    const long long *njobs;        // device: number of jobs
+    int nsplit;                    // pixel ranges per job
+    unsigned long long *head;      // next work item (zero at launch)
+    int *arrive;                   // [njobs] items finished (zero at launch)
+    float *part;                   // [nfine][nsplit] partial cross sums
+    float *npart;                  // [njobs][8][nsplit] partial norms
+};
+
 __global__ void __launch_bounds__(kFineThreads, 4)
-k_fine_diff2(const FineJob *__restrict__ jobs, const unsigned int *__restrict__ mask, int R, int T,
-             int W, int nOR, int nOT, const float2 *__restrict__ projf, int ldpf, const float2 *__restrict__ b_f,
-             const float *__restrict__ a_f, int nf, const float2 *__restrict__ phase_f,
-             float *__restrict__ d, int *__restrict__ ejob, unsigned int *__restrict__ ecode,
-             ParticleState *__restrict__ ps) {
+k_fine_diff2(const FineJob *__restrict__ jobs, const FineQueue qu, const unsigned int *__restrict__ mask, int R,
+             int T, int W, int nOR, int nOT, const float2 *__restrict__ projf, int ldpf,
+             const float2 *__restrict__ b_f, const float *__restrict__ a_f, int nf,
+             const float2 *__restrict__ phase_f, float *__restrict__ d, int *__restrict__ ejob,
+             unsigned int *__restrict__ ecode, ParticleState *__restrict__ ps) {
     extern __shared__ float4 fsm[];
     float2 *Q = reinterpret_cast<float2 *>(fsm);                   // [8][kFineChunk]
     float *acc = reinterpret_cast<float *>(Q + 8 * kFineChunk);    // [rows][nOR]
     int *tlist = reinterpret_cast<int *>(acc + T * nOT * nOR);     // [T]
     float *norm = reinterpret_cast<float *>(tlist + T);            // [nOR]
     __shared__ unsigned int smin;
-    const long long jid = blockIdx.x;
-    const FineJob job = jobs[jid];
-    const int p = job.p, r = job.r, n_t = job.n_t;
-    const int rows = n_t * nOT;
+    __shared__ unsigned long long item_s;
+    __shared__ int last_s;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-    const unsigned int *mk = mask + ((size_t)p * R + r) * W;
-    if (threadIdx.x == 0) {
-        int m = 0;
-        for (int w = 0; w < W; ++w) {
-            unsigned int bits = mk[w];
-            while (bits) {
-                const int b = __ffs(bits) - 1;
-                bits &= bits - 1;
-                tlist[m++] = w * 32 + b;
-            }
-        }
-        smin = 0xFFFFFFFFu;
-    }
-    for (int i = threadIdx.x; i < rows * nOR; i += blockDim.x) acc[i] = 0.f;
-    for (int i = threadIdx.x; i < nOR; i += blockDim.x) norm[i] = 0.f;
+    const int S = qu.nsplit;
+    const unsigned long long total = (unsigned long long)(*qu.njobs) * (unsigned long long)S;
     // orientations nOR..7 of Q stay zero (their sums are not stored)
     for (int i = nOR * kFineChunk + threadIdx.x; i < 8 * kFineChunk; i += blockDim.x) Q[i] = make_float2(0.f, 0.f);
-    __syncthreads();
-    const float2 *bp = b_f + (size_t)p * ldpf;
-    const float *ap = a_f + (size_t)p * ldpf;
-    for (int c0 = 0; c0 < nf; c0 += kFineChunk) {
-        const int cl = min(kFineChunk, nf - c0);
-        // stage Q, accumulate norms (one warp per ior at a time)
-        for (int ior = warp; ior < nOR; ior += nwarp) {
-            const float2 *P = projf + ((size_t)r * nOR + ior) * ldpf + c0;
-            float nacc = 0.f;
-            for (int k = lane; k < cl; k += 32) {
-                const float2 pv = P[k], bv = bp[c0 + k];
-                Q[ior * kFineChunk + k] = make_float2(pv.x * bv.x + pv.y * bv.y, pv.y * bv.x - pv.x * bv.y);
-                nacc = fmaf(ap[c0 + k], pv.x * pv.x + pv.y * pv.y, nacc);
-            }
-            nacc = warp_sum(nacc);
-            if (lane == 0) norm[ior] += nacc;
-        }
+    for (;;) {
+        if (threadIdx.x == 0) item_s = atomicAdd(qu.head, 1ull);
         __syncthreads();
-        for (int row0 = warp * kFineRows; row0 < rows; row0 += nwarp * kFineRows) {
-            const float2 *E[kFineRows];
-#pragma unroll
-            for (int j = 0; j < kFineRows; ++j) {
-                const int row = min(row0 + j, rows - 1);  // rows past the end repeat the last (not stored)
-                const int tr = row / nOT, iot = row - tr * nOT;
-                E[j] = phase_f + (size_t)(tlist[tr] * nOT + iot) * nf + c0;
-            }
-            float s[32];
-#pragma unroll
-            for (int i = 0; i < 32; ++i) s[i] = 0.f;
-            for (int k = lane; k < cl; k += 32) {
-                float2 q[8];
-#pragma unroll
-                for (int i = 0; i < 8; ++i) q[i] = Q[i * kFineChunk + k];
-#pragma unroll
-                for (int j = 0; j < kFineRows; ++j) {
-                    const float2 e = E[j][k];
-#pragma unroll
-                    for (int i = 0; i < 8; ++i) s[j * 8 + i] = fmaf(q[i].x, e.x, fmaf(q[i].y, e.y, s[j * 8 + i]));
+        const unsigned long long item = item_s;
+        if (item >= total) break;
+        const long long jid = (long long)(item / (unsigned long long)S);
+        const int sidx = (int)(item - (unsigned long long)jid * S);
+        const FineJob job = jobs[jid];
+        const int p = job.p, r = job.r, n_t = job.n_t;
+        const int rows = n_t * nOT;
+        if (threadIdx.x == 0) {
+            const unsigned int *mk = mask + ((size_t)p * R + r) * W;
+            int m = 0;
+            for (int w = 0; w < W; ++w) {
+                unsigned int bits = mk[w];
+                while (bits) {
+                    const int b = __ffs(bits) - 1;
+                    bits &= bits - 1;
+                    tlist[m++] = w * 32 + b;
                 }
             }
-            const float v = warp_transpose_sum32(s, lane);
-            const int row = row0 + (lane >> 3), ior = lane & 7;
-            if (row < rows && ior < nOR) acc[row * nOR + ior] += v;
+            smin = 0xFFFFFFFFu;
         }
+        for (int i = threadIdx.x; i < rows * nOR; i += blockDim.x) acc[i] = 0.f;
+        for (int i = threadIdx.x; i < nOR; i += blockDim.x) norm[i] = 0.f;
         __syncthreads();
+        const float2 *bp = b_f + (size_t)p * ldpf;
+        const float *ap = a_f + (size_t)p * ldpf;
+        const int kend = min(nf, (sidx + 1) * kFineSplit);
+        for (int c0 = sidx * kFineSplit; c0 < kend; c0 += kFineChunk) {
+            const int cl = min(kFineChunk, kend - c0);
+            // stage Q, accumulate norms (one warp per ior at a time)
+            for (int ior = warp; ior < nOR; ior += nwarp) {
+                const float2 *P = projf + ((size_t)r * nOR + ior) * ldpf + c0;
+                float nacc = 0.f;
+                for (int k = lane; k < cl; k += 32) {
+                    const float2 pv = P[k], bv = bp[c0 + k];
+                    Q[ior * kFineChunk + k] = make_float2(pv.x * bv.x + pv.y * bv.y, pv.y * bv.x - pv.x * bv.y);
+                    nacc = fmaf(ap[c0 + k], pv.x * pv.x + pv.y * pv.y, nacc);
+                }
+                nacc = warp_sum(nacc);
+                if (lane == 0) norm[ior] += nacc;
+            }
+            __syncthreads();
+            for (int row0 = warp * kFineRows; row0 < rows; row0 += nwarp * kFineRows) {
+                const float2 *E[kFineRows];
+#pragma unroll
+                for (int j = 0; j < kFineRows; ++j) {
+                    const int row = min(row0 + j, rows - 1);  // rows past the end repeat the last (not stored)
+                    const int tr = row / nOT, iot = row - tr * nOT;
+                    E[j] = phase_f + (size_t)(tlist[tr] * nOT + iot) * nf + c0;
+                }
+                float sacc[32];
+#pragma unroll
+                for (int i = 0; i < 32; ++i) sacc[i] = 0.f;
+                for (int k = lane; k < cl; k += 32) {
+                    float2 q[8];
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) q[i] = Q[i * kFineChunk + k];
+#pragma unroll
+                    for (int j = 0; j < kFineRows; ++j) {
+                        const float2 e = E[j][k];
+#pragma unroll
+                        for (int i = 0; i < 8; ++i)
+                            sacc[j * 8 + i] = fmaf(q[i].x, e.x, fmaf(q[i].y, e.y, sacc[j * 8 + i]));
+                    }
+                }
+                const float v = warp_transpose_sum32(sacc, lane);
+                const int row = row0 + (lane >> 3), ior = lane & 7;
+                if (row < rows && ior < nOR) acc[row * nOR + ior] += v;
+            }
+            __syncthreads();
+        }
+        // this range's partial sums; entry = off + (tr*nOR + ior)*nOT + iot
+        for (int i = threadIdx.x; i < rows * nOR; i += blockDim.x) {
+            const int row = i / nOR, ior = i - row * nOR;
+            const int tr = row / nOT, iot = row - tr * nOT;
+            const long long e = job.off + ((long long)tr * nOR + ior) * nOT + iot;
+            qu.part[e * S + sidx] = acc[i];
+        }
+        for (int i = threadIdx.x; i < nOR; i += blockDim.x) qu.npart[((size_t)jid * 8 + i) * S + sidx] = norm[i];
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0) last_s = atomicAdd(&qu.arrive[jid], 1) == S - 1;
+        __syncthreads();
+        if (last_s) {
+            // the job's last range: sum the partials in range order
+            __threadfence();
+            if (threadIdx.x < nOR) {
+                float nsum = 0.f;
+                for (int q = 0; q < S; ++q) nsum += __ldcg(&qu.npart[((size_t)jid * 8 + threadIdx.x) * S + q]);
+                norm[threadIdx.x] = nsum;
+            }
+            __syncthreads();
+            float lmin = FLT_MAX;
+            for (int i = threadIdx.x; i < rows * nOR; i += blockDim.x) {
+                const int row = i / nOR, ior = i - row * nOR;
+                const int tr = row / nOT, iot = row - tr * nOT;
+                const long long e = job.off + ((long long)tr * nOR + ior) * nOT + iot;
+                float csum = 0.f;
+                for (int q = 0; q < S; ++q) csum += __ldcg(&qu.part[e * S + q]);
+                const float v = norm[ior] - 2.f * csum;
+                d[e] = v;
+                ejob[e] = (int)jid;
+                ecode[e] = ((unsigned)tlist[tr] * nOR + ior) * nOT + iot;
+                lmin = fminf(lmin, v);
+            }
+            if (lmin < FLT_MAX) atomicMin(&smin, f2ord(lmin));
+            __syncthreads();
+            if (threadIdx.x == 0 && smin != 0xFFFFFFFFu) atomicMin(&ps[p].min_fine, smin);
+        }
+        __syncthreads();  // shared state of this item is done before the next item
     }
-    // write entries: entry = off + (tr*nOR + ior)*nOT + iot
-    float lmin = FLT_MAX;
-    for (int i = threadIdx.x; i < rows * nOR; i += blockDim.x) {
-        const int row = i / nOR, ior = i - row * nOR;
-        const int tr = row / nOT, iot = row - tr * nOT;
-        const float v = norm[ior] - 2.f * acc[i];
-        const long long e = job.off + ((long long)tr * nOR + ior) * nOT + iot;
-        d[e] = v;
-        ejob[e] = (int)jid;
-        ecode[e] = ((unsigned)tlist[tr] * nOR + ior) * nOT + iot;
-        lmin = fminf(lmin, v);
-    }
-    if (lmin < FLT_MAX) atomicMin(&smin, f2ord(lmin));
-    __syncthreads();
-    if (threadIdx.x == 0 && smin != 0xFFFFFFFFu) atomicMin(&ps[p].min_fine, smin);
 }
 
 // ---------------------------------------------------------------------------
@@ -1712,25 +1764,42 @@ long long fine_jobs_nblocks(long long tot) {
     return (tot + per_block - 1) / per_block;
 }
 
-cudaError_t launch_fine_diff2(const FineJob *jobs, long long njobs, const unsigned int *mask, int R,
-                              int T, int W, int nOR, int nOT, const float2 *projf, int ldpf, const float2 *b_f,
-                              const float *a_f, int nf, const float2 *phase_f, float *d, int *ejob,
-                              unsigned int *ecode, ParticleState *ps, cudaStream_t st) {
-    if (njobs <= 0) return cudaSuccess;
-    if (nOR > 8) return cudaErrorInvalidValue;
+int fine_diff2_nsplit(int nf) { return (nf + kFineSplit - 1) / kFineSplit; }
+
+cudaError_t launch_fine_diff2(const FineJob *jobs, const long long *njobs_dev, long long njobs_max, int nsplit,
+                              unsigned long long *head, int *arrive, float *part, float *npart,
+                              const unsigned int *mask, int R, int T, int W, int nOR, int nOT, const float2 *projf,
+                              int ldpf, const float2 *b_f, const float *a_f, int nf, const float2 *phase_f, float *d,
+                              int *ejob, unsigned int *ecode, ParticleState *ps, cudaStream_t st) {
+    if (njobs_max <= 0) return cudaSuccess;
+    if (nOR > 8 || nsplit != fine_diff2_nsplit(nf)) return cudaErrorInvalidValue;
     const size_t smem = sizeof(float2) * 8 * kFineChunk + sizeof(float) * T * nOT * nOR +
                         sizeof(int) * T + sizeof(float) * nOR + 16;
     static size_t attr = 0;
+    static int slots = 0;
     if (smem > attr) {
         cudaError_t e = cudaFuncSetAttribute(k_fine_diff2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         attr = smem;
+        slots = 0;
     }
-    for (long long j0 = 0; j0 < njobs; j0 += 0x7fffffffLL) {
-        const long long nj = njobs - j0 < 0x7fffffffLL ? njobs - j0 : 0x7fffffffLL;
-        k_fine_diff2<<<(unsigned)nj, kFineThreads, smem, st>>>(jobs + j0, mask, R, T, W, nOR, nOT, projf, ldpf,
-                                                               b_f, a_f, nf, phase_f, d, ejob, ecode, ps);
+    if (!slots) {
+        // persistent grid: as many blocks as fit on the device at once
+        int dev = 0, nsm = 0, per = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_fine_diff2, kFineThreads, smem);
+        if (e != cudaSuccess) return e;
+        slots = std::max(1, nsm * std::max(per, 1));
     }
+    cudaError_t e = cudaMemsetAsync(head, 0, sizeof(unsigned long long), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(arrive, 0, sizeof(int) * njobs_max, st);
+    if (e != cudaSuccess) return e;
+    const long long items = njobs_max * nsplit;
+    const int grid = (int)std::min<long long>(items, slots);
+    const FineQueue qu{njobs_dev, nsplit, head, arrive, part, npart};
+    k_fine_diff2<<<grid, kFineThreads, smem, st>>>(jobs, qu, mask, R, T, W, nOR, nOT, projf, ldpf, b_f, a_f, nf,
+                                                   phase_f, d, ejob, ecode, ps);
     return cudaGetLastError();
 }
 

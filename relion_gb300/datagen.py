@@ -47,6 +47,14 @@ CONFIGS = {
                              ini_high=2.0, healpix_order=3, psi_step=-1.0, offset_range_px=6.0,
                              offset_step_px=1.0, diameter=200.0, classes=1, current_size=256,
                              coarse_size=48),
+    # the late-iteration shape at box 128 (current size 128, coarse 32,
+    # HEALPix order 2, psi 30 deg): a few GB on the device, for profiler
+    # captures of the fine pass, weighted sums and backprojection
+    "cfg1_box128_late": dict(box=128, pixel=1.0, n_particles=20000, n_blobs=2000, blob_sigma=1.5,
+                             blob_radius=45.0, max_shift=3.0, defocus=(8000.0, 25000.0), snr=0.03,
+                             ini_high=2.0, healpix_order=2, psi_step=30.0, offset_range_px=6.0,
+                             offset_step_px=1.0, diameter=100.0, classes=1, current_size=128,
+                             coarse_size=32),
     "cfg4_box256_K4": dict(box=256, pixel=1.0, n_particles=50000, n_blobs=4000, blob_sigma=1.5,
                            blob_radius=90.0, max_shift=3.0, defocus=(8000.0, 25000.0), snr=0.03,
                            ini_high=20.0, healpix_order=3, psi_step=-1.0, offset_range_px=6.0,
