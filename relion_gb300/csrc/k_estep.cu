@@ -1129,10 +1129,11 @@ k_fine_diff2(const FineJob *__restrict__ jobs, const FineQueue qu, const unsigne
 //                       reference forms it per translation)
 //   backprojection:     img += C Minv Xn Phi,  weight += W C^2 Minv
 // (the per-translation sums of :8562-8780 rewritten with Phi).
-// Blocks cover (job, chunk of kWsumPix fine pixels), one thread per pixel
+// Blocks cover (job, chunk of kWsumPix x kWsumPer fine pixels), a thread per pixel at a time
 // for all oversampled orientations, so each phase value is loaded once.
 // ---------------------------------------------------------------------------
 constexpr int kWsumPix = 128;
+constexpr int kWsumPer = 4;
 constexpr int kMaxOR = 8;
 
 __global__ void __launch_bounds__(kWsumPix) k_wsum(WsumArgs a) {
@@ -1233,8 +1234,11 @@ __global__ void __launch_bounds__(kWsumPix) k_wsum(WsumArgs a) {
         }
     }
     const int nrz = nnz;
-    const int k = blockIdx.y * kWsumPix + threadIdx.x;
     double l_xa = 0., l_aa = 0.;
+    // kWsumPer pixels per thread: the job's weights, compaction and sums
+    // above are made once per kWsumPer x kWsumPix pixels
+    for (int sub = 0; sub < kWsumPer; ++sub) {
+    const int k = (blockIdx.y * kWsumPer + sub) * kWsumPix + threadIdx.x;
     if (k < a.nf) {
         const float2 x = a.Xf[(size_t)p * a.nf + k], xn = a.Xnf[(size_t)p * a.nf + k];
         const float cs = a.Cf[(size_t)p * a.nf + k] * scale;
@@ -1291,6 +1295,7 @@ __global__ void __launch_bounds__(kWsumPix) k_wsum(WsumArgs a) {
             if (first && threadIdx.x == 0) a.active[rf] = 1;
         }
         if (sh >= 0 && s2tot != 0.) atomicAdd(&shell[sh], s2tot);
+    }
     }
     if (a.do_scale) {
         l_xa = warp_sum(l_xa);
@@ -1815,7 +1820,7 @@ cudaError_t launch_wsum(const WsumArgs &a, cudaStream_t st) {
         if (e != cudaSuccess) return e;
         attr = smem;
     }
-    dim3 grid((unsigned)a.njobs, (unsigned)((a.nf + kWsumPix - 1) / kWsumPix));
+    dim3 grid((unsigned)a.njobs, (unsigned)((a.nf + kWsumPix * kWsumPer - 1) / (kWsumPix * kWsumPer)));
     k_wsum<<<grid, kWsumPix, smem, st>>>(a);
     return cudaGetLastError();
 }
