@@ -194,11 +194,17 @@ typedef enum {
                                  (default 2048; 0: after every pass).  Reading,
                                  replacing or reconstructing the volumes flushes
                                  first.                                               */
-    GBR_OPT_GRAPH = 11        /* 1 (default): the coarse part of a pass (up to the
+    GBR_OPT_GRAPH = 11,       /* 1 (default): the coarse part of a pass (up to the
                                  read-back of the fine job lists) is captured as
                                  a CUDA graph on the second pass of a batch size
                                  and replayed while buffers, model and settings
                                  are unchanged; 0: always launched directly      */
+    GBR_OPT_BP_DIRECT = 12    /* sparse fine pass: 1 inserts each job's weighted
+                                 slices into the backprojection's staging volumes
+                                 from the weighted-sum kernel (no per-orientation
+                                 slice sums; pays when particles share few
+                                 orientations, late iterations); 0 (default) sums
+                                 slices per orientation first                    */
 } gbr_worker_option;
 int gbr_worker_set_option(gbr_worker *w, int option, int64_t value);
 

@@ -3,15 +3,17 @@
 The reference fixes its kernels' block sizes and schedules at compile time
 (src/acc/cuda/cuda_settings.h); here the choices that depend on the shape of
 an iteration -- the coarse tensor-core kernel's tile-order group and its
-one-SM or SM-pair form, the fine pass as sparse jobs or dense contractions --
-are measured on the iteration's first batch and the fastest kept.
+one-SM or SM-pair form, the fine pass as sparse jobs or dense contractions,
+the sparse pass's slices summed per orientation before the backprojection or
+inserted directly -- are measured on the iteration's first batch and the
+fastest kept.
 
 Each choice is timed on its own stage (CUDA events of the worker's stages):
 the coarse-kernel candidates on the cross-term stage, the fine-pass forms on
 the stages they run (fine diff2, fine weights, weighted sums,
 backprojection; the dense form runs only where its arrays fit the device
 budget, otherwise the library keeps the sparse one).  The coarse candidates
-give bit-identical results; the two fine-pass forms agree to FP32 rounding.
+give bit-identical results; the fine-pass forms agree to FP32 rounding.
 Tuning runs the E-step on the batch, which adds to the bundle's weighted
 sums and volumes: tune() therefore clears them afterwards
 (gbr_bundle_reset_wsum), so it belongs at the start of an iteration, before
@@ -23,7 +25,8 @@ from .estep import STAGES
 
 # candidate settings, each a dict of worker options
 COARSE_CANDIDATES = [dict(tile_group=g, pair=p) for p in (0, 1) for g in (16, 24, 32, 48)]
-FINE_CANDIDATES = [dict(fine_mode="sparse"), dict(fine_mode="dense")]
+FINE_CANDIDATES = [dict(fine_mode="sparse", bp_direct=0), dict(fine_mode="sparse", bp_direct=1),
+                   dict(fine_mode="dense", bp_direct=0)]
 COARSE_STAGES = ("cross_gemm",)
 FINE_STAGES = ("diff2_fine", "weights_fine", "wsum", "backproject")
 

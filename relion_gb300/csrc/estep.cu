@@ -332,6 +332,8 @@ struct gbr_worker {
     DevBuf<unsigned char> ytp;  // per-particle BF16 Y tiles of the restricted pass
     int batch_cap = 0;           // particles per pass (GBR_OPT_BATCH_CAP; 0 = from the budget)
     int bp_flush = kBpFlushDefault;  // flush the staging volumes at this many particles (GBR_OPT_BP_FLUSH)
+    int bp_direct = 0;    // sparse fine pass: weighted slices inserted by the weighted sums (GBR_OPT_BP_DIRECT)
+    int last_direct = 0;  // the last pass inserted its slices directly
     // CUDA graph of the coarse segment (run_coarse; GBR_OPT_GRAPH)
     int use_graph = 1;
     cudaGraphExec_t gexec = nullptr;
@@ -803,6 +805,14 @@ int fine_sparse(gbr_worker *w, int n, long long njobs, long long nfine, const st
     wa.pdf_dir = b->w_pdf_dir.p; wa.pdf_cls = b->w_pdf_cls.p;
     wa.class_prior = b->is2d ? b->class_prior.p : nullptr;
     wa.w_prior_off = b->is2d ? b->w_prior_off.p : nullptr;
+    // direct insertion of each job's weighted slices into the staging volumes
+    wa.bp_direct = w->bp_direct;
+    wa.eul_f = b->eul_f.p;
+    wa.stage = b->bps_ptrs.p;
+    wa.bg = b->bg;
+    wa.circ = b->use_circ ? b->bcirc_f.p : nullptr;
+    wa.cmask = b->use_circ ? b->bmask_f.p : nullptr;
+    w->last_direct = w->bp_direct;
     GBR_CUDA(launch_wsum(wa, st));
     w->launches += 3;
     return GBR_OK;
@@ -1240,6 +1250,7 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
     w->last_dense = dense ? 1 : 0;
     long long max_seg = 0;
     if (dense) {
+        w->last_direct = 0;  // the dense form fills the slice accumulators
         s = fine_dense(w, n, max_seg);
     } else {
         const long long fine_cap = std::min<long long>(0x7fffffffLL, b->budget ? (long long)b->budget / 24 : (2LL << 30));
@@ -1250,14 +1261,18 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
     }
     if (s) return s;
     GBR_CUDA(cudaEventRecord(w->ev[8], st));
-    // ---- backprojection of the touched slices ----
-    GBR_CUDA(w->act_list.reserve(b->RF));
-    GBR_CUDA(w->act_count.reserve(1));
-    GBR_CUDA(cudaMemsetAsync(w->act_count.p, 0, sizeof(int), st));
-    GBR_CUDA(launch_compact_flags(b->active.p, (int)b->RF, w->act_list.p, w->act_count.p, st));
-    GBR_CUDA(launch_backproject(w->act_list.p, w->act_count.p, (int)b->RF, b->eul_f.p, nOR, b->cls_of_r.p,
-                                b->bpimg.p, b->bpw.p, b->pf.p, b->nf, b->bg, b->bps_ptrs.p, b->active.p, st,
-                                b->use_circ ? b->bcirc_f.p : nullptr, b->use_circ ? b->bmask_f.p : nullptr));
+    // ---- backprojection of the touched slices (already inserted by the
+    // weighted sums in the direct form) ----
+    if (!w->last_direct) {
+        GBR_CUDA(w->act_list.reserve(b->RF));
+        GBR_CUDA(w->act_count.reserve(1));
+        GBR_CUDA(cudaMemsetAsync(w->act_count.p, 0, sizeof(int), st));
+        GBR_CUDA(launch_compact_flags(b->active.p, (int)b->RF, w->act_list.p, w->act_count.p, st));
+        GBR_CUDA(launch_backproject(w->act_list.p, w->act_count.p, (int)b->RF, b->eul_f.p, nOR, b->cls_of_r.p,
+                                    b->bpimg.p, b->bpw.p, b->pf.p, b->nf, b->bg, b->bps_ptrs.p, b->active.p, st,
+                                    b->use_circ ? b->bcirc_f.p : nullptr, b->use_circ ? b->bmask_f.p : nullptr));
+        w->launches += 2;
+    }
     // the FP32 staging volumes are added into the FP64 volumes once they hold
     // bp_flush particles (and before anything reads the FP64 volumes)
     b->staged += n;
@@ -1268,7 +1283,6 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
         w->launches += (int)b->K;
     }
     GBR_CUDA(cudaEventRecord(w->ev[9], st));
-    w->launches += 2;
     // ---- results ----
     GBR_CUDA(w->h_ps.reserve(n));
     GBR_CUDA(w->h_shell.reserve((size_t)n * b->nshell));
@@ -1569,6 +1583,10 @@ int gbr_worker_set_option(gbr_worker *w, int option, int64_t value) {
             w->tc_tune.pair = (int)value;
             break;
         case GBR_OPT_BP_FLUSH: w->bp_flush = (int)value; break;
+        case GBR_OPT_BP_DIRECT:
+            if (value > 1) return fail(GBR_ERR_INVALID, "bp_direct must be 0 or 1");
+            w->bp_direct = (int)value;
+            break;
         case GBR_OPT_GRAPH:
             if (value > 1) return fail(GBR_ERR_INVALID, "graph must be 0 or 1");
             w->use_graph = (int)value;

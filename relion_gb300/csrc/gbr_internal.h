@@ -264,6 +264,14 @@ struct WsumArgs {
     double *pdf_cls;           // [K]
     const double *class_prior; // [K][2] 2D classification: per-class offset prior, else null
     double *w_prior_off;       // [K][2] 2D: sum w pixel (old offset + shift), else null
+    // direct insertion (bp_direct): each job's weighted slices go straight
+    // into the staging volumes (no slice accumulators, no backprojection pass)
+    int bp_direct;
+    const float *eul_f;        // [R*nOR][9]
+    float4 *const *stage;      // [K] staging volumes
+    VolGeom bg;
+    const int *circ;           // [nf] r_max-circle pixel bit, -1 off the circle (or null)
+    const unsigned long long *cmask;  // [R*nOR] circle pixels inserted per slice (or null)
 };
 cudaError_t launch_wsum(const WsumArgs &a, cudaStream_t st);
 // Image preparation (getFourierTransformsAndCtfs) of n real-space images of

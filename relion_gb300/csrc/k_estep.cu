@@ -1120,6 +1120,55 @@ k_fine_diff2(const FineJob *__restrict__ jobs, const FineQueue qu, const unsigne
     }
 }
 
+// One slice pixel's trilinear (3D) or bilinear (2D) insertion: value val,
+// weight w, pixel (px, py), rotation Ai.
+__device__ __forceinline__ void bp_insert(const float *Ai, int px, int py, float2 val, float w, const VolGeom &g,
+                                          float4 *sv) {
+    float xp = fmaf(Ai[0], (float)px, Ai[1] * (float)py);
+    float yp = fmaf(Ai[3], (float)px, Ai[4] * (float)py);
+    if (g.dim == 2) {
+        // BackProjector::backrotate2D (src/backprojector.cpp:471-660):
+        // bilinear insertion into the 2D data / weight planes
+        if (xp < 0.f) {
+            xp = -xp;
+            yp = -yp;
+            val.y = -val.y;
+        }
+        const float fx0 = floorf(xp), fy0 = floorf(yp);
+        const float fx = xp - fx0, fy = yp - fy0;
+        const int x0 = (int)fx0, y0 = (int)fy0 - g.yinit;
+        if (x0 < 0 || x0 + 1 >= g.xdim || y0 < 0 || y0 + 1 >= g.ydim) return;
+        const float mfx = 1.f - fx, mfy = 1.f - fy;
+        const float d4[4] = {mfy * mfx, mfy * fx, fy * mfx, fy * fx};
+        const size_t base = (size_t)y0 * g.xdim + x0;
+        const size_t off4[4] = {0, 1, (size_t)g.xdim, (size_t)g.xdim + 1};
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+            atomicAdd(&sv[base + off4[c]], make_float4(d4[c] * val.x, d4[c] * val.y, d4[c] * w, 0.f));
+        return;
+    }
+    float zp = fmaf(Ai[6], (float)px, Ai[7] * (float)py);
+    if (xp < 0.f) {
+        xp = -xp;
+        yp = -yp;
+        zp = -zp;
+        val.y = -val.y;
+    }
+    const float fx0 = floorf(xp), fy0 = floorf(yp), fz0 = floorf(zp);
+    const float fx = xp - fx0, fy = yp - fy0, fz = zp - fz0;
+    const int x0 = (int)fx0, y0 = (int)fy0 - g.yinit, z0 = (int)fz0 - g.zinit;
+    if (x0 < 0 || x0 + 1 >= g.xdim || y0 < 0 || y0 + 1 >= g.ydim || z0 < 0 || z0 + 1 >= g.zdim) return;
+    const float mfx = 1.f - fx, mfy = 1.f - fy, mfz = 1.f - fz;
+    const float dd[8] = {mfz * mfy * mfx, mfz * mfy * fx, mfz * fy * mfx, mfz * fy * fx,
+                         fz * mfy * mfx,  fz * mfy * fx,  fz * fy * mfx,  fz * fy * fx};
+    const size_t sy = (size_t)g.xdim, sz = (size_t)g.xdim * g.ydim;
+    const size_t base = (size_t)z0 * sz + (size_t)y0 * sy + x0;
+    const size_t off[8] = {0, 1, sy, sy + 1, sz, sz + 1, sz + sy, sz + sy + 1};
+#pragma unroll
+    for (int c = 0; c < 8; ++c)
+        atomicAdd(&sv[base + off[c]], make_float4(dd[c] * val.x, dd[c] * val.y, dd[c] * w, 0.f));
+}
+
 // ---------------------------------------------------------------------------
 // storeWeightedSums for one job (particle p, coarse orientation r): for each
 // oversampled orientation, the significant fine weights (w >= thr_fine,
@@ -1144,6 +1193,7 @@ __global__ void __launch_bounds__(kWsumPix) k_wsum(WsumArgs a) {
     int *rlist = tlist + a.T;                                       // [rows] rows with a significant weight
     __shared__ double red[6];  // sumw, sigma2_offset, XA, AA, 2D class offset sums x / y
     __shared__ int wcount[kWsumPix / 32], nnz;
+    __shared__ float Aj[kMaxOR][9];  // direct insertion: the job's slice rotations
     const FineJob job = a.jobs[blockIdx.x];
     const int p = job.p, r = job.r, n_t = job.n_t;
     const int nOR = a.nOR, nOT = a.nOT;
@@ -1168,6 +1218,8 @@ __global__ void __launch_bounds__(kWsumPix) k_wsum(WsumArgs a) {
     }
     if (threadIdx.x < 6) red[threadIdx.x] = 0.;
     if (threadIdx.x == 0) nnz = 0;
+    if (a.bp_direct && threadIdx.x < nOR * 9)
+        Aj[threadIdx.x / 9][threadIdx.x % 9] = a.eul_f[((size_t)r * nOR + threadIdx.x / 9) * 9 + threadIdx.x % 9];
     for (int i = threadIdx.x; i < a.nshell; i += blockDim.x) shell[i] = 0.;
     __syncthreads();
     // 2D classification: the offset prior is the class's (:8449-8456)
@@ -1287,6 +1339,18 @@ __global__ void __launch_bounds__(kWsumPix) k_wsum(WsumArgs a) {
                 l_aa += (double)W[ior] * cs * cs * (pv[ior].x * pv[ior].x + pv[ior].y * pv[ior].y);
             }
             const float wgt = W[ior] * cs * cs * minv;
+            if (a.bp_direct) {
+                // the backprojection's pixel tests (k_backproject), then the
+                // trilinear insertion of this slice pixel
+                if (!(wgt > 0.f)) continue;
+                const int px = a.pf[k].x, py = a.pf[k].y;
+                const int rr = (int)lrintf((float)a.bg.r_max * a.bg.pad);
+                if (a.bg.pad * a.bg.pad * (px * px + py * py) > rr * rr) continue;
+                const int cb = a.circ ? a.circ[k] : -1;
+                if (cb >= 0 && !((a.cmask[rf] >> cb) & 1ull)) continue;
+                bp_insert(Aj[ior], px, py, make_float2(f * zn.x, f * zn.y), wgt, a.bg, a.stage[ic]);
+                continue;
+            }
             if (wgt != 0.f || f != 0.f) {
                 atomicAdd(&a.bpimg[rf * a.nf + k].x, f * zn.x);
                 atomicAdd(&a.bpimg[rf * a.nf + k].y, f * zn.y);
@@ -1335,55 +1399,6 @@ __global__ void k_compact_flags(const unsigned char *__restrict__ flags, int n, 
         const int pos = atomicAdd(count, 1);
         list[pos] = i;
     }
-}
-
-// One slice pixel's trilinear (3D) or bilinear (2D) insertion: value val,
-// weight w, pixel (px, py), rotation Ai.
-__device__ __forceinline__ void bp_insert(const float *Ai, int px, int py, float2 val, float w, const VolGeom &g,
-                                          float4 *sv) {
-    float xp = fmaf(Ai[0], (float)px, Ai[1] * (float)py);
-    float yp = fmaf(Ai[3], (float)px, Ai[4] * (float)py);
-    if (g.dim == 2) {
-        // BackProjector::backrotate2D (src/backprojector.cpp:471-660):
-        // bilinear insertion into the 2D data / weight planes
-        if (xp < 0.f) {
-            xp = -xp;
-            yp = -yp;
-            val.y = -val.y;
-        }
-        const float fx0 = floorf(xp), fy0 = floorf(yp);
-        const float fx = xp - fx0, fy = yp - fy0;
-        const int x0 = (int)fx0, y0 = (int)fy0 - g.yinit;
-        if (x0 < 0 || x0 + 1 >= g.xdim || y0 < 0 || y0 + 1 >= g.ydim) return;
-        const float mfx = 1.f - fx, mfy = 1.f - fy;
-        const float d4[4] = {mfy * mfx, mfy * fx, fy * mfx, fy * fx};
-        const size_t base = (size_t)y0 * g.xdim + x0;
-        const size_t off4[4] = {0, 1, (size_t)g.xdim, (size_t)g.xdim + 1};
-#pragma unroll
-        for (int c = 0; c < 4; ++c)
-            atomicAdd(&sv[base + off4[c]], make_float4(d4[c] * val.x, d4[c] * val.y, d4[c] * w, 0.f));
-        return;
-    }
-    float zp = fmaf(Ai[6], (float)px, Ai[7] * (float)py);
-    if (xp < 0.f) {
-        xp = -xp;
-        yp = -yp;
-        zp = -zp;
-        val.y = -val.y;
-    }
-    const float fx0 = floorf(xp), fy0 = floorf(yp), fz0 = floorf(zp);
-    const float fx = xp - fx0, fy = yp - fy0, fz = zp - fz0;
-    const int x0 = (int)fx0, y0 = (int)fy0 - g.yinit, z0 = (int)fz0 - g.zinit;
-    if (x0 < 0 || x0 + 1 >= g.xdim || y0 < 0 || y0 + 1 >= g.ydim || z0 < 0 || z0 + 1 >= g.zdim) return;
-    const float mfx = 1.f - fx, mfy = 1.f - fy, mfz = 1.f - fz;
-    const float dd[8] = {mfz * mfy * mfx, mfz * mfy * fx, mfz * fy * mfx, mfz * fy * fx,
-                         fz * mfy * mfx,  fz * mfy * fx,  fz * fy * mfx,  fz * fy * fx};
-    const size_t sy = (size_t)g.xdim, sz = (size_t)g.xdim * g.ydim;
-    const size_t base = (size_t)z0 * sz + (size_t)y0 * sy + x0;
-    const size_t off[8] = {0, 1, sy, sy + 1, sz, sz + 1, sz + sy, sz + sy + 1};
-#pragma unroll
-    for (int c = 0; c < 8; ++c)
-        atomicAdd(&sv[base + off[c]], make_float4(dd[c] * val.x, dd[c] * val.y, dd[c] * w, 0.f));
 }
 
 // Trilinear insertion of the accumulated 2D slices of the active fine

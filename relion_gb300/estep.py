@@ -208,7 +208,7 @@ ALL_BLOCKS = -2
 
 # gbr_worker_set_option selectors (include/gbrelion.h, gbr_worker_option)
 WORKER_OPTIONS = dict(debug=1, fine_mode=2, coarse_rows=3, cand_cap=4, cand_buf=5, batch_cap=6, tile_group=7,
-                      keep_a=8, pair=9, bp_flush=10, graph=11)
+                      keep_a=8, pair=9, bp_flush=10, graph=11, bp_direct=12)
 FINE_MODES = dict(auto=0, dense=1, sparse=2)
 COARSE_ROWS = dict(skip=0, full=1)
 
@@ -225,7 +225,8 @@ class MlOptimiserCuda:
     collected in the FP32 staging volumes before they are added into the
     FP64 volumes; 0: after every pass) and graph (1, default: the coarse
     segment of a pass captured as a CUDA graph and replayed; 0: launched
-    directly)."""
+    directly) and bp_direct (1: the sparse fine pass inserts each job's
+    weighted slices into the staging volumes from the weighted sums)."""
 
     def __init__(self, bundle, debug=False, **options):
         self.bundle = bundle

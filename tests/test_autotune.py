@@ -26,7 +26,8 @@ class FakeBundle:
 
 
 class FakeWorker:
-    """Cross-term time by tile group / pair, fine-stage time by fine mode."""
+    """Cross-term time by tile group / pair, fine-stage time by fine mode and
+    direct slice insertion (slower weighted sums, no backprojection pass)."""
 
     def __init__(self, refuse=None):
         self.opts = {}
@@ -42,8 +43,10 @@ class FakeWorker:
         g, p = self.opts.get("tile_group", 32), self.opts.get("pair", 0)
         self.t[STAGES.index("cross_gemm")] += 6.0 + abs(g - 24) * 0.01 + 0.9 * p
         dense = self.opts.get("fine_mode") == "dense"
+        direct = self.opts.get("bp_direct", 0) == 1
         self.t[STAGES.index("diff2_fine")] += 0.5 if dense else 0.3
-        self.t[STAGES.index("wsum")] += 0.2
+        self.t[STAGES.index("wsum")] += 0.25 if direct else 0.2
+        self.t[STAGES.index("backproject")] += 0.0 if direct else 0.1
         self.t[STAGES.index("prep")] += 0.05
 
     def stage_times(self):
@@ -61,7 +64,7 @@ def test_tune_picks_fastest_per_stage_group_and_resets():
     autotune._cache.clear()
     bundle, worker = FakeBundle(), FakeWorker()
     out = autotune.tune(bundle, worker, {"n": 8}, repeats=2)
-    assert out["options"] == dict(tile_group=24, pair=0, fine_mode="sparse")
+    assert out["options"] == dict(tile_group=24, pair=0, fine_mode="sparse", bp_direct=1)
     assert worker.opts == out["options"]
     assert bundle.resets == 1
     ms = dict((tuple(sorted(o.items())), v) for o, v in out["coarse"])
@@ -90,4 +93,4 @@ def test_refused_candidate_is_skipped():
 def test_plain_path_skips_coarse_candidates():
     autotune._cache.clear()
     out = autotune.tune(FakeBundle(precision=0), FakeWorker(), {"n": 4})
-    assert out["coarse"] == [] and out["options"] == dict(fine_mode="sparse")
+    assert out["coarse"] == [] and out["options"] == dict(fine_mode="sparse", bp_direct=1)
