@@ -46,16 +46,21 @@ def stage_cost(times_before, times_after, stages, calls):
     return float(np.sum((np.asarray(times_after) - np.asarray(times_before))[idx])) / calls
 
 
-def time_candidate(worker, batch, options, stages, repeats=2, warmup=1):
+def time_candidate(worker, batch, options, stages, repeats=2, warmup=1, bail=None):
     """Set the options on the worker, run the batch warmup + repeats times
     and return the mean cost of the stages (ms per call); inf if the library
-    refuses the setting for this shape (an error status, e.g. no memory)."""
+    refuses the setting for this shape (an error status, e.g. no memory).
+    With bail (ms), a candidate whose warm-up call already costs more is not
+    repeated: the warm-up cost is returned."""
     try:
         for k, v in options.items():
             worker.set_option(k, v)
+        t_w = worker.stage_times().copy()
         for _ in range(warmup):
             worker.do_expectation_some_particles(batch)
         t0 = worker.stage_times().copy()
+        if bail is not None and warmup > 0 and stage_cost(t_w, t0, stages, warmup) > bail:
+            return stage_cost(t_w, t0, stages, warmup)
         for _ in range(repeats):
             worker.do_expectation_some_particles(batch)
     except RuntimeError:
@@ -96,7 +101,13 @@ def tune(bundle, worker, batch, repeats=2, coarse=None, fine=None, use_cache=Tru
         best_c = {}
     for k, v in best_c.items():
         worker.set_option(k, v)
-    fm = [(opts, time_candidate(worker, batch, opts, FINE_STAGES, repeats)) for opts in fine]
+    # a fine-pass form whose warm-up call costs 4x the best so far is not
+    # repeated (the dense form on a shape with few significant poses)
+    fm = []
+    for opts in fine:
+        best = min([ms for _, ms in fm], default=float("inf"))
+        fm.append((opts, time_candidate(worker, batch, opts, FINE_STAGES, repeats,
+                                        bail=4 * best if best < float("inf") else None)))
     best_f = pick(fm)[0]
     chosen = dict(best_c)
     chosen.update(best_f)
