@@ -887,6 +887,16 @@ def late_section(args, local, B=512, steps=3, warmup=3):
     dev_batch = {"n": B, "device_resident": 1}
     dev_batch.update({k: v.data_ptr() for k, v in dev_t.items()})
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    # the first call builds the iteration's projection tables (every coarse and
+    # oversampled orientation at the current size); timed on its own
+    t1 = time.time()
+    worker.do_expectation_some_particles(dev_batch)
+    torch.cuda.synchronize()
+    first_call_s = time.time() - t1
+    bundle.reset_wsum()
+    # the same per-shape choices as the headline worker
+    from relion_gb300 import autotune
+    tuned = autotune.tune(bundle, worker, dev_batch, repeats=2)
 
     def timed(call, arg):
         for _ in range(warmup):
@@ -926,9 +936,12 @@ def late_section(args, local, B=512, steps=3, warmup=3):
         "mean_nr_sign": float(np.mean(res["nr_sign"])),
         "mean_fine_poses": float(np.mean(res["n_fine"])),
         "setup_s": round(setup_s, 2),
-        "note": "projection tables of every coarse and oversampled orientation at current size 256 built once "
-                "per iteration (setup_s); the fine pass, weighted sums and backprojection grow x30 over "
-                "iteration 1, the coarse pass barely",
+        "first_call_s": round(first_call_s, 3),
+        "autotune": tuned["options"],
+        "note": "setup_s: bundle and reference upload; first_call_s: the first call, which also builds the "
+                "projection tables of every coarse and oversampled orientation at current size 256 (once per "
+                "iteration); the fine pass, weighted sums and backprojection grow x30 over iteration 1, the "
+                "coarse pass barely",
     }
     worker.close()
     bundle.close()
