@@ -548,9 +548,12 @@ def learned_section(args, ds, model, bundle, worker, batch, dev_batch, res_ex, f
                blocks_total=int(nblk), fallback_fraction=round(float(np.mean(fallback)), 4),
                scored_orientation_fraction=round(float(np.sum(scored)) / (B * nblk), 4),
                proposal_mass_median=round(float(np.median(prop.last["mass"])), 4))
-    # ---- timed learned steps: proposal + restricted E-step ----
+    # ---- timed learned steps: proposal + restricted E-step, both on the
+    # device-resident batch (the proposer reads the images in place) ----
+    fimg_dev = torch.from_numpy(np.ascontiguousarray(batch["fimg"])).to(torch.complex64).to(
+        torch.device("cuda", local))
     for _ in range(max(1, min(args.warmup, 3))):
-        worker.do_expectation_some_particles(dev_batch, blocks=prop(batch["fimg"]))
+        worker.do_expectation_some_particles(dev_batch, blocks=prop(fimg_dev))
     torch.cuda.synchronize()
     ms, prop_ms = [], []
     for _ in range(args.steps):
@@ -559,7 +562,7 @@ def learned_section(args, ds, model, bundle, worker, batch, dev_batch, res_ex, f
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         ev0.record()
         t0 = time.perf_counter()
-        blk = prop(batch["fimg"])
+        blk = prop(fimg_dev)
         prop_ms.append(1e3 * (time.perf_counter() - t0))
         res_l = worker.do_expectation_some_particles(dev_batch, blocks=blk)
         ev1.record()

@@ -511,8 +511,10 @@ int gbr_posenet_sizes(const gbr_posenet *n, int64_t *nparams, int64_t *nfeat, in
 int gbr_posenet_pixels(const gbr_posenet *n, int32_t *xy, float *minv);
 int gbr_posenet_get_params(const gbr_posenet *n, float *out);
 int gbr_posenet_set_params(gbr_posenet *n, const float *in);
-/* features [count][nfeat] of prepared images fimg (host, complex float
- * [count][current_size][current_size/2+1], the layout of gbr_particle_batch) */
+/* features [count][nfeat] of prepared images fimg (complex float
+ * [count][current_size][current_size/2+1], the layout of gbr_particle_batch;
+ * host or device memory, here and in gbr_posenet_block_probs /
+ * gbr_posenet_propose) */
 int gbr_posenet_features(gbr_posenet *n, const float *fimg, int64_t count, float *feat_out);
 /* mean loss and its gradient for given features [count][nfeat] and target
  * distributions [count][ndir] (host; each target row sums to 1) */
@@ -532,7 +534,7 @@ int gbr_posenet_train_targets(gbr_posenet *n, const float *fimg, const float *ta
                               int64_t batch, double lr, double *loss_out);
 /* probability of each block of dirs_per_block consecutive directions
  * [count][ndir / dirs_per_block] under softmax(logits / temperature), for
- * prepared images fimg [count] (host) */
+ * prepared images fimg [count] (host or device) */
 int gbr_posenet_block_probs(gbr_posenet *n, const float *fimg, int64_t count, int64_t dirs_per_block,
                             double temperature, float *out);
 /* top-m directions [count][m] (most probable first) and their probabilities */

@@ -433,12 +433,21 @@ int circle_bits(const std::vector<PixelRef> &px, long pad, long r2, std::vector<
     return nb;
 }
 
-unsigned long long circle_mask(const std::vector<PixelRef> &px, const std::vector<int> &bit, const double Ai[9],
-                               bool backproject, int r2, int sh) {
+// The pixels of a list that lie on the circle (bit >= 0), in bit order.
+std::vector<int> circle_pixels(const std::vector<int> &bit) {
+    std::vector<int> idx;
+    for (size_t j = 0; j < bit.size(); ++j)
+        if (bit[j] >= 0) idx.push_back((int)j);
+    return idx;
+}
+
+// Bit mask of the circle pixels (indices `on`) that the reference projects
+// (or inserts) for the inverse rotation Ai.
+unsigned long long circle_mask(const std::vector<PixelRef> &px, const std::vector<int> &on,
+                               const std::vector<int> &bit, const double Ai[9], bool backproject, int r2, int sh) {
     unsigned long long m = 0ull;
-    for (size_t j = 0; j < px.size(); ++j)
-        if (bit[j] >= 0 &&
-            (backproject ? ref_inserts(Ai, px[j].x, px[j].y, r2, sh) : ref_projects(Ai, px[j].x, px[j].y, r2)))
+    for (int j : on)
+        if (backproject ? ref_inserts(Ai, px[j].x, px[j].y, r2, sh) : ref_projects(Ai, px[j].x, px[j].y, r2))
             m |= 1ull << bit[j];
     return m;
 }
@@ -524,6 +533,7 @@ int build_tables(gbr_bundle *b) {
               nbb = circle_bits(b->pf_h, b->bg.pad, br2, bcf);
     if (b->use_circ && (nbc > 64 || nbf > 64 || nbb > 64))
         return fail(GBR_ERR_UNSUPPORTED, "more than 64 pixels on the r_max circle");
+    const std::vector<int> onc = circle_pixels(pcc), onf = circle_pixels(pcf), onb = circle_pixels(bcf);
     std::vector<unsigned long long> pmc(b->use_circ ? R : 0), pmf(b->use_circ ? RF : 0), bmf(b->use_circ ? RF : 0);
     const int shf = b->cur / 2 + 1;
     for (long ic = 0; ic < b->K; ++ic)
@@ -535,7 +545,7 @@ int build_tables(gbr_bundle *b) {
                     for (int c = 0; c < 3; ++c) ec[(size_t)r * 9 + a * 3 + c] = (float)(A[c * 3 + a] * d.padding_factor);
                 if (b->use_circ && nbc) {
                     ref_inverse_pad(A, (double)b->pg.pad, Ai);
-                    pmc[r] = circle_mask(b->pc_h, pcc, Ai, false, (int)pr2, 0);
+                    pmc[r] = circle_mask(b->pc_h, onc, pcc, Ai, false, (int)pr2, 0);
                 }
                 double pdf = b->pdf_dir[ic * b->ND + id];
                 if (mean != 0.) pdf /= mean;
@@ -551,9 +561,9 @@ int build_tables(gbr_bundle *b) {
                             ef[(size_t)rf * 9 + a * 3 + c] = (float)(A[c * 3 + a] * d.padding_factor);
                     if (b->use_circ && (nbf || nbb)) {
                         ref_inverse_pad(A, (double)b->pg.pad, Ai);
-                        if (nbf) pmf[rf] = circle_mask(b->pf_h, pcf, Ai, false, (int)pr2, 0);
+                        if (nbf) pmf[rf] = circle_mask(b->pf_h, onf, pcf, Ai, false, (int)pr2, 0);
                         if (b->bg.pad != b->pg.pad) ref_inverse_pad(A, (double)b->bg.pad, Ai);
-                        if (nbb) bmf[rf] = circle_mask(b->pf_h, bcf, Ai, true, (int)br2, shf);
+                        if (nbb) bmf[rf] = circle_mask(b->pf_h, onb, bcf, Ai, true, (int)br2, shf);
                     }
                     cf[rf] = (int)ic;
                 }
@@ -2339,7 +2349,8 @@ uint64_t host_mix64(uint64_t z) {
 int pn_features_dev(gbr_posenet *n, const float *fimg, int count) {
     gbr_bundle *b = n->b;
     const size_t full = (size_t)b->full_npix;
-    GBR_CUDA(cudaMemcpyAsync(n->fimg.p, fimg, sizeof(float2) * full * count, cudaMemcpyHostToDevice, n->st));
+    // host or device images (the copy's direction from the unified address)
+    GBR_CUDA(cudaMemcpyAsync(n->fimg.p, fimg, sizeof(float2) * full * count, cudaMemcpyDefault, n->st));
     GBR_CUDA(gbr::pn_power(n->fimg.p, (int)full, b->pc.p, b->nc, b->minv_c.p, count, n->pw.p, n->st));
     GBR_CUDA(gbr::pn_bin(n->pw.p, b->nc, n->bin.p, n->inv_cnt.p, n->nbins, count, n->feat.p, n->st));
     return GBR_OK;

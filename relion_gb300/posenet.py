@@ -55,14 +55,31 @@ class PoseProposer:
         p = np.ascontiguousarray(p, dtype=np.float32).reshape(self.nparams)
         check(self.lib.gbr_posenet_set_params(self.h, p.ctypes.data))
 
+    class _Images:
+        """Prepared images as the library takes them: a host array (complex64,
+        contiguous) or a CUDA tensor (complex64, contiguous; no host copy)."""
+
+        def __init__(self, fimg):
+            if hasattr(fimg, "data_ptr") and getattr(fimg, "is_cuda", False):
+                import torch
+                if fimg.dtype != torch.complex64 or not fimg.is_contiguous():
+                    raise ValueError("device images must be contiguous complex64")
+                self.keep, self.ptr, self.n = fimg, fimg.data_ptr(), int(fimg.shape[0])
+            else:
+                a = np.ascontiguousarray(fimg, dtype=np.complex64)
+                self.keep, self.ptr, self.n = a, a.ctypes.data, len(a)
+
+        def __len__(self):
+            return self.n
+
     @staticmethod
     def _fimg(fimg):
-        return np.ascontiguousarray(fimg, dtype=np.complex64)
+        return PoseProposer._Images(fimg)
 
     def features(self, fimg):
         f = self._fimg(fimg)
         out = np.zeros((len(f), self.nfeat), np.float32)
-        check(self.lib.gbr_posenet_features(self.h, f.ctypes.data, len(f), out.ctypes.data))
+        check(self.lib.gbr_posenet_features(self.h, f.ptr, len(f), out.ctypes.data))
         return out
 
     def loss_grad(self, feat, target):
@@ -91,7 +108,7 @@ class PoseProposer:
         if t.shape != (len(f), self.ndir):
             raise ValueError("target must be [n][ndir]")
         loss = C.c_double()
-        check(self.lib.gbr_posenet_train_targets(self.h, f.ctypes.data, t.ctypes.data, len(f), int(steps),
+        check(self.lib.gbr_posenet_train_targets(self.h, f.ptr, t.ctypes.data, len(f), int(steps),
                                                  int(min(batch, len(f), self.max_batch)), float(lr),
                                                  C.byref(loss)))
         return loss.value
@@ -101,7 +118,7 @@ class PoseProposer:
         [n][ndir / dirs_per_block] under softmax(logits / temperature)."""
         f = self._fimg(fimg)
         out = np.zeros((len(f), self.ndir // int(dirs_per_block)), np.float32)
-        check(self.lib.gbr_posenet_block_probs(self.h, f.ctypes.data, len(f), int(dirs_per_block),
+        check(self.lib.gbr_posenet_block_probs(self.h, f.ptr, len(f), int(dirs_per_block),
                                                float(temperature), out.ctypes.data))
         return out
 
@@ -110,7 +127,7 @@ class PoseProposer:
         f = self._fimg(fimg)
         idx = np.zeros((len(f), m), np.int32)
         prob = np.zeros((len(f), m), np.float32)
-        check(self.lib.gbr_posenet_propose(self.h, f.ctypes.data, len(f), int(m), idx.ctypes.data,
+        check(self.lib.gbr_posenet_propose(self.h, f.ptr, len(f), int(m), idx.ctypes.data,
                                            prob.ctypes.data))
         return idx, prob
 

@@ -64,8 +64,9 @@ def test_row_skip_matches_full_coarse_pass(seed):
         assert np.array_equal(cn[i], cf[i])
     for k in wf:
         assert _rel(wn[k], wf[k]) <= 1e-6, k
-    assert _rel(dn, df) <= 1e-6
-    assert _rel(gn, gf) <= 1e-6
+    # volumes: FP32 staging sums in atomic (run-dependent) order
+    assert _rel(dn, df) <= 1e-5
+    assert _rel(gn, gf) <= 1e-5
 
 
 @pytest.mark.parametrize("cand_cap,cand_buf", [(None, None), (16, None), (None, 8)])
@@ -86,5 +87,6 @@ def test_sparse_writes_match_full_coarse_pass(cand_cap, cand_buf):
         np.testing.assert_allclose(rn[k], rf[k], rtol=1e-9, err_msg=k)
     for k in wf:
         assert _rel(wn[k], wf[k]) <= 1e-6, k
-    assert _rel(dn, df) <= 1e-6
-    assert _rel(gn, gf) <= 1e-6
+    # volumes: FP32 staging sums in atomic (run-dependent) order
+    assert _rel(dn, df) <= 1e-5
+    assert _rel(gn, gf) <= 1e-5

@@ -149,3 +149,26 @@ def test_block_probs_and_target_training():
     assert l1 < 0.5 * l0
     net.close()
     b.close()
+
+
+def test_device_images_equal_host_images():
+    """The proposer reads prepared images in device memory in place: the
+    features, block probabilities and proposals equal those of the same
+    images passed from the host, bit for bit."""
+    _need_cuda()
+    import torch
+    from relion_gb300 import datagen
+    from relion_gb300.posenet import PoseProposer
+    ds = datagen.Dataset("cfg0_box64", seed=5, n_particles=12)
+    b = _bundle(ds, ds.model(precision=1))
+    net = PoseProposer(b, nangle=24, max_batch=8, seed=2)  # two chunks
+    fimg = np.ascontiguousarray(ds.particles(0, 12)["fimg"], dtype=np.complex64)
+    dev = torch.from_numpy(fimg).to("cuda")
+    np.testing.assert_array_equal(net.features(dev), net.features(fimg))
+    np.testing.assert_array_equal(net.block_probs(dev, 4, 1.5), net.block_probs(fimg, 4, 1.5))
+    ih, ph = net.propose(fimg, 5)
+    idv, pdv = net.propose(dev, 5)
+    np.testing.assert_array_equal(idv, ih)
+    np.testing.assert_array_equal(pdv, ph)
+    net.close()
+    b.close()

@@ -3,7 +3,8 @@ CUDA E-step of its half of a batch in its own bundle, then the one exchange
 step, combine_weighted_sums (an all-reduce over gloo ranks on host buffers,
 MlOptimiserMpi::combineAllWeightedSums), against the one-rank E-step of the
 whole batch: PMAX to 1e-9 relative, the significant-sample counts within 1,
-the summed weighted sums and volumes to 1e-6.  The runs may differ by a pose
+the summed weighted sums to 1e-6 and volumes to 1e-5 (FP32 staging sums in
+atomic order).  The runs may differ by a pose
 at the significance boundary (and so pick another of two nearly equal best
 poses): the FP64 weight sums that set the threshold are formed by atomics in
 another order.  The two ranks'
@@ -83,5 +84,5 @@ def test_two_ranks_on_halves_equal_one_rank(tmp_path):
         for k in KEYS:
             a, b = np.ravel(z["ws_" + k]), np.ravel(np.asarray(ws[k]))
             assert np.linalg.norm(a - b) <= 1e-6 * max(np.linalg.norm(b), 1e-300), k
-        assert np.linalg.norm(z["d"] - bd) <= 1e-6 * np.linalg.norm(bd)
-        assert np.linalg.norm(z["w"] - bw) <= 1e-6 * np.linalg.norm(bw)
+        assert np.linalg.norm(z["d"] - bd) <= 1e-5 * np.linalg.norm(bd)
+        assert np.linalg.norm(z["w"] - bw) <= 1e-5 * np.linalg.norm(bw)
