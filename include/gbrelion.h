@@ -493,7 +493,7 @@ typedef struct gbr_posenet gbr_posenet;
 typedef struct {
     int32_t nring;      /* rings 1..nring of the coarse image (<= coarse size / 2) */
     int32_t nangle;     /* angle bins over [0, pi) */
-    int32_t c1, c2;     /* channels of the two convolutions */
+    int32_t c1, c2;     /* channels of the two convolutions (1..32) */
     int32_t max_batch;  /* particles or training views per launch */
     int32_t reserved;
     uint64_t seed;      /* weight initialisation and training views */

@@ -2364,8 +2364,9 @@ int gbr_posenet_create(gbr_bundle *b, const gbr_posenet_desc *desc, gbr_posenet 
     int s = build_tables(b);
     if (s) return s;
     if (desc->nring < 1 || desc->nring > b->crs / 2 || desc->nangle < 5 || desc->nangle > 256 || desc->c1 < 1 ||
-        desc->c1 > 256 || desc->c2 < 1 || desc->c2 > 256 || desc->max_batch < 1 || desc->max_batch > 65536)
-        return fail(GBR_ERR_INVALID, "gbr_posenet_create: invalid sizes (nring <= coarse size / 2, nangle >= 5)");
+        desc->c1 > 32 || desc->c2 < 1 || desc->c2 > 32 || desc->max_batch < 1 || desc->max_batch > 65536)
+        return fail(GBR_ERR_INVALID,
+                    "gbr_posenet_create: invalid sizes (nring <= coarse size / 2, nangle >= 5, 1 <= c1, c2 <= 32)");
     if (b->is2d) return fail(GBR_ERR_UNSUPPORTED, "gbr_posenet_create: 2D classification has one direction");
     if ((size_t)desc->nring * desc->nangle * sizeof(float) > 48 * 1024 || b->ND > 8192)
         return fail(GBR_ERR_UNSUPPORTED, "gbr_posenet_create: nring x nangle <= 12288 bins, <= 8192 directions");

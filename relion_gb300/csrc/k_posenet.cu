@@ -105,28 +105,61 @@ __global__ void k_pn_bin(const float *__restrict__ v, int npix, const int *__res
 }
 
 // out[b][co][y][x] = relu(bias[co] + sum W[co][ci][ky][kx] in[b][ci][y+ky-1][(x+kx-2) mod W])
-__global__ void k_pn_conv_fwd(const float *__restrict__ in, int Ci, const float *__restrict__ w,
-                              const float *__restrict__ bias, int Co, int H, int W, int B, float *__restrict__ out) {
+// One thread per output position (b, y, x) computes every output channel:
+// each input value is loaded once for all Co channels, the weights and
+// biases sit in shared memory (read as broadcasts).  Per channel the sum
+// runs over ci, then ky, then kx, as a one-output-per-thread form would.
+constexpr int kPnMaxCo = 32;
+
+__global__ void __launch_bounds__(256)
+k_pn_conv_fwd(const float *__restrict__ in, int Ci, const float *__restrict__ w, const float *__restrict__ bias,
+              int Co, int H, int W, int B, float *__restrict__ out) {
+    extern __shared__ float wsh[];  // [Co][Ci][KH*KW], then bias[Co]
+    const int nw = Co * Ci * KH * KW;
+    for (int j = threadIdx.x; j < nw + Co; j += blockDim.x) wsh[j] = j < nw ? w[j] : bias[j - nw];
+    __syncthreads();
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= (long long)B * Co * H * W) return;
-    const int x = (int)(i % W), y = (int)((i / W) % H), co = (int)((i / ((long long)W * H)) % Co);
-    const int b = (int)(i / ((long long)W * H * Co));
-    float s = bias[co];
+    if (i >= (long long)B * H * W) return;
+    const int x = (int)(i % W), y = (int)((i / W) % H), b = (int)(i / ((long long)W * H));
+    float acc[kPnMaxCo];
+#pragma unroll
+    for (int co = 0; co < kPnMaxCo; ++co) acc[co] = co < Co ? wsh[nw + co] : 0.f;
     for (int ci = 0; ci < Ci; ++ci) {
         const float *src = in + ((size_t)b * Ci + ci) * H * W;
-        const float *wk = w + ((size_t)co * Ci + ci) * KH * KW;
+        float v[KH * KW];
+        bool ok[KH];
+#pragma unroll
         for (int ky = 0; ky < KH; ++ky) {
             const int yy = y + ky - 1;
-            if (yy < 0 || yy >= H) continue;
+            ok[ky] = yy >= 0 && yy < H;
+#pragma unroll
             for (int kx = 0; kx < KW; ++kx) {
                 int xx = x + kx - 2;
                 xx += (xx < 0) ? W : 0;
                 xx -= (xx >= W) ? W : 0;
-                s += wk[ky * KW + kx] * src[yy * W + xx];
+                v[ky * KW + kx] = ok[ky] ? src[yy * W + xx] : 0.f;
             }
         }
+#pragma unroll
+        for (int co = 0; co < kPnMaxCo; ++co) {
+            if (co >= Co) break;
+            const float *wk = wsh + ((size_t)co * Ci + ci) * KH * KW;
+            float s = acc[co];
+#pragma unroll
+            for (int ky = 0; ky < KH; ++ky) {
+                if (!ok[ky]) continue;
+#pragma unroll
+                for (int kx = 0; kx < KW; ++kx) s += wk[ky * KW + kx] * v[ky * KW + kx];
+            }
+            acc[co] = s;
+        }
     }
-    out[i] = s > 0.f ? s : 0.f;
+#pragma unroll
+    for (int co = 0; co < kPnMaxCo; ++co)
+        if (co < Co) {
+            const float s = acc[co];
+            out[(((size_t)b * Co + co) * H + y) * W + x] = s > 0.f ? s : 0.f;
+        }
 }
 
 // h[b][c*H + y] = mean over x of a[b][c][y][x]
@@ -389,8 +422,10 @@ cudaError_t pn_forward(const PnDims &d, const float *params, const float *feat, 
     const int H = d.H, W = d.W, B = d.B;
     const float *w1 = params + d.o_w1, *b1 = params + d.o_b1, *w2 = params + d.o_w2, *b2 = params + d.o_b2;
     const float *w3 = params + d.o_w3, *b3 = params + d.o_b3;
-    k_pn_conv_fwd<<<nblk((long long)B * d.C1 * H * W, 256), 256, 0, st>>>(feat, 1, w1, b1, d.C1, H, W, B, a1);
-    k_pn_conv_fwd<<<nblk((long long)B * d.C2 * H * W, 256), 256, 0, st>>>(a1, d.C1, w2, b2, d.C2, H, W, B, a2);
+    if (d.C1 > kPnMaxCo || d.C2 > kPnMaxCo) return cudaErrorInvalidValue;
+    const size_t s1 = sizeof(float) * (d.C1 * 1 * KH * KW + d.C1), s2 = sizeof(float) * (d.C2 * d.C1 * KH * KW + d.C2);
+    k_pn_conv_fwd<<<nblk((long long)B * H * W, 256), 256, s1, st>>>(feat, 1, w1, b1, d.C1, H, W, B, a1);
+    k_pn_conv_fwd<<<nblk((long long)B * H * W, 256), 256, s2, st>>>(a1, d.C1, w2, b2, d.C2, H, W, B, a2);
     k_pn_pool<<<nblk((long long)B * d.C2 * H, 256), 256, 0, st>>>(a2, d.C2, H, W, B, h);
     k_pn_linear<<<nblk((long long)B * d.ND, 256), 256, 0, st>>>(h, d.C2 * H, w3, b3, d.ND, B, logits);
     return cudaGetLastError();

@@ -201,7 +201,16 @@ class BlockProposer:
     def __call__(self, fimg):
         from .estep import ALL_BLOCKS
         bp = self.block_probabilities(fimg)
-        order = np.argsort(-bp, axis=1, kind="stable")[:, :self.blocks]
+        # the `blocks` most probable blocks, most probable first: a partial
+        # selection, then a sort of the selected few (ties at the cut are
+        # broken arbitrarily; probabilities of distinct blocks rarely tie)
+        m = self.blocks
+        if m < bp.shape[1]:
+            part = np.argpartition(-bp, m - 1, axis=1)[:, :m]
+            o = np.argsort(-np.take_along_axis(bp, part, axis=1), axis=1, kind="stable")
+            order = np.take_along_axis(part, o, axis=1)
+        else:
+            order = np.argsort(-bp, axis=1, kind="stable")
         mass = np.take_along_axis(bp, order, axis=1).sum(axis=1)
         out = np.concatenate([order + c * self.per_class for c in range(self.K)], axis=1).astype(np.int32)
         fallback = mass < self.mass_threshold
