@@ -2329,6 +2329,7 @@ struct gbr_posenet {
     DevBuf<float> inv_cnt;
     DevBuf<float> pw, feat, a1, a2, h, logits, dl, d1, d2, loss, target, ctf_pool, prob;
     DevBuf<float> feat_all, target_all;  // training on particle images with given targets
+    DevBuf<float> bw_scratch;            // partial weight gradients of the convolutions
     DevBuf<int> label, idx;
     DevBuf<float2> fimg;
     ~gbr_posenet() {
@@ -2422,6 +2423,7 @@ int gbr_posenet_create(gbr_bundle *b, const gbr_posenet_desc *desc, gbr_posenet 
     fill(d.o_w3, F * d.ND, (double)F);
     GBR_CUDA(n->params.upload(p.data(), p.size()));
     GBR_CUDA(n->grad.reserve(d.nparams));
+    GBR_CUDA(n->bw_scratch.reserve(gbr::pn_backward_scratch(d)));
     GBR_CUDA(n->m.reserve(d.nparams));
     GBR_CUDA(n->v.reserve(d.nparams));
     GBR_CUDA(n->m.zero());
@@ -2517,7 +2519,7 @@ int gbr_posenet_loss_grad(gbr_posenet *n, const float *feat, const float *target
     GBR_CUDA(cudaMemcpyAsync(n->target.p, target, sizeof(float) * d.ND * count, cudaMemcpyHostToDevice, n->st));
     GBR_CUDA(gbr::pn_forward(d, n->params.p, n->feat.p, n->a1.p, n->a2.p, n->h.p, n->logits.p, n->st));
     GBR_CUDA(gbr::pn_loss_backward(d, n->params.p, n->feat.p, n->a1.p, n->a2.p, n->h.p, n->logits.p, nullptr,
-                                   n->target.p, n->dl.p, n->loss.p, n->d2.p, n->d1.p, n->grad.p, n->st));
+                                   n->target.p, n->dl.p, n->loss.p, n->d2.p, n->d1.p, n->grad.p, n->bw_scratch.p, n->st));
     std::vector<float> ls(count);
     GBR_CUDA(cudaMemcpyAsync(ls.data(), n->loss.p, sizeof(float) * count, cudaMemcpyDeviceToHost, n->st));
     GBR_CUDA(cudaMemcpyAsync(grad_out, n->grad.p, sizeof(float) * d.nparams, cudaMemcpyDeviceToHost, n->st));
@@ -2552,7 +2554,7 @@ int gbr_posenet_train(gbr_posenet *n, const float *ctf_pool, int64_t n_pool, int
         GBR_CUDA(gbr::pn_forward(d, n->params.p, n->feat.p, n->a1.p, n->a2.p, n->h.p, n->logits.p, n->st));
         GBR_CUDA(gbr::pn_loss_backward(d, n->params.p, n->feat.p, n->a1.p, n->a2.p, n->h.p, n->logits.p,
                                        n->label.p, nullptr, n->dl.p, n->loss.p, n->d2.p, n->d1.p, n->grad.p,
-                                       n->st));
+                                       n->bw_scratch.p, n->st));
         GBR_CUDA(gbr::pn_adam(n->params.p, n->grad.p, n->m.p, n->v.p, d.nparams, (float)lr, (int)n->t, n->st));
         if (k >= steps - 20) {
             GBR_CUDA(cudaMemcpyAsync(ls.data(), n->loss.p, sizeof(float) * batch, cudaMemcpyDeviceToHost, n->st));
@@ -2601,7 +2603,7 @@ int gbr_posenet_train_targets(gbr_posenet *n, const float *fimg, const float *ta
         const float *tg = n->target_all.p + (size_t)ND * s0;
         GBR_CUDA(gbr::pn_forward(d, n->params.p, f, n->a1.p, n->a2.p, n->h.p, n->logits.p, n->st));
         GBR_CUDA(gbr::pn_loss_backward(d, n->params.p, f, n->a1.p, n->a2.p, n->h.p, n->logits.p, nullptr, tg,
-                                       n->dl.p, n->loss.p, n->d2.p, n->d1.p, n->grad.p, n->st));
+                                       n->dl.p, n->loss.p, n->d2.p, n->d1.p, n->grad.p, n->bw_scratch.p, n->st));
         GBR_CUDA(gbr::pn_adam(n->params.p, n->grad.p, n->m.p, n->v.p, d.nparams, (float)lr, (int)n->t, n->st));
         if (k >= steps - 20) {
             GBR_CUDA(cudaMemcpyAsync(ls.data(), n->loss.p, sizeof(float) * batch, cudaMemcpyDeviceToHost, n->st));

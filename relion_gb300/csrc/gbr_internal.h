@@ -358,10 +358,12 @@ cudaError_t pn_bin(const float *v, int npix, const int *bin, const float *inv_cn
                    cudaStream_t st);
 cudaError_t pn_forward(const PnDims &d, const float *params, const float *feat, float *a1, float *a2, float *h,
                        float *logits, cudaStream_t st);
+// scratch of pn_loss_backward: pn_backward_scratch(d) floats
+size_t pn_backward_scratch(const PnDims &d);
 cudaError_t pn_loss_backward(const PnDims &d, const float *params, const float *feat, const float *a1,
                              const float *a2, const float *h, const float *logits, const int *label,
                              const float *target, float *dl, float *loss, float *d2, float *d1, float *grad,
-                             cudaStream_t st);
+                             float *scratch, cudaStream_t st);
 cudaError_t pn_adam(float *p, const float *g, float *m, float *v, long long n, float lr, int t, cudaStream_t st);
 cudaError_t pn_topm(const float *logits, int N, int M, int B, int *idx, float *prob, cudaStream_t st);
 cudaError_t pn_block_probs(const float *logits, int N, int dpb, float temperature, int B, float *out,

@@ -256,70 +256,139 @@ __global__ void k_pn_linear_bwd_x(const float *__restrict__ dl, const float *__r
     for (int x = 0; x < W; ++x) db[x] = ab[x] > 0.f ? s : 0.f;
 }
 
-// Weight gradient of a convolution: one block per (co, ci, ky, kx), blocks
-// Co*Ci*KH*KW .. +Co hold the bias gradients.
-__global__ void k_pn_conv_bwd_w(const float *__restrict__ in, int Ci, const float *__restrict__ d, int Co, int H,
-                                int W, int B, float *__restrict__ dw, float *__restrict__ db) {
-    __shared__ float sh[32];
-    const int nw = Co * Ci * KH * KW;
-    const int k = blockIdx.x;
-    const long long tot = (long long)B * H * W;
-    float s = 0.f;
-    if (k < nw) {
-        const int kx = k % KW, ky = (k / KW) % KH, ci = (k / (KW * KH)) % Ci, co = k / (KW * KH * Ci);
-        for (long long e = threadIdx.x; e < tot; e += blockDim.x) {
-            const int x = (int)(e % W), y = (int)((e / W) % H), b = (int)(e / ((long long)W * H));
-            const int yy = y + ky - 1;
-            if (yy < 0 || yy >= H) continue;
-            int xx = x + kx - 2;
-            xx += (xx < 0) ? W : 0;
-            xx -= (xx >= W) ? W : 0;
-            s += d[(((size_t)b * Co + co) * H + y) * W + x] * in[(((size_t)b * Ci + ci) * H + yy) * W + xx];
-        }
-    } else {
-        const int co = k - nw;
-        for (long long e = threadIdx.x; e < tot; e += blockDim.x) {
-            const int x = (int)(e % W), y = (int)((e / W) % H), b = (int)(e / ((long long)W * H));
-            s += d[(((size_t)b * Co + co) * H + y) * W + x];
+// Weight and bias gradients of a convolution, in two deterministic steps:
+// block k of k_pn_conv_bwd_w_part accumulates, for particles k, k + grid, ...,
+// every gradient entry (co, ci, ky, kx), then the biases (co), over row
+// tiles staged in shared memory (inputs with their halo rows, output
+// gradients); thread t owns entries t, t + kBwThreads, ...  k_pn_sum_parts
+// adds the blocks' partial sums in block order.
+constexpr int kBwThreads = 1024, kBwPer = 16;  // up to 16,384 entries
+constexpr int kBwParts = 256;                 // partial-sum blocks at most
+
+__global__ void __launch_bounds__(kBwThreads)
+k_pn_conv_bwd_w_part(const float *__restrict__ in, int Ci, const float *__restrict__ d, int Co, int H, int W, int B,
+                     int rows, float *__restrict__ part) {
+    extern __shared__ float bsm[];
+    float *sin = bsm;                           // [Ci][rows + 2][W]
+    float *sd = bsm + (size_t)Ci * (rows + 2) * W;  // [Co][rows][W]
+    const int nw = Co * Ci * KH * KW, nent = nw + Co;
+    float acc[kBwPer];
+#pragma unroll
+    for (int j = 0; j < kBwPer; ++j) acc[j] = 0.f;
+    for (int b = blockIdx.x; b < B; b += gridDim.x) {
+        for (int y0 = 0; y0 < H; y0 += rows) {
+            const int ry = min(rows, H - y0);
+            __syncthreads();  // the previous tile's readers are done
+            for (int i = threadIdx.x; i < Ci * (ry + 2) * W; i += blockDim.x) {
+                const int x = i % W, yy = (i / W) % (ry + 2), ci = i / (W * (ry + 2));
+                const int gy = y0 + yy - 1;
+                sin[((size_t)ci * (rows + 2) + yy) * W + x] =
+                    (gy >= 0 && gy < H) ? in[(((size_t)b * Ci + ci) * H + gy) * W + x] : 0.f;
+            }
+            for (int i = threadIdx.x; i < Co * ry * W; i += blockDim.x) {
+                const int x = i % W, yy = (i / W) % ry, co = i / (W * ry);
+                sd[((size_t)co * rows + yy) * W + x] = d[(((size_t)b * Co + co) * H + y0 + yy) * W + x];
+            }
+            __syncthreads();
+#pragma unroll
+            for (int j = 0; j < kBwPer; ++j) {
+                const int e = threadIdx.x + j * kBwThreads;
+                if (e >= nent) continue;
+                float sacc = acc[j];
+                if (e < nw) {
+                    const int kx = e % KW, ky = (e / KW) % KH, ci = (e / (KW * KH)) % Ci, co = e / (KW * KH * Ci);
+                    for (int yy = 0; yy < ry; ++yy) {
+                        const float *dr = sd + ((size_t)co * rows + yy) * W;
+                        const float *ir = sin + ((size_t)ci * (rows + 2) + yy + ky) * W;
+                        for (int x = 0; x < W; ++x) {
+                            int xx = x + kx - 2;
+                            xx += (xx < 0) ? W : 0;
+                            xx -= (xx >= W) ? W : 0;
+                            sacc = fmaf(dr[x], ir[xx], sacc);
+                        }
+                    }
+                } else {
+                    const int co = e - nw;
+                    for (int yy = 0; yy < ry; ++yy) {
+                        const float *dr = sd + ((size_t)co * rows + yy) * W;
+                        for (int x = 0; x < W; ++x) sacc += dr[x];
+                    }
+                }
+                acc[j] = sacc;
+            }
         }
     }
-    s = block_reduce(s, sh, false);
-    if (threadIdx.x == 0) {
-        if (k < nw)
-            dw[k] = s;
-        else
-            db[k - nw] = s;
+#pragma unroll
+    for (int j = 0; j < kBwPer; ++j) {
+        const int e = threadIdx.x + j * kBwThreads;
+        if (e < nent) part[(size_t)blockIdx.x * nent + e] = acc[j];
     }
 }
 
-// Input gradient of a convolution through the ReLU of its input a:
-// din[b][ci][y][x] = (a > 0) * sum d[b][co][y-ky+1][(x-kx+2) mod W] W[co][ci][ky][kx]
-__global__ void k_pn_conv_bwd_x(const float *__restrict__ d, int Co, const float *__restrict__ w, int Ci, int H,
-                                int W, int B, const float *__restrict__ a, float *__restrict__ din) {
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= (long long)B * Ci * H * W) return;
-    if (!(a[i] > 0.f)) {
-        din[i] = 0.f;
-        return;
-    }
-    const int x = (int)(i % W), y = (int)((i / W) % H), ci = (int)((i / ((long long)W * H)) % Ci);
-    const int b = (int)(i / ((long long)W * H * Ci));
+__global__ void k_pn_sum_parts(const float *__restrict__ part, int nparts, int nw, int nent, float *__restrict__ dw,
+                               float *__restrict__ db) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nent) return;
     float s = 0.f;
+    for (int k = 0; k < nparts; ++k) s += part[(size_t)k * nent + e];
+    if (e < nw)
+        dw[e] = s;
+    else
+        db[e - nw] = s;
+}
+
+// Input gradient of a convolution through the ReLU of its input
+// activation: one thread per input position (b, y, x) computes every input
+// channel, the weights in shared memory; din = 0 where a <= 0.
+__global__ void __launch_bounds__(256)
+k_pn_conv_bwd_x(const float *__restrict__ d, int Co, const float *__restrict__ w, int Ci, int H, int W, int B,
+                const float *__restrict__ a, float *__restrict__ din) {
+    extern __shared__ float wsx[];  // [Co][Ci][KH*KW]
+    const int nw = Co * Ci * KH * KW;
+    for (int j = threadIdx.x; j < nw; j += blockDim.x) wsx[j] = w[j];
+    __syncthreads();
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)B * H * W) return;
+    const int x = (int)(i % W), y = (int)((i / W) % H), b = (int)(i / ((long long)W * H));
+    float acc[kPnMaxCo];
+#pragma unroll
+    for (int ci = 0; ci < kPnMaxCo; ++ci) acc[ci] = 0.f;
     for (int co = 0; co < Co; ++co) {
         const float *src = d + ((size_t)b * Co + co) * H * W;
-        const float *wk = w + ((size_t)co * Ci + ci) * KH * KW;
+        float v[KH * KW];
+        bool ok[KH];
+#pragma unroll
         for (int ky = 0; ky < KH; ++ky) {
             const int yy = y - ky + 1;
-            if (yy < 0 || yy >= H) continue;
+            ok[ky] = yy >= 0 && yy < H;
+#pragma unroll
             for (int kx = 0; kx < KW; ++kx) {
                 int xx = x - kx + 2;
                 xx += (xx < 0) ? W : 0;
                 xx -= (xx >= W) ? W : 0;
-                s += wk[ky * KW + kx] * src[yy * W + xx];
+                v[ky * KW + kx] = ok[ky] ? src[yy * W + xx] : 0.f;
             }
         }
+#pragma unroll
+        for (int ci = 0; ci < kPnMaxCo; ++ci) {
+            if (ci >= Ci) continue;
+            const float *wk = wsx + ((size_t)co * Ci + ci) * KH * KW;
+            float s = acc[ci];
+#pragma unroll
+            for (int ky = 0; ky < KH; ++ky) {
+                if (!ok[ky]) continue;
+#pragma unroll
+                for (int kx = 0; kx < KW; ++kx) s += wk[ky * KW + kx] * v[ky * KW + kx];
+            }
+            acc[ci] = s;
+        }
     }
-    din[i] = s;
+#pragma unroll
+    for (int ci = 0; ci < kPnMaxCo; ++ci)
+        if (ci < Ci) {
+            const size_t o = (((size_t)b * Ci + ci) * H + y) * W + x;
+            din[o] = a[o] > 0.f ? acc[ci] : 0.f;
+        }
 }
 
 // Adam (Kingma & Ba 2015) with bias corrections c1 = 1 - beta1^t, c2 = 1 - beta2^t.
@@ -431,21 +500,48 @@ cudaError_t pn_forward(const PnDims &d, const float *params, const float *feat, 
     return cudaGetLastError();
 }
 
+size_t pn_backward_scratch(const PnDims &d) {
+    return (size_t)kBwParts * (d.C2 * d.C1 * KH * KW + d.C2);
+}
+
+// weight / bias gradients of one convolution (partials, then their sum)
+static cudaError_t conv_bwd_w(const float *in, int Ci, const float *dd, int Co, int H, int W, int B, float *dw,
+                              float *db, float *scratch, cudaStream_t st) {
+    const int nent = Co * Ci * KH * KW + Co;
+    if (nent > kBwThreads * kBwPer) return cudaErrorInvalidValue;
+    // row tile: inputs with halo and output gradients within 96 KB
+    const size_t cap = 96 * 1024 / sizeof(float);
+    int rows = (int)std::min<long long>(H, ((long long)cap / W - 2 * Ci) / (Ci + Co));
+    if (rows < 1) return cudaErrorInvalidValue;
+    const size_t smem = sizeof(float) * ((size_t)Ci * (rows + 2) + (size_t)Co * rows) * W;
+    static size_t attr = 0;
+    if (smem > attr) {
+        cudaError_t e = cudaFuncSetAttribute(k_pn_conv_bwd_w_part, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)std::max<size_t>(smem, 96 * 1024));
+        if (e != cudaSuccess) return e;
+        attr = std::max<size_t>(smem, 96 * 1024);
+    }
+    const int nparts = std::min(B, kBwParts);
+    k_pn_conv_bwd_w_part<<<nparts, kBwThreads, smem, st>>>(in, Ci, dd, Co, H, W, B, rows, scratch);
+    k_pn_sum_parts<<<nblk(nent, 256), 256, 0, st>>>(scratch, nparts, nent - Co, nent, dw, db);
+    return cudaGetLastError();
+}
+
 cudaError_t pn_loss_backward(const PnDims &d, const float *params, const float *feat, const float *a1,
                              const float *a2, const float *h, const float *logits, const int *label,
                              const float *target, float *dl, float *loss, float *d2, float *d1, float *grad,
-                             cudaStream_t st) {
+                             float *scratch, cudaStream_t st) {
     const int H = d.H, W = d.W, B = d.B, F = d.C2 * d.H;
     k_pn_xent<<<B, 256, 0, st>>>(logits, d.ND, label, target, B, dl, loss);
     k_pn_linear_bwd_w<<<nblk((long long)(F + 1) * d.ND, 256), 256, 0, st>>>(h, dl, F, d.ND, B, grad + d.o_w3,
                                                                              grad + d.o_b3);
     k_pn_linear_bwd_x<<<nblk((long long)B * F, 256), 256, 0, st>>>(dl, params + d.o_w3, F, d.ND, B, a2, W, d2);
-    k_pn_conv_bwd_w<<<d.C2 * d.C1 * KH * KW + d.C2, 256, 0, st>>>(a1, d.C1, d2, d.C2, H, W, B, grad + d.o_w2,
-                                                                   grad + d.o_b2);
-    k_pn_conv_bwd_x<<<nblk((long long)B * d.C1 * H * W, 256), 256, 0, st>>>(d2, d.C2, params + d.o_w2, d.C1, H, W,
-                                                                             B, a1, d1);
-    k_pn_conv_bwd_w<<<d.C1 * 1 * KH * KW + d.C1, 256, 0, st>>>(feat, 1, d1, d.C1, H, W, B, grad + d.o_w1,
-                                                                grad + d.o_b1);
+    cudaError_t e = conv_bwd_w(a1, d.C1, d2, d.C2, H, W, B, grad + d.o_w2, grad + d.o_b2, scratch, st);
+    if (e != cudaSuccess) return e;
+    k_pn_conv_bwd_x<<<nblk((long long)B * H * W, 256), 256, sizeof(float) * d.C2 * d.C1 * KH * KW, st>>>(
+        d2, d.C2, params + d.o_w2, d.C1, H, W, B, a1, d1);
+    e = conv_bwd_w(feat, 1, d1, d.C1, H, W, B, grad + d.o_w1, grad + d.o_b1, scratch, st);
+    if (e != cudaSuccess) return e;
     return cudaGetLastError();
 }
 
