@@ -62,6 +62,10 @@ def parse():
     ap.add_argument("--no-mstep", action="store_true", help="skip the reconstruction-side section (profiling runs)")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP32 path leg (profiling runs)")
     ap.add_argument("--no-late", action="store_true", help="skip the late-iteration section (profiling runs)")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="skip the autotuner; the worker keeps its defaults and --options (profiling runs)")
+    ap.add_argument("--options", default="{}",
+                    help="worker options as JSON (e.g. '{\"bp_direct\": 1}'), set before the autotuner")
     ap.add_argument("--workload", default=CONFIG,
                     choices=["cfg1_box256", "cfg1_box256_late", "cfg1_box128_late", "cfg4_box256_K4", "cfg3_box128_2d",
                              "cfg0_box64"],
@@ -146,7 +150,7 @@ def run_ours(args, world, rank, local):
     for k, r in enumerate(ds.refs):
         bundle.setup_projector(k, r["data"], r["yinit"], r["zinit"], r["r_max"], r["pad"])
     bundle.reserve(64 << 30)
-    worker = MlOptimiserCuda(bundle)
+    worker = MlOptimiserCuda(bundle, **json.loads(args.options))
 
     # device-resident copy of the batch (for `value`) and pinned host copy (for `e2e`)
     keys = ("fimg", "fimg_nomask", "fctf", "power_img", "old_offset", "prior", "highres_Xi2",
@@ -168,7 +172,10 @@ def run_ours(args, world, rank, local):
     # tile order, coarse-kernel form and fine-pass form picked on this batch
     # (the autotuner clears the sums its own runs added)
     from relion_gb300 import autotune
-    tuned = autotune.tune(bundle, worker, dev_batch, repeats=2)
+    if args.no_autotune:
+        tuned = {"options": json.loads(args.options), "coarse": [], "fine": [], "cached": False}
+    else:
+        tuned = autotune.tune(bundle, worker, dev_batch, repeats=2)
 
     def barrier():
         if world > 1:
