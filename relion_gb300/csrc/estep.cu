@@ -188,6 +188,8 @@ struct gbr_bundle {
     std::vector<DevBuf<float2>> vol;
     std::vector<char> have_vol;
     DevBuf<const float2 *> vols_d;
+    std::vector<gbr::VolTexture> vtex;   // 3D: array copies of the volumes for the projector's texture fetches
+    DevBuf<unsigned long long> texs_d;
     // backprojector (FP64)
     std::vector<DevBuf<double2>> bp_data;
     std::vector<DevBuf<double>> bp_weight;
@@ -618,6 +620,17 @@ int build_tables(gbr_bundle *b) {
     std::vector<const float2 *> vp(b->K);
     for (long k = 0; k < b->K; ++k) vp[k] = b->vol[k].p;
     GBR_CUDA(b->vols_d.upload(vp.data(), vp.size()));
+    const unsigned long long *texs = nullptr;
+    if (!b->is2d) {
+        b->vtex.resize(b->K);
+        std::vector<unsigned long long> th(b->K);
+        for (long k = 0; k < b->K; ++k) {
+            GBR_CUDA(gbr::vol_texture_update(b->vtex[k], b->vol[k].p, b->pg, 0));
+            th[k] = (unsigned long long)b->vtex[k].tex;
+        }
+        GBR_CUDA(b->texs_d.upload(th.data(), th.size()));
+        texs = b->texs_d.p;
+    }
     GBR_CUDA(b->proj_c.reserve((size_t)R * b->lda_c));
     GBR_CUDA(b->proj2_c.reserve((size_t)R * b->ldk_c));
     GBR_CUDA(b->proj_c.zero());
@@ -625,7 +638,7 @@ int build_tables(gbr_bundle *b) {
     GBR_CUDA(launch_project_rows(b->vols_d.p, b->pg, b->eul_c.p, b->cls_c.p, nullptr, (int)R, b->pc.p, b->nc,
                                  b->proj_c.p, b->lda_c, b->proj2_c.p, b->ldk_c, nullptr, 0,
                                  b->use_circ ? b->pcirc_c.p : nullptr, b->use_circ ? b->pmask_c.p : nullptr,
-                                 (b->crs / 2) * (b->crs / 2)));
+                                 (b->crs / 2) * (b->crs / 2), texs));
     if (d.precision == GBR_PREC_BF16) {
         GBR_CUDA(b->proj_c_tc.reserve(tc_a_bytes((int)R, 2 * b->nc)));
         GBR_CUDA(launch_tc_pack_a(b->proj_c.p, b->lda_c, (int)R, 2 * b->nc, b->proj_c_tc.p, 0));
@@ -644,7 +657,7 @@ int build_tables(gbr_bundle *b) {
     GBR_CUDA(launch_project_rows(b->vols_d.p, b->pg, b->eul_f.p, b->cls_f.p, nullptr, (int)RF, b->pf.p, b->nf,
                                  b->proj_f.p, b->lda_f, b->proj2_f.p, b->ldk_f, nullptr, 0,
                                  b->use_circ ? b->pcirc_f.p : nullptr, b->use_circ ? b->pmask_f.p : nullptr,
-                                 (b->cur / 2) * (b->cur / 2)));
+                                 (b->cur / 2) * (b->cur / 2), texs));
     // ---- slice accumulators ----
     GBR_CUDA(b->bpimg.reserve((size_t)RF * b->nf));
     GBR_CUDA(b->bpw.reserve((size_t)RF * b->nf));
@@ -2312,6 +2325,7 @@ int gbr_bundle_destroy(gbr_bundle *b) {
     if (!b) return GBR_OK;
     cudaSetDevice(b->device);
     cudaDeviceSynchronize();
+    for (gbr::VolTexture &t : b->vtex) gbr::vol_texture_release(t);
     delete b;
     return GBR_OK;
 }

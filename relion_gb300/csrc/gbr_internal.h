@@ -84,11 +84,24 @@ cudaError_t launch_phase_table(float2 *out, const double *tx, const double *ty, 
 // reference projects (Projector::project decides them in double precision).
 // rout2 >= 0: pixels with x^2 + y^2 > rout2 are zero (the output image's
 // circle, radius size / 2, as the reference fills it).
+// texs: per-class texture objects of 3D CUDA array copies of the volumes
+// (vol_texture_update; null: the linear volumes are read directly).
 cudaError_t launch_project_rows(const float2 *const *vols, const VolGeom &g, const float *eul,
                                 const int *cls, const int *orient_ids, int n_orient,
                                 const PixelRef *pix, int npix, float *out_ri, int ld, float *out_p2,
                                 int ld2, float2 *out_c, cudaStream_t st, const int *circ = nullptr,
-                                const unsigned long long *mask = nullptr, int rout2 = -1);
+                                const unsigned long long *mask = nullptr, int rout2 = -1,
+                                const unsigned long long *texs = nullptr);
+// A 3D CUDA array copy of a padded volume with a point-sampling texture
+// object on it (the projector's fetch path); updated in place when the
+// dimensions are unchanged.
+struct VolTexture {
+    cudaArray_t arr = nullptr;
+    cudaTextureObject_t tex = 0;
+    int x = 0, y = 0, z = 0;
+};
+cudaError_t vol_texture_update(VolTexture &t, const float2 *vol, const VolGeom &g, cudaStream_t st);
+void vol_texture_release(VolTexture &t);
 
 // FP32 FMA throughput probe (ms of one timed launch and its flop count).
 cudaError_t launch_fp32_probe(float *ms, double *flops);

@@ -9,7 +9,10 @@
 // filtering (src/acc/acc_projector_impl.h:65-105), whose 8-bit fixed-point
 // weights cannot hold the CPU's double result to 1e-5; this kernel
 // interpolates in FP32 in software.  Each output pixel is independent; the
-// 8 corners are read as four 16-byte (x0, x0+1) pairs from L2.
+// 8 corners of a 3D sample are fetched through the texture path from a 3D
+// CUDA array copy of the volume (point sampling: the stored values exactly;
+// the array's blocked layout keeps a cell's corners and the cells of
+// neighbouring pixels in few cache lines), or read from the linear volume.
 #include "gbr_internal.h"
 
 namespace gbr {
@@ -22,8 +25,12 @@ __device__ __forceinline__ float2 lerp2(float a, float2 l, float2 h) {
 
 // Trilinear sample of one class volume at 2D frequency (x, y) rotated by Ai.
 // Returns false if the pixel lies outside r_max (value 0 then).
+__device__ __forceinline__ float2 tex_at(cudaTextureObject_t t, int x, int y, int z) {
+    return tex3D<float2>(t, (float)x + 0.5f, (float)y + 0.5f, (float)z + 0.5f);
+}
+
 __device__ __forceinline__ float2 sample_slice(const float2 *__restrict__ vol, const VolGeom g,
-                                               const float *Ai, int x, int y) {
+                                               const float *Ai, int x, int y, cudaTextureObject_t tex = 0) {
     // Inside-radius test in integers: |Ai (x,y,0)|^2 = pad^2 (x^2+y^2).
     const int rref = g.r_max * g.pad;
     if (g.pad * g.pad * (x * x + y * y) > rref * rref) return make_float2(0.f, 0.f);
@@ -62,12 +69,28 @@ __device__ __forceinline__ float2 sample_slice(const float2 *__restrict__ vol, c
     const int z0 = (int)fz0 - g.zinit;
     if (x0 < 0 || x0 + 1 >= g.xdim || y0 < 0 || y0 + 1 >= g.ydim || z0 < 0 || z0 + 1 >= g.zdim)
         return make_float2(0.f, 0.f);
-    const size_t sy = (size_t)g.xdim, sz = (size_t)g.xdim * g.ydim;
-    const float2 *b = vol + (size_t)z0 * sz + (size_t)y0 * sy + x0;
-    const float2 d000 = __ldg(b), d001 = __ldg(b + 1);
-    const float2 d010 = __ldg(b + sy), d011 = __ldg(b + sy + 1);
-    const float2 d100 = __ldg(b + sz), d101 = __ldg(b + sz + 1);
-    const float2 d110 = __ldg(b + sz + sy), d111 = __ldg(b + sz + sy + 1);
+    float2 d000, d001, d010, d011, d100, d101, d110, d111;
+    if (tex) {
+        d000 = tex_at(tex, x0, y0, z0);
+        d001 = tex_at(tex, x0 + 1, y0, z0);
+        d010 = tex_at(tex, x0, y0 + 1, z0);
+        d011 = tex_at(tex, x0 + 1, y0 + 1, z0);
+        d100 = tex_at(tex, x0, y0, z0 + 1);
+        d101 = tex_at(tex, x0 + 1, y0, z0 + 1);
+        d110 = tex_at(tex, x0, y0 + 1, z0 + 1);
+        d111 = tex_at(tex, x0 + 1, y0 + 1, z0 + 1);
+    } else {
+        const size_t sy = (size_t)g.xdim, sz = (size_t)g.xdim * g.ydim;
+        const float2 *b = vol + (size_t)z0 * sz + (size_t)y0 * sy + x0;
+        d000 = __ldg(b);
+        d001 = __ldg(b + 1);
+        d010 = __ldg(b + sy);
+        d011 = __ldg(b + sy + 1);
+        d100 = __ldg(b + sz);
+        d101 = __ldg(b + sz + 1);
+        d110 = __ldg(b + sz + sy);
+        d111 = __ldg(b + sz + sy + 1);
+    }
     const float2 dx00 = lerp2(fx, d000, d001);
     const float2 dx01 = lerp2(fx, d100, d101);
     const float2 dx10 = lerp2(fx, d010, d011);
@@ -92,7 +115,7 @@ __global__ void k_project_rows(const float2 *const *__restrict__ vols, const Vol
                                const PixelRef *__restrict__ pix, int npix, float *__restrict__ out_ri,
                                int ld, float *__restrict__ out_p2, int ld2, float2 *__restrict__ out_c,
                                const int *__restrict__ circ, const unsigned long long *__restrict__ mask,
-                               int rout2) {
+                               int rout2, const unsigned long long *__restrict__ texs) {
     const int o = blockIdx.y;
     if (o >= n_orient) return;
     const int oid = orient_ids ? orient_ids[o] : o;
@@ -100,13 +123,14 @@ __global__ void k_project_rows(const float2 *const *__restrict__ vols, const Vol
     if (threadIdx.x < 9) Ai[threadIdx.x] = eul[(size_t)oid * 9 + threadIdx.x];
     __syncthreads();
     const float2 *vol = vols[cls[oid]];
+    const cudaTextureObject_t tex = (texs && g.dim == 3) ? (cudaTextureObject_t)texs[cls[oid]] : 0;
     const unsigned long long cm = mask ? mask[oid] : ~0ull;
     for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < npix; j += gridDim.x * blockDim.x) {
         const PixelRef pr = pix[j];
         const int cb = circ ? circ[j] : -1;
         const bool outside = rout2 >= 0 && pr.x * pr.x + pr.y * pr.y > rout2;
         const float2 v = (outside || (cb >= 0 && !((cm >> cb) & 1ull))) ? make_float2(0.f, 0.f)
-                                                                        : sample_slice(vol, g, Ai, pr.x, pr.y);
+                                                                        : sample_slice(vol, g, Ai, pr.x, pr.y, tex);
         if (out_ri) {
             float *row = out_ri + (size_t)oid * ld;
             row[2 * j] = v.x;
@@ -140,11 +164,50 @@ __global__ void k_phase_table(float2 *__restrict__ out, const double *__restrict
 
 }  // namespace
 
+cudaError_t vol_texture_update(VolTexture &t, const float2 *vol, const VolGeom &g, cudaStream_t st) {
+    if (g.dim != 3) return cudaSuccess;
+    cudaError_t e = cudaSuccess;
+    if (!t.arr || t.x != g.xdim || t.y != g.ydim || t.z != g.zdim) {
+        vol_texture_release(t);
+        const cudaChannelFormatDesc fd = cudaCreateChannelDesc<float2>();
+        e = cudaMalloc3DArray(&t.arr, &fd, make_cudaExtent(g.xdim, g.ydim, g.zdim));
+        if (e != cudaSuccess) {
+            t.arr = nullptr;
+            return e;
+        }
+        t.x = g.xdim;
+        t.y = g.ydim;
+        t.z = g.zdim;
+        cudaResourceDesc rd = {};
+        rd.resType = cudaResourceTypeArray;
+        rd.res.array.array = t.arr;
+        cudaTextureDesc td = {};
+        td.addressMode[0] = td.addressMode[1] = td.addressMode[2] = cudaAddressModeClamp;
+        td.filterMode = cudaFilterModePoint;
+        td.readMode = cudaReadModeElementType;
+        td.normalizedCoords = 0;
+        e = cudaCreateTextureObject(&t.tex, &rd, &td, nullptr);
+        if (e != cudaSuccess) return e;
+    }
+    cudaMemcpy3DParms cp = {};
+    cp.srcPtr = make_cudaPitchedPtr(const_cast<float2 *>(vol), sizeof(float2) * g.xdim, g.xdim, g.ydim);
+    cp.dstArray = t.arr;
+    cp.extent = make_cudaExtent(g.xdim, g.ydim, g.zdim);
+    cp.kind = cudaMemcpyDeviceToDevice;
+    return cudaMemcpy3DAsync(&cp, st);
+}
+
+void vol_texture_release(VolTexture &t) {
+    if (t.tex) cudaDestroyTextureObject(t.tex);
+    if (t.arr) cudaFreeArray(t.arr);
+    t = VolTexture();
+}
+
 cudaError_t launch_project_rows(const float2 *const *vols, const VolGeom &g, const float *eul,
                                 const int *cls, const int *orient_ids, int n_orient,
                                 const PixelRef *pix, int npix, float *out_ri, int ld, float *out_p2,
                                 int ld2, float2 *out_c, cudaStream_t st, const int *circ,
-                                const unsigned long long *mask, int rout2) {
+                                const unsigned long long *mask, int rout2, const unsigned long long *texs) {
     if (n_orient <= 0 || npix <= 0) return cudaSuccess;
     const int threads = 128;
     const int bx = (npix + threads - 1) / threads;
@@ -155,7 +218,7 @@ cudaError_t launch_project_rows(const float2 *const *vols, const VolGeom &g, con
                                                  n, pix, npix, out_ri ? out_ri + (orient_ids ? 0 : (size_t)o0 * ld) : nullptr,
                                                  ld, out_p2 ? out_p2 + (orient_ids ? 0 : (size_t)o0 * ld2) : nullptr,
                                                  ld2, out_c ? out_c + (orient_ids ? 0 : (size_t)o0 * npix) : nullptr,
-                                                 circ, mask, rout2);
+                                                 circ, mask, rout2, texs);
         if (!orient_ids) {
             // rows are addressed by the orientation index; shift eul/cls/mask too
             eul += (size_t)n * 9;
