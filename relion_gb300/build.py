@@ -71,7 +71,7 @@ def _build_lib(verbose, force):
         return LIB
     nvcc = _nvcc()
     flags = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
-                    "-Xcompiler", "-ffp-contract=off", "-Xptxas", "-v"]
+                    "-Xcompiler", "-ffp-contract=off", "-Xcompiler", "-fopenmp", "-Xptxas", "-v"]
 
     def one(src):
         obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
@@ -83,7 +83,7 @@ def _build_lib(verbose, force):
     with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(one, SOURCES))
     tmp = LIB + ".tmp"
-    _run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart", "-lcufft"])
+    _run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart", "-lcufft", "-lgomp"])
     os.replace(tmp, LIB)
     if verbose:
         print("built", LIB)

@@ -1340,64 +1340,99 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
         w->dbg_n += n;
     }
     // ---- per-particle finalisation (storeWeightedSums :8990-9150) ----
-    for (int p = 0; p < n; ++p) {
-        const ParticleState &ps = psh[p];
-        gbr_particle_result &o = res[p];
-        std::memset(&o, 0, sizeof(o));
-        if (!(ps.sum_fine > 0.) || !std::isfinite(ps.sum_fine))
-            return fail(GBR_ERR_NUMERICAL, "zero sum of weights for particle " + std::to_string(p));
-        const double *pd = pdat_h + (size_t)p * 8;
-        o.coarse_min_diff2 = ps.c_coarse + (double)ord2f_host(ps.min_coarse);
-        o.coarse_sum_weight = ps.sum_coarse;
-        o.coarse_significant_weight = ps.thr_coarse;
-        o.fine_min_diff2 = ps.c_fine + (double)ord2f_host(ps.min_fine);
-        o.fine_sum_weight = ps.sum_fine;
-        o.fine_significant_weight = ps.thr_fine;
-        o.nr_sign = ps.nr_sign;
-        o.n_fine = segf[p + 1] - segf[p];
-        const unsigned long long key = ps.argmax_key;
-        const unsigned long long idx = 0xFFFFFFFFull - (key & 0xFFFFFFFFull);
-        unsigned int wb = (unsigned int)(key >> 32);
-        float wmax;
-        std::memcpy(&wmax, &wb, 4);
-        const long iot = (long)(idx % nOT), t = (long)((idx / nOT) % T);
-        const long ior = (long)((idx / ((unsigned long long)nOT * T)) % nOR);
-        const long r = (long)(idx / ((unsigned long long)nOT * T * nOR));
-        const long ic = r / (b->ND * b->NP), id = (r / b->NP) % b->ND, is = r % b->NP;
-        b->grid.fine_orientation(id, is, ior, o.rot, o.tilt, o.psi);
-        o.xoff = pd[0] + b->otx_h[t * nOT + iot];
-        o.yoff = pd[1] + b->oty_h[t * nOT + iot];
-        o.cls = (double)ic + 1;
-        o.pmax = (double)wmax / ps.sum_fine;
-        o.best_ihidden_over = ((r * T + t) * nOR + ior) * nOT + iot;
-        o.dLL = std::log(ps.sum_fine) - o.fine_min_diff2 - b->logsigma2;
-        // four partial sums: no serial dependency chain through wnorm
-        double wn[4] = {0., 0., 0., 0.};
-        const double *__restrict__ sp = &shell[(size_t)p * b->nshell];
-        const double *__restrict__ pw = &power_h[(size_t)p * b->nshell];
+    // particles in contiguous ranges over a few host threads; each range
+    // adds into its own shell and scalar sums, which are then added in range
+    // order
+    const int nth = std::max(1, std::min(8, n / 96));
+    const int nsh = (int)b->nshell;
+    std::vector<double> sig_part((size_t)nth * nsh, 0.);
+    struct RangeSums {
+        double avg_norm = 0., XA = 0., AA = 0., sumw = 0., off = 0., LL = 0., pmax = 0.;
+        int bad = -1;  // first particle with a zero sum of weights
+    };
+    std::vector<RangeSums> rs(nth);
+#pragma omp parallel for num_threads(nth) schedule(static, 1)
+    for (int th = 0; th < nth; ++th) {
+        const int pa = (int)((long long)n * th / nth), pb = (int)((long long)n * (th + 1) / nth);
+        RangeSums &acc = rs[th];
+        double *__restrict__ wsig = sig_part.data() + (size_t)th * nsh;
+        for (int p = pa; p < pb; ++p) {
+            const ParticleState &ps = psh[p];
+            gbr_particle_result &o = res[p];
+            std::memset(&o, 0, sizeof(o));
+            if (!(ps.sum_fine > 0.) || !std::isfinite(ps.sum_fine)) {
+                if (acc.bad < 0) acc.bad = p;
+                continue;
+            }
+            const double *pd = pdat_h + (size_t)p * 8;
+            o.coarse_min_diff2 = ps.c_coarse + (double)ord2f_host(ps.min_coarse);
+            o.coarse_sum_weight = ps.sum_coarse;
+            o.coarse_significant_weight = ps.thr_coarse;
+            o.fine_min_diff2 = ps.c_fine + (double)ord2f_host(ps.min_fine);
+            o.fine_sum_weight = ps.sum_fine;
+            o.fine_significant_weight = ps.thr_fine;
+            o.nr_sign = ps.nr_sign;
+            o.n_fine = segf[p + 1] - segf[p];
+            const unsigned long long key = ps.argmax_key;
+            const unsigned long long idx = 0xFFFFFFFFull - (key & 0xFFFFFFFFull);
+            unsigned int wb = (unsigned int)(key >> 32);
+            float wmax;
+            std::memcpy(&wmax, &wb, 4);
+            const long iot = (long)(idx % nOT), t = (long)((idx / nOT) % T);
+            const long ior = (long)((idx / ((unsigned long long)nOT * T)) % nOR);
+            const long r = (long)(idx / ((unsigned long long)nOT * T * nOR));
+            const long ic = r / (b->ND * b->NP), id = (r / b->NP) % b->ND, is = r % b->NP;
+            b->grid.fine_orientation(id, is, ior, o.rot, o.tilt, o.psi);
+            o.xoff = pd[0] + b->otx_h[t * nOT + iot];
+            o.yoff = pd[1] + b->oty_h[t * nOT + iot];
+            o.cls = (double)ic + 1;
+            o.pmax = (double)wmax / ps.sum_fine;
+            o.best_ihidden_over = ((r * T + t) * nOR + ior) * nOT + iot;
+            o.dLL = std::log(ps.sum_fine) - o.fine_min_diff2 - b->logsigma2;
+            // four partial sums: no serial dependency chain through wnorm
+            double wn[4] = {0., 0., 0., 0.};
+            const double *__restrict__ sp = &shell[(size_t)p * nsh];
+            const double *__restrict__ pw = &power_h[(size_t)p * nsh];
+            for (int i = 0; i < nsh; ++i) {
+                wsig[i] += sp[i];
+                wn[i & 3] += sp[i];
+            }
+            for (int i = b->cur / 2 + 1; i < nsh; ++i) {
+                wsig[i] += pw[i];
+                wn[i & 3] += pw[i];
+            }
+            const double wnorm = (wn[0] + wn[1]) + (wn[2] + wn[3]);
+            o.norm = pd[5];
+            if (d.do_norm_correction) {
+                o.norm = pd[5] / d.avg_norm_correction * std::sqrt(wnorm * 2.);
+                acc.avg_norm += o.norm;
+            }
+            if (d.do_scale_correction) {
+                acc.XA += pacc[(size_t)p * 8 + 2] / pd[6];
+                acc.AA += pacc[(size_t)p * 8 + 3] / (pd[6] * pd[6]);
+            }
+            acc.sumw += pacc[(size_t)p * 8 + 0];
+            acc.off += pacc[(size_t)p * 8 + 1];
+            acc.LL += o.dLL;
+            acc.pmax += o.pmax;
+        }
+    }
+    for (int th = 0; th < nth; ++th)
+        if (rs[th].bad >= 0) return fail(GBR_ERR_NUMERICAL, "zero sum of weights for particle " + std::to_string(rs[th].bad));
+    {
         double *__restrict__ wsig = b->w_sigma2.data();
-        for (int i = 0; i < b->nshell; ++i) {
-            wsig[i] += sp[i];
-            wn[i & 3] += sp[i];
+        for (int th = 0; th < nth; ++th) {
+            const double *src = sig_part.data() + (size_t)th * nsh;
+            for (int i = 0; i < nsh; ++i) wsig[i] += src[i];
+            const RangeSums &a = rs[th];
+            b->w_avg_norm += a.avg_norm;
+            b->w_XA += a.XA;
+            b->w_AA += a.AA;
+            b->w_sumw_group += a.sumw;
+            b->w_sigma2_offset += a.off;
+            b->w_LL += a.LL;
+            b->w_ave_Pmax += a.pmax;
         }
-        for (int i = b->cur / 2 + 1; i < b->nshell; ++i) {
-            wsig[i] += pw[i];
-            wn[i & 3] += pw[i];
-        }
-        const double wnorm = (wn[0] + wn[1]) + (wn[2] + wn[3]);
-        o.norm = pd[5];
-        if (d.do_norm_correction) {
-            o.norm = pd[5] / d.avg_norm_correction * std::sqrt(wnorm * 2.);
-            b->w_avg_norm += o.norm;
-        }
-        if (d.do_scale_correction) {
-            b->w_XA += pacc[(size_t)p * 8 + 2] / pd[6];
-            b->w_AA += pacc[(size_t)p * 8 + 3] / (pd[6] * pd[6]);
-        }
-        b->w_sumw_group += pacc[(size_t)p * 8 + 0];
-        b->w_sigma2_offset += pacc[(size_t)p * 8 + 1];
-        b->w_LL += o.dLL;
-        b->w_ave_Pmax += o.pmax;
     }
     w->stage_ms[ST_N + 1] +=
         std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_final).count();
