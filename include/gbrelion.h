@@ -537,6 +537,12 @@ int gbr_posenet_train_targets(gbr_posenet *n, const float *fimg, const float *ta
  * prepared images fimg [count] (host or device) */
 int gbr_posenet_block_probs(gbr_posenet *n, const float *fimg, int64_t count, int64_t dirs_per_block,
                             double temperature, float *out);
+/* the m most probable blocks of dirs_per_block consecutive directions under
+ * softmax(logits / temperature) [count][m] (most probable first, lower
+ * index first among equals) and their summed probability [count], for
+ * prepared images fimg [count] (host or device) */
+int gbr_posenet_propose_blocks(gbr_posenet *n, const float *fimg, int64_t count, int64_t dirs_per_block,
+                               double temperature, int64_t m, int32_t *blocks_out, float *mass_out);
 /* top-m directions [count][m] (most probable first) and their probabilities */
 int gbr_posenet_propose(gbr_posenet *n, const float *fimg, int64_t count, int64_t m, int32_t *dir_out,
                         float *prob_out);

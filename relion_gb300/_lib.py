@@ -129,6 +129,7 @@ EXPORTS = {
     "gbr_posenet_loss_grad": (C.c_int, [P, P, P, I64, P, P]),
     "gbr_posenet_train": (C.c_int, [P, P, I64, I64, I64, F64, P]),
     "gbr_posenet_propose": (C.c_int, [P, P, I64, I64, P, P]),
+    "gbr_posenet_propose_blocks": (C.c_int, [P, P, I64, I64, F64, I64, P, P]),
     "gbr_posenet_train_targets": (C.c_int, [P, P, P, I64, I64, I64, F64, P]),
     "gbr_posenet_block_probs": (C.c_int, [P, P, I64, I64, F64, P]),
     "gbr_recon_set_precision": (C.c_int, [P, C.c_int]),

@@ -2379,6 +2379,7 @@ struct gbr_posenet {
     DevBuf<float> pw, feat, a1, a2, h, logits, dl, d1, d2, loss, target, ctf_pool, prob;
     DevBuf<float> feat_all, target_all;  // training on particle images with given targets
     DevBuf<float> bw_scratch;            // partial weight gradients of the convolutions
+    DevBuf<float> mass;                  // proposed blocks' probability per particle
     DevBuf<int> label, idx;
     DevBuf<float2> fimg;
     ~gbr_posenet() {
@@ -2686,6 +2687,36 @@ int gbr_posenet_block_probs(gbr_posenet *n, const float *fimg, int64_t count, in
                                      n->st));
         GBR_CUDA(cudaMemcpyAsync(out + (size_t)nb * c0, n->prob.p, sizeof(float) * nb * c, cudaMemcpyDeviceToHost,
                                  n->st));
+    }
+    GBR_CUDA(cudaStreamSynchronize(n->st));
+    return GBR_OK;
+}
+
+int gbr_posenet_propose_blocks(gbr_posenet *n, const float *fimg, int64_t count, int64_t dirs_per_block,
+                               double temperature, int64_t m, int32_t *blocks_out, float *mass_out) {
+    if (!n || (count > 0 && (!fimg || !blocks_out || !mass_out))) return fail(GBR_ERR_INVALID, "null argument");
+    if (dirs_per_block < 1 || n->d.ND % dirs_per_block != 0 || !(temperature > 0.))
+        return fail(GBR_ERR_INVALID, "gbr_posenet_propose_blocks: dirs_per_block must divide ndir, temperature > 0");
+    const int nb = n->d.ND / (int)dirs_per_block;
+    if (m < 1 || m > nb) return fail(GBR_ERR_INVALID, "gbr_posenet_propose_blocks: 1 <= m <= number of blocks");
+    GBR_CUDA(cudaSetDevice(n->b->device));
+    const size_t full = (size_t)n->b->full_npix;
+    GBR_CUDA(n->prob.reserve((size_t)n->d.B * nb));
+    GBR_CUDA(n->idx.reserve((size_t)n->d.B * m));
+    GBR_CUDA(n->mass.reserve(n->d.B));
+    for (int64_t c0 = 0; c0 < count; c0 += n->d.B) {
+        const int c = (int)std::min<int64_t>(n->d.B, count - c0);
+        int s = pn_features_dev(n, fimg + 2 * full * c0, c);
+        if (s) return s;
+        gbr::PnDims d = n->d;
+        d.B = c;
+        GBR_CUDA(gbr::pn_forward(d, n->params.p, n->feat.p, n->a1.p, n->a2.p, n->h.p, n->logits.p, n->st));
+        GBR_CUDA(gbr::pn_block_probs(n->logits.p, d.ND, (int)dirs_per_block, (float)temperature, c, n->prob.p,
+                                     n->st));
+        GBR_CUDA(gbr::pn_top_blocks(n->prob.p, nb, (int)m, c, n->idx.p, n->mass.p, n->st));
+        GBR_CUDA(cudaMemcpyAsync(blocks_out + m * c0, n->idx.p, sizeof(int32_t) * m * c, cudaMemcpyDeviceToHost,
+                                 n->st));
+        GBR_CUDA(cudaMemcpyAsync(mass_out + c0, n->mass.p, sizeof(float) * c, cudaMemcpyDeviceToHost, n->st));
     }
     GBR_CUDA(cudaStreamSynchronize(n->st));
     return GBR_OK;

@@ -379,6 +379,8 @@ cudaError_t pn_loss_backward(const PnDims &d, const float *params, const float *
                              float *scratch, cudaStream_t st);
 cudaError_t pn_adam(float *p, const float *g, float *m, float *v, long long n, float lr, int t, cudaStream_t st);
 cudaError_t pn_topm(const float *logits, int N, int M, int B, int *idx, float *prob, cudaStream_t st);
+// the m most probable of nb block probabilities per particle and their sum
+cudaError_t pn_top_blocks(const float *probs, int nb, int m, int B, int *idx, float *mass, cudaStream_t st);
 cudaError_t pn_block_probs(const float *logits, int N, int dpb, float temperature, int B, float *out,
                            cudaStream_t st);
 }  // namespace gbr

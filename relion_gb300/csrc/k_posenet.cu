@@ -581,6 +581,52 @@ cudaError_t pn_block_probs(const float *logits, int N, int dpb, float temperatur
     return cudaGetLastError();
 }
 
+// The m most probable blocks of each particle (probability descending,
+// lower index first among equals) and their summed probability: one warp
+// per particle, m rounds of a warp arg-max over the block probabilities.
+__global__ void k_pn_top_blocks(const float *__restrict__ probs, int nb, int m, int *__restrict__ idx,
+                                float *__restrict__ mass) {
+    extern __shared__ float pv[];  // [nb]
+    const int b = blockIdx.x, lane = threadIdx.x;
+    const float *pb = probs + (size_t)b * nb;
+    for (int j = lane; j < nb; j += 32) pv[j] = pb[j];
+    __syncwarp();
+    float sum = 0.f;
+    for (int k = 0; k < m; ++k) {
+        float best = -1.f;
+        int bi = 0x7fffffff;
+        for (int j = lane; j < nb; j += 32) {
+            const float v = pv[j];
+            if (v > best || (v == best && j < bi)) {
+                best = v;
+                bi = j;
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float ov = __shfl_xor_sync(0xffffffffu, best, o);
+            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            if (ov > best || (ov == best && oi < bi)) {
+                best = ov;
+                bi = oi;
+            }
+        }
+        if (lane == 0) {
+            idx[(size_t)b * m + k] = bi;
+            pv[bi] = -2.f;  // taken
+        }
+        sum += best;
+        __syncwarp();
+    }
+    if (lane == 0) mass[b] = sum;
+}
+
+cudaError_t pn_top_blocks(const float *probs, int nb, int m, int B, int *idx, float *mass, cudaStream_t st) {
+    if (m < 1 || m > nb) return cudaErrorInvalidValue;
+    k_pn_top_blocks<<<B, 32, sizeof(float) * nb, st>>>(probs, nb, m, idx, mass);
+    return cudaGetLastError();
+}
+
 cudaError_t pn_topm(const float *logits, int N, int M, int B, int *idx, float *prob, cudaStream_t st) {
     k_pn_topm<<<B, 256, sizeof(float) * N, st>>>(logits, N, M, idx, prob);
     return cudaGetLastError();

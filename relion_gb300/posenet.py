@@ -122,6 +122,17 @@ class PoseProposer:
                                                float(temperature), out.ctypes.data))
         return out
 
+    def propose_blocks(self, fimg, dirs_per_block, temperature, m):
+        """The m most probable blocks of dirs_per_block directions [n][m]
+        (most probable first, lower index first among equals) and their
+        summed probability [n], selected on the device."""
+        f = self._fimg(fimg)
+        idx = np.zeros((len(f), m), np.int32)
+        mass = np.zeros(len(f), np.float32)
+        check(self.lib.gbr_posenet_propose_blocks(self.h, f.ptr, len(f), int(dirs_per_block), float(temperature),
+                                                  int(m), idx.ctypes.data, mass.ctypes.data))
+        return idx, mass
+
     def propose(self, fimg, m):
         """Top-m directions [n][m] (most probable first) and their probabilities."""
         f = self._fimg(fimg)
@@ -200,18 +211,10 @@ class BlockProposer:
 
     def __call__(self, fimg):
         from .estep import ALL_BLOCKS
-        bp = self.block_probabilities(fimg)
-        # the `blocks` most probable blocks, most probable first: a partial
-        # selection, then a sort of the selected few (ties at the cut are
-        # broken arbitrarily; probabilities of distinct blocks rarely tie)
-        m = self.blocks
-        if m < bp.shape[1]:
-            part = np.argpartition(-bp, m - 1, axis=1)[:, :m]
-            o = np.argsort(-np.take_along_axis(bp, part, axis=1), axis=1, kind="stable")
-            order = np.take_along_axis(part, o, axis=1)
-        else:
-            order = np.argsort(-bp, axis=1, kind="stable")
-        mass = np.take_along_axis(bp, order, axis=1).sum(axis=1)
+        # the `blocks` most probable blocks (most probable first) and their
+        # mass, selected on the device
+        order, mass = self.net.propose_blocks(fimg, self.dpb, self.temperature, self.blocks)
+        mass = mass.astype(np.float64)
         out = np.concatenate([order + c * self.per_class for c in range(self.K)], axis=1).astype(np.int32)
         fallback = mass < self.mass_threshold
         out[fallback, 0] = ALL_BLOCKS

@@ -172,3 +172,24 @@ def test_device_images_equal_host_images():
     np.testing.assert_array_equal(pdv, ph)
     net.close()
     b.close()
+
+
+def test_top_blocks_on_device_match_host_selection():
+    """gbr_posenet_propose_blocks: the device selection of the m most probable
+    blocks equals a stable host sort of gbr_posenet_block_probs, and the
+    mass their summed probability."""
+    _need_cuda()
+    from relion_gb300 import datagen
+    from relion_gb300.posenet import PoseProposer
+    ds = datagen.Dataset("cfg0_box64", seed=6, n_particles=20)
+    b = _bundle(ds, ds.model(precision=1))
+    net = PoseProposer(b, nangle=24, max_batch=8, seed=3)  # three chunks
+    fimg = ds.particles(0, 20)["fimg"]
+    for dpb, t, m in ((4, 1.7, 5), (1, 1.0, 12)):
+        bp = net.block_probs(fimg, dpb, t)
+        want = np.argsort(-bp, axis=1, kind="stable")[:, :m]
+        idx, mass = net.propose_blocks(fimg, dpb, t, m)
+        np.testing.assert_array_equal(idx, want)
+        np.testing.assert_allclose(mass, np.take_along_axis(bp, want, 1).sum(1), rtol=1e-5)
+    net.close()
+    b.close()
