@@ -340,6 +340,7 @@ struct gbr_worker {
     int use_graph = 1;
     cudaGraphExec_t gexec = nullptr;
     unsigned long long buf_gen = 0;  // bumped when the worker's batch buffers are reallocated
+    bool masks_clean = false;        // mask / cnt are all zero (cleared after each pass)
     struct GraphKey {
         int n = -1;
         unsigned long long api = 0, buf = 0;
@@ -679,6 +680,7 @@ int ensure_capacity(gbr_worker *w, int n) {
     gbr_bundle *b = w->b;
     if (n <= w->cap) return GBR_OK;
     ++w->buf_gen;
+    w->masks_clean = false;
     const size_t full = (size_t)b->full_npix;
     GBR_CUDA(w->X.reserve(n * full));
     GBR_CUDA(w->Xn.reserve(n * full));
@@ -1164,8 +1166,8 @@ int coarse_segment(gbr_worker *w, int n, const CoarseFlags &cf) {
     GBR_CUDA(launch_cand_seg(w->cand_cnt.p, n, cap, w->cand_seg.p, st));
     int s = threshold_search(w, n, w->cand_w.p, w->cand_seg.p, cap, 1, w->cand_seg.p + n, RT);
     if (s) return s;
-    GBR_CUDA(cudaMemsetAsync(w->mask.p, 0, sizeof(unsigned int) * (size_t)n * R * W, st));
-    GBR_CUDA(cudaMemsetAsync(w->cnt.p, 0, sizeof(int) * (size_t)n * R, st));
+    // mask and cnt are all zero here (cleared after the previous pass's fine
+    // pass, or by run_batch after a reallocation or a failed call)
     GBR_CUDA(launch_cand_masks(w->cand_idx.p, w->cand_w.p, w->cand_cnt.p, cap, n, R, T, W, w->ps.p, w->mask.p,
                                w->cnt.p, st));
     GBR_CUDA(cudaMemcpyAsync(w->h_ccnt.p, w->cand_cnt.p, sizeof(unsigned int) * n, cudaMemcpyDeviceToHost, st));
@@ -1241,6 +1243,13 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
     const int W = (T + 31) / 32;
     const long long RT = (long long)R * T;
     const CoarseFlags cf = coarse_flags(w, n);
+    if (!w->masks_clean) {
+        // first pass, new buffers or a failed pass: the significance masks and
+        // counts start from zero (afterwards each pass clears the rows it used)
+        GBR_CUDA(cudaMemsetAsync(w->mask.p, 0, sizeof(unsigned int) * w->mask.n, st));
+        GBR_CUDA(cudaMemsetAsync(w->cnt.p, 0, sizeof(int) * w->cnt.n, st));
+    }
+    w->masks_clean = false;  // until this pass's rows are cleared again
     int s = run_coarse(w, n, cf);
     if (s) return s;
     GBR_CUDA(cudaStreamSynchronize(st));
@@ -1283,6 +1292,11 @@ int run_batch(gbr_worker *w, int n, const double *power_h, const double *pdat_h,
         s = fine_sparse(w, n, njobs, nfine, segf, max_seg);
     }
     if (s) return s;
+    // the rows this pass set in mask / cnt back to zero for the next pass
+    GBR_CUDA(launch_clear_job_rows(w->jobs.p, w->scan_tmp.p + 2 * fine_jobs_nblocks((long long)n * R), njobs, R,
+                                   (T + 31) / 32, w->mask.p, w->cnt.p, st));
+    w->launches += 1;
+    w->masks_clean = true;
     GBR_CUDA(cudaEventRecord(w->ev[8], st));
     // ---- backprojection of the touched slices (already inserted by the
     // weighted sums in the direct form) ----

@@ -237,6 +237,9 @@ cudaError_t launch_sig_masks(const float *w, int n, int R, int T, int W, const P
 // blocks of the job-list scan for tot (particle, orientation) counts; the
 // totals (jobs, entries) land at sums[2 nblocks], sums[2 nblocks + 1]
 long long fine_jobs_nblocks(long long tot);
+// zero the mask words and counts of the job rows (job count read on the device)
+cudaError_t launch_clear_job_rows(const FineJob *jobs, const long long *njobs_dev, long long njobs_max, int R, int W,
+                                  unsigned int *mask, int *cnt, cudaStream_t st);
 cudaError_t launch_fine_jobs(const int *cnt, int n, int R, int per, long long *sums, FineJob *jobs, long long *seg,
                              unsigned char *need_r, cudaStream_t st);
 // Fine diff2 over a device work queue of (job, pixel range) items: the job

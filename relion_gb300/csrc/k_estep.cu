@@ -1779,6 +1779,29 @@ cudaError_t launch_fine_jobs(const int *cnt, int n, int R, int per, long long *s
     return cudaGetLastError();
 }
 
+// After a pass: the significance mask words and counts of every job's row
+// back to zero (the rows with a nonzero count are exactly the jobs), so the
+// next pass starts from clear arrays without a full memset.
+__global__ void k_clear_job_rows(const FineJob *__restrict__ jobs, const long long *__restrict__ njobs, int R,
+                                 int W, unsigned int *__restrict__ mask, int *__restrict__ cnt) {
+    const long long nj = *njobs;
+    for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < nj;
+         j += (long long)gridDim.x * blockDim.x) {
+        const FineJob jb = jobs[j];
+        const size_t row = (size_t)jb.p * R + jb.r;
+        cnt[row] = 0;
+        for (int k = 0; k < W; ++k) mask[row * W + k] = 0u;
+    }
+}
+
+cudaError_t launch_clear_job_rows(const FineJob *jobs, const long long *njobs_dev, long long njobs_max, int R, int W,
+                                  unsigned int *mask, int *cnt, cudaStream_t st) {
+    if (njobs_max <= 0) return cudaSuccess;
+    const int grid = (int)std::min<long long>((njobs_max + 255) / 256, 4096);
+    k_clear_job_rows<<<grid, 256, 0, st>>>(jobs, njobs_dev, R, W, mask, cnt);
+    return cudaGetLastError();
+}
+
 long long fine_jobs_nblocks(long long tot) {
     const long long per_block = (long long)kJobsThreads * kJobsPer;
     return (tot + per_block - 1) / per_block;
