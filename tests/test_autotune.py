@@ -94,3 +94,24 @@ def test_plain_path_skips_coarse_candidates():
     autotune._cache.clear()
     out = autotune.tune(FakeBundle(precision=0), FakeWorker(), {"n": 4})
     assert out["coarse"] == [] and out["options"] == dict(fine_mode="sparse", bp_direct=1)
+
+
+class SlowDenseWorker(FakeWorker):
+    """The dense fine-pass form 10x slower than the sparse ones."""
+
+    def do_expectation_some_particles(self, batch):
+        super().do_expectation_some_particles(batch)
+        if self.opts.get("fine_mode") == "dense":
+            self.t[STAGES.index("diff2_fine")] += 10.0
+        self.calls = getattr(self, "calls", 0) + 1
+
+
+def test_slow_fine_candidate_is_not_repeated():
+    autotune._cache.clear()
+    w = SlowDenseWorker()
+    out = autotune.tune(FakeBundle(), w, {"n": 8}, repeats=2)
+    ms = {(o["fine_mode"], o["bp_direct"]): v for o, v in out["fine"]}
+    assert ms[("dense", 0)] > 4 * min(ms[("sparse", 0)], ms[("sparse", 1)])
+    # 8 coarse candidates x 3 calls, 2 sparse forms x 3 calls, the dense form's warm-up call only
+    assert w.calls == 8 * 3 + 2 * 3 + 1
+    assert out["options"]["fine_mode"] == "sparse"
