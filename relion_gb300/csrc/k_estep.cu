@@ -956,7 +956,7 @@ __global__ void __launch_bounds__(kJobsThreads) k_jobs_emit(const int *__restric
 // in hidden-index order (t, ior, iot) and the particle's minimum.
 // ---------------------------------------------------------------------------
 constexpr int kFineChunk = 512;
-constexpr int kFineSplit = 4 * kFineChunk;  // fine pixels per work item
+constexpr int kFineSplit = 2 * kFineChunk;  // fine pixels per work item
 constexpr int kFineThreads = 256;
 constexpr int kFineRows = 4;  // rows per warp pass; kFineRows x 8 orientations = 32 lanes
 
