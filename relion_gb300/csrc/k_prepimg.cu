@@ -55,6 +55,8 @@ __global__ void k_img_shift_bg(const float *__restrict__ in, int N, const int *_
     const float *src = in + (size_t)p * N * N;
     float *dst = A + (size_t)p * N * N;
     const int NN = N * N, base = blockIdx.x * (blockDim.x * kImgPer) + threadIdx.x;
+    const bool pow2 = (N & (N - 1)) == 0;
+    const int lgN = __ffs(N) - 1;
     float v[kImgPer], wv[kImgPer];
 #pragma unroll
     for (int k = 0; k < kImgPer; ++k) {
@@ -62,7 +64,7 @@ __global__ void k_img_shift_bg(const float *__restrict__ in, int N, const int *_
         v[k] = 0.f;
         wv[k] = 0.f;
         if (i < NN) {
-            const int y = i / N, x = i - y * N;
+            const int y = pow2 ? (i >> lgN) : i / N, x = i - y * N;
             const int sy = y - dy, sx = x - dx;
             if (sy >= 0 && sy < N && sx >= 0 && sx < N) v[k] = src[(size_t)sy * N + sx];
             wv[k] = W[i];
@@ -105,8 +107,14 @@ __global__ void k_mask_apply(const float *__restrict__ A, int N, const float *__
     const int p = blockIdx.y;
     const float *src = A + (size_t)p * N * N;
     float *dst = B + (size_t)p * N * N;
-    const double sw = sums[2 * p + 1];
-    const float b = (float)(sw > 0. ? sums[2 * p] / sw : 0.);
+    // the background value, one FP64 division per block (FP64 is slow here)
+    __shared__ float s_b;
+    if (threadIdx.x == 0) {
+        const double sw = sums[2 * p + 1];
+        s_b = (float)(sw > 0. ? sums[2 * p] / sw : 0.);
+    }
+    __syncthreads();
+    const float b = s_b;
     const int NN = N * N, base = blockIdx.x * (blockDim.x * kImgPer) + threadIdx.x;
     float a[kImgPer], w[kImgPer];
 #pragma unroll
@@ -260,8 +268,9 @@ cudaError_t launch_prepare_images(const PrepImagesArgs &a, cudaStream_t st) {
     // spectrum: 8 row chunks per particle (few FP64 atomics per shell)
     const dim3 gs((unsigned)std::min(8, std::max(1, N / 32)), (unsigned)n);
     if (cur < N) k_img_spectrum<<<gs, 256, sizeof(float) * half, st>>>(a.FB, N, cur, a.power, a.xi2);
-    // CTF: one block per particle, its constants formed once
-    k_ctf_image<<<dim3(1, (unsigned)n), 256, 0, st>>>(a.ctf, N, cur, a.pixel, a.kV, a.Cs, a.Q0, a.fctf);
+    // CTF: the particle's constants formed once per block, blocks over its pixels
+    k_ctf_image<<<dim3((unsigned)((cur * X + 255) / 256), (unsigned)n), 256, 0, st>>>(a.ctf, N, cur, a.pixel, a.kV,
+                                                                                   a.Cs, a.Q0, a.fctf);
     return cudaGetLastError();
 }
 
