@@ -220,24 +220,54 @@ __device__ CtfConst ctf_const(const double *c, double kV, double Cs, double Q0) 
 // (CTF::getFftwImage, src/ctf.cpp:314-450, no padding).  The phase gamma is
 // formed in FP64 and reduced modulo 2 pi there; the sine and the damping
 // exponential of the reduced values are FP32 (|CTF| <= 1, error ~1e-7).
-__global__ void k_ctf_image(const double *__restrict__ ctf, int N, int cur, double pixel, double kV, double Cs,
-                            double Q0, float *__restrict__ out) {
-    __shared__ CtfConst sk;
-    const int p = blockIdx.y, X = cur / 2 + 1;
-    if (threadIdx.x == 0) sk = ctf_const(ctf + (size_t)p * 6, kV, Cs, Q0);
+// FP64 runs at a small fraction of the FP32 rate on this part, so along a
+// row (frequency y = ip s, x = j s, s = 1 / (N pixel)) the phase is taken as
+// the polynomial in the column index j that it is,
+//   gamma = K1 s^2 (Axx j^2 + 2 Axy ip j + Ayy ip^2) + K2 s^4 (j^2 + ip^2)^2 - K5 - K3
+//         = C0 + B j + A2 j^2 + Q j^4,
+// with the row's coefficients formed once per block: three FP64 FMAs per
+// pixel instead of the twenty-odd FP64 operations of the direct form.  A
+// block covers kCtfRows rows of one particle.
+constexpr int kCtfRows = 16;
+__global__ void __launch_bounds__(256) k_ctf_image(const double *__restrict__ ctf, int N, int cur, double pixel,
+                                                   double kV, double Cs, double Q0, float *__restrict__ out) {
+    extern __shared__ double s_tab[];  // [2 X]: j, j^2
+    __shared__ double s_c0[kCtfRows], s_b[kCtfRows], s_a2[kCtfRows], s_q;
+    __shared__ float s_e0[kCtfRows], s_e2, s_scale;
+    const int p = blockIdx.y, X = cur / 2 + 1, r0 = blockIdx.x * kCtfRows;
+    const int nr = min(kCtfRows, cur - r0);
+    for (int j = threadIdx.x; j < X; j += blockDim.x) {
+        s_tab[j] = (double)j;
+        s_tab[X + j] = (double)j * (double)j;
+    }
+    if (threadIdx.x < nr) {
+        const CtfConst k = ctf_const(ctf + (size_t)p * 6, kV, Cs, Q0);
+        const double s = 1. / ((double)N * pixel), s2 = s * s, q = k.K2 * s2 * s2;
+        const int i = r0 + threadIdx.x;
+        const double ip = (double)(i < X ? i : i - cur), ip2 = ip * ip;
+        s_c0[threadIdx.x] = k.K1 * s2 * k.Ayy * ip2 + q * ip2 * ip2 - k.K5 - k.K3;
+        s_b[threadIdx.x] = k.K1 * s2 * 2.0 * k.Axy * ip;
+        s_a2[threadIdx.x] = k.K1 * s2 * k.Axx + 2.0 * q * ip2;
+        s_e0[threadIdx.x] = (float)(k.K4 * s2 * ip2);
+        if (threadIdx.x == 0) {
+            s_q = q;
+            s_e2 = (float)(k.K4 * s2);
+            s_scale = (float)k.scale;
+        }
+    }
     __syncthreads();
-    const CtfConst k = sk;
-    const double inv_xs = 1. / ((double)N * pixel);
-    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < cur * X; e += gridDim.x * blockDim.x) {
-        const int i = e / X, j = e - i * X;
-        const int ip = i < X ? i : i - cur;
-        const double x = (double)j * inv_xs, y = (double)ip * inv_xs;
-        const double u2 = x * x + y * y;
-        double g = k.K1 * (k.Axx * x * x + 2.0 * k.Axy * x * y + k.Ayy * y * y) + k.K2 * u2 * u2 - k.K5 - k.K3;
+    const double q = s_q;
+    const float e2 = s_e2, scale = s_scale;
+    float *o = out + (size_t)p * cur * X + (size_t)r0 * X;
+    for (int e = threadIdx.x; e < nr * X; e += blockDim.x) {
+        const int il = e / X, j = e - il * X;
+        const double jd = s_tab[j], t = s_tab[X + j];
+        double g = fma(fma(q, t, s_a2[il]), t, fma(s_b[il], jd, s_c0[il]));
         g -= 2. * kPiD * rint(g * (0.5 / kPiD));
-        float r = -sinf((float)g) * expf((float)(k.K4 * u2)) * (float)k.scale;
+        const float arg = fmaf(e2, (float)(j * j), s_e0[il]);
+        float r = -sinf((float)g) * expf(arg) * scale;
         if (fabsf(r) < 1e-8f) r = (r < 0.f ? -1.f : 1.f) * 1e-8f;
-        out[(size_t)p * cur * X + e] = r;
+        o[e] = r;
     }
 }
 
@@ -268,9 +298,9 @@ cudaError_t launch_prepare_images(const PrepImagesArgs &a, cudaStream_t st) {
     // spectrum: 8 row chunks per particle (few FP64 atomics per shell)
     const dim3 gs((unsigned)std::min(8, std::max(1, N / 32)), (unsigned)n);
     if (cur < N) k_img_spectrum<<<gs, 256, sizeof(float) * half, st>>>(a.FB, N, cur, a.power, a.xi2);
-    // CTF: the particle's constants formed once per block, blocks over its pixels
-    k_ctf_image<<<dim3((unsigned)((cur * X + 255) / 256), (unsigned)n), 256, 0, st>>>(a.ctf, N, cur, a.pixel, a.kV,
-                                                                                   a.Cs, a.Q0, a.fctf);
+    // CTF: blocks of kCtfRows rows of each particle
+    k_ctf_image<<<dim3((unsigned)((cur + kCtfRows - 1) / kCtfRows), (unsigned)n), 256, sizeof(double) * 2 * X, st>>>(
+        a.ctf, N, cur, a.pixel, a.kV, a.Cs, a.Q0, a.fctf);
     return cudaGetLastError();
 }
 
