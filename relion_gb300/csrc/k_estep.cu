@@ -55,6 +55,15 @@ __device__ double block_sum(double v, double *sh) {
 //   c = Xi2/2 + sum m |X|^2 in FP64 for each pass.
 // pdat[p] = {old_x, old_y, prior_x, prior_y, highres_Xi2, norm, scale, 0}.
 // ---------------------------------------------------------------------------
+// Compensated (Kahan) FP32 summation: the sum's error stays near one FP32
+// rounding of the total, whatever the number of terms, without FP64 adds
+// (FP64 runs at a small fraction of the FP32 rate on this part).
+__device__ __forceinline__ void kahan_add(float &s, float &c, float x) {
+    const float y = x - c, t = s + y;
+    c = (t - s) - y;
+    s = t;
+}
+
 __global__ void k_prep(const float2 *__restrict__ X, const float *__restrict__ C,
                        const float2 *__restrict__ Xn, const double *__restrict__ pdat,
                        int full_npix, const PixelRef *__restrict__ pc, int nc,
@@ -70,7 +79,7 @@ __global__ void k_prep(const float2 *__restrict__ X, const float *__restrict__ C
     const float2 *x = X + (size_t)p * full_npix;
     const float2 *xn = Xn + (size_t)p * full_npix;
     const float *c = C + (size_t)p * full_npix;
-    double acc = 0.;
+    float ks = 0.f, kc = 0.f;  // sum of m |x|^2: FP32 terms, compensated FP32 per thread, FP64 across
     for (int j = threadIdx.x; j < ldk_c; j += blockDim.x) {
         float a = 0.f;
         float2 b = make_float2(0.f, 0.f);
@@ -80,12 +89,12 @@ __global__ void k_prep(const float2 *__restrict__ X, const float *__restrict__ C
             const float2 v = x[k];
             a = m * cs * cs;
             b = make_float2(m * cs * v.x, m * cs * v.y);
-            acc += (double)m * ((double)v.x * v.x + (double)v.y * v.y);
+            kahan_add(ks, kc, m * (v.x * v.x + v.y * v.y));
         }
         a_c[(size_t)p * ldk_c + j] = a;
         b_c[(size_t)p * ldk_c + j] = b;
     }
-    double tot = block_sum(acc, sh);
+    double tot = block_sum((double)ks - (double)kc, sh);
     if (threadIdx.x == 0) {
         ParticleState s{};
         s.c_coarse = pd[4] / 2. + tot;
@@ -93,7 +102,8 @@ __global__ void k_prep(const float2 *__restrict__ X, const float *__restrict__ C
         s.min_fine = 0xFFFFFFFFu;
         ps[p] = s;
     }
-    acc = 0.;
+    ks = 0.f;
+    kc = 0.f;
     for (int j = threadIdx.x; j < ldk_f; j += blockDim.x) {
         if (j >= nf) {
             a_f[(size_t)p * ldk_f + j] = 0.f;
@@ -109,9 +119,9 @@ __global__ void k_prep(const float2 *__restrict__ X, const float *__restrict__ C
         Xf[(size_t)p * nf + j] = v;
         Xnf[(size_t)p * nf + j] = xn[k];
         Cf[(size_t)p * nf + j] = cr;
-        acc += (double)m * ((double)v.x * v.x + (double)v.y * v.y);
+        kahan_add(ks, kc, m * (v.x * v.x + v.y * v.y));
     }
-    tot = block_sum(acc, sh);
+    tot = block_sum((double)ks - (double)kc, sh);
     if (threadIdx.x == 0) ps[p].c_fine = pd[4] / 2. + tot;
 }
 

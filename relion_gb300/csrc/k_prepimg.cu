@@ -40,7 +40,7 @@ __global__ void k_mask_weights(int N, double radius, double width, float *__rest
 // A[p][y][x] = f_p in[p][y - dy_p][x - dx_p], 0 where the source is outside
 // (translate with DONT_WRAP, src/transformations.h; V2(r) = V1(r - v)),
 // together with the weighted background sums of the soft mask (sum w A,
-// sum w): a few pixels per thread in FP32, FP64 across threads and blocks.
+// sum w): FP32 within a warp, FP64 across warps and blocks.
 // Each thread takes kImgPer pixels one block-width apart, loads all of them
 // before using any (memory-level parallelism), grid (N^2 / (256 kImgPer), n).
 constexpr int kImgPer = 8;
@@ -81,14 +81,15 @@ __global__ void k_img_shift_bg(const float *__restrict__ in, int N, const int *_
             fv = fmaf(wv[k], val, fv);
         }
     }
-    double sw = fw, sv = fv;
+    // FP32 across the warp (a warp's 256 pixels), FP64 from there on: FP64
+    // adds run at a small fraction of the FP32 rate on this part
     for (int o = 16; o > 0; o >>= 1) {
-        sw += __shfl_xor_sync(0xffffffffu, sw, o);
-        sv += __shfl_xor_sync(0xffffffffu, sv, o);
+        fw += __shfl_xor_sync(0xffffffffu, fw, o);
+        fv += __shfl_xor_sync(0xffffffffu, fv, o);
     }
     if ((threadIdx.x & 31) == 0) {
-        s_w[threadIdx.x >> 5] = sw;
-        s_v[threadIdx.x >> 5] = sv;
+        s_w[threadIdx.x >> 5] = (double)fw;
+        s_v[threadIdx.x >> 5] = (double)fv;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -216,56 +217,106 @@ __device__ CtfConst ctf_const(const double *c, double kV, double Cs, double Q0) 
     return k;
 }
 
+// Double-float arithmetic (Dekker, "A floating-point technique for extending
+// the available precision", 1971): a value carried as an unevaluated FP32 sum
+// hi + lo (~48 significant bits), with the error-free transformations of a
+// sum (Knuth's two-sum) and of a product (by FMA).  The _rn intrinsics keep
+// the compiler from contracting them.
+struct DFloat {
+    float hi, lo;
+};
+
+__device__ __forceinline__ DFloat df_split(double x) {
+    const float h = (float)x;
+    return {h, (float)(x - (double)h)};
+}
+
+__device__ __forceinline__ DFloat two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b), v = __fadd_rn(s, -a);
+    return {s, __fadd_rn(__fadd_rn(a, -__fadd_rn(s, -v)), __fadd_rn(b, -v))};
+}
+
+// a * f for an FP32 f
+__device__ __forceinline__ DFloat df_mul_f(DFloat a, float f) {
+    const float p = __fmul_rn(a.hi, f);
+    return two_sum(p, fmaf(a.lo, f, fmaf(a.hi, f, -p)));
+}
+
+__device__ __forceinline__ DFloat df_add(DFloat a, DFloat b) {
+    const DFloat s = two_sum(a.hi, b.hi);
+    return two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+
+// 2 pi as an FP32 pair, for the reduction of the phase (Cody and Waite,
+// "Software Manual for the Elementary Functions", 1980): g - n 2 pi with
+// n 2pi_hi formed exactly by FMA.
+constexpr float kTwoPiHi = (float)(2.0 * kPiD);
+constexpr float kTwoPiLo = (float)(2.0 * kPiD - (double)kTwoPiHi);
+constexpr float kInvTwoPiF = (float)(0.5 / kPiD);
+
 // CTF image of the current size on the full-box frequencies
-// (CTF::getFftwImage, src/ctf.cpp:314-450, no padding).  The phase gamma is
-// formed in FP64 and reduced modulo 2 pi there; the sine and the damping
-// exponential of the reduced values are FP32 (|CTF| <= 1, error ~1e-7).
-// FP64 runs at a small fraction of the FP32 rate on this part, so along a
-// row (frequency y = ip s, x = j s, s = 1 / (N pixel)) the phase is taken as
-// the polynomial in the column index j that it is,
-//   gamma = K1 s^2 (Axx j^2 + 2 Axy ip j + Ayy ip^2) + K2 s^4 (j^2 + ip^2)^2 - K5 - K3
-//         = C0 + B j + A2 j^2 + Q j^4,
-// with the row's coefficients formed once per block: three FP64 FMAs per
-// pixel instead of the twenty-odd FP64 operations of the direct form.  A
-// block covers kCtfRows rows of one particle.
-constexpr int kCtfRows = 16;
+// (CTF::getFftwImage, src/ctf.cpp:314-450, no padding).  FP64 runs at a
+// small fraction of the FP32 rate on this part, so:
+//  * along a row (frequency y = ip s, x = j s, s = 1 / (N pixel)) the phase
+//    is the polynomial in the column index j that it is,
+//      gamma = K1 s^2 (Axx j^2 + 2 Axy ip j + Ayy ip^2) + K2 s^4 (j^2 + ip^2)^2 - K5 - K3
+//            = C0 + B j + A2 j^2 + Q j^4,
+//    with the particle's constants (K1 s^2 Axx, ..., K2 s^4) formed in FP64
+//    once per block and the rows' coefficients from them in double-float
+//    (an FP64 instruction occupies the FP64 pipe for tens of cycles whatever
+//    the active lanes: the blocks are large so that this setup is rare);
+//  * per pixel it is evaluated in double-float (j and j^2 are exact in FP32;
+//    ~1e-14 relative, where FP64 gives ~1e-16) and reduced modulo 2 pi, all
+//    in FP32 units;
+//  * the sine of the reduced phase and the damping exponential are FP32
+//    (|CTF| <= 1, error ~1e-7, the rounding of the reduced phase).
+// A block covers kCtfRows rows of one particle.
+constexpr int kCtfRows = 128;
 __global__ void __launch_bounds__(256) k_ctf_image(const double *__restrict__ ctf, int N, int cur, double pixel,
                                                    double kV, double Cs, double Q0, float *__restrict__ out) {
-    extern __shared__ double s_tab[];  // [2 X]: j, j^2
-    __shared__ double s_c0[kCtfRows], s_b[kCtfRows], s_a2[kCtfRows], s_q;
-    __shared__ float s_e0[kCtfRows], s_e2, s_scale;
+    __shared__ DFloat s_c0[kCtfRows], s_b[kCtfRows], s_a2[kCtfRows];
+    __shared__ float s_e0[kCtfRows];
+    // particle constants: K1 s^2 Ayy, 2 K1 s^2 Axy, K1 s^2 Axx, K2 s^4, -K5 - K3
+    __shared__ DFloat s_ayy, s_axy, s_axx, s_q, s_k53;
+    __shared__ float s_e2, s_scale;
     const int p = blockIdx.y, X = cur / 2 + 1, r0 = blockIdx.x * kCtfRows;
     const int nr = min(kCtfRows, cur - r0);
-    for (int j = threadIdx.x; j < X; j += blockDim.x) {
-        s_tab[j] = (double)j;
-        s_tab[X + j] = (double)j * (double)j;
-    }
-    if (threadIdx.x < nr) {
+    if (threadIdx.x == 0) {
         const CtfConst k = ctf_const(ctf + (size_t)p * 6, kV, Cs, Q0);
-        const double s = 1. / ((double)N * pixel), s2 = s * s, q = k.K2 * s2 * s2;
-        const int i = r0 + threadIdx.x;
-        const double ip = (double)(i < X ? i : i - cur), ip2 = ip * ip;
-        s_c0[threadIdx.x] = k.K1 * s2 * k.Ayy * ip2 + q * ip2 * ip2 - k.K5 - k.K3;
-        s_b[threadIdx.x] = k.K1 * s2 * 2.0 * k.Axy * ip;
-        s_a2[threadIdx.x] = k.K1 * s2 * k.Axx + 2.0 * q * ip2;
-        s_e0[threadIdx.x] = (float)(k.K4 * s2 * ip2);
-        if (threadIdx.x == 0) {
-            s_q = q;
-            s_e2 = (float)(k.K4 * s2);
-            s_scale = (float)k.scale;
-        }
+        const double sc = 1. / ((double)N * pixel), s2 = sc * sc, k1 = k.K1 * s2;
+        s_ayy = df_split(k1 * k.Ayy);
+        s_axy = df_split(2.0 * k1 * k.Axy);
+        s_axx = df_split(k1 * k.Axx);
+        s_q = df_split(k.K2 * s2 * s2);
+        s_k53 = df_split(-k.K5 - k.K3);
+        s_e2 = (float)(k.K4 * s2);
+        s_scale = (float)k.scale;
     }
     __syncthreads();
-    const double q = s_q;
+    if (threadIdx.x < nr) {
+        // C0 = K1 s^2 Ayy ip^2 + Q ip^4 - K5 - K3, B = 2 K1 s^2 Axy ip,
+        // A2 = K1 s^2 Axx + 2 Q ip^2 (ip and ip^2 exact in FP32)
+        const int i = r0 + threadIdx.x;
+        const float ip = (float)(i < X ? i : i - cur), ip2 = ip * ip;
+        const DFloat qip2 = df_mul_f(s_q, ip2);
+        s_c0[threadIdx.x] = df_add(df_add(df_mul_f(s_ayy, ip2), df_mul_f(qip2, ip2)), s_k53);
+        s_b[threadIdx.x] = df_mul_f(s_axy, ip);
+        s_a2[threadIdx.x] = df_add(s_axx, df_mul_f(qip2, 2.f));
+        s_e0[threadIdx.x] = s_e2 * ip2;
+    }
+    __syncthreads();
+    const DFloat q = s_q;
     const float e2 = s_e2, scale = s_scale;
     float *o = out + (size_t)p * cur * X + (size_t)r0 * X;
     for (int e = threadIdx.x; e < nr * X; e += blockDim.x) {
         const int il = e / X, j = e - il * X;
-        const double jd = s_tab[j], t = s_tab[X + j];
-        double g = fma(fma(q, t, s_a2[il]), t, fma(s_b[il], jd, s_c0[il]));
-        g -= 2. * kPiD * rint(g * (0.5 / kPiD));
-        const float arg = fmaf(e2, (float)(j * j), s_e0[il]);
-        float r = -sinf((float)g) * expf(arg) * scale;
+        const float jf = (float)j, tf = (float)(j * j);  // exact: j < 2^12
+        const DFloat g = df_add(df_mul_f(df_add(df_mul_f(q, tf), s_a2[il]), tf), df_add(df_mul_f(s_b[il], jf), s_c0[il]));
+        const float n = rintf(g.hi * kInvTwoPiF);
+        const float pn = __fmul_rn(n, kTwoPiHi), pe = fmaf(n, kTwoPiHi, -pn);
+        const float rg = __fadd_rn(__fadd_rn(g.hi, -pn), __fadd_rn(__fadd_rn(g.lo, -pe), -__fmul_rn(n, kTwoPiLo)));
+        const float arg = fmaf(e2, tf, s_e0[il]);
+        float r = -sinf(rg) * expf(arg) * scale;
         if (fabsf(r) < 1e-8f) r = (r < 0.f ? -1.f : 1.f) * 1e-8f;
         o[e] = r;
     }
@@ -276,7 +327,8 @@ __global__ void __launch_bounds__(256) k_ctf_image(const double *__restrict__ ct
 cudaError_t launch_prepare_images(const PrepImagesArgs &a, cudaStream_t st) {
     const int n = a.n, N = a.N, cur = a.cur;
     if (n <= 0) return cudaSuccess;
-    if (N <= 0 || (N & 1) || cur <= 0 || (cur & 1) || cur > N) return cudaErrorInvalidValue;
+    // (the CTF image takes j^2 exact in FP32: j = cur / 2 below 2^12)
+    if (N <= 0 || (N & 1) || cur <= 0 || (cur & 1) || cur > N || cur / 2 >= 4096) return cudaErrorInvalidValue;
     const int X = cur / 2 + 1, half = N / 2 + 1;
     const dim3 gimg((unsigned)((N * N + 256 * kImgPer - 1) / (256 * kImgPer)), (unsigned)n);
     if (a.mask_fresh) k_mask_weights<<<(N * N + 255) / 256, 256, 0, st>>>(N, a.mask_radius, a.mask_width, a.W);
@@ -299,7 +351,7 @@ cudaError_t launch_prepare_images(const PrepImagesArgs &a, cudaStream_t st) {
     const dim3 gs((unsigned)std::min(8, std::max(1, N / 32)), (unsigned)n);
     if (cur < N) k_img_spectrum<<<gs, 256, sizeof(float) * half, st>>>(a.FB, N, cur, a.power, a.xi2);
     // CTF: blocks of kCtfRows rows of each particle
-    k_ctf_image<<<dim3((unsigned)((cur + kCtfRows - 1) / kCtfRows), (unsigned)n), 256, sizeof(double) * 2 * X, st>>>(
+    k_ctf_image<<<dim3((unsigned)((cur + kCtfRows - 1) / kCtfRows), (unsigned)n), 256, 0, st>>>(
         a.ctf, N, cur, a.pixel, a.kV, a.Cs, a.Q0, a.fctf);
     return cudaGetLastError();
 }
