@@ -1335,7 +1335,9 @@ __global__ void __launch_bounds__(kWsumPix) k_wsum(WsumArgs a) {
         const bool scale_shell = sh >= 0 && a.do_scale && a.dvp_mask[(size_t)ic * a.nshell + sh];
         const float minv = a.minv_store[k];
         const float f = cs * minv;
-        double s2tot = 0.;
+        // the pixel's sums over its kMaxOR orientations in FP32, FP64 from
+        // there on (FP64 runs at a small fraction of the FP32 rate here)
+        float s2tot = 0.f, xa = 0.f, aa = 0.f;
 #pragma unroll
         for (int ior = 0; ior < kMaxOR; ++ior) {
             if (!(W[ior] > 0.f)) continue;
@@ -1343,10 +1345,10 @@ __global__ void __launch_bounds__(kWsumPix) k_wsum(WsumArgs a) {
             const float2 zx = make_float2(x.x * phi[ior].x - x.y * phi[ior].y, x.x * phi[ior].y + x.y * phi[ior].x);
             const float2 zn =
                 make_float2(xn.x * phi[ior].x - xn.y * phi[ior].y, xn.x * phi[ior].y + xn.y * phi[ior].x);
-            s2tot += (double)s2[ior];
+            s2tot += s2[ior];
             if (scale_shell) {
-                l_xa += (double)cs * (pv[ior].x * zx.x + pv[ior].y * zx.y);
-                l_aa += (double)W[ior] * cs * cs * (pv[ior].x * pv[ior].x + pv[ior].y * pv[ior].y);
+                xa = fmaf(cs, pv[ior].x * zx.x + pv[ior].y * zx.y, xa);
+                aa = fmaf(W[ior] * cs * cs, pv[ior].x * pv[ior].x + pv[ior].y * pv[ior].y, aa);
             }
             const float wgt = W[ior] * cs * cs * minv;
             if (a.bp_direct) {
@@ -1368,7 +1370,11 @@ __global__ void __launch_bounds__(kWsumPix) k_wsum(WsumArgs a) {
             }
             if (first && threadIdx.x == 0) a.active[rf] = 1;
         }
-        if (sh >= 0 && s2tot != 0.) atomicAdd(&shell[sh], s2tot);
+        if (scale_shell) {
+            l_xa += (double)xa;
+            l_aa += (double)aa;
+        }
+        if (sh >= 0 && s2tot != 0.f) atomicAdd(&shell[sh], (double)s2tot);
     }
     }
     if (a.do_scale) {
