@@ -1700,7 +1700,7 @@ cudaError_t launch_prep(const float2 *X, const float *C, const double *pdat, int
                         float *a_f, float2 *b_f, float2 *Xf, float2 *Xnf, float *Cf,
                         const float2 *Xn, int do_scale, ParticleState *ps, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    k_prep<<<n, 256, 0, st>>>(X, C, Xn, pdat, full_npix, pc, nc, minv_c, ldk_c, pf, nf, ldk_f, minv_f, a_c,
+    k_prep<<<n, 512, 0, st>>>(X, C, Xn, pdat, full_npix, pc, nc, minv_c, ldk_c, pf, nf, ldk_f, minv_f, a_c,
                               b_c, a_f, b_f, Xf, Xnf, Cf, do_scale, ps);
     return cudaGetLastError();
 }

@@ -132,8 +132,12 @@ __global__ void k_mask_apply(const float *__restrict__ A, int N, const float *__
 }
 
 // windowFourierTransform to `cur` (src/fftw.h:809-857) + CenterFFTbySign
-// (src/fftw.h:390-403) + the 1/N^2 of the forward transform.
-__global__ void k_window_center(const float2 *__restrict__ F, int N, int cur, float2 *__restrict__ out) {
+// (src/fftw.h:390-403) + the 1/N^2 of the forward transform, of two
+// transforms in one launch (blockIdx.z: F0 -> out0, F1 -> out1).
+__global__ void k_window_center(const float2 *__restrict__ F0, const float2 *__restrict__ F1, int N, int cur,
+                                float2 *__restrict__ out0, float2 *__restrict__ out1) {
+    const float2 *__restrict__ F = blockIdx.z ? F1 : F0;
+    float2 *__restrict__ out = blockIdx.z ? out1 : out0;
     const int p = blockIdx.y;
     const int X = cur / 2 + 1, half = N / 2 + 1;
     const float s = 1.f / ((float)N * (float)N);
@@ -344,9 +348,8 @@ cudaError_t launch_prepare_images(const PrepImagesArgs &a, cudaStream_t st) {
     if (cufftSetStream(plan, st) != CUFFT_SUCCESS) return cudaErrorUnknown;
     if (cufftExecR2C(plan, a.A, reinterpret_cast<cufftComplex *>(a.FA)) != CUFFT_SUCCESS) return cudaErrorUnknown;
     if (cufftExecR2C(plan, a.B, reinterpret_cast<cufftComplex *>(a.FB)) != CUFFT_SUCCESS) return cudaErrorUnknown;
-    const dim3 gw((unsigned)((cur * X + 255) / 256), (unsigned)n);
-    k_window_center<<<gw, 256, 0, st>>>(a.FA, N, cur, a.fimg_nomask);
-    k_window_center<<<gw, 256, 0, st>>>(a.FB, N, cur, a.fimg);
+    const dim3 gw((unsigned)((cur * X + 255) / 256), (unsigned)n, 2u);
+    k_window_center<<<gw, 256, 0, st>>>(a.FA, a.FB, N, cur, a.fimg_nomask, a.fimg);
     // spectrum: 8 row chunks per particle (few FP64 atomics per shell)
     const dim3 gs((unsigned)std::min(8, std::max(1, N / 32)), (unsigned)n);
     if (cur < N) k_img_spectrum<<<gs, 256, sizeof(float) * half, st>>>(a.FB, N, cur, a.power, a.xi2);
