@@ -40,7 +40,7 @@ __global__ void k_mask_weights(int N, double radius, double width, float *__rest
 // A[p][y][x] = f_p in[p][y - dy_p][x - dx_p], 0 where the source is outside
 // (translate with DONT_WRAP, src/transformations.h; V2(r) = V1(r - v)),
 // together with the weighted background sums of the soft mask (sum w A,
-// sum w): FP32 within a warp, FP64 across warps and blocks.
+// sum w): FP32 within a warp, FP64 across warps.
 // Each thread takes kImgPer pixels one block-width apart, loads all of them
 // before using any (memory-level parallelism), grid (N^2 / (256 kImgPer), n).
 constexpr int kImgPer = 8;
@@ -48,7 +48,6 @@ constexpr int kImgPer = 8;
 __global__ void k_img_shift_bg(const float *__restrict__ in, int N, const int *__restrict__ shift,
                                const float *__restrict__ factor, const float *__restrict__ W,
                                float *__restrict__ A, double *__restrict__ sums) {
-    __shared__ double s_v[32], s_w[32];
     const int p = blockIdx.y;
     const int dx = shift[2 * p], dy = shift[2 * p + 1];
     const float f = factor[p];
@@ -81,25 +80,16 @@ __global__ void k_img_shift_bg(const float *__restrict__ in, int N, const int *_
             fv = fmaf(wv[k], val, fv);
         }
     }
-    // FP32 across the warp (a warp's 256 pixels), FP64 from there on: FP64
-    // adds run at a small fraction of the FP32 rate on this part
+    // FP32 across the warp (a warp's 256 pixels), then each warp adds into
+    // the particle's FP64 sums (L2 atomics): no block barrier and no serial
+    // FP64 tail, so warps retire as their own loads complete
     for (int o = 16; o > 0; o >>= 1) {
         fw += __shfl_xor_sync(0xffffffffu, fw, o);
         fv += __shfl_xor_sync(0xffffffffu, fv, o);
     }
     if ((threadIdx.x & 31) == 0) {
-        s_w[threadIdx.x >> 5] = (double)fw;
-        s_v[threadIdx.x >> 5] = (double)fv;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double tw = 0., tv = 0.;
-        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {
-            tw += s_w[i];
-            tv += s_v[i];
-        }
-        atomicAdd(&sums[2 * p], tv);
-        atomicAdd(&sums[2 * p + 1], tw);
+        atomicAdd(&sums[2 * p], (double)fv);
+        atomicAdd(&sums[2 * p + 1], (double)fw);
     }
 }
 
@@ -108,14 +98,6 @@ __global__ void k_mask_apply(const float *__restrict__ A, int N, const float *__
     const int p = blockIdx.y;
     const float *src = A + (size_t)p * N * N;
     float *dst = B + (size_t)p * N * N;
-    // the background value, one FP64 division per block (FP64 is slow here)
-    __shared__ float s_b;
-    if (threadIdx.x == 0) {
-        const double sw = sums[2 * p + 1];
-        s_b = (float)(sw > 0. ? sums[2 * p] / sw : 0.);
-    }
-    __syncthreads();
-    const float b = s_b;
     const int NN = N * N, base = blockIdx.x * (blockDim.x * kImgPer) + threadIdx.x;
     float a[kImgPer], w[kImgPer];
 #pragma unroll
@@ -124,6 +106,15 @@ __global__ void k_mask_apply(const float *__restrict__ A, int N, const float *__
         a[k] = i < NN ? src[i] : 0.f;
         w[k] = i < NN ? W[i] : 0.f;
     }
+    // the background value, one FP64 division per block (FP64 is slow
+    // here), while the pixel loads above are in flight
+    __shared__ float s_b;
+    if (threadIdx.x == 0) {
+        const double sw = sums[2 * p + 1];
+        s_b = (float)(sw > 0. ? sums[2 * p] / sw : 0.);
+    }
+    __syncthreads();
+    const float b = s_b;
 #pragma unroll
     for (int k = 0; k < kImgPer; ++k) {
         const int i = base + k * blockDim.x;
